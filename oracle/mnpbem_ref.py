@@ -1,0 +1,755 @@
+"""FP64 NumPy restatement of the MNPBEM retarded BEM path (oracle; test-only).
+
+Conventions follow the reference: faces are ``[n, 4]`` 0-based vertex indices
+with ``-1`` in the 4th column for triangles (the reference uses NaN), arrays of
+surface vectors are ``[n, 3, npol]``, matrices are ``[n1, n2]`` with rows the
+observation faces and columns the source faces.  Linear indices into matrices
+are column-major like MATLAB's (``i + j * n1``), so the ordering of near-field
+pairs is the reference's ordering.
+"""
+import math
+
+import numpy as np
+import scipy.special
+
+EPS = np.finfo(float).eps
+EV2NM = 1.0 / 8.0655477e-4          # Misc/units.m:2
+
+
+# --------------------------------------------------------------------------
+# materials  (Material/@epsconst/subsref.m:15-17, Material/epsfun.m:41-58)
+# --------------------------------------------------------------------------
+class EpsConst:
+    def __init__(self, eps):
+        self.eps = complex(eps)
+
+    def __call__(self, enei):
+        enei = np.asarray(enei, dtype=float)
+        eps = np.full(enei.shape, self.eps, dtype=complex)
+        return eps, 2 * np.pi / enei * np.sqrt(eps)
+
+
+class EpsFun:
+    """``epsfun(fun, key)``: user function of wavelength (nm) or energy (eV)."""
+
+    def __init__(self, fun, key="nm"):
+        self.fun, self.key = fun, key
+
+    def __call__(self, enei):
+        enei = np.asarray(enei, dtype=float)
+        arg = enei if self.key == "nm" else EV2NM / enei
+        eps = np.asarray(self.fun(arg), dtype=complex)
+        return eps, 2 * np.pi / enei * np.sqrt(eps)
+
+
+def drude_eps(eps_inf=10.0, wp=9.065, gamma=0.0708):
+    """Drude metal as ``epsfun(@(w) eps_inf - wp^2./(w.*(w+1i*gamma)), 'eV')``."""
+    return EpsFun(lambda w: eps_inf - wp ** 2 / (w * (w + 1j * gamma)), "eV")
+
+
+# --------------------------------------------------------------------------
+# quadrature rules  (Misc/integration/lglnodes.m:13-32,
+#                    Misc/integration/@quadface/private/init.m:5-80)
+# --------------------------------------------------------------------------
+def lglnodes(n):
+    """Legendre-Gauss-Lobatto nodes/weights, n+1 points (lglnodes.m:13-32)."""
+    n1 = n + 1
+    x = np.cos(np.pi * np.arange(n1) / n)
+    P = np.zeros((n1, n1))
+    xold = 2.0 * np.ones_like(x)
+    while np.max(np.abs(x - xold)) > EPS:
+        xold = x
+        P[:, 0] = 1.0
+        P[:, 1] = x
+        for k in range(2, n1):
+            P[:, k] = ((2 * k - 1) * x * P[:, k - 1] - (k - 1) * P[:, k - 2]) / k
+        x = xold - (x * P[:, n] - P[:, n - 1]) / (n1 * P[:, n])
+    w = 2.0 / (n * n1 * P[:, n] ** 2)
+    return x, w
+
+
+class QuadFace:
+    """``quadface`` with ``rule = 18`` (28 points) and ``npol = [7, 5]``.
+
+    ``rule18`` is the (x, y, w) table of the 28-point Lyness-Jespersen rule
+    (triangle_unit_set.m:471-505), passed in by the caller.
+    """
+
+    def __init__(self, rule18, npol=(7, 5)):
+        self.x, self.y, self.w = [np.asarray(a, dtype=float) for a in rule18]
+        # polar triangle integration (init.m:27-53)
+        x1, w1 = lglnodes(npol[0])
+        rho = 0.5 * (x1 + 1 + 1e-6)
+        x2, w2 = lglnodes(npol[1])
+        phi = (270 + 60 * x2) / 180 * np.pi
+        phi0 = 120 / 180 * np.pi
+        rho_g, phi_g = np.meshgrid(rho, phi, indexing="ij")
+        rho_f, phi_f = rho_g.ravel(order="F"), phi_g.ravel(order="F")
+        rad = 1.0 / np.abs(2 * np.sin(phi_f))
+        phis = np.stack([phi_f, phi_f + phi0, phi_f + 2 * phi0], axis=1)
+        xx = (np.cos(phis) * (rho_f * rad)[:, None]).ravel(order="F")
+        yy = (np.sin(phis) * (rho_f * rad)[:, None]).ravel(order="F")
+        self.x3 = (1 - np.sqrt(3) * xx - yy) / 3
+        self.y3 = (1 + np.sqrt(3) * xx - yy) / 3
+        w = np.outer(w1, w2).ravel(order="F")
+        w = np.tile(w * rho_f * rad ** 2, 3)
+        self.w3 = w / w.sum()
+        # polar quadrilateral integration (init.m:57-80)
+        x1, w1 = lglnodes(npol[0])
+        rho = 0.5 * (x1 + 1 + 1e-6)
+        x2, w2 = lglnodes(npol[1])
+        phi = (90 + 45 * x2) / 180 * np.pi
+        phi0 = np.pi / 2
+        rho_g, phi_g = np.meshgrid(rho, phi, indexing="ij")
+        rho_f, phi_f = rho_g.ravel(order="F"), phi_g.ravel(order="F")
+        rad = 1.0 / np.abs(np.sin(phi_f))
+        phis = np.stack([phi_f + i * phi0 for i in range(4)], axis=1)
+        self.x4 = (np.cos(phis) * (rho_f * rad)[:, None]).ravel(order="F")
+        self.y4 = (np.sin(phis) * (rho_f * rad)[:, None]).ravel(order="F")
+        w = np.outer(w1, w2).ravel(order="F")
+        w = np.tile(w * rho_f * rad ** 2, 4)
+        self.w4 = 4 * w / w.sum()
+
+
+# --------------------------------------------------------------------------
+# particle geometry  (Particles/@particle/private/norm_flat.m:8-62,
+#   quad_flat.m:13-56, quadpol_flat.m:15-78, Misc/+misc/bradius.m:11-32)
+# --------------------------------------------------------------------------
+def _quad_shape(x, y):
+    """Bilinear 4-node shape functions and derivatives (Misc/+shape/@quad)."""
+    s = 0.25 * np.stack([(1 - x) * (1 - y), (1 + x) * (1 - y), (1 + x) * (1 + y), (1 - x) * (1 + y)], 1)
+    sx = 0.25 * np.stack([-(1 - y), (1 - y), (1 + y), -(1 + y)], 1)
+    sy = 0.25 * np.stack([-(1 - x), -(1 + x), (1 + x), (1 - x)], 1)
+    return s, sx, sy
+
+
+class Particle:
+    """Flat-faced particle: ``pos``, ``area``, ``tvec1``, ``tvec2``, ``nvec``."""
+
+    def __init__(self, verts, faces, quad):
+        self.verts = np.asarray(verts, dtype=float)
+        faces = np.asarray(faces, dtype=np.int64)
+        if faces.shape[1] == 3:
+            faces = np.hstack([faces, -np.ones((faces.shape[0], 1), np.int64)])
+        self.faces = faces
+        self.quad = quad
+        self.n = faces.shape[0]
+        self._norm_flat()
+
+    # index34.m
+    def index34(self, ind=None):
+        f = self.faces if ind is None else self.faces[ind]
+        return np.nonzero(f[:, 3] < 0)[0], np.nonzero(f[:, 3] >= 0)[0]
+
+    # totriangles_flat.m
+    def totriangles(self, ind=None):
+        ind = np.arange(self.n) if ind is None else np.asarray(ind)
+        _, i4 = self.index34(ind)
+        faces = self.faces[ind][:, [0, 1, 2]]
+        if i4.size:
+            faces = np.vstack([faces, self.faces[ind[i4]][:, [2, 3, 0]]])
+            i4 = np.stack([i4, ind.size + np.arange(i4.size)], 1)
+        else:
+            i4 = np.zeros((0, 2), np.int64)
+        return faces, i4
+
+    def _norm_flat(self):
+        v, f, n = self.verts, self.faces, self.n
+        i3, i4 = self.index34()
+        pos = np.zeros((n, 3))
+        pos[i3] = (v[f[i3, 0]] + v[f[i3, 1]] + v[f[i3, 2]]) / 3
+        if i4.size:
+            pos[i4] = (v[f[i4, 0]] + v[f[i4, 1]] + v[f[i4, 2]] + v[f[i4, 3]]) / 4
+        faces, ind4 = self.totriangles()
+        v1, v2, v3 = v[faces[:, 0]], v[faces[:, 1]], v[faces[:, 2]]
+        vec1, vec2 = v1 - v2, v3 - v2
+        nvec = np.cross(vec1, vec2)
+        area = 0.5 * np.sqrt(np.sum(nvec * nvec, 1))
+        vec1 = vec1 / np.sqrt(np.sum(vec1 * vec1, 1))[:, None]
+        nvec = nvec / np.sqrt(np.sum(nvec * nvec, 1))[:, None]
+        vec2 = np.cross(nvec, vec1)
+        if ind4.shape[0] == 0:
+            self.area = area
+        else:
+            self.area = area[:n].copy()
+            np.add.at(self.area, ind4[:, 0], area[ind4[:, 1]])
+            big2 = area[ind4[:, 1]] > area[ind4[:, 0]]
+            src, dst = ind4[big2, 1], ind4[big2, 0]
+            vec1[dst], vec2[dst], nvec[dst] = vec1[src], vec2[src], nvec[src]
+        self.pos = pos
+        self.tvec1, self.tvec2, self.nvec = vec1[:n], vec2[:n], nvec[:n]
+
+    def quad_points(self, ind):
+        """Boundary-element points/weights for faces ``ind`` (quad_flat.m:13-56).
+
+        Returns ``pos [m, 3]``, ``w [m]`` and ``row [m]`` (index into ``ind``).
+        """
+        ind = np.asarray(ind)
+        faces, ind4 = self.totriangles(ind)
+        ind3 = np.arange(ind.size)
+        if ind4.shape[0]:
+            ind3 = np.concatenate([ind3, ind4[:, 0]])
+        v = self.verts
+        nv = np.cross(v[faces[:, 1]] - v[faces[:, 0]], v[faces[:, 2]] - v[faces[:, 0]])
+        area = 0.5 * np.sqrt(np.sum(nv * nv, 1))
+        q = self.quad
+        tri = np.stack([q.x, q.y, 1 - q.x - q.y], 1)
+        pos = np.einsum("pk,tkc->tpc", tri, v[faces[:, :3]]).reshape(-1, 3)
+        w = (q.w[None, :] * area[:, None]).ravel()
+        row = np.repeat(ind3, q.w.size)
+        return pos, w, row
+
+    def quadpol_points(self, ind):
+        """Polar points/weights around centroids (quadpol_flat.m:15-78)."""
+        ind = np.asarray(ind)
+        i3, i4 = self.index34(ind)
+        q, v = self.quad, self.verts
+        pos, w, row = [], [], []
+        if i3.size:
+            tri = np.stack([q.x3, q.y3, 1 - q.x3 - q.y3], 1)
+            for i in i3:
+                pos.append(tri @ v[self.faces[ind[i], :3]])
+                w.append(q.w3 * self.area[ind[i]])
+                row.append(np.full(q.w3.size, i))
+        if i4.size:
+            s, sx, sy = _quad_shape(q.x4, q.y4)
+            for i in i4:
+                vv = v[self.faces[ind[i], :4]]
+                px, py = sx @ vv, sy @ vv
+                nv = np.cross(px, py)
+                pos.append(s @ vv)
+                w.append(q.w4 * np.sqrt(np.sum(nv * nv, 1)))
+                row.append(np.full(q.w4.size, i))
+        return np.vstack(pos), np.concatenate(w), np.concatenate(row)
+
+    def bradius(self):
+        """Max centroid-to-vertex distance per face (bradius.m:11-32)."""
+        r = np.zeros(self.n)
+        i3, i4 = self.index34()
+        for idx, nvert in ((i3, 3), (i4, 4)):
+            for k in range(nvert):
+                d = np.sqrt(np.sum((self.pos[idx] - self.verts[self.faces[idx, k]]) ** 2, 1))
+                r[idx] = np.maximum(r[idx], d)
+        return r
+
+
+# --------------------------------------------------------------------------
+# composite particle  (Particles/@comparticle, Particles/@compound/connect.m)
+# --------------------------------------------------------------------------
+class ComParticle:
+    """Concatenation of particles with their media (``inout``) and closed flags.
+
+    ``inout[i] = (medium inside, medium outside)`` (1-based medium indices into
+    ``eps``), ``closed[i]`` is True when particle i is a closed surface by
+    itself (the ``comparticle(..., 1, 2, ...)`` case of the demos).
+    """
+
+    def __init__(self, eps, parts, inout, closed):
+        self.eps = eps
+        self.parts = parts
+        self.inout = np.asarray(inout, dtype=np.int64).reshape(-1, 2)
+        self.closed = list(closed)
+        offs = np.cumsum([0] + [p.n for p in parts])
+        self.offsets = offs
+        self.n = int(offs[-1])
+        verts, faces = [], []
+        voff = 0
+        for p in parts:
+            verts.append(p.verts)
+            f = p.faces.copy()
+            f[f >= 0] += voff
+            faces.append(f)
+            voff += p.verts.shape[0]
+        self.pc = Particle(np.vstack(verts), np.vstack(faces), parts[0].quad)
+        self.pos, self.area, self.nvec = self.pc.pos, self.pc.area, self.pc.nvec
+        self.tvec1, self.tvec2 = self.pc.tvec1, self.pc.tvec2
+
+    def index(self, i):
+        return np.arange(self.offsets[i], self.offsets[i + 1])
+
+    def bradius(self):
+        return self.pc.bradius()
+
+    def quad_points(self, ind):
+        return self.pc.quad_points(ind)
+
+    def quadpol_points(self, ind):
+        return self.pc.quadpol_points(ind)
+
+    def face_media(self):
+        """Per-face inside/outside medium (``expand`` of inout)."""
+        return np.repeat(self.inout, [p.n for p in self.parts], axis=0)
+
+    def eps_faces(self, enei, side):
+        med = self.face_media()[:, side]
+        vals = {m: self.eps[m - 1](enei)[0] for m in np.unique(med)}
+        return np.array([vals[m] for m in med], dtype=complex)
+
+
+def connect(inout):
+    """Connectivity ``con[a][b][i1, i2]`` (Particles/@compound/connect.m:40-57)."""
+    con = [[None, None], [None, None]]
+    for a in range(2):
+        for b in range(2):
+            c1 = inout[:, a][:, None]
+            c2 = inout[:, b][None, :]
+            con[a][b] = np.where(c1 == c2, c1 + 0 * c2, 0)
+    return con
+
+
+# --------------------------------------------------------------------------
+# refinement pattern  (Greenfun/+green/refinematrix.m:28-68,
+#                      Misc/+misc/pdist2.m:13-17)
+# --------------------------------------------------------------------------
+def refinematrix(p, rel_cutoff=3.0, abs_cutoff=0.0):
+    """Dense int8 pattern: 2 = self element, 1 = near pair, 0 = far."""
+    pos = p.pos
+    rad = p.bradius()
+    sq = np.sum(pos * pos, 1)
+    d2 = sq[:, None] + sq[None, :] - 2 * pos @ pos.T
+    d2[d2 < 1e-10] = 0
+    d = np.sqrt(d2)
+    dd = d - rad[None, :]
+    idist = dd / rad[:, None]
+    ir = np.zeros(d.shape, np.int8)
+    ir[d == 0] = 2
+    ir[((dd < abs_cutoff) | (idist < rel_cutoff)) & (d != 0)] = 1
+    return ir
+
+
+# --------------------------------------------------------------------------
+# greenret: refined Taylor coefficients  (Greenfun/@greenret/private/init.m)
+# --------------------------------------------------------------------------
+class GreenRet:
+    """Retarded Green function with 'cart' derivative and near-field refinement.
+
+    ``ind`` are the column-major linear indices of refined elements
+    (init.m:24), ``g [nref, order+1]`` and ``f [nref, 3, order+1]`` their Taylor
+    coefficients in powers of (i k).
+    """
+
+    def __init__(self, p, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+        self.p = p
+        self.order = order
+        ir = refinematrix(p, rel_cutoff, abs_cutoff)
+        n = p.n
+        rows, cols = np.nonzero(ir.T)          # column-major order of find()
+        rows, cols = cols, rows
+        self.ind = rows + cols * n
+        self.rows, self.cols = rows, cols
+        lookup = {(int(r), int(c)): k for k, (r, c) in enumerate(zip(rows, cols))}
+        g = np.zeros((rows.size, order + 1))
+        f = np.zeros((rows.size, 3, order + 1))
+        pos1 = p.pos
+        # ---- diagonal elements (init.m:42-95)
+        dface = np.nonzero(np.diag(ir) == 2)[0]
+        if dface.size:
+            iface = np.array([lookup[(int(i), int(i))] for i in dface])
+            pos, w, row = p.quadpol_points(dface)
+            vec = pos1[dface[row]] - pos
+            r = np.sqrt(np.sum(vec * vec, 1))
+
+            def acc(x, o):
+                return np.bincount(row, weights=w * x, minlength=dface.size) / math.factorial(o)
+
+            for o in range(order + 1):
+                g[iface, o] = acc(r ** (o - 1), o)
+            nv, t1, t2 = p.nvec[dface[row]], p.tvec1[dface[row]], p.tvec2[dface[row]]
+            inn = np.sum(vec * nv, 1)
+            rr = np.maximum(r, 1e-4 * np.max(r))
+            in1 = np.sum(vec * t1, 1)
+            in2 = np.sum(vec * t2, 1)
+            for o in range(order + 1):
+                fn = acc((o - 1) * inn * r ** (o - 3), o)
+                f1 = acc((o - 1) * in1 * r ** o / rr ** 3, o)
+                f2 = acc((o - 1) * in2 * r ** o / rr ** 3, o)
+                f[iface, :, o] = (p.nvec[dface] * fn[:, None] + p.tvec1[dface] * f1[:, None]
+                                  + p.tvec2[dface] * f2[:, None])
+        # ---- off-diagonal elements (init.m:98-177)
+        reface = np.nonzero(np.any(ir == 1, axis=0))[0]
+        if reface.size:
+            postab, wtab, rowtab = p.quad_points(reface)
+            for k2, face in enumerate(reface):
+                nb = np.nonzero(ir[:, face] == 1)[0]
+                iface = np.array([lookup[(int(i), int(face))] for i in nb])
+                sel = rowtab == k2
+                pts, w = postab[sel], wtab[sel]
+                x = pos1[nb, 0][:, None] - pts[None, :, 0]
+                y = pos1[nb, 1][:, None] - pts[None, :, 1]
+                z = pos1[nb, 2][:, None] - pts[None, :, 2]
+                r = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+                vec0 = -(pos1[nb] - p.pos[face])
+                r0 = np.sqrt(np.sum(vec0 * vec0, 1))
+                dr = r - r0[:, None]
+                for o in range(order + 1):
+                    g[iface, o] = (dr ** o / r / math.factorial(o)) @ w
+
+                def fun(ff):
+                    return np.stack([(x * ff) @ w, (y * ff) @ w, (z * ff) @ w], 1)
+
+                f[iface, :, 0] = -fun(1.0 / r ** 3)
+                for o in range(1, order + 1):
+                    f[iface, :, o] = fun(-dr ** o / (r ** 3 * math.factorial(o))
+                                         + dr ** (o - 1) / (r ** 2 * math.factorial(o - 1)))
+        self.g, self.f = g, f
+
+    # greenret/private/eval2.m:19-117, 'cart' branch with only F requested
+    def eval_F_indexed(self, rows, cols, k):
+        p = self.p
+        d = np.maximum(np.sqrt(np.sum((p.pos[rows] - p.pos[cols]) ** 2, 1)), EPS)
+        fr = (1j * k) ** np.arange(self.order + 1)
+        inn = np.sum(p.nvec[rows] * (p.pos[rows] - p.pos[cols]), 1)
+        F = inn * (1j * k - 1 / d) / d ** 2 * p.area[cols]
+        lin = rows + cols * p.n
+        _, i1, i2 = np.intersect1d(self.ind, lin, return_indices=True)
+        if i1.size:
+            F[i2] = np.einsum("kc,kco->ko", p.nvec[rows[i2]], self.f[i1]) @ fr
+        return F * np.exp(1j * k * d)
+
+    # greenret/diag.m:10-30 ('cart' f: add a 3-vector to the order-0 term)
+    def add_diag(self, faces, fvec):
+        lin = faces + faces * self.p.n
+        pos = np.searchsorted(self.ind, lin)
+        assert np.all(self.ind[pos] == lin)
+        self.f[pos, :, 0] += fvec
+
+    def eval_full(self, k, rows, cols):
+        """G and F for the sub-block rows x cols (eval1.m:18-40, 110-124).
+
+        Returns the block of G and F (before adding +-2*pi on the diagonal)
+        and a mask of the d == 0 entries.
+        """
+        p = self.p
+        x = p.pos[rows, 0][:, None] - p.pos[cols, 0][None, :]
+        y = p.pos[rows, 1][:, None] - p.pos[cols, 1][None, :]
+        z = p.pos[rows, 2][:, None] - p.pos[cols, 2][None, :]
+        d = np.maximum(np.sqrt(x ** 2 + y ** 2 + z ** 2), EPS)
+        area = p.area[cols][None, :]
+        G = (1.0 / d * area).astype(complex)
+        ff = (1j * k - 1.0 / d) / d ** 2
+        nv = p.nvec[rows]
+        F = (ff * x * nv[:, 0:1] + ff * y * nv[:, 1:2] + ff * z * nv[:, 2:3]) * area
+        # refined entries that fall inside the block
+        n = p.n
+        rpos = np.full(n, -1)
+        rpos[rows] = np.arange(rows.size)
+        cpos = np.full(n, -1)
+        cpos[cols] = np.arange(cols.size)
+        sel = (rpos[self.rows] >= 0) & (cpos[self.cols] >= 0)
+        if np.any(sel):
+            fr = (1j * k) ** np.arange(self.order + 1)
+            ri, ci = rpos[self.rows[sel]], cpos[self.cols[sel]]
+            G[ri, ci] = self.g[sel] @ fr
+            F[ri, ci] = np.einsum("kc,kco->ko", p.nvec[self.rows[sel]], self.f[sel]) @ fr
+        ph = np.exp(1j * k * d)
+        return G * ph, F * ph, d == EPS
+
+
+def initclosed(gr, cp):
+    """Fuchs-Liu sum rule on the order-0 diagonal (initclosed.m:19-89)."""
+    for i in range(len(cp.parts)):
+        if not cp.closed[i]:
+            continue
+        ind = cp.index(i)
+        rows = np.repeat(ind, ind.size)           # closed surface = particle i
+        cols = np.tile(ind, ind.size)
+        F = gr.eval_F_indexed(rows, cols, 0.0).real.reshape(ind.size, ind.size)
+        f = np.sum(cp.area[ind][:, None] * F / cp.area[ind][None, :], 0)
+        gr.add_diag(ind, cp.nvec[ind] * (-2 * np.pi * 1 - f)[:, None])
+
+
+class CompGreenRet:
+    """compgreenret(p, p, op): greenret + closed-surface diagonal + con."""
+
+    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+        self.p = cp
+        self.g = GreenRet(cp, order, rel_cutoff, abs_cutoff)
+        initclosed(self.g, cp)
+        self.con = connect(cp.inout)
+
+    # compgreenret/private/eval1.m:16-51
+    def eval(self, a, b, key, enei):
+        cp = self.p
+        k = np.array([e(enei)[1] for e in cp.eps], dtype=complex)
+        con = self.con[a][b]
+        out = np.zeros((cp.n, cp.n), dtype=complex)
+        any_block = False
+        for i1 in range(con.shape[0]):
+            for i2 in range(con.shape[1]):
+                if con[i1, i2]:
+                    any_block = True
+                    r, c = cp.index(i1), cp.index(i2)
+                    G, F, dz = self.g.eval_full(k[con[i1, i2] - 1], r, c)
+                    if key == "G":
+                        blk = G
+                    elif key == "F":
+                        blk = F
+                    elif key == "H1":
+                        blk = F + 2 * np.pi * dz
+                    elif key == "H2":
+                        blk = F - 2 * np.pi * dz
+                    out[np.ix_(r, c)] = blk
+        if not any_block or not np.any(out):
+            return 0
+        return out
+
+
+# --------------------------------------------------------------------------
+# bemret  (BEM/@bemret/private/initmat.m:5-74, excitation.m:4-29,
+#          mldivide.m:12-49)
+# --------------------------------------------------------------------------
+def _matmul(a, x):
+    """Misc/matmul.m: scalar / matrix times [n, ...] array."""
+    if np.isscalar(a) or np.ndim(a) == 0:
+        return 0 if a == 0 else a * x
+    if np.isscalar(x) and x == 0:
+        return 0
+    sh = x.shape
+    return (a @ x.reshape(sh[0], -1)).reshape(sh)
+
+
+def _inner(nvec, a):
+    """Misc/inner.m: sum_k nvec[i,k] * a[i,k,...] (nvec real)."""
+    if np.isscalar(a):
+        return 0
+    return np.einsum("ik,ik...->i...", nvec, a)
+
+
+def _outer(nvec, val):
+    """Misc/outer.m: a[i,k,...] = nvec[i,k] * val[i,...]."""
+    if np.isscalar(val):
+        return 0
+    return nvec[:, :, None] * val[:, None, ...] if val.ndim == 2 else np.einsum("ik,i->ik", nvec, val)
+
+
+class BemRet:
+    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+        self.p = cp
+        self.g = CompGreenRet(cp, order, rel_cutoff, abs_cutoff)
+        self.enei = None
+
+    def matrices(self, enei):
+        """G1, H1, G2, H2 as in initmat.m:27-31."""
+        g = self.g
+
+        def sub(a, b):
+            if np.isscalar(b) and b == 0:
+                return a
+            return a - b
+        G1 = sub(g.eval(0, 0, "G", enei), g.eval(1, 0, "G", enei))
+        G2 = sub(g.eval(1, 1, "G", enei), g.eval(0, 1, "G", enei))
+        H1 = sub(g.eval(0, 0, "H1", enei), g.eval(1, 0, "H1", enei))
+        H2 = sub(g.eval(1, 1, "H2", enei), g.eval(0, 1, "H2", enei))
+        return G1, H1, G2, H2
+
+    def _eps12(self, enei):
+        cp = self.p
+        e1, e2 = cp.eps_faces(enei, 0), cp.eps_faces(enei, 1)
+        if np.unique(e1).size == 1 and np.unique(e2).size == 1:
+            return e1[0], e2[0]
+        return np.diag(e1), np.diag(e2)
+
+    def initmat(self, enei):
+        if self.enei == enei:
+            return
+        self.enei = enei
+        nvec = self.p.nvec
+        k = 2 * np.pi / enei
+        eps1, eps2 = self._eps12(enei)
+        G1, H1, G2, H2 = self.matrices(enei)
+        G1i = np.linalg.inv(G1)
+        G2i = np.linalg.inv(G2)
+        if not np.any(self.g.con[0][1]):
+            L1, L2 = eps1, eps2
+        else:
+            L1 = G1 @ (eps1 * np.eye(G1.shape[0]) if np.ndim(eps1) == 0 else eps1) @ G1i
+            L2 = G2 @ (eps2 * np.eye(G2.shape[0]) if np.ndim(eps2) == 0 else eps2) @ G2i
+        Sigma1 = H1 @ G1i
+        Sigma2 = H2 @ G2i
+        Deltai = np.linalg.inv(Sigma1 - Sigma2)
+        L = L1 - L2
+        nn = nvec @ nvec.T
+        if np.ndim(L) == 0:
+            Sigma = Sigma1 * L1 - Sigma2 * L2 + k ** 2 * ((L * Deltai) * nn) * L
+        else:
+            Sigma = Sigma1 @ L1 - Sigma2 @ L2 + k ** 2 * ((L @ Deltai) * nn) @ L
+        self.k, self.nvec = k, nvec
+        self.eps1, self.eps2 = eps1, eps2
+        self.G1i, self.G2i, self.L1, self.L2 = G1i, G2i, L1, L2
+        self.Sigma1, self.Deltai = Sigma1, Deltai
+        self.Sigmai = np.linalg.inv(Sigma)
+        self.G1, self.H1, self.G2, self.H2 = G1, H1, G2, H2
+
+    def excitation(self, exc):
+        """excitation.m:4-29 for potentials a1, a1p, a2, a2p (no scalar phi)."""
+        k = 2 * np.pi / exc["enei"]
+        eps1 = self.p.eps_faces(exc["enei"], 0)
+        eps2 = self.p.eps_faces(exc["enei"], 1)
+        nvec = self.nvec
+        a1, a1p, a2, a2p = exc["a1"], exc["a1p"], exc["a2"], exc["a2p"]
+        phi = np.zeros((nvec.shape[0], a1.shape[2]), dtype=complex)
+        a = a2 - a1
+        alpha = a2p - a1p
+        De = -1j * k * (eps2[:, None] * _inner(nvec, a2) - eps1[:, None] * _inner(nvec, a1))
+        return phi, a, alpha, De
+
+    def solve(self, exc):
+        """mldivide.m:12-49 -> dict with sig1, sig2 [n, npol], h1, h2 [n, 3, npol]."""
+        self.initmat(exc["enei"])
+        phi, a, alpha, De = self.excitation(exc)
+        k, nvec = self.k, self.nvec
+        G1i, G2i, L1, L2 = self.G1i, self.G2i, self.L1, self.L2
+        Sigma1, Deltai, Sigmai = self.Sigma1, self.Deltai, self.Sigmai
+        alpha = alpha - _matmul(Sigma1, a) + 1j * k * _outer(nvec, _matmul(L1, phi))
+        De = De - _matmul(Sigma1, _matmul(L1, phi)) + 1j * k * _inner(nvec, _matmul(L1, a))
+        sig2 = _matmul(Sigmai, De + 1j * k * _inner(nvec, _matmul(L1 - L2, _matmul(Deltai, alpha))))
+        h2 = _matmul(Deltai, 1j * k * _outer(nvec, _matmul(L1 - L2, sig2)) + alpha)
+        sig1 = _matmul(G1i, sig2 + phi)
+        h1 = _matmul(G1i, h2 + a)
+        sig2 = _matmul(G2i, sig2)
+        h2 = _matmul(G2i, h2)
+        return {"enei": exc["enei"], "sig1": sig1, "sig2": sig2, "h1": h1, "h2": h2}
+
+    def afun(self, sig1, h1, sig2, h2):
+        """Full BEM operator (BEM/@bemretiter/private/afun.m:6-35).
+
+        Maps (sig1, h1, sig2, h2) to (phi, a, De, alpha) using the stored
+        G1, G2, H1, H2 and per-face eps1, eps2.
+        """
+        k, nvec = self.k, self.nvec
+        e1 = self.p.eps_faces(self.enei, 0)
+        e2 = self.p.eps_faces(self.enei, 1)
+        G1, G2, H1, H2 = self.G1, self.G2, self.H1, self.H2
+        Gs1, Gh1 = _matmul(G1, sig1), _matmul(G1, h1)
+        Gs2, Gh2 = _matmul(G2, sig2), _matmul(G2, h2)
+        Hs1, Hh1 = _matmul(H1, sig1), _matmul(H1, h1)
+        Hs2, Hh2 = _matmul(H2, sig2), _matmul(H2, h2)
+        phi = Gs1 - Gs2
+        a = Gh1 - Gh2
+        alpha = Hh1 - Hh2 - 1j * k * _outer(nvec, e1[:, None] * Gs1 - e2[:, None] * Gs2)
+        De = (e1[:, None] * Hs1 - e2[:, None] * Hs2
+              - 1j * k * _inner(nvec, e1[:, None, None] * Gh1 - e2[:, None, None] * Gh2))
+        return phi, a, De, alpha
+
+
+# --------------------------------------------------------------------------
+# plane wave + spectra  (Simulation/retarded/@planewaveret/potential.m:13-57,
+#   extinction.m:12-16, scattering.m:13-19, @spectrumret/farfield.m:15-74,
+#   Simulation/retarded/scattering.m:14-31)
+# --------------------------------------------------------------------------
+class PlaneWaveRet:
+    def __init__(self, pol, dir, pinfty, medium=1):
+        self.pol = np.atleast_2d(np.asarray(pol, dtype=float))
+        self.dir = np.atleast_2d(np.asarray(dir, dtype=float))
+        assert not np.any(np.sum(self.pol * self.dir, 1))
+        self.medium = medium
+        self.pinfty = pinfty        # Particle: unit sphere at infinity
+
+    def potential(self, cp, enei):
+        nb = np.sqrt(cp.eps[self.medium - 1](enei)[0])
+        k0 = 2 * np.pi / enei
+        k = k0 * nb
+        npol = self.pol.shape[0]
+        media = cp.face_media()
+        exc = {"enei": enei}
+        for side, (ka, kp) in enumerate((("a1", "a1p"), ("a2", "a2p"))):
+            a = np.zeros((cp.n, 3, npol), dtype=complex)
+            ap = np.zeros((cp.n, 3, npol), dtype=complex)
+            ind = np.nonzero(media[:, side] == self.medium)[0]
+            for i in range(npol):
+                phase = np.exp(1j * k * cp.pos[ind] @ self.dir[i]) / (1j * k0)
+                a[ind, :, i] = phase[:, None] * self.pol[i][None, :]
+                ap[ind, :, i] = ((1j * k * cp.nvec[ind] @ self.dir[i]) * phase)[:, None] * self.pol[i][None, :]
+            exc[ka], exc[kp] = a, ap
+        return exc
+
+    def farfield(self, cp, sig, dirs):
+        enei = sig["enei"]
+        k = cp.eps[self.medium - 1](enei)[1]
+        k0 = 2 * np.pi / enei
+        phase = np.exp(-1j * k * dirs @ cp.pos.T) * cp.area[None, :]
+        media = cp.face_media()
+        npol = sig["sig2"].shape[1]
+        e = np.zeros((dirs.shape[0], 3, npol), dtype=complex)
+        h = np.zeros_like(e)
+        for side, (ks, kh) in enumerate((("sig1", "h1"), ("sig2", "h2"))):
+            ind = np.nonzero(media[:, side] == self.medium)[0]
+            if ind.size == 0:
+                continue
+            ph = phase[:, ind]
+            Ph = np.einsum("dn,nkp->dkp", ph, sig[kh][ind])
+            Ps = ph @ sig[ks][ind]
+            e += 1j * k0 * Ph - 1j * k * dirs[:, :, None] * Ps[:, None, :]
+            h += 1j * k * np.cross(np.broadcast_to(dirs[:, :, None], Ph.shape), Ph, axis=1)
+        return e, h, k
+
+    def extinction(self, cp, sig):
+        e, h, k = self.farfield(cp, sig, self.dir)
+        npol = self.pol.shape[0]
+        val = np.array([np.sum(np.conj(self.pol[i]) * e[i, :, i]) for i in range(npol)])
+        return 4 * np.pi / k * np.imag(val)
+
+    def scattering(self, cp, sig):
+        pinf = self.pinfty
+        e, h, k = self.farfield(cp, sig, pinf.nvec)
+        dsca = 0.5 * np.real(np.einsum("dk,dkp->dp", pinf.nvec, np.cross(e, np.conj(h), axis=1)))
+        sca = pinf.area @ dsca
+        nb = np.sqrt(cp.eps[0](sig["enei"])[0])
+        return np.real(sca / (0.5 * nb))
+
+
+# --------------------------------------------------------------------------
+# Mie theory  (Mie/@mieret/extinction.m:9-28, scattering.m:9-28,
+#   private/miecoefficients.m:14-31, private/riccatibessel.m:17-34)
+# --------------------------------------------------------------------------
+def _riccatibessel(z, lmax):
+    l = np.arange(1, lmax + 1)
+    j0 = np.sin(z) / z
+    j = np.sqrt(np.pi / (2 * z)) * scipy.special.jv(l + 0.5, z)
+    y0 = -np.cos(z) / z
+    y = np.sqrt(np.pi / (2 * z)) * scipy.special.yv(l + 0.5, z)
+    h0 = j0 + 1j * y0
+    h = j + 1j * y
+    zjp = z * np.concatenate([[j0], j[:-1]]) - l * j
+    zhp = z * np.concatenate([[h0], h[:-1]]) - l * h
+    return j, h, zjp, zhp
+
+
+def mie_coefficients(k, diameter, epsr, lmax=20, mur=1.0):
+    nr = np.sqrt(epsr * mur)
+    j1, _, zjp1, _ = _riccatibessel(nr * k * diameter / 2, lmax)
+    j2, h2, zjp2, zhp2 = _riccatibessel(k * diameter / 2 + 0j, lmax)
+    a = (nr ** 2 * j1 * zjp2 - mur * j2 * zjp1) / (nr ** 2 * j1 * zhp2 - mur * h2 * zjp1)
+    b = (mur * j1 * zjp2 - j2 * zjp1) / (mur * j1 * zhp2 - h2 * zjp1)
+    return a, b
+
+
+def mie_ext_sca(epsin, epsout, diameter, enei, lmax=20):
+    enei = np.atleast_1d(np.asarray(enei, dtype=float))
+    epsb = epsout(enei)[0]
+    nb = np.sqrt(epsb)
+    k = 2 * np.pi / enei * nb
+    epsz = epsin(enei)[0] / epsb
+    l = np.arange(1, lmax + 1)
+    ext, sca = np.zeros(enei.size), np.zeros(enei.size)
+    for i in range(enei.size):
+        a, b = mie_coefficients(k[i], diameter, epsz[i], lmax)
+        ext[i] = np.real(2 * np.pi / k[i] ** 2 * np.sum((2 * l + 1) * np.real(a + b)))
+        sca[i] = np.real(2 * np.pi / k[i] ** 2 * np.sum((2 * l + 1) * (np.abs(a) ** 2 + np.abs(b) ** 2)))
+    return ext, sca
+
+
+# --------------------------------------------------------------------------
+# one-call driver used by tests and the CPU baseline
+# --------------------------------------------------------------------------
+def solve_spectrum(cp, pw, eneis, order=5, rel_cutoff=3.0):
+    """bemsolver + loop over wavelengths: returns ext, sca [nenei, npol] and
+    the list of solutions (demospecret1.m:20-41)."""
+    bem = BemRet(cp, order, rel_cutoff)
+    ext, sca, sols = [], [], []
+    for enei in eneis:
+        sig = bem.solve(pw.potential(cp, enei))
+        ext.append(pw.extinction(cp, sig))
+        sca.append(pw.scattering(cp, sig))
+        sols.append(sig)
+    return np.array(ext), np.array(sca), sols, bem
