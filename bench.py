@@ -1,0 +1,436 @@
+#!/usr/bin/env python
+"""Throughput of the retarded BEM path: wavelength-solves/s on GB300.
+
+One wavelength-solve = assembly of G1, H1, G2, H2 (with near-field
+refinement), the bemret inversions and products, the mldivide chain for all
+polarisations, FP64 iterative refinement (mixed precision), and the extinction
+and scattering cross sections.  The per-geometry set-up (refinement
+coefficients, closed-surface sum rule) runs once before timing, like
+``bem = bemsolver(p, op)`` in MNPBEM.
+
+Workload (synthetic, deterministic): sphere of diameter 50 nm with 4000 flat
+faces, Drude metal eps(w) = 10 - 9.065^2 / (w (w + 0.0708 i)) (w in eV) in
+eps = 1.77, x-polarised plane wave along +z, wavelengths on the 60-point grid
+450..750 nm.  A step is one batch of ``--batch`` wavelengths per GPU; with N
+GPUs rank r takes its own wavelengths (weak scaling, no collective on the
+data path).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "wavelength-solves/s at N faces: mixed+batched vs FP64 GPU, ext err ≤1e-6"
+UNIT = "wavelength-solves/s"
+DRUDE = (10.0, 9.065, 0.0708)
+NGRID = 60
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--faces", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=10, help="wavelengths per step per GPU")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (default: workload)")
+    return ap.parse_args()
+
+
+def grid():
+    return np.linspace(450.0, 750.0, NGRID)
+
+
+def step_wavelengths(step, rank, world, batch):
+    base = (step * world + rank) * batch
+    return grid()[(base + np.arange(batch)) % NGRID]
+
+
+def workload_desc(a):
+    return ("sphere d=50 nm, %d flat faces, Drude eps_inf=10 wp=9.065 eV gamma=0.0708 eV in eps=1.77, "
+            "x-pol along +z, %d-point wavelength grid 450-750 nm, %d wavelengths per step per GPU"
+            % (a.faces, NGRID, a.batch))
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- our arm
+def drude():
+    import mnpbem_gb300 as m
+    e0, wp, g = DRUDE
+    return m.epsfun(lambda w: e0 - wp ** 2 / (w * (w + 1j * g)), "eV")
+
+
+def make_problem(a, device, precision):
+    import mnpbem_gb300 as m
+    from mnpbem_gb300 import shapes
+    v, f = shapes.fibsphere(a.faces, 50.0)
+    p = m.particle(v, f)
+    cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
+    bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device))
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    return cp, bem, exc
+
+
+class DeviceSweep:
+    """Direct C-ABI call with device-resident outputs (the ``value`` path)."""
+
+    def __init__(self, bem, exc, batch, torch):
+        from mnpbem_gb300 import _lib
+        self._lib, self.bem, self.exc, self.batch = _lib, bem, exc, batch
+        n, P = bem.p.n, exc.npol
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.ext = torch.empty((batch, P), dtype=torch.float64, device=dev)
+        self.sca = torch.empty((batch, P), dtype=torch.float64, device=dev)
+        self.sig1 = torch.empty((batch, n, P, 2), dtype=torch.float64, device=dev)
+        self.sig2 = torch.empty((batch, n, P, 2), dtype=torch.float64, device=dev)
+        self.h1 = torch.empty((batch, n, 3, P, 2), dtype=torch.float64, device=dev)
+        self.h2 = torch.empty((batch, n, 3, P, 2), dtype=torch.float64, device=dev)
+        self.iters = np.zeros(batch, dtype=np.int32)
+        self.resid = np.zeros(batch)
+        self.pw = exc._struct()
+        self.ref = _lib.Refine(bem.refine_iters, bem.refine_tol)
+
+    def run(self, enei):
+        _lib = self._lib
+        enei = np.ascontiguousarray(enei, dtype=np.float64)
+        em = np.ascontiguousarray(self.bem.p.eps_media(enei))
+        sol = _lib.Solution()
+        sol.ext, sol.sca = self.ext.data_ptr(), self.sca.data_ptr()
+        sol.sig1, sol.sig2 = self.sig1.data_ptr(), self.sig2.data_ptr()
+        sol.h1, sol.h2 = self.h1.data_ptr(), self.h2.data_ptr()
+        sol.ir_iters, sol.ir_resid = self.iters.ctypes.data, self.resid.ctypes.data
+        sol.outputs_on_device = 1
+        _lib.check(self.bem._lib.mnpbem_solve(
+            self.bem.handle, ctypes.byref(self.pw), enei.size, _lib.dptr(enei),
+            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.shape[1], self.bem.precision,
+            ctypes.byref(self.ref), ctypes.byref(sol)))
+
+
+def lib_stream(bem, torch):
+    from mnpbem_gb300 import _lib
+    s = ctypes.c_void_p()
+    _lib.check(bem._lib.mnpbem_geom_stream(bem.handle, ctypes.byref(s)))
+    return torch.cuda.ExternalStream(s.value)
+
+
+def read_profile(bem):
+    from mnpbem_gb300 import _lib
+    names = ["assembly", "gemm_n3", "gemm_thin", "block_inverse", "elementwise", "spectra", "geometry"]
+    out = {}
+    for ph, nm in enumerate(names):
+        ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        nl = ctypes.c_int64()
+        _lib.check(bem._lib.mnpbem_profile_read(bem.handle, ph, ctypes.byref(ms), ctypes.byref(fl),
+                                                ctypes.byref(by), ctypes.byref(nl)))
+        out[nm] = {"ms": ms.value, "flops": fl.value, "bytes": by.value, "launches": nl.value}
+    return out
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def run_ours(a, rank, world, dist, torch):
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    cp, bem, exc = make_problem(a, device, a.precision)
+    sweep = DeviceSweep(bem, exc, a.batch, torch)
+    stream = lib_stream(bem, torch)
+    n, P = cp.n, exc.npol
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for s in range(a.warmup):
+        sweep.run(step_wavelengths(s, rank, world, a.batch))
+    # ---------------- timed region (device-resident outputs)
+    bem_lib = bem._lib
+    bem_lib.mnpbem_profile_reset(bem.handle)
+    bem_lib.mnpbem_profile_enable(bem.handle, 1)
+    clocks = ClockSampler(device)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(a.steps):
+        sweep.run(step_wavelengths(a.warmup + s, rank, world, a.batch))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    bem_lib.mnpbem_profile_enable(bem.handle, 0)
+    ms = e0.elapsed_time(e1)
+    prof = read_profile(bem)
+    iters = sweep.iters.copy()
+    # ---------------- e2e: public API, host (pinned) outputs, copies inside the region
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    host = {"ext": pin((a.batch, P), torch.float64), "sca": pin((a.batch, P), torch.float64),
+            "sig1": pin((a.batch, n, P), torch.complex128), "sig2": pin((a.batch, n, P), torch.complex128),
+            "h1": pin((a.batch, n, 3, P), torch.complex128), "h2": pin((a.batch, n, 3, P), torch.complex128)}
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for s in range(a.steps):
+        r = bem.spectrum(exc, step_wavelengths(a.warmup + a.steps + s, rank, world, a.batch),
+                         fields=True, out=host)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    e2e_wall = (time.perf_counter() - t0) * 1e3
+    nmed = len(cp.eps)
+    h2d = a.batch * (8 + 16 * nmed + 32 * n) + 48 * P + 32 * exc.spec.pinfty.n + 2 * n
+    d2h = a.batch * (16 * P * 8 * n + 16 * P + 16)
+    # ---------------- max over ranks
+    if dist is not None:
+        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    total = a.batch * a.steps * world
+    value = total / (ms / 1e3)
+    e2e_value = total / (e2e_ms / 1e3)
+    # ---------------- roofline of the dominant kernel class
+    dom = max((k for k in prof if k != "geometry"), key=lambda k: prof[k]["ms"])
+    hbm, bf16, src = peaks()
+    d = prof[dom]
+    if d["flops"] > 0:
+        achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
+        roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": bf16,
+                "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": src + " bf16 dense",
+                "traffic": None, "launches": d["launches"], "ms": d["ms"]}
+    else:
+        achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                "launches": d["launches"], "ms": d["ms"]}
+    asm = prof["assembly"]
+    extra = {"phases_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+             "assembly_hbm_gbs": asm["bytes"] / (asm["ms"] / 1e3) / 1e9 if asm["ms"] > 0 else None,
+             "assembled_pairs_per_s": (n * n * a.batch * a.steps) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
+             "refinement_iterations": iters.tolist()}
+    launches = int(sum(v["launches"] for k, v in prof.items() if k != "geometry"))
+    out = {"value": value, "ms": ms, "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                                             "d2h_bytes_per_step": int(d2h), "ms": e2e_ms,
+                                             "wall_ms": e2e_wall},
+           "roofline": roof, "gpu_launches": launches, "clocks": clk, "extra": extra,
+           "bem": bem, "exc": exc, "cp": cp, "sweep": sweep}
+    return out
+
+
+def fp64_comparison(a, cp, exc, torch, mixed_bem):
+    """Plain FP64 GPU path on one wavelength + accuracy of the mixed path."""
+    import mnpbem_gb300 as m
+    device = torch.cuda.current_device()
+    bem64 = m.bemsolver(cp, m.bemoptions(precision="fp64", device=device))
+    lam = [600.0]
+    bem64.spectrum(exc, [450.0])          # warm-up (kernel loading)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r64 = bem64.spectrum(exc, lam)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    rmx = mixed_bem.spectrum(exc, lam)
+    err_ext = float(np.max(np.abs(rmx["ext"] - r64["ext"]) / np.abs(r64["ext"])))
+    err_sca = float(np.max(np.abs(rmx["sca"] - r64["sca"]) / np.abs(r64["sca"])))
+    return {"value": 1.0 / t64, "unit": UNIT, "sample": "1 wavelength (600 nm), same workload",
+            "ext_rel_err_mixed_vs_fp64": err_ext, "sca_rel_err_mixed_vs_fp64": err_sca}
+
+
+# ---------------------------------------------------------- CPU / reference
+def cpu_problem(faces):
+    from mnpbem_gb300 import shapes
+    from oracle import mnpbem_ref as R
+    t = shapes.tables()
+    q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    v, f = shapes.fibsphere(faces, 50.0)
+    cp = R.ComParticle([R.EpsConst(1.77), R.drude_eps(*DRUDE)], [R.Particle(v, f, q)], [[2, 1]], [True])
+    vi, fi = shapes.trisphere(256, 2.0)
+    pw = R.PlaneWaveRet([1, 0, 0], [0, 0, 1], R.Particle(vi, fi, q))
+    return R, cp, pw
+
+
+def cpu_solve_one(R, bem, cp, pw, enei):
+    bem.enei = None
+    sig = bem.solve(pw.potential(cp, enei))
+    return pw.extinction(cp, sig), pw.scattering(cp, sig)
+
+
+def cpu_baseline(a, nsolves=1):
+    faces = a.cpu_faces or a.faces
+    R, cp, pw = cpu_problem(faces)
+    bem = R.BemRet(cp)              # set-up (refinement, sum rule) is not timed
+    t0 = time.perf_counter()
+    for i in range(nsolves):
+        cpu_solve_one(R, bem, cp, pw, float(grid()[(7 * i + 3) % NGRID]))
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count()
+    scale = (faces / a.faces) ** 3
+    return {"value": nsolves / dt * scale, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d wavelength-solve(s) of the NumPy/SciPy FP64 oracle at %d faces "
+                      "(initmat with explicit inverses + mldivide + ext + sca; set-up excluded), "
+                      "OpenBLAS on all %d host threads%s" % (
+                          nsolves, faces, cores,
+                          "" if faces == a.faces else ", scaled by (n/%d)^3" % a.faces),
+            "seconds": dt}
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return None
+    # warm-up: small solves (NumPy/BLAS thread pools, page-in)
+    R, cps, pws = cpu_problem(284)
+    bs = R.BemRet(cps)
+    for s in range(a.warmup):
+        cpu_solve_one(R, bs, cps, pws, 500.0)
+    faces = a.cpu_faces or a.faces
+    R, cp, pw = cpu_problem(faces)
+    bem = R.BemRet(cp)
+    times = []
+    for s in range(a.steps):
+        lam = float(step_wavelengths(s, 0, 1, 1)[0])
+        t0 = time.perf_counter()
+        cpu_solve_one(R, bem, cp, pw, lam)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.sum(times))
+    scale = (faces / a.faces) ** 3
+    value = a.steps / (ms / 1e3) * scale
+    cores = os.cpu_count()
+    sample = ("1 wavelength-solve per step of the NumPy/SciPy FP64 oracle (restatement of the "
+              "reference CPU path) at %d faces, OpenBLAS on all %d host threads%s"
+              % (faces, cores, "" if faces == a.faces else ", scaled by (n/%d)^3" % a.faces))
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload_desc(a), "faces": a.faces, "wavelengths_per_step": 1,
+                       "l2": "working set of dense n x n complex128 matrices > L2"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------------- main
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if a.impl == "reference":
+        line = run_reference(a, rank, world)
+        if line is not None:
+            print(json.dumps(line))
+        return
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    r = run_ours(a, rank, world, dist, torch)
+    fp64 = None
+    if rank == 0 and not a.skip_fp64:
+        fp64 = fp64_comparison(a, r["cp"], r["exc"], torch, r["bem"])
+    cpu = None
+    if rank == 0 and not a.skip_cpu:
+        cpu = cpu_baseline(a)
+    if dist is not None:
+        dist.barrier()
+    if rank == 0:
+        n = r["cp"].n
+        wset = (5 * 8 + 4 * 16) * n * n
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": r["ms"] / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
+                "config": {"workload": workload_desc(a), "faces": n, "wavelengths_per_step": a.batch,
+                           "precision": a.precision,
+                           "l2": "no flush: per-wavelength working set %.2f GB > 129 MB L2" % (wset / 1e9)},
+                "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],
+                "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64}
+        if fp64:
+            line["speedup_vs_fp64_gpu"] = r["value"] / fp64["value"]
+        line.update(r["extra"])
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/*
+ * mnpbem_gpu.h — C ABI of the GB300-native retarded BEM path of MNPBEM.
+ *
+ * The library replaces, behind MNPBEM's own calling surface, the MATLAB code of
+ *   bem = bemsolver(p, op)            (Base/bemsolver.m:18-27 -> BEM/@bemret/private/init.m:16-31
+ *                                      -> Greenfun/@compgreenret/private/init.m:5-31)
+ *   sig = bem \ exc(p, enei)          (BEM/@bemret/mldivide.m:12-49, private/initmat.m:5-74,
+ *                                      Simulation/retarded/@planewaveret/potential.m:13-57)
+ *   exc.ext(sig), exc.sca(sig)        (Simulation/retarded/@planewaveret/extinction.m:12-16,
+ *                                      scattering.m:13-19, @spectrumret/farfield.m:15-74)
+ * A MATLAB MEX gateway (the pattern of mex/hmatgreenret.cpp:21-61) or a Python
+ * ctypes harness calls these symbols.  Conventions:
+ *   - every function returns an mnpbem_status; nothing calls exit();
+ *     mnpbem_last_error() gives a message for the last failure on this thread;
+ *   - arrays are C order (row-major); complex numbers are interleaved
+ *     (re, im) doubles; face and vertex indices are 0-based; the 4th face
+ *     column is -1 for triangles (MNPBEM uses NaN there);
+ *   - the caller owns host buffers, the library owns device buffers and the
+ *     handle; one CUDA stream per handle; a handle is not shared across threads.
+ */
+#ifndef MNPBEM_GPU_H
+#define MNPBEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define MNPBEM_API __declspec(dllexport)
+#else
+#define MNPBEM_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mnpbem_status {
+  MNPBEM_OK = 0,
+  MNPBEM_ERR_INVALID_ARG = 1,
+  MNPBEM_ERR_CUDA = 2,
+  MNPBEM_ERR_OUT_OF_MEMORY = 3,
+  MNPBEM_ERR_SINGULAR = 4,      /* pivot guard of the block inversion tripped      */
+  MNPBEM_ERR_NOT_CONVERGED = 5, /* FP64 refinement did not reach its tolerance     */
+  MNPBEM_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up              */
+  MNPBEM_ERR_UNSUPPORTED = 7
+} mnpbem_status;
+
+typedef enum mnpbem_precision {
+  MNPBEM_FP64 = 0,  /* all assembly / inversion / products in FP64 (plain FP64 path)  */
+  MNPBEM_MIXED = 1, /* complex64 TF32 tensor-core inversion + FP64 refinement         */
+  MNPBEM_FP32 = 2   /* assembly output only: complex64 matrices                        */
+} mnpbem_precision;
+
+/* Quadrature rules carried by a particle (p.quad, Misc/integration/@quadface):
+ * the triangle rule (rule 18: 28 points, weights summing to 1) and the polar
+ * rules around the centroid for triangles (x3, y3, w3) and quadrilaterals
+ * (x4, y4, w4) (@quadface/private/init.m:25-80). */
+typedef struct mnpbem_quad {
+  int32_t n_tri;
+  const double *x, *y, *w;
+  int32_t n_pol3;
+  const double *x3, *y3, *w3;
+  int32_t n_pol4;
+  const double *x4, *y4, *w4;
+} mnpbem_quad;
+
+/* Options of the Green function (Misc/bemoptions.m:16-25). */
+typedef struct mnpbem_options {
+  double rel_cutoff; /* RelCutoff (3)                         */
+  double abs_cutoff; /* AbsCutoff (0)                         */
+  int32_t order;     /* order of the exp(ikr) expansion (5)   */
+  int32_t device;    /* CUDA device ordinal                   */
+} mnpbem_options;
+
+typedef struct mnpbem_geom mnpbem_geom;
+
+/* comparticle(eps, {p1..pnp}, inout, closed) + compgreenret(p, p, op):
+ * flat-face geometry (Particles/@particle/private/norm_flat.m:8-62), the
+ * refinement pattern (Greenfun/+green/refinematrix.m:28-68), the Taylor
+ * coefficients of the near elements (Greenfun/@greenret/private/init.m:42-177)
+ * and the closed-surface sum rule (Greenfun/@compgreenret/private/initclosed.m:19-89).
+ *   verts  [nverts][3];  faces [nfaces][4] (concatenated particles)
+ *   part_nfaces [nparts]: faces of each particle, in order
+ *   inout [nparts][2]: 1-based media (inside, outside)
+ *   closed [nparts]: 1 when particle i is a closed surface by itself           */
+MNPBEM_API mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts,
+                                 const int64_t* faces, int64_t nfaces,
+                                 int32_t nparts, const int64_t* part_nfaces,
+                                 const int32_t* inout, const int32_t* closed,
+                                 const mnpbem_quad* quad, const mnpbem_options* opts,
+                                 mnpbem_geom** out);
+MNPBEM_API mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g);
+
+/* Sizes: number of faces and of refined (near + self) elements. */
+MNPBEM_API mnpbem_status mnpbem_geom_size(const mnpbem_geom* g, int64_t* nfaces, int64_t* nref);
+
+/* Copy geometry and refinement data to host (any pointer may be NULL).
+ *   pos, nvec, tvec1, tvec2 [n][3]; area [n];
+ *   ref_row, ref_col [nref] in MATLAB's find() order (column-major);
+ *   ref_g [nref][order+1]; ref_f [nref][3][order+1]   (greenret obj.g, obj.f)   */
+MNPBEM_API mnpbem_status mnpbem_geom_export(const mnpbem_geom* g, double* pos, double* nvec,
+                                 double* tvec1, double* tvec2, double* area,
+                                 int64_t* ref_row, int64_t* ref_col, double* ref_g,
+                                 double* ref_f);
+
+/* compgreenret matrices of bemret (BEM/@bemret/private/initmat.m:27-31):
+ *   G1 = G{1,1} - G{2,1}, H1 = H1{1,1} - H1{2,1}, G2 = G{2,2} - G{1,2}, H2 = H2{2,2} - H2{1,2}
+ * for wavenumbers k_media [nmed] (complex, interleaved) of the media.
+ * precision MNPBEM_FP64 -> complex128 [n][n] outputs, MNPBEM_FP32 -> complex64.
+ * Outputs are host pointers (NULL to skip).                                     */
+MNPBEM_API mnpbem_status mnpbem_assemble(mnpbem_geom* g, const double* k_media, int32_t nmed,
+                              int32_t precision, void* G1, void* H1, void* G2, void* H2);
+
+/* Plane-wave excitation (planewaveret(pol, dir, op)) plus the unit sphere at
+ * infinity used for the scattering cross section (op.pinfty, default
+ * trisphere(256, 2); Simulation/retarded/@planewaveret/init.m:26-30). */
+typedef struct mnpbem_planewave {
+  int32_t npol;
+  const double* pol; /* [npol][3] */
+  const double* dir; /* [npol][3] */
+  int32_t medium;    /* 1-based excitation medium (default 1) */
+  int32_t ninf;
+  const double* inf_nvec; /* [ninf][3] outer normals of the sphere at infinity */
+  const double* inf_area; /* [ninf] */
+} mnpbem_planewave;
+
+/* Outputs of a wavelength sweep (NULL to skip any of them). */
+typedef struct mnpbem_solution {
+  double* ext;      /* [nenei][npol]  extinction cross section  */
+  double* sca;      /* [nenei][npol]  scattering cross section  */
+  double* sig1;     /* [nenei][n][npol]    complex  */
+  double* sig2;     /* [nenei][n][npol]    complex  */
+  double* h1;       /* [nenei][n][3][npol] complex  */
+  double* h2;       /* [nenei][n][3][npol] complex  */
+  int32_t* ir_iters;  /* [nenei] refinement iterations used (MIXED) */
+  double* ir_resid;   /* [nenei] final relative FP64 residual of the BEM equations */
+  int32_t outputs_on_device; /* 1: sig1/sig2/h1/h2/ext/sca are device pointers */
+} mnpbem_solution;
+
+/* Refinement control for MNPBEM_MIXED (ignored for FP64). */
+typedef struct mnpbem_refine {
+  int32_t max_iter; /* default 10 */
+  double tol;       /* stop when ||dx|| <= tol * ||x|| (default 1e-12) */
+} mnpbem_refine;
+
+/* Wavelength sweep: for each enei[w] (nm) with dielectric functions
+ * eps_media [nenei][nmed] (complex; eps of medium m at enei[w]):
+ * excitation (planewaveret/potential.m), bemret initmat + mldivide, and
+ * ext / sca.  precision: MNPBEM_FP64 or MNPBEM_MIXED.  refine may be NULL. */
+MNPBEM_API mnpbem_status mnpbem_solve(mnpbem_geom* g, const mnpbem_planewave* exc, int32_t nenei,
+                           const double* enei, const double* eps_media, int32_t nmed,
+                           int32_t precision, const mnpbem_refine* refine,
+                           mnpbem_solution* out);
+
+/* The matrices bemret stores per wavelength (initmat.m:27-72), copied to host
+ * as complex128 [n][n] (NULL to skip): G1i, G2i, Sigma1, Deltai, Sigmai.       */
+MNPBEM_API mnpbem_status mnpbem_bem_matrices(mnpbem_geom* g, double enei, const double* eps_media,
+                                  int32_t nmed, int32_t precision, double* G1i,
+                                  double* G2i, double* Sigma1, double* Deltai,
+                                  double* Sigmai);
+
+/* Per-phase accounting of the library's kernels on a handle (the tracing that
+ * the reference does with named timer maps, mex/hlib/hoptions.h:65-72, and
+ * BEM/@bemiter/tocout.m).  Phases: 0 assembly, 1 O(n^3) GEMMs, 2 thin/panel GEMMs,
+ * 3 pivot-block inversions, 4 element-wise kernels, 5 spectra, 6 geometry set-up.
+ * Launch counts are always kept; with profiling enabled each launch is also
+ * bracketed by CUDA events on the handle's stream (durations in ms) and the
+ * algorithmic FLOPs / bytes of the launches are accumulated.                */
+MNPBEM_API mnpbem_status mnpbem_profile_enable(mnpbem_geom* g, int32_t on);
+MNPBEM_API mnpbem_status mnpbem_profile_reset(mnpbem_geom* g);
+MNPBEM_API mnpbem_status mnpbem_profile_read(mnpbem_geom* g, int32_t phase, double* ms,
+                                             double* flops, double* bytes, int64_t* launches);
+
+/* Complex64 GEMM C = alpha A B + beta C on host buffers (row-major, interleaved
+ * complex, leading dimensions in elements): path 0 = CUDA-core kernel, path 1 =
+ * tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation).  The building
+ * block of the inversions and products of initmat.m (MATLAB mtimes on complex
+ * matrices); beta must be real for path 1.                                   */
+MNPBEM_API mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N,
+                                         int64_t K, const float* alpha, const float* A,
+                                         int64_t lda, const float* B, int64_t ldb,
+                                         const float* beta, float* C, int64_t ldc);
+
+/* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
+MNPBEM_API mnpbem_status mnpbem_geom_stream(const mnpbem_geom* g, void** stream);
+
+/* Message of the last failure on the calling thread ("" if none). */
+MNPBEM_API const char* mnpbem_last_error(void);
+
+/* Library version string. */
+MNPBEM_API const char* mnpbem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MNPBEM_GPU_H */

@@ -1,1 +1,14 @@
-"""GB300-native retarded BEM hot path of MNPBEM (compgreenret + bemret + planewave spectra)."""
+"""GB300-native retarded BEM hot path of MNPBEM.
+
+compgreenret assembly (G, F -> G1, H1, G2, H2 with near-field refinement),
+the bemret solve (Garcia de Abajo & Howie) and plane-wave extinction /
+scattering spectra run in ``libmnpbem_gpu.so`` (hand-written CUDA for
+sm_103a, C ABI in ``include/mnpbem_gpu.h``).  This package mirrors MNPBEM's
+MATLAB calling surface on top of that library.
+"""
+from .materials import EV2NM, epsconst, epsdrude, epsfun  # noqa: F401
+from .particles import comparticle, lglnodes, particle, quadface, trisphere  # noqa: F401
+from .bem import (bemoptions, bemret, bemsolver, compstruct, planewave,  # noqa: F401
+                  planewaveret, spectrumret)
+
+__version__ = "0.1.0"

@@ -1,0 +1,276 @@
+"""MNPBEM's calling surface for the retarded BEM path, backed by the GPU library.
+
+    op  = bemoptions(sim='ret', interp='flat')
+    p   = comparticle(epstab, [trisphere(256, 20)], [[2, 1]], 1, op=op)
+    bem = bemsolver(p, op)                   # Base/bemsolver.m -> bemret
+    exc = planewave([1, 0, 0], [0, 0, 1], op)
+    sig = bem.mldivide(exc(p, enei))         # sig = bem \\ exc(p, enei)
+    ext, sca = exc.ext(sig), exc.sca(sig)
+
+``bem.spectrum(exc, enei)`` runs a whole wavelength sweep in one library call.
+``op['precision']`` selects ``'mixed'`` (complex64 TF32 tensor-core inversion
+plus FP64 refinement, default) or ``'fp64'``.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .particles import comparticle, trisphere
+
+
+def bemoptions(op=None, **kw):
+    """Default options (Misc/bemoptions.m:16-25) updated by keyword pairs."""
+    base = {"sim": "ret", "waitbar": 0, "RelCutoff": 3, "order": 5, "interp": "flat"}
+    if op:
+        base.update(op)
+    base.update(kw)
+    return base
+
+
+class compstruct:
+    """Structure holding particle, wavelength and named fields (@compstruct)."""
+
+    def __init__(self, p, enei, **fields):
+        self.p, self.enei = p, enei
+        self.__dict__.update(fields)
+
+    def __repr__(self):
+        keys = [k for k in self.__dict__ if k not in ("p", "enei")]
+        return "compstruct(enei=%r, fields=%s)" % (self.enei, keys)
+
+
+class spectrumret:
+    """Unit sphere at infinity used for far fields (@spectrumret)."""
+
+    def __init__(self, pinfty=None, medium=1):
+        self.pinfty = pinfty if pinfty is not None else trisphere(256, 2)
+        self.medium = medium
+
+    @property
+    def nvec(self):
+        return np.ascontiguousarray(self.pinfty.nvec, dtype=np.float64)
+
+    @property
+    def area(self):
+        return np.ascontiguousarray(self.pinfty.area, dtype=np.float64)
+
+
+class planewaveret:
+    """Plane-wave excitation for the retarded solver (@planewaveret)."""
+
+    name = "planewave"
+    needs = [{"sim": "ret"}]
+
+    def __init__(self, pol, dir, op=None, medium=None, pinfty=None):
+        op = op or {}
+        self.pol = np.ascontiguousarray(np.atleast_2d(np.asarray(pol, dtype=np.float64)))
+        self.dir = np.ascontiguousarray(np.atleast_2d(np.asarray(dir, dtype=np.float64)))
+        if self.pol.shape != self.dir.shape or self.pol.shape[1] != 3:
+            raise ValueError("pol and dir must both be [npol, 3]")
+        if np.any(np.sum(self.pol * self.dir, 1) != 0):
+            raise ValueError("polarisation and propagation direction must be orthogonal")
+        self.medium = int(medium if medium is not None else op.get("medium", 1))
+        self.spec = spectrumret(pinfty if pinfty is not None else op.get("pinfty"), self.medium)
+
+    @property
+    def npol(self):
+        return self.pol.shape[0]
+
+    def __call__(self, p, enei):
+        """External potential for bemret at wavelength enei (potential.m)."""
+        return compstruct(p, float(enei), exc=self)
+
+    def _struct(self):
+        pw = _lib.PlaneWave()
+        pw.npol = self.npol
+        pw.pol = _lib.dptr(self.pol)
+        pw.dir = _lib.dptr(self.dir)
+        pw.medium = self.medium
+        self._nv, self._ar = self.spec.nvec, self.spec.area
+        pw.ninf = self._nv.shape[0]
+        pw.inf_nvec = _lib.dptr(self._nv)
+        pw.inf_area = _lib.dptr(self._ar)
+        return pw
+
+    def extinction(self, sig):
+        return sig.ext
+
+    def scattering(self, sig):
+        return sig.sca
+
+    ext = extinction
+    sca = scattering
+
+    def absorption(self, sig):
+        return sig.ext - sig.sca
+
+
+def planewave(pol, dir, op=None, **kw):
+    """Factory of Base/planewave.m for sim = 'ret'."""
+    op = bemoptions(op)
+    if op.get("sim", "ret") != "ret":
+        raise NotImplementedError("only the retarded plane-wave excitation is implemented")
+    return planewaveret(pol, dir, op, **kw)
+
+
+class bemret:
+    """Retarded BEM solver on one GPU (BEM/@bemret).
+
+    Construction builds the composite Green function on the GPU: geometry,
+    refinement pattern, Taylor coefficients of the near elements and the
+    closed-surface sum rule (compgreenret(p, p, op)).
+    """
+
+    name = "bemsolver"
+    needs = [{"sim": "ret"}]
+
+    def __init__(self, p, op=None):
+        if not isinstance(p, comparticle):
+            raise TypeError("bemret needs a comparticle")
+        self.p = p
+        self.op = bemoptions(op)
+        prec = self.op.get("precision", "mixed")
+        if prec not in ("mixed", "fp64"):
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        self.precision = _lib.MIXED if prec == "mixed" else _lib.FP64
+        self.refine_iters = int(self.op.get("refine_iters", 10))
+        self.refine_tol = float(self.op.get("refine_tol", 1e-12))
+        lib = _lib.load()
+        q = p.quad
+        self._quad_arrays = [np.ascontiguousarray(a, dtype=np.float64)
+                             for a in (q.x, q.y, q.w, q.x3, q.y3, q.w3, q.x4, q.y4, q.w4)]
+        qa = self._quad_arrays
+        quad = _lib.Quad(qa[0].size, _lib.dptr(qa[0]), _lib.dptr(qa[1]), _lib.dptr(qa[2]),
+                         qa[3].size, _lib.dptr(qa[3]), _lib.dptr(qa[4]), _lib.dptr(qa[5]),
+                         qa[6].size, _lib.dptr(qa[6]), _lib.dptr(qa[7]), _lib.dptr(qa[8]))
+        opts = _lib.Options(float(self.op.get("RelCutoff", 3)), float(self.op.get("AbsCutoff", 0)),
+                            int(self.op.get("order", 5)), int(self.op.get("device", 0)))
+        part_n = np.ascontiguousarray([q.n for q in p.p], dtype=np.int64)
+        inout = np.ascontiguousarray(p.inout, dtype=np.int32)
+        closed = np.ascontiguousarray(p.closed, dtype=np.int32)
+        h = ctypes.c_void_p()
+        _lib.check(lib.mnpbem_geom_create(
+            _lib.dptr(p.verts), p.verts.shape[0], p.faces.ctypes.data_as(_lib.c_int64_p), p.n,
+            len(p.p), part_n.ctypes.data_as(_lib.c_int64_p), inout.ctypes.data_as(_lib.c_int32_p),
+            closed.ctypes.data_as(_lib.c_int32_p), ctypes.byref(quad), ctypes.byref(opts),
+            ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.mnpbem_geom_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ----------------------------------------------------------- queries
+    @property
+    def handle(self):
+        return self._h
+
+    def sizes(self):
+        n, nref = ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self._lib.mnpbem_geom_size(self._h, ctypes.byref(n), ctypes.byref(nref)))
+        return n.value, nref.value
+
+    def refinement(self):
+        """Geometry and greenret refinement data (pos, nvec, ..., ind, g, f)."""
+        n, nref = self.sizes()
+        O = int(self.op.get("order", 5))
+        out = {k: np.zeros((n, 3)) for k in ("pos", "nvec", "tvec1", "tvec2")}
+        out["area"] = np.zeros(n)
+        out["row"] = np.zeros(nref, dtype=np.int64)
+        out["col"] = np.zeros(nref, dtype=np.int64)
+        out["g"] = np.zeros((nref, O + 1))
+        out["f"] = np.zeros((nref, 3, O + 1))
+        _lib.check(self._lib.mnpbem_geom_export(
+            self._h, *[_lib.vptr(out[k]) for k in ("pos", "nvec", "tvec1", "tvec2", "area", "row",
+                                                   "col", "g", "f")]))
+        return out
+
+    def _eps(self, enei):
+        em = np.ascontiguousarray(self.p.eps_media(enei), dtype=np.complex128)
+        return em
+
+    def matrices(self, enei, precision="fp64"):
+        """G1, H1, G2, H2 of initmat.m:27-31 at wavelength enei (host arrays)."""
+        em = self._eps(enei)[0]
+        k = np.ascontiguousarray(2 * np.pi / enei * np.sqrt(em))
+        n = self.p.n
+        dt = np.complex128 if precision == "fp64" else np.complex64
+        mats = [np.zeros((n, n), dtype=dt) for _ in range(4)]
+        _lib.check(self._lib.mnpbem_assemble(self._h, k.view(np.float64).ctypes.data_as(_lib.c_double_p),
+                                             k.size, _lib.FP64 if precision == "fp64" else _lib.FP32,
+                                             *[_lib.vptr(m) for m in mats]))
+        return tuple(mats)
+
+    def bem_matrices(self, enei, precision=None):
+        """G1i, G2i, Sigma1, Deltai, Sigmai (initmat.m:27-72) as complex128."""
+        prec = self.precision if precision is None else (_lib.MIXED if precision == "mixed" else _lib.FP64)
+        em = np.ascontiguousarray(self._eps(enei)[0])
+        n = self.p.n
+        mats = [np.zeros((n, n), dtype=np.complex128) for _ in range(5)]
+        _lib.check(self._lib.mnpbem_bem_matrices(self._h, float(enei),
+                                                 em.view(np.float64).ctypes.data_as(_lib.c_double_p),
+                                                 em.size, prec, *[_lib.vptr(m) for m in mats]))
+        return dict(zip(("G1i", "G2i", "Sigma1", "Deltai", "Sigmai"), mats))
+
+    # ------------------------------------------------------------- solves
+    def spectrum(self, exc, enei, fields=False, out=None):
+        """Wavelength sweep: returns dict with ext, sca [nenei, npol] (+ fields).
+
+        ``out`` may supply preallocated (e.g. pinned) C-contiguous host arrays
+        for any of ext, sca, sig1, sig2, h1, h2 with the shapes below.
+        """
+        enei = np.ascontiguousarray(np.atleast_1d(np.asarray(enei, dtype=np.float64)))
+        nw, P, n = enei.size, exc.npol, self.p.n
+        em = np.ascontiguousarray(self._eps(enei))
+        pw = exc._struct()
+        shapes_ = {"ext": ((nw, P), np.float64), "sca": ((nw, P), np.float64),
+                   "sig1": ((nw, n, P), np.complex128), "sig2": ((nw, n, P), np.complex128),
+                   "h1": ((nw, n, 3, P), np.complex128), "h2": ((nw, n, 3, P), np.complex128)}
+        given = out or {}
+        out = {"ir_iters": np.zeros(nw, dtype=np.int32), "ir_resid": np.zeros(nw)}
+        for key, (shp, dt) in shapes_.items():
+            if key in ("sig1", "sig2", "h1", "h2") and not fields:
+                continue
+            if key in given:
+                arr = given[key]
+                if arr.shape != shp or arr.dtype != dt or not arr.flags["C_CONTIGUOUS"]:
+                    raise ValueError("out[%r] must be a C-contiguous %s array of shape %s" % (key, dt, shp))
+                out[key] = arr
+            else:
+                out[key] = np.zeros(shp, dtype=dt)
+        sol = _lib.Solution()
+        for key in ("ext", "sca", "sig1", "sig2", "h1", "h2", "ir_iters", "ir_resid"):
+            if key in out:
+                setattr(sol, key, out[key].ctypes.data)
+        sol.outputs_on_device = 0
+        ref = _lib.Refine(self.refine_iters, self.refine_tol)
+        _lib.check(self._lib.mnpbem_solve(self._h, ctypes.byref(pw), nw, _lib.dptr(enei),
+                                          em.view(np.float64).ctypes.data_as(_lib.c_double_p),
+                                          em.shape[1], self.precision, ctypes.byref(ref),
+                                          ctypes.byref(sol)))
+        return out
+
+    def mldivide(self, exc):
+        """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m)."""
+        pw = exc.exc
+        r = self.spectrum(pw, exc.enei, fields=True)
+        return compstruct(self.p, exc.enei, sig1=r["sig1"][0], sig2=r["sig2"][0], h1=r["h1"][0],
+                          h2=r["h2"][0], ext=r["ext"][0], sca=r["sca"][0],
+                          ir_iters=int(r["ir_iters"][0]), ir_resid=float(r["ir_resid"][0]))
+
+    solve = mldivide
+
+
+def bemsolver(p, op=None, **kw):
+    """Factory of Base/bemsolver.m: picks the solver class whose needs match op."""
+    op = bemoptions(op, **kw)
+    if op.get("sim", "ret") != "ret":
+        raise NotImplementedError("only the retarded solver (sim='ret') is implemented")
+    return bemret(p, op)

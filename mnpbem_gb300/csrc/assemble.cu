@@ -1,0 +1,167 @@
+// Per-wavelength assembly of the bemret matrices (compgreenret eval, FP64 math).
+//
+//  k_asm_far   Greenfun/@greenret/private/eval1.m:24-40 (G) and :110-124 (F, 'cart'),
+//              H1/H2 = F +- 2 pi [d == 0] (:141-143), combined per particle block as in
+//              Greenfun/@compgreenret/private/eval1.m:16-34 and BEM/@bemret/private/initmat.m:27-31
+//  k_asm_near  the refined elements: G = sum_o g_o (ik)^o, F = sum_o (n_i . f_o) (ik)^o,
+//              both times exp(ik d) (eval1.m:36-39, 119-123)
+//
+// One pass writes G1, H1, G2, H2 as complex128 and/or complex64 (row-major, ld).
+#include "assemble.cuh"
+#include "profile.cuh"
+
+namespace mnpbem {
+
+struct PairVal { double2 G, F; };
+
+// G and F of one pair for wavenumber k (far-field formula)
+__device__ __forceinline__ PairVal far_pair(double2 k, double dd, double in, double area) {
+  double s, c;
+  sincos(k.x * dd, &s, &c);
+  double e = exp(-k.y * dd);
+  double2 ph = make_double2(e * c, e * s);
+  double ga = area / dd;
+  PairVal v;
+  v.G = make_double2(ga * ph.x, ga * ph.y);
+  // (ik - 1/d) / d^2 * (n . r) * area
+  double inv = 1.0 / dd;
+  double2 t = make_double2((-k.y - inv) * inv * inv, k.x * inv * inv);
+  double fa = in * area;
+  double2 tf = make_double2(t.x * fa, t.y * fa);
+  v.F = cmul(tf, ph);
+  return v;
+}
+
+template <bool W64, bool W32>
+__device__ __forceinline__ void store4(const AsmParams& p, int64_t i, int64_t j, double2 g1, double2 h1,
+                                       double2 g2, double2 h2) {
+  if (W64) {
+    int64_t o = i * p.ld64 + j;
+    if (p.G1) p.G1[o] = g1;
+    if (p.H1) p.H1[o] = h1;
+    if (p.G2) p.G2[o] = g2;
+    if (p.H2) p.H2[o] = h2;
+  }
+  if (W32) {
+    int64_t o = i * p.ld32 + j;
+    if (p.g1) p.g1[o] = to_f(g1);
+    if (p.h1) p.h1[o] = to_f(h1);
+    if (p.g2) p.g2[o] = to_f(g2);
+    if (p.h2) p.h2[o] = to_f(h2);
+  }
+}
+
+constexpr int ASM_COLS = 128;
+constexpr int ASM_ROWS = 4;
+
+template <bool W64, bool W32>
+__global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
+  int64_t j = (int64_t)blockIdx.x * ASM_COLS + threadIdx.x;
+  int64_t i0 = (int64_t)blockIdx.y * ASM_ROWS;
+  if (j >= p.n) return;
+  double4_32a sj = p.src[j];
+  int pj = p.part[j];
+  const double twopi = 2.0 * M_PI;
+#pragma unroll
+  for (int r = 0; r < ASM_ROWS; ++r) {
+    int64_t i = i0 + r;
+    if (i >= p.n) break;
+    double4_32a si = p.src[i];
+    double4_32a ni = p.nrm[i];
+    double x = si.x - sj.x, y = si.y - sj.y, z = si.z - sj.z;
+    double dist = sqrt(x * x + y * y + z * z);
+    double dd = fmax(dist, DBL_EPS_ASM);
+    double delta = (dd == DBL_EPS_ASM) ? twopi : 0.0;
+    double in = x * ni.x + y * ni.y + z * ni.z;
+    int pi = p.part[i];
+    int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
+    double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
+    if (m11) { PairVal v = far_pair(p.k[m11 - 1], dd, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
+    if (m21) { PairVal v = far_pair(p.k[m21 - 1], dd, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
+    if (m22) { PairVal v = far_pair(p.k[m22 - 1], dd, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
+    if (m12) { PairVal v = far_pair(p.k[m12 - 1], dd, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
+    store4<W64, W32>(p, i, j, g1, h1, g2, h2);
+  }
+}
+
+// refined value for wavenumber k
+__device__ __forceinline__ PairVal near_pair(const AsmParams& p, int64_t e, double2 k, double dd,
+                                             double3 ni) {
+  const int O = p.order;
+  const double* g = p.ref_g + e * (O + 1);
+  const double* f = p.ref_f + e * 3 * (O + 1);
+  double2 ik = make_double2(-k.y, k.x);
+  double2 pw = make_double2(1.0, 0.0);
+  double2 G = make_double2(0, 0), F = make_double2(0, 0);
+  for (int o = 0; o <= O; ++o) {
+    double fo = ni.x * f[o] + ni.y * f[(O + 1) + o] + ni.z * f[2 * (O + 1) + o];
+    G.x += g[o] * pw.x; G.y += g[o] * pw.y;
+    F.x += fo * pw.x; F.y += fo * pw.y;
+    pw = cmul(pw, ik);
+  }
+  double s, c;
+  sincos(k.x * dd, &s, &c);
+  double ee = exp(-k.y * dd);
+  double2 ph = make_double2(ee * c, ee * s);
+  PairVal v;
+  v.G = cmul(G, ph);
+  v.F = cmul(F, ph);
+  return v;
+}
+
+template <bool W64, bool W32>
+__global__ void k_asm_near(AsmParams p) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.nref) return;
+  int i = p.ref_row[e], j = p.ref_col[e];
+  double4_32a si = p.src[i], sj = p.src[j];
+  double4_32a nn = p.nrm[i];
+  double3 ni = make_double3(nn.x, nn.y, nn.z);
+  double x = si.x - sj.x, y = si.y - sj.y, z = si.z - sj.z;
+  double dist = sqrt(x * x + y * y + z * z);
+  double dd = fmax(dist, DBL_EPS_ASM);
+  double delta = (dd == DBL_EPS_ASM) ? 2.0 * M_PI : 0.0;
+  int pi = p.part[i], pj = p.part[j];
+  int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
+  double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
+  if (m11) { PairVal v = near_pair(p, e, p.k[m11 - 1], dd, ni); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
+  if (m21) { PairVal v = near_pair(p, e, p.k[m21 - 1], dd, ni); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
+  if (m22) { PairVal v = near_pair(p, e, p.k[m22 - 1], dd, ni); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
+  if (m12) { PairVal v = near_pair(p, e, p.k[m12 - 1], dd, ni); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
+  store4<W64, W32>(p, i, j, g1, h1, g2, h2);
+}
+
+__global__ void k_pack_src(int n, const double* pos, const double* area, const double* nvec,
+                           double4_32a* src, double4_32a* nrm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  src[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], area[i]);
+  nrm[i] = make_double4_32a(nvec[3 * i], nvec[3 * i + 1], nvec[3 * i + 2], 0.0);
+}
+
+void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
+                  double4_32a* nrm, cudaStream_t st) {
+  k_pack_src<<<(n + 255) / 256, 256, 0, st>>>(n, pos, area, nvec, src, nrm);
+}
+
+mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st) {
+  // algorithmic bytes: the four n x n outputs written once per precision
+  const double nn = (double)p.n * p.n;
+  ProfScope ps(PH_ASSEMBLE, st, 0.0, nn * 4.0 * ((w64 ? 16.0 : 0.0) + (w32 ? 8.0 : 0.0)),
+               p.nref > 0 ? 2 : 1);
+  dim3 grid((unsigned)cdiv_up(p.n, ASM_COLS), (unsigned)cdiv_up(p.n, ASM_ROWS));
+  if (w64 && w32) k_asm_far<true, true><<<grid, ASM_COLS, 0, st>>>(p);
+  else if (w64) k_asm_far<true, false><<<grid, ASM_COLS, 0, st>>>(p);
+  else k_asm_far<false, true><<<grid, ASM_COLS, 0, st>>>(p);
+  MNP_CHECK_LAUNCH();
+  if (p.nref > 0) {
+    unsigned nb = (unsigned)cdiv_up(p.nref, 128);
+    if (w64 && w32) k_asm_near<true, true><<<nb, 128, 0, st>>>(p);
+    else if (w64) k_asm_near<true, false><<<nb, 128, 0, st>>>(p);
+    else k_asm_near<false, true><<<nb, 128, 0, st>>>(p);
+    MNP_CHECK_LAUNCH();
+  }
+  return MNPBEM_OK;
+}
+
+}  // namespace mnpbem

@@ -1,0 +1,34 @@
+#pragma once
+#include "common.cuh"
+
+namespace mnpbem {
+
+constexpr int ASM_MAXP = 16;    // particles per composite
+constexpr int ASM_MAXMED = 16;  // media
+constexpr double DBL_EPS_ASM = 2.220446049250313e-16;
+
+struct AsmParams {
+  int64_t n = 0;
+  int64_t nref = 0;
+  int order = 5;
+  int64_t ld64 = 0, ld32 = 0;
+  const int* part = nullptr;      // [n] particle index of each face
+  const double4_32a* src = nullptr;   // [n] (x, y, z, area)
+  const double4_32a* nrm = nullptr;   // [n] (nx, ny, nz, 0)
+  const int* ref_row = nullptr;
+  const int* ref_col = nullptr;
+  const double* ref_g = nullptr;
+  const double* ref_f = nullptr;
+  double2 k[ASM_MAXMED];
+  // media (1-based, 0 = block not connected) of the four connectivity
+  // blocks: 0 -> con{1,1} (+G1), 1 -> con{2,1} (-G1), 2 -> con{2,2} (+G2), 3 -> con{1,2} (-G2)
+  signed char med[4][ASM_MAXP][ASM_MAXP];
+  double2 *G1 = nullptr, *H1 = nullptr, *G2 = nullptr, *H2 = nullptr;  // complex128 outputs
+  float2 *g1 = nullptr, *h1 = nullptr, *g2 = nullptr, *h2 = nullptr;   // complex64 outputs
+};
+
+void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
+                  double4_32a* nrm, cudaStream_t st);
+mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st);
+
+}  // namespace mnpbem

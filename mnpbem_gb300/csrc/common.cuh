@@ -1,0 +1,114 @@
+// Shared device/host helpers for the MNPBEM retarded-BEM GPU library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/mnpbem_gpu.h"
+
+namespace mnpbem {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+const char* get_error();
+
+#define MNP_CUDA(call)                                                         \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::mnpbem::set_error("%s:%d CUDA error %s: %s", __FILE__, __LINE__,       \
+                          cudaGetErrorName(e_), cudaGetErrorString(e_));       \
+      return MNPBEM_ERR_CUDA;                                                  \
+    }                                                                          \
+  } while (0)
+
+#define MNP_CHECK_LAUNCH() MNP_CUDA(cudaGetLastError())
+
+#define MNP_TRY(expr)                                                          \
+  do {                                                                         \
+    mnpbem_status s_ = (expr);                                                 \
+    if (s_ != MNPBEM_OK) return s_;                                            \
+  } while (0)
+
+// ------------------------------------------------------------ complex math
+template <typename R> struct cplx_t;
+template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<double> { using type = double2; };
+template <typename R> using cplx = typename cplx_t<R>::type;
+
+template <typename R> __host__ __device__ __forceinline__ cplx<R> mk(R x, R y) {
+  cplx<R> c; c.x = x; c.y = y; return c;
+}
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) {
+  C c; c.x = a.x + b.x; c.y = a.y + b.y; return c;
+}
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) {
+  C c; c.x = a.x - b.x; c.y = a.y - b.y; return c;
+}
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  C c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c;
+}
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) {
+  C c; c.x = a.x * s; c.y = a.y * s; return c;
+}
+// c += a * b
+template <typename C> __host__ __device__ __forceinline__ void cfma(C& c, C a, C b) {
+  c.x = fma(a.x, b.x, c.x); c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y); c.y = fma(a.y, b.x, c.y);
+}
+template <typename C> __host__ __device__ __forceinline__ C cdiv(C a, C b) {
+  // Smith's algorithm
+  C c;
+  if (fabs(b.x) >= fabs(b.y)) {
+    auto r = b.y / b.x; auto den = b.x + b.y * r;
+    c.x = (a.x + a.y * r) / den; c.y = (a.y - a.x * r) / den;
+  } else {
+    auto r = b.x / b.y; auto den = b.x * r + b.y;
+    c.x = (a.x * r + a.y) / den; c.y = (a.y * r - a.x) / den;
+  }
+  return c;
+}
+template <typename C> __host__ __device__ __forceinline__ double cabs2(C a) {
+  return (double)a.x * a.x + (double)a.y * a.y;
+}
+
+__host__ __device__ __forceinline__ float2 to_f(double2 a) { return make_float2((float)a.x, (float)a.y); }
+__host__ __device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
+__host__ __device__ __forceinline__ double2 to_d(double2 a) { return a; }
+template <typename C> __host__ __device__ __forceinline__ C from_d(double2 a);
+template <> __host__ __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
+template <> __host__ __device__ __forceinline__ float2 from_d<float2>(double2 a) { return to_f(a); }
+
+inline int64_t cdiv_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline int64_t round_up(int64_t a, int64_t b) { return cdiv_up(a, b) * b; }
+
+// ------------------------------------------------------- device buffers
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr; bytes = 0;
+  }
+  mnpbem_status ensure(size_t nbytes) {
+    if (bytes >= nbytes && ptr) return MNPBEM_OK;
+    release();
+    if (nbytes == 0) return MNPBEM_OK;
+    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc of %zu bytes failed: %s", nbytes, cudaGetErrorString(e));
+      ptr = nullptr;
+      return MNPBEM_ERR_OUT_OF_MEMORY;
+    }
+    bytes = nbytes;
+    return MNPBEM_OK;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(ptr); }
+};
+
+}  // namespace mnpbem

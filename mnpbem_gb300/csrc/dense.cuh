@@ -1,0 +1,32 @@
+// Dense complex linear algebra on the device (row-major, interleaved complex).
+#pragma once
+#include "common.cuh"
+
+namespace mnpbem {
+
+// C = alpha * A[M x K] * B[K x N] + beta * C      (SIMT CUDA-core kernel)
+template <typename R>
+mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cplx<R>* A,
+                        int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta, cplx<R>* C,
+                        int64_t ldc, cudaStream_t st);
+
+// Workspace for in-place inversion of an n x n matrix by blocked Gauss-Jordan
+// elimination without row interchanges.
+template <typename R>
+struct GJWork {
+  DevBuf ccol, rrow, ncol, xblk, status, tf32;
+  int64_t n = 0;
+  int nb = 64;
+};
+
+// A <- inv(A) in place.  Returns MNPBEM_ERR_SINGULAR if a pivot guard trips.
+// gemm_fn performs the rank-nb trailing updates (SIMT or tensor-core).
+template <typename R>
+using GemmFn = mnpbem_status (*)(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cplx<R>* A,
+                                 int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta,
+                                 cplx<R>* C, int64_t ldc, cudaStream_t st, void* ctx);
+template <typename R>
+mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn<R> big_gemm,
+                        void* ctx, cudaStream_t st);
+
+}  // namespace mnpbem

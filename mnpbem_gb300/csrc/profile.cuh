@@ -1,0 +1,89 @@
+// Per-phase accounting of the library's kernels: launch counts (always) and,
+// when enabled, CUDA-event durations plus the algorithmic FLOPs / bytes that
+// each launch processes.  Events are recorded on the launching stream.
+#pragma once
+#include <vector>
+#include "common.cuh"
+
+namespace mnpbem {
+
+enum Phase {
+  PH_ASSEMBLE = 0,  // k_asm_far + k_asm_near
+  PH_GEMM_BIG,      // O(n^3) complex GEMMs (Gauss-Jordan trailing updates, Sigma products)
+  PH_GEMM_SMALL,    // panel GEMMs of the block inversion and the thin GEMMs of the chain / residual
+  PH_BLOCKINV,      // shared-memory pivot-block inversions
+  PH_ELEMWISE,      // Sigma stage, chain steps, conversions, excitation
+  PH_SPECTRA,       // far fields + cross sections
+  PH_GEOMETRY,      // one-time geometry / refinement set-up
+  PH_COUNT
+};
+
+struct PhaseAcc {
+  double ms = 0, flops = 0, bytes = 0;
+  int64_t launches = 0;
+};
+
+struct Profiler {
+  bool enabled = false;
+  PhaseAcc acc[PH_COUNT];
+  struct Pending { cudaEvent_t a, b; int ph; double flops, bytes; int64_t launches; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+
+  cudaEvent_t get_event() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void flush() {
+    for (auto& p : pending) {
+      float ms = 0;
+      if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+        acc[p.ph].ms += ms;
+      pool.push_back(p.a);
+      pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+  void reset() {
+    flush();
+    for (auto& a : acc) a = PhaseAcc();
+  }
+  ~Profiler() {
+    flush();
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// the profiler of the handle that the current API call works on
+Profiler*& current_profiler();
+
+struct ProfScope {
+  Profiler* p;
+  cudaStream_t st;
+  int ph;
+  double flops, bytes;
+  int64_t launches;
+  cudaEvent_t a = nullptr;
+  ProfScope(int phase, cudaStream_t s, double fl = 0, double by = 0, int64_t nl = 1)
+      : p(current_profiler()), st(s), ph(phase), flops(fl), bytes(by), launches(nl) {
+    if (p && p->enabled) {
+      a = p->get_event();
+      cudaEventRecord(a, st);
+    }
+  }
+  ~ProfScope() {
+    if (!p) return;
+    p->acc[ph].launches += launches;
+    p->acc[ph].flops += flops;
+    p->acc[ph].bytes += bytes;
+    if (p->enabled && a) {
+      cudaEvent_t b = p->get_event();
+      cudaEventRecord(b, st);
+      p->pending.push_back({a, b, ph, 0, 0, 0});
+    }
+  }
+};
+
+}  // namespace mnpbem

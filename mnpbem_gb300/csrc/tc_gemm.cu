@@ -1,0 +1,382 @@
+// Complex64 GEMM on the 5th-generation tensor cores: tcgen05.mma kind::tf32
+// with operands staged by TMA (cp.async.bulk.tensor) into 128-byte-swizzled
+// shared memory, the accumulator in tensor memory, and an mbarrier pipeline.
+//
+// A complex product C = alpha A B + beta C (row-major, interleaved complex)
+// is one real GEMM on the interleaved view:
+//     C_r[M][2N] = A_r[M][2K] * B'[2N][2K]^T (+ beta C_r)
+// A_r is the complex64 matrix A read as floats (K-major, no copy).  B' is built
+// from alpha * B by k_expand_b (O(K N) work):
+//     B'[2j  ][2l] =  Re b_lj   B'[2j  ][2l+1] = -Im b_lj
+//     B'[2j+1][2l] =  Im b_lj   B'[2j+1][2l+1] =  Re b_lj
+// so that C_r[i][2j] = sum_l (Re a Re b - Im a Im b) and
+// C_r[i][2j+1] = sum_l (Re a Im b + Im a Re b).  B' is rounded to TF32.
+//
+// Tile: 128 x 256 real outputs per CTA, K chunks of 32 floats (one 128-byte
+// swizzle row), 4 pipeline stages (48 KB each).  Warp 0 / lane 0 issues TMA,
+// warp 1 / lane 0 issues the MMAs, all four warps run the epilogue from TMEM.
+// Every mbarrier wait is bounded by a wall-clock limit; on expiry the kernel
+// records an error code, waits (bounded) for its own copies in flight, frees
+// its tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "profile.cuh"
+#include "tc_gemm.cuh"
+
+namespace mnpbem {
+
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32, TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;   // 16 KB
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;   // 32 KB
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024;
+constexpr uint32_t TC_TMEM_COLS = 256;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
+
+// instruction descriptor: D f32, A/B tf32, K-major A and B, N = 256, M = 128
+constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+                              ((uint32_t)(TC_BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false (and err |= code) when the limit expires
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (gtimer() - t0 > TC_WAIT_NS) {
+      atomicOr(err, code);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(dst), "l"((unsigned long long)map), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused with one swizzle atom along K)
+  d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+      "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// C_r[M][N2] = A_r[M][K2] * B'[N2][K2]^T + beta * C_r        (all row-major floats)
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M,
+              int N2, int K2, float* __restrict__ C, int64_t ldc, float beta, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[2 * TC_STAGES + 1];
+  __shared__ uint32_t tmem_slot;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+  const int KT = (K2 + TC_BK - 1) / TC_BK;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[TC_STAGES]),
+                 done = smem_u32(&bars[2 * TC_STAGES]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    for (int kt = 0; kt < KT; ++kt) {
+      const int s = kt % TC_STAGES;
+      if (kt >= TC_STAGES && !mbar_wait(empty0 + 8 * s, ((kt / TC_STAGES) - 1) & 1, err, 1)) break;
+      if (*(volatile int*)err) break;
+      const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
+      mbar_expect_tx(full0 + 8 * s, TC_STAGE_BYTES);
+      tma_load_2d(sa, &mapA, full0 + 8 * s, kt * TC_BK, m0);
+      tma_load_2d(sb, &mapB, full0 + 8 * s, kt * TC_BK, n0);
+      ++issued;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    bool ok = true;
+    for (int kt = 0; kt < KT && ok; ++kt) {
+      const int s = kt % TC_STAGES;
+      ok = mbar_wait(full0 + 8 * s, (kt / TC_STAGES) & 1, err, 2);
+      if (!ok) break;
+      tc_fence_after();
+      const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
+      const uint64_t da = desc_sw128(sa), db = desc_sw128(sb);
+#pragma unroll
+      for (int kk = 0; kk < TC_BK / 8; ++kk) {
+        // advance 8 tf32 = 32 bytes along K inside the swizzle row
+        mma_tf32(tmem, da + 2 * kk, db + 2 * kk, TC_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
+      }
+      mma_commit(empty0 + 8 * s);
+    }
+    if (ok) mma_commit(done);
+  }
+  __syncwarp();
+  // ---------------- epilogue: TMEM -> registers -> C
+  // (tcgen05.ld is warp-collective: keep the decision warp-uniform)
+  const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, err, 4) ? 1 : 0) != 0;
+  __syncwarp();
+  tc_fence_after();
+  if (ok) {
+    const int row = m0 + warp * 32 + lane;
+    const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+    for (int c = 0; c < TC_BN / 32; ++c) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+      const int col0 = n0 + c * 32;
+      if (row >= M || col0 >= N2) continue;
+      float* crow = C + (int64_t)row * ldc + col0;
+      if (vec && col0 + 32 <= N2) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          float4 v = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                 __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+          float4* dst = reinterpret_cast<float4*>(crow) + q;
+          if (beta != 0.0f) {
+            float4 o = *dst;
+            v.x += beta * o.x; v.y += beta * o.y; v.z += beta * o.z; v.w += beta * o.w;
+          }
+          *dst = v;
+        }
+      } else {
+        for (int q = 0; q < 32 && col0 + q < N2; ++q) {
+          float v = __uint_as_float(r[q]);
+          if (beta != 0.0f) v += beta * crow[q];
+          crow[q] = v;
+        }
+      }
+    }
+  }
+  // ---------------- drain copies still in flight after an error, free TMEM
+  if (warp == 0 && lane == 0 && *(volatile int*)err) {
+    for (int kt = 0; kt < issued; ++kt) {
+      const int s = kt % TC_STAGES;
+      mbar_wait(full0 + 8 * s, (kt / TC_STAGES) & 1, err, 8);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+// B'[2N][K2p] from alpha * B (B: K x N complex, row-major ldb), tf32-rounded,
+// zero-padded for 2K <= k < K2p.
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+__global__ void k_expand_b(int K, int N, float2 alpha, const float2* __restrict__ B, int64_t ldb, float* __restrict__ Bp,
+                           int K2p) {
+  __shared__ float2 tile[32][33];
+  const int l0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    int l = l0 + r, j = j0 + tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (l < K && j < N) {
+      float2 b = B[(int64_t)l * ldb + j];
+      v = make_float2(alpha.x * b.x - alpha.y * b.y, alpha.x * b.y + alpha.y * b.x);
+    }
+    tile[r][tx] = v;
+  }
+  __syncthreads();
+  // write: rows 2j, 2j+1; columns 2l, 2l+1 (coalesced along l)
+  for (int r = ty; r < 32; r += 8) {
+    int j = j0 + r, l = l0 + tx;
+    if (j >= N) continue;
+    float2 v = tile[tx][r];
+    float re = to_tf32(v.x), im = to_tf32(v.y);
+    if (l < K) {
+      float2* r0 = reinterpret_cast<float2*>(Bp + (int64_t)(2 * j) * K2p) + l;
+      float2* r1 = reinterpret_cast<float2*>(Bp + (int64_t)(2 * j + 1) * K2p) + l;
+      *r0 = make_float2(re, -im);
+      *r1 = make_float2(im, re);
+    } else if (2 * l < K2p) {
+      float2* r0 = reinterpret_cast<float2*>(Bp + (int64_t)(2 * j) * K2p) + l;
+      float2* r1 = reinterpret_cast<float2*>(Bp + (int64_t)(2 * j + 1) * K2p) + l;
+      *r0 = make_float2(0.f, 0.f);
+      *r1 = make_float2(0.f, 0.f);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode(TcGemmCtx& c) {
+  if (!c.encode_fn) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      c.encode_fn = fn;
+    else
+      cudaGetLastError();
+  }
+  return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(c.encode_fn);
+}
+
+static bool make_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, const void* ptr, uint64_t inner,
+                     uint64_t rows, uint64_t row_bytes, uint32_t box_rows) {
+  cuuint64_t dims[2] = {inner, rows};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {(cuuint32_t)TC_BK, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K) {
+  if (!c.checked) {
+    c.checked = true;
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    c.usable = (major == 10 && minor == 3) && get_encode(c) != nullptr &&
+               cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) == cudaSuccess;
+    if (!c.usable) cudaGetLastError();
+  }
+  if (!c.usable || !c.enabled) return false;
+  return M >= 128 && N >= 64 && K >= 16 && M < (1 << 30) && 2 * N < (1 << 30) && 2 * K < (1 << 30);
+}
+
+mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
+                          int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc,
+                          cudaStream_t st) {
+  if (beta.y != 0.0f || (lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||
+      (reinterpret_cast<uintptr_t>(C) & 15)) {
+    set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base or complex beta)");
+    return MNPBEM_ERR_UNSUPPORTED;
+  }
+  const int64_t K2 = 2 * K, N2 = 2 * N;
+  const int64_t K2p = round_up(K2, TC_BK);
+  MNP_TRY(c.bexp.ensure(sizeof(float) * N2 * K2p));
+  MNP_TRY(c.err.ensure(sizeof(int)));
+  float* Bp = c.bexp.as<float>();
+  {
+    ProfScope ps(PH_ELEMWISE, st, 0.0, 8.0 * K * N + 16.0 * K * N);
+    dim3 g((unsigned)cdiv_up(N, 32), (unsigned)cdiv_up(K2p / 2, 32));
+    k_expand_b<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p);
+    MNP_CHECK_LAUNCH();
+  }
+  auto enc = get_encode(c);
+  CUtensorMap ma, mb;
+  if (!make_map(enc, &ma, A, (uint64_t)K2, (uint64_t)M, (uint64_t)lda * 8, TC_BM) ||
+      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, TC_BN)) {
+    set_error("cuTensorMapEncodeTiled failed");
+    return MNPBEM_ERR_CUDA;
+  }
+  if (!c.err_cleared) {
+    MNP_CUDA(cudaMemsetAsync(c.err.ptr, 0, sizeof(int), st));
+    c.err_cleared = true;
+  }
+  dim3 grid((unsigned)cdiv_up(N2, TC_BN), (unsigned)cdiv_up(M, TC_BM));
+  if (grid.y > 65535) { set_error("tc_gemm_c64: M too large"); return MNPBEM_ERR_INVALID_ARG; }
+  {
+    ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
+                 8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
+    k_tc_gemm<<<grid, 128, TC_SMEM, st>>>(ma, mb, (int)M, (int)N2, (int)K2, reinterpret_cast<float*>(C),
+                                         ldc * 2, beta.x, c.err.as<int>());
+    MNP_CHECK_LAUNCH();
+  }
+  return MNPBEM_OK;
+}
+
+mnpbem_status tc_check_error(TcGemmCtx& c, cudaStream_t st) {
+  if (!c.err.ptr || !c.err_cleared) return MNPBEM_OK;
+  int h = 0;
+  MNP_CUDA(cudaMemcpyAsync(&h, c.err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  c.err_cleared = false;
+  if (h) {
+    set_error("tensor-core GEMM: a bounded pipeline wait expired (code %d)", h);
+    c.enabled = false;
+    return MNPBEM_ERR_TIMEOUT;
+  }
+  return MNPBEM_OK;
+}
+
+void tc_release(TcGemmCtx& c) {
+  c.bexp.release();
+  c.err.release();
+}
+
+}  // namespace mnpbem

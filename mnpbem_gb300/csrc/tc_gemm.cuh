@@ -1,0 +1,25 @@
+// Complex64 GEMM on the 5th-generation tensor cores (tcgen05, kind::tf32).
+#pragma once
+#include "common.cuh"
+
+namespace mnpbem {
+
+struct TcGemmCtx {
+  bool checked = false;   // device capability probed
+  bool usable = false;    // sm_103 device, driver entry point and kernel attributes available
+  bool enabled = true;    // switched off after a device-side error
+  bool err_cleared = false;
+  DevBuf bexp;            // expanded B operand [2N][2K] (real, K-major, tf32)
+  DevBuf err;             // device error word of the bounded waits
+  void* encode_fn = nullptr;
+};
+
+bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K);
+mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha,
+                          const float2* A, int64_t lda, const float2* B, int64_t ldb, float2 beta,
+                          float2* C, int64_t ldc, cudaStream_t st);
+// reads (and clears) the device error word; MNPBEM_ERR_TIMEOUT if a wait expired
+mnpbem_status tc_check_error(TcGemmCtx& c, cudaStream_t st);
+void tc_release(TcGemmCtx& c);
+
+}  // namespace mnpbem

@@ -687,7 +687,7 @@ class PlaneWaveRet:
         e, h, k = self.farfield(cp, sig, self.dir)
         npol = self.pol.shape[0]
         val = np.array([np.sum(np.conj(self.pol[i]) * e[i, :, i]) for i in range(npol)])
-        return 4 * np.pi / k * np.imag(val)
+        return np.real(4 * np.pi / k * np.imag(val))
 
     def scattering(self, cp, sig):
         pinf = self.pinfty
