@@ -181,6 +181,32 @@ MNPBEM_API mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M
                                          int64_t lda, const float* B, int64_t ldb,
                                          const float* beta, float* C, int64_t ldc);
 
+/* Extinction and scattering cross sections of given surface charges and
+ * currents, like mnpbem_solve's ext/sca, for callers that cannot allocate GPU
+ * memory (a MEX gateway inside a MATLAB session whose GPU memory belongs to
+ * MATLAB, a plugin whose host application owns all device memory through its
+ * own pool, a real-time loop that must not meet allocation failures).
+ * It calls no cudaMalloc/cudaFree: every input and output is a caller-owned
+ * DEVICE pointer and the scratch (far fields) is a fixed __device__ array in
+ * the library, shared by all calls on a device and held until process exit.
+ * No counterpart in the reference.  Limits: npol <= 4 and npol + ninf <= 2048
+ * directions (larger sizes return MNPBEM_ERR_INVALID_ARG).  The first call on
+ * a device looks up the scratch address: make it before any stream capture.
+ * Calls whose kernels overlap on the GPU race on the shared scratch.
+ * Asynchronous on `stream` (cudaStream_t, NULL = default stream).
+ *   pos [n][3], area [n]; exc_in / exc_out [n]: 1 where the inside / outside
+ *   medium of a face is the excitation medium; sig1, sig2 [n][npol] and
+ *   h1, h2 [n][3][npol] complex; pol, dir [npol][3]; inf_nvec [ninf][3],
+ *   inf_area [ninf]; eps_exc, eps_1: complex dielectric function of the
+ *   excitation medium and of medium 1 at enei (host, 2 doubles each);
+ *   ext, sca [npol] (device outputs).                                          */
+MNPBEM_API mnpbem_status mnpbem_cross_sections_noalloc(
+    int32_t device, void* stream, int64_t n, int32_t npol, const double* pos, const double* area,
+    const unsigned char* exc_in, const unsigned char* exc_out, const double* sig1, const double* h1,
+    const double* sig2, const double* h2, const double* pol, const double* dir, int32_t ninf,
+    const double* inf_nvec, const double* inf_area, double enei, const double* eps_exc,
+    const double* eps_1, double* ext, double* sca);
+
 /* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
 MNPBEM_API mnpbem_status mnpbem_geom_stream(const mnpbem_geom* g, void** stream);
 

@@ -80,6 +80,11 @@ SIGNATURES = {
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                        ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int64]),
+    "mnpbem_cross_sections_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+                                                     ctypes.c_int32] + [ctypes.c_void_p] * 10
+                                                    + [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                       ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                                       ctypes.c_void_p, ctypes.c_void_p]),
     "mnpbem_geom_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_last_error": (ctypes.c_char_p, []),
     "mnpbem_version": (ctypes.c_char_p, []),

@@ -1,0 +1,181 @@
+// Extinction and scattering cross sections of given surface charges and
+// currents (exc.ext(sig), exc.sca(sig):
+// Simulation/retarded/@planewaveret/extinction.m:12-16, scattering.m:13-19,
+// @spectrumret/farfield.m:15-74) with no device allocation at all.
+//
+// Some callers cannot call cudaMalloc: a MEX gateway running inside a MATLAB
+// session whose GPU memory is owned by MATLAB's own allocator, a plugin inside
+// a host application that owns all device memory through its own pool, or a
+// real-time loop that must not meet allocation latency or an out-of-memory
+// failure in the middle of a run.  For them this entry point takes only
+// caller-owned device pointers for its inputs and outputs, and keeps its one
+// piece of scratch — the far fields e and h of every direction and
+// polarisation — in a file-scope __device__ array of fixed size
+// (NOALLOC_MAX_DIRS directions x 6 components x NOALLOC_MAX_POL
+// polarisations of complex128 = 768 KB), which every GPU that loads the
+// library holds until the process exits.
+//
+// Host code cannot use the array's name as a device address (in host code it
+// is only a stand-in).  The first call on a device, with that device current,
+// looks the address up with cudaGetSymbolAddress and caches it; make that
+// first call before any stream capture.  Every call shares the array and it
+// keeps the previous call's contents: each call first writes every entry it
+// later reads, so nothing needs clearing, but calls whose kernels overlap on
+// the GPU (different streams, or threads sharing a device) race on it.
+#include <complex>
+#include <mutex>
+
+#include "bem.cuh"
+
+namespace mnpbem {
+
+constexpr int NOALLOC_MAX_POL = 4;
+constexpr int NOALLOC_MAX_DIRS = 2048;   // excitation directions + sphere-at-infinity directions
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) double2 g_noalloc_fields[NOALLOC_MAX_DIRS * 6 * NOALLOC_MAX_POL];
+
+static double2* g_noalloc_addr[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mutex;
+
+// Far fields of one direction per block, inputs in the public solution layout
+// (sig [n][P], h [n][3][P]); direction d < P is dir[d], else inf_nvec[d - P].
+// Same arithmetic as the far-field kernel of the solve.
+__global__ void __launch_bounds__(256) k_farfield_noalloc(
+    int64_t n, int P, const double* __restrict__ pos, const double* __restrict__ area,
+    const unsigned char* __restrict__ exc_in, const unsigned char* __restrict__ exc_out,
+    const double2* __restrict__ sig1, const double2* __restrict__ h1, const double2* __restrict__ sig2,
+    const double2* __restrict__ h2, const double* __restrict__ dir, const double* __restrict__ inf_nvec,
+    double2 k, double k0, double2* fields) {
+  const int d = blockIdx.x;
+  const double* dv_ = d < P ? dir + 3 * d : inf_nvec + 3 * (d - P);
+  const double dx = dv_[0], dy = dv_[1], dz = dv_[2];
+  double2 Ps[NOALLOC_MAX_POL], Ph[3][NOALLOC_MAX_POL];
+  for (int p = 0; p < NOALLOC_MAX_POL; ++p) {
+    Ps[p] = make_double2(0, 0);
+    for (int c = 0; c < 3; ++c) Ph[c][p] = make_double2(0, 0);
+  }
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+    const bool in1 = exc_in[j] != 0, in2 = exc_out[j] != 0;
+    if (!in1 && !in2) continue;
+    const double s = dx * pos[3 * j] + dy * pos[3 * j + 1] + dz * pos[3 * j + 2];
+    double sn, cs;
+    sincos(k.x * s, &sn, &cs);
+    const double ee = exp(k.y * s) * area[j];
+    const double2 ph = make_double2(ee * cs, -ee * sn);
+    for (int p = 0; p < P; ++p) {
+      double2 sv = make_double2(0, 0);
+      double2 hv[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+      if (in1) {
+        sv = cadd(sv, sig1[j * P + p]);
+        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], h1[(j * 3 + c) * P + p]);
+      }
+      if (in2) {
+        sv = cadd(sv, sig2[j * P + p]);
+        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], h2[(j * 3 + c) * P + p]);
+      }
+      cfma(Ps[p], ph, sv);
+      for (int c = 0; c < 3; ++c) cfma(Ph[c][p], ph, hv[c]);
+    }
+  }
+  __shared__ double2 red[8][4 * NOALLOC_MAX_POL];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int p = 0; p < P; ++p) {
+    for (int q = 0; q < 4; ++q) {
+      double2 v = q == 0 ? Ps[p] : Ph[q - 1][p];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[wid][q * NOALLOC_MAX_POL + p] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x / 32;
+    const double2 ik = make_double2(-k.y, k.x);
+    const double2 ik0 = make_double2(0, k0);
+    const double dv[3] = {dx, dy, dz};
+    for (int p = 0; p < P; ++p) {
+      double2 S[4];
+      for (int q = 0; q < 4; ++q) {
+        S[q] = make_double2(0, 0);
+        for (int w = 0; w < nw; ++w) S[q] = cadd(S[q], red[w][q * NOALLOC_MAX_POL + p]);
+      }
+      const double2 ph3[3] = {S[1], S[2], S[3]};
+      for (int c = 0; c < 3; ++c)
+        fields[((int64_t)d * 6 + c) * P + p] = csub(cmul(ik0, ph3[c]), cmul(ik, cscale(S[0], dv[c])));
+      double2 cr[3];
+      cr[0] = csub(cscale(ph3[2], dv[1]), cscale(ph3[1], dv[2]));
+      cr[1] = csub(cscale(ph3[0], dv[2]), cscale(ph3[2], dv[0]));
+      cr[2] = csub(cscale(ph3[1], dv[0]), cscale(ph3[0], dv[1]));
+      for (int c = 0; c < 3; ++c) fields[((int64_t)d * 6 + 3 + c) * P + p] = cmul(ik, cr[c]);
+    }
+  }
+}
+
+// device address of the scratch array on the current device (set-up, once per device)
+static mnpbem_status noalloc_scratch(int device, double2** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_fields);
+    if (e != cudaSuccess || !ptr) {
+      cudaGetLastError();
+      set_error("cudaGetSymbolAddress of the cross-section scratch failed: %s", cudaGetErrorString(e));
+      return MNPBEM_ERR_CUDA;
+    }
+    g_noalloc_addr[device] = static_cast<double2*>(ptr);
+  }
+  *out = g_noalloc_addr[device];
+  return MNPBEM_OK;
+}
+
+}  // namespace mnpbem
+
+using namespace mnpbem;
+
+extern "C" mnpbem_status mnpbem_cross_sections_noalloc(
+    int32_t device, void* stream, int64_t n, int32_t npol, const double* pos, const double* area,
+    const unsigned char* exc_in, const unsigned char* exc_out, const double* sig1, const double* h1,
+    const double* sig2, const double* h2, const double* pol, const double* dir, int32_t ninf,
+    const double* inf_nvec, const double* inf_area, double enei, const double* eps_exc,
+    const double* eps_1, double* ext, double* sca) {
+  if (n <= 0 || npol <= 0 || ninf < 0 || !pos || !area || !exc_in || !exc_out || !sig1 || !h1 || !sig2 ||
+      !h2 || !pol || !dir || (ninf > 0 && (!inf_nvec || !inf_area)) || !eps_exc || !eps_1 || !ext ||
+      !sca || !(enei > 0)) {
+    set_error("mnpbem_cross_sections_noalloc: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if (npol > NOALLOC_MAX_POL) {
+    set_error("mnpbem_cross_sections_noalloc: npol = %d exceeds the maximum of %d polarisations",
+              (int)npol, NOALLOC_MAX_POL);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if ((int64_t)npol + ninf > NOALLOC_MAX_DIRS) {
+    set_error("mnpbem_cross_sections_noalloc: npol + ninf = %lld directions exceed the maximum of %d",
+              (long long)npol + ninf, NOALLOC_MAX_DIRS);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) {
+    set_error("mnpbem_cross_sections_noalloc: invalid device %d", (int)device);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  MNP_CUDA(cudaSetDevice(device));
+  double2* fields = nullptr;
+  MNP_TRY(noalloc_scratch(device, &fields));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double k0 = 2 * M_PI / enei;
+  const std::complex<double> kmed = k0 * std::sqrt(std::complex<double>(eps_exc[0], eps_exc[1]));
+  const std::complex<double> nb1 = std::sqrt(std::complex<double>(eps_1[0], eps_1[1]));
+  const double2 k = make_double2(kmed.real(), kmed.imag());
+  k_farfield_noalloc<<<npol + ninf, 256, 0, st>>>(
+      n, npol, pos, area, exc_in, exc_out, reinterpret_cast<const double2*>(sig1),
+      reinterpret_cast<const double2*>(h1), reinterpret_cast<const double2*>(sig2),
+      reinterpret_cast<const double2*>(h2), dir, inf_nvec, k, k0, fields);
+  MNP_CHECK_LAUNCH();
+  launch_cross_sections(npol, pol, inf_nvec, inf_area, ninf, fields, k,
+                        make_double2(nb1.real(), nb1.imag()), ext, sca, st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
