@@ -140,7 +140,7 @@ typedef struct mnpbem_solution {
 /* Refinement control for MNPBEM_MIXED (ignored for FP64). */
 typedef struct mnpbem_refine {
   int32_t max_iter; /* default 10 */
-  double tol;       /* stop when ||dx|| <= tol * ||x|| (default 1e-12) */
+  double tol;       /* stop when ||dx|| <= tol * ||x|| (default 1e-10) */
 } mnpbem_refine;
 
 /* Wavelength sweep: for each enei[w] (nm) with dielectric functions

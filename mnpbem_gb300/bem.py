@@ -135,7 +135,7 @@ class bemret:
             raise ValueError("precision must be 'mixed' or 'fp64'")
         self.precision = _lib.MIXED if prec == "mixed" else _lib.FP64
         self.refine_iters = int(self.op.get("refine_iters", 10))
-        self.refine_tol = float(self.op.get("refine_tol", 1e-12))
+        self.refine_tol = float(self.op.get("refine_tol", 1e-10))
         lib = _lib.load()
         q = p.quad
         self._quad_arrays = [np.ascontiguousarray(a, dtype=np.float64)

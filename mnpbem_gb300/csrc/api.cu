@@ -37,6 +37,15 @@ void set_error(const char* fmt, ...) {
 }
 const char* get_error() { return g_err.c_str(); }
 
+uint64_t& alloc_generation() {
+  static uint64_t gen = 0;
+  return gen;
+}
+bool& capturing_now() {
+  static thread_local bool c = false;
+  return c;
+}
+
 Profiler*& current_profiler() {
   static thread_local Profiler* p = nullptr;
   return p;
@@ -59,7 +68,7 @@ static mnpbem_status gemm32(int64_t M, int64_t N, int64_t K, float2 al, const fl
                             const float2* B, int64_t ldb, float2 be, float2* C, int64_t ldc,
                             cudaStream_t st, void* ctx) {
   TcGemmCtx* tc = reinterpret_cast<TcGemmCtx*>(ctx);
-  if (tc && tc_gemm_eligible(*tc, M, N, K))
+  if (tc && tc_gemm_eligible(*tc, M, N, K, A, lda, C, ldc, be))
     return tc_gemm_c64(*tc, M, N, K, al, A, lda, B, ldb, be, C, ldc, st);
   return gemm_simt<float>(M, N, K, al, A, lda, B, ldb, be, C, ldc, st);
 }
@@ -84,11 +93,27 @@ struct mnpbem_geom {
   DevBuf mat[5];      // working-precision matrices
   DevBuf mat64[4];    // FP64 G1, H1, G2, H2 for refinement (MIXED)
   DevBuf vec64, vecw, facebuf, exbuf, fields, norms, outbuf;
-  GJWork<float> gj32;
+  GJWork<float> gj32;    // block width set per solve (256 on the tensor-core path)
   GJWork<double> gj64;
   TcGemmCtx tc;
   bool tc_enabled = true;
   Profiler prof;
+  // per-wavelength parameters: device block + pinned host ring (one slot per wavelength)
+  DevBuf lp_dev, face_med;
+  LamParams* lp_ring = nullptr;
+  int lp_cap = 0;
+  int* status_host = nullptr;     // pinned: pivot status words (4)
+  double* norms_host = nullptr;   // pinned: refinement norms (4)
+  // CUDA graphs of the per-wavelength stages
+  bool use_graphs = true;
+  struct Graphs {
+    bool valid = false;
+    int precision = -1, P = 0, ninf = 0;
+    bool prof = false;
+    uint64_t gen = 0;
+    cudaGraphExec_t exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    Profiler::GraphRec rec[5];
+  } graphs;
 };
 
 namespace {
@@ -133,8 +158,8 @@ AsmParams base_params(mnpbem_geom* G, const std::vector<std::complex<double>>& k
   p.ref_col = G->g.ref_col;
   p.ref_g = G->g.ref_g;
   p.ref_f = G->g.ref_f;
-  for (size_t m = 0; m < kmed.size() && m < (size_t)ASM_MAXMED; ++m)
-    p.k[m] = make_double2(kmed[m].real(), kmed[m].imag());
+  (void)kmed;
+  p.lp = G->lp_dev.as<LamParams>();
   fill_media(G, p);
   return p;
 }
@@ -217,6 +242,22 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   G->g.order = op.order;
   mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, nfaces, cs.data(), ce.data(),
                                    (int)cs.size(), quad, op.rel_cutoff, op.abs_cutoff, G->st);
+  if (s == MNPBEM_OK) s = G->lp_dev.ensure(sizeof(LamParams));
+  if (s == MNPBEM_OK) s = G->face_med.ensure(sizeof(int) * 2 * nfaces);
+  if (s == MNPBEM_OK) {
+    std::vector<int> fm(2 * nfaces);
+    for (int64_t k = 0; k < nfaces; ++k) {
+      fm[k] = G->inout[2 * G->face_part[k]] - 1;
+      fm[nfaces + k] = G->inout[2 * G->face_part[k] + 1] - 1;
+    }
+    if (cudaMemcpy(G->face_med.ptr, fm.data(), sizeof(int) * 2 * nfaces, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMallocHost(&G->status_host, 4 * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&G->norms_host, 4 * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("geometry set-up: upload of face media or pinned allocation failed");
+      s = MNPBEM_ERR_CUDA;
+    }
+  }
   if (s == MNPBEM_OK) s = G->d_part.ensure(sizeof(int) * nfaces);
   if (s == MNPBEM_OK) s = G->d_src.ensure(sizeof(double4_32a) * nfaces);
   if (s == MNPBEM_OK) s = G->d_nrm.ensure(sizeof(double4_32a) * nfaces);
@@ -243,6 +284,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   G->ld = round_up(nfaces, 32);
   const char* env = getenv("MNPBEM_TC");
   if (env && env[0] == '0') G->tc_enabled = false;
+  const char* genv = getenv("MNPBEM_GRAPHS");
+  if (genv && genv[0] == '0') G->use_graphs = false;
   *out = G;
   return MNPBEM_OK;
 }
@@ -252,6 +295,13 @@ mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g) {
   cudaSetDevice(g->device);
   if (g->st) cudaStreamSynchronize(g->st);
   tc_release(g->tc);
+  for (int q = 0; q < 5; ++q) {
+    if (g->graphs.exec[q]) cudaGraphExecDestroy(g->graphs.exec[q]);
+    Profiler::release(g->graphs.rec[q]);
+  }
+  if (g->lp_ring) cudaFreeHost(g->lp_ring);
+  if (g->status_host) cudaFreeHost(g->status_host);
+  if (g->norms_host) cudaFreeHost(g->norms_host);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
   return MNPBEM_OK;
@@ -307,6 +357,12 @@ mnpbem_status mnpbem_assemble(mnpbem_geom* G, const double* k_media, int32_t nme
   ProfBind pb_(&G->prof);
   std::vector<std::complex<double>> km(nmed);
   for (int m = 0; m < nmed; ++m) km[m] = cx(k_media + 2 * m);
+  {
+    LamParams lp{};
+    for (int m = 0; m < nmed; ++m) lp.k[m] = make_double2(km[m].real(), km[m].imag());
+    MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(lp), cudaMemcpyHostToDevice, G->st));
+    MNP_CUDA(cudaStreamSynchronize(G->st));
+  }
   AsmParams p = base_params(G, km);
   const int64_t n = G->g.n;
   const bool w64 = precision == MNPBEM_FP64;
@@ -383,7 +439,7 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
   MNP_CUDA(cudaMemcpyAsync(dC.ptr, C, sizeof(float2) * M * ldc, cudaMemcpyHostToDevice, st));
   const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
   if (path == 1) {
-    if (!tc_gemm_eligible(tc[device], M, N, K)) {
+    if (!tc_gemm_eligible(tc[device], M, N, K, dA.ptr, lda, dC.ptr, ldc, be)) {
       set_error("tensor-core GEMM not available for this device or shape");
       return MNPBEM_ERR_UNSUPPORTED;
     }
@@ -411,43 +467,60 @@ mnpbem_status mnpbem_geom_stream(const mnpbem_geom* G, void** stream) {
 // ======================================================================
 // per-wavelength solver
 // ======================================================================
+// The work of one wavelength is split into stages that depend on the
+// wavelength only through the device parameter block G->lp_dev:
+//   S0 assemble        per-face eps + G1, H1, G2, H2 (complex64 and/or complex128)
+//   S1 initmat         inversions, products, Sigma stage
+//   S2 first solve     excitation + mldivide chain (+ conversions)
+//   S3 refinement step FP64 residual of the full operator + chain + update (MIXED)
+//   S4 spectra         far fields + extinction / scattering into a fixed slot
+// The first wavelength of a configuration runs the stages directly (sizing
+// every buffer); later wavelengths replay the stages as CUDA graphs.
 namespace {
 
 struct SolveCtx {
   mnpbem_geom* G;
   int P;
-  double enei, k0;
-  std::complex<double> kmed_exc, nb1;
-  std::vector<std::complex<double>> kmed;   // per medium
-  double2* eps1;   // device per-face
-  double2* eps2;
+  int precision;
+  const mnpbem_planewave* exc;
   FaceData fd;
 };
 
-// upload per-face eps for this wavelength
-mnpbem_status prepare_faces(mnpbem_geom* G, SolveCtx& c, const double* eps_media, int nmed) {
-  const int64_t n = G->g.n;
-  std::vector<double2> e(2 * n);
-  for (int64_t i = 0; i < n; ++i) {
-    int p = G->face_part[i];
-    int mi = G->inout[2 * p] - 1, mo = G->inout[2 * p + 1] - 1;
-    e[i] = make_double2(eps_media[2 * mi], eps_media[2 * mi + 1]);
-    e[n + i] = make_double2(eps_media[2 * mo], eps_media[2 * mo + 1]);
-  }
-  (void)nmed;
-  MNP_TRY(G->facebuf.ensure(sizeof(double2) * 2 * n + 2 * n + 64));
-  MNP_CUDA(cudaMemcpyAsync(G->facebuf.ptr, e.data(), sizeof(double2) * 2 * n, cudaMemcpyHostToDevice, G->st));
-  c.eps1 = G->facebuf.as<double2>();
-  c.eps2 = c.eps1 + n;
-  c.fd.n = n;
-  c.fd.pos = G->g.pos;
-  c.fd.nvec = G->g.nvec;
-  c.fd.area = G->g.area;
-  c.fd.eps1 = c.eps1;
-  c.fd.eps2 = c.eps2;
-  c.fd.exc_in = reinterpret_cast<const unsigned char*>(c.eps2 + n);
-  c.fd.exc_out = c.fd.exc_in + n;
+mnpbem_status ensure_workspace(mnpbem_geom* G, int precision, int P, int ninf) {
+  const int64_t n = G->g.n, ld = G->ld;
+  const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
+  for (int q = 0; q < 5; ++q) MNP_TRY(G->mat[q].ensure(es * n * ld));
+  if (precision == MNPBEM_MIXED)
+    for (int q = 0; q < 4; ++q) MNP_TRY(G->mat64[q].ensure(sizeof(double2) * n * ld));
+  // FP64 vectors: b (8nP) x (8nP) r (8nP) YZ (16nP) + chain work for FP64 (32nP)
+  MNP_TRY(G->vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32)));
+  // working-precision vectors for MIXED: in (8nP) out (8nP) work (32nP)
+  MNP_TRY(G->vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
+  MNP_TRY(G->norms.ensure(sizeof(double) * 4));
+  MNP_TRY(G->facebuf.ensure(sizeof(double2) * 2 * n + sizeof(float2) * 3 * n + sizeof(float) * 3 * n + 2 * n + 256));
+  MNP_TRY(G->fields.ensure(sizeof(double2) * (size_t)(P + ninf) * 6 * P));
+  MNP_TRY(G->outbuf.ensure(sizeof(double) * 2 * P));   // ext / sca slot of the current wavelength
   return MNPBEM_OK;
+}
+
+FaceData face_data(mnpbem_geom* G) {
+  const int64_t n = G->g.n;
+  FaceData f;
+  f.n = n;
+  f.pos = G->g.pos;
+  f.nvec = G->g.nvec;
+  f.area = G->g.area;
+  double2* e = G->facebuf.as<double2>();
+  f.eps1 = e;
+  f.eps2 = e + n;
+  float2* ef = reinterpret_cast<float2*>(e + 2 * n);
+  f.eps1f = ef;
+  f.eps2f = ef + n;
+  f.Lf = ef + 2 * n;
+  f.nvecf = reinterpret_cast<const float*>(ef + 3 * n);
+  f.exc_in = reinterpret_cast<const unsigned char*>(f.nvecf + 3 * n);
+  f.exc_out = f.exc_in + n;
+  return f;
 }
 
 mnpbem_status upload_masks(mnpbem_geom* G, int medium) {
@@ -458,8 +531,7 @@ mnpbem_status upload_masks(mnpbem_geom* G, int medium) {
     m[i] = G->inout[2 * p] == medium;
     m[n + i] = G->inout[2 * p + 1] == medium;
   }
-  MNP_TRY(G->facebuf.ensure(sizeof(double2) * 2 * n + 2 * n + 64));
-  unsigned char* dst = reinterpret_cast<unsigned char*>(G->facebuf.as<double2>() + 2 * n);
+  unsigned char* dst = const_cast<unsigned char*>(face_data(G).exc_in);
   MNP_CUDA(cudaMemcpyAsync(dst, m.data(), 2 * n, cudaMemcpyHostToDevice, G->st));
   MNP_CUDA(cudaStreamSynchronize(G->st));
   return MNPBEM_OK;
@@ -487,32 +559,6 @@ mnpbem_status gemm_w<double>(int64_t M, int64_t N, int64_t K, double2 al, const 
   return mnpbem::gemm64(M, N, K, al, A, lda, B, ldb, be, C, ldc, st, ctx);
 }
 
-// initmat in precision R on matrices M0..M4 (assembled G1, G2, H1, H2 in M0..M3)
-template <typename R>
-mnpbem_status initmat(mnpbem_geom* G, SolveCtx& c) {
-  using Cx = cplx<R>;
-  const int64_t n = G->g.n, ld = G->ld;
-  Cx* M[5];
-  for (int q = 0; q < 5; ++q) M[q] = G->mat[q].as<Cx>();
-  void* ctx = (sizeof(R) == 4 && G->tc_enabled) ? (void*)&G->tc : nullptr;
-  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
-  // G1i, G2i
-  MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st));
-  MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st));
-  // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, G->st, ctx));
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, G->st, ctx));
-  // Delta -> M3, Sigma (partial) -> M2
-  launch_delta_sigma<R>(n, M[4], M[2], M[3], ld, c.eps1, c.eps2, G->st);
-  MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[3], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st));
-  launch_sigma_add<R>(n, M[2], M[3], ld, c.eps1, c.eps2, G->g.nvec, c.k0, G->st);
-  MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st));
-  if (ctx) MNP_TRY(tc_check_error(G->tc, G->st));
-  return MNPBEM_OK;
-}
-
 template <typename R>
 ChainMats<R> chain_mats(mnpbem_geom* G) {
   using Cx = cplx<R>;
@@ -526,9 +572,16 @@ ChainMats<R> chain_mats(mnpbem_geom* G) {
   return m;
 }
 
-mnpbem_status assemble_into(mnpbem_geom* G, SolveCtx& c, int precision) {
-  AsmParams p = base_params(G, c.kmed);
-  const int64_t ld = G->ld;
+// ---------------------------------------------------------------- S0
+mnpbem_status stage_assemble(mnpbem_geom* G, int precision) {
+  const int64_t n = G->g.n, ld = G->ld;
+  const int* fm = G->face_med.as<int>();
+  FaceData f = face_data(G);
+  launch_face_eps(n, fm, fm + n, G->lp_dev.as<LamParams>(), G->g.nvec, const_cast<double2*>(f.eps1),
+                  const_cast<double2*>(f.eps2), const_cast<float2*>(f.eps1f), const_cast<float2*>(f.eps2f),
+                  const_cast<float2*>(f.Lf), const_cast<float*>(f.nvecf), G->st);
+  MNP_CHECK_LAUNCH();
+  AsmParams p = base_params(G, {});
   if (precision == MNPBEM_FP64) {
     p.ld64 = ld;
     p.G1 = G->mat[0].as<double2>(); p.G2 = G->mat[1].as<double2>();
@@ -544,111 +597,270 @@ mnpbem_status assemble_into(mnpbem_geom* G, SolveCtx& c, int precision) {
   return assemble_launch(p, true, true, G->st);
 }
 
-mnpbem_status ensure_workspace(mnpbem_geom* G, int precision, int P) {
+// ---------------------------------------------------------------- S1
+template <typename R>
+mnpbem_status stage_initmat(mnpbem_geom* G, bool direct) {
+  using Cx = cplx<R>;
   const int64_t n = G->g.n, ld = G->ld;
-  const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
-  for (int q = 0; q < 5; ++q) MNP_TRY(G->mat[q].ensure(es * n * ld));
-  if (precision == MNPBEM_MIXED)
-    for (int q = 0; q < 4; ++q) MNP_TRY(G->mat64[q].ensure(sizeof(double2) * n * ld));
-  // FP64 vectors: b (8nP) x (8nP) r (8nP) YZ (16nP) + chain work for FP64 (32nP)
-  MNP_TRY(G->vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32)));
-  // working-precision vectors for MIXED: in (8nP) out (8nP) work (32nP)
-  MNP_TRY(G->vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
-  MNP_TRY(G->norms.ensure(sizeof(double) * 4));
+  Cx* M[5];
+  for (int q = 0; q < 5; ++q) M[q] = G->mat[q].as<Cx>();
+  void* ctx = (sizeof(R) == 4 && G->tc_enabled) ? (void*)&G->tc : nullptr;
+  // wider Gauss-Jordan steps when the rank-nb updates run on tensor cores:
+  // fewer passes over the n x n matrix (each step reads and writes it once)
+  gjw<R>(G).nb = (ctx && n >= 1024) ? 256 : 64;
+  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
+  const FaceData fd = face_data(G);
+  const LamParams* lp = G->lp_dev.as<LamParams>();
+  // G1i, G2i
+  MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
+  MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
+  // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2
+  MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, G->st, ctx));
+  MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, G->st, ctx));
+  // Delta -> M3, Sigma (partial) -> M2
+  launch_delta_sigma<R>(n, M[4], M[2], M[3], ld, fd, G->st);
+  MNP_CHECK_LAUNCH();
+  MNP_TRY(gj_invert<R>(M[3], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
+  launch_sigma_add<R>(n, M[2], M[3], ld, fd, lp, G->st);
+  MNP_CHECK_LAUNCH();
+  MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
+  if (direct && ctx) MNP_TRY(tc_check_error(G->tc, G->st));
   return MNPBEM_OK;
 }
 
-// one wavelength
-mnpbem_status solve_one(mnpbem_geom* G, SolveCtx& c, const mnpbem_planewave* exc, int precision,
-                        const mnpbem_refine* ref, double* dext, double* dsca, int32_t* iters,
-                        double* resid) {
+// FP64 vector arena layout
+struct Vec64 {
+  double2 *phi, *a, *alpha, *De, *x1, *x2, *rphi, *ra, *ral, *rDe, *Y1, *Y2, *Z1, *Z2, *work;
+};
+Vec64 vec64(mnpbem_geom* G, int P) {
+  const int64_t n = G->g.n;
+  Vec64 v;
+  double2* V = G->vec64.as<double2>();
+  v.phi = V; v.a = v.phi + n * P; v.alpha = v.a + 3 * n * P; v.De = v.alpha + 3 * n * P;
+  v.x1 = v.De + n * P; v.x2 = v.x1 + 4 * n * P;
+  v.rphi = v.x2 + 4 * n * P; v.ra = v.rphi + n * P; v.ral = v.ra + 3 * n * P; v.rDe = v.ral + 3 * n * P;
+  v.Y1 = v.rDe + n * P; v.Y2 = v.Y1 + 4 * n * P; v.Z1 = v.Y2 + 4 * n * P; v.Z2 = v.Z1 + 4 * n * P;
+  v.work = v.Z2 + 4 * n * P;
+  return v;
+}
+
+// complex64 chain applied to FP64 inputs, result in fx1/fx2
+mnpbem_status apply32(mnpbem_geom* G, const FaceData& fd, int P, const double2* p_, const double2* a_,
+                      const double2* al_, const double2* De_) {
+  const int64_t n = G->g.n;
+  cudaStream_t st = G->st;
+  float2* W = G->vecw.as<float2>();
+  float2 *fphi = W, *fa = fphi + n * P, *fal = fa + 3 * n * P, *fDe = fal + 3 * n * P;
+  float2 *fx1 = fDe + n * P, *fx2 = fx1 + 4 * n * P, *fwork = fx2 + 4 * n * P;
+  launch_cvt_d2f(p_, fphi, n * P, st);
+  launch_cvt_d2f(a_, fa, 3 * n * P, st);
+  launch_cvt_d2f(al_, fal, 3 * n * P, st);
+  launch_cvt_d2f(De_, fDe, n * P, st);
+  MNP_CHECK_LAUNCH();
+  void* ctx = G->tc_enabled ? (void*)&G->tc : nullptr;
+  return apply_mldivide<float>(fd, P, G->lp_dev.as<LamParams>(), chain_mats<float>(G), fphi, fa, fal, fDe,
+                               fx1, fx2, fwork, gemm_w<float>, ctx, st);
+}
+float2* fx_ptr(mnpbem_geom* G, int P, int which) {
+  const int64_t n = G->g.n;
+  return G->vecw.as<float2>() + 8 * n * P + (which ? 4 * n * P : 0);
+}
+
+// ---------------------------------------------------------------- S2
+mnpbem_status stage_first(mnpbem_geom* G, const SolveCtx& c) {
+  const int64_t n = G->g.n;
+  const int P = c.P;
+  Vec64 v = vec64(G, P);
+  const double* pol = G->exbuf.as<double>();
+  const double* dirs = pol + 3 * P;
+  const LamParams* lp = G->lp_dev.as<LamParams>();
+  launch_excitation(c.fd, P, pol, dirs, lp, v.phi, v.a, v.alpha, v.De, G->st);
+  MNP_CHECK_LAUNCH();
+  if (c.precision == MNPBEM_FP64)
+    return apply_mldivide<double>(c.fd, P, lp, chain_mats<double>(G), v.phi, v.a, v.alpha, v.De, v.x1, v.x2,
+                                  v.work, gemm_w<double>, nullptr, G->st);
+  MNP_TRY(apply32(G, c.fd, P, v.phi, v.a, v.alpha, v.De));
+  launch_cvt_f2d(fx_ptr(G, P, 0), v.x1, 4 * n * P, G->st);
+  launch_cvt_f2d(fx_ptr(G, P, 1), v.x2, 4 * n * P, G->st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+// ---------------------------------------------------------------- S3
+// norms[0..1] = ||r||^2, ||b||^2 ; norms[2..3] = ||dx||^2, ||x||^2
+mnpbem_status stage_iter(mnpbem_geom* G, const SolveCtx& c) {
   const int64_t n = G->g.n;
   const int P = c.P;
   cudaStream_t st = G->st;
-  MNP_TRY(assemble_into(G, c, precision));
-  if (precision == MNPBEM_FP64) MNP_TRY(initmat<double>(G, c));
-  else MNP_TRY(initmat<float>(G, c));
-  // FP64 vectors
-  double2* V = G->vec64.as<double2>();
-  double2 *phi = V, *a = phi + n * P, *alpha = a + 3 * n * P, *De = alpha + 3 * n * P;
-  double2 *x1 = De + n * P, *x2 = x1 + 4 * n * P;
-  double2 *rphi = x2 + 4 * n * P, *ra = rphi + n * P, *ral = ra + 3 * n * P, *rDe = ral + 3 * n * P;
-  double2 *Y1 = rDe + n * P, *Y2 = Y1 + 4 * n * P, *Z1 = Y2 + 4 * n * P, *Z2 = Z1 + 4 * n * P;
-  double2* work64 = Z2 + 4 * n * P;
+  Vec64 v = vec64(G, P);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  const double2* A64[4] = {G->mat64[0].as<double2>(), G->mat64[1].as<double2>(),
+                           G->mat64[2].as<double2>(), G->mat64[3].as<double2>()};
+  double* norms = G->norms.as<double>();
+  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[0], G->ld, v.x1, 4 * P, zero, v.Y1, 4 * P, st));
+  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[2], G->ld, v.x2, 4 * P, zero, v.Y2, 4 * P, st));
+  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[1], G->ld, v.x1, 4 * P, zero, v.Z1, 4 * P, st));
+  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[3], G->ld, v.x2, 4 * P, zero, v.Z2, 4 * P, st));
+  MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
+  launch_residual(c.fd, P, G->lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.phi, v.a, v.alpha, v.De,
+                  v.rphi, v.ra, v.ral, v.rDe, norms, st);
+  MNP_CHECK_LAUNCH();
+  MNP_TRY(apply32(G, c.fd, P, v.rphi, v.ra, v.ral, v.rDe));
+  launch_axpy_norm(v.x1, fx_ptr(G, P, 0), 4 * n * P, norms + 2, st);
+  launch_axpy_norm(v.x2, fx_ptr(G, P, 1), 4 * n * P, norms + 2, st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+// ---------------------------------------------------------------- S4
+mnpbem_status stage_spectra(mnpbem_geom* G, const SolveCtx& c) {
+  const int P = c.P;
+  Vec64 v = vec64(G, P);
   const double* pol = G->exbuf.as<double>();
   const double* dirs = pol + 3 * P;
-  launch_excitation(c.fd, P, pol, dirs, make_double2(c.kmed_exc.real(), c.kmed_exc.imag()), c.k0,
-                    phi, a, alpha, De, st);
+  const int ninf = c.exc->ninf;
+  const double* inf_nvec = dirs + 3 * P;
+  const double* inf_area = inf_nvec + 3 * ninf;
+  double2* fields = G->fields.as<double2>();
+  const LamParams* lp = G->lp_dev.as<LamParams>();
+  launch_farfield(c.fd, P, v.x1, v.x2, dirs, P + ninf, lp, fields, G->st);
   MNP_CHECK_LAUNCH();
-  double* norms = G->norms.as<double>();
+  double* slot = G->outbuf.as<double>();
+  launch_cross_sections_lp(P, pol, inf_nvec, inf_area, ninf, fields, lp, slot, slot + P, G->st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+mnpbem_status run_stage(mnpbem_geom* G, const SolveCtx& c, int stage, bool direct) {
+  switch (stage) {
+    case 0: return stage_assemble(G, c.precision);
+    case 1: return c.precision == MNPBEM_FP64 ? stage_initmat<double>(G, direct) : stage_initmat<float>(G, direct);
+    case 2: return stage_first(G, c);
+    case 3: return stage_iter(G, c);
+    default: return stage_spectra(G, c);
+  }
+}
+
+// capture one stage into a graph; profiling events recorded during the
+// capture become event nodes whose timings are read after every replay
+mnpbem_status capture_stage(mnpbem_geom* G, const SolveCtx& c, int stage) {
+  auto& gr = G->graphs;
+  Profiler cap;
+  cap.enabled = G->prof.enabled;
+  ProfBind pb(&cap);
+  capturing_now() = true;
+  cudaError_t e = cudaStreamBeginCapture(G->st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    capturing_now() = false;
+    MNP_CUDA(e);
+  }
+  mnpbem_status s = run_stage(G, c, stage, false);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(G->st, &graph);
+  capturing_now() = false;
+  if (s != MNPBEM_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return s;
+  }
+  MNP_CUDA(e);
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  MNP_CUDA(e);
+  if (gr.exec[stage]) cudaGraphExecDestroy(gr.exec[stage]);
+  Profiler::release(gr.rec[stage]);
+  gr.exec[stage] = exec;
+  cap.move_to(gr.rec[stage]);
+  return MNPBEM_OK;
+}
+
+void drop_graphs(mnpbem_geom* G) {
+  auto& gr = G->graphs;
+  cudaStreamSynchronize(G->st);
+  G->prof.flush();          // replayed records must be read before their events go
+  for (int q = 0; q < 5; ++q) {
+    if (gr.exec[q]) cudaGraphExecDestroy(gr.exec[q]);
+    gr.exec[q] = nullptr;
+    Profiler::release(gr.rec[q]);
+  }
+  gr.valid = false;
+  cudaGetLastError();
+}
+
+mnpbem_status launch_stage(mnpbem_geom* G, const SolveCtx& c, int stage, bool graphs) {
+  if (!graphs) return run_stage(G, c, stage, true);
+  MNP_CUDA(cudaGraphLaunch(G->graphs.exec[stage], G->st));
+  G->prof.replayed.push_back(&G->graphs.rec[stage]);
+  return MNPBEM_OK;
+}
+
+mnpbem_status check_pivots(mnpbem_geom* G) {
+  if (G->status_host[0] | G->status_host[1]) {
+    set_error("block Gauss-Jordan inversion: zero or non-finite pivot");
+    return MNPBEM_ERR_SINGULAR;
+  }
+  return MNPBEM_OK;
+}
+
+// one wavelength through all stages; graphs == true replays captured stages
+mnpbem_status solve_one(mnpbem_geom* G, const SolveCtx& c, const mnpbem_refine* ref, bool graphs,
+                        int32_t* iters, double* resid) {
+  cudaStream_t st = G->st;
+  for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, c, stage, graphs));
+  if (graphs) {
+    if (c.precision == MNPBEM_FP64) MNP_TRY(gj_status_copy<double>(G->gj64, G->status_host, st));
+    else MNP_TRY(gj_status_copy<float>(G->gj32, G->status_host, st));
+  } else {
+    G->status_host[0] = G->status_host[1] = 0;
+  }
   int used = 0;
   double final_res = -1.0;
-  if (precision == MNPBEM_FP64) {
-    MNP_TRY(apply_mldivide<double>(c.fd, P, c.k0, chain_mats<double>(G), phi, a, alpha, De, x1, x2,
-                                   work64, gemm_w<double>, nullptr, st));
-  } else {
-    float2* W = G->vecw.as<float2>();
-    float2 *fphi = W, *fa = fphi + n * P, *fal = fa + 3 * n * P, *fDe = fal + 3 * n * P;
-    float2 *fx1 = fDe + n * P, *fx2 = fx1 + 4 * n * P, *fwork = fx2 + 4 * n * P;
-    void* ctx = G->tc_enabled ? (void*)&G->tc : nullptr;
-    ChainMats<float> cm = chain_mats<float>(G);
-    auto apply32 = [&](const double2* p_, const double2* a_, const double2* al_,
-                       const double2* De_) -> mnpbem_status {
-      launch_cvt_d2f(p_, fphi, n * P, st);
-      launch_cvt_d2f(a_, fa, 3 * n * P, st);
-      launch_cvt_d2f(al_, fal, 3 * n * P, st);
-      launch_cvt_d2f(De_, fDe, n * P, st);
-      MNP_CHECK_LAUNCH();
-      return apply_mldivide<float>(c.fd, P, c.k0, cm, fphi, fa, fal, fDe, fx1, fx2, fwork,
-                                   gemm_w<float>, ctx, st);
-    };
-    MNP_TRY(apply32(phi, a, alpha, De));
-    launch_cvt_f2d(fx1, x1, 4 * n * P, st);
-    launch_cvt_f2d(fx2, x2, 4 * n * P, st);
-    MNP_CHECK_LAUNCH();
+  if (c.precision == MNPBEM_MIXED) {
     const int maxit = ref && ref->max_iter > 0 ? ref->max_iter : 10;
-    const double tol = ref && ref->tol > 0 ? ref->tol : 1e-12;
-    const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
-    const double2* A64[4] = {G->mat64[0].as<double2>(), G->mat64[1].as<double2>(),
-                             G->mat64[2].as<double2>(), G->mat64[3].as<double2>()};
-    bool conv = false;
+    const double tol = ref && ref->tol > 0 ? ref->tol : 1e-10;
+    double* hn = G->norms_host;
     for (int it = 0; it < maxit; ++it) {
-      MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[0], G->ld, x1, 4 * P, zero, Y1, 4 * P, st));
-      MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[2], G->ld, x2, 4 * P, zero, Y2, 4 * P, st));
-      MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[1], G->ld, x1, 4 * P, zero, Z1, 4 * P, st));
-      MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[3], G->ld, x2, 4 * P, zero, Z2, 4 * P, st));
-      MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
-      launch_residual(c.fd, P, c.k0, Y1, Y2, Z1, Z2, phi, a, alpha, De, rphi, ra, ral, rDe, norms, st);
-      MNP_CHECK_LAUNCH();
-      MNP_TRY(apply32(rphi, ra, ral, rDe));
-      launch_axpy_norm(x1, fx1, 4 * n * P, norms + 2, st);
-      launch_axpy_norm(x2, fx2, 4 * n * P, norms + 2, st);
-      MNP_CHECK_LAUNCH();
-      double hn[4];
-      MNP_CUDA(cudaMemcpyAsync(hn, norms, sizeof(hn), cudaMemcpyDeviceToHost, st));
+      MNP_TRY(launch_stage(G, c, 3, graphs));
+      MNP_CUDA(cudaMemcpyAsync(hn, G->norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       MNP_CUDA(cudaStreamSynchronize(st));
+      G->prof.flush();
+      MNP_TRY(check_pivots(G));
       used = it + 1;
       final_res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
       if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-      if (sqrt(hn[2]) <= tol * sqrt(hn[3])) { conv = true; break; }
+      if (sqrt(hn[2]) <= tol * sqrt(hn[3])) break;
     }
-    (void)conv;
   }
-  // spectra (FP64)
-  const int ndir = P + exc->ninf;
-  const double* inf_nvec = dirs + 3 * P;
-  const double* inf_area = inf_nvec + 3 * exc->ninf;
-  double2* fields = G->fields.as<double2>();
-  launch_farfield(c.fd, P, x1, x2, dirs, ndir, make_double2(c.kmed_exc.real(), c.kmed_exc.imag()),
-                  c.k0, fields, st);
-  MNP_CHECK_LAUNCH();
-  launch_cross_sections(P, pol, inf_nvec, inf_area, exc->ninf, fields,
-                        make_double2(c.kmed_exc.real(), c.kmed_exc.imag()),
-                        make_double2(c.nb1.real(), c.nb1.imag()), dext, dsca, st);
-  MNP_CHECK_LAUNCH();
+  MNP_TRY(launch_stage(G, c, 4, graphs));
   if (iters) *iters = used;
   if (resid) *resid = final_res;
-  if (precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(G->tc, st));
+  return MNPBEM_OK;
+}
+
+void fill_lp(LamParams& lp, double enei, const double* em, int nmed, int medium, int w) {
+  lp = LamParams{};
+  const double k0 = 2 * M_PI / enei;
+  for (int m = 0; m < nmed; ++m) {
+    const std::complex<double> e(em[2 * m], em[2 * m + 1]);
+    const std::complex<double> k = k0 * std::sqrt(e);
+    lp.eps[m] = make_double2(e.real(), e.imag());
+    lp.k[m] = make_double2(k.real(), k.imag());
+  }
+  lp.kexc = lp.k[medium - 1];
+  const std::complex<double> nb1 = std::sqrt(std::complex<double>(em[0], em[1]));
+  lp.nb1 = make_double2(nb1.real(), nb1.imag());
+  lp.k0 = k0;
+  lp.w = w;
+}
+
+mnpbem_status ensure_lp_ring(mnpbem_geom* G, int count) {
+  if (G->lp_cap >= count) return MNPBEM_OK;
+  if (G->lp_ring) cudaFreeHost(G->lp_ring);
+  G->lp_ring = nullptr;
+  G->lp_cap = 0;
+  MNP_CUDA(cudaMallocHost(&G->lp_ring, sizeof(LamParams) * count));
+  G->lp_cap = count;
   return MNPBEM_OK;
 }
 
@@ -685,7 +897,7 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
   ProfBind pb_(&G->prof);
   const int P = exc->npol;
   const int64_t n = G->g.n;
-  MNP_TRY(ensure_workspace(G, precision, P));
+  MNP_TRY(ensure_workspace(G, precision, P, exc->ninf));
   // excitation buffer: pol, dir, inf nvec, inf area
   {
     std::vector<double> eb;
@@ -697,50 +909,78 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
     }
     MNP_TRY(G->exbuf.ensure(sizeof(double) * eb.size()));
     MNP_CUDA(cudaMemcpyAsync(G->exbuf.ptr, eb.data(), sizeof(double) * eb.size(), cudaMemcpyHostToDevice, G->st));
-    MNP_TRY(G->fields.ensure(sizeof(double2) * (size_t)(P + exc->ninf) * 6 * P));
   }
   MNP_TRY(upload_masks(G, exc->medium));
-  MNP_TRY(G->outbuf.ensure(sizeof(double) * 2 * P * (size_t)nenei));
-  double* dext = G->outbuf.as<double>();
-  double* dsca = dext + P * (size_t)nenei;
+  MNP_TRY(ensure_lp_ring(G, nenei));
+  SolveCtx c;
+  c.G = G;
+  c.P = P;
+  c.precision = precision;
+  c.exc = exc;
+  c.fd = face_data(G);
+  auto& gr = G->graphs;
+  const cudaMemcpyKind kind = out->outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  const size_t cs = sizeof(double2);
   for (int w = 0; w < nenei; ++w) {
-    SolveCtx c;
-    c.G = G;
-    c.P = P;
-    c.enei = enei[w];
-    c.k0 = 2 * M_PI / enei[w];
-    const double* em = eps_media + 2 * (size_t)nmed * w;
-    c.kmed.resize(nmed);
-    for (int m = 0; m < nmed; ++m) c.kmed[m] = 2 * M_PI / enei[w] * std::sqrt(cx(em + 2 * m));
-    c.kmed_exc = c.kmed[exc->medium - 1];
-    c.nb1 = std::sqrt(cx(em));
-    MNP_TRY(prepare_faces(G, c, em, nmed));
+    LamParams& lp = G->lp_ring[w];
+    fill_lp(lp, enei[w], eps_media + 2 * (size_t)nmed * w, nmed, exc->medium, 0);
+    MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, G->st));
+    const bool want_graphs = G->use_graphs;
+    bool graphs = want_graphs && gr.valid && gr.precision == precision && gr.P == P &&
+                  gr.ninf == exc->ninf && gr.prof == G->prof.enabled && gr.gen == alloc_generation();
+    if (want_graphs && !graphs && gr.valid) drop_graphs(G);
     int32_t it = 0;
     double res = -1;
-    MNP_TRY(solve_one(G, c, exc, precision, refine, dext + (size_t)w * P, dsca + (size_t)w * P, &it, &res));
+    MNP_TRY(solve_one(G, c, refine, graphs, &it, &res));
+    if (want_graphs && !graphs) {
+      // first wavelength of this configuration ran directly and sized every
+      // buffer: capture the stages for the following wavelengths
+      MNP_CUDA(cudaStreamSynchronize(G->st));
+      G->prof.flush();
+      bool ok = true;
+      for (int stage = 0; stage < 5 && ok; ++stage) {
+        if (stage == 3 && precision != MNPBEM_MIXED) continue;
+        ok = capture_stage(G, c, stage) == MNPBEM_OK;
+      }
+      if (ok) {
+        gr.valid = true;
+        gr.precision = precision;
+        gr.P = P;
+        gr.ninf = exc->ninf;
+        gr.prof = G->prof.enabled;
+        gr.gen = alloc_generation();
+      } else {
+        drop_graphs(G);
+        G->use_graphs = false;   // run directly from now on
+      }
+    }
     if (out->ir_iters) out->ir_iters[w] = it;
     if (out->ir_resid) out->ir_resid[w] = res;
-    // field outputs
-    double2* x1 = G->vec64.as<double2>() + 8 * n * P;
-    double2* x2 = x1 + 4 * n * P;
-    const cudaMemcpyKind kind = out->outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    const size_t cs = sizeof(double2);
+    // outputs of this wavelength
+    Vec64 v = vec64(G, P);
     auto cp2 = [&](double* dst, const double2* src, int off, int width) -> mnpbem_status {
       if (!dst) return MNPBEM_OK;
       MNP_CUDA(cudaMemcpy2DAsync(dst + 2 * (size_t)w * n * width, cs * width, src + off, cs * 4 * P,
                                  cs * width, n, kind, G->st));
       return MNPBEM_OK;
     };
-    MNP_TRY(cp2(out->sig1, x1, 0, P));
-    MNP_TRY(cp2(out->h1, x1, P, 3 * P));
-    MNP_TRY(cp2(out->sig2, x2, 0, P));
-    MNP_TRY(cp2(out->h2, x2, P, 3 * P));
+    MNP_TRY(cp2(out->sig1, v.x1, 0, P));
+    MNP_TRY(cp2(out->h1, v.x1, P, 3 * P));
+    MNP_TRY(cp2(out->sig2, v.x2, 0, P));
+    MNP_TRY(cp2(out->h2, v.x2, P, 3 * P));
+    const double* slot = G->outbuf.as<double>();
+    if (out->ext) MNP_CUDA(cudaMemcpyAsync(out->ext + (size_t)w * P, slot, sizeof(double) * P, kind, G->st));
+    if (out->sca) MNP_CUDA(cudaMemcpyAsync(out->sca + (size_t)w * P, slot + P, sizeof(double) * P, kind, G->st));
+    if (precision == MNPBEM_FP64 && graphs) {
+      MNP_CUDA(cudaStreamSynchronize(G->st));
+      G->prof.flush();
+      MNP_TRY(check_pivots(G));
+    }
   }
-  const cudaMemcpyKind kind = out->outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  if (out->ext) MNP_CUDA(cudaMemcpyAsync(out->ext, dext, sizeof(double) * P * nenei, kind, G->st));
-  if (out->sca) MNP_CUDA(cudaMemcpyAsync(out->sca, dsca, sizeof(double) * P * nenei, kind, G->st));
   MNP_CUDA(cudaStreamSynchronize(G->st));
   G->prof.flush();
+  MNP_TRY(check_pivots(G));
+  if (precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(G->tc, G->st));
   return MNPBEM_OK;
 }
 
@@ -757,15 +997,13 @@ mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps
   MNP_CUDA(cudaSetDevice(G->device));
   ProfBind pb_(&G->prof);
   const int64_t n = G->g.n, ld = G->ld;
-  MNP_TRY(ensure_workspace(G, precision, 1));
-  SolveCtx c;
-  c.G = G; c.P = 1; c.enei = enei; c.k0 = 2 * M_PI / enei;
-  c.kmed.resize(nmed);
-  for (int m = 0; m < nmed; ++m) c.kmed[m] = 2 * M_PI / enei * std::sqrt(cx(eps_media + 2 * m));
-  MNP_TRY(prepare_faces(G, c, eps_media, nmed));
-  MNP_TRY(assemble_into(G, c, precision));
-  if (precision == MNPBEM_FP64) MNP_TRY(initmat<double>(G, c));
-  else MNP_TRY(initmat<float>(G, c));
+  MNP_TRY(ensure_workspace(G, precision, 1, 0));
+  LamParams lp;
+  fill_lp(lp, enei, eps_media, nmed, 1, 0);
+  MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, G->st));
+  MNP_TRY(stage_assemble(G, precision));
+  if (precision == MNPBEM_FP64) MNP_TRY(stage_initmat<double>(G, true));
+  else MNP_TRY(stage_initmat<float>(G, true));
   double* outs[5] = {G1i, G2i, Sigmai, Deltai, Sigma1};  // order of mat[0..4]
   DevBuf conv;
   if (precision == MNPBEM_MIXED) MNP_TRY(conv.ensure(sizeof(double2) * n * ld));
@@ -781,6 +1019,7 @@ mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps
                                sizeof(double2) * n, n, cudaMemcpyDeviceToHost, G->st));
     MNP_CUDA(cudaStreamSynchronize(G->st));
   }
+  G->prof.flush();
   return MNPBEM_OK;
 }
 

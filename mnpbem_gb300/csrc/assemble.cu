@@ -76,10 +76,10 @@ __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
     int pi = p.part[i];
     int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
     double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
-    if (m11) { PairVal v = far_pair(p.k[m11 - 1], dd, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
-    if (m21) { PairVal v = far_pair(p.k[m21 - 1], dd, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
-    if (m22) { PairVal v = far_pair(p.k[m22 - 1], dd, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
-    if (m12) { PairVal v = far_pair(p.k[m12 - 1], dd, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
+    if (m11) { PairVal v = far_pair(p.lp->k[m11 - 1], dd, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
+    if (m21) { PairVal v = far_pair(p.lp->k[m21 - 1], dd, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
+    if (m22) { PairVal v = far_pair(p.lp->k[m22 - 1], dd, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
+    if (m12) { PairVal v = far_pair(p.lp->k[m12 - 1], dd, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
     store4<W64, W32>(p, i, j, g1, h1, g2, h2);
   }
 }
@@ -124,10 +124,10 @@ __global__ void k_asm_near(AsmParams p) {
   int pi = p.part[i], pj = p.part[j];
   int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
   double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
-  if (m11) { PairVal v = near_pair(p, e, p.k[m11 - 1], dd, ni); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
-  if (m21) { PairVal v = near_pair(p, e, p.k[m21 - 1], dd, ni); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
-  if (m22) { PairVal v = near_pair(p, e, p.k[m22 - 1], dd, ni); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
-  if (m12) { PairVal v = near_pair(p, e, p.k[m12 - 1], dd, ni); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
+  if (m11) { PairVal v = near_pair(p, e, p.lp->k[m11 - 1], dd, ni); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
+  if (m21) { PairVal v = near_pair(p, e, p.lp->k[m21 - 1], dd, ni); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
+  if (m22) { PairVal v = near_pair(p, e, p.lp->k[m22 - 1], dd, ni); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
+  if (m12) { PairVal v = near_pair(p, e, p.lp->k[m12 - 1], dd, ni); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
   store4<W64, W32>(p, i, j, g1, h1, g2, h2);
 }
 

@@ -19,7 +19,7 @@ struct AsmParams {
   const int* ref_col = nullptr;
   const double* ref_g = nullptr;
   const double* ref_f = nullptr;
-  double2 k[ASM_MAXMED];
+  const LamParams* lp = nullptr;   // wavenumbers of the media (device)
   // media (1-based, 0 = block not connected) of the four connectivity
   // blocks: 0 -> con{1,1} (+G1), 1 -> con{2,1} (-G1), 2 -> con{2,2} (+G2), 3 -> con{1,2} (-G2)
   signed char med[4][ASM_MAXP][ASM_MAXP];

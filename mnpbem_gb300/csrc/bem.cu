@@ -11,10 +11,12 @@ template <typename R> __device__ __forceinline__ cplx<R> cvt(double2 v) { return
 
 // ------------------------------------------------------------- excitation
 __global__ void k_excitation(FaceData f, int P, const double* __restrict__ pol,
-                             const double* __restrict__ dir, double2 k, double k0, double2* phi,
-                             double2* a, double2* alpha, double2* De) {
+                             const double* __restrict__ dir, const LamParams* __restrict__ lp,
+                             double2* phi, double2* a, double2* alpha, double2* De) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.n) return;
+  const double2 k = lp->kexc;
+  const double k0 = lp->k0;
   double px = f.pos[3 * i], py = f.pos[3 * i + 1], pz = f.pos[3 * i + 2];
   double nx = f.nvec[3 * i], ny = f.nvec[3 * i + 1], nz = f.nvec[3 * i + 2];
   bool in1 = f.exc_in[i] != 0, in2 = f.exc_out[i] != 0;
@@ -51,10 +53,32 @@ __global__ void k_excitation(FaceData f, int P, const double* __restrict__ pol,
 }
 
 void launch_excitation(const FaceData& f, int P, const double* pol, const double* dir,
-                       double2 k_med, double k0, double2* phi, double2* a, double2* alpha,
+                       const LamParams* lp, double2* phi, double2* a, double2* alpha,
                        double2* De, cudaStream_t st) {
   ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
-  k_excitation<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, pol, dir, k_med, k0, phi, a, alpha, De);
+  k_excitation<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, pol, dir, lp, phi, a, alpha, De);
+}
+
+__global__ void k_face_eps(int64_t n, const int* __restrict__ med_in, const int* __restrict__ med_out,
+                           const LamParams* __restrict__ lp, const double* __restrict__ nvec, double2* eps1,
+                           double2* eps2, float2* eps1f, float2* eps2f, float2* Lf, float* nvecf) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 a = lp->eps[med_in[i]], b = lp->eps[med_out[i]];
+  eps1[i] = a;
+  eps2[i] = b;
+  eps1f[i] = to_f(a);
+  eps2f[i] = to_f(b);
+  Lf[i] = to_f(csub(a, b));
+  for (int c = 0; c < 3; ++c) nvecf[3 * i + c] = (float)nvec[3 * i + c];
+}
+
+void launch_face_eps(int64_t n, const int* med_in, const int* med_out, const LamParams* lp,
+                     const double* nvec, double2* eps1, double2* eps2, float2* eps1f, float2* eps2f,
+                     float2* Lf, float* nvecf, cudaStream_t st) {
+  ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
+  k_face_eps<<<(unsigned)cdiv_up(n, 256), 256, 0, st>>>(n, med_in, med_out, lp, nvec, eps1, eps2, eps1f,
+                                                         eps2f, Lf, nvecf);
 }
 
 // ------------------------------------------------------ mldivide chain steps
@@ -70,7 +94,7 @@ __global__ void k_chain_pre(FaceData f, int P, const cplx<R>* phi, const cplx<R>
 
 // alpha' = alpha - Sigma1 a + ik n (x) (L1 phi);  De' = De - Sigma1 (L1 phi) + ik n . (L1 a)
 template <typename R>
-__global__ void k_chain_alpha_de(FaceData f, int P, R k0, const cplx<R>* phi, const cplx<R>* a,
+__global__ void k_chain_alpha_de(FaceData f, int P, const LamParams* lp, const cplx<R>* phi, const cplx<R>* a,
                                  const cplx<R>* alpha, const cplx<R>* De, const cplx<R>* T4,
                                  cplx<R>* al, cplx<R>* Dp) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -78,7 +102,7 @@ __global__ void k_chain_alpha_de(FaceData f, int P, R k0, const cplx<R>* phi, co
   cplx<R> L1 = cvt<R>(f.eps1[i]);
   R n[3] = {(R)f.nvec[3 * i], (R)f.nvec[3 * i + 1], (R)f.nvec[3 * i + 2]};
   const int W = 4 * P;
-  cplx<R> ik = mk<R>(0, k0);
+  cplx<R> ik = mk<R>(0, (R)lp->k0);
   for (int p = 0; p < P; ++p) {
     cplx<R> lphi = cmul(L1, phi[i * P + p]);
     cplx<R> na = mk<R>(0, 0);
@@ -96,12 +120,12 @@ __global__ void k_chain_alpha_de(FaceData f, int P, R k0, const cplx<R>* phi, co
 
 // u = De' + ik n . ((L1 - L2) t)
 template <typename R>
-__global__ void k_chain_u(FaceData f, int P, R k0, const cplx<R>* Dp, const cplx<R>* t3, cplx<R>* u) {
+__global__ void k_chain_u(FaceData f, int P, const LamParams* lp, const cplx<R>* Dp, const cplx<R>* t3, cplx<R>* u) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.n) return;
   cplx<R> L = csub(cvt<R>(f.eps1[i]), cvt<R>(f.eps2[i]));
   R n[3] = {(R)f.nvec[3 * i], (R)f.nvec[3 * i + 1], (R)f.nvec[3 * i + 2]};
-  cplx<R> ik = mk<R>(0, k0);
+  cplx<R> ik = mk<R>(0, (R)lp->k0);
   for (int p = 0; p < P; ++p) {
     cplx<R> nt = mk<R>(0, 0);
     for (int c = 0; c < 3; ++c) nt = cadd(nt, cscale(t3[(i * 3 + c) * P + p], n[c]));
@@ -111,12 +135,12 @@ __global__ void k_chain_u(FaceData f, int P, R k0, const cplx<R>* Dp, const cplx
 
 // v = ik n (x) ((L1 - L2) sig2) + alpha'
 template <typename R>
-__global__ void k_chain_v(FaceData f, int P, R k0, const cplx<R>* s2, const cplx<R>* al, cplx<R>* v3) {
+__global__ void k_chain_v(FaceData f, int P, const LamParams* lp, const cplx<R>* s2, const cplx<R>* al, cplx<R>* v3) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= f.n) return;
   cplx<R> L = csub(cvt<R>(f.eps1[i]), cvt<R>(f.eps2[i]));
   R n[3] = {(R)f.nvec[3 * i], (R)f.nvec[3 * i + 1], (R)f.nvec[3 * i + 2]};
-  cplx<R> ik = mk<R>(0, k0);
+  cplx<R> ik = mk<R>(0, (R)lp->k0);
   for (int p = 0; p < P; ++p) {
     cplx<R> ls = cmul(ik, cmul(L, s2[i * P + p]));
     for (int c = 0; c < 3; ++c) {
@@ -144,7 +168,7 @@ __global__ void k_chain_y(int64_t n, int P, const cplx<R>* s2, const cplx<R>* h2
 }
 
 template <typename R>
-mnpbem_status apply_mldivide(const FaceData& f, int P, double k0, const ChainMats<R>& m,
+mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, const ChainMats<R>& m,
                              const cplx<R>* phi, const cplx<R>* a, const cplx<R>* alpha,
                              const cplx<R>* De, cplx<R>* x1, cplx<R>* x2, cplx<R>* work,
                              ChainGemm<R> gemm, void* ctx, cudaStream_t st) {
@@ -167,13 +191,13 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, double k0, const ChainMat
   k_chain_pre<R><<<nb, 128, 0, st>>>(f, P, phi, a, X4);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, 4 * P, n, one, m.Sigma1, m.ld, X4, 4 * P, zero, T4, 4 * P, st, ctx));
-  k_chain_alpha_de<R><<<nb, 128, 0, st>>>(f, P, (R)k0, phi, a, alpha, De, T4, al, Dp);
+  k_chain_alpha_de<R><<<nb, 128, 0, st>>>(f, P, lp, phi, a, alpha, De, T4, al, Dp);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, 3 * P, n, one, m.Deltai, m.ld, al, 3 * P, zero, t3, 3 * P, st, ctx));
-  k_chain_u<R><<<nb, 128, 0, st>>>(f, P, (R)k0, Dp, t3, u);
+  k_chain_u<R><<<nb, 128, 0, st>>>(f, P, lp, Dp, t3, u);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, P, n, one, m.Sigmai, m.ld, u, P, zero, s2, P, st, ctx));
-  k_chain_v<R><<<nb, 128, 0, st>>>(f, P, (R)k0, s2, al, v3);
+  k_chain_v<R><<<nb, 128, 0, st>>>(f, P, lp, s2, al, v3);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, 3 * P, n, one, m.Deltai, m.ld, v3, 3 * P, zero, h2, 3 * P, st, ctx));
   k_chain_y<R><<<nb, 128, 0, st>>>(n, P, s2, h2, phi, a, Y4, Z4);
@@ -182,11 +206,11 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, double k0, const ChainMat
   MNP_TRY(gemm(n, 4 * P, n, one, m.G2i, m.ld, Z4, 4 * P, zero, x2, 4 * P, st, ctx));
   return MNPBEM_OK;
 }
-template mnpbem_status apply_mldivide<float>(const FaceData&, int, double, const ChainMats<float>&,
+template mnpbem_status apply_mldivide<float>(const FaceData&, int, const LamParams*, const ChainMats<float>&,
                                              const float2*, const float2*, const float2*,
                                              const float2*, float2*, float2*, float2*,
                                              ChainGemm<float>, void*, cudaStream_t);
-template mnpbem_status apply_mldivide<double>(const FaceData&, int, double, const ChainMats<double>&,
+template mnpbem_status apply_mldivide<double>(const FaceData&, int, const LamParams*, const ChainMats<double>&,
                                               const double2*, const double2*, const double2*,
                                               const double2*, double2*, double2*, double2*,
                                               ChainGemm<double>, void*, cudaStream_t);
@@ -203,7 +227,7 @@ __device__ __forceinline__ void block_add2(double v0, double v1, double* norms) 
   }
 }
 
-__global__ void k_residual(FaceData f, int P, double k0, const double2* Y1, const double2* Y2,
+__global__ void k_residual(FaceData f, int P, const LamParams* lp, const double2* Y1, const double2* Y2,
                            const double2* Z1, const double2* Z2, const double2* phi,
                            const double2* a, const double2* alpha, const double2* De,
                            double2* rphi, double2* ra, double2* ralpha, double2* rDe,
@@ -214,7 +238,7 @@ __global__ void k_residual(FaceData f, int P, double k0, const double2* Y1, cons
     const int W = 4 * P;
     double2 e1 = f.eps1[i], e2 = f.eps2[i];
     double n[3] = {f.nvec[3 * i], f.nvec[3 * i + 1], f.nvec[3 * i + 2]};
-    double2 ik = make_double2(0, k0);
+    double2 ik = make_double2(0, lp->k0);
     for (int p = 0; p < P; ++p) {
       double2 y1s = Y1[i * W + p], y2s = Y2[i * W + p];
       double2 z1s = Z1[i * W + p], z2s = Z2[i * W + p];
@@ -244,12 +268,12 @@ __global__ void k_residual(FaceData f, int P, double k0, const double2* Y1, cons
   block_add2(rr, bb, norms);
 }
 
-void launch_residual(const FaceData& f, int P, double k0, const double2* Y1, const double2* Y2,
+void launch_residual(const FaceData& f, int P, const LamParams* lp, const double2* Y1, const double2* Y2,
                      const double2* Z1, const double2* Z2, const double2* phi, const double2* a,
                      const double2* alpha, const double2* De, double2* rphi, double2* ra,
                      double2* ralpha, double2* rDe, double* norms, cudaStream_t st) {
   ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
-  k_residual<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, k0, Y1, Y2, Z1, Z2, phi, a, alpha,
+  k_residual<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, lp, Y1, Y2, Z1, Z2, phi, a, alpha,
                                                          De, rphi, ra, ralpha, rDe, norms);
 }
 
@@ -293,57 +317,76 @@ void launch_axpy_norm(double2* x, const double2* dx, int64_t count, double* norm
 }
 
 // ------------------------------------------------------------ Sigma stage
+// per-face values in the working precision of the kernel
+template <typename R> struct FaceVals;
+template <> struct FaceVals<float> {
+  const float2 *e1, *e2, *L;
+  const float* nv;
+  __host__ explicit FaceVals(const FaceData& f) : e1(f.eps1f), e2(f.eps2f), L(f.Lf), nv(f.nvecf) {}
+};
+template <> struct FaceVals<double> {
+  const double2 *e1, *e2;
+  const double* nv;
+  __host__ explicit FaceVals(const FaceData& f) : e1(f.eps1), e2(f.eps2), nv(f.nvec) {}
+};
+__device__ __forceinline__ float2 face_L(const FaceVals<float>& v, int64_t i) { return v.L[i]; }
+__device__ __forceinline__ double2 face_L(const FaceVals<double>& v, int64_t i) { return csub(v.e1[i], v.e2[i]); }
+
 template <typename R>
 __global__ void k_delta_sigma(int64_t n, const cplx<R>* S1, cplx<R>* S2, cplx<R>* D, int64_t ld,
-                              const double2* e1, const double2* e2) {
+                              FaceVals<R> fv) {
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t i = blockIdx.y;
   if (j >= n) return;
   cplx<R> s1 = S1[i * ld + j], s2 = S2[i * ld + j];
   D[i * ld + j] = csub(s1, s2);
-  S2[i * ld + j] = csub(cmul(s1, cvt<R>(e1[j])), cmul(s2, cvt<R>(e2[j])));
+  S2[i * ld + j] = csub(cmul(s1, fv.e1[j]), cmul(s2, fv.e2[j]));
 }
 template <typename R>
 void launch_delta_sigma(int64_t n, const cplx<R>* S1, cplx<R>* S2_to_S, cplx<R>* D, int64_t ld,
-                        const double2* e1, const double2* e2, cudaStream_t st) {
+                        const FaceData& f, cudaStream_t st) {
   ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
   dim3 grid((unsigned)cdiv_up(n, 256), (unsigned)n);
-  k_delta_sigma<R><<<grid, 256, 0, st>>>(n, S1, S2_to_S, D, ld, e1, e2);
+  k_delta_sigma<R><<<grid, 256, 0, st>>>(n, S1, S2_to_S, D, ld, FaceVals<R>(f));
 }
-template void launch_delta_sigma<float>(int64_t, const float2*, float2*, float2*, int64_t,
-                                        const double2*, const double2*, cudaStream_t);
+template void launch_delta_sigma<float>(int64_t, const float2*, float2*, float2*, int64_t, const FaceData&,
+                                        cudaStream_t);
 template void launch_delta_sigma<double>(int64_t, const double2*, double2*, double2*, int64_t,
-                                         const double2*, const double2*, cudaStream_t);
+                                         const FaceData&, cudaStream_t);
 
+// S_ij += k0^2 L_i Deltai_ij (n_i . n_j) L_j
 template <typename R>
-__global__ void k_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, const double2* e1,
-                            const double2* e2, const double* nvec, double k2) {
+__global__ void k_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, FaceVals<R> fv,
+                            const LamParams* lp) {
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t i = blockIdx.y;
   if (j >= n) return;
-  double2 Li = csub(e1[i], e2[i]), Lj = csub(e1[j], e2[j]);
-  double nn = nvec[3 * i] * nvec[3 * j] + nvec[3 * i + 1] * nvec[3 * j + 1] + nvec[3 * i + 2] * nvec[3 * j + 2];
-  cplx<R> t = cmul(cmul(cvt<R>(Li), Di[i * ld + j]), mk<R>((R)nn, 0));
-  t = cmul(t, cvt<R>(Lj));
-  S[i * ld + j] = cadd(S[i * ld + j], cscale(t, (R)k2));
+  const R k2 = (R)(lp->k0 * lp->k0);
+  const cplx<R> Li = face_L(fv, i), Lj = face_L(fv, j);
+  const R nn = fv.nv[3 * i] * fv.nv[3 * j] + fv.nv[3 * i + 1] * fv.nv[3 * j + 1] + fv.nv[3 * i + 2] * fv.nv[3 * j + 2];
+  cplx<R> t = cmul(cmul(Li, Di[i * ld + j]), mk<R>(nn, 0));
+  t = cmul(t, Lj);
+  S[i * ld + j] = cadd(S[i * ld + j], cscale(t, k2));
 }
 template <typename R>
-void launch_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, const double2* e1,
-                      const double2* e2, const double* nvec, double k0, cudaStream_t st) {
+void launch_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, const FaceData& f,
+                      const LamParams* lp, cudaStream_t st) {
   ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
   dim3 grid((unsigned)cdiv_up(n, 256), (unsigned)n);
-  k_sigma_add<R><<<grid, 256, 0, st>>>(n, S, Di, ld, e1, e2, nvec, k0 * k0);
+  k_sigma_add<R><<<grid, 256, 0, st>>>(n, S, Di, ld, FaceVals<R>(f), lp);
 }
-template void launch_sigma_add<float>(int64_t, float2*, const float2*, int64_t, const double2*,
-                                      const double2*, const double*, double, cudaStream_t);
-template void launch_sigma_add<double>(int64_t, double2*, const double2*, int64_t, const double2*,
-                                       const double2*, const double*, double, cudaStream_t);
+template void launch_sigma_add<float>(int64_t, float2*, const float2*, int64_t, const FaceData&,
+                                      const LamParams*, cudaStream_t);
+template void launch_sigma_add<double>(int64_t, double2*, const double2*, int64_t, const FaceData&,
+                                       const LamParams*, cudaStream_t);
 
 // ------------------------------------------------------------- far fields
 __global__ void __launch_bounds__(256) k_farfield(FaceData f, int P, const double2* x1,
                                                   const double2* x2, const double* dirs,
-                                                  double2 k, double k0, double2* fields) {
+                                                  const LamParams* lp, double2* fields) {
   const int d = blockIdx.x;
+  const double2 k = lp->kexc;
+  const double k0 = lp->k0;
   const double dx = dirs[3 * d], dy = dirs[3 * d + 1], dz = dirs[3 * d + 2];
   double2 Ps[MAXPOL], Ph[3][MAXPOL];
   for (int p = 0; p < MAXPOL; ++p) {
@@ -416,15 +459,16 @@ __global__ void __launch_bounds__(256) k_farfield(FaceData f, int P, const doubl
 }
 
 void launch_farfield(const FaceData& f, int P, const double2* x1, const double2* x2,
-                     const double* dirs, int ndir, double2 k_med, double k0, double2* fields,
+                     const double* dirs, int ndir, const LamParams* lp, double2* fields,
                      cudaStream_t st) {
   ProfScope ps_(PH_SPECTRA, st, 0.0, 0.0, 1);
-  k_farfield<<<ndir, 256, 0, st>>>(f, P, x1, x2, dirs, k_med, k0, fields);
+  k_farfield<<<ndir, 256, 0, st>>>(f, P, x1, x2, dirs, lp, fields);
 }
 
-__global__ void k_cross_sections(int P, const double* pol, const double* inf_nvec,
-                                 const double* inf_area, int ninf, const double2* fields,
-                                 double2 k, double2 nb1, double* ext, double* sca) {
+__device__ __forceinline__ void cross_sections_body(int P, const double* pol, const double* inf_nvec,
+                                                    const double* inf_area, int ninf,
+                                                    const double2* fields, double2 k, double2 nb1,
+                                                    double* ext, double* sca) {
   __shared__ double red[256];
   for (int p = 0; p < P; ++p) {
     double acc = 0.0;
@@ -458,6 +502,27 @@ __global__ void k_cross_sections(int P, const double* pol, const double* inf_nve
     }
     __syncthreads();
   }
+}
+
+__global__ void k_cross_sections(int P, const double* pol, const double* inf_nvec,
+                                 const double* inf_area, int ninf, const double2* fields,
+                                 double2 k, double2 nb1, double* ext, double* sca) {
+  cross_sections_body(P, pol, inf_nvec, inf_area, ninf, fields, k, nb1, ext, sca);
+}
+
+__global__ void k_cross_sections_lp(int P, const double* pol, const double* inf_nvec,
+                                    const double* inf_area, int ninf, const double2* fields,
+                                    const LamParams* lp, double* ext, double* sca) {
+  const int w = lp->w;
+  cross_sections_body(P, pol, inf_nvec, inf_area, ninf, fields, lp->kexc, lp->nb1, ext + (int64_t)w * P,
+                      sca + (int64_t)w * P);
+}
+
+void launch_cross_sections_lp(int P, const double* pol, const double* inf_nvec,
+                              const double* inf_area, int ninf, const double2* fields,
+                              const LamParams* lp, double* ext, double* sca, cudaStream_t st) {
+  ProfScope ps_(PH_SPECTRA, st, 0.0, 0.0, 1);
+  k_cross_sections_lp<<<1, 256, 0, st>>>(P, pol, inf_nvec, inf_area, ninf, fields, lp, ext, sca);
 }
 
 void launch_cross_sections(int P, const double* pol, const double* inf_nvec, const double* inf_area,

@@ -13,6 +13,11 @@ struct FaceData {
   const double2* eps2 = nullptr; // [n] outside
   const unsigned char* exc_in = nullptr;   // [n] inside medium == excitation medium
   const unsigned char* exc_out = nullptr;  // [n] outside medium == excitation medium
+  // complex64 copies for the complex64 kernels: eps1, eps2, L = eps1 - eps2, nvec
+  const float2* eps1f = nullptr;
+  const float2* eps2f = nullptr;
+  const float2* Lf = nullptr;
+  const float* nvecf = nullptr;   // [n][3]
 };
 
 // Right-hand side / solution sets of P polarisations:
@@ -26,8 +31,14 @@ struct Fields {
 // planewaveret potential (potential.m:13-57) + bemret excitation (excitation.m:4-29):
 // phi [n][P] (= 0), a, alpha [n][3][P], De [n][P]  (FP64)
 void launch_excitation(const FaceData& f, int P, const double* pol, const double* dir,
-                       double2 k_med, double k0, double2* phi, double2* a, double2* alpha,
+                       const LamParams* lp, double2* phi, double2* a, double2* alpha,
                        double2* De, cudaStream_t st);
+
+// per-face dielectric functions eps1 (inside) / eps2 (outside) of this wavelength,
+// plus their complex64 copies, L = eps1 - eps2 and the normals in FP32
+void launch_face_eps(int64_t n, const int* med_in, const int* med_out, const LamParams* lp,
+                     const double* nvec, double2* eps1, double2* eps2, float2* eps1f, float2* eps2f,
+                     float2* Lf, float* nvecf, cudaStream_t st);
 
 template <typename R> struct ChainMats {
   const cplx<R>* G1i; const cplx<R>* G2i; const cplx<R>* Sigma1; const cplx<R>* Deltai;
@@ -41,9 +52,9 @@ using ChainGemm = mnpbem_status (*)(int64_t M, int64_t N, int64_t K, cplx<R> alp
                                     void* ctx);
 
 // mldivide.m:12-49 in precision R.  in: phi, a, alpha, De; out: x1 = [sig1 | h1],
-// x2 = [sig2 | h2] as [n][4P].  work must hold 24 n P complex values.
+// x2 = [sig2 | h2] as [n][4P].  work must hold 32 n P complex values.
 template <typename R>
-mnpbem_status apply_mldivide(const FaceData& f, int P, double k0, const ChainMats<R>& m,
+mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, const ChainMats<R>& m,
                              const cplx<R>* phi, const cplx<R>* a, const cplx<R>* alpha,
                              const cplx<R>* De, cplx<R>* x1, cplx<R>* x2, cplx<R>* work,
                              ChainGemm<R> gemm, void* ctx, cudaStream_t st);
@@ -51,7 +62,7 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, double k0, const ChainMat
 // r = b - A x with the full BEM operator (BEM/@bemretiter/private/afun.m:6-35), FP64.
 // Y1 = G1 x1, Y2 = G2 x2, Z1 = H1 x1, Z2 = H2 x2 already computed ([n][4P]).
 // Outputs r_phi, r_a, r_alpha, r_De; accumulates ||r||^2 and ||b||^2 into norms[0..1].
-void launch_residual(const FaceData& f, int P, double k0, const double2* Y1, const double2* Y2,
+void launch_residual(const FaceData& f, int P, const LamParams* lp, const double2* Y1, const double2* Y2,
                      const double2* Z1, const double2* Z2, const double2* phi, const double2* a,
                      const double2* alpha, const double2* De, double2* rphi, double2* ra,
                      double2* ralpha, double2* rDe, double* norms, cudaStream_t st);
@@ -67,20 +78,24 @@ void launch_axpy_norm(double2* x, const double2* dx, int64_t count, double* norm
 //   S += k^2 diag(L) (Deltai o (n n^T)) diag(L), L = e1 - e2   (launch_sigma_add)
 template <typename R>
 void launch_delta_sigma(int64_t n, const cplx<R>* S1, cplx<R>* S2_to_S, cplx<R>* D, int64_t ld,
-                        const double2* e1, const double2* e2, cudaStream_t st);
+                        const FaceData& f, cudaStream_t st);
 template <typename R>
-void launch_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, const double2* e1,
-                      const double2* e2, const double* nvec, double k0, cudaStream_t st);
+void launch_sigma_add(int64_t n, cplx<R>* S, const cplx<R>* Di, int64_t ld, const FaceData& f,
+                      const LamParams* lp, cudaStream_t st);
 
 // Far fields and cross sections (farfield.m:15-74, scattering.m, extinction.m).
 // dirs [ndir][3]: first P rows are the excitation directions (extinction),
 // the remaining ninf rows the sphere at infinity with weights inf_area.
 // fields: scratch of ndir * 6 * P complex values.
 void launch_farfield(const FaceData& f, int P, const double2* x1, const double2* x2,
-                     const double* dirs, int ndir, double2 k_med, double k0, double2* fields,
+                     const double* dirs, int ndir, const LamParams* lp, double2* fields,
                      cudaStream_t st);
 void launch_cross_sections(int P, const double* pol, const double* inf_nvec, const double* inf_area,
                            int ninf, const double2* fields, double2 k_med, double2 nb1,
                            double* ext, double* sca, cudaStream_t st);
+// same, with k_med / nb1 from lp and outputs at ext + lp->w * P, sca + lp->w * P
+void launch_cross_sections_lp(int P, const double* pol, const double* inf_nvec,
+                              const double* inf_area, int ninf, const double2* fields,
+                              const LamParams* lp, double* ext, double* sca, cudaStream_t st);
 
 }  // namespace mnpbem

@@ -79,10 +79,28 @@ template <typename C> __host__ __device__ __forceinline__ C from_d(double2 a);
 template <> __host__ __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
 template <> __host__ __device__ __forceinline__ float2 from_d<float2>(double2 a) { return to_f(a); }
 
+// Per-wavelength scalars, kept in device memory so that the kernels of one
+// wavelength can be captured once in CUDA graphs and replayed for the next.
+constexpr int LAM_MAXMED = 16;
+struct LamParams {
+  double2 k[LAM_MAXMED];    // wavenumber 2 pi / enei sqrt(eps_m) of each medium
+  double2 eps[LAM_MAXMED];  // dielectric function of each medium
+  double2 kexc;             // wavenumber in the excitation medium
+  double2 nb1;              // refractive index sqrt(eps_1) of medium 1
+  double k0;                // vacuum wavenumber 2 pi / enei
+  int w;                    // index of the wavelength in the sweep (output slot)
+  int pad;
+};
+
 inline int64_t cdiv_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return cdiv_up(a, b) * b; }
 
 // ------------------------------------------------------- device buffers
+// Every (re)allocation bumps alloc_generation(), which invalidates CUDA graphs
+// that captured buffer addresses; during a capture no allocation may happen.
+uint64_t& alloc_generation();
+bool& capturing_now();
+
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
@@ -96,7 +114,12 @@ struct DevBuf {
   }
   mnpbem_status ensure(size_t nbytes) {
     if (bytes >= nbytes && ptr) return MNPBEM_OK;
+    if (capturing_now()) {
+      set_error("internal: device allocation of %zu bytes requested during graph capture", nbytes);
+      return MNPBEM_ERR_CUDA;
+    }
     release();
+    ++alloc_generation();
     if (nbytes == 0) return MNPBEM_OK;
     cudaError_t e = cudaMalloc(&ptr, nbytes);
     if (e != cudaSuccess) {

@@ -72,11 +72,91 @@ __global__ void __launch_bounds__(256) k_gemm_nn(int64_t M, int64_t N, int64_t K
   }
 }
 
+// ------------------------------------------------------- thin GEMM (N <= 16)
+// Matrix times a few vectors: memory-bound on A.  Each warp owns THIN_ROWS rows
+// and strides over K with coalesced loads of A; chunks of B are staged in
+// shared memory transposed (Bs[n][k]) so that lanes read consecutive k.
+constexpr int THIN_NMAX = 16, THIN_ROWS = 2, THIN_KC = 128, THIN_WARPS = 8;
+
+template <typename R, int N>
+__global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin(int64_t M, int64_t K, cplx<R> alpha,
+                                                             const cplx<R>* __restrict__ A, int64_t lda,
+                                                             const cplx<R>* __restrict__ B, int64_t ldb,
+                                                             cplx<R> beta, cplx<R>* __restrict__ C,
+                                                             int64_t ldc) {
+  using Cx = cplx<R>;
+  __shared__ Cx Bs[N][THIN_KC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = ((int64_t)blockIdx.x * THIN_WARPS + warp) * THIN_ROWS;
+  Cx acc[THIN_ROWS][N];
+#pragma unroll
+  for (int r = 0; r < THIN_ROWS; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) acc[r][c] = mk<R>(0, 0);
+  for (int64_t k0 = 0; k0 < K; k0 += THIN_KC) {
+    const int kc = (int)((K - k0) < THIN_KC ? (K - k0) : THIN_KC);
+    __syncthreads();
+    for (int l = threadIdx.x; l < kc * N; l += blockDim.x) {
+      int kk = l / N, c = l % N;
+      Bs[c][kk] = B[(k0 + kk) * ldb + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < THIN_ROWS; ++r) {
+      const int64_t row = row0 + r;
+      if (row >= M) continue;
+      const Cx* arow = A + row * lda + k0;
+#pragma unroll 4
+      for (int kk = lane; kk < kc; kk += 32) {
+        const Cx a = arow[kk];
+#pragma unroll
+        for (int c = 0; c < N; ++c) cfma(acc[r][c], a, Bs[c][kk]);
+      }
+    }
+  }
+  const bool zero_beta = (beta.x == 0 && beta.y == 0);
+#pragma unroll
+  for (int r = 0; r < THIN_ROWS; ++r) {
+    const int64_t row = row0 + r;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      Cx v = acc[r][c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == c && row < M) {
+        Cx out = cmul(alpha, v);
+        if (!zero_beta) out = cadd(out, cmul(beta, C[row * ldc + c]));
+        C[row * ldc + c] = out;
+      }
+    }
+  }
+}
+
 template <typename R>
 mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cplx<R>* A,
                         int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta, cplx<R>* C,
                         int64_t ldc, cudaStream_t st) {
   if (M <= 0 || N <= 0) return MNPBEM_OK;
+  if (N <= THIN_NMAX && K > 0) {
+    ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K,
+                 (double)sizeof(cplx<R>) * ((double)M * K + (double)K * N + 2.0 * M * N));
+    const int64_t rows_per_block = (int64_t)THIN_ROWS * THIN_WARPS;
+    const unsigned nblk = (unsigned)cdiv_up(M, rows_per_block);
+#define THIN_CASE(NN)                                                                           \
+  case NN:                                                                                      \
+    k_gemm_thin<R, NN><<<nblk, 32 * THIN_WARPS, 0, st>>>(M, K, alpha, A, lda, B, ldb, beta, C, ldc); \
+    break;
+    switch (N) {
+      THIN_CASE(1) THIN_CASE(2) THIN_CASE(3) THIN_CASE(4) THIN_CASE(5) THIN_CASE(6) THIN_CASE(7)
+      THIN_CASE(8) THIN_CASE(9) THIN_CASE(10) THIN_CASE(11) THIN_CASE(12) THIN_CASE(13) THIN_CASE(14)
+      THIN_CASE(15) THIN_CASE(16)
+    }
+#undef THIN_CASE
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
   dim3 grid((unsigned)cdiv_up(N, 64), (unsigned)cdiv_up(M, 64));
   if (grid.y > 65535) { set_error("gemm_simt: M too large"); return MNPBEM_ERR_INVALID_ARG; }
   constexpr int BK = sizeof(R) == 4 ? 16 : 8;
@@ -93,51 +173,95 @@ template mnpbem_status gemm_simt<double>(int64_t, int64_t, int64_t, double2, con
                                          const double2*, int64_t, double2, double2*, int64_t,
                                          cudaStream_t);
 
-// --------------------------------------------------- block inversion (smem)
-// In-place Gauss-Jordan of one w x w block (w <= 64) held in shared memory.
+// --------------------------------------------------- block inversion
+// In-place Gauss-Jordan of one w x w block (w <= 64).  256 threads as a 16 x 16
+// grid; thread (ty, tx) keeps the 16 entries (ty + 16 i, tx + 16 j) in
+// registers.  Each pivot step publishes the pivot row and column through a
+// double-buffered shared array, so one __syncthreads per step suffices.
 template <typename R>
 __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A, int64_t lda, int w,
                                                    cplx<R>* __restrict__ X, int64_t ldx, int* status) {
   using Cx = cplx<R>;
-  extern __shared__ unsigned char smem_raw[];
-  Cx* S = reinterpret_cast<Cx*>(smem_raw);      // [w][w+1]
-  Cx* prow = S + w * (w + 1);
-  Cx* pcol = prow + w;
-  const int ws = w + 1;
-  const int t = threadIdx.x;
-  for (int l = t; l < w * w; l += blockDim.x) {
-    int r = l / w, c = l % w;
-    S[r * ws + c] = A[r * lda + c];
-  }
+  __shared__ Cx prow[2][64], pcol[2][64];
+  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+  Cx a[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = ty + 16 * i, c = tx + 16 * j;
+      a[i][j] = (r < w && c < w) ? A[r * lda + c] : mk<R>(r == c ? 1 : 0, 0);
+    }
+  // publish pivot row / column 0
+  const auto publish = [&](int p, int buf) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = ty + 16 * i, c = tx + 16 * j;
+        if (r == p) prow[buf][c] = a[i][j];
+        if (c == p) pcol[buf][r] = a[i][j];
+      }
+  };
+  publish(0, 0);
   __syncthreads();
   for (int p = 0; p < w; ++p) {
-    if (t < w) { prow[t] = S[p * ws + t]; pcol[t] = S[t * ws + p]; }
-    __syncthreads();
-    Cx piv = prow[p];
-    double a2 = cabs2(piv);
-    if (t == 0 && !(a2 > 1e-280 && a2 < 1e280)) atomicOr(status, 1);
-    Cx inv = cdiv(mk<R>(1, 0), piv);
-    for (int l = t; l < w * w; l += blockDim.x) {
-      int r = l / w, c = l % w;
-      Cx v;
-      if (r == p && c == p) v = inv;
-      else if (r == p) v = cmul(prow[c], inv);
-      else if (c == p) { v = cmul(pcol[r], inv); v.x = -v.x; v.y = -v.y; }
-      else v = csub(S[r * ws + c], cmul(pcol[r], cmul(prow[c], inv)));
-      S[r * ws + c] = v;
+    const int buf = p & 1;
+    const Cx piv = prow[buf][p];
+    const R n2 = piv.x * piv.x + piv.y * piv.y;
+    if (t == 0 && !(n2 > (R)1e-30 && n2 < (R)1e30)) atomicOr(status, 1);
+    const R rn2 = (R)1 / n2;
+    const Cx inv = mk<R>(piv.x * rn2, -piv.y * rn2);
+    // One update a - pc_r pr_c serves every entry when the pivot column of pr
+    // holds 1 + 1/a_pp and the pivot row of pc holds a_pp - 1:
+    //   row p:    a_pc - (a_pp - 1) a_pc / a_pp = a_pc / a_pp
+    //   column p: a_rp - a_rp (1 + 1/a_pp)      = -a_rp / a_pp
+    // (the pivot itself is set to 1/a_pp directly).
+    Cx pr[4], pc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = tx + 16 * j;
+      pr[j] = (c == p) ? mk<R>(1 + inv.x, inv.y) : cmul(prow[buf][c], inv);
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = ty + 16 * i;
+      pc[i] = (r == p) ? mk<R>(piv.x - 1, piv.y) : pcol[buf][r];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const Cx v = csub(a[i][j], cmul(pc[i], pr[j]));
+        a[i][j] = (ty + 16 * i == p && tx + 16 * j == p) ? inv : v;
+      }
+    if (p + 1 < w) publish(p + 1, buf ^ 1);
     __syncthreads();
   }
-  for (int l = t; l < w * w; l += blockDim.x) {
-    int r = l / w, c = l % w;
-    X[r * ldx + c] = S[r * ws + c];
-  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = ty + 16 * i, c = tx + 16 * j;
+      if (r < w && c < w) X[r * ldx + c] = a[i][j];
+    }
 }
 
 // --------------------------------------------------- blocked Gauss-Jordan
 template <typename R>
+mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st) {
+  host2[0] = host2[1] = 0;
+  if (w.status.ptr) MNP_CUDA(cudaMemcpyAsync(host2, w.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (w.inner && w.inner->status.ptr)
+    MNP_CUDA(cudaMemcpyAsync(host2 + 1, w.inner->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  return MNPBEM_OK;
+}
+template mnpbem_status gj_status_copy<float>(GJWork<float>&, int*, cudaStream_t);
+template mnpbem_status gj_status_copy<double>(GJWork<double>&, int*, cudaStream_t);
+
+template <typename R>
 mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn<R> big_gemm,
-                        void* ctx, cudaStream_t st) {
+                        void* ctx, cudaStream_t st, bool read_status) {
   using Cx = cplx<R>;
   const int nb = w.nb;
   const size_t cs = sizeof(Cx);
@@ -146,32 +270,40 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
   MNP_TRY(w.ncol.ensure(cs * n * nb));
   MNP_TRY(w.xblk.ensure(cs * nb * nb));
   MNP_TRY(w.status.ensure(sizeof(int)));
-  MNP_CUDA(cudaMemsetAsync(w.status.ptr, 0, sizeof(int), st));
+  if (!w.nested) MNP_CUDA(cudaMemsetAsync(w.status.ptr, 0, sizeof(int), st));
+  if (!w.nested && nb > 64) {
+    // pivot blocks wider than 64 are inverted by an inner Gauss-Jordan whose
+    // pivot status this (outer) level clears now and reads at the end
+    if (!w.inner) w.inner.reset(new GJWork<R>());
+    w.inner->nb = 64;
+    w.inner->nested = true;
+    MNP_TRY(w.inner->status.ensure(sizeof(int)));
+    MNP_CUDA(cudaMemsetAsync(w.inner->status.ptr, 0, sizeof(int), st));
+  }
   Cx* Ccol = w.ccol.template as<Cx>();   // [n][nb]
   Cx* Rrow = w.rrow.template as<Cx>();   // [nb][n]
   Cx* Ncol = w.ncol.template as<Cx>();   // [n][nb]
   Cx* X = w.xblk.template as<Cx>();      // [nb][nb]
-  const size_t smem = cs * ((size_t)nb * (nb + 1) + 2 * nb);
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[sizeof(R) == 8]) {
-    MNP_CUDA(cudaFuncSetAttribute(k_block_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(cs * (64 * 65 + 128))));
-    attr_set[sizeof(R) == 8] = true;
-  }
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
   for (int64_t k0 = 0; k0 < n; k0 += nb) {
     const int bw = (int)std::min<int64_t>(nb, n - k0);
     // 1. Ccol <- A[:, k-block]
     MNP_CUDA(cudaMemcpy2DAsync(Ccol, cs * bw, A + k0, cs * lda, cs * bw, n, cudaMemcpyDeviceToDevice, st));
-    // 2. X <- inv(A_kk)
-    ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
-    k_block_inv<R><<<1, 256, smem, st>>>(Ccol + k0 * bw, bw, bw, X, bw, w.status.template as<int>());
-    MNP_CHECK_LAUNCH();
+    // 2. X <- inv(A_kk): one shared-memory kernel for blocks up to 64, else
+    //    an inner Gauss-Jordan with 64-wide steps on a copy of the block
+    if (bw <= 64) {
+      ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
+      k_block_inv<R><<<1, 256, 0, st>>>(Ccol + k0 * bw, bw, bw, X, bw, w.status.template as<int>());
+      MNP_CHECK_LAUNCH();
+    } else {
+      MNP_CUDA(cudaMemcpyAsync(X, Ccol + k0 * bw, cs * bw * bw, cudaMemcpyDeviceToDevice, st));
+      MNP_TRY(gj_invert<R>(X, bw, bw, *w.inner, big_gemm, ctx, st));
+    }
     // 3. R <- X * A[k-block, :], then zero its k-block columns
-    MNP_TRY(gemm_simt<R>(bw, n, bw, one, X, bw, A + k0 * lda, lda, zero, Rrow, n, st));
+    MNP_TRY(big_gemm(bw, n, bw, one, X, bw, A + k0 * lda, lda, zero, Rrow, n, st, ctx));
     MNP_CUDA(cudaMemset2DAsync(Rrow + k0, cs * n, 0, cs * bw, bw, st));
     // 4. new column block <- -Ccol * X, then zero Ccol's k-block rows
-    MNP_TRY(gemm_simt<R>(n, bw, bw, mone, Ccol, bw, X, bw, zero, Ncol, bw, st));
+    MNP_TRY(big_gemm(n, bw, bw, mone, Ccol, bw, X, bw, zero, Ncol, bw, st, ctx));
     MNP_CUDA(cudaMemsetAsync(Ccol + k0 * bw, 0, cs * bw * bw, st));
     // 5. A <- A - Ccol * R  (rank-bw update of the whole matrix)
     MNP_TRY(big_gemm(n, n, bw, mone, Ccol, bw, Rrow, n, one, A, lda, st, ctx));
@@ -180,9 +312,16 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
     MNP_CUDA(cudaMemcpy2DAsync(A + k0, cs * lda, Ncol, cs * bw, cs * bw, n, cudaMemcpyDeviceToDevice, st));
     MNP_CUDA(cudaMemcpy2DAsync(A + k0 * lda + k0, cs * lda, X, cs * bw, cs * bw, bw, cudaMemcpyDeviceToDevice, st));
   }
+  if (w.nested || !read_status) return MNPBEM_OK;
   int hs = 0;
   MNP_CUDA(cudaMemcpyAsync(&hs, w.status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
   MNP_CUDA(cudaStreamSynchronize(st));
+  if (w.inner) {
+    int hi = 0;
+    MNP_CUDA(cudaMemcpyAsync(&hi, w.inner->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MNP_CUDA(cudaStreamSynchronize(st));
+    hs |= hi;
+  }
   if (hs) {
     set_error("block Gauss-Jordan inversion: zero or non-finite pivot");
     return MNPBEM_ERR_SINGULAR;
@@ -191,8 +330,8 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
 }
 
 template mnpbem_status gj_invert<float>(float2*, int64_t, int64_t, GJWork<float>&, GemmFn<float>,
-                                        void*, cudaStream_t);
+                                        void*, cudaStream_t, bool);
 template mnpbem_status gj_invert<double>(double2*, int64_t, int64_t, GJWork<double>&,
-                                         GemmFn<double>, void*, cudaStream_t);
+                                         GemmFn<double>, void*, cudaStream_t, bool);
 
 }  // namespace mnpbem

@@ -1,5 +1,6 @@
 // Dense complex linear algebra on the device (row-major, interleaved complex).
 #pragma once
+#include <memory>
 #include "common.cuh"
 
 namespace mnpbem {
@@ -14,9 +15,10 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
 // elimination without row interchanges.
 template <typename R>
 struct GJWork {
-  DevBuf ccol, rrow, ncol, xblk, status, tf32;
-  int64_t n = 0;
+  DevBuf ccol, rrow, ncol, xblk, status;
   int nb = 64;
+  bool nested = false;               // inner level: the outer level reads the pivot status
+  std::unique_ptr<GJWork<R>> inner;  // Gauss-Jordan of pivot blocks wider than 64
 };
 
 // A <- inv(A) in place.  Returns MNPBEM_ERR_SINGULAR if a pivot guard trips.
@@ -25,8 +27,13 @@ template <typename R>
 using GemmFn = mnpbem_status (*)(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cplx<R>* A,
                                  int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta,
                                  cplx<R>* C, int64_t ldc, cudaStream_t st, void* ctx);
+// read_status = false: nothing synchronises (usable inside a graph capture);
+// the caller reads the pivot status later with gj_status_copy.
 template <typename R>
 mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn<R> big_gemm,
-                        void* ctx, cudaStream_t st);
+                        void* ctx, cudaStream_t st, bool read_status = true);
+// enqueue copies of the pivot status words (outer, inner) into host memory
+template <typename R>
+mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st);
 
 }  // namespace mnpbem

@@ -119,8 +119,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 // C_r[M][N2] = A_r[M][K2] * B'[N2][K2]^T + beta * C_r        (all row-major floats)
 __global__ void __launch_bounds__(128, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M,
-              int N2, int K2, float* __restrict__ C, int64_t ldc, float beta, int* err) {
+    k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+              const __grid_constant__ CUtensorMap mapC, int M, int N2, int K2, int accumulate, int* err) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bars[2 * TC_STAGES + 1];
   __shared__ uint32_t tmem_slot;
@@ -190,34 +190,44 @@ __global__ void __launch_bounds__(128, 1)
   __syncwarp();
   tc_fence_after();
   if (ok) {
-    const int row = m0 + warp * 32 + lane;
-    const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+    // Each warp owns 32 accumulator rows (TMEM lanes 32w..32w+31).  A 32 x 32
+    // chunk goes TMEM -> registers -> a staging tile in the (now idle)
+    // pipeline shared memory, and one lane hands it to TMA: a bulk tensor
+    // store when C is overwritten, a bulk tensor reduce-add when C
+    // accumulates (the read-modify-write of C happens in L2, the SMs never
+    // read C).  Two staging tiles per warp let the next chunk overlap the
+    // previous copy.  TMA clips rows / columns outside C.
+    const uint32_t stage0 = base + (uint32_t)warp * 2u * 4096u;
+    float* stage_gen = reinterpret_cast<float*>(smem_raw + (base - smem_u32(smem_raw))) + warp * 2 * 1024;
     for (int c = 0; c < TC_BN / 32; ++c) {
+      const int col0 = n0 + c * 32, row0 = m0 + warp * 32;
       uint32_t r[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
-      const int col0 = n0 + c * 32;
-      if (row >= M || col0 >= N2) continue;
-      float* crow = C + (int64_t)row * ldc + col0;
-      if (vec && col0 + 32 <= N2) {
+      if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
+      const int buf = c & 1;
+      if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      __syncwarp();
+      float* st = stage_gen + buf * 1024;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          float4 v = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                                 __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
-          float4* dst = reinterpret_cast<float4*>(crow) + q;
-          if (beta != 0.0f) {
-            float4 o = *dst;
-            v.x += beta * o.x; v.y += beta * o.y; v.z += beta * o.z; v.w += beta * o.w;
-          }
-          *dst = v;
-        }
-      } else {
-        for (int q = 0; q < 32 && col0 + q < N2; ++q) {
-          float v = __uint_as_float(r[q]);
-          if (beta != 0.0f) v += beta * crow[q];
-          crow[q] = v;
-        }
+      for (int j = 0; j < 32; ++j) st[lane * 32 + ((j + lane) & 31)] = __uint_as_float(r[(j + lane) & 31]);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        const uint32_t src = stage0 + (uint32_t)buf * 4096u;
+        if (accumulate)
+          asm volatile(
+              "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%1, %2}], [%3];"
+              ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+              : "memory");
+        else
+          asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                       ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+                       : "memory");
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
       }
     }
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncwarp();
   }
   // ---------------- drain copies still in flight after an error, free TMEM
   if (warp == 0 && lane == 0 && *(volatile int*)err) {
@@ -292,18 +302,19 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode(TcGemmCtx& c) {
 }
 
 static bool make_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, const void* ptr, uint64_t inner,
-                     uint64_t rows, uint64_t row_bytes, uint32_t box_rows) {
+                     uint64_t rows, uint64_t row_bytes, uint32_t box_rows, bool swizzle = true) {
   cuuint64_t dims[2] = {inner, rows};
   cuuint64_t strides[1] = {row_bytes};
   cuuint32_t box[2] = {(cuuint32_t)TC_BK, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
-bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K) {
+bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                      const void* C, int64_t ldc, float2 beta) {
   if (!c.checked) {
     c.checked = true;
     int dev = 0, major = 0, minor = 0;
@@ -315,15 +326,18 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K) {
     if (!c.usable) cudaGetLastError();
   }
   if (!c.usable || !c.enabled) return false;
+  if ((lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||
+      (reinterpret_cast<uintptr_t>(C) & 15) || beta.y != 0.0f || (beta.x != 0.0f && beta.x != 1.0f))
+    return false;
   return M >= 128 && N >= 64 && K >= 16 && M < (1 << 30) && 2 * N < (1 << 30) && 2 * K < (1 << 30);
 }
 
 mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
                           int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc,
                           cudaStream_t st) {
-  if (beta.y != 0.0f || (lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||
-      (reinterpret_cast<uintptr_t>(C) & 15)) {
-    set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base or complex beta)");
+  if (beta.y != 0.0f || (beta.x != 0.0f && beta.x != 1.0f) || (lda & 1) || (ldc & 1) ||
+      (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(C) & 15)) {
+    set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base, beta not 0 or 1)");
     return MNPBEM_ERR_UNSUPPORTED;
   }
   const int64_t K2 = 2 * K, N2 = 2 * N;
@@ -338,9 +352,10 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     MNP_CHECK_LAUNCH();
   }
   auto enc = get_encode(c);
-  CUtensorMap ma, mb;
+  CUtensorMap ma, mb, mc;
   if (!make_map(enc, &ma, A, (uint64_t)K2, (uint64_t)M, (uint64_t)lda * 8, TC_BM) ||
-      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, TC_BN)) {
+      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, TC_BN) ||
+      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, false)) {
     set_error("cuTensorMapEncodeTiled failed");
     return MNPBEM_ERR_CUDA;
   }
@@ -353,8 +368,8 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
   {
     ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
-    k_tc_gemm<<<grid, 128, TC_SMEM, st>>>(ma, mb, (int)M, (int)N2, (int)K2, reinterpret_cast<float*>(C),
-                                         ldc * 2, beta.x, c.err.as<int>());
+    k_tc_gemm<<<grid, 128, TC_SMEM, st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2, beta.x != 0.0f ? 1 : 0,
+                                         c.err.as<int>());
     MNP_CHECK_LAUNCH();
   }
   return MNPBEM_OK;

@@ -14,7 +14,10 @@ struct TcGemmCtx {
   void* encode_fn = nullptr;
 };
 
-bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K);
+// true when the tensor-core path can run this product (device, shape and layout:
+// even leading dimensions and 16-byte aligned A and C, real beta)
+bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                      const void* C, int64_t ldc, float2 beta);
 mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha,
                           const float2* A, int64_t lda, const float2* B, int64_t ldb, float2 beta,
                           float2* C, int64_t ldc, cudaStream_t st);
