@@ -92,7 +92,7 @@ struct mnpbem_geom {
   int64_t ld = 0;
   DevBuf mat[5];      // working-precision matrices
   DevBuf mat64[4];    // FP64 G1, H1, G2, H2 for refinement (MIXED)
-  DevBuf vec64, vecw, facebuf, exbuf, fields, norms, outbuf;
+  DevBuf vec64, vecw, facebuf, exbuf, fields, norms, outbuf, bsplit;
   GJWork<float> gj32;    // block width set per solve (256 on the tensor-core path)
   GJWork<double> gj64;
   TcGemmCtx tc;
@@ -497,6 +497,7 @@ mnpbem_status ensure_workspace(mnpbem_geom* G, int precision, int P, int ninf) {
   // working-precision vectors for MIXED: in (8nP) out (8nP) work (32nP)
   MNP_TRY(G->vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
   MNP_TRY(G->norms.ensure(sizeof(double) * 4));
+  MNP_TRY(G->bsplit.ensure(sizeof(float2) * 2 * n * 4 * P));
   MNP_TRY(G->facebuf.ensure(sizeof(double2) * 2 * n + sizeof(float2) * 3 * n + sizeof(float) * 3 * n + 2 * n + 256));
   MNP_TRY(G->fields.ensure(sizeof(double2) * (size_t)(P + ninf) * 6 * P));
   MNP_TRY(G->outbuf.ensure(sizeof(double) * 2 * P));   // ext / sca slot of the current wavelength
@@ -589,11 +590,15 @@ mnpbem_status stage_assemble(mnpbem_geom* G, int precision) {
     return assemble_launch(p, true, false, G->st);
   }
   p.ld32 = ld;
-  p.ld64 = ld;
   p.g1 = G->mat[0].as<float2>(); p.g2 = G->mat[1].as<float2>();
   p.h1 = G->mat[2].as<float2>(); p.h2 = G->mat[3].as<float2>();
-  p.G1 = G->mat64[0].as<double2>(); p.H1 = G->mat64[1].as<double2>();
-  p.G2 = G->mat64[2].as<double2>(); p.H2 = G->mat64[3].as<double2>();
+  // residual matrices as hi / lo complex64 planes (mat64[q]: hi [n][ld] then lo [n][ld])
+  float2* hl[4];
+  for (int q = 0; q < 4; ++q) hl[q] = G->mat64[q].as<float2>();
+  p.G1hi = hl[0]; p.G1lo = hl[0] + n * ld;
+  p.H1hi = hl[1]; p.H1lo = hl[1] + n * ld;
+  p.G2hi = hl[2]; p.G2lo = hl[2] + n * ld;
+  p.H2hi = hl[3]; p.H2lo = hl[3] + n * ld;
   return assemble_launch(p, true, true, G->st);
 }
 
@@ -693,14 +698,16 @@ mnpbem_status stage_iter(mnpbem_geom* G, const SolveCtx& c) {
   const int P = c.P;
   cudaStream_t st = G->st;
   Vec64 v = vec64(G, P);
-  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
-  const double2* A64[4] = {G->mat64[0].as<double2>(), G->mat64[1].as<double2>(),
-                           G->mat64[2].as<double2>(), G->mat64[3].as<double2>()};
+  const int64_t ld = G->ld;
+  const float2* hl[4];
+  for (int q = 0; q < 4; ++q) hl[q] = G->mat64[q].as<float2>();
   double* norms = G->norms.as<double>();
-  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[0], G->ld, v.x1, 4 * P, zero, v.Y1, 4 * P, st));
-  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[2], G->ld, v.x2, 4 * P, zero, v.Y2, 4 * P, st));
-  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[1], G->ld, v.x1, 4 * P, zero, v.Z1, 4 * P, st));
-  MNP_TRY(gemm_simt<double>(n, 4 * P, n, one, A64[3], G->ld, v.x2, 4 * P, zero, v.Z2, 4 * P, st));
+  // G1 x1, G2 x2, H1 x1, H2 x2 in double-single arithmetic from the hi / lo planes
+  float2* bs = G->bsplit.as<float2>();
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], hl[0] + n * ld, ld, v.x1, 4 * P, v.Y1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], hl[1] + n * ld, ld, v.x1, 4 * P, v.Z1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], hl[2] + n * ld, ld, v.x2, 4 * P, v.Y2, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], hl[3] + n * ld, ld, v.x2, 4 * P, v.Z2, 4 * P, bs, st));
   MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
   launch_residual(c.fd, P, G->lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.phi, v.a, v.alpha, v.De,
                   v.rphi, v.ra, v.ral, v.rDe, norms, st);

@@ -32,9 +32,25 @@ __device__ __forceinline__ PairVal far_pair(double2 k, double dd, double in, dou
   return v;
 }
 
+__device__ __forceinline__ void store_split(float2* hi, float2* lo, int64_t o, double2 v) {
+  const float2 h = to_f(v);
+  hi[o] = h;
+  lo[o] = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
+}
+
 template <bool W64, bool W32>
 __device__ __forceinline__ void store4(const AsmParams& p, int64_t i, int64_t j, double2 g1, double2 h1,
                                        double2 g2, double2 h2) {
+  if (W64 && W32) {
+    int64_t o = i * p.ld32 + j;
+    const float2 a = to_f(g1), b = to_f(h1), c = to_f(g2), d = to_f(h2);
+    p.g1[o] = a; p.h1[o] = b; p.g2[o] = c; p.h2[o] = d;
+    store_split(p.G1hi, p.G1lo, o, g1);
+    store_split(p.H1hi, p.H1lo, o, h1);
+    store_split(p.G2hi, p.G2lo, o, g2);
+    store_split(p.H2hi, p.H2lo, o, h2);
+    return;
+  }
   if (W64) {
     int64_t o = i * p.ld64 + j;
     if (p.G1) p.G1[o] = g1;

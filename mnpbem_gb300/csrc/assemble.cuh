@@ -25,10 +25,16 @@ struct AsmParams {
   signed char med[4][ASM_MAXP][ASM_MAXP];
   double2 *G1 = nullptr, *H1 = nullptr, *G2 = nullptr, *H2 = nullptr;  // complex128 outputs
   float2 *g1 = nullptr, *h1 = nullptr, *g2 = nullptr, *h2 = nullptr;   // complex64 outputs
+  // mixed precision: the FP64 value of G1, H1, G2, H2 as complex64 pairs
+  // hi = fl32(v), lo = fl32(v - hi) in planes [n][ld32] (used instead of G1..H2)
+  float2 *G1lo = nullptr, *H1lo = nullptr, *G2lo = nullptr, *H2lo = nullptr;
+  float2 *G1hi = nullptr, *H1hi = nullptr, *G2hi = nullptr, *H2hi = nullptr;
 };
 
 void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
                   double4_32a* nrm, cudaStream_t st);
+// w64 && !w32: complex128 outputs; !w64 && w32: complex64 outputs;
+// w64 && w32: complex64 working matrices plus hi / lo planes
 mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st);
 
 }  // namespace mnpbem

@@ -73,51 +73,47 @@ __global__ void __launch_bounds__(256) k_gemm_nn(int64_t M, int64_t N, int64_t K
 }
 
 // ------------------------------------------------------- thin GEMM (N <= 16)
-// Matrix times a few vectors: memory-bound on A.  Each warp owns THIN_ROWS rows
-// and strides over K with coalesced loads of A; chunks of B are staged in
-// shared memory transposed (Bs[n][k]) so that lanes read consecutive k.
-constexpr int THIN_NMAX = 16, THIN_ROWS = 2, THIN_KC = 128, THIN_WARPS = 8;
+// Matrix times a few vectors, memory-bound on A.  A block of 8 warps owns
+// TR rows; warp w streams its own slice of K (no barriers in the main loop),
+// lanes stride by 32 over consecutive k (coalesced rows of A), each B row is
+// read once per lane through L1 and reused for the TR rows.  The 8 partial
+// sums per entry are combined in shared memory at the end.
+constexpr int THIN_NMAX = 16, THIN_WARPS = 8;
 
-template <typename R, int N>
+template <typename R, int N, int TR>
 __global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin(int64_t M, int64_t K, cplx<R> alpha,
                                                              const cplx<R>* __restrict__ A, int64_t lda,
                                                              const cplx<R>* __restrict__ B, int64_t ldb,
                                                              cplx<R> beta, cplx<R>* __restrict__ C,
                                                              int64_t ldc) {
   using Cx = cplx<R>;
-  __shared__ Cx Bs[N][THIN_KC];
+  __shared__ Cx red[THIN_WARPS][TR][N];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row0 = ((int64_t)blockIdx.x * THIN_WARPS + warp) * THIN_ROWS;
-  Cx acc[THIN_ROWS][N];
+  const int64_t row0 = (int64_t)blockIdx.x * TR;
+  const int64_t kw = (K + THIN_WARPS - 1) / THIN_WARPS;
+  const int64_t kbeg = warp * kw, kend = min(K, kbeg + kw);
+  const Cx* arow[TR];
 #pragma unroll
-  for (int r = 0; r < THIN_ROWS; ++r)
+  for (int r = 0; r < TR; ++r) arow[r] = A + min(row0 + r, M - 1) * lda;
+  Cx acc[TR][N];
+#pragma unroll
+  for (int r = 0; r < TR; ++r)
 #pragma unroll
     for (int c = 0; c < N; ++c) acc[r][c] = mk<R>(0, 0);
-  for (int64_t k0 = 0; k0 < K; k0 += THIN_KC) {
-    const int kc = (int)((K - k0) < THIN_KC ? (K - k0) : THIN_KC);
-    __syncthreads();
-    for (int l = threadIdx.x; l < kc * N; l += blockDim.x) {
-      int kk = l / N, c = l % N;
-      Bs[c][kk] = B[(k0 + kk) * ldb + c];
-    }
-    __syncthreads();
+#pragma unroll 2
+  for (int64_t k = kbeg + lane; k < kend; k += 32) {
+    Cx bv[N];
 #pragma unroll
-    for (int r = 0; r < THIN_ROWS; ++r) {
-      const int64_t row = row0 + r;
-      if (row >= M) continue;
-      const Cx* arow = A + row * lda + k0;
-#pragma unroll 4
-      for (int kk = lane; kk < kc; kk += 32) {
-        const Cx a = arow[kk];
+    for (int c = 0; c < N; ++c) bv[c] = __ldg(B + k * ldb + c);
 #pragma unroll
-        for (int c = 0; c < N; ++c) cfma(acc[r][c], a, Bs[c][kk]);
-      }
+    for (int r = 0; r < TR; ++r) {
+      const Cx av = __ldg(arow[r] + k);
+#pragma unroll
+      for (int c = 0; c < N; ++c) cfma(acc[r][c], av, bv[c]);
     }
   }
-  const bool zero_beta = (beta.x == 0 && beta.y == 0);
 #pragma unroll
-  for (int r = 0; r < THIN_ROWS; ++r) {
-    const int64_t row = row0 + r;
+  for (int r = 0; r < TR; ++r)
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       Cx v = acc[r][c];
@@ -125,13 +121,154 @@ __global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin(int64_t M, int64_
         v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
         v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
       }
-      if (lane == c && row < M) {
-        Cx out = cmul(alpha, v);
-        if (!zero_beta) out = cadd(out, cmul(beta, C[row * ldc + c]));
-        C[row * ldc + c] = out;
+      if (lane == 0) red[warp][r][c] = v;
+    }
+  __syncthreads();
+  const bool zero_beta = (beta.x == 0 && beta.y == 0);
+  for (int t = threadIdx.x; t < TR * N; t += blockDim.x) {
+    const int r = t / N, c = t % N;
+    const int64_t row = row0 + r;
+    if (row >= M) continue;
+    Cx v = mk<R>(0, 0);
+#pragma unroll
+    for (int w = 0; w < THIN_WARPS; ++w) v = cadd(v, red[w][r][c]);
+    Cx out = cmul(alpha, v);
+    if (!zero_beta) out = cadd(out, cmul(beta, C[row * ldc + c]));
+    C[row * ldc + c] = out;
+  }
+}
+
+// ------------------------------------------- double-single thin GEMM (N <= 16)
+// Error-free transformations (Dekker / Knuth): the product a*b = p + e exactly
+// with p = fl(a*b), e = fma(a, b, -p); the sum s + p = t + err exactly with
+// TwoSum.  Each accumulator is a pair (hi, lo) of floats.
+struct DS { float hi, lo; };
+
+__device__ __forceinline__ void ds_acc_prod(DS& s, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float t = s.hi + p;
+  const float bp = t - s.hi;
+  const float err = (s.hi - (t - bp)) + (p - bp);
+  s.hi = t;
+  s.lo += err + e;
+}
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+  const float t = a.hi + b.hi;
+  const float bp = t - a.hi;
+  const float err = (a.hi - (t - bp)) + (b.hi - bp);
+  const float lo = a.lo + b.lo + err;
+  DS r;
+  r.hi = t + lo;                 // renormalise (FastTwoSum)
+  r.lo = lo - (r.hi - t);
+  return r;
+}
+
+constexpr int DS_WARPS = 8, DS_TR = 4;
+
+// B (complex128) -> hi / lo complex64 planes
+__global__ void k_split_hi_lo(const double2* __restrict__ B, int64_t count, float2* hi, float2* lo) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double2 b = B[i];
+  const float2 h = make_float2((float)b.x, (float)b.y);
+  hi[i] = h;
+  lo[i] = make_float2((float)(b.x - (double)h.x), (float)(b.y - (double)h.y));
+}
+
+template <int N>
+__global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64_t K, const float2* __restrict__ Ahi,
+                                                              const float2* __restrict__ Alo, int64_t lda,
+                                                              const float2* __restrict__ Bh,
+                                                              const float2* __restrict__ Bl, int64_t ldb,
+                                                              double2* __restrict__ C, int64_t ldc) {
+  __shared__ DS red[DS_WARPS][DS_TR][N][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = (int64_t)blockIdx.x * DS_TR;
+  const int64_t kw = (K + DS_WARPS - 1) / DS_WARPS;
+  const int64_t kbeg = warp * kw, kend = min(K, kbeg + kw);
+  int64_t roff[DS_TR];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r) roff[r] = min(row0 + r, M - 1) * lda;
+  DS re[DS_TR][N], im[DS_TR][N];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) re[r][c] = im[r][c] = DS{0.f, 0.f};
+  for (int64_t k = kbeg + lane; k < kend; k += 32) {
+    float2 xh[N], xl[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      xh[c] = __ldg(Bh + k * ldb + c);
+      xl[c] = __ldg(Bl + k * ldb + c);
+    }
+#pragma unroll
+    for (int r = 0; r < DS_TR; ++r) {
+      const float2 ah = __ldg(Ahi + roff[r] + k), al = __ldg(Alo + roff[r] + k);
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        ds_acc_prod(re[r][c], ah.x, xh[c].x);
+        ds_acc_prod(re[r][c], -ah.y, xh[c].y);
+        ds_acc_prod(im[r][c], ah.x, xh[c].y);
+        ds_acc_prod(im[r][c], ah.y, xh[c].x);
+        // first-order corrections from the low parts (relative size 2^-24)
+        re[r][c].lo += (ah.x * xl[c].x - ah.y * xl[c].y) + (al.x * xh[c].x - al.y * xh[c].y);
+        im[r][c].lo += (ah.x * xl[c].y + ah.y * xl[c].x) + (al.x * xh[c].y + al.y * xh[c].x);
       }
     }
   }
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      DS a = re[r][c], b = im[r][c];
+      for (int o = 16; o; o >>= 1) {
+        DS oa{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+        DS ob{__shfl_xor_sync(0xffffffffu, b.hi, o), __shfl_xor_sync(0xffffffffu, b.lo, o)};
+        a = ds_add(a, oa);
+        b = ds_add(b, ob);
+      }
+      if (lane == 0) { red[warp][r][c][0] = a; red[warp][r][c][1] = b; }
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < DS_TR * N; t += blockDim.x) {
+    const int r = t / N, c = t % N;
+    const int64_t row = row0 + r;
+    if (row >= M) continue;
+    DS a{0.f, 0.f}, b{0.f, 0.f};
+#pragma unroll
+    for (int w = 0; w < DS_WARPS; ++w) {
+      a = ds_add(a, red[w][r][c][0]);
+      b = ds_add(b, red[w][r][c][1]);
+    }
+    C[row * ldc + c] = make_double2((double)a.hi + (double)a.lo, (double)b.hi + (double)b.lo);
+  }
+}
+
+mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
+                           int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
+                           float2* bsplit, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return MNPBEM_OK;
+  if (N > 8 || K <= 0 || ldb != N) { set_error("gemm_thin_ds: N must be 1..8 and B packed"); return MNPBEM_ERR_INVALID_ARG; }
+  float2* Bh = bsplit;
+  float2* Bl = bsplit + K * N;
+  {
+    ProfScope ps(PH_ELEMWISE, st, 0.0, 0.0, 1);
+    k_split_hi_lo<<<(unsigned)cdiv_up(K * N, 256), 256, 0, st>>>(B, K * N, Bh, Bl);
+    MNP_CHECK_LAUNCH();
+  }
+  ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 16.0 * M * K + 16.0 * K * N + 16.0 * M * N);
+  const unsigned nblk = (unsigned)cdiv_up(M, (int64_t)DS_TR);
+#define DS_CASE(NN)                                                                                   \
+  case NN:                                                                                            \
+    k_gemm_thin_ds<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, Alo, lda, Bh, Bl, N, C, ldc);     \
+    break;
+  switch (N) {
+    DS_CASE(1) DS_CASE(2) DS_CASE(3) DS_CASE(4) DS_CASE(5) DS_CASE(6) DS_CASE(7) DS_CASE(8)
+  }
+#undef DS_CASE
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
 }
 
 template <typename R>
@@ -142,12 +279,13 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
   if (N <= THIN_NMAX && K > 0) {
     ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  (double)sizeof(cplx<R>) * ((double)M * K + (double)K * N + 2.0 * M * N));
-    const int64_t rows_per_block = (int64_t)THIN_ROWS * THIN_WARPS;
-    const unsigned nblk = (unsigned)cdiv_up(M, rows_per_block);
-#define THIN_CASE(NN)                                                                           \
-  case NN:                                                                                      \
-    k_gemm_thin<R, NN><<<nblk, 32 * THIN_WARPS, 0, st>>>(M, K, alpha, A, lda, B, ldb, beta, C, ldc); \
-    break;
+    // rows per block: fewer for wide B so that the accumulators stay in registers
+#define THIN_CASE(NN)                                                                              \
+  case NN: {                                                                                       \
+    constexpr int TR = NN <= 8 ? 4 : (sizeof(R) == 8 ? 1 : 2);                                     \
+    k_gemm_thin<R, NN, TR><<<(unsigned)cdiv_up(M, TR), 32 * THIN_WARPS, 0, st>>>(M, K, alpha, A, lda, B, ldb, beta, C, ldc); \
+    break;                                                                                         \
+  }
     switch (N) {
       THIN_CASE(1) THIN_CASE(2) THIN_CASE(3) THIN_CASE(4) THIN_CASE(5) THIN_CASE(6) THIN_CASE(7)
       THIN_CASE(8) THIN_CASE(9) THIN_CASE(10) THIN_CASE(11) THIN_CASE(12) THIN_CASE(13) THIN_CASE(14)

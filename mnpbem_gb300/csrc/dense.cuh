@@ -11,6 +11,15 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
                         int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta, cplx<R>* C,
                         int64_t ldc, cudaStream_t st);
 
+// C[M x N] = (A_hi + A_lo)[M x K] * B[K x N] for N <= 8 with the product
+// evaluated in double-single FP32 arithmetic (error-free products and
+// TwoSum accumulation, ~48-bit accuracy): A_hi = fl32(A), A_lo = fl32(A - A_hi)
+// are complex64 planes, B (packed, ldb = N) and C are complex128.
+// bsplit: workspace of 2 K N complex64 (hi / lo planes of B).
+mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
+                           int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
+                           float2* bsplit, cudaStream_t st);
+
 // Workspace for in-place inversion of an n x n matrix by blocked Gauss-Jordan
 // elimination without row interchanges.
 template <typename R>
