@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--faces", type=int, default=4000)
-    ap.add_argument("--batch", type=int, default=10, help="wavelengths per step per GPU")
+    ap.add_argument("--batch", type=int, default=20, help="wavelengths per step per GPU")
+    ap.add_argument("--lanes", type=int, default=0, help="wavelengths in flight at once (0: library default)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
@@ -135,7 +136,7 @@ def make_problem(a, device, precision):
     v, f = shapes.fibsphere(a.faces, 50.0)
     p = m.particle(v, f)
     cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
-    bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device))
+    bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device, lanes=a.lanes))
     exc = m.planewave([1, 0, 0], [0, 0, 1])
     return cp, bem, exc
 
@@ -431,7 +432,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": workload_desc(a), "faces": n, "wavelengths_per_step": a.batch,
-                           "precision": a.precision,
+                           "precision": a.precision, "lanes": a.lanes or "auto",
                            "l2": "no flush: per-wavelength working set %.2f GB > 129 MB L2" % (wset / 1e9)},
                 "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],
                 "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64}

@@ -207,7 +207,17 @@ MNPBEM_API mnpbem_status mnpbem_cross_sections_noalloc(
     const double* inf_nvec, const double* inf_area, double enei, const double* eps_exc,
     const double* eps_1, double* ext, double* sca);
 
-/* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
+/* Number of wavelengths a sweep keeps in flight at once (0 = automatic: 4,
+ * fewer when device memory is short; 1 while profiling).  Each lane owns its
+ * own stream and per-wavelength workspace (the five working matrices, the
+ * refinement matrices and vectors), so device memory grows with the lane
+ * count.  No counterpart in the reference, which solves one wavelength at a
+ * time (Simulation/retarded/@spectrumret and the demo loops over enei).      */
+MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
+
+/* The handle's CUDA stream (cudaStream_t).  mnpbem_solve runs lane 0 on it
+ * and makes it wait for the other lanes before returning, so work queued on
+ * this stream after a call is ordered after all of the call's kernels.       */
 MNPBEM_API mnpbem_status mnpbem_geom_stream(const mnpbem_geom* g, void** stream);
 
 /* Message of the last failure on the calling thread ("" if none). */

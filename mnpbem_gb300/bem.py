@@ -157,6 +157,8 @@ class bemret:
             ctypes.byref(h)))
         self._h = h
         self._lib = lib
+        if "lanes" in self.op:
+            self.set_lanes(int(self.op["lanes"]))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -166,6 +168,10 @@ class bemret:
             except Exception:
                 pass
             self._h = None
+
+    def set_lanes(self, lanes):
+        """Wavelengths kept in flight at once by ``spectrum`` (0 = automatic)."""
+        _lib.check(self._lib.mnpbem_geom_set_lanes(self._h, int(lanes)))
 
     # ----------------------------------------------------------- queries
     @property

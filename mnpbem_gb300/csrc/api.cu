@@ -15,6 +15,9 @@
 #include <cstdio>
 #include <cstring>
 #include <complex>
+#include <algorithm>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "assemble.cuh"
@@ -77,6 +80,38 @@ static mnpbem_status gemm32(int64_t M, int64_t N, int64_t K, float2 al, const fl
 
 using namespace mnpbem;
 
+// Per-wavelength working state.  A handle owns one or more lanes; each lane
+// has its own stream, matrices, vectors, Gauss-Jordan and tensor-core
+// workspaces and captured stage graphs, so that several wavelengths of a
+// sweep run concurrently: the latency-bound steps of one wavelength (pivot
+// blocks, panel products, refinement vectors) overlap the tensor-core
+// updates of the others.  Lane 0 runs on the handle's stream.
+struct Lane {
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  DevBuf mat[5];      // working-precision matrices
+  DevBuf mat64[4];    // G1, H1, G2, H2 for the refinement residual (MIXED): hi / lo complex64 planes
+  DevBuf vec64, vecw, facebuf, fields, norms, outbuf, bsplit, lp_dev;
+  GJWork<float> gj32;    // block width set per solve (256 on the tensor-core path)
+  GJWork<double> gj64;
+  TcGemmCtx tc;
+  int* status_host = nullptr;     // pinned: pivot status words (2)
+  double* norms_host = nullptr;   // pinned: refinement norms (4)
+  cudaEvent_t ev = nullptr;       // completion of the work last queued by the scheduler
+  struct Graphs {
+    bool valid = false;
+    int precision = -1, P = 0, ninf = 0;
+    bool prof = false;
+    uint64_t sig = 0;             // addresses of every buffer the graphs captured
+    cudaGraphExec_t exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    Profiler::GraphRec rec[5];
+  } graphs;
+  // scheduler state
+  enum { IDLE = 0, ITER, DONE } state = IDLE;
+  int w = -1, iters = 0;
+  double res = -1.0;
+};
+
 struct mnpbem_geom {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -87,41 +122,70 @@ struct mnpbem_geom {
   std::vector<int> inout;   // [np][2]
   std::vector<int> face_part;
   int max_medium = 0;
-  DevBuf d_part, d_src, d_nrm;
-  // workspace
+  DevBuf d_part, d_src, d_nrm, face_med, exbuf;
   int64_t ld = 0;
-  DevBuf mat[5];      // working-precision matrices
-  DevBuf mat64[4];    // FP64 G1, H1, G2, H2 for refinement (MIXED)
-  DevBuf vec64, vecw, facebuf, exbuf, fields, norms, outbuf, bsplit;
-  GJWork<float> gj32;    // block width set per solve (256 on the tensor-core path)
-  GJWork<double> gj64;
-  TcGemmCtx tc;
+  std::vector<std::unique_ptr<Lane>> lanes;
+  int lanes_req = 0;        // 0: automatic
   bool tc_enabled = true;
+  bool use_graphs = true;
   Profiler prof;
-  // per-wavelength parameters: device block + pinned host ring (one slot per wavelength)
-  DevBuf lp_dev, face_med;
+  // per-wavelength parameters: pinned host ring (one slot per wavelength)
   LamParams* lp_ring = nullptr;
   int lp_cap = 0;
-  int* status_host = nullptr;     // pinned: pivot status words (4)
-  double* norms_host = nullptr;   // pinned: refinement norms (4)
-  // CUDA graphs of the per-wavelength stages
-  bool use_graphs = true;
-  struct Graphs {
-    bool valid = false;
-    int precision = -1, P = 0, ninf = 0;
-    bool prof = false;
-    uint64_t gen = 0;
-    cudaGraphExec_t exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    Profiler::GraphRec rec[5];
-  } graphs;
 };
 
 namespace {
 
-std::complex<double> cx(const double* p) { return {p[0], p[1]}; }
+constexpr int MAX_LANES = 16;
+constexpr int DEFAULT_LANES = 4;
 
 mnpbem_status check_geom(const mnpbem_geom* g) {
   if (!g) { set_error("null geometry handle"); return MNPBEM_ERR_INVALID_ARG; }
+  return MNPBEM_OK;
+}
+
+void lane_release(Lane& L) {
+  if (L.st) cudaStreamSynchronize(L.st);
+  tc_release(L.tc);
+  for (int q = 0; q < 5; ++q) {
+    if (L.graphs.exec[q]) cudaGraphExecDestroy(L.graphs.exec[q]);
+    L.graphs.exec[q] = nullptr;
+    Profiler::release(L.graphs.rec[q]);
+  }
+  if (L.status_host) cudaFreeHost(L.status_host);
+  if (L.norms_host) cudaFreeHost(L.norms_host);
+  if (L.ev) cudaEventDestroy(L.ev);
+  if (L.own_stream && L.st) cudaStreamDestroy(L.st);
+  L.status_host = nullptr;
+  L.norms_host = nullptr;
+  L.ev = nullptr;
+  L.st = nullptr;
+}
+
+mnpbem_status add_lane(mnpbem_geom* G) {
+  std::unique_ptr<Lane> L(new Lane());
+  if (G->lanes.empty()) {
+    L->st = G->st;
+  } else {
+    MNP_CUDA(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking));
+    L->own_stream = true;
+  }
+  cudaError_t e = cudaMallocHost(&L->status_host, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMallocHost(&L->norms_host, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming);
+  mnpbem_status s = MNPBEM_OK;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("lane set-up failed: %s", cudaGetErrorString(e));
+    s = MNPBEM_ERR_CUDA;
+  }
+  if (s == MNPBEM_OK) s = L->lp_dev.ensure(sizeof(LamParams));
+  if (s != MNPBEM_OK) {
+    lane_release(*L);
+    return s;
+  }
+  L->status_host[0] = L->status_host[1] = 0;
+  G->lanes.push_back(std::move(L));
   return MNPBEM_OK;
 }
 
@@ -146,7 +210,7 @@ bool con12_zero(const mnpbem_geom* G) {
   return true;
 }
 
-AsmParams base_params(mnpbem_geom* G, const std::vector<std::complex<double>>& kmed) {
+AsmParams base_params(mnpbem_geom* G, const LamParams* lp) {
   AsmParams p;
   p.n = G->g.n;
   p.nref = G->g.nref;
@@ -158,8 +222,7 @@ AsmParams base_params(mnpbem_geom* G, const std::vector<std::complex<double>>& k
   p.ref_col = G->g.ref_col;
   p.ref_g = G->g.ref_g;
   p.ref_f = G->g.ref_f;
-  (void)kmed;
-  p.lp = G->lp_dev.as<LamParams>();
+  p.lp = lp;
   fill_media(G, p);
   return p;
 }
@@ -169,7 +232,7 @@ AsmParams base_params(mnpbem_geom* G, const std::vector<std::complex<double>>& k
 extern "C" {
 
 const char* mnpbem_last_error(void) { return get_error(); }
-const char* mnpbem_version(void) { return "mnpbem-gb300 0.1 (sm_103a)"; }
+const char* mnpbem_version(void) { return "mnpbem-gb300 0.2 (sm_103a)"; }
 
 mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int64_t* faces,
                                  int64_t nfaces, int32_t nparts, const int64_t* part_nfaces,
@@ -242,7 +305,6 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   G->g.order = op.order;
   mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, nfaces, cs.data(), ce.data(),
                                    (int)cs.size(), quad, op.rel_cutoff, op.abs_cutoff, G->st);
-  if (s == MNPBEM_OK) s = G->lp_dev.ensure(sizeof(LamParams));
   if (s == MNPBEM_OK) s = G->face_med.ensure(sizeof(int) * 2 * nfaces);
   if (s == MNPBEM_OK) {
     std::vector<int> fm(2 * nfaces);
@@ -250,14 +312,13 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
       fm[k] = G->inout[2 * G->face_part[k]] - 1;
       fm[nfaces + k] = G->inout[2 * G->face_part[k] + 1] - 1;
     }
-    if (cudaMemcpy(G->face_med.ptr, fm.data(), sizeof(int) * 2 * nfaces, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMallocHost(&G->status_host, 4 * sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(&G->norms_host, 4 * sizeof(double)) != cudaSuccess) {
+    if (cudaMemcpy(G->face_med.ptr, fm.data(), sizeof(int) * 2 * nfaces, cudaMemcpyHostToDevice) != cudaSuccess) {
       cudaGetLastError();
-      set_error("geometry set-up: upload of face media or pinned allocation failed");
+      set_error("geometry set-up: upload of face media failed");
       s = MNPBEM_ERR_CUDA;
     }
   }
+  if (s == MNPBEM_OK) s = add_lane(G);
   if (s == MNPBEM_OK) s = G->d_part.ensure(sizeof(int) * nfaces);
   if (s == MNPBEM_OK) s = G->d_src.ensure(sizeof(double4_32a) * nfaces);
   if (s == MNPBEM_OK) s = G->d_nrm.ensure(sizeof(double4_32a) * nfaces);
@@ -286,6 +347,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (env && env[0] == '0') G->tc_enabled = false;
   const char* genv = getenv("MNPBEM_GRAPHS");
   if (genv && genv[0] == '0') G->use_graphs = false;
+  const char* lenv = getenv("MNPBEM_LANES");
+  if (lenv && atoi(lenv) > 0) G->lanes_req = std::min(MAX_LANES, atoi(lenv));
   *out = G;
   return MNPBEM_OK;
 }
@@ -294,16 +357,22 @@ mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g) {
   if (!g) return MNPBEM_OK;
   cudaSetDevice(g->device);
   if (g->st) cudaStreamSynchronize(g->st);
-  tc_release(g->tc);
-  for (int q = 0; q < 5; ++q) {
-    if (g->graphs.exec[q]) cudaGraphExecDestroy(g->graphs.exec[q]);
-    Profiler::release(g->graphs.rec[q]);
-  }
+  g->prof.flush();
+  for (auto& L : g->lanes) lane_release(*L);
+  g->lanes.clear();
   if (g->lp_ring) cudaFreeHost(g->lp_ring);
-  if (g->status_host) cudaFreeHost(g->status_host);
-  if (g->norms_host) cudaFreeHost(g->norms_host);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
+  return MNPBEM_OK;
+}
+
+mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes) {
+  MNP_TRY(check_geom(g));
+  if (lanes < 0 || lanes > MAX_LANES) {
+    set_error("lanes must be 0 (automatic) .. %d", MAX_LANES);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  g->lanes_req = lanes;
   return MNPBEM_OK;
 }
 
@@ -355,15 +424,14 @@ mnpbem_status mnpbem_assemble(mnpbem_geom* G, const double* k_media, int32_t nme
   }
   MNP_CUDA(cudaSetDevice(G->device));
   ProfBind pb_(&G->prof);
-  std::vector<std::complex<double>> km(nmed);
-  for (int m = 0; m < nmed; ++m) km[m] = cx(k_media + 2 * m);
+  Lane& L = *G->lanes[0];
   {
     LamParams lp{};
-    for (int m = 0; m < nmed; ++m) lp.k[m] = make_double2(km[m].real(), km[m].imag());
-    MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(lp), cudaMemcpyHostToDevice, G->st));
+    for (int m = 0; m < nmed; ++m) lp.k[m] = make_double2(k_media[2 * m], k_media[2 * m + 1]);
+    MNP_CUDA(cudaMemcpyAsync(L.lp_dev.ptr, &lp, sizeof(lp), cudaMemcpyHostToDevice, G->st));
     MNP_CUDA(cudaStreamSynchronize(G->st));
   }
-  AsmParams p = base_params(G, km);
+  AsmParams p = base_params(G, L.lp_dev.as<LamParams>());
   const int64_t n = G->g.n;
   const bool w64 = precision == MNPBEM_FP64;
   const size_t es = w64 ? sizeof(double2) : sizeof(float2);
@@ -468,50 +536,87 @@ mnpbem_status mnpbem_geom_stream(const mnpbem_geom* G, void** stream) {
 // per-wavelength solver
 // ======================================================================
 // The work of one wavelength is split into stages that depend on the
-// wavelength only through the device parameter block G->lp_dev:
+// wavelength only through the lane's device parameter block lp_dev:
 //   S0 assemble        per-face eps + G1, H1, G2, H2 (complex64 and/or complex128)
 //   S1 initmat         inversions, products, Sigma stage
 //   S2 first solve     excitation + mldivide chain (+ conversions)
 //   S3 refinement step FP64 residual of the full operator + chain + update (MIXED)
 //   S4 spectra         far fields + extinction / scattering into a fixed slot
-// The first wavelength of a configuration runs the stages directly (sizing
-// every buffer); later wavelengths replay the stages as CUDA graphs.
+// The first wavelength a lane runs for a configuration goes through the
+// stages directly (sizing every buffer); the lane then captures each stage as
+// a CUDA graph and replays the graphs for its later wavelengths.
 namespace {
 
 struct SolveCtx {
-  mnpbem_geom* G;
   int P;
   int precision;
   const mnpbem_planewave* exc;
-  FaceData fd;
 };
 
-mnpbem_status ensure_workspace(mnpbem_geom* G, int precision, int P, int ninf) {
+size_t lane_bytes_estimate(const mnpbem_geom* G, int precision, int P, int ninf) {
+  const size_t n = G->g.n, ld = G->ld;
+  const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
+  size_t b = 5 * es * n * ld;
+  if (precision == MNPBEM_MIXED) b += 4 * 2 * sizeof(float2) * n * ld + 16 * n * n;  // planes + B' of the n^3 GEMMs
+  b += sizeof(double2) * n * P * 72 + sizeof(float2) * n * P * 56;
+  b += 3 * es * n * 256 + sizeof(double2) * (size_t)(P + ninf) * 6 * P + 64 * n;
+  return b;
+}
+
+mnpbem_status ensure_workspace(mnpbem_geom* G, Lane& L, int precision, int P, int ninf) {
   const int64_t n = G->g.n, ld = G->ld;
   const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
-  for (int q = 0; q < 5; ++q) MNP_TRY(G->mat[q].ensure(es * n * ld));
+  for (int q = 0; q < 5; ++q) MNP_TRY(L.mat[q].ensure(es * n * ld));
   if (precision == MNPBEM_MIXED)
-    for (int q = 0; q < 4; ++q) MNP_TRY(G->mat64[q].ensure(sizeof(double2) * n * ld));
+    for (int q = 0; q < 4; ++q) MNP_TRY(L.mat64[q].ensure(2 * sizeof(float2) * n * ld));
   // FP64 vectors: b (8nP) x (8nP) r (8nP) YZ (16nP) + chain work for FP64 (32nP)
-  MNP_TRY(G->vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32)));
+  MNP_TRY(L.vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32)));
   // working-precision vectors for MIXED: in (8nP) out (8nP) work (32nP)
-  MNP_TRY(G->vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
-  MNP_TRY(G->norms.ensure(sizeof(double) * 4));
-  MNP_TRY(G->bsplit.ensure(sizeof(float2) * 2 * n * 4 * P));
-  MNP_TRY(G->facebuf.ensure(sizeof(double2) * 2 * n + sizeof(float2) * 3 * n + sizeof(float) * 3 * n + 2 * n + 256));
-  MNP_TRY(G->fields.ensure(sizeof(double2) * (size_t)(P + ninf) * 6 * P));
-  MNP_TRY(G->outbuf.ensure(sizeof(double) * 2 * P));   // ext / sca slot of the current wavelength
+  MNP_TRY(L.vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
+  MNP_TRY(L.norms.ensure(sizeof(double) * 4));
+  MNP_TRY(L.bsplit.ensure(sizeof(float2) * 2 * n * 4 * P));
+  MNP_TRY(L.facebuf.ensure(sizeof(double2) * 2 * n + sizeof(float2) * 3 * n + sizeof(float) * 3 * n + 2 * n + 256));
+  MNP_TRY(L.fields.ensure(sizeof(double2) * (size_t)(P + ninf) * 6 * P));
+  MNP_TRY(L.outbuf.ensure(sizeof(double) * 2 * P));   // ext / sca slot of the current wavelength
   return MNPBEM_OK;
 }
 
-FaceData face_data(mnpbem_geom* G) {
+// fingerprint of every device address a lane's graphs capture
+uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](const void* p, size_t b) {
+    h = (h ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
+    h = (h ^ (uint64_t)b) * 1099511628211ull;
+  };
+  auto mixbuf = [&](const DevBuf& d) { mix(d.ptr, d.bytes); };
+  for (int q = 0; q < 5; ++q) mixbuf(L.mat[q]);
+  for (int q = 0; q < 4; ++q) mixbuf(L.mat64[q]);
+  mixbuf(L.vec64); mixbuf(L.vecw); mixbuf(L.facebuf); mixbuf(L.fields); mixbuf(L.norms);
+  mixbuf(L.outbuf); mixbuf(L.bsplit); mixbuf(L.lp_dev); mixbuf(G->exbuf);
+  mixbuf(L.tc.bexp); mixbuf(L.tc.err);
+  auto gj = [&](const auto& w) {
+    mixbuf(w.ccol); mixbuf(w.rrow); mixbuf(w.ncol); mixbuf(w.xblk); mixbuf(w.status);
+    mix(nullptr, (size_t)w.nb);
+    if (w.inner) {
+      mixbuf(w.inner->ccol); mixbuf(w.inner->rrow); mixbuf(w.inner->ncol); mixbuf(w.inner->xblk);
+      mixbuf(w.inner->status);
+    }
+  };
+  gj(L.gj32);
+  gj(L.gj64);
+  mix(L.status_host, 0);
+  mix(L.norms_host, 0);
+  return h;
+}
+
+FaceData face_data(mnpbem_geom* G, Lane& L) {
   const int64_t n = G->g.n;
   FaceData f;
   f.n = n;
   f.pos = G->g.pos;
   f.nvec = G->g.nvec;
   f.area = G->g.area;
-  double2* e = G->facebuf.as<double2>();
+  double2* e = L.facebuf.as<double2>();
   f.eps1 = e;
   f.eps2 = e + n;
   float2* ef = reinterpret_cast<float2*>(e + 2 * n);
@@ -524,24 +629,17 @@ FaceData face_data(mnpbem_geom* G) {
   return f;
 }
 
-mnpbem_status upload_masks(mnpbem_geom* G, int medium) {
-  const int64_t n = G->g.n;
-  std::vector<unsigned char> m(2 * n);
-  for (int64_t i = 0; i < n; ++i) {
-    int p = G->face_part[i];
-    m[i] = G->inout[2 * p] == medium;
-    m[n + i] = G->inout[2 * p + 1] == medium;
-  }
-  unsigned char* dst = const_cast<unsigned char*>(face_data(G).exc_in);
-  MNP_CUDA(cudaMemcpyAsync(dst, m.data(), 2 * n, cudaMemcpyHostToDevice, G->st));
-  MNP_CUDA(cudaStreamSynchronize(G->st));
+mnpbem_status upload_masks(mnpbem_geom* G, Lane& L, const std::vector<unsigned char>& m) {
+  unsigned char* dst = const_cast<unsigned char*>(face_data(G, L).exc_in);
+  MNP_CUDA(cudaMemcpyAsync(dst, m.data(), m.size(), cudaMemcpyHostToDevice, L.st));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
   return MNPBEM_OK;
 }
 
 template <typename R>
-GJWork<R>& gjw(mnpbem_geom* G);
-template <> GJWork<float>& gjw<float>(mnpbem_geom* G) { return G->gj32; }
-template <> GJWork<double>& gjw<double>(mnpbem_geom* G) { return G->gj64; }
+GJWork<R>& gjw(Lane& L);
+template <> GJWork<float>& gjw<float>(Lane& L) { return L.gj32; }
+template <> GJWork<double>& gjw<double>(Lane& L) { return L.gj64; }
 
 template <typename R>
 mnpbem_status gemm_w(int64_t M, int64_t N, int64_t K, cplx<R> al, const cplx<R>* A, int64_t lda,
@@ -561,75 +659,78 @@ mnpbem_status gemm_w<double>(int64_t M, int64_t N, int64_t K, double2 al, const 
 }
 
 template <typename R>
-ChainMats<R> chain_mats(mnpbem_geom* G) {
+ChainMats<R> chain_mats(const mnpbem_geom* G, Lane& L) {
   using Cx = cplx<R>;
   ChainMats<R> m;
-  m.G1i = G->mat[0].as<Cx>();
-  m.G2i = G->mat[1].as<Cx>();
-  m.Sigma1 = G->mat[4].as<Cx>();
-  m.Deltai = G->mat[3].as<Cx>();
-  m.Sigmai = G->mat[2].as<Cx>();
+  m.G1i = L.mat[0].as<Cx>();
+  m.G2i = L.mat[1].as<Cx>();
+  m.Sigma1 = L.mat[4].as<Cx>();
+  m.Deltai = L.mat[3].as<Cx>();
+  m.Sigmai = L.mat[2].as<Cx>();
   m.ld = G->ld;
   return m;
 }
 
+void* tc_ctx(mnpbem_geom* G, Lane& L) { return G->tc_enabled ? (void*)&L.tc : nullptr; }
+
 // ---------------------------------------------------------------- S0
-mnpbem_status stage_assemble(mnpbem_geom* G, int precision) {
+mnpbem_status stage_assemble(mnpbem_geom* G, Lane& L, int precision) {
   const int64_t n = G->g.n, ld = G->ld;
   const int* fm = G->face_med.as<int>();
-  FaceData f = face_data(G);
-  launch_face_eps(n, fm, fm + n, G->lp_dev.as<LamParams>(), G->g.nvec, const_cast<double2*>(f.eps1),
+  FaceData f = face_data(G, L);
+  const LamParams* lp = L.lp_dev.as<LamParams>();
+  launch_face_eps(n, fm, fm + n, lp, G->g.nvec, const_cast<double2*>(f.eps1),
                   const_cast<double2*>(f.eps2), const_cast<float2*>(f.eps1f), const_cast<float2*>(f.eps2f),
-                  const_cast<float2*>(f.Lf), const_cast<float*>(f.nvecf), G->st);
+                  const_cast<float2*>(f.Lf), const_cast<float*>(f.nvecf), L.st);
   MNP_CHECK_LAUNCH();
-  AsmParams p = base_params(G, {});
+  AsmParams p = base_params(G, lp);
   if (precision == MNPBEM_FP64) {
     p.ld64 = ld;
-    p.G1 = G->mat[0].as<double2>(); p.G2 = G->mat[1].as<double2>();
-    p.H1 = G->mat[2].as<double2>(); p.H2 = G->mat[3].as<double2>();
-    return assemble_launch(p, true, false, G->st);
+    p.G1 = L.mat[0].as<double2>(); p.G2 = L.mat[1].as<double2>();
+    p.H1 = L.mat[2].as<double2>(); p.H2 = L.mat[3].as<double2>();
+    return assemble_launch(p, true, false, L.st);
   }
   p.ld32 = ld;
-  p.g1 = G->mat[0].as<float2>(); p.g2 = G->mat[1].as<float2>();
-  p.h1 = G->mat[2].as<float2>(); p.h2 = G->mat[3].as<float2>();
+  p.g1 = L.mat[0].as<float2>(); p.g2 = L.mat[1].as<float2>();
+  p.h1 = L.mat[2].as<float2>(); p.h2 = L.mat[3].as<float2>();
   // residual matrices as hi / lo complex64 planes (mat64[q]: hi [n][ld] then lo [n][ld])
   float2* hl[4];
-  for (int q = 0; q < 4; ++q) hl[q] = G->mat64[q].as<float2>();
+  for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
   p.G1hi = hl[0]; p.G1lo = hl[0] + n * ld;
   p.H1hi = hl[1]; p.H1lo = hl[1] + n * ld;
   p.G2hi = hl[2]; p.G2lo = hl[2] + n * ld;
   p.H2hi = hl[3]; p.H2lo = hl[3] + n * ld;
-  return assemble_launch(p, true, true, G->st);
+  return assemble_launch(p, true, true, L.st);
 }
 
 // ---------------------------------------------------------------- S1
 template <typename R>
-mnpbem_status stage_initmat(mnpbem_geom* G, bool direct) {
+mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   using Cx = cplx<R>;
   const int64_t n = G->g.n, ld = G->ld;
   Cx* M[5];
-  for (int q = 0; q < 5; ++q) M[q] = G->mat[q].as<Cx>();
-  void* ctx = (sizeof(R) == 4 && G->tc_enabled) ? (void*)&G->tc : nullptr;
+  for (int q = 0; q < 5; ++q) M[q] = L.mat[q].as<Cx>();
+  void* ctx = sizeof(R) == 4 ? tc_ctx(G, L) : nullptr;
   // wider Gauss-Jordan steps when the rank-nb updates run on tensor cores:
   // fewer passes over the n x n matrix (each step reads and writes it once)
-  gjw<R>(G).nb = (ctx && n >= 1024) ? 256 : 64;
+  gjw<R>(L).nb = (ctx && n >= 1024) ? 256 : 64;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
-  const FaceData fd = face_data(G);
-  const LamParams* lp = G->lp_dev.as<LamParams>();
+  const FaceData fd = face_data(G, L);
+  const LamParams* lp = L.lp_dev.as<LamParams>();
   // G1i, G2i
-  MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
-  MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
+  MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
+  MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
   // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, G->st, ctx));
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, G->st, ctx));
+  MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, L.st, ctx));
+  MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, L.st, ctx));
   // Delta -> M3, Sigma (partial) -> M2
-  launch_delta_sigma<R>(n, M[4], M[2], M[3], ld, fd, G->st);
+  launch_delta_sigma<R>(n, M[4], M[2], M[3], ld, fd, L.st);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[3], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
-  launch_sigma_add<R>(n, M[2], M[3], ld, fd, lp, G->st);
+  MNP_TRY(gj_invert<R>(M[3], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
+  launch_sigma_add<R>(n, M[2], M[3], ld, fd, lp, L.st);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(G), gemm_w<R>, ctx, G->st, direct));
-  if (direct && ctx) MNP_TRY(tc_check_error(G->tc, G->st));
+  MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
+  if (direct && ctx) MNP_TRY(tc_check_error(L.tc, L.st));
   return MNPBEM_OK;
 }
 
@@ -637,10 +738,10 @@ mnpbem_status stage_initmat(mnpbem_geom* G, bool direct) {
 struct Vec64 {
   double2 *phi, *a, *alpha, *De, *x1, *x2, *rphi, *ra, *ral, *rDe, *Y1, *Y2, *Z1, *Z2, *work;
 };
-Vec64 vec64(mnpbem_geom* G, int P) {
+Vec64 vec64(const mnpbem_geom* G, Lane& L, int P) {
   const int64_t n = G->g.n;
   Vec64 v;
-  double2* V = G->vec64.as<double2>();
+  double2* V = L.vec64.as<double2>();
   v.phi = V; v.a = v.phi + n * P; v.alpha = v.a + 3 * n * P; v.De = v.alpha + 3 * n * P;
   v.x1 = v.De + n * P; v.x2 = v.x1 + 4 * n * P;
   v.rphi = v.x2 + 4 * n * P; v.ra = v.rphi + n * P; v.ral = v.ra + 3 * n * P; v.rDe = v.ral + 3 * n * P;
@@ -650,11 +751,11 @@ Vec64 vec64(mnpbem_geom* G, int P) {
 }
 
 // complex64 chain applied to FP64 inputs, result in fx1/fx2
-mnpbem_status apply32(mnpbem_geom* G, const FaceData& fd, int P, const double2* p_, const double2* a_,
+mnpbem_status apply32(mnpbem_geom* G, Lane& L, int P, const double2* p_, const double2* a_,
                       const double2* al_, const double2* De_) {
   const int64_t n = G->g.n;
-  cudaStream_t st = G->st;
-  float2* W = G->vecw.as<float2>();
+  cudaStream_t st = L.st;
+  float2* W = L.vecw.as<float2>();
   float2 *fphi = W, *fa = fphi + n * P, *fal = fa + 3 * n * P, *fDe = fal + 3 * n * P;
   float2 *fx1 = fDe + n * P, *fx2 = fx1 + 4 * n * P, *fwork = fx2 + 4 * n * P;
   launch_cvt_d2f(p_, fphi, n * P, st);
@@ -662,108 +763,108 @@ mnpbem_status apply32(mnpbem_geom* G, const FaceData& fd, int P, const double2* 
   launch_cvt_d2f(al_, fal, 3 * n * P, st);
   launch_cvt_d2f(De_, fDe, n * P, st);
   MNP_CHECK_LAUNCH();
-  void* ctx = G->tc_enabled ? (void*)&G->tc : nullptr;
-  return apply_mldivide<float>(fd, P, G->lp_dev.as<LamParams>(), chain_mats<float>(G), fphi, fa, fal, fDe,
-                               fx1, fx2, fwork, gemm_w<float>, ctx, st);
+  return apply_mldivide<float>(face_data(G, L), P, L.lp_dev.as<LamParams>(), chain_mats<float>(G, L), fphi, fa,
+                               fal, fDe, fx1, fx2, fwork, gemm_w<float>, tc_ctx(G, L), st);
 }
-float2* fx_ptr(mnpbem_geom* G, int P, int which) {
+float2* fx_ptr(const mnpbem_geom* G, Lane& L, int P, int which) {
   const int64_t n = G->g.n;
-  return G->vecw.as<float2>() + 8 * n * P + (which ? 4 * n * P : 0);
+  return L.vecw.as<float2>() + 8 * n * P + (which ? 4 * n * P : 0);
 }
 
 // ---------------------------------------------------------------- S2
-mnpbem_status stage_first(mnpbem_geom* G, const SolveCtx& c) {
+mnpbem_status stage_first(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const int64_t n = G->g.n;
   const int P = c.P;
-  Vec64 v = vec64(G, P);
+  Vec64 v = vec64(G, L, P);
   const double* pol = G->exbuf.as<double>();
   const double* dirs = pol + 3 * P;
-  const LamParams* lp = G->lp_dev.as<LamParams>();
-  launch_excitation(c.fd, P, pol, dirs, lp, v.phi, v.a, v.alpha, v.De, G->st);
+  const LamParams* lp = L.lp_dev.as<LamParams>();
+  const FaceData fd = face_data(G, L);
+  launch_excitation(fd, P, pol, dirs, lp, v.phi, v.a, v.alpha, v.De, L.st);
   MNP_CHECK_LAUNCH();
   if (c.precision == MNPBEM_FP64)
-    return apply_mldivide<double>(c.fd, P, lp, chain_mats<double>(G), v.phi, v.a, v.alpha, v.De, v.x1, v.x2,
-                                  v.work, gemm_w<double>, nullptr, G->st);
-  MNP_TRY(apply32(G, c.fd, P, v.phi, v.a, v.alpha, v.De));
-  launch_cvt_f2d(fx_ptr(G, P, 0), v.x1, 4 * n * P, G->st);
-  launch_cvt_f2d(fx_ptr(G, P, 1), v.x2, 4 * n * P, G->st);
+    return apply_mldivide<double>(fd, P, lp, chain_mats<double>(G, L), v.phi, v.a, v.alpha, v.De, v.x1, v.x2,
+                                  v.work, gemm_w<double>, nullptr, L.st);
+  MNP_TRY(apply32(G, L, P, v.phi, v.a, v.alpha, v.De));
+  launch_cvt_f2d(fx_ptr(G, L, P, 0), v.x1, 4 * n * P, L.st);
+  launch_cvt_f2d(fx_ptr(G, L, P, 1), v.x2, 4 * n * P, L.st);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
 }
 
 // ---------------------------------------------------------------- S3
 // norms[0..1] = ||r||^2, ||b||^2 ; norms[2..3] = ||dx||^2, ||x||^2
-mnpbem_status stage_iter(mnpbem_geom* G, const SolveCtx& c) {
+mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const int64_t n = G->g.n;
   const int P = c.P;
-  cudaStream_t st = G->st;
-  Vec64 v = vec64(G, P);
+  cudaStream_t st = L.st;
+  Vec64 v = vec64(G, L, P);
   const int64_t ld = G->ld;
   const float2* hl[4];
-  for (int q = 0; q < 4; ++q) hl[q] = G->mat64[q].as<float2>();
-  double* norms = G->norms.as<double>();
+  for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
+  double* norms = L.norms.as<double>();
   // G1 x1, G2 x2, H1 x1, H2 x2 in double-single arithmetic from the hi / lo planes
-  float2* bs = G->bsplit.as<float2>();
+  float2* bs = L.bsplit.as<float2>();
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], hl[0] + n * ld, ld, v.x1, 4 * P, v.Y1, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], hl[1] + n * ld, ld, v.x1, 4 * P, v.Z1, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], hl[2] + n * ld, ld, v.x2, 4 * P, v.Y2, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], hl[3] + n * ld, ld, v.x2, 4 * P, v.Z2, 4 * P, bs, st));
   MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
-  launch_residual(c.fd, P, G->lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.phi, v.a, v.alpha, v.De,
-                  v.rphi, v.ra, v.ral, v.rDe, norms, st);
+  launch_residual(face_data(G, L), P, L.lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.phi, v.a, v.alpha,
+                  v.De, v.rphi, v.ra, v.ral, v.rDe, norms, st);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(apply32(G, c.fd, P, v.rphi, v.ra, v.ral, v.rDe));
-  launch_axpy_norm(v.x1, fx_ptr(G, P, 0), 4 * n * P, norms + 2, st);
-  launch_axpy_norm(v.x2, fx_ptr(G, P, 1), 4 * n * P, norms + 2, st);
+  MNP_TRY(apply32(G, L, P, v.rphi, v.ra, v.ral, v.rDe));
+  launch_axpy_norm(v.x1, fx_ptr(G, L, P, 0), 4 * n * P, norms + 2, st);
+  launch_axpy_norm(v.x2, fx_ptr(G, L, P, 1), 4 * n * P, norms + 2, st);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
 }
 
 // ---------------------------------------------------------------- S4
-mnpbem_status stage_spectra(mnpbem_geom* G, const SolveCtx& c) {
+mnpbem_status stage_spectra(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const int P = c.P;
-  Vec64 v = vec64(G, P);
+  Vec64 v = vec64(G, L, P);
   const double* pol = G->exbuf.as<double>();
   const double* dirs = pol + 3 * P;
   const int ninf = c.exc->ninf;
   const double* inf_nvec = dirs + 3 * P;
   const double* inf_area = inf_nvec + 3 * ninf;
-  double2* fields = G->fields.as<double2>();
-  const LamParams* lp = G->lp_dev.as<LamParams>();
-  launch_farfield(c.fd, P, v.x1, v.x2, dirs, P + ninf, lp, fields, G->st);
+  double2* fields = L.fields.as<double2>();
+  const LamParams* lp = L.lp_dev.as<LamParams>();
+  launch_farfield(face_data(G, L), P, v.x1, v.x2, dirs, P + ninf, lp, fields, L.st);
   MNP_CHECK_LAUNCH();
-  double* slot = G->outbuf.as<double>();
-  launch_cross_sections_lp(P, pol, inf_nvec, inf_area, ninf, fields, lp, slot, slot + P, G->st);
+  double* slot = L.outbuf.as<double>();
+  launch_cross_sections_lp(P, pol, inf_nvec, inf_area, ninf, fields, lp, slot, slot + P, L.st);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
 }
 
-mnpbem_status run_stage(mnpbem_geom* G, const SolveCtx& c, int stage, bool direct) {
+mnpbem_status run_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage, bool direct) {
   switch (stage) {
-    case 0: return stage_assemble(G, c.precision);
-    case 1: return c.precision == MNPBEM_FP64 ? stage_initmat<double>(G, direct) : stage_initmat<float>(G, direct);
-    case 2: return stage_first(G, c);
-    case 3: return stage_iter(G, c);
-    default: return stage_spectra(G, c);
+    case 0: return stage_assemble(G, L, c.precision);
+    case 1: return c.precision == MNPBEM_FP64 ? stage_initmat<double>(G, L, direct) : stage_initmat<float>(G, L, direct);
+    case 2: return stage_first(G, L, c);
+    case 3: return stage_iter(G, L, c);
+    default: return stage_spectra(G, L, c);
   }
 }
 
 // capture one stage into a graph; profiling events recorded during the
 // capture become event nodes whose timings are read after every replay
-mnpbem_status capture_stage(mnpbem_geom* G, const SolveCtx& c, int stage) {
-  auto& gr = G->graphs;
+mnpbem_status capture_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage) {
+  auto& gr = L.graphs;
   Profiler cap;
   cap.enabled = G->prof.enabled;
   ProfBind pb(&cap);
   capturing_now() = true;
-  cudaError_t e = cudaStreamBeginCapture(G->st, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) {
     capturing_now() = false;
     MNP_CUDA(e);
   }
-  mnpbem_status s = run_stage(G, c, stage, false);
+  mnpbem_status s = run_stage(G, L, c, stage, false);
   cudaGraph_t graph = nullptr;
-  e = cudaStreamEndCapture(G->st, &graph);
+  e = cudaStreamEndCapture(L.st, &graph);
   capturing_now() = false;
   if (s != MNPBEM_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -782,9 +883,9 @@ mnpbem_status capture_stage(mnpbem_geom* G, const SolveCtx& c, int stage) {
   return MNPBEM_OK;
 }
 
-void drop_graphs(mnpbem_geom* G) {
-  auto& gr = G->graphs;
-  cudaStreamSynchronize(G->st);
+void drop_graphs(mnpbem_geom* G, Lane& L) {
+  auto& gr = L.graphs;
+  cudaStreamSynchronize(L.st);
   G->prof.flush();          // replayed records must be read before their events go
   for (int q = 0; q < 5; ++q) {
     if (gr.exec[q]) cudaGraphExecDestroy(gr.exec[q]);
@@ -795,51 +896,65 @@ void drop_graphs(mnpbem_geom* G) {
   cudaGetLastError();
 }
 
-mnpbem_status launch_stage(mnpbem_geom* G, const SolveCtx& c, int stage, bool graphs) {
-  if (!graphs) return run_stage(G, c, stage, true);
-  MNP_CUDA(cudaGraphLaunch(G->graphs.exec[stage], G->st));
-  G->prof.replayed.push_back(&G->graphs.rec[stage]);
+bool graphs_match(const mnpbem_geom* G, const Lane& L, const SolveCtx& c) {
+  const auto& gr = L.graphs;
+  return gr.valid && gr.precision == c.precision && gr.P == c.P && gr.ninf == c.exc->ninf &&
+         gr.prof == G->prof.enabled && gr.sig == lane_sig(G, L);
+}
+
+mnpbem_status launch_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage, bool graphs) {
+  if (!graphs) return run_stage(G, L, c, stage, true);
+  MNP_CUDA(cudaGraphLaunch(L.graphs.exec[stage], L.st));
+  G->prof.replayed.push_back(&L.graphs.rec[stage]);
   return MNPBEM_OK;
 }
 
-mnpbem_status check_pivots(mnpbem_geom* G) {
-  if (G->status_host[0] | G->status_host[1]) {
+mnpbem_status check_pivots(const Lane& L) {
+  if (L.status_host[0] | L.status_host[1]) {
     set_error("block Gauss-Jordan inversion: zero or non-finite pivot");
     return MNPBEM_ERR_SINGULAR;
   }
   return MNPBEM_OK;
 }
 
-// one wavelength through all stages; graphs == true replays captured stages
-mnpbem_status solve_one(mnpbem_geom* G, const SolveCtx& c, const mnpbem_refine* ref, bool graphs,
+mnpbem_status status_copy(Lane& L, int precision) {
+  if (precision == MNPBEM_FP64) return gj_status_copy<double>(L.gj64, L.status_host, L.st);
+  return gj_status_copy<float>(L.gj32, L.status_host, L.st);
+}
+
+struct Refine {
+  int maxit;
+  double tol;
+};
+
+// one wavelength through all stages, synchronously (graphs == true replays
+// captured stages; false runs the stages directly and sizes the buffers)
+mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine& ref, bool graphs,
                         int32_t* iters, double* resid) {
-  cudaStream_t st = G->st;
-  for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, c, stage, graphs));
-  if (graphs) {
-    if (c.precision == MNPBEM_FP64) MNP_TRY(gj_status_copy<double>(G->gj64, G->status_host, st));
-    else MNP_TRY(gj_status_copy<float>(G->gj32, G->status_host, st));
-  } else {
-    G->status_host[0] = G->status_host[1] = 0;
-  }
+  cudaStream_t st = L.st;
+  for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, L, c, stage, graphs));
+  if (graphs) MNP_TRY(status_copy(L, c.precision));
+  else L.status_host[0] = L.status_host[1] = 0;
   int used = 0;
   double final_res = -1.0;
   if (c.precision == MNPBEM_MIXED) {
-    const int maxit = ref && ref->max_iter > 0 ? ref->max_iter : 10;
-    const double tol = ref && ref->tol > 0 ? ref->tol : 1e-10;
-    double* hn = G->norms_host;
-    for (int it = 0; it < maxit; ++it) {
-      MNP_TRY(launch_stage(G, c, 3, graphs));
-      MNP_CUDA(cudaMemcpyAsync(hn, G->norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    double* hn = L.norms_host;
+    for (int it = 0; it < ref.maxit; ++it) {
+      MNP_TRY(launch_stage(G, L, c, 3, graphs));
+      MNP_CUDA(cudaMemcpyAsync(hn, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       MNP_CUDA(cudaStreamSynchronize(st));
       G->prof.flush();
-      MNP_TRY(check_pivots(G));
+      MNP_TRY(check_pivots(L));
       used = it + 1;
       final_res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
       if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-      if (sqrt(hn[2]) <= tol * sqrt(hn[3])) break;
+      if (sqrt(hn[2]) <= ref.tol * sqrt(hn[3])) break;
     }
   }
-  MNP_TRY(launch_stage(G, c, 4, graphs));
+  MNP_TRY(launch_stage(G, L, c, 4, graphs));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  G->prof.flush();
+  MNP_TRY(check_pivots(L));
   if (iters) *iters = used;
   if (resid) *resid = final_res;
   return MNPBEM_OK;
@@ -863,11 +978,221 @@ void fill_lp(LamParams& lp, double enei, const double* em, int nmed, int medium,
 
 mnpbem_status ensure_lp_ring(mnpbem_geom* G, int count) {
   if (G->lp_cap >= count) return MNPBEM_OK;
-  if (G->lp_ring) cudaFreeHost(G->lp_ring);
+  if (G->lp_ring) cudaFreeHost(G->lp_ring);   // every lane was synchronised at the end of the last call
   G->lp_ring = nullptr;
   G->lp_cap = 0;
   MNP_CUDA(cudaMallocHost(&G->lp_ring, sizeof(LamParams) * count));
   G->lp_cap = count;
+  return MNPBEM_OK;
+}
+
+// ----------------------------------------------------------- sweep scheduler
+struct Sweep {
+  int nenei;
+  const double* enei;
+  const double* eps;
+  int nmed;
+  int medium;
+  Refine ref;
+  mnpbem_solution* out;
+};
+
+mnpbem_status upload_lp(mnpbem_geom* G, Lane& L, const Sweep& s, int w) {
+  LamParams& lp = G->lp_ring[w];
+  fill_lp(lp, s.enei[w], s.eps + 2 * (size_t)s.nmed * w, s.nmed, s.medium, 0);
+  MNP_CUDA(cudaMemcpyAsync(L.lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, L.st));
+  return MNPBEM_OK;
+}
+
+// copies of wavelength w's results from the lane into the caller's outputs
+mnpbem_status write_outputs(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s, int w) {
+  mnpbem_solution* out = s.out;
+  const int P = c.P;
+  const int64_t n = G->g.n;
+  const cudaMemcpyKind kind = out->outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  const size_t cs = sizeof(double2);
+  Vec64 v = vec64(G, L, P);
+  auto cp2 = [&](double* dst, const double2* src, int off, int width) -> mnpbem_status {
+    if (!dst) return MNPBEM_OK;
+    MNP_CUDA(cudaMemcpy2DAsync(dst + 2 * (size_t)w * n * width, cs * width, src + off, cs * 4 * P,
+                               cs * width, n, kind, L.st));
+    return MNPBEM_OK;
+  };
+  MNP_TRY(cp2(out->sig1, v.x1, 0, P));
+  MNP_TRY(cp2(out->h1, v.x1, P, 3 * P));
+  MNP_TRY(cp2(out->sig2, v.x2, 0, P));
+  MNP_TRY(cp2(out->h2, v.x2, P, 3 * P));
+  const double* slot = L.outbuf.as<double>();
+  if (out->ext) MNP_CUDA(cudaMemcpyAsync(out->ext + (size_t)w * P, slot, sizeof(double) * P, kind, L.st));
+  if (out->sca) MNP_CUDA(cudaMemcpyAsync(out->sca + (size_t)w * P, slot + P, sizeof(double) * P, kind, L.st));
+  if (out->ir_iters) out->ir_iters[w] = L.iters;
+  if (out->ir_resid) out->ir_resid[w] = L.res;
+  return MNPBEM_OK;
+}
+
+mnpbem_status queue_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
+  MNP_TRY(launch_stage(G, L, c, 3, true));
+  MNP_CUDA(cudaMemcpyAsync(L.norms_host, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+  MNP_CUDA(cudaEventRecord(L.ev, L.st));
+  L.state = Lane::ITER;
+  return MNPBEM_OK;
+}
+
+mnpbem_status queue_finish(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
+  MNP_TRY(launch_stage(G, L, c, 4, true));
+  MNP_CUDA(cudaEventRecord(L.ev, L.st));
+  L.state = Lane::DONE;
+  return MNPBEM_OK;
+}
+
+// queue wavelength w on a lane with captured graphs (returns without waiting)
+mnpbem_status lane_start(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s, int w) {
+  L.w = w;
+  L.iters = 0;
+  L.res = -1.0;
+  MNP_TRY(upload_lp(G, L, s, w));
+  for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, L, c, stage, true));
+  MNP_TRY(status_copy(L, c.precision));
+  if (c.precision == MNPBEM_MIXED && s.ref.maxit > 0) return queue_iter(G, L, c);
+  return queue_finish(G, L, c);
+}
+
+// the lane's queued work has completed: decide what comes next
+mnpbem_status lane_advance(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s) {
+  if (G->prof.enabled) G->prof.flush();
+  MNP_TRY(check_pivots(L));
+  if (L.state == Lane::ITER) {
+    const double* hn = L.norms_host;
+    ++L.iters;
+    L.res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
+    if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
+    if (sqrt(hn[2]) <= s.ref.tol * sqrt(hn[3]) || L.iters >= s.ref.maxit) return queue_finish(G, L, c);
+    return queue_iter(G, L, c);
+  }
+  // DONE: results of L.w are in the lane; the stream is idle, so host-side
+  // copies into pageable memory do not wait on other work
+  MNP_TRY(write_outputs(G, L, c, s, L.w));
+  L.state = Lane::IDLE;
+  L.w = -1;
+  return MNPBEM_OK;
+}
+
+// number of lanes for this call: requested (or default), bounded by the
+// wavelengths and by the free device memory for lanes not yet allocated
+int choose_lanes(mnpbem_geom* G, int precision, int P, int ninf, int nenei) {
+  int want = G->lanes_req > 0 ? G->lanes_req : DEFAULT_LANES;
+  if (G->prof.enabled || !G->use_graphs) want = 1;
+  want = std::max(1, std::min(want, std::min(nenei, MAX_LANES)));
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  const size_t est = lane_bytes_estimate(G, precision, P, ninf);
+  const size_t reserve = std::max<size_t>((size_t)2 << 30, tot / 20);
+  int nl = 1;
+  for (int l = 1; l < want; ++l) {
+    size_t have = 0;
+    if (l < (int)G->lanes.size()) {
+      const Lane& L = *G->lanes[l];
+      for (int q = 0; q < 5; ++q) have += L.mat[q].bytes;
+      for (int q = 0; q < 4; ++q) have += L.mat64[q].bytes;
+    }
+    const size_t need = est > have ? est - have : 0;
+    if (fr < need + reserve) break;
+    fr -= need;
+    nl = l + 1;
+  }
+  return nl;
+}
+
+// phases of one call: lanes without graphs for this configuration run one
+// wavelength directly and capture their stages; the remaining wavelengths go
+// to the lanes as they free up
+mnpbem_status run_sweep(mnpbem_geom* G, const SolveCtx& c, const Sweep& s, int nl) {
+  const int nenei = s.nenei, precision = c.precision, P = c.P;
+  const mnpbem_planewave* exc = c.exc;
+  int next = 0;
+  // 1. lanes without graphs for this configuration: run one wavelength
+  //    directly (sizing every buffer), then capture the stages
+  std::vector<int> fresh;
+  for (int l = 0; l < nl && next < nenei; ++l) {
+    Lane& L = *G->lanes[l];
+    if (graphs_match(G, L, c)) continue;
+    if (L.graphs.valid) drop_graphs(G, L);
+    const int w = next++;
+    MNP_TRY(upload_lp(G, L, s, w));
+    L.w = w;
+    MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
+    MNP_TRY(write_outputs(G, L, c, s, w));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
+    if (G->use_graphs) fresh.push_back(l);
+    if (!G->use_graphs) break;
+  }
+  for (int l : fresh) {
+    Lane& L = *G->lanes[l];
+    bool ok = true;
+    for (int stage = 0; stage < 5 && ok; ++stage) {
+      if (stage == 3 && precision != MNPBEM_MIXED) continue;
+      ok = capture_stage(G, L, c, stage) == MNPBEM_OK;
+    }
+    if (ok) {
+      auto& gr = L.graphs;
+      gr.valid = true;
+      gr.precision = precision;
+      gr.P = P;
+      gr.ninf = exc->ninf;
+      gr.prof = G->prof.enabled;
+      gr.sig = lane_sig(G, L);
+    } else {
+      drop_graphs(G, L);
+      G->use_graphs = false;   // run directly from now on
+    }
+  }
+  if (!G->use_graphs) {
+    // 2a. no graphs: every remaining wavelength directly on lane 0
+    Lane& L = *G->lanes[0];
+    for (; next < nenei; ++next) {
+      MNP_TRY(upload_lp(G, L, s, next));
+      L.w = next;
+      MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
+      MNP_TRY(write_outputs(G, L, c, s, next));
+    }
+  } else {
+    // 2b. the remaining wavelengths go to the lanes as they free up; the host
+    //     polls each lane's completion event and queues its next step
+    std::vector<Lane*> run;
+    for (int l = 0; l < nl; ++l)
+      if (graphs_match(G, *G->lanes[l], c)) run.push_back(G->lanes[l].get());
+    cudaEvent_t start;
+    MNP_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } eg{start};
+    MNP_CUDA(cudaEventRecord(start, G->st));
+    int active = 0;
+    for (Lane* L : run) {
+      MNP_CUDA(cudaStreamWaitEvent(L->st, start, 0));
+      if (next < nenei) {
+        MNP_TRY(lane_start(G, *L, c, s, next++));
+        ++active;
+      }
+    }
+    while (active > 0) {
+      bool progressed = false;
+      for (Lane* L : run) {
+        if (L->state == Lane::IDLE) continue;
+        const cudaError_t q = cudaEventQuery(L->ev);
+        if (q == cudaErrorNotReady) continue;
+        MNP_CUDA(q);
+        progressed = true;
+        MNP_TRY(lane_advance(G, *L, c, s));
+        if (L->state == Lane::IDLE) {
+          if (next < nenei) MNP_TRY(lane_start(G, *L, c, s, next++));
+          else --active;
+        }
+      }
+      if (!progressed) std::this_thread::yield();
+    }
+  }
   return MNPBEM_OK;
 }
 
@@ -904,8 +1229,7 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
   ProfBind pb_(&G->prof);
   const int P = exc->npol;
   const int64_t n = G->g.n;
-  MNP_TRY(ensure_workspace(G, precision, P, exc->ninf));
-  // excitation buffer: pol, dir, inf nvec, inf area
+  // excitation buffer shared by the lanes: pol, dir, inf nvec, inf area
   {
     std::vector<double> eb;
     eb.insert(eb.end(), exc->pol, exc->pol + 3 * P);
@@ -914,80 +1238,59 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
       eb.insert(eb.end(), exc->inf_nvec, exc->inf_nvec + 3 * exc->ninf);
       eb.insert(eb.end(), exc->inf_area, exc->inf_area + exc->ninf);
     }
+    for (auto& L : G->lanes) MNP_CUDA(cudaStreamSynchronize(L->st));   // nothing may still read exbuf
     MNP_TRY(G->exbuf.ensure(sizeof(double) * eb.size()));
-    MNP_CUDA(cudaMemcpyAsync(G->exbuf.ptr, eb.data(), sizeof(double) * eb.size(), cudaMemcpyHostToDevice, G->st));
+    MNP_CUDA(cudaMemcpy(G->exbuf.ptr, eb.data(), sizeof(double) * eb.size(), cudaMemcpyHostToDevice));
   }
-  MNP_TRY(upload_masks(G, exc->medium));
+  // lanes and their workspaces
+  const int nl = choose_lanes(G, precision, P, exc->ninf, nenei);
+  while ((int)G->lanes.size() < nl) MNP_TRY(add_lane(G));
+  std::vector<unsigned char> masks(2 * n);
+  for (int64_t i = 0; i < n; ++i) {
+    const int p = G->face_part[i];
+    masks[i] = G->inout[2 * p] == exc->medium;
+    masks[n + i] = G->inout[2 * p + 1] == exc->medium;
+  }
+  for (int l = 0; l < nl; ++l) {
+    MNP_TRY(ensure_workspace(G, *G->lanes[l], precision, P, exc->ninf));
+    MNP_TRY(upload_masks(G, *G->lanes[l], masks));
+  }
   MNP_TRY(ensure_lp_ring(G, nenei));
   SolveCtx c;
-  c.G = G;
   c.P = P;
   c.precision = precision;
   c.exc = exc;
-  c.fd = face_data(G);
-  auto& gr = G->graphs;
-  const cudaMemcpyKind kind = out->outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  const size_t cs = sizeof(double2);
-  for (int w = 0; w < nenei; ++w) {
-    LamParams& lp = G->lp_ring[w];
-    fill_lp(lp, enei[w], eps_media + 2 * (size_t)nmed * w, nmed, exc->medium, 0);
-    MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, G->st));
-    const bool want_graphs = G->use_graphs;
-    bool graphs = want_graphs && gr.valid && gr.precision == precision && gr.P == P &&
-                  gr.ninf == exc->ninf && gr.prof == G->prof.enabled && gr.gen == alloc_generation();
-    if (want_graphs && !graphs && gr.valid) drop_graphs(G);
-    int32_t it = 0;
-    double res = -1;
-    MNP_TRY(solve_one(G, c, refine, graphs, &it, &res));
-    if (want_graphs && !graphs) {
-      // first wavelength of this configuration ran directly and sized every
-      // buffer: capture the stages for the following wavelengths
-      MNP_CUDA(cudaStreamSynchronize(G->st));
-      G->prof.flush();
-      bool ok = true;
-      for (int stage = 0; stage < 5 && ok; ++stage) {
-        if (stage == 3 && precision != MNPBEM_MIXED) continue;
-        ok = capture_stage(G, c, stage) == MNPBEM_OK;
-      }
-      if (ok) {
-        gr.valid = true;
-        gr.precision = precision;
-        gr.P = P;
-        gr.ninf = exc->ninf;
-        gr.prof = G->prof.enabled;
-        gr.gen = alloc_generation();
-      } else {
-        drop_graphs(G);
-        G->use_graphs = false;   // run directly from now on
-      }
-    }
-    if (out->ir_iters) out->ir_iters[w] = it;
-    if (out->ir_resid) out->ir_resid[w] = res;
-    // outputs of this wavelength
-    Vec64 v = vec64(G, P);
-    auto cp2 = [&](double* dst, const double2* src, int off, int width) -> mnpbem_status {
-      if (!dst) return MNPBEM_OK;
-      MNP_CUDA(cudaMemcpy2DAsync(dst + 2 * (size_t)w * n * width, cs * width, src + off, cs * 4 * P,
-                                 cs * width, n, kind, G->st));
-      return MNPBEM_OK;
-    };
-    MNP_TRY(cp2(out->sig1, v.x1, 0, P));
-    MNP_TRY(cp2(out->h1, v.x1, P, 3 * P));
-    MNP_TRY(cp2(out->sig2, v.x2, 0, P));
-    MNP_TRY(cp2(out->h2, v.x2, P, 3 * P));
-    const double* slot = G->outbuf.as<double>();
-    if (out->ext) MNP_CUDA(cudaMemcpyAsync(out->ext + (size_t)w * P, slot, sizeof(double) * P, kind, G->st));
-    if (out->sca) MNP_CUDA(cudaMemcpyAsync(out->sca + (size_t)w * P, slot + P, sizeof(double) * P, kind, G->st));
-    if (precision == MNPBEM_FP64 && graphs) {
-      MNP_CUDA(cudaStreamSynchronize(G->st));
-      G->prof.flush();
-      MNP_TRY(check_pivots(G));
-    }
+  Sweep s;
+  s.nenei = nenei;
+  s.enei = enei;
+  s.eps = eps_media;
+  s.nmed = nmed;
+  s.medium = exc->medium;
+  s.ref.maxit = refine && refine->max_iter > 0 ? refine->max_iter : 10;
+  s.ref.tol = refine && refine->tol > 0 ? refine->tol : 1e-10;
+  s.out = out;
+  const mnpbem_status rs = run_sweep(G, c, s, nl);
+  if (rs != MNPBEM_OK) {
+    // leave nothing in flight that writes the caller's buffers
+    for (int l = 0; l < nl; ++l) cudaStreamSynchronize(G->lanes[l]->st);
+    cudaGetLastError();
+    G->prof.flush();
+    return rs;
   }
-  MNP_CUDA(cudaStreamSynchronize(G->st));
+  // join: the handle's stream waits for every lane
+  for (int l = 0; l < nl; ++l) {
+    Lane& L = *G->lanes[l];
+    if (L.st == G->st) continue;
+    MNP_CUDA(cudaEventRecord(L.ev, L.st));
+    MNP_CUDA(cudaStreamWaitEvent(G->st, L.ev, 0));
+  }
+  for (int l = 0; l < nl; ++l) MNP_CUDA(cudaStreamSynchronize(G->lanes[l]->st));
   G->prof.flush();
-  MNP_TRY(check_pivots(G));
-  if (precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(G->tc, G->st));
+  for (int l = 0; l < nl; ++l) {
+    Lane& L = *G->lanes[l];
+    MNP_TRY(check_pivots(L));
+    if (precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(L.tc, L.st));
+  }
   return MNPBEM_OK;
 }
 
@@ -1004,27 +1307,28 @@ mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps
   MNP_CUDA(cudaSetDevice(G->device));
   ProfBind pb_(&G->prof);
   const int64_t n = G->g.n, ld = G->ld;
-  MNP_TRY(ensure_workspace(G, precision, 1, 0));
+  Lane& L = *G->lanes[0];
+  MNP_TRY(ensure_workspace(G, L, precision, 1, 0));
   LamParams lp;
   fill_lp(lp, enei, eps_media, nmed, 1, 0);
-  MNP_CUDA(cudaMemcpyAsync(G->lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, G->st));
-  MNP_TRY(stage_assemble(G, precision));
-  if (precision == MNPBEM_FP64) MNP_TRY(stage_initmat<double>(G, true));
-  else MNP_TRY(stage_initmat<float>(G, true));
+  MNP_CUDA(cudaMemcpyAsync(L.lp_dev.ptr, &lp, sizeof(LamParams), cudaMemcpyHostToDevice, L.st));
+  MNP_TRY(stage_assemble(G, L, precision));
+  if (precision == MNPBEM_FP64) MNP_TRY(stage_initmat<double>(G, L, true));
+  else MNP_TRY(stage_initmat<float>(G, L, true));
   double* outs[5] = {G1i, G2i, Sigmai, Deltai, Sigma1};  // order of mat[0..4]
   DevBuf conv;
   if (precision == MNPBEM_MIXED) MNP_TRY(conv.ensure(sizeof(double2) * n * ld));
   for (int q = 0; q < 5; ++q) {
     if (!outs[q]) continue;
-    const double2* src = G->mat[q].as<double2>();
+    const double2* src = L.mat[q].as<double2>();
     if (precision == MNPBEM_MIXED) {
-      launch_cvt_f2d(G->mat[q].as<float2>(), conv.as<double2>(), n * ld, G->st);
+      launch_cvt_f2d(L.mat[q].as<float2>(), conv.as<double2>(), n * ld, L.st);
       MNP_CHECK_LAUNCH();
       src = conv.as<double2>();
     }
     MNP_CUDA(cudaMemcpy2DAsync(outs[q], sizeof(double2) * n, src, sizeof(double2) * ld,
-                               sizeof(double2) * n, n, cudaMemcpyDeviceToHost, G->st));
-    MNP_CUDA(cudaStreamSynchronize(G->st));
+                               sizeof(double2) * n, n, cudaMemcpyDeviceToHost, L.st));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
   }
   G->prof.flush();
   return MNPBEM_OK;

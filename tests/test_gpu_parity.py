@@ -205,3 +205,26 @@ def test_error_status(gpu_lib):
     assert e.value.status == 1
     with pytest.raises(m._lib.MnpbemError):
         bem.spectrum(m.planewave([1, 0, 0], [0, 0, 1]), [-5.0])
+
+
+def test_concurrent_lanes_match_serial(gpu_lib):
+    """Wavelengths in flight on several lanes give the results of one lane.
+
+    1200-face sphere (tensor-core path with 256-wide Gauss-Jordan steps), two
+    polarisations, seven wavelengths; the second call on three lanes replays
+    the graphs captured by the first."""
+    v, f = shapes.fibsphere(1200, 30.0)
+    cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
+    exc = m.planewave([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]])
+    enei = np.linspace(450.0, 700.0, 7)
+    bem = m.bemsolver(cp, m.bemoptions(precision="mixed", lanes=1))
+    ref = bem.spectrum(exc, enei, fields=True)
+    bem.set_lanes(3)
+    for rep in range(2):
+        r = bem.spectrum(exc, enei, fields=True)
+        errs = {"ext": rel(r["ext"], ref["ext"]), "sca": rel(r["sca"], ref["sca"]),
+                "sig2": rel(r["sig2"], ref["sig2"]), "h1": rel(r["h1"], ref["h1"])}
+        record("lanes3_vs_1_rep%d" % rep, **errs)
+        assert errs["ext"] < 1e-12 and errs["sca"] < 1e-12, errs
+        assert errs["sig2"] < 1e-10 and errs["h1"] < 1e-10, errs
+        assert np.all(np.abs(r["ir_iters"] - ref["ir_iters"]) <= 1)
