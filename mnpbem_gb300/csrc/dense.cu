@@ -8,6 +8,8 @@
 // reference's own native dense LU relies on (mex/hlib/lu.cpp:79-105 factorises
 // without pivoting).  Each block step costs one rank-nb update of the whole
 // matrix, so all O(n^3) work is a GEMM.  A pivot guard reports singular blocks.
+#include <cooperative_groups.h>
+
 #include "dense.cuh"
 #include "profile.cuh"
 
@@ -385,6 +387,151 @@ __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A
     }
 }
 
+// ------------------------------------- 256-wide pivot block on a CTA cluster
+// In-place Gauss-Jordan of one w x w complex64 block (w <= 256) by a cluster
+// of PB_CL CTAs.  CTA r keeps rows [r*PB_RPC, (r+1)*PB_RPC) in registers:
+// PB_TPR threads per row, thread (row l, phase ph) holding the columns
+// ph + PB_TPR * j.  The pivots are taken in panels of 16:
+//   1. the CTA owning the panel rows stages them in shared memory, inverts
+//      the 16 x 16 pivot block X (Gauss-Jordan, one entry per thread) and
+//      forms the new panel rows R = X * P (pivot columns replaced by X);
+//   2. it writes R into every CTA of the cluster (distributed shared memory),
+//      every CTA stages its own 16 panel-column entries C; cluster barrier;
+//   3. every row i outside the panel: a_ij <- [j not a pivot column] a_ij
+//      - sum_k C_ik R_kj; the panel rows take R.
+// One cluster barrier per panel (R is double-buffered), 16 panels for w = 256.
+// Rows and columns beyond w are identity and stay identity.
+constexpr int PB_W = 256, PB_CL = 8, PB_RPC = PB_W / PB_CL, PB_THREADS = 512;
+constexpr int PB_TPR = PB_THREADS / PB_RPC, PB_CPT = PB_W / PB_TPR, PB_PAN = 16;
+constexpr int PB_SMEM = (2 * PB_PAN * PB_W + 2 * PB_RPC * PB_PAN + PB_PAN * PB_PAN) * (int)sizeof(float2);
+static_assert(PB_PAN % PB_TPR == 0 || PB_TPR % PB_PAN == 0, "panel / thread layout");
+static_assert(PB_RPC % PB_PAN == 0, "a panel lies inside one CTA");
+
+__global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
+    k_block_inv_cluster(const float2* __restrict__ A, int64_t lda, int w, float2* __restrict__ X,
+                        int64_t ldx, int* status) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ float2 pb_smem[];
+  float2* Rb = pb_smem;                              // [2][PAN][W]  panel rows (broadcast)
+  float2* Cb = Rb + 2 * PB_PAN * PB_W;               // [2][RPC][PAN] own panel-column entries
+  float2* Xs = Cb + 2 * PB_RPC * PB_PAN;             // [PAN][PAN] pivot block (owner)
+  const int rank = (int)cluster.block_rank();
+  const int t = threadIdx.x, lr = t / PB_TPR, ph = t % PB_TPR;
+  const int grow = rank * PB_RPC + lr;
+  float2 a[PB_CPT];
+#pragma unroll
+  for (int j = 0; j < PB_CPT; ++j) {
+    const int c = ph + PB_TPR * j;
+    a[j] = (grow < w && c < w) ? A[(int64_t)grow * lda + c] : make_float2(grow == c ? 1.f : 0.f, 0.f);
+  }
+  const int npan = (w + PB_PAN - 1) / PB_PAN;
+  for (int pp = 0; pp < npan; ++pp) {
+    const int p0 = pp * PB_PAN, owner = p0 / PB_RPC, lp0 = p0 % PB_RPC, buf = pp & 1;
+    float2* R = Rb + buf * PB_PAN * PB_W;
+    float2* P = Rb + (buf ^ 1) * PB_PAN * PB_W;      // owner scratch: raw panel rows
+    float2* C = Cb + buf * PB_RPC * PB_PAN;
+    __syncthreads();                                  // the previous panel's reads of P / C are done
+    // own panel-column entries (every CTA)
+#pragma unroll
+    for (int j = 0; j < PB_CPT; ++j) {
+      const int c = ph + PB_TPR * j;
+      if (c >= p0 && c < p0 + PB_PAN) C[lr * PB_PAN + (c - p0)] = a[j];
+    }
+    if (rank == owner) {
+      if (lr >= lp0 && lr < lp0 + PB_PAN) {
+#pragma unroll
+        for (int j = 0; j < PB_CPT; ++j) P[(lr - lp0) * PB_W + ph + PB_TPR * j] = a[j];
+      }
+      __syncthreads();
+      // 16 x 16 Gauss-Jordan of the pivot block, one entry per thread
+      const int bi = t / PB_PAN, bj = t % PB_PAN;
+      const bool act = t < PB_PAN * PB_PAN;
+      if (act) Xs[bi * PB_PAN + bj] = P[bi * PB_W + p0 + bj];
+      __syncthreads();
+      for (int k = 0; k < PB_PAN; ++k) {
+        float2 v = make_float2(0.f, 0.f);
+        if (act) {
+          const float2 piv = Xs[k * PB_PAN + k];
+          const float n2 = piv.x * piv.x + piv.y * piv.y;
+          if (t == 0 && !(n2 > 1e-30f && n2 < 1e30f)) atomicOr(status, 1);
+          const float rn = 1.f / n2;
+          const float2 inv = make_float2(piv.x * rn, -piv.y * rn);
+          const float2 aik = Xs[bi * PB_PAN + k], akj = Xs[k * PB_PAN + bj], aij = Xs[bi * PB_PAN + bj];
+          if (bi == k && bj == k) v = inv;
+          else if (bi == k) v = cmul(akj, inv);
+          else if (bj == k) v = make_float2(-(aik.x * inv.x - aik.y * inv.y), -(aik.x * inv.y + aik.y * inv.x));
+          else v = csub(aij, cmul(aik, cmul(akj, inv)));
+        }
+        __syncthreads();
+        if (act) Xs[bi * PB_PAN + bj] = v;
+        __syncthreads();
+      }
+      // R = X * P with the pivot columns replaced by X, written to every CTA
+      for (int e = t; e < PB_PAN * PB_W; e += PB_THREADS) {
+        const int i = e / PB_W, c = e % PB_W;
+        float2 r;
+        if (c >= p0 && c < p0 + PB_PAN) {
+          r = Xs[i * PB_PAN + (c - p0)];
+        } else {
+          r = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int k = 0; k < PB_PAN; ++k) cfma(r, Xs[i * PB_PAN + k], P[k * PB_W + c]);
+        }
+#pragma unroll
+        for (int q = 0; q < PB_CL; ++q) cluster.map_shared_rank(R, q)[e] = r;
+      }
+    }
+    cluster.sync();
+    // update of this CTA's rows
+    const bool prow = (rank == owner) && lr >= lp0 && lr < lp0 + PB_PAN;
+    if (prow) {
+#pragma unroll
+      for (int j = 0; j < PB_CPT; ++j) a[j] = R[(lr - lp0) * PB_W + ph + PB_TPR * j];
+    } else {
+      float2 cr[PB_PAN];
+#pragma unroll
+      for (int k = 0; k < PB_PAN; ++k) cr[k] = C[lr * PB_PAN + k];
+#pragma unroll
+      for (int j = 0; j < PB_CPT; ++j) {
+        const int c = ph + PB_TPR * j;
+        float2 acc = (c >= p0 && c < p0 + PB_PAN) ? make_float2(0.f, 0.f) : a[j];
+#pragma unroll
+        for (int k = 0; k < PB_PAN; ++k) {
+          const float2 rv = R[k * PB_W + c];
+          acc.x = fmaf(-cr[k].x, rv.x, acc.x);
+          acc.x = fmaf(cr[k].y, rv.y, acc.x);
+          acc.y = fmaf(-cr[k].x, rv.y, acc.y);
+          acc.y = fmaf(-cr[k].y, rv.x, acc.y);
+        }
+        a[j] = acc;
+      }
+    }
+  }
+  // no CTA may exit while another can still write into its shared memory
+  cluster.sync();
+  if (grow < w) {
+#pragma unroll
+    for (int j = 0; j < PB_CPT; ++j) {
+      const int c = ph + PB_TPR * j;
+      if (c < w) X[(int64_t)grow * ldx + c] = a[j];
+    }
+  }
+}
+
+static mnpbem_status launch_block_inv_cluster(const float2* A, int64_t lda, int w, float2* X, int64_t ldx,
+                                              int* status, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    MNP_CUDA(cudaFuncSetAttribute(k_block_inv_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, PB_SMEM));
+    attr_set = true;
+  }
+  ProfScope ps(PH_BLOCKINV, st, 8.0 * w * w * w, 0.0);
+  k_block_inv_cluster<<<PB_CL, PB_THREADS, PB_SMEM, st>>>(A, lda, w, X, ldx, status);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 // --------------------------------------------------- blocked Gauss-Jordan
 template <typename R>
 mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st) {
@@ -409,7 +556,7 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
   MNP_TRY(w.xblk.ensure(cs * nb * nb));
   MNP_TRY(w.status.ensure(sizeof(int)));
   if (!w.nested) MNP_CUDA(cudaMemsetAsync(w.status.ptr, 0, sizeof(int), st));
-  if (!w.nested && nb > 64) {
+  if (!w.nested && nb > 64 && (sizeof(R) == 8 || nb > PB_W)) {
     // pivot blocks wider than 64 are inverted by an inner Gauss-Jordan whose
     // pivot status this (outer) level clears now and reads at the end
     if (!w.inner) w.inner.reset(new GJWork<R>());
@@ -433,6 +580,9 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
       ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
       k_block_inv<R><<<1, 256, 0, st>>>(Ccol + k0 * bw, bw, bw, X, bw, w.status.template as<int>());
       MNP_CHECK_LAUNCH();
+    } else if (sizeof(R) == 4 && bw <= PB_W) {
+      MNP_TRY(launch_block_inv_cluster(reinterpret_cast<const float2*>(Ccol + k0 * bw), bw, bw,
+                                       reinterpret_cast<float2*>(X), bw, w.status.template as<int>(), st));
     } else {
       MNP_CUDA(cudaMemcpyAsync(X, Ccol + k0 * bw, cs * bw * bw, cudaMemcpyDeviceToDevice, st));
       MNP_TRY(gj_invert<R>(X, bw, bw, *w.inner, big_gemm, ctx, st));

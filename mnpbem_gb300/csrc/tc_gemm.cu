@@ -12,9 +12,9 @@
 // so that C_r[i][2j] = sum_l (Re a Re b - Im a Im b) and
 // C_r[i][2j+1] = sum_l (Re a Im b + Im a Re b).  B' is rounded to TF32.
 //
-// Tile: 128 x 256 real outputs per CTA, K chunks of 32 floats (one 128-byte
-// swizzle row), 4 pipeline stages (48 KB each).  Warp 0 / lane 0 issues TMA,
-// warp 1 / lane 0 issues the MMAs, all four warps run the epilogue from TMEM.
+// Tile: 128 x 256 real outputs, K chunks of 32 floats (one 128-byte swizzle
+// row), 3 or 4 pipeline stages (48 KB each), two TMEM accumulators; the kernel is
+// persistent with warp-specialised producer / MMA / epilogue roles (below).
 // Every mbarrier wait is bounded by a wall-clock limit; on expiry the kernel
 // records an error code, waits (bounded) for its own copies in flight, frees
 // its tensor memory and returns.
@@ -24,13 +24,14 @@
 #include "profile.cuh"
 #include "tc_gemm.cuh"
 
+#include <algorithm>
+
 namespace mnpbem {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32, TC_STAGES = 4;
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 32;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;   // 16 KB
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024;
 constexpr uint32_t TC_TMEM_COLS = 256;
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
 
@@ -48,6 +49,11 @@ __device__ __forceinline__ unsigned long long gtimer() {
 }
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  uint64_t state;
+  asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(bar) : "memory");
+  (void)state;
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -118,31 +124,65 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 }
 
 // C_r[M][N2] = A_r[M][K2] * B'[N2][K2]^T + beta * C_r        (all row-major floats)
-__global__ void __launch_bounds__(128, 1)
+//
+// Persistent kernel, one CTA per SM, 192 threads in three roles:
+//   warp 0      TMA producer: takes tile indices from a global counter
+//               (dynamic schedule: CTAs that start late take fewer tiles) and
+//               streams the K chunks of A and B' through ST buffers (3 or 4:
+//               with 3 the kernel leaves ~50 KB of shared memory per SM to
+//               kernels of other streams),
+//               running ahead across tile boundaries;
+//   warp 1      MMA issuer: accumulates each tile into one of two TMEM
+//               accumulators (2 x 256 columns) so that the next tile's MMAs
+//               overlap the previous tile's epilogue;
+//   warps 2-5   epilogue: TMEM -> registers -> shared staging -> TMA bulk
+//               tensor store (beta = 0) or reduce-add (beta = 1) into C.
+// The tile indices pass from the producer to the other roles through a
+// four-slot ring in shared memory guarded by mbarriers.
+constexpr int TC_EPI_WARPS = 4;
+constexpr int TC_THREADS = 32 * (2 + TC_EPI_WARPS);
+constexpr int TC_STAGE_SMEM = TC_EPI_WARPS * 2 * 4096;   // two 32 x 32 float staging tiles per epilogue warp
+constexpr int tc_psmem(int stages) { return stages * TC_STAGE_BYTES + TC_STAGE_SMEM + 1024; }
+constexpr int TC_TQ = 4;                                  // tile-index ring slots
+
+template <int ST>
+__global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-              const __grid_constant__ CUtensorMap mapC, int M, int N2, int K2, int accumulate, int* err) {
+              const __grid_constant__ CUtensorMap mapC, int M, int N2, int K2, int accumulate,
+              int* tile_ctr, int* err) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[2 * TC_STAGES + 1];
+  __shared__ __align__(8) unsigned long long bars[2 * ST + 4 + 2 * TC_TQ];
+  __shared__ int tq[TC_TQ];
   __shared__ uint32_t tmem_slot;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
   const int KT = (K2 + TC_BK - 1) / TC_BK;
-  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[TC_STAGES]),
-                 done = smem_u32(&bars[2 * TC_STAGES]);
+  const int MT = (M + TC_BM - 1) / TC_BM, NT = (N2 + TC_BN - 1) / TC_BN;
+  const int ntiles = MT * NT;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[ST]);
+  const uint32_t accf0 = smem_u32(&bars[2 * ST]), acce0 = smem_u32(&bars[2 * ST + 2]);
+  const uint32_t tqf0 = smem_u32(&bars[2 * ST + 4]), tqe0 = smem_u32(&bars[2 * ST + 4 + TC_TQ]);
+  const uint32_t stage_base = base + ST * TC_STAGE_BYTES;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
+    for (int s = 0; s < ST; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, TC_EPI_WARPS);
+    }
+    for (int q = 0; q < TC_TQ; ++q) {
+      mbar_init(tqf0 + 8 * q, 1);
+      mbar_init(tqe0 + 8 * q, 1 + TC_EPI_WARPS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncwarp();
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(TC_TMEM_COLS)
+                 "r"(2 * TC_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -151,96 +191,146 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  int issued = 0;
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    for (int kt = 0; kt < KT; ++kt) {
-      const int s = kt % TC_STAGES;
-      if (kt >= TC_STAGES && !mbar_wait(empty0 + 8 * s, ((kt / TC_STAGES) - 1) & 1, err, 1)) break;
-      if (*(volatile int*)err) break;
-      const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
-      mbar_expect_tx(full0 + 8 * s, TC_STAGE_BYTES);
-      tma_load_2d(sa, &mapA, full0 + 8 * s, kt * TC_BK, m0);
-      tma_load_2d(sb, &mapB, full0 + 8 * s, kt * TC_BK, n0);
-      ++issued;
+  int issued = 0;   // producer: K chunks issued (for the drain after an error)
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- tile scheduler + TMA producer
+      int it = 0;
+      for (int j = 0;; ++j) {
+        const int q = j % TC_TQ;
+        if (j >= TC_TQ && !mbar_wait(tqe0 + 8 * q, ((j / TC_TQ) - 1) & 1, err, 16)) break;
+        int t = *(volatile int*)err ? -1 : atomicAdd(tile_ctr, 1);
+        if (t >= ntiles) t = -1;
+        tq[q] = t;
+        mbar_arrive(tqf0 + 8 * q);
+        if (t < 0) break;
+        const int m0 = (t % MT) * TC_BM, n0 = (t / MT) * TC_BN;
+        bool ok = true;
+        for (int kt = 0; kt < KT; ++kt, ++it) {
+          const int s = it % ST;
+          if (it >= ST && !mbar_wait(empty0 + 8 * s, ((it / ST) - 1) & 1, err, 1)) { ok = false; break; }
+          const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
+          mbar_expect_tx(full0 + 8 * s, TC_STAGE_BYTES);
+          tma_load_2d(sa, &mapA, full0 + 8 * s, kt * TC_BK, m0);
+          tma_load_2d(sb, &mapB, full0 + 8 * s, kt * TC_BK, n0);
+          issued = it + 1;
+        }
+        if (!ok) {
+          // hand out an end marker in the next slot so that the other roles stop
+          const int q2 = (j + 1) % TC_TQ;
+          if (j + 1 < TC_TQ || mbar_wait(tqe0 + 8 * q2, (((j + 1) / TC_TQ) - 1) & 1, err, 16)) {
+            tq[q2] = -1;
+            mbar_arrive(tqf0 + 8 * q2);
+          }
+          break;
+        }
+      }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
-    bool ok = true;
-    for (int kt = 0; kt < KT && ok; ++kt) {
-      const int s = kt % TC_STAGES;
-      ok = mbar_wait(full0 + 8 * s, (kt / TC_STAGES) & 1, err, 2);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      int it = 0;
+      for (int j = 0;; ++j) {
+        const int q = j % TC_TQ;
+        if (!mbar_wait(tqf0 + 8 * q, (j / TC_TQ) & 1, err, 32)) break;
+        const int t = *(volatile int*)&tq[q];
+        mbar_arrive(tqe0 + 8 * q);
+        if (t < 0) break;
+        const int b = j & 1;
+        if (j >= 2 && !mbar_wait(acce0 + 8 * b, ((j >> 1) - 1) & 1, err, 64)) break;
+        tc_fence_after();
+        const uint32_t dt = tmem + (uint32_t)(b * TC_TMEM_COLS);
+        bool ok = true;
+        for (int kt = 0; kt < KT; ++kt, ++it) {
+          const int s = it % ST;
+          if (!mbar_wait(full0 + 8 * s, (it / ST) & 1, err, 2)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
+          const uint64_t da = desc_sw128(sa), db = desc_sw128(sb);
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 8; ++kk) {
+            // advance 8 tf32 = 32 bytes along K inside the swizzle row
+            mma_tf32(dt, da + 2 * kk, db + 2 * kk, TC_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
+          }
+          mma_commit(empty0 + 8 * s);
+        }
+        if (!ok) break;
+        mma_commit(accf0 + 8 * b);
+      }
+    }
+  } else {
+    // ---------------- epilogue warps: TMEM lane quarter (warp % 4) = 32 rows of the tile
+    const int ew = warp - 2;                 // staging slot
+    const int quarter = warp & 3;
+    const uint32_t stage0 = stage_base + (uint32_t)ew * 2u * 4096u;
+    float* stage_gen = reinterpret_cast<float*>(smem_raw + (stage_base - smem_u32(smem_raw))) + ew * 2 * 1024;
+    int nstores = 0;
+    for (int j = 0;; ++j) {
+      const int q = j % TC_TQ;
+      int t = -1;
+      const bool okq = __all_sync(0xffffffffu, mbar_wait(tqf0 + 8 * q, (j / TC_TQ) & 1, err, 128) ? 1 : 0) != 0;
+      if (okq) t = *(volatile int*)&tq[q];
+      __syncwarp();
+      if (lane == 0 && okq) mbar_arrive(tqe0 + 8 * q);
+      if (!okq || t < 0) break;
+      const int b = j & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (j >> 1) & 1, err, 4) ? 1 : 0) != 0;
       if (!ok) break;
       tc_fence_after();
-      const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
-      const uint64_t da = desc_sw128(sa), db = desc_sw128(sb);
+      const int m0 = (t % MT) * TC_BM, n0 = (t / MT) * TC_BN;
+      const int row0 = m0 + quarter * 32;
+      for (int c = 0; c < TC_BN / 32; ++c) {
+        const int col0 = n0 + c * 32;
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * TC_TMEM_COLS + c * 32), r);
+        if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
+        const int buf = nstores & 1;
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        __syncwarp();
+        // row = lane of a 32 x 32 tile in the 128-byte swizzled layout of the
+        // C tensor map: 16-byte chunk c of row l sits at chunk c ^ (l & 7)
+        float4* st = reinterpret_cast<float4*>(stage_gen + buf * 1024) + lane * 8;
 #pragma unroll
-      for (int kk = 0; kk < TC_BK / 8; ++kk) {
-        // advance 8 tf32 = 32 bytes along K inside the swizzle row
-        mma_tf32(tmem, da + 2 * kk, db + 2 * kk, TC_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
+        for (int c4 = 0; c4 < 8; ++c4)
+          st[c4 ^ (lane & 7)] = make_float4(__uint_as_float(r[4 * c4]), __uint_as_float(r[4 * c4 + 1]),
+                                            __uint_as_float(r[4 * c4 + 2]), __uint_as_float(r[4 * c4 + 3]));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          const uint32_t src = stage0 + (uint32_t)buf * 4096u;
+          if (accumulate)
+            asm volatile(
+                "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%1, %2}], [%3];"
+                ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+                : "memory");
+          else
+            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                         ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+                         : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
+        ++nstores;
       }
-      mma_commit(empty0 + 8 * s);
-    }
-    if (ok) mma_commit(done);
-  }
-  __syncwarp();
-  // ---------------- epilogue: TMEM -> registers -> C
-  // (tcgen05.ld is warp-collective: keep the decision warp-uniform)
-  const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, err, 4) ? 1 : 0) != 0;
-  __syncwarp();
-  tc_fence_after();
-  if (ok) {
-    // Each warp owns 32 accumulator rows (TMEM lanes 32w..32w+31).  A 32 x 32
-    // chunk goes TMEM -> registers -> a staging tile in the (now idle)
-    // pipeline shared memory, and one lane hands it to TMA: a bulk tensor
-    // store when C is overwritten, a bulk tensor reduce-add when C
-    // accumulates (the read-modify-write of C happens in L2, the SMs never
-    // read C).  Two staging tiles per warp let the next chunk overlap the
-    // previous copy.  TMA clips rows / columns outside C.
-    const uint32_t stage0 = base + (uint32_t)warp * 2u * 4096u;
-    float* stage_gen = reinterpret_cast<float*>(smem_raw + (base - smem_u32(smem_raw))) + warp * 2 * 1024;
-    for (int c = 0; c < TC_BN / 32; ++c) {
-      const int col0 = n0 + c * 32, row0 = m0 + warp * 32;
-      uint32_t r[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
-      if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
-      const int buf = c & 1;
-      if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      // this accumulator has been read: the MMA warp may overwrite it
+      tc_fence_before();
       __syncwarp();
-      float* st = stage_gen + buf * 1024;
-#pragma unroll
-      for (int j = 0; j < 32; ++j) st[lane * 32 + ((j + lane) & 31)] = __uint_as_float(r[(j + lane) & 31]);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) {
-        const uint32_t src = stage0 + (uint32_t)buf * 4096u;
-        if (accumulate)
-          asm volatile(
-              "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%1, %2}], [%3];"
-              ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
-              : "memory");
-        else
-          asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
-                       ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
-                       : "memory");
-        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-      }
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
     }
     if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     __syncwarp();
   }
-  // ---------------- drain copies still in flight after an error, free TMEM
+  // ---------------- drain loads still in flight after an error, free TMEM
   if (warp == 0 && lane == 0 && *(volatile int*)err) {
-    for (int kt = 0; kt < issued; ++kt) {
-      const int s = kt % TC_STAGES;
-      mbar_wait(full0 + 8 * s, (kt / TC_STAGES) & 1, err, 8);
+    for (int i = issued - ST > 0 ? issued - ST : 0; i < issued; ++i) {
+      const int s = i % ST;
+      mbar_wait(full0 + 8 * s, (i / ST) & 1, err, 8);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_TMEM_COLS) : "memory");
   }
 }
 
@@ -322,8 +412,12 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     c.usable = (major == 10 && minor == 3) && get_encode(c) != nullptr &&
-               cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) == cudaSuccess;
+               cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess;
     if (!c.usable) cudaGetLastError();
+    const char* env = getenv("MNPBEM_TC_STAGES");
+    if (env && (env[0] == '3' || env[0] == '4')) c.stages = env[0] - '0';
   }
   if (!c.usable || !c.enabled) return false;
   if ((lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||
@@ -355,7 +449,7 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
   CUtensorMap ma, mb, mc;
   if (!make_map(enc, &ma, A, (uint64_t)K2, (uint64_t)M, (uint64_t)lda * 8, TC_BM) ||
       !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, TC_BN) ||
-      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, false)) {
+      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, true)) {
     set_error("cuTensorMapEncodeTiled failed");
     return MNPBEM_ERR_CUDA;
   }
@@ -363,13 +457,20 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     MNP_CUDA(cudaMemsetAsync(c.err.ptr, 0, sizeof(int), st));
     c.err_cleared = true;
   }
-  dim3 grid((unsigned)cdiv_up(N2, TC_BN), (unsigned)cdiv_up(M, TC_BM));
-  if (grid.y > 65535) { set_error("tc_gemm_c64: M too large"); return MNPBEM_ERR_INVALID_ARG; }
+  const int64_t MT = cdiv_up(M, TC_BM), NT = cdiv_up(N2, TC_BN);
+  if (MT * NT >= (1ll << 31)) { set_error("tc_gemm_c64: too many tiles"); return MNPBEM_ERR_INVALID_ARG; }
+  MNP_TRY(c.ctr.ensure(sizeof(int)));
+  MNP_CUDA(cudaMemsetAsync(c.ctr.ptr, 0, sizeof(int), st));
+  const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, c.num_sms > 0 ? c.num_sms : 148);
   {
     ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
-    k_tc_gemm<<<grid, 128, TC_SMEM, st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2, beta.x != 0.0f ? 1 : 0,
-                                         c.err.as<int>());
+    if (c.stages == 3)
+      k_tc_gemm<3><<<grid, TC_THREADS, tc_psmem(3), st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2,
+                                                          beta.x != 0.0f ? 1 : 0, c.ctr.as<int>(), c.err.as<int>());
+    else
+      k_tc_gemm<4><<<grid, TC_THREADS, tc_psmem(4), st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2,
+                                                          beta.x != 0.0f ? 1 : 0, c.ctr.as<int>(), c.err.as<int>());
     MNP_CHECK_LAUNCH();
   }
   return MNPBEM_OK;
@@ -392,6 +493,7 @@ mnpbem_status tc_check_error(TcGemmCtx& c, cudaStream_t st) {
 void tc_release(TcGemmCtx& c) {
   c.bexp.release();
   c.err.release();
+  c.ctr.release();
 }
 
 }  // namespace mnpbem

@@ -11,6 +11,9 @@ struct TcGemmCtx {
   bool err_cleared = false;
   DevBuf bexp;            // expanded B operand [2N][2K] (real, K-major, tf32)
   DevBuf err;             // device error word of the bounded waits
+  DevBuf ctr;             // tile counter of the persistent kernel (zeroed before each launch)
+  int num_sms = 0;
+  int stages = 4;         // pipeline depth of the persistent kernel (3 or 4)
   void* encode_fn = nullptr;
 };
 

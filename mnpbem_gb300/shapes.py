@@ -82,3 +82,148 @@ def sphere(n_faces, diameter=1.0, center=(0.0, 0.0, 0.0)):
         v, f = trisphere(npts, diameter)
         return v + np.asarray(center, dtype=np.float64)[None, :], f
     return fibsphere(n_faces, diameter, center)
+
+
+def _orient_outward(verts, faces, center):
+    """Flip faces whose normal (v1 - v2) x (v3 - v2) points towards ``center``."""
+    out = faces.copy()
+    for k, f in enumerate(out):
+        idx = f[f >= 0]
+        p = verts[idx]
+        nv = np.cross(p[0] - p[1], p[2] - p[1])
+        if np.dot(nv, p.mean(0) - center) < 0:
+            out[k, :idx.size] = idx[::-1]
+    return out
+
+
+def _merge(verts, faces, tol=1e-9):
+    """Merge coincident vertices; quads that collapse to three vertices become triangles."""
+    key = np.round(verts / tol).astype(np.int64)
+    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    inv = inv.reshape(-1)
+    order = np.argsort(first)                 # keep first-occurrence order
+    rank = np.empty_like(order)
+    rank[order] = np.arange(order.size)
+    new_verts = verts[first[order]]
+    out = []
+    for f in faces:
+        idx = [int(rank[inv[i]]) for i in f if i >= 0]
+        uniq = []
+        for i in idx:
+            if i not in uniq:
+                uniq.append(i)
+        if len(uniq) < 3:
+            continue
+        out.append(uniq + [-1] * (4 - len(uniq)))
+    return new_verts, np.asarray(out, dtype=np.int64)
+
+
+def trirod(diameter, height, n=(15, 20, 20), triangles=False):
+    """Rod with hemispherical caps along z (``Particles/particleshapes/trirod.m``).
+
+    ``n = (nphi, ntheta, nz)``: points around the axis (the first and last
+    coincide), polar points per cap (pole to equator) and points along the
+    cylinder.  The surface is a grid of quadrilaterals (triangles at the
+    poles); ``(nphi - 1) * (2 * (ntheta - 1) + nz - 1)`` faces.  With
+    ``triangles`` every quadrilateral is split in two.
+    """
+    nphi, nth, nz = n
+    r = 0.5 * diameter
+    half = 0.5 * (height - diameter)
+    phi = np.linspace(0.0, 2 * np.pi, nphi)[:-1]
+    theta = np.linspace(0.0, 0.5 * np.pi, nth)
+    z = half * np.linspace(-1.0, 1.0, nz)
+    m = phi.size
+    verts, faces = [], []
+
+    def ring(rho, zz):
+        base = len(verts)
+        for ph in phi:
+            verts.append((rho * np.cos(ph), rho * np.sin(ph), zz))
+        return base
+
+    def band(b0, b1):
+        for i in range(m):
+            j = (i + 1) % m
+            faces.append([b0 + i, b0 + j, b1 + j, b1 + i])
+
+    # upper cap: pole ring (theta[1]) down to the equator, lower cap mirrored
+    for sgn in (1.0, -1.0):
+        pole = len(verts)
+        verts.append((0.0, 0.0, sgn * (half + r)))
+        rings = [ring(r * np.sin(t), sgn * (half + r * np.cos(t))) for t in theta[1:]]
+        for i in range(m):
+            faces.append([pole, rings[0] + i, rings[0] + (i + 1) % m, -1])
+        for a, b in zip(rings[:-1], rings[1:]):
+            band(a, b)
+    cyl = [ring(r, zz) for zz in z]
+    for a, b in zip(cyl[:-1], cyl[1:]):
+        band(a, b)
+    verts = np.asarray(verts, dtype=np.float64)
+    faces = np.asarray(faces, dtype=np.int64)
+    verts, faces = _merge(verts, faces, tol=1e-9 * max(1.0, height))
+    if triangles:
+        faces = _split_quads(faces)
+    return verts, _orient_outward(verts, faces, np.zeros(3))
+
+
+def _split_quads(faces):
+    out = []
+    for f in faces:
+        if f[3] < 0:
+            out.append(list(f))
+        else:
+            out.append([f[0], f[1], f[2], -1])
+            out.append([f[2], f[3], f[0], -1])
+    return np.asarray(out, dtype=np.int64)
+
+
+def tricube(n, length=1.0, e=0.25, triangles=False):
+    """Cube with rounded edges (``Particles/particleshapes/tricube.m``).
+
+    Each side is an ``(n - 1) x (n - 1)`` grid whose coordinates
+    ``sign(u) |u|^(1/e)`` (u uniform in ``[-0.5^e, 0.5^e]``) cluster towards
+    the edges; the merged points are then moved onto the super-sphere
+    ``x = 0.5 c(theta)^e c(phi)^e, y = 0.5 c(theta)^e s(phi)^e,
+    z = 0.5 s(theta)^e`` (signed powers of sin / cos of the spherical angles),
+    which rounds the edges, and scaled by ``length``.  6 (n - 1)^2 faces.
+    """
+    u = np.linspace(-0.5 ** e, 0.5 ** e, n)
+    g = np.sign(u) * np.abs(u) ** (1.0 / e)
+    X, Y = np.meshgrid(g, g, indexing="xy")
+    x, y = X.ravel(), Y.ravel()
+    zz = 0.5 * np.ones_like(x)
+    quads = []
+    for i in range(n - 1):
+        for j in range(n - 1):
+            a = i * n + j
+            quads.append([a, a + 1, a + n + 1, a + n])
+    quads = np.asarray(quads, dtype=np.int64)
+    sides = [(x, y, zz), (y, x, -zz), (y, zz, x), (x, -zz, y), (zz, x, y), (-zz, y, x)]
+    verts, faces = [], []
+    for sx, sy, sz in sides:
+        off = sum(v.shape[0] for v in verts)
+        verts.append(np.stack([sx, sy, sz], 1))
+        faces.append(quads + off)
+    verts = np.vstack(verts)
+    faces = np.vstack(faces)
+    verts, faces = _merge(verts, faces, tol=1e-10)
+    ph = np.arctan2(verts[:, 1], verts[:, 0])
+    th = np.arctan2(verts[:, 2], np.hypot(verts[:, 0], verts[:, 1]))
+    isin = lambda a: np.sign(np.sin(a)) * np.abs(np.sin(a)) ** e
+    icos = lambda a: np.sign(np.cos(a)) * np.abs(np.cos(a)) ** e
+    verts = np.stack([0.5 * icos(th) * icos(ph), 0.5 * icos(th) * isin(ph), 0.5 * isin(th)], 1) * length
+    if triangles:
+        faces = _split_quads(faces)
+    return verts, _orient_outward(verts, faces, np.zeros(3))
+
+
+def rounding_to_e(length, radius):
+    """Super-sphere parameter ``e`` of ``tricube`` for an edge rounding ``radius``.
+
+    Chosen so that the rounded edge passes through the point that a circular
+    rounding of that radius gives on the diagonal of the cross section:
+    ``h 2^(-e/2) = h - radius (1 - 1/sqrt(2))`` with ``h = length / 2``.
+    """
+    h = 0.5 * length
+    return -2.0 * np.log2(1.0 - radius * (1.0 - 1.0 / np.sqrt(2.0)) / h)

@@ -3,7 +3,9 @@
 The tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation) and the
 CUDA-core kernel are compared with a complex128 NumPy product on seeded
 random matrices, including ragged shapes (M, N, K not multiples of the
-tile), alpha = -1 / complex alpha, and beta = 1 accumulation.
+tile, and more output tiles than SMs so that the persistent tensor-core kernel
+runs several tiles per CTA), alpha = -1 / complex alpha, and beta = 1
+accumulation.
 Tolerances (max |diff| / max |ref|): CUDA core 1e-5, tensor core 5e-3.
 """
 import ctypes
@@ -14,7 +16,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(256, 128, 64), (300, 200, 70), (1000, 64, 1000), (129, 258, 34), (640, 640, 512),
-          (4000, 4, 4000), (700, 16, 900)]
+          (4000, 4, 4000), (700, 16, 900),
+          # more tiles than SMs: each persistent CTA runs several tiles
+          (3000, 2000, 256), (1100, 1300, 514)]
 
 
 def run(lib, path, M, N, K, alpha, beta, seed):

@@ -228,3 +228,28 @@ def test_concurrent_lanes_match_serial(gpu_lib):
         assert errs["ext"] < 1e-12 and errs["sca"] < 1e-12, errs
         assert errs["sig2"] < 1e-10 and errs["h1"] < 1e-10, errs
         assert np.all(np.abs(r["ir_iters"] - ref["ir_iters"]) <= 1)
+
+
+def test_tensor_core_inversions_at_1200_faces(gpu_lib):
+    """n >= 1024: 256-wide Gauss-Jordan steps whose pivot blocks are inverted
+    on a CTA cluster and whose updates run on the tensor cores (TF32).  The
+    complex64 bemret matrices agree with the FP64 ones to TF32 accuracy, and
+    the refined cross sections with the FP64 path to 1e-8."""
+    v, f = shapes.fibsphere(1200, 30.0)
+    cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
+    b64 = m.bemsolver(cp, m.bemoptions(precision="fp64"))
+    bmx = m.bemsolver(cp, m.bemoptions(precision="mixed"))
+    M64 = b64.bem_matrices(560.0)
+    Mmx = bmx.bem_matrices(560.0)
+    errs = {k: rel(Mmx[k], M64[k]) for k in M64}
+    record("bem_matrices_mixed_vs_fp64_1200", **errs)
+    for k, e in errs.items():
+        assert e < 2e-2, (k, errs)
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    enei = [480.0, 560.0, 640.0]
+    r64 = b64.spectrum(exc, enei)
+    rmx = bmx.spectrum(exc, enei)
+    e = {"ext": rel(rmx["ext"], r64["ext"]), "sca": rel(rmx["sca"], r64["sca"]),
+         "iters": rmx["ir_iters"].tolist()}
+    record("solve_mixed_vs_fp64_1200", **e)
+    assert e["ext"] < 1e-8 and e["sca"] < 1e-8, e
