@@ -152,6 +152,26 @@ MNPBEM_API mnpbem_status mnpbem_solve(mnpbem_geom* g, const mnpbem_planewave* ex
                            int32_t precision, const mnpbem_refine* refine,
                            mnpbem_solution* out);
 
+/* One particle's sweep inside mnpbem_solve_batch (fields as in mnpbem_solve). */
+typedef struct mnpbem_job {
+  mnpbem_geom* g;
+  const mnpbem_planewave* exc;
+  int32_t nenei;
+  const double* enei;       /* [nenei] nm */
+  const double* eps_media;  /* [nenei][nmed] complex */
+  int32_t nmed;
+  mnpbem_solution* out;
+} mnpbem_job;
+
+/* Several independent sweeps (e.g. particles of uneven size, each its own
+ * handle) solved together: every handle's lanes are fed by one scheduler, so
+ * the small particles' wavelengths fill the GPU while the large ones run.
+ * Same results as one mnpbem_solve per job.  The handles must be distinct and
+ * on one device.  The reference has no batch call: its user code loops over
+ * particles and wavelengths (Demo/planewave/ret/demospecret*.m).             */
+MNPBEM_API mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs, int32_t njobs, int32_t precision,
+                                            const mnpbem_refine* refine);
+
 /* The matrices bemret stores per wavelength (initmat.m:27-72), copied to host
  * as complex128 [n][n] (NULL to skip): G1i, G2i, Sigma1, Deltai, Sigmai.       */
 MNPBEM_API mnpbem_status mnpbem_bem_matrices(mnpbem_geom* g, double enei, const double* eps_media,

@@ -55,6 +55,12 @@ class Refine(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int32), ("tol", ctypes.c_double)]
 
 
+class Job(ctypes.Structure):
+    _fields_ = [("g", ctypes.c_void_p), ("exc", ctypes.POINTER(PlaneWave)), ("nenei", ctypes.c_int32),
+                ("enei", c_double_p), ("eps_media", c_double_p), ("nmed", ctypes.c_int32),
+                ("out", ctypes.POINTER(Solution))]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "mnpbem_geom_create": (ctypes.c_int, [c_double_p, ctypes.c_int64, c_int64_p, ctypes.c_int64,
@@ -70,6 +76,8 @@ SIGNATURES = {
     "mnpbem_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlaneWave), ctypes.c_int32,
                                     c_double_p, c_double_p, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.POINTER(Refine), ctypes.POINTER(Solution)]),
+    "mnpbem_solve_batch": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.POINTER(Refine)]),
     "mnpbem_bem_matrices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p,
                                            ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 5),
     "mnpbem_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

@@ -226,12 +226,8 @@ class bemret:
         return dict(zip(("G1i", "G2i", "Sigma1", "Deltai", "Sigmai"), mats))
 
     # ------------------------------------------------------------- solves
-    def spectrum(self, exc, enei, fields=False, out=None):
-        """Wavelength sweep: returns dict with ext, sca [nenei, npol] (+ fields).
-
-        ``out`` may supply preallocated (e.g. pinned) C-contiguous host arrays
-        for any of ext, sca, sig1, sig2, h1, h2 with the shapes below.
-        """
+    def _sweep_args(self, exc, enei, fields, out):
+        """Arrays and C structures of one sweep (kept alive by the caller)."""
         enei = np.ascontiguousarray(np.atleast_1d(np.asarray(enei, dtype=np.float64)))
         nw, P, n = enei.size, exc.npol, self.p.n
         em = np.ascontiguousarray(self._eps(enei))
@@ -240,7 +236,7 @@ class bemret:
                    "sig1": ((nw, n, P), np.complex128), "sig2": ((nw, n, P), np.complex128),
                    "h1": ((nw, n, 3, P), np.complex128), "h2": ((nw, n, 3, P), np.complex128)}
         given = out or {}
-        out = {"ir_iters": np.zeros(nw, dtype=np.int32), "ir_resid": np.zeros(nw)}
+        res = {"ir_iters": np.zeros(nw, dtype=np.int32), "ir_resid": np.zeros(nw)}
         for key, (shp, dt) in shapes_.items():
             if key in ("sig1", "sig2", "h1", "h2") and not fields:
                 continue
@@ -248,20 +244,29 @@ class bemret:
                 arr = given[key]
                 if arr.shape != shp or arr.dtype != dt or not arr.flags["C_CONTIGUOUS"]:
                     raise ValueError("out[%r] must be a C-contiguous %s array of shape %s" % (key, dt, shp))
-                out[key] = arr
+                res[key] = arr
             else:
-                out[key] = np.zeros(shp, dtype=dt)
+                res[key] = np.zeros(shp, dtype=dt)
         sol = _lib.Solution()
         for key in ("ext", "sca", "sig1", "sig2", "h1", "h2", "ir_iters", "ir_resid"):
-            if key in out:
-                setattr(sol, key, out[key].ctypes.data)
+            if key in res:
+                setattr(sol, key, res[key].ctypes.data)
         sol.outputs_on_device = 0
+        return {"enei": enei, "em": em, "pw": pw, "sol": sol, "exc": exc, "res": res}
+
+    def spectrum(self, exc, enei, fields=False, out=None):
+        """Wavelength sweep: returns dict with ext, sca [nenei, npol] (+ fields).
+
+        ``out`` may supply preallocated (e.g. pinned) C-contiguous host arrays
+        for any of ext, sca, sig1, sig2, h1, h2 with the shapes below.
+        """
+        a = self._sweep_args(exc, enei, fields, out)
         ref = _lib.Refine(self.refine_iters, self.refine_tol)
-        _lib.check(self._lib.mnpbem_solve(self._h, ctypes.byref(pw), nw, _lib.dptr(enei),
-                                          em.view(np.float64).ctypes.data_as(_lib.c_double_p),
-                                          em.shape[1], self.precision, ctypes.byref(ref),
-                                          ctypes.byref(sol)))
-        return out
+        _lib.check(self._lib.mnpbem_solve(self._h, ctypes.byref(a["pw"]), a["enei"].size, _lib.dptr(a["enei"]),
+                                          a["em"].view(np.float64).ctypes.data_as(_lib.c_double_p),
+                                          a["em"].shape[1], self.precision, ctypes.byref(ref),
+                                          ctypes.byref(a["sol"])))
+        return a["res"]
 
     def mldivide(self, exc):
         """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m)."""
@@ -272,6 +277,36 @@ class bemret:
                           ir_iters=int(r["ir_iters"][0]), ir_resid=float(r["ir_resid"][0]))
 
     solve = mldivide
+
+
+def spectrum_batch(items, fields=False):
+    """Sweeps of several particles in one library call (``mnpbem_solve_batch``).
+
+    ``items``: sequence of ``(bem, exc, enei)`` with distinct solvers of one
+    precision; returns one result dict per item, as ``bemret.spectrum``.  The
+    reference loops over particles in user code; here the wavelengths of all
+    particles share the GPU at once.
+    """
+    items = list(items)
+    if not items:
+        return []
+    prec = {b.precision for b, _, _ in items}
+    if len(prec) != 1:
+        raise ValueError("spectrum_batch: all solvers must use one precision")
+    args = [b._sweep_args(e, w, fields, None) for b, e, w in items]
+    jobs = (_lib.Job * len(items))()
+    for k, ((b, _, _), a) in enumerate(zip(items, args)):
+        jobs[k].g = b.handle.value
+        jobs[k].exc = ctypes.pointer(a["pw"])
+        jobs[k].nenei = a["enei"].size
+        jobs[k].enei = _lib.dptr(a["enei"])
+        jobs[k].eps_media = a["em"].view(np.float64).ctypes.data_as(_lib.c_double_p)
+        jobs[k].nmed = a["em"].shape[1]
+        jobs[k].out = ctypes.pointer(a["sol"])
+    b0 = items[0][0]
+    ref = _lib.Refine(b0.refine_iters, b0.refine_tol)
+    _lib.check(b0._lib.mnpbem_solve_batch(jobs, len(items), b0.precision, ctypes.byref(ref)))
+    return [a["res"] for a in args]
 
 
 def bemsolver(p, op=None, **kw):

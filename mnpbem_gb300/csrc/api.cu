@@ -86,6 +86,8 @@ using namespace mnpbem;
 // sweep run concurrently: the latency-bound steps of one wavelength (pivot
 // blocks, panel products, refinement vectors) overlap the tensor-core
 // updates of the others.  Lane 0 runs on the handle's stream.
+constexpr int NSTAGES = 6;   // assemble, initmat, first solve, refine (DS), spectra, refine (FP32)
+
 struct Lane {
   cudaStream_t st = nullptr;
   bool own_stream = false;
@@ -103,13 +105,14 @@ struct Lane {
     int precision = -1, P = 0, ninf = 0;
     bool prof = false;
     uint64_t sig = 0;             // addresses of every buffer the graphs captured
-    cudaGraphExec_t exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    Profiler::GraphRec rec[5];
+    cudaGraphExec_t exec[NSTAGES] = {};
+    Profiler::GraphRec rec[NSTAGES];
   } graphs;
   // scheduler state
   enum { IDLE = 0, ITER, DONE } state = IDLE;
   int w = -1, iters = 0;
   double res = -1.0;
+  bool last_ds = false;      // the last refinement step used the double-single residual
 };
 
 struct mnpbem_geom {
@@ -147,7 +150,7 @@ mnpbem_status check_geom(const mnpbem_geom* g) {
 void lane_release(Lane& L) {
   if (L.st) cudaStreamSynchronize(L.st);
   tc_release(L.tc);
-  for (int q = 0; q < 5; ++q) {
+  for (int q = 0; q < NSTAGES; ++q) {
     if (L.graphs.exec[q]) cudaGraphExecDestroy(L.graphs.exec[q]);
     L.graphs.exec[q] = nullptr;
     Profiler::release(L.graphs.rec[q]);
@@ -792,9 +795,12 @@ mnpbem_status stage_first(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   return MNPBEM_OK;
 }
 
-// ---------------------------------------------------------------- S3
+// ---------------------------------------------------------------- S3 / S5
 // norms[0..1] = ||r||^2, ||b||^2 ; norms[2..3] = ||dx||^2, ||x||^2
-mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
+// ds: residual products in double-single arithmetic from the hi / lo planes
+// (S3); otherwise FP32 products of the hi planes (S5), enough while the
+// residual is still large compared with their rounding error.
+mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c, bool ds) {
   const int64_t n = G->g.n;
   const int P = c.P;
   cudaStream_t st = L.st;
@@ -803,12 +809,13 @@ mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const float2* hl[4];
   for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
   double* norms = L.norms.as<double>();
-  // G1 x1, G2 x2, H1 x1, H2 x2 in double-single arithmetic from the hi / lo planes
+  // G1 x1, H1 x1, G2 x2, H2 x2
   float2* bs = L.bsplit.as<float2>();
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], hl[0] + n * ld, ld, v.x1, 4 * P, v.Y1, 4 * P, bs, st));
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], hl[1] + n * ld, ld, v.x1, 4 * P, v.Z1, 4 * P, bs, st));
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], hl[2] + n * ld, ld, v.x2, 4 * P, v.Y2, 4 * P, bs, st));
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], hl[3] + n * ld, ld, v.x2, 4 * P, v.Z2, 4 * P, bs, st));
+  auto lo = [&](int q) -> const float2* { return ds ? hl[q] + n * ld : nullptr; };
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], lo(0), ld, v.x1, 4 * P, v.Y1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], lo(1), ld, v.x1, 4 * P, v.Z1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], lo(2), ld, v.x2, 4 * P, v.Y2, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], lo(3), ld, v.x2, 4 * P, v.Z2, 4 * P, bs, st));
   MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
   launch_residual(face_data(G, L), P, L.lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.phi, v.a, v.alpha,
                   v.De, v.rphi, v.ra, v.ral, v.rDe, norms, st);
@@ -844,7 +851,8 @@ mnpbem_status run_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage, b
     case 0: return stage_assemble(G, L, c.precision);
     case 1: return c.precision == MNPBEM_FP64 ? stage_initmat<double>(G, L, direct) : stage_initmat<float>(G, L, direct);
     case 2: return stage_first(G, L, c);
-    case 3: return stage_iter(G, L, c);
+    case 3: return stage_iter(G, L, c, true);
+    case 5: return stage_iter(G, L, c, false);
     default: return stage_spectra(G, L, c);
   }
 }
@@ -887,7 +895,7 @@ void drop_graphs(mnpbem_geom* G, Lane& L) {
   auto& gr = L.graphs;
   cudaStreamSynchronize(L.st);
   G->prof.flush();          // replayed records must be read before their events go
-  for (int q = 0; q < 5; ++q) {
+  for (int q = 0; q < NSTAGES; ++q) {
     if (gr.exec[q]) cudaGraphExecDestroy(gr.exec[q]);
     gr.exec[q] = nullptr;
     Profiler::release(gr.rec[q]);
@@ -927,6 +935,14 @@ struct Refine {
   double tol;
 };
 
+// residual precision of the next refinement step: FP32 while the last
+// relative residual is above 1e-3 (the FP32 rounding of the products,
+// ~1e-6 of |A| |x|, is then far below what the step resolves), double-single
+// afterwards.  The first step always starts in FP32.
+constexpr double DS_SWITCH = 1e-3;
+bool next_ds(const Lane& L) { return L.iters > 0 && L.res <= DS_SWITCH; }
+int iter_stage(bool ds) { return ds ? 3 : 5; }
+
 // one wavelength through all stages, synchronously (graphs == true replays
 // captured stages; false runs the stages directly and sizes the buffers)
 mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine& ref, bool graphs,
@@ -939,16 +955,21 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
   double final_res = -1.0;
   if (c.precision == MNPBEM_MIXED) {
     double* hn = L.norms_host;
+    L.iters = 0;
+    L.res = -1.0;
     for (int it = 0; it < ref.maxit; ++it) {
-      MNP_TRY(launch_stage(G, L, c, 3, graphs));
+      const bool ds = next_ds(L);
+      MNP_TRY(launch_stage(G, L, c, iter_stage(ds), graphs));
       MNP_CUDA(cudaMemcpyAsync(hn, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       MNP_CUDA(cudaStreamSynchronize(st));
       G->prof.flush();
       MNP_TRY(check_pivots(L));
       used = it + 1;
+      L.iters = used;
       final_res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
+      L.res = final_res;
       if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-      if (sqrt(hn[2]) <= ref.tol * sqrt(hn[3])) break;
+      if (ds && sqrt(hn[2]) <= ref.tol * sqrt(hn[3])) break;
     }
   }
   MNP_TRY(launch_stage(G, L, c, 4, graphs));
@@ -1031,7 +1052,8 @@ mnpbem_status write_outputs(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sw
 }
 
 mnpbem_status queue_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
-  MNP_TRY(launch_stage(G, L, c, 3, true));
+  L.last_ds = next_ds(L);
+  MNP_TRY(launch_stage(G, L, c, iter_stage(L.last_ds), true));
   MNP_CUDA(cudaMemcpyAsync(L.norms_host, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
   MNP_CUDA(cudaEventRecord(L.ev, L.st));
   L.state = Lane::ITER;
@@ -1066,7 +1088,8 @@ mnpbem_status lane_advance(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Swe
     ++L.iters;
     L.res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
     if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-    if (sqrt(hn[2]) <= s.ref.tol * sqrt(hn[3]) || L.iters >= s.ref.maxit) return queue_finish(G, L, c);
+    if ((L.last_ds && sqrt(hn[2]) <= s.ref.tol * sqrt(hn[3])) || L.iters >= s.ref.maxit)
+      return queue_finish(G, L, c);
     return queue_iter(G, L, c);
   }
   // DONE: results of L.w are in the lane; the stream is idle, so host-side
@@ -1106,103 +1129,21 @@ int choose_lanes(mnpbem_geom* G, int precision, int P, int ninf, int nenei) {
   return nl;
 }
 
-// phases of one call: lanes without graphs for this configuration run one
-// wavelength directly and capture their stages; the remaining wavelengths go
-// to the lanes as they free up
-mnpbem_status run_sweep(mnpbem_geom* G, const SolveCtx& c, const Sweep& s, int nl) {
-  const int nenei = s.nenei, precision = c.precision, P = c.P;
-  const mnpbem_planewave* exc = c.exc;
-  int next = 0;
-  // 1. lanes without graphs for this configuration: run one wavelength
-  //    directly (sizing every buffer), then capture the stages
-  std::vector<int> fresh;
-  for (int l = 0; l < nl && next < nenei; ++l) {
-    Lane& L = *G->lanes[l];
-    if (graphs_match(G, L, c)) continue;
-    if (L.graphs.valid) drop_graphs(G, L);
-    const int w = next++;
-    MNP_TRY(upload_lp(G, L, s, w));
-    L.w = w;
-    MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
-    MNP_TRY(write_outputs(G, L, c, s, w));
-    MNP_CUDA(cudaStreamSynchronize(L.st));
-    if (G->use_graphs) fresh.push_back(l);
-    if (!G->use_graphs) break;
-  }
-  for (int l : fresh) {
-    Lane& L = *G->lanes[l];
-    bool ok = true;
-    for (int stage = 0; stage < 5 && ok; ++stage) {
-      if (stage == 3 && precision != MNPBEM_MIXED) continue;
-      ok = capture_stage(G, L, c, stage) == MNPBEM_OK;
-    }
-    if (ok) {
-      auto& gr = L.graphs;
-      gr.valid = true;
-      gr.precision = precision;
-      gr.P = P;
-      gr.ninf = exc->ninf;
-      gr.prof = G->prof.enabled;
-      gr.sig = lane_sig(G, L);
-    } else {
-      drop_graphs(G, L);
-      G->use_graphs = false;   // run directly from now on
-    }
-  }
-  if (!G->use_graphs) {
-    // 2a. no graphs: every remaining wavelength directly on lane 0
-    Lane& L = *G->lanes[0];
-    for (; next < nenei; ++next) {
-      MNP_TRY(upload_lp(G, L, s, next));
-      L.w = next;
-      MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
-      MNP_TRY(write_outputs(G, L, c, s, next));
-    }
-  } else {
-    // 2b. the remaining wavelengths go to the lanes as they free up; the host
-    //     polls each lane's completion event and queues its next step
-    std::vector<Lane*> run;
-    for (int l = 0; l < nl; ++l)
-      if (graphs_match(G, *G->lanes[l], c)) run.push_back(G->lanes[l].get());
-    cudaEvent_t start;
-    MNP_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-    struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } eg{start};
-    MNP_CUDA(cudaEventRecord(start, G->st));
-    int active = 0;
-    for (Lane* L : run) {
-      MNP_CUDA(cudaStreamWaitEvent(L->st, start, 0));
-      if (next < nenei) {
-        MNP_TRY(lane_start(G, *L, c, s, next++));
-        ++active;
-      }
-    }
-    while (active > 0) {
-      bool progressed = false;
-      for (Lane* L : run) {
-        if (L->state == Lane::IDLE) continue;
-        const cudaError_t q = cudaEventQuery(L->ev);
-        if (q == cudaErrorNotReady) continue;
-        MNP_CUDA(q);
-        progressed = true;
-        MNP_TRY(lane_advance(G, *L, c, s));
-        if (L->state == Lane::IDLE) {
-          if (next < nenei) MNP_TRY(lane_start(G, *L, c, s, next++));
-          else --active;
-        }
-      }
-      if (!progressed) std::this_thread::yield();
-    }
-  }
-  return MNPBEM_OK;
-}
+// One wavelength sweep on one handle.  A call of mnpbem_solve is one job; a
+// call of mnpbem_solve_batch runs several jobs (particles) through one
+// scheduler loop, so that the lanes of every handle stay busy together.
+struct Job {
+  mnpbem_geom* G = nullptr;
+  SolveCtx c;
+  Sweep s;
+  int nl = 1;
+  int next = 0;                 // next wavelength to hand out
+  int active = 0;               // lanes with queued work
+  std::vector<Lane*> run;       // lanes with graphs for this configuration
+};
 
-}  // namespace
-
-extern "C" {
-
-mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t nenei,
-                           const double* enei, const double* eps_media, int32_t nmed,
-                           int32_t precision, const mnpbem_refine* refine, mnpbem_solution* out) {
+mnpbem_status validate_job(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t nenei, const double* enei,
+                           const double* eps_media, int32_t nmed, int32_t precision, mnpbem_solution* out) {
   MNP_TRY(check_geom(G));
   if (!exc || !enei || !eps_media || nenei <= 0 || nmed < G->max_medium || nmed > ASM_MAXMED ||
       exc->npol <= 0 || exc->npol > 4 || !exc->pol || !exc->dir || exc->medium < 1 ||
@@ -1225,11 +1166,17 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
     set_error("nested media (inside medium of one particle equals the outside of another) are not supported");
     return MNPBEM_ERR_UNSUPPORTED;
   }
-  MNP_CUDA(cudaSetDevice(G->device));
+  return MNPBEM_OK;
+}
+
+// excitation buffer, lanes, workspaces, masks and the parameter ring of a job
+mnpbem_status job_setup(Job& j, const mnpbem_planewave* exc, int32_t nenei, const double* enei,
+                        const double* eps_media, int32_t nmed, int32_t precision,
+                        const mnpbem_refine* refine, mnpbem_solution* out) {
+  mnpbem_geom* G = j.G;
   ProfBind pb_(&G->prof);
   const int P = exc->npol;
   const int64_t n = G->g.n;
-  // excitation buffer shared by the lanes: pol, dir, inf nvec, inf area
   {
     std::vector<double> eb;
     eb.insert(eb.end(), exc->pol, exc->pol + 3 * P);
@@ -1242,56 +1189,227 @@ mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t 
     MNP_TRY(G->exbuf.ensure(sizeof(double) * eb.size()));
     MNP_CUDA(cudaMemcpy(G->exbuf.ptr, eb.data(), sizeof(double) * eb.size(), cudaMemcpyHostToDevice));
   }
-  // lanes and their workspaces
-  const int nl = choose_lanes(G, precision, P, exc->ninf, nenei);
-  while ((int)G->lanes.size() < nl) MNP_TRY(add_lane(G));
+  j.nl = choose_lanes(G, precision, P, exc->ninf, nenei);
+  while ((int)G->lanes.size() < j.nl) MNP_TRY(add_lane(G));
   std::vector<unsigned char> masks(2 * n);
   for (int64_t i = 0; i < n; ++i) {
     const int p = G->face_part[i];
     masks[i] = G->inout[2 * p] == exc->medium;
     masks[n + i] = G->inout[2 * p + 1] == exc->medium;
   }
-  for (int l = 0; l < nl; ++l) {
+  for (int l = 0; l < j.nl; ++l) {
     MNP_TRY(ensure_workspace(G, *G->lanes[l], precision, P, exc->ninf));
     MNP_TRY(upload_masks(G, *G->lanes[l], masks));
   }
   MNP_TRY(ensure_lp_ring(G, nenei));
-  SolveCtx c;
-  c.P = P;
-  c.precision = precision;
-  c.exc = exc;
-  Sweep s;
-  s.nenei = nenei;
-  s.enei = enei;
-  s.eps = eps_media;
-  s.nmed = nmed;
-  s.medium = exc->medium;
-  s.ref.maxit = refine && refine->max_iter > 0 ? refine->max_iter : 10;
-  s.ref.tol = refine && refine->tol > 0 ? refine->tol : 1e-10;
-  s.out = out;
-  const mnpbem_status rs = run_sweep(G, c, s, nl);
-  if (rs != MNPBEM_OK) {
+  j.c.P = P;
+  j.c.precision = precision;
+  j.c.exc = exc;
+  j.s.nenei = nenei;
+  j.s.enei = enei;
+  j.s.eps = eps_media;
+  j.s.nmed = nmed;
+  j.s.medium = exc->medium;
+  j.s.ref.maxit = refine && refine->max_iter > 0 ? refine->max_iter : 10;
+  j.s.ref.tol = refine && refine->tol > 0 ? refine->tol : 1e-10;
+  j.s.out = out;
+  j.next = 0;
+  j.active = 0;
+  j.run.clear();
+  return MNPBEM_OK;
+}
+
+// lanes without graphs for this configuration run one wavelength directly
+// (sizing every buffer), then capture the stages; without graphs every
+// wavelength runs directly on lane 0
+mnpbem_status job_prepare(Job& j) {
+  mnpbem_geom* G = j.G;
+  ProfBind pb_(&G->prof);
+  const SolveCtx& c = j.c;
+  const Sweep& s = j.s;
+  std::vector<int> fresh;
+  for (int l = 0; l < j.nl && j.next < s.nenei; ++l) {
+    Lane& L = *G->lanes[l];
+    if (graphs_match(G, L, c)) continue;
+    if (L.graphs.valid) drop_graphs(G, L);
+    const int w = j.next++;
+    MNP_TRY(upload_lp(G, L, s, w));
+    L.w = w;
+    MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
+    MNP_TRY(write_outputs(G, L, c, s, w));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
+    if (!G->use_graphs) break;
+    fresh.push_back(l);
+  }
+  for (int l : fresh) {
+    Lane& L = *G->lanes[l];
+    bool ok = true;
+    for (int stage = 0; stage < NSTAGES && ok; ++stage) {
+      if ((stage == 3 || stage == 5) && c.precision != MNPBEM_MIXED) continue;
+      ok = capture_stage(G, L, c, stage) == MNPBEM_OK;
+    }
+    if (ok) {
+      auto& gr = L.graphs;
+      gr.valid = true;
+      gr.precision = c.precision;
+      gr.P = c.P;
+      gr.ninf = c.exc->ninf;
+      gr.prof = G->prof.enabled;
+      gr.sig = lane_sig(G, L);
+    } else {
+      drop_graphs(G, L);
+      G->use_graphs = false;   // run directly from now on
+    }
+  }
+  if (!G->use_graphs) {
+    Lane& L = *G->lanes[0];
+    for (; j.next < s.nenei; ++j.next) {
+      MNP_TRY(upload_lp(G, L, s, j.next));
+      L.w = j.next;
+      MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
+      MNP_TRY(write_outputs(G, L, c, s, j.next));
+    }
+    return MNPBEM_OK;
+  }
+  for (int l = 0; l < j.nl; ++l)
+    if (graphs_match(G, *G->lanes[l], c)) j.run.push_back(G->lanes[l].get());
+  return MNPBEM_OK;
+}
+
+// the remaining wavelengths of every job go to its lanes as they free up; the
+// host polls each lane's completion event and queues the lane's next step
+mnpbem_status jobs_poll(std::vector<Job*>& jobs) {
+  cudaEvent_t start;
+  MNP_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } eg{start};
+  int active = 0;
+  for (Job* j : jobs) {
+    ProfBind pb_(&j->G->prof);
+    MNP_CUDA(cudaEventRecord(start, j->G->st));
+    for (Lane* L : j->run) {
+      MNP_CUDA(cudaStreamWaitEvent(L->st, start, 0));
+      if (j->next < j->s.nenei) {
+        MNP_TRY(lane_start(j->G, *L, j->c, j->s, j->next++));
+        ++j->active;
+        ++active;
+      }
+    }
+  }
+  while (active > 0) {
+    bool progressed = false;
+    for (Job* j : jobs) {
+      if (!j->active) continue;
+      ProfBind pb_(&j->G->prof);
+      for (Lane* L : j->run) {
+        if (L->state == Lane::IDLE) continue;
+        const cudaError_t q = cudaEventQuery(L->ev);
+        if (q == cudaErrorNotReady) continue;
+        MNP_CUDA(q);
+        progressed = true;
+        MNP_TRY(lane_advance(j->G, *L, j->c, j->s));
+        if (L->state == Lane::IDLE) {
+          if (j->next < j->s.nenei) {
+            MNP_TRY(lane_start(j->G, *L, j->c, j->s, j->next++));
+          } else {
+            --j->active;
+            --active;
+          }
+        }
+      }
+    }
+    if (!progressed) std::this_thread::yield();
+  }
+  return MNPBEM_OK;
+}
+
+// join (the handle's stream waits for every lane), synchronise, read the
+// pivot and tensor-core status words
+mnpbem_status job_finish(Job& j, bool failed) {
+  mnpbem_geom* G = j.G;
+  if (failed) {
     // leave nothing in flight that writes the caller's buffers
-    for (int l = 0; l < nl; ++l) cudaStreamSynchronize(G->lanes[l]->st);
+    for (int l = 0; l < j.nl && l < (int)G->lanes.size(); ++l) cudaStreamSynchronize(G->lanes[l]->st);
     cudaGetLastError();
     G->prof.flush();
-    return rs;
+    return MNPBEM_OK;
   }
-  // join: the handle's stream waits for every lane
-  for (int l = 0; l < nl; ++l) {
+  for (int l = 0; l < j.nl; ++l) {
     Lane& L = *G->lanes[l];
     if (L.st == G->st) continue;
     MNP_CUDA(cudaEventRecord(L.ev, L.st));
     MNP_CUDA(cudaStreamWaitEvent(G->st, L.ev, 0));
   }
-  for (int l = 0; l < nl; ++l) MNP_CUDA(cudaStreamSynchronize(G->lanes[l]->st));
+  for (int l = 0; l < j.nl; ++l) MNP_CUDA(cudaStreamSynchronize(G->lanes[l]->st));
   G->prof.flush();
-  for (int l = 0; l < nl; ++l) {
+  for (int l = 0; l < j.nl; ++l) {
     Lane& L = *G->lanes[l];
     MNP_TRY(check_pivots(L));
-    if (precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(L.tc, L.st));
+    if (j.c.precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(L.tc, L.st));
   }
   return MNPBEM_OK;
+}
+
+mnpbem_status run_jobs(std::vector<Job>& jobs) {
+  mnpbem_status st = MNPBEM_OK;
+  for (Job& j : jobs)
+    if (st == MNPBEM_OK) st = job_prepare(j);
+  if (st == MNPBEM_OK) {
+    std::vector<Job*> js;
+    for (Job& j : jobs) js.push_back(&j);
+    st = jobs_poll(js);
+  }
+  if (st != MNPBEM_OK) {
+    const std::string keep = get_error();
+    for (Job& j : jobs) job_finish(j, true);
+    set_error("%s", keep.c_str());
+    return st;
+  }
+  for (Job& j : jobs) MNP_TRY(job_finish(j, false));
+  return MNPBEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mnpbem_status mnpbem_solve(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t nenei,
+                           const double* enei, const double* eps_media, int32_t nmed,
+                           int32_t precision, const mnpbem_refine* refine, mnpbem_solution* out) {
+  MNP_TRY(validate_job(G, exc, nenei, enei, eps_media, nmed, precision, out));
+  MNP_CUDA(cudaSetDevice(G->device));
+  std::vector<Job> jobs(1);
+  jobs[0].G = G;
+  MNP_TRY(job_setup(jobs[0], exc, nenei, enei, eps_media, nmed, precision, refine, out));
+  return run_jobs(jobs);
+}
+
+mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs_in, int32_t njobs, int32_t precision,
+                                 const mnpbem_refine* refine) {
+  if (!jobs_in || njobs <= 0) {
+    set_error("mnpbem_solve_batch: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  for (int a = 0; a < njobs; ++a) {
+    const mnpbem_job& q = jobs_in[a];
+    MNP_TRY(validate_job(q.g, q.exc, q.nenei, q.enei, q.eps_media, q.nmed, precision, q.out));
+    if (q.g->device != jobs_in[0].g->device) {
+      set_error("mnpbem_solve_batch: all handles must be on one device");
+      return MNPBEM_ERR_INVALID_ARG;
+    }
+    for (int b = 0; b < a; ++b)
+      if (jobs_in[b].g == q.g) {
+        set_error("mnpbem_solve_batch: a handle appears twice (job %d and %d)", b, a);
+        return MNPBEM_ERR_INVALID_ARG;
+      }
+  }
+  MNP_CUDA(cudaSetDevice(jobs_in[0].g->device));
+  std::vector<Job> jobs(njobs);
+  for (int a = 0; a < njobs; ++a) {
+    const mnpbem_job& q = jobs_in[a];
+    jobs[a].G = q.g;
+    MNP_TRY(job_setup(jobs[a], q.exc, q.nenei, q.enei, q.eps_media, q.nmed, precision, refine, q.out));
+  }
+  return run_jobs(jobs);
 }
 
 mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps_media,

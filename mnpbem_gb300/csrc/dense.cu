@@ -247,6 +247,60 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64
   }
 }
 
+// FP32 variant of the same product from the hi planes only (plain FMA
+// accumulation): for refinement steps whose residual is still large.
+template <int N>
+__global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_hi(int64_t M, int64_t K, const float2* __restrict__ Ahi,
+                                                              int64_t lda, const float2* __restrict__ Bh, int64_t ldb,
+                                                              double2* __restrict__ C, int64_t ldc) {
+  __shared__ float2 red[DS_WARPS][DS_TR][N];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = (int64_t)blockIdx.x * DS_TR;
+  const int64_t kw = (K + DS_WARPS - 1) / DS_WARPS;
+  const int64_t kbeg = warp * kw, kend = min(K, kbeg + kw);
+  int64_t roff[DS_TR];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r) roff[r] = min(row0 + r, M - 1) * lda;
+  float2 acc[DS_TR][N];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) acc[r][c] = make_float2(0.f, 0.f);
+#pragma unroll 2
+  for (int64_t k = kbeg + lane; k < kend; k += 32) {
+    float2 xh[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) xh[c] = __ldg(Bh + k * ldb + c);
+#pragma unroll
+    for (int r = 0; r < DS_TR; ++r) {
+      const float2 ah = __ldg(Ahi + roff[r] + k);
+#pragma unroll
+      for (int c = 0; c < N; ++c) cfma(acc[r][c], ah, xh[c]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      float2 v = acc[r][c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[warp][r][c] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < DS_TR * N; t += blockDim.x) {
+    const int r = t / N, c = t % N;
+    const int64_t row = row0 + r;
+    if (row >= M) continue;
+    float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int w = 0; w < DS_WARPS; ++w) v = cadd(v, red[w][r][c]);
+    C[row * ldc + c] = make_double2(v.x, v.y);
+  }
+}
+
 mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
                            float2* bsplit, cudaStream_t st) {
@@ -259,8 +313,21 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
     k_split_hi_lo<<<(unsigned)cdiv_up(K * N, 256), 256, 0, st>>>(B, K * N, Bh, Bl);
     MNP_CHECK_LAUNCH();
   }
-  ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 16.0 * M * K + 16.0 * K * N + 16.0 * M * N);
   const unsigned nblk = (unsigned)cdiv_up(M, (int64_t)DS_TR);
+  if (!Alo) {
+    ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 8.0 * M * K + 8.0 * K * N + 16.0 * M * N);
+#define HI_CASE(NN)                                                                                \
+  case NN:                                                                                         \
+    k_gemm_thin_hi<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, lda, Bh, N, C, ldc);            \
+    break;
+    switch (N) {
+      HI_CASE(1) HI_CASE(2) HI_CASE(3) HI_CASE(4) HI_CASE(5) HI_CASE(6) HI_CASE(7) HI_CASE(8)
+    }
+#undef HI_CASE
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 16.0 * M * K + 16.0 * K * N + 16.0 * M * N);
 #define DS_CASE(NN)                                                                                   \
   case NN:                                                                                            \
     k_gemm_thin_ds<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, Alo, lda, Bh, Bl, N, C, ldc);     \
@@ -395,15 +462,18 @@ __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A
 //   1. the CTA owning the panel rows stages them in shared memory, inverts
 //      the 16 x 16 pivot block X (Gauss-Jordan, one entry per thread) and
 //      forms the new panel rows R = X * P (pivot columns replaced by X);
-//   2. it writes R into every CTA of the cluster (distributed shared memory),
-//      every CTA stages its own 16 panel-column entries C; cluster barrier;
+//   2. every CTA stages its own 16 panel-column entries C; cluster barrier;
+//      the other CTAs copy R out of the owner's shared memory (distributed
+//      shared memory reads, spread over the cluster);
 //   3. every row i outside the panel: a_ij <- [j not a pivot column] a_ij
 //      - sum_k C_ik R_kj; the panel rows take R.
-// One cluster barrier per panel (R is double-buffered), 16 panels for w = 256.
+// One cluster barrier per panel (R is double-buffered: a CTA may still be
+// copying panel p's R when the owner of panel p + 1 writes the other buffer),
+// 16 panels for w = 256.
 // Rows and columns beyond w are identity and stay identity.
 constexpr int PB_W = 256, PB_CL = 8, PB_RPC = PB_W / PB_CL, PB_THREADS = 512;
 constexpr int PB_TPR = PB_THREADS / PB_RPC, PB_CPT = PB_W / PB_TPR, PB_PAN = 16;
-constexpr int PB_SMEM = (2 * PB_PAN * PB_W + 2 * PB_RPC * PB_PAN + PB_PAN * PB_PAN) * (int)sizeof(float2);
+constexpr int PB_SMEM = (3 * PB_PAN * PB_W + 2 * PB_RPC * PB_PAN + PB_PAN * PB_PAN) * (int)sizeof(float2);
 static_assert(PB_PAN % PB_TPR == 0 || PB_TPR % PB_PAN == 0, "panel / thread layout");
 static_assert(PB_RPC % PB_PAN == 0, "a panel lies inside one CTA");
 
@@ -413,8 +483,9 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ float2 pb_smem[];
-  float2* Rb = pb_smem;                              // [2][PAN][W]  panel rows (broadcast)
-  float2* Cb = Rb + 2 * PB_PAN * PB_W;               // [2][RPC][PAN] own panel-column entries
+  float2* Rb = pb_smem;                              // [2][PAN][W]  new panel rows
+  float2* P = Rb + 2 * PB_PAN * PB_W;                // [PAN][W]     owner: raw panel rows
+  float2* Cb = P + PB_PAN * PB_W;                    // [2][RPC][PAN] own panel-column entries
   float2* Xs = Cb + 2 * PB_RPC * PB_PAN;             // [PAN][PAN] pivot block (owner)
   const int rank = (int)cluster.block_rank();
   const int t = threadIdx.x, lr = t / PB_TPR, ph = t % PB_TPR;
@@ -429,7 +500,6 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
   for (int pp = 0; pp < npan; ++pp) {
     const int p0 = pp * PB_PAN, owner = p0 / PB_RPC, lp0 = p0 % PB_RPC, buf = pp & 1;
     float2* R = Rb + buf * PB_PAN * PB_W;
-    float2* P = Rb + (buf ^ 1) * PB_PAN * PB_W;      // owner scratch: raw panel rows
     float2* C = Cb + buf * PB_RPC * PB_PAN;
     __syncthreads();                                  // the previous panel's reads of P / C are done
     // own panel-column entries (every CTA)
@@ -467,7 +537,7 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
         if (act) Xs[bi * PB_PAN + bj] = v;
         __syncthreads();
       }
-      // R = X * P with the pivot columns replaced by X, written to every CTA
+      // R = X * P with the pivot columns replaced by X
       for (int e = t; e < PB_PAN * PB_W; e += PB_THREADS) {
         const int i = e / PB_W, c = e % PB_W;
         float2 r;
@@ -478,11 +548,17 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
 #pragma unroll
           for (int k = 0; k < PB_PAN; ++k) cfma(r, Xs[i * PB_PAN + k], P[k * PB_W + c]);
         }
-#pragma unroll
-        for (int q = 0; q < PB_CL; ++q) cluster.map_shared_rank(R, q)[e] = r;
+        R[e] = r;
       }
     }
     cluster.sync();
+    if (rank != owner) {
+      const float4* src = reinterpret_cast<const float4*>(cluster.map_shared_rank(R, owner));
+      float4* dst = reinterpret_cast<float4*>(R);
+#pragma unroll 4
+      for (int e = t; e < PB_PAN * PB_W / 2; e += PB_THREADS) dst[e] = src[e];
+      __syncthreads();
+    }
     // update of this CTA's rows
     const bool prow = (rank == owner) && lr >= lp0 && lr < lp0 + PB_PAN;
     if (prow) {

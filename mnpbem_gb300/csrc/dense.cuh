@@ -16,6 +16,7 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
 // TwoSum accumulation, ~48-bit accuracy): A_hi = fl32(A), A_lo = fl32(A - A_hi)
 // are complex64 planes, B (packed, ldb = N) and C are complex128.
 // bsplit: workspace of 2 K N complex64 (hi / lo planes of B).
+// Alo == NULL: FP32 product of the hi planes (FMA accumulation, ~24 bits).
 mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
                            float2* bsplit, cudaStream_t st);

@@ -328,10 +328,13 @@ class GreenRet:
     coefficients in powers of (i k).
     """
 
-    def __init__(self, p, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+    def __init__(self, p, order=5, rel_cutoff=3.0, abs_cutoff=0.0, pattern=None):
         self.p = p
         self.order = order
-        ir = refinematrix(p, rel_cutoff, abs_cutoff)
+        # pattern: a fixed refinement pattern (finite-difference checks keep
+        # it constant while the vertices move)
+        ir = refinematrix(p, rel_cutoff, abs_cutoff) if pattern is None else pattern
+        self.pattern = ir
         n = p.n
         rows, cols = np.nonzero(ir.T)          # column-major order of find()
         rows, cols = cols, rows
@@ -461,9 +464,9 @@ def initclosed(gr, cp):
 class CompGreenRet:
     """compgreenret(p, p, op): greenret + closed-surface diagonal + con."""
 
-    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0, pattern=None):
         self.p = cp
-        self.g = GreenRet(cp, order, rel_cutoff, abs_cutoff)
+        self.g = GreenRet(cp, order, rel_cutoff, abs_cutoff, pattern)
         initclosed(self.g, cp)
         self.con = connect(cp.inout)
 
@@ -523,9 +526,9 @@ def _outer(nvec, val):
 
 
 class BemRet:
-    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0):
+    def __init__(self, cp, order=5, rel_cutoff=3.0, abs_cutoff=0.0, pattern=None):
         self.p = cp
-        self.g = CompGreenRet(cp, order, rel_cutoff, abs_cutoff)
+        self.g = CompGreenRet(cp, order, rel_cutoff, abs_cutoff, pattern)
         self.enei = None
 
     def matrices(self, enei):

@@ -253,3 +253,38 @@ def test_tensor_core_inversions_at_1200_faces(gpu_lib):
          "iters": rmx["ir_iters"].tolist()}
     record("solve_mixed_vs_fp64_1200", **e)
     assert e["ext"] < 1e-8 and e["sca"] < 1e-8, e
+
+
+def test_batch_of_uneven_particles_matches_single_solves(gpu_lib):
+    """mnpbem_solve_batch: a sphere, a capped rod (quadrilaterals) and a rounded
+    cube of different face counts, two polarisations, solved together give
+    the results of one mnpbem_solve per particle; the FP64 rod also agrees with
+    the oracle solved live."""
+    v1, f1 = shapes.fibsphere(300, 30.0)
+    v2, f2 = shapes.trirod(10.0, 40.0, (17, 5, 9))
+    v3, f3 = shapes.tricube(7, 40.0, shapes.rounding_to_e(40.0, 4.0))
+    exc = m.planewave([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]])
+    enei = np.linspace(450.0, 800.0, 5)
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-12)):
+        bems = []
+        for v, f in ((v1, f1), (v2, f2), (v3, f3)):
+            cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
+            bems.append(m.bemsolver(cp, m.bemoptions(precision=prec)))
+        single = [b.spectrum(exc, enei) for b in bems]
+        batch = m.spectrum_batch([(b, exc, enei) for b in bems])
+        for k, (a, b) in enumerate(zip(batch, single)):
+            errs = {"ext": rel(a["ext"], b["ext"]), "sca": rel(a["sca"], b["sca"])}
+            record("batch_vs_single_%s_%d" % (prec, k), **errs)
+            assert errs["ext"] < tol and errs["sca"] < tol, (prec, k, errs)
+    # the rod (quadrilateral faces) against the live oracle, FP64
+    cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v2, f2)], [[2, 1]], 1)
+    R, ocp, _ = oracle_setup(cp)
+    t = shapes.tables()
+    q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    vi, fi = shapes.trisphere(256, 2.0)
+    pw = R.PlaneWaveRet([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]], R.Particle(vi, fi, q))
+    oext, osca, _, _ = R.solve_spectrum(ocp, pw, enei[:2])
+    r = m.bemsolver(cp, m.bemoptions(precision="fp64")).spectrum(exc, enei[:2])
+    errs = {"ext": rel(r["ext"], oext), "sca": rel(r["sca"], osca)}
+    record("rod_quads_fp64_vs_oracle", **errs)
+    assert errs["ext"] < 1e-10 and errs["sca"] < 1e-10, errs
