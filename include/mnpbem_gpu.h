@@ -172,6 +172,23 @@ typedef struct mnpbem_job {
 MNPBEM_API mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs, int32_t njobs, int32_t precision,
                                             const mnpbem_refine* refine);
 
+/* Gradient of the extinction cross section of polarisation ipol at one
+ * wavelength by the adjoint method: a transposed solve through the transposed
+ * inverses of the forward solve, then the derivatives of G, F (far pairs,
+ * refined near pairs, self elements, closed-surface diagonal), of the
+ * excitation and of the far field contracted with the adjoint and forward
+ * surface charges, chained to the vertices through norm_flat.m.  No
+ * counterpart in the reference (MNPBEM has no derivatives).  The refinement
+ * pattern is held fixed.  Scope: one closed particle excited from its outside
+ * medium; precision MNPBEM_FP64.
+ *   ext: the cross section (may be NULL); verts_grad [nverts][3] (host):
+ *   dext / dvertex; eps_grad [2] (host): dext / dRe(eps), dext / dIm(eps) of
+ *   the medium inside the particle.                                          */
+MNPBEM_API mnpbem_status mnpbem_ext_gradient(mnpbem_geom* g, const mnpbem_planewave* exc, int32_t ipol,
+                                             double enei, const double* eps_media, int32_t nmed,
+                                             int32_t precision, double* ext, double* verts_grad,
+                                             double* eps_grad);
+
 /* The matrices bemret stores per wavelength (initmat.m:27-72), copied to host
  * as complex128 [n][n] (NULL to skip): G1i, G2i, Sigma1, Deltai, Sigmai.       */
 MNPBEM_API mnpbem_status mnpbem_bem_matrices(mnpbem_geom* g, double enei, const double* eps_media,

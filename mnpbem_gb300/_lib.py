@@ -78,6 +78,9 @@ SIGNATURES = {
                                     ctypes.POINTER(Refine), ctypes.POINTER(Solution)]),
     "mnpbem_solve_batch": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(Refine)]),
+    "mnpbem_ext_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlaneWave), ctypes.c_int32,
+                                           ctypes.c_double, c_double_p, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mnpbem_bem_matrices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p,
                                            ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 5),
     "mnpbem_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

@@ -268,6 +268,23 @@ class bemret:
                                           ctypes.byref(a["sol"])))
         return a["res"]
 
+    def ext_gradient(self, exc, enei, ipol=0):
+        """Extinction of polarisation ``ipol`` at ``enei`` and its gradient
+        (adjoint method, FP64): returns ``(ext, dext/dverts [nverts, 3],
+        dext/deps)`` with ``dext/deps = dext/dRe(eps) + 1j dext/dIm(eps)`` of
+        the medium inside the particle.  One closed particle excited from its
+        outside medium; the refinement pattern is held fixed."""
+        em = np.ascontiguousarray(self._eps(float(enei))[0])
+        pw = exc._struct()
+        ext = np.zeros(1)
+        gv = np.zeros((self.p.verts.shape[0], 3))
+        ge = np.zeros(2)
+        _lib.check(self._lib.mnpbem_ext_gradient(
+            self._h, ctypes.byref(pw), int(ipol), float(enei),
+            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, _lib.FP64,
+            _lib.vptr(ext), _lib.vptr(gv), _lib.vptr(ge)))
+        return float(ext[0]), gv, complex(ge[0], ge[1])
+
     def mldivide(self, exc):
         """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m)."""
         pw = exc.exc

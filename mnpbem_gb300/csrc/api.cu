@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "assemble.cuh"
 #include "bem.cuh"
 #include "dense.cuh"
@@ -125,7 +126,11 @@ struct mnpbem_geom {
   std::vector<int> inout;   // [np][2]
   std::vector<int> face_part;
   int max_medium = 0;
+  int64_t nverts = 0;
+  bool all_closed = true;
   DevBuf d_part, d_src, d_nrm, face_med, exbuf;
+  DevBuf adj, adj_mats, adj_off;   // adjoint gradient workspace
+  int adj_noff = -1;
   int64_t ld = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
   int lanes_req = 0;        // 0: automatic
@@ -305,6 +310,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   std::vector<int> cs, ce;
   for (int i = 0; i < nparts; ++i)
     if (!closed || closed[i]) { cs.push_back((int)G->part_off[i]); ce.push_back((int)G->part_off[i + 1]); }
+  G->nverts = nverts;
+  G->all_closed = (int)cs.size() == nparts;
   G->g.order = op.order;
   mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, nfaces, cs.data(), ce.data(),
                                    (int)cs.size(), quad, op.rel_cutoff, op.abs_cutoff, G->st);
@@ -1410,6 +1417,139 @@ mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs_in, int32_t njobs, int32
     MNP_TRY(job_setup(jobs[a], q.exc, q.nenei, q.enei, q.eps_media, q.nmed, precision, refine, q.out));
   }
   return run_jobs(jobs);
+}
+
+mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t ipol, double enei,
+                                  const double* eps_media, int32_t nmed, int32_t precision, double* ext,
+                                  double* verts_grad, double* eps_grad) {
+  MNP_TRY(check_geom(G));
+  if (!exc || ipol < 0 || ipol >= exc->npol || !verts_grad || !eps_grad) {
+    set_error("mnpbem_ext_gradient: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if (precision != MNPBEM_FP64) {
+    set_error("mnpbem_ext_gradient: only MNPBEM_FP64 is implemented");
+    return MNPBEM_ERR_UNSUPPORTED;
+  }
+  if (G->nparts != 1 || !G->all_closed || G->inout[0] == G->inout[1] || exc->medium != G->inout[1]) {
+    set_error("mnpbem_ext_gradient: one closed particle excited from its outside medium is required");
+    return MNPBEM_ERR_UNSUPPORTED;
+  }
+  double sol_ext[4] = {0, 0, 0, 0};
+  mnpbem_solution sol{};
+  sol.ext = sol_ext;
+  MNP_TRY(validate_job(G, exc, 1, &enei, eps_media, nmed, precision, &sol));
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  std::vector<Job> jobs(1);
+  Job& j = jobs[0];
+  j.G = G;
+  MNP_TRY(job_setup(j, exc, 1, &enei, eps_media, nmed, precision, nullptr, &sol));
+  Lane& L = *G->lanes[0];
+  cudaStream_t st = L.st;
+  // forward solve (FP64, direct) on lane 0
+  MNP_TRY(upload_lp(G, L, j.s, 0));
+  L.w = 0;
+  MNP_TRY(solve_one(G, L, j.c, j.s.ref, false, &L.iters, &L.res));
+  MNP_TRY(write_outputs(G, L, j.c, j.s, 0));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  if (ext) *ext = sol_ext[ipol];
+  const int64_t n = G->g.n, ld = G->ld, nv = G->nverts;
+  const int P = exc->npol;
+  // refined off-diagonal entries (once per geometry)
+  if (G->adj_noff < 0) {
+    std::vector<int> rr(G->g.nref), cc(G->g.nref), off;
+    MNP_CUDA(cudaMemcpy(rr.data(), G->g.ref_row, sizeof(int) * G->g.nref, cudaMemcpyDeviceToHost));
+    MNP_CUDA(cudaMemcpy(cc.data(), G->g.ref_col, sizeof(int) * G->g.nref, cudaMemcpyDeviceToHost));
+    for (int64_t e = 0; e < G->g.nref; ++e)
+      if (rr[e] != cc[e]) off.push_back((int)e);
+    MNP_TRY(G->adj_off.ensure(sizeof(int) * std::max<size_t>(1, off.size())));
+    if (!off.empty()) MNP_CUDA(cudaMemcpy(G->adj_off.ptr, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    G->adj_noff = (int)off.size();
+  }
+  // workspace: complex vectors, weights, accumulators, three FP64 matrices
+  const size_t cs = sizeof(double2);
+  const size_t nvec_c = 40 * (size_t)n;         // complex vectors of the transposed chain + products
+  const size_t nacc = 7 * (size_t)n + 3 * (size_t)nv + 4;
+  MNP_TRY(G->adj.ensure(cs * (nvec_c + 24 * (size_t)n) + sizeof(double) * (nacc + (size_t)n) + 256));
+  MNP_TRY(G->adj_mats.ensure(cs * 3 * (size_t)n * ld));
+  double2* V = G->adj.as<double2>();
+  double2 *gs2 = V, *gh2 = gs2 + n, *gS2 = gh2 + 3 * n, *gH2p = gS2 + n, *gAl = gH2p + 3 * n, *gDe = gAl + 3 * n;
+  double2 *v3b = gDe + n, *tS1 = v3b + 3 * n, *ga = tS1 + n, *gphi = ga + 3 * n;
+  double2 *GX1 = gphi + n, *GX2 = GX1 + 4 * n, *HX1 = GX2 + 4 * n;   // 40 n in total
+  double2* Ub = V + nvec_c;
+  double2* Xb = Ub + 16 * n;
+  double* acc = reinterpret_cast<double*>(Xb + 8 * n);
+  double* cb = acc + nacc;
+  MNP_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * nacc, st));
+  const LamParams& lp = G->lp_ring[0];
+  const int in = G->inout[0], out = G->inout[1];
+  AdjParams p;
+  p.n = n;
+  p.order = G->g.order;
+  p.pos = G->g.pos; p.nvec = G->g.nvec; p.area = G->g.area; p.verts = G->g.verts; p.faces = G->g.faces;
+  p.xt = G->g.xt; p.yt = G->g.yt; p.wt = G->g.wt; p.ntri = G->g.ntri;
+  p.x3 = G->g.x3; p.y3 = G->g.y3; p.w3 = G->g.w3; p.n3 = G->g.n3;
+  p.x4 = G->g.x4; p.y4 = G->g.y4; p.w4 = G->g.w4; p.n4 = G->g.n4;
+  p.ref_row = G->g.ref_row; p.ref_col = G->g.ref_col;
+  p.off_idx = G->adj_off.as<int>(); p.noff = G->adj_noff;
+  const FaceData fd = face_data(G, L);
+  p.eps1 = fd.eps1; p.eps2 = fd.eps2; p.exc_out = fd.exc_out;
+  p.k1 = lp.k[in - 1]; p.k2 = lp.k[out - 1]; p.kb = lp.kexc; p.k0 = lp.k0;
+  p.U = Ub; p.X = Xb; p.cb = cb;
+  p.gpos = acc; p.gnv = acc + 3 * n; p.garea = acc + 6 * n; p.gv = acc + 7 * n; p.gk1 = acc + 7 * n + 3 * nv;
+  double* geps = p.gk1 + 2;
+  const double* pol_d = G->exbuf.as<double>() + 3 * ipol;
+  const double* dir_d = G->exbuf.as<double>() + 3 * P + 3 * ipol;
+  // ---- adjoint solve A^T lam = dJ/dx through the transposed chain of mldivide.m
+  double2* M[5];
+  for (int q = 0; q < 5; ++q) {
+    M[q] = L.mat[q].as<double2>();
+    adj_transpose(M[q], n, ld, st);   // G1i, G2i, Sigmai, Deltai, Sigma1 -> transposes
+  }
+  MNP_CHECK_LAUNCH();
+  adj_rhs(p, pol_d, dir_d, gs2, gh2, st);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[1], ld, gs2, 1, zero, gS2, 1, st));     // G2i^T w_sig2
+  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[1], ld, gh2, 3, zero, gH2p, 3, st));    // G2i^T w_h2
+  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[3], ld, gH2p, 3, zero, gAl, 3, st));    // Deltai^T
+  adj_chain_step(p, 0, gAl, nullptr, gS2, nullptr, nullptr, st);
+  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[2], ld, gS2, 1, zero, gDe, 1, st));     // Sigmai^T
+  adj_chain_step(p, 1, gDe, nullptr, v3b, nullptr, nullptr, st);
+  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[3], ld, v3b, 3, one, gAl, 3, st));      // += Deltai^T v
+  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[4], ld, gDe, 1, zero, tS1, 1, st));     // Sigma1^T
+  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[4], ld, gAl, 3, zero, ga, 3, st));
+  adj_chain_step(p, 2, tS1, gAl, gphi, ga, gDe, st);
+  MNP_CHECK_LAUNCH();
+  // ---- weights, then G1 [sig1 h1], G2 [sig2 h2], H1 sig1 from freshly assembled FP64 matrices
+  Vec64 vv = vec64(G, L, P);
+  adj_weights(p, gphi, ga, gDe, gAl, vv.x1, vv.x2, P, ipol, st);
+  MNP_CHECK_LAUNCH();
+  {
+    AsmParams ap = base_params(G, L.lp_dev.as<LamParams>());
+    double2* AM = G->adj_mats.as<double2>();
+    ap.ld64 = ld;
+    ap.G1 = AM; ap.H1 = AM + n * ld; ap.G2 = AM + 2 * n * ld; ap.H2 = nullptr;
+    MNP_TRY(assemble_launch(ap, true, false, st));
+    MNP_TRY(gemm_simt<double>(n, 4, n, one, ap.G1, ld, Xb, 8, zero, GX1, 4, st));
+    MNP_TRY(gemm_simt<double>(n, 4, n, one, ap.G2, ld, Xb + 4, 8, zero, GX2, 4, st));
+    MNP_TRY(gemm_simt<double>(n, 1, n, one, ap.H1, ld, Xb, 8, zero, HX1, 1, st));
+  }
+  // ---- geometric contractions and the chain rule to the vertices
+  adj_geometry(p, pol_d, dir_d, gphi, ga, gDe, gAl, GX1, GX2, HX1, geps, st);
+  MNP_CHECK_LAUNCH();
+  MNP_CUDA(cudaMemcpyAsync(verts_grad, p.gv, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, st));
+  double hk[4];
+  MNP_CUDA(cudaMemcpyAsync(hk, p.gk1, sizeof(double) * 4, cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  G->prof.flush();
+  // eps of the inside medium: k1 = k0 sqrt(eps) (dk1/deps = k1 / (2 eps)) plus the explicit eps1
+  const std::complex<double> gk1(hk[0], hk[1]), gex(hk[2], hk[3]);
+  const std::complex<double> k1(p.k1.x, p.k1.y), e1(lp.eps[in - 1].x, lp.eps[in - 1].y);
+  const std::complex<double> g = -(gk1 * (k1 / (2.0 * e1)) + gex);
+  eps_grad[0] = g.real();     // dJ / dRe(eps)
+  eps_grad[1] = -g.imag();    // dJ / dIm(eps)
+  return MNPBEM_OK;
 }
 
 mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps_media,

@@ -14,20 +14,107 @@ namespace mnpbem {
 
 struct PairVal { double2 G, F; };
 
-// G and F of one pair for wavenumber k (far-field formula)
-__device__ __forceinline__ PairVal far_pair(double2 k, double dd, double in, double area) {
+// ------------------------------------------------------- exp(i k d), FP64
+// Table-driven evaluation (Cody-Waite argument reduction + short Taylor
+// polynomials), a few FP64 FMAs per call instead of a library sincos and exp:
+//   phase  th = Re(k) d = j (2 pi / 256) + t,  |t| <= pi / 256:
+//          cis(th) = cis(2 pi j / 256) * (cos t + i sin t), Taylor to t^8;
+//   decay  x = Im(k) d = y (ln 2 / 64) + u,   |u| <= ln 2 / 128:
+//          exp(-x) = 2^(-floor(y/64)) * 2^(-(y mod 64)/64) * exp(-u), Taylor to u^7.
+// The reduction constants are split in a 32-bit head (exact products with
+// |j| < 2^20) and a tail; the tables come from the device's sincospi / exp2
+// once per device.  Accuracy: a few ulp of the FP64 result.
+constexpr int CIS_N = 256;
+constexpr double CIS_INV = 40.74366543152521;        // 256 / (2 pi)
+constexpr double CIS_C1 = 0.024543692605220713;      // 2 pi / 256, head
+constexpr double CIS_C2 = 9.495469541415925e-13;     // 2 pi / 256, tail
+constexpr double EXP_INV = 92.33248261689366;        // 64 / ln 2
+constexpr double EXP_L1 = 0.01083042469326756;       // ln 2 / 64, head
+constexpr double EXP_L2 = 2.9815858269852933e-12;    // ln 2 / 64, tail
+
+struct CisTable {
+  double2 cs[CIS_N];   // (cos, sin)(2 pi j / 256)
+  double e2[64];       // 2^(-m / 64)
+};
+__device__ CisTable g_cis;
+
+__global__ void k_cis_init() {
+  const int j = threadIdx.x;
   double s, c;
-  sincos(k.x * dd, &s, &c);
-  double e = exp(-k.y * dd);
-  double2 ph = make_double2(e * c, e * s);
-  double ga = area / dd;
+  sincospi(2.0 * j / CIS_N, &s, &c);
+  g_cis.cs[j] = make_double2(c, s);
+  if (j < 64) g_cis.e2[j] = exp2(-j / 64.0);
+}
+
+struct CisShared {
+  double2 cs[CIS_N];
+  double e2[64];
+};
+
+__device__ __forceinline__ void cis_load(CisShared& t) {
+  for (int q = threadIdx.x; q < CIS_N; q += blockDim.x) t.cs[q] = g_cis.cs[q];
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) t.e2[q] = g_cis.e2[q];
+  __syncthreads();
+}
+
+// exp(i k d) for complex k (Im k >= 0 for passive media; any sign works)
+__device__ __forceinline__ double2 cis_exp(const CisShared& T, double2 k, double d) {
+  const double th = k.x * d;
+  const double jf = rint(th * CIS_INV);
+  const double t = fma(-jf, CIS_C2, fma(-jf, CIS_C1, th));
+  const double t2 = t * t;
+  const double sn = t * fma(t2, fma(t2, fma(t2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), 1.0);
+  const double cn = fma(t2, fma(t2, fma(t2, fma(t2, 1.0 / 40320.0, -1.0 / 720.0), 1.0 / 24.0), -0.5), 1.0);
+  const double2 tb = T.cs[((long long)jf) & (CIS_N - 1)];
+  double cr = tb.x * cn - tb.y * sn;
+  double sr = fma(tb.y, cn, tb.x * sn);
+  if (k.y != 0.0) {
+    const double x = k.y * d;
+    double e;
+    if (x > 700.0) {
+      e = 0.0;
+    } else {
+      const double yf = rint(x * EXP_INV);
+      const double u = fma(-yf, EXP_L2, fma(-yf, EXP_L1, x));
+      const double v = -u;
+      const double ev = fma(v, fma(v, fma(v, fma(v, fma(v, fma(v, fma(v, 1.0 / 5040.0, 1.0 / 720.0), 1.0 / 120.0),
+                                                          1.0 / 24.0), 1.0 / 6.0), 0.5), 1.0), 1.0);
+      const long long yi = (long long)yf;
+      const long long nn = yi >> 6;                 // floor(y / 64)
+      const int m = (int)(yi - (nn << 6));
+      const double scale = __longlong_as_double((unsigned long long)(1023 - nn) << 52);   // 2^(-nn)
+      e = ev * T.e2[m] * scale;
+    }
+    cr *= e;
+    sr *= e;
+  }
+  return make_double2(cr, sr);
+}
+
+static bool g_cis_ready[64];
+static mnpbem_status ensure_cis(cudaStream_t st) {
+  int dev = 0;
+  MNP_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return MNPBEM_ERR_INVALID_ARG; }
+  if (!g_cis_ready[dev]) {
+    k_cis_init<<<1, CIS_N, 0, st>>>();
+    MNP_CHECK_LAUNCH();
+    if (!capturing_now()) g_cis_ready[dev] = true;
+  }
+  return MNPBEM_OK;
+}
+
+// G and F of one pair for wavenumber k (far-field formula); inv = 1 / d
+__device__ __forceinline__ PairVal far_pair(const CisShared& T, double2 k, double dd, double inv, double in,
+                                            double area) {
+  const double2 ph = cis_exp(T, k, dd);
+  const double ga = area * inv;
   PairVal v;
   v.G = make_double2(ga * ph.x, ga * ph.y);
   // (ik - 1/d) / d^2 * (n . r) * area
-  double inv = 1.0 / dd;
-  double2 t = make_double2((-k.y - inv) * inv * inv, k.x * inv * inv);
-  double fa = in * area;
-  double2 tf = make_double2(t.x * fa, t.y * fa);
+  const double inv2 = inv * inv;
+  const double fa = in * area;
+  const double2 tf = make_double2((-k.y - inv) * inv2 * fa, k.x * inv2 * fa);
   v.F = cmul(tf, ph);
   return v;
 }
@@ -72,6 +159,8 @@ constexpr int ASM_ROWS = 4;
 
 template <bool W64, bool W32>
 __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
+  __shared__ CisShared T;
+  cis_load(T);
   int64_t j = (int64_t)blockIdx.x * ASM_COLS + threadIdx.x;
   int64_t i0 = (int64_t)blockIdx.y * ASM_ROWS;
   if (j >= p.n) return;
@@ -88,14 +177,15 @@ __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
     double dist = sqrt(x * x + y * y + z * z);
     double dd = fmax(dist, DBL_EPS_ASM);
     double delta = (dd == DBL_EPS_ASM) ? twopi : 0.0;
+    double inv = 1.0 / dd;
     double in = x * ni.x + y * ni.y + z * ni.z;
     int pi = p.part[i];
     int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
     double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
-    if (m11) { PairVal v = far_pair(p.lp->k[m11 - 1], dd, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
-    if (m21) { PairVal v = far_pair(p.lp->k[m21 - 1], dd, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
-    if (m22) { PairVal v = far_pair(p.lp->k[m22 - 1], dd, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
-    if (m12) { PairVal v = far_pair(p.lp->k[m12 - 1], dd, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
+    if (m11) { PairVal v = far_pair(T, p.lp->k[m11 - 1], dd, inv, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
+    if (m21) { PairVal v = far_pair(T, p.lp->k[m21 - 1], dd, inv, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
+    if (m22) { PairVal v = far_pair(T, p.lp->k[m22 - 1], dd, inv, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
+    if (m12) { PairVal v = far_pair(T, p.lp->k[m12 - 1], dd, inv, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
     store4<W64, W32>(p, i, j, g1, h1, g2, h2);
   }
 }
@@ -162,6 +252,7 @@ void pack_sources(int n, const double* pos, const double* area, const double* nv
 
 mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st) {
   // algorithmic bytes: the four n x n outputs written once per precision
+  MNP_TRY(ensure_cis(st));
   const double nn = (double)p.n * p.n;
   ProfScope ps(PH_ASSEMBLE, st, 0.0, nn * 4.0 * ((w64 ? 16.0 : 0.0) + (w32 ? 8.0 : 0.0)),
                p.nref > 0 ? 2 : 1);
