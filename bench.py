@@ -35,6 +35,11 @@ METRIC = "wavelength-solves/s at N faces: mixed+batched vs FP64 GPU, ext err ≤
 UNIT = "wavelength-solves/s"
 DRUDE = (10.0, 9.065, 0.0708)
 NGRID = 60
+# DRAM bytes (read + write) of one full-size rank-256 Gauss-Jordan update of the
+# 4000-face workload, from one ncu capture (profiles/tc_gemm_rank256_update_sphere4000.md)
+TC_TRAFFIC_PER_LAUNCH = 152.7e6 + 67.5e6
+TC_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum of the full-size rank-256 update "
+                   "(4000 x 8000 x 512 real) from one ncu capture; algorithmic bytes of that launch 280 MB")
 
 
 def parse():
@@ -50,6 +55,11 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (default: workload)")
+    ap.add_argument("--workload", default="sphere4000", choices=["sphere4000", "batch3", "dimer24k"],
+                    help="sphere4000: the headline sweep; batch3: three particles of uneven size, 128 "
+                         "wavelengths, two polarisations; dimer24k: two 12000-face spheres, 32 wavelengths")
+    ap.add_argument("--fp64-faces", type=int, default=12000,
+                    help="dimer24k: total faces of the FP64 timing sample (scaled by n^3 to 24000)")
     return ap.parse_args()
 
 
@@ -276,25 +286,31 @@ def run_ours(a, rank, world, dist, torch):
     total = a.batch * a.steps * world
     value = total / (ms / 1e3)
     e2e_value = total / (e2e_ms / 1e3)
-    # ---------------- roofline of the dominant kernel class
-    dom = max((k for k in prof if k != "geometry"), key=lambda k: prof[k]["ms"])
+    # ---------------- roofline: the tensor-core GEMMs (the dominant kernel class
+    # in FLOPs and, with several wavelengths in flight, in device time; the
+    # pivot-block inversions run on one 8-CTA cluster each and overlap other
+    # wavelengths' GEMMs); every other kernel class is listed in phases_roofline
     hbm, bf16, src = peaks()
-    d = prof[dom]
     timing = ("CUDA events on the library stream around each launch, over a profiled repeat of "
-              "the %d timed steps" % a.steps)
-    if dom in ("gemm_n3",):
-        achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
-        roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": bf16,
-                "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": src + " bf16 dense",
-                "traffic": None, "launches": d["launches"], "ms": d["ms"], "timing": timing}
-    else:
-        achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
-        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": src, "traffic": None,
-                "launches": d["launches"], "ms": d["ms"], "timing": timing,
-                "flops_tflops": d["flops"] / (d["ms"] / 1e3) / 1e12 if d["flops"] else None}
+              "the %d timed steps (one wavelength in flight)" % a.steps)
+    d = prof["gemm_n3"]
+    achieved = d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0
+    roof = {"kernel": "k_tc_gemm (tcgen05 kind::tf32, all tensor-core GEMM launches)", "bound": "tensor",
+            "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+            "peak_source": src + " dense bf16 (TF32 runs at half the bf16 rate: frac of the TF32 rate = %.3f)"
+                           % (2 * achieved / bf16),
+            "traffic": TC_TRAFFIC_PER_LAUNCH, "traffic_note": TC_TRAFFIC_NOTE,
+            "launches": d["launches"], "ms": d["ms"], "timing": timing}
+    phases_roof = {}
+    for k, v in prof.items():
+        if v["ms"] <= 0 or k == "geometry":
+            continue
+        phases_roof[k] = {"ms": round(v["ms"], 3), "launches": v["launches"],
+                          "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["bytes"] else None,
+                          "hbm_frac": round(v["bytes"] / (v["ms"] / 1e3) / 1e9 / hbm, 4) if v["bytes"] else None,
+                          "TFLOP/s": round(v["flops"] / (v["ms"] / 1e3) / 1e12, 2) if v["flops"] else None}
     asm = prof["assembly"]
-    extra = {"phases_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+    extra = {"phases_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "phases_roofline": phases_roof,
              "assembly_hbm_gbs": asm["bytes"] / (asm["ms"] / 1e3) / 1e9 if asm["ms"] > 0 else None,
              "assembled_pairs_per_s": (n * n * a.batch * a.steps) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
              "refinement_iterations": iters.tolist()}
@@ -324,6 +340,111 @@ def fp64_comparison(a, cp, exc, torch, mixed_bem):
     err_sca = float(np.max(np.abs(rmx["sca"] - r64["sca"]) / np.abs(r64["sca"])))
     return {"value": 1.0 / t64, "unit": UNIT, "sample": "1 wavelength (600 nm), same workload",
             "ext_rel_err_mixed_vs_fp64": err_ext, "sca_rel_err_mixed_vs_fp64": err_sca}
+
+
+# ------------------------------------------------- secondary workloads
+def _timed(fn, torch):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def run_batch3(a, torch):
+    """Three particles of uneven size (sphere d = 30 nm / 1000 faces, capped rod
+    10 x 40 nm / 2500 quadrilaterals, cube 40 nm with 4 nm edge rounding / 2904
+    faces), 128 wavelengths 400-900 nm, x and y polarisation along +z, solved
+    together by mnpbem_solve_batch; one wavelength-solve = one particle at one
+    wavelength (both polarisations)."""
+    import mnpbem_gb300 as m
+    from mnpbem_gb300 import shapes
+    dev = torch.cuda.current_device()
+    geo = [shapes.fibsphere(1000, 30.0), shapes.trirod(10.0, 40.0, (51, 11, 31)),
+           shapes.tricube(23, 40.0, shapes.rounding_to_e(40.0, 4.0))]
+    exc = m.planewave([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]])
+    enei = np.linspace(400.0, 900.0, 128)
+
+    def solvers(prec, lanes):
+        out = []
+        for v, f in geo:
+            cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
+            out.append(m.bemsolver(cp, m.bemoptions(precision=prec, device=dev, lanes=lanes)))
+        return out
+    bems = solvers("mixed", a.lanes)
+    for _ in range(max(1, a.warmup)):
+        m.spectrum_batch([(b, exc, enei) for b in bems])
+    times = []
+    for _ in range(a.steps):
+        res, dt = _timed(lambda: m.spectrum_batch([(b, exc, enei) for b in bems]), torch)
+        times.append(dt)
+    nsol = len(bems) * enei.size
+    value = nsol * a.steps / sum(times)
+    # FP64 GPU on two wavelengths per particle, and the accuracy of the mixed results there
+    b64 = solvers("fp64", 1)
+    lam = enei[[20, 90]]
+    m.spectrum_batch([(b, exc, lam[:1]) for b in b64])
+    r64, t64 = _timed(lambda: m.spectrum_batch([(b, exc, lam) for b in b64]), torch)
+    idx = [20, 90]
+    err = max(float(np.max(np.abs(res[k]["ext"][idx] - r64[k]["ext"]) / np.abs(r64[k]["ext"]))) for k in range(3))
+    v64 = 3 * lam.size / t64
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64(tf32)+f64", "data": "synthetic",
+            "config": {"workload": "batch of 3 particles (sphere d=30 nm 1000 faces, capped rod 10x40 nm 2500 "
+                                   "quadrilaterals, rounded cube 40 nm / 4 nm rounding 2904 faces), Drude metal in "
+                                   "eps=1.77, x and y polarisation along +z, 128 wavelengths 400-900 nm per particle",
+                       "faces": [int(b.p.n) for b in bems], "wavelength_solves_per_step": nsol,
+                       "timing": "host wall clock around mnpbem_solve_batch (public API, ext/sca to host)"},
+            "fp64_gpu": {"value": v64, "unit": UNIT, "sample": "2 wavelengths x 3 particles, FP64 path"},
+            "speedup_vs_fp64_gpu": value / v64, "ext_rel_err_mixed_vs_fp64": err,
+            "refinement_iterations_max": int(max(int(r["ir_iters"].max()) for r in res))}
+
+
+def dimer_problem(faces_total, precision, dev, lanes):
+    import mnpbem_gb300 as m
+    from mnpbem_gb300 import shapes
+    nf = faces_total // 2
+    v1, f1 = shapes.fibsphere(nf, 50.0, center=(-26.0, 0.0, 0.0))
+    v2, f2 = shapes.fibsphere(nf, 50.0, center=(26.0, 0.0, 0.0))
+    cp = m.comparticle([m.epsconst(1.77), drude(), drude()], [m.particle(v1, f1), m.particle(v2, f2)],
+                       [[2, 1], [3, 1]], 1, 2)
+    return m.bemsolver(cp, m.bemoptions(precision=precision, device=dev, lanes=lanes))
+
+
+def run_dimer(a, torch):
+    """Two spheres d = 50 nm, 2 nm gap, 12000 faces each (separate media: G1
+    block-diagonal, factored as a full matrix), x-polarised along +z, 32
+    wavelengths 500-900 nm, mixed precision; the FP64 path is timed on one
+    wavelength of a dimer with --fp64-faces faces and scaled by n^3."""
+    import mnpbem_gb300 as m
+    dev = torch.cuda.current_device()
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    enei = np.linspace(500.0, 900.0, 32)
+    bem = dimer_problem(24000, "mixed", dev, a.lanes)
+    bem.spectrum(exc, enei[:max(1, a.lanes or 3)])        # warm-up: sizes and captures every lane
+    res, dt = _timed(lambda: bem.spectrum(exc, enei), torch)
+    value = enei.size / dt
+    b64 = dimer_problem(a.fp64_faces, "fp64", dev, 1)
+    b64.spectrum(exc, [700.0])
+    r64, t64 = _timed(lambda: b64.spectrum(exc, [700.0]), torch)
+    bmx = dimer_problem(a.fp64_faces, "mixed", dev, 1)
+    rmx = bmx.spectrum(exc, [700.0])
+    err = float(abs(rmx["ext"][0, 0] - r64["ext"][0, 0]) / abs(r64["ext"][0, 0]))
+    scale = (24000.0 / a.fp64_faces) ** 3
+    v64 = 1.0 / (t64 * scale)
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64(tf32)+f64", "data": "synthetic",
+            "config": {"workload": "dimer of two d=50 nm spheres, 2 nm gap, 2 x 12000 faces, Drude metal in "
+                                   "eps=1.77, x-pol along +z, 32 wavelengths 500-900 nm", "faces": 24000,
+                       "timing": "host wall clock around bemsolver.spectrum (public API, ext/sca to host)"},
+            "fp64_gpu": {"value": v64, "unit": UNIT,
+                         "sample": "1 wavelength (700 nm) of a %d-face dimer, %.3f s, scaled by (24000/%d)^3"
+                                   % (a.fp64_faces, t64, a.fp64_faces)},
+            "speedup_vs_fp64_gpu": value / v64,
+            "ext_rel_err_mixed_vs_fp64": err, "ext_err_sample": "%d-face dimer at 700 nm" % a.fp64_faces,
+            "refinement_iterations": res["ir_iters"].tolist()}
 
 
 # ---------------------------------------------------------- CPU / reference
@@ -410,6 +531,12 @@ def main():
             print(json.dumps(line))
         return
     import torch
+    if a.workload != "sphere4000":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        line = run_batch3(a, torch) if a.workload == "batch3" else run_dimer(a, torch)
+        if rank == 0:
+            print(json.dumps(line))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

@@ -134,6 +134,7 @@ struct mnpbem_geom {
   int64_t ld = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
   int lanes_req = 0;        // 0: automatic
+  int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -357,6 +358,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (env && env[0] == '0') G->tc_enabled = false;
   const char* genv = getenv("MNPBEM_GRAPHS");
   if (genv && genv[0] == '0') G->use_graphs = false;
+  const char* nbenv = getenv("MNPBEM_GJ_NB");
+  if (nbenv && atoi(nbenv) == 512) G->gj_nb = 512;
   const char* lenv = getenv("MNPBEM_LANES");
   if (lenv && atoi(lenv) > 0) G->lanes_req = std::min(MAX_LANES, atoi(lenv));
   *out = G;
@@ -723,7 +726,7 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   void* ctx = sizeof(R) == 4 ? tc_ctx(G, L) : nullptr;
   // wider Gauss-Jordan steps when the rank-nb updates run on tensor cores:
   // fewer passes over the n x n matrix (each step reads and writes it once)
-  gjw<R>(L).nb = (ctx && n >= 1024) ? 256 : 64;
+  gjw<R>(L).nb = (ctx && n >= 1024) ? G->gj_nb : 64;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
   const FaceData fd = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();

@@ -636,7 +636,9 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
     // pivot blocks wider than 64 are inverted by an inner Gauss-Jordan whose
     // pivot status this (outer) level clears now and reads at the end
     if (!w.inner) w.inner.reset(new GJWork<R>());
-    w.inner->nb = 64;
+    // complex64 with pivot blocks wider than 256: 256-wide inner steps whose
+    // own pivot blocks go to the cluster kernel; otherwise 64-wide steps
+    w.inner->nb = (sizeof(R) == 4 && nb > PB_W) ? PB_W : 64;
     w.inner->nested = true;
     MNP_TRY(w.inner->status.ensure(sizeof(int)));
     MNP_CUDA(cudaMemsetAsync(w.inner->status.ptr, 0, sizeof(int), st));
