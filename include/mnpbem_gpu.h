@@ -189,6 +189,16 @@ MNPBEM_API mnpbem_status mnpbem_ext_gradient(mnpbem_geom* g, const mnpbem_planew
                                              int32_t precision, double* ext, double* verts_grad,
                                              double* eps_grad);
 
+/* Same for the extinction (which = 0) or the scattering cross section
+ * (which = 1, scattering.m:14-31 over the sphere at infinity of exc, whose
+ * ninf must be > 0); value receives the cross section.  No counterpart in
+ * the reference.                                                             */
+MNPBEM_API mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* g, const mnpbem_planewave* exc,
+                                                       int32_t ipol, int32_t which, double enei,
+                                                       const double* eps_media, int32_t nmed,
+                                                       int32_t precision, double* value,
+                                                       double* verts_grad, double* eps_grad);
+
 /* The matrices bemret stores per wavelength (initmat.m:27-72), copied to host
  * as complex128 [n][n] (NULL to skip): G1i, G2i, Sigma1, Deltai, Sigmai.       */
 MNPBEM_API mnpbem_status mnpbem_bem_matrices(mnpbem_geom* g, double enei, const double* eps_media,

@@ -81,6 +81,10 @@ SIGNATURES = {
     "mnpbem_ext_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlaneWave), ctypes.c_int32,
                                            ctypes.c_double, c_double_p, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mnpbem_cross_section_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(PlaneWave), ctypes.c_int32,
+                                                     ctypes.c_int32, ctypes.c_double, c_double_p, ctypes.c_int32,
+                                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p]),
     "mnpbem_bem_matrices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p,
                                            ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 5),
     "mnpbem_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

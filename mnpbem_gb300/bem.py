@@ -274,16 +274,22 @@ class bemret:
         dext/deps)`` with ``dext/deps = dext/dRe(eps) + 1j dext/dIm(eps)`` of
         the medium inside the particle.  One closed particle excited from its
         outside medium; the refinement pattern is held fixed."""
+        return self.cross_section_gradient(exc, enei, ipol, "ext")
+
+    def cross_section_gradient(self, exc, enei, ipol=0, which="ext"):
+        """``which`` = 'ext' or 'sca': the cross section and its gradient
+        (see ``ext_gradient``); 'sca' integrates over ``exc``'s sphere at
+        infinity as ``scattering.m``."""
         em = np.ascontiguousarray(self._eps(float(enei))[0])
         pw = exc._struct()
-        ext = np.zeros(1)
+        val = np.zeros(1)
         gv = np.zeros((self.p.verts.shape[0], 3))
         ge = np.zeros(2)
-        _lib.check(self._lib.mnpbem_ext_gradient(
-            self._h, ctypes.byref(pw), int(ipol), float(enei),
+        _lib.check(self._lib.mnpbem_cross_section_gradient(
+            self._h, ctypes.byref(pw), int(ipol), {"ext": 0, "sca": 1}[which], float(enei),
             em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, _lib.FP64,
-            _lib.vptr(ext), _lib.vptr(gv), _lib.vptr(ge)))
-        return float(ext[0]), gv, complex(ge[0], ge[1])
+            _lib.vptr(val), _lib.vptr(gv), _lib.vptr(ge)))
+        return float(val[0]), gv, complex(ge[0], ge[1])
 
     def mldivide(self, exc):
         """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m)."""

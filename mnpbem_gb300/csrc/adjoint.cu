@@ -529,7 +529,7 @@ __global__ void k_adj_weights(AdjParams p, const double2* lphi, const double2* l
 // per face: J's far-field phase and area, the plane-wave excitation b, and
 // the explicit normals / eps1 of the alpha and De rows of afun.m
 // GX1 = G1 [sig1 h1] and GX2 = G2 [sig2 h2] as [n][4], HX1 = H1 sig1 [n]
-__global__ void k_adj_faces(AdjParams p, const double* pol, const double* dir, const double2* lphi,
+__global__ void k_adj_faces(AdjParams p, int which, const double* pol, const double* dir, const double2* lphi,
                             const double2* la, const double2* lDe, const double2* lal, const double2* GX1,
                             const double2* GX2, const double2* HX1, double* geps) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -545,14 +545,16 @@ __global__ void k_adj_faces(AdjParams p, const double* pol, const double* dir, c
   const double2 e1 = p.eps1[i], e2 = p.eps2[i];
   const double s = vdot(r, dv);
   if (p.exc_out[i]) {
-    // J = Re(ah . h2 + as sig2), Phi = exp(-i kb dir.r) A
-    const double2 Phi = cscl(cexpi(cscl(kb, -1.0), s), A);
-    const double2 kq = cdiv(cx(4.0 * M_PI * k0, 0.0), kb);
-    const double2 ph2 = cadd(cadd(cscl(X[5], pl.x), cscl(X[6], pl.y)), cscl(X[7], pl.z));
-    const double2 Jt = cadd(cmul(cmul(kq, Phi), ph2), cscl(cmul(Phi, X[4]), -4.0 * M_PI * vdot(pl, dv)));
-    const double2 dJr = cmul(imul(kb), Jt);   // i kb Jt; dJ/dr = Re(-i kb Jt) dir
-    gpos = vsub(gpos, vscale(dv, dJr.x));
-    garea += Jt.x / A;
+    if (which == 0) {
+      // ext: J = Re(ah . h2 + as sig2), Phi = exp(-i kb dir.r) A
+      const double2 Phi = cscl(cexpi(cscl(kb, -1.0), s), A);
+      const double2 kq = cdiv(cx(4.0 * M_PI * k0, 0.0), kb);
+      const double2 ph2 = cadd(cadd(cscl(X[5], pl.x), cscl(X[6], pl.y)), cscl(X[7], pl.z));
+      const double2 Jt = cadd(cmul(cmul(kq, Phi), ph2), cscl(cmul(Phi, X[4]), -4.0 * M_PI * vdot(pl, dv)));
+      const double2 dJr = cmul(imul(kb), Jt);   // i kb Jt; dJ/dr = Re(-i kb Jt) dir
+      gpos = vsub(gpos, vscale(dv, dJr.x));
+      garea += Jt.x / A;
+    }
     // excitation on the outside: a = e / (i k0) pol, De = -e2 (n.pol) e, alpha = (kb/k0)(n.dir) e pol
     const double2 ph = cexpi(kb, s);
     const double2 lap = cadd(cadd(cscl(la[3 * i], pl.x), cscl(la[3 * i + 1], pl.y)), cscl(la[3 * i + 2], pl.z));
@@ -669,6 +671,78 @@ __global__ void k_adj_rhs(AdjParams p, const double* pol, const double* dir, dou
   for (int c = 0; c < 3; ++c) gh2[3 * i + c] = h[c];
 }
 
+// right-hand side w = dJ/dx of the scattering cross section (scattering.m:14-31,
+// farfield.m:15-74) and its explicit dependence on the face positions and
+// areas through Phi_di = exp(-i k n_d . r_i) A_i, from the far fields e_d, h_d
+// of the forward solve on the sphere at infinity (directions n_d, weights
+// area_d, c_d = area_d / nb):
+//   g_h2_i  = sum_d c_d Phi_di [i k0 (h_d* x n_d) + i k ((n_d x e_d*) x n_d)]
+//   g_sig2_i = -i k sum_d c_d Phi_di n_d . (h_d* x n_d)
+__global__ void k_adj_rhs_sca(AdjParams p, const double2* fields, const double* inf_nvec, const double* inf_area,
+                              int ninf, int P, int ip, double nb, const double2* x2, double2* gs2, double2* gh2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  double2 s = cx(0, 0), h[3] = {cx(0, 0), cx(0, 0), cx(0, 0)};
+  double3 gpos = v3(0, 0, 0);
+  double garea = 0.0;
+  if (p.exc_out[i]) {
+    const double3 r = vld(p.pos, i);
+    const double A = p.area[i];
+    const double2 k = p.kb;
+    const double2 ik = imul(k), ik0 = cx(0.0, p.k0);
+    // forward sig2 and h2 of face i (polarisation ip); X[4..7] as in the weights
+    double2 X[8];
+    X[4] = x2[i * 4 * P + ip];
+    for (int c = 0; c < 3; ++c) X[5 + c] = x2[i * 4 * P + P + c * P + ip];
+    for (int q = 0; q < ninf; ++q) {
+      const int d = P + q;
+      const double3 nd = vld(inf_nvec, q);
+      const double c = inf_area[q] / nb;
+      double2 e[3], hh[3];
+      for (int cc = 0; cc < 3; ++cc) {
+        e[cc] = fields[((int64_t)d * 6 + cc) * P + ip];
+        hh[cc] = fields[((int64_t)d * 6 + 3 + cc) * P + ip];
+        hh[cc].y = -hh[cc].y;   // conj(h)
+        e[cc].y = -e[cc].y;     // conj(e)
+      }
+      const double nc[3] = {nd.x, nd.y, nd.z};
+      // A1 = h* x n ; B = n x e* ; A2 = B x n
+      double2 A1[3], B[3], A2[3];
+      for (int a = 0; a < 3; ++a) {
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        A1[a] = csub(cscl(hh[b1], nc[b2]), cscl(hh[b2], nc[b1]));
+        B[a] = csub(cscl(e[b2], nc[b1]), cscl(e[b1], nc[b2]));
+      }
+      for (int a = 0; a < 3; ++a) {
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        A2[a] = csub(cscl(B[b1], nc[b2]), cscl(B[b2], nc[b1]));
+      }
+      const double2 Phi = cscl(cexpi(cscl(k, -1.0), vdot(nd, r)), A);
+      const double2 cP = cscl(Phi, c);
+      double2 nA1 = cx(0, 0);
+      for (int a = 0; a < 3; ++a) {
+        h[a] = cadd(h[a], cmul(cP, cadd(cmul(ik0, A1[a]), cmul(ik, A2[a]))));
+        nA1 = cadd(nA1, cscl(A1[a], nc[a]));
+      }
+      s = csub(s, cmul(ik, cmul(cP, nA1)));
+      // explicit: T = Phi [A1 . (i k0 h2) - i k (n . A1) sig2 + B . (i k (n x h2))]
+      double2 T = csub(cx(0, 0), cmul(cmul(ik, nA1), X[4]));
+      for (int a = 0; a < 3; ++a) {
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        const double2 nxh = csub(cscl(X[5 + b2], nc[b1]), cscl(X[5 + b1], nc[b2]));
+        T = cadd(T, cadd(cmul(A1[a], cmul(ik0, X[5 + a])), cmul(B[a], cmul(ik, nxh))));
+      }
+      const double2 cT = cmul(cP, T);
+      gpos = vadd(gpos, vscale(nd, cmul(cscl(ik, -1.0), cT).x));
+      garea += cT.x / A;
+    }
+  }
+  gs2[i] = s;
+  for (int c = 0; c < 3; ++c) gh2[3 * i + c] = h[c];
+  vatomic(p.gpos, i, gpos);
+  atomicAdd(p.garea + i, garea);
+}
+
 // elementwise steps of the transposed chain (per face, P = 1):
 //   mode 0: gS2 += i k (L1 - L2) (n . t3)                 (after t3 = Di^T gH2')
 //   mode 1: v3 = i k (L1 - L2) n t                         (t = Si^T gS2)
@@ -709,6 +783,12 @@ void adj_rhs(const AdjParams& p, const double* pol, const double* dir, double2* 
   k_adj_rhs<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, pol, dir, gs2, gh2);
 }
 
+void adj_rhs_sca(const AdjParams& p, const double2* fields, const double* inf_nvec, const double* inf_area,
+                 int ninf, int P, int ip, double nb, const double2* x2, double2* gs2, double2* gh2, cudaStream_t st) {
+  k_adj_rhs_sca<<<(unsigned)cdiv_up(p.n, 64), 64, 0, st>>>(p, fields, inf_nvec, inf_area, ninf, P, ip, nb, x2, gs2,
+                                                           gh2);
+}
+
 void adj_chain_step(const AdjParams& p, int mode, const double2* a, const double2* b, double2* o1, double2* o2,
                     const double2* c, cudaStream_t st) {
   k_adj_chain<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, mode, a, b, o1, o2, c);
@@ -719,7 +799,7 @@ void adj_weights(const AdjParams& p, const double2* lphi, const double2* la, con
   k_adj_weights<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, lphi, la, lDe, lal, x1, x2, P, ip);
 }
 
-void adj_geometry(const AdjParams& p, const double* pol, const double* dir, const double2* lphi,
+void adj_geometry(const AdjParams& p, int which, const double* pol, const double* dir, const double2* lphi,
                   const double2* la, const double2* lDe, const double2* lal, const double2* GX1,
                   const double2* GX2, const double2* HX1, double* geps, cudaStream_t st) {
   ProfScope ps(PH_ASSEMBLE, st, 0.0, 0.0, 5);
@@ -727,7 +807,8 @@ void adj_geometry(const AdjParams& p, const double* pol, const double* dir, cons
   k_adj_pairs<<<g, PG_COLS, 0, st>>>(p);
   if (p.noff > 0) k_adj_near<<<(unsigned)cdiv_up(p.noff, 64), 64, 0, st>>>(p);
   k_adj_self<<<(unsigned)cdiv_up(p.n, 64), 64, 0, st>>>(p);
-  k_adj_faces<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, pol, dir, lphi, la, lDe, lal, GX1, GX2, HX1, geps);
+  k_adj_faces<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, which, pol, dir, lphi, la, lDe, lal, GX1, GX2, HX1,
+                                                           geps);
   k_adj_norm_flat<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p);
 }
 

@@ -44,14 +44,18 @@ struct AdjParams {
 };
 
 void adj_transpose(double2* A, int64_t n, int64_t ld, cudaStream_t st);
+// dJ/dx of ext (adj_rhs) or sca (adj_rhs_sca, which also adds the explicit
+// far-field terms of sca to the position / area accumulators)
 void adj_rhs(const AdjParams& p, const double* pol, const double* dir, double2* gs2, double2* gh2, cudaStream_t st);
+void adj_rhs_sca(const AdjParams& p, const double2* fields, const double* inf_nvec, const double* inf_area,
+                 int ninf, int P, int ip, double nb, const double2* x2, double2* gs2, double2* gh2, cudaStream_t st);
 // elementwise steps of the transposed bemret chain (see adjoint.cu)
 void adj_chain_step(const AdjParams& p, int mode, const double2* a, const double2* b, double2* o1, double2* o2,
                     const double2* c, cudaStream_t st);
 void adj_weights(const AdjParams& p, const double2* lphi, const double2* la, const double2* lDe,
                  const double2* lal, const double2* x1, const double2* x2, int P, int ip, cudaStream_t st);
-// all geometric contractions and the chain rule to the vertices
-void adj_geometry(const AdjParams& p, const double* pol, const double* dir, const double2* lphi,
+// all geometric contractions and the chain rule to the vertices (which: 0 ext, 1 sca)
+void adj_geometry(const AdjParams& p, int which, const double* pol, const double* dir, const double2* lphi,
                   const double2* la, const double2* lDe, const double2* lal, const double2* GX1,
                   const double2* GX2, const double2* HX1, double* geps, cudaStream_t st);
 

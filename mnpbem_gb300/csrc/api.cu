@@ -87,7 +87,7 @@ using namespace mnpbem;
 // sweep run concurrently: the latency-bound steps of one wavelength (pivot
 // blocks, panel products, refinement vectors) overlap the tensor-core
 // updates of the others.  Lane 0 runs on the handle's stream.
-constexpr int NSTAGES = 6;   // assemble, initmat, first solve, refine (DS), spectra, refine (FP32)
+constexpr int NSTAGES = 7;   // assemble, initmat, first solve, refine (DS), spectra, refine (FP32), refine (incremental)
 
 struct Lane {
   cudaStream_t st = nullptr;
@@ -113,7 +113,9 @@ struct Lane {
   enum { IDLE = 0, ITER, DONE } state = IDLE;
   int w = -1, iters = 0;
   double res = -1.0;
-  bool last_ds = false;      // the last refinement step used the double-single residual
+  int last_kind = 0;         // stage of the last refinement step
+  bool ds_done = false;      // a double-single residual has been computed for this wavelength
+  double bnorm2 = 0.0;       // ||b||^2 of the excitation (from the last full residual)
 };
 
 struct mnpbem_geom {
@@ -135,6 +137,7 @@ struct mnpbem_geom {
   std::vector<std::unique_ptr<Lane>> lanes;
   int lanes_req = 0;        // 0: automatic
   int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
+  bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -358,6 +361,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (env && env[0] == '0') G->tc_enabled = false;
   const char* genv = getenv("MNPBEM_GRAPHS");
   if (genv && genv[0] == '0') G->use_graphs = false;
+  const char* rnaenv = getenv("MNPBEM_TF32_RNA");
+  if (rnaenv && rnaenv[0] == '0') G->tf32_rna = false;
   const char* nbenv = getenv("MNPBEM_GJ_NB");
   if (nbenv && atoi(nbenv) == 512) G->gj_nb = 512;
   const char* lenv = getenv("MNPBEM_LANES");
@@ -571,7 +576,7 @@ size_t lane_bytes_estimate(const mnpbem_geom* G, int precision, int P, int ninf)
   const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
   size_t b = 5 * es * n * ld;
   if (precision == MNPBEM_MIXED) b += 4 * 2 * sizeof(float2) * n * ld + 16 * n * n;  // planes + B' of the n^3 GEMMs
-  b += sizeof(double2) * n * P * 72 + sizeof(float2) * n * P * 56;
+  b += sizeof(double2) * n * P * 80 + sizeof(float2) * n * P * 56;
   b += 3 * es * n * 256 + sizeof(double2) * (size_t)(P + ninf) * 6 * P + 64 * n;
   return b;
 }
@@ -583,7 +588,7 @@ mnpbem_status ensure_workspace(mnpbem_geom* G, Lane& L, int precision, int P, in
   if (precision == MNPBEM_MIXED)
     for (int q = 0; q < 4; ++q) MNP_TRY(L.mat64[q].ensure(2 * sizeof(float2) * n * ld));
   // FP64 vectors: b (8nP) x (8nP) r (8nP) YZ (16nP) + chain work for FP64 (32nP)
-  MNP_TRY(L.vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32)));
+  MNP_TRY(L.vec64.ensure(sizeof(double2) * n * P * (8 + 8 + 8 + 16 + 32 + 8)));
   // working-precision vectors for MIXED: in (8nP) out (8nP) work (32nP)
   MNP_TRY(L.vecw.ensure(sizeof(float2) * n * P * (8 + 8 + 32)));
   MNP_TRY(L.norms.ensure(sizeof(double) * 4));
@@ -727,13 +732,19 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   // wider Gauss-Jordan steps when the rank-nb updates run on tensor cores:
   // fewer passes over the n x n matrix (each step reads and writes it once)
   gjw<R>(L).nb = (ctx && n >= 1024) ? G->gj_nb : 64;
+  gjw<R>(L).round_a = G->tf32_rna;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
   const FaceData fd = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();
   // G1i, G2i
   MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
   MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
-  // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2
+  // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2 (H1, H2 are read only here:
+  // round them to TF32 for the tensor cores)
+  if (sizeof(R) == 4 && ctx && gjw<R>(L).round_a) {
+    round_tf32(reinterpret_cast<float*>(M[2]), 2 * n * ld, L.st);
+    round_tf32(reinterpret_cast<float*>(M[3]), 2 * n * ld, L.st);
+  }
   MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, L.st, ctx));
   MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, L.st, ctx));
   // Delta -> M3, Sigma (partial) -> M2
@@ -749,7 +760,7 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
 
 // FP64 vector arena layout
 struct Vec64 {
-  double2 *phi, *a, *alpha, *De, *x1, *x2, *rphi, *ra, *ral, *rDe, *Y1, *Y2, *Z1, *Z2, *work;
+  double2 *phi, *a, *alpha, *De, *x1, *x2, *rphi, *ra, *ral, *rDe, *Y1, *Y2, *Z1, *Z2, *work, *d1, *d2;
 };
 Vec64 vec64(const mnpbem_geom* G, Lane& L, int P) {
   const int64_t n = G->g.n;
@@ -760,6 +771,8 @@ Vec64 vec64(const mnpbem_geom* G, Lane& L, int P) {
   v.rphi = v.x2 + 4 * n * P; v.ra = v.rphi + n * P; v.ral = v.ra + 3 * n * P; v.rDe = v.ral + 3 * n * P;
   v.Y1 = v.rDe + n * P; v.Y2 = v.Y1 + 4 * n * P; v.Z1 = v.Y2 + 4 * n * P; v.Z2 = v.Z1 + 4 * n * P;
   v.work = v.Z2 + 4 * n * P;
+  v.d1 = v.work + 32 * n * P;   // last correction in FP64 (incremental residual)
+  v.d2 = v.d1 + 4 * n * P;
   return v;
 }
 
@@ -837,6 +850,40 @@ mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c, bool ds) {
   return MNPBEM_OK;
 }
 
+// ---------------------------------------------------------------- S6
+// incremental refinement step: r <- r - A dx with the last correction dx and
+// FP32 products of the hi planes (their rounding, ~1e-7 of |A| |dx|, shrinks
+// with dx), then the complex64 chain and x += dx'.  Used after the first full
+// residual; one double-single residual in between anchors the accuracy.
+mnpbem_status stage_incr(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
+  const int64_t n = G->g.n;
+  const int P = c.P;
+  cudaStream_t st = L.st;
+  Vec64 v = vec64(G, L, P);
+  const int64_t ld = G->ld;
+  const float2* hl[4];
+  for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
+  double* norms = L.norms.as<double>();
+  launch_cvt_f2d(fx_ptr(G, L, P, 0), v.d1, 4 * n * P, st);
+  launch_cvt_f2d(fx_ptr(G, L, P, 1), v.d2, 4 * n * P, st);
+  MNP_CHECK_LAUNCH();
+  float2* bs = L.bsplit.as<float2>();
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], nullptr, ld, v.d1, 4 * P, v.Y1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], nullptr, ld, v.d1, 4 * P, v.Z1, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], nullptr, ld, v.d2, 4 * P, v.Y2, 4 * P, bs, st));
+  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], nullptr, ld, v.d2, 4 * P, v.Z2, 4 * P, bs, st));
+  MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
+  // in place: the residual kernel reads each entry of r before writing it
+  launch_residual(face_data(G, L), P, L.lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, v.rphi, v.ra, v.ral,
+                  v.rDe, v.rphi, v.ra, v.ral, v.rDe, norms, st);
+  MNP_CHECK_LAUNCH();
+  MNP_TRY(apply32(G, L, P, v.rphi, v.ra, v.ral, v.rDe));
+  launch_axpy_norm(v.x1, fx_ptr(G, L, P, 0), 4 * n * P, norms + 2, st);
+  launch_axpy_norm(v.x2, fx_ptr(G, L, P, 1), 4 * n * P, norms + 2, st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 // ---------------------------------------------------------------- S4
 mnpbem_status stage_spectra(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const int P = c.P;
@@ -863,6 +910,7 @@ mnpbem_status run_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage, b
     case 2: return stage_first(G, L, c);
     case 3: return stage_iter(G, L, c, true);
     case 5: return stage_iter(G, L, c, false);
+    case 6: return stage_incr(G, L, c);
     default: return stage_spectra(G, L, c);
   }
 }
@@ -945,13 +993,38 @@ struct Refine {
   double tol;
 };
 
-// residual precision of the next refinement step: FP32 while the last
-// relative residual is above 1e-3 (the FP32 rounding of the products,
-// ~1e-6 of |A| |x|, is then far below what the step resolves), double-single
-// afterwards.  The first step always starts in FP32.
-constexpr double DS_SWITCH = 1e-3;
-bool next_ds(const Lane& L) { return L.iters > 0 && L.res <= DS_SWITCH; }
-int iter_stage(bool ds) { return ds ? 3 : 5; }
+// Refinement schedule of one wavelength (stages 3, 5, 6):
+//   step 1      full residual b - A x with FP32 products of the hi planes (5)
+//   then        incremental residuals r - A dx, FP32 products (6)
+//   once        a full double-single residual (3), when the relative residual
+//               is below 1e-5 or after three steps: it removes the FP32
+//               rounding of the first residual (~1e-7 of |A| |x|)
+//   then        incremental residuals again, whose rounding (~1e-7 of |A| |dx|)
+//               is far below the 1e-10 tolerance once dx is small.
+// The stopping test (||dx|| <= tol ||x||) counts only after the double-single
+// residual.  Relative residuals are measured against ||b|| of the last full one.
+constexpr double DS_SWITCH = 1e-5;
+constexpr int STEP_DS = 3, STEP_FP32 = 5, STEP_INCR = 6;
+int next_step(const Lane& L) {
+  if (L.iters == 0) return STEP_FP32;
+  if (!L.ds_done && (L.res <= DS_SWITCH || L.iters >= 3)) return STEP_DS;
+  return STEP_INCR;
+}
+void step_done(Lane& L, int kind, const double* hn) {
+  if (kind != STEP_INCR) L.bnorm2 = hn[1];
+  if (kind == STEP_DS) L.ds_done = true;
+  L.res = L.bnorm2 > 0 ? sqrt(hn[0] / L.bnorm2) : 0.0;
+  ++L.iters;
+}
+bool step_converged(const Lane& L, const double* hn, double tol) {
+  return L.ds_done && sqrt(hn[2]) <= tol * sqrt(hn[3]);
+}
+void refine_reset(Lane& L) {
+  L.iters = 0;
+  L.res = -1.0;
+  L.ds_done = false;
+  L.bnorm2 = 0.0;
+}
 
 // one wavelength through all stages, synchronously (graphs == true replays
 // captured stages; false runs the stages directly and sizes the buffers)
@@ -965,21 +1038,19 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
   double final_res = -1.0;
   if (c.precision == MNPBEM_MIXED) {
     double* hn = L.norms_host;
-    L.iters = 0;
-    L.res = -1.0;
+    refine_reset(L);
     for (int it = 0; it < ref.maxit; ++it) {
-      const bool ds = next_ds(L);
-      MNP_TRY(launch_stage(G, L, c, iter_stage(ds), graphs));
+      const int kind = next_step(L);
+      MNP_TRY(launch_stage(G, L, c, kind, graphs));
       MNP_CUDA(cudaMemcpyAsync(hn, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       MNP_CUDA(cudaStreamSynchronize(st));
       G->prof.flush();
       MNP_TRY(check_pivots(L));
-      used = it + 1;
-      L.iters = used;
-      final_res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
-      L.res = final_res;
+      step_done(L, kind, hn);
+      used = L.iters;
+      final_res = L.res;
       if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-      if (ds && sqrt(hn[2]) <= ref.tol * sqrt(hn[3])) break;
+      if (step_converged(L, hn, ref.tol)) break;
     }
   }
   MNP_TRY(launch_stage(G, L, c, 4, graphs));
@@ -1062,8 +1133,8 @@ mnpbem_status write_outputs(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sw
 }
 
 mnpbem_status queue_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
-  L.last_ds = next_ds(L);
-  MNP_TRY(launch_stage(G, L, c, iter_stage(L.last_ds), true));
+  L.last_kind = next_step(L);
+  MNP_TRY(launch_stage(G, L, c, L.last_kind, true));
   MNP_CUDA(cudaMemcpyAsync(L.norms_host, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
   MNP_CUDA(cudaEventRecord(L.ev, L.st));
   L.state = Lane::ITER;
@@ -1080,8 +1151,7 @@ mnpbem_status queue_finish(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
 // queue wavelength w on a lane with captured graphs (returns without waiting)
 mnpbem_status lane_start(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s, int w) {
   L.w = w;
-  L.iters = 0;
-  L.res = -1.0;
+  refine_reset(L);
   MNP_TRY(upload_lp(G, L, s, w));
   for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, L, c, stage, true));
   MNP_TRY(status_copy(L, c.precision));
@@ -1095,11 +1165,9 @@ mnpbem_status lane_advance(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Swe
   MNP_TRY(check_pivots(L));
   if (L.state == Lane::ITER) {
     const double* hn = L.norms_host;
-    ++L.iters;
-    L.res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
+    step_done(L, L.last_kind, hn);
     if (!(hn[2] == hn[2])) { set_error("refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
-    if ((L.last_ds && sqrt(hn[2]) <= s.ref.tol * sqrt(hn[3])) || L.iters >= s.ref.maxit)
-      return queue_finish(G, L, c);
+    if (step_converged(L, hn, s.ref.tol) || L.iters >= s.ref.maxit) return queue_finish(G, L, c);
     return queue_iter(G, L, c);
   }
   // DONE: results of L.w are in the lane; the stream is idle, so host-side
@@ -1255,7 +1323,7 @@ mnpbem_status job_prepare(Job& j) {
     Lane& L = *G->lanes[l];
     bool ok = true;
     for (int stage = 0; stage < NSTAGES && ok; ++stage) {
-      if ((stage == 3 || stage == 5) && c.precision != MNPBEM_MIXED) continue;
+      if ((stage == 3 || stage == 5 || stage == 6) && c.precision != MNPBEM_MIXED) continue;
       ok = capture_stage(G, L, c, stage) == MNPBEM_OK;
     }
     if (ok) {
@@ -1425,9 +1493,18 @@ mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs_in, int32_t njobs, int32
 mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t ipol, double enei,
                                   const double* eps_media, int32_t nmed, int32_t precision, double* ext,
                                   double* verts_grad, double* eps_grad) {
+  return mnpbem_cross_section_gradient(G, exc, ipol, 0, enei, eps_media, nmed, precision, ext, verts_grad,
+                                       eps_grad);
+}
+
+mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, int32_t ipol,
+                                            int32_t which, double enei, const double* eps_media, int32_t nmed,
+                                            int32_t precision, double* value, double* verts_grad,
+                                            double* eps_grad) {
   MNP_TRY(check_geom(G));
-  if (!exc || ipol < 0 || ipol >= exc->npol || !verts_grad || !eps_grad) {
-    set_error("mnpbem_ext_gradient: invalid arguments");
+  if (!exc || ipol < 0 || ipol >= exc->npol || !verts_grad || !eps_grad || (which != 0 && which != 1) ||
+      (which == 1 && exc->ninf <= 0)) {
+    set_error("mnpbem_cross_section_gradient: invalid arguments");
     return MNPBEM_ERR_INVALID_ARG;
   }
   if (precision != MNPBEM_FP64) {
@@ -1438,9 +1515,10 @@ mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, i
     set_error("mnpbem_ext_gradient: one closed particle excited from its outside medium is required");
     return MNPBEM_ERR_UNSUPPORTED;
   }
-  double sol_ext[4] = {0, 0, 0, 0};
+  double sol_ext[4] = {0, 0, 0, 0}, sol_sca[4] = {0, 0, 0, 0};
   mnpbem_solution sol{};
   sol.ext = sol_ext;
+  sol.sca = sol_sca;
   MNP_TRY(validate_job(G, exc, 1, &enei, eps_media, nmed, precision, &sol));
   MNP_CUDA(cudaSetDevice(G->device));
   ProfBind pb_(&G->prof);
@@ -1456,7 +1534,7 @@ mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, i
   MNP_TRY(solve_one(G, L, j.c, j.s.ref, false, &L.iters, &L.res));
   MNP_TRY(write_outputs(G, L, j.c, j.s, 0));
   MNP_CUDA(cudaStreamSynchronize(st));
-  if (ext) *ext = sol_ext[ipol];
+  if (value) *value = which == 0 ? sol_ext[ipol] : sol_sca[ipol];
   const int64_t n = G->g.n, ld = G->ld, nv = G->nverts;
   const int P = exc->npol;
   // refined off-diagonal entries (once per geometry)
@@ -1511,7 +1589,14 @@ mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, i
     adj_transpose(M[q], n, ld, st);   // G1i, G2i, Sigmai, Deltai, Sigma1 -> transposes
   }
   MNP_CHECK_LAUNCH();
-  adj_rhs(p, pol_d, dir_d, gs2, gh2, st);
+  if (which == 0) {
+    adj_rhs(p, pol_d, dir_d, gs2, gh2, st);
+  } else {
+    const double* inf_nvec = G->exbuf.as<double>() + 6 * P;
+    const double* inf_area = inf_nvec + 3 * exc->ninf;
+    adj_rhs_sca(p, L.fields.as<double2>(), inf_nvec, inf_area, exc->ninf, P, ipol, lp.nb1.x, vec64(G, L, P).x2,
+                gs2, gh2, st);
+  }
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   MNP_TRY(gemm_simt<double>(n, 1, n, one, M[1], ld, gs2, 1, zero, gS2, 1, st));     // G2i^T w_sig2
   MNP_TRY(gemm_simt<double>(n, 3, n, one, M[1], ld, gh2, 3, zero, gH2p, 3, st));    // G2i^T w_h2
@@ -1539,7 +1624,7 @@ mnpbem_status mnpbem_ext_gradient(mnpbem_geom* G, const mnpbem_planewave* exc, i
     MNP_TRY(gemm_simt<double>(n, 1, n, one, ap.H1, ld, Xb, 8, zero, HX1, 1, st));
   }
   // ---- geometric contractions and the chain rule to the vertices
-  adj_geometry(p, pol_d, dir_d, gphi, ga, gDe, gAl, GX1, GX2, HX1, geps, st);
+  adj_geometry(p, which, pol_d, dir_d, gphi, ga, gDe, gAl, GX1, GX2, HX1, geps, st);
   MNP_CHECK_LAUNCH();
   MNP_CUDA(cudaMemcpyAsync(verts_grad, p.gv, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, st));
   double hk[4];

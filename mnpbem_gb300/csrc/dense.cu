@@ -140,6 +140,83 @@ __global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin(int64_t M, int64_
   }
 }
 
+// complex64 variant with 16-byte loads: each lane takes two consecutive k
+// (one float4 of A per row, two rows of B), halving the load instructions of
+// the matrix stream.  Needs lda even and A 16-byte aligned; an odd K leaves
+// one k that warp 0 adds at the end.
+template <int N, int TR>
+__global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin_c64(int64_t M, int64_t K, float2 alpha,
+                                                                 const float2* __restrict__ A, int64_t lda,
+                                                                 const float2* __restrict__ B, int64_t ldb,
+                                                                 float2 beta, float2* __restrict__ C,
+                                                                 int64_t ldc) {
+  __shared__ float2 red[THIN_WARPS][TR][N];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = (int64_t)blockIdx.x * TR;
+  const int64_t KP = K >> 1;   // pairs
+  const int64_t kw = (KP + THIN_WARPS - 1) / THIN_WARPS;
+  const int64_t pbeg = warp * kw, pend = min(KP, pbeg + kw);
+  const float2* arow[TR];
+#pragma unroll
+  for (int r = 0; r < TR; ++r) arow[r] = A + min(row0 + r, M - 1) * lda;
+  float2 acc[TR][N];
+#pragma unroll
+  for (int r = 0; r < TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) acc[r][c] = make_float2(0.f, 0.f);
+#pragma unroll 2
+  for (int64_t kp = pbeg + lane; kp < pend; kp += 32) {
+    const int64_t k = 2 * kp;
+    float2 b0[N], b1[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      b0[c] = __ldg(B + k * ldb + c);
+      b1[c] = __ldg(B + (k + 1) * ldb + c);
+    }
+#pragma unroll
+    for (int r = 0; r < TR; ++r) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(arow[r] + k));
+      const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        cfma(acc[r][c], a0, b0[c]);
+        cfma(acc[r][c], a1, b1[c]);
+      }
+    }
+  }
+  if ((K & 1) && warp == 0 && lane == 0) {
+    const int64_t k = K - 1;
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+      for (int c = 0; c < N; ++c) cfma(acc[r][c], arow[r][k], B[k * ldb + c]);
+  }
+#pragma unroll
+  for (int r = 0; r < TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      float2 v = acc[r][c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[warp][r][c] = v;
+    }
+  __syncthreads();
+  const bool zero_beta = (beta.x == 0 && beta.y == 0);
+  for (int t = threadIdx.x; t < TR * N; t += blockDim.x) {
+    const int r = t / N, c = t % N;
+    const int64_t row = row0 + r;
+    if (row >= M) continue;
+    float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int w = 0; w < THIN_WARPS; ++w) v = cadd(v, red[w][r][c]);
+    float2 out = cmul(alpha, v);
+    if (!zero_beta) out = cadd(out, cmul(beta, C[row * ldc + c]));
+    C[row * ldc + c] = out;
+  }
+}
+
 // ------------------------------------------- double-single thin GEMM (N <= 16)
 // Error-free transformations (Dekker / Knuth): the product a*b = p + e exactly
 // with p = fl(a*b), e = fma(a, b, -p); the sum s + p = t + err exactly with
@@ -178,25 +255,26 @@ __global__ void k_split_hi_lo(const double2* __restrict__ B, int64_t count, floa
   lo[i] = make_float2((float)(b.x - (double)h.x), (float)(b.y - (double)h.y));
 }
 
-template <int N>
+template <int N, int TR, int UNR>
 __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64_t K, const float2* __restrict__ Ahi,
                                                               const float2* __restrict__ Alo, int64_t lda,
                                                               const float2* __restrict__ Bh,
                                                               const float2* __restrict__ Bl, int64_t ldb,
                                                               double2* __restrict__ C, int64_t ldc) {
-  __shared__ DS red[DS_WARPS][DS_TR][N][2];
+  __shared__ DS red[DS_WARPS][TR][N][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row0 = (int64_t)blockIdx.x * DS_TR;
+  const int64_t row0 = (int64_t)blockIdx.x * TR;
   const int64_t kw = (K + DS_WARPS - 1) / DS_WARPS;
   const int64_t kbeg = warp * kw, kend = min(K, kbeg + kw);
-  int64_t roff[DS_TR];
+  int64_t roff[TR];
 #pragma unroll
-  for (int r = 0; r < DS_TR; ++r) roff[r] = min(row0 + r, M - 1) * lda;
-  DS re[DS_TR][N], im[DS_TR][N];
+  for (int r = 0; r < TR; ++r) roff[r] = min(row0 + r, M - 1) * lda;
+  DS re[TR][N], im[TR][N];
 #pragma unroll
-  for (int r = 0; r < DS_TR; ++r)
+  for (int r = 0; r < TR; ++r)
 #pragma unroll
     for (int c = 0; c < N; ++c) re[r][c] = im[r][c] = DS{0.f, 0.f};
+#pragma unroll UNR
   for (int64_t k = kbeg + lane; k < kend; k += 32) {
     float2 xh[N], xl[N];
 #pragma unroll
@@ -205,7 +283,7 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64
       xl[c] = __ldg(Bl + k * ldb + c);
     }
 #pragma unroll
-    for (int r = 0; r < DS_TR; ++r) {
+    for (int r = 0; r < TR; ++r) {
       const float2 ah = __ldg(Ahi + roff[r] + k), al = __ldg(Alo + roff[r] + k);
 #pragma unroll
       for (int c = 0; c < N; ++c) {
@@ -220,7 +298,7 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64
     }
   }
 #pragma unroll
-  for (int r = 0; r < DS_TR; ++r)
+  for (int r = 0; r < TR; ++r)
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       DS a = re[r][c], b = im[r][c];
@@ -233,7 +311,7 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_ds(int64_t M, int64
       if (lane == 0) { red[warp][r][c][0] = a; red[warp][r][c][1] = b; }
     }
   __syncthreads();
-  for (int t = threadIdx.x; t < DS_TR * N; t += blockDim.x) {
+  for (int t = threadIdx.x; t < TR * N; t += blockDim.x) {
     const int r = t / N, c = t % N;
     const int64_t row = row0 + r;
     if (row >= M) continue;
@@ -328,9 +406,13 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
     return MNPBEM_OK;
   }
   ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 16.0 * M * K + 16.0 * K * N + 16.0 * M * N);
-#define DS_CASE(NN)                                                                                   \
-  case NN:                                                                                            \
-    k_gemm_thin_ds<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, Alo, lda, Bh, Bl, N, C, ldc);     \
+  // two rows per block (80 registers, 3 blocks per SM) measured faster than
+  // four rows (128 registers) or an unrolled k loop
+  constexpr int TR = 2;
+  const unsigned nb2 = (unsigned)cdiv_up(M, (int64_t)TR);
+#define DS_CASE(NN)                                                                                        \
+  case NN:                                                                                                 \
+    k_gemm_thin_ds<NN, TR, 1><<<nb2, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, Alo, lda, Bh, Bl, N, C, ldc);       \
     break;
   switch (N) {
     DS_CASE(1) DS_CASE(2) DS_CASE(3) DS_CASE(4) DS_CASE(5) DS_CASE(6) DS_CASE(7) DS_CASE(8)
@@ -345,6 +427,24 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
                         int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta, cplx<R>* C,
                         int64_t ldc, cudaStream_t st) {
   if (M <= 0 || N <= 0) return MNPBEM_OK;
+  if (sizeof(R) == 4 && N <= 8 && K > 1 && !(lda & 1) && !(reinterpret_cast<uintptr_t>(A) & 15)) {
+    ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K,
+                 (double)sizeof(cplx<R>) * ((double)M * K + (double)K * N + 2.0 * M * N));
+    const float2* Af = reinterpret_cast<const float2*>(A);
+    const float2* Bf = reinterpret_cast<const float2*>(B);
+    float2* Cf = reinterpret_cast<float2*>(C);
+    const float2 al = make_float2((float)alpha.x, (float)alpha.y), be = make_float2((float)beta.x, (float)beta.y);
+#define C64_CASE(NN)                                                                                    \
+  case NN:                                                                                              \
+    k_gemm_thin_c64<NN, 4><<<(unsigned)cdiv_up(M, 4), 32 * THIN_WARPS, 0, st>>>(M, K, al, Af, lda, Bf, ldb, be, Cf, ldc); \
+    break;
+    switch (N) {
+      C64_CASE(1) C64_CASE(2) C64_CASE(3) C64_CASE(4) C64_CASE(5) C64_CASE(6) C64_CASE(7) C64_CASE(8)
+    }
+#undef C64_CASE
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
   if (N <= THIN_NMAX && K > 0) {
     ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  (double)sizeof(cplx<R>) * ((double)M * K + (double)K * N + 2.0 * M * N));
@@ -608,6 +708,25 @@ static mnpbem_status launch_block_inv_cluster(const float2* A, int64_t lda, int 
   return MNPBEM_OK;
 }
 
+// ------------------------------------------------ TF32 rounding in place
+// The tensor cores read an FP32 operand as TF32 by dropping its 13 low
+// mantissa bits (truncation, biased towards zero); operands rounded to nearest
+// beforehand (cvt.rna.tf32) carry half the error and no bias.  The B operand
+// is rounded when it is expanded; this rounds an A operand.
+__global__ void k_round_tf32(float* x, int64_t count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x[i]));
+  x[i] = __uint_as_float(r);
+}
+
+void round_tf32(float* x, int64_t count, cudaStream_t st) {
+  if (count <= 0) return;
+  ProfScope ps(PH_ELEMWISE, st, 0.0, 8.0 * count, 1);
+  k_round_tf32<<<(unsigned)cdiv_up(count, 256), 256, 0, st>>>(x, count);
+}
+
 // --------------------------------------------------- blocked Gauss-Jordan
 template <typename R>
 mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st) {
@@ -669,6 +788,10 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
     MNP_TRY(big_gemm(bw, n, bw, one, X, bw, A + k0 * lda, lda, zero, Rrow, n, st, ctx));
     MNP_CUDA(cudaMemset2DAsync(Rrow + k0, cs * n, 0, cs * bw, bw, st));
     // 4. new column block <- -Ccol * X, then zero Ccol's k-block rows
+    //    (on the tensor-core path Ccol, the A operand of this product and of
+    //    the rank update, is first rounded to TF32; the pivot block it holds
+    //    has already been inverted in full FP32)
+    if (sizeof(R) == 4 && ctx && w.round_a) round_tf32(reinterpret_cast<float*>(Ccol), 2 * n * bw, st);
     MNP_TRY(big_gemm(n, bw, bw, mone, Ccol, bw, X, bw, zero, Ncol, bw, st, ctx));
     MNP_CUDA(cudaMemsetAsync(Ccol + k0 * bw, 0, cs * bw * bw, st));
     // 5. A <- A - Ccol * R  (rank-bw update of the whole matrix)

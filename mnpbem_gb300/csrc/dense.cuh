@@ -21,12 +21,16 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
                            float2* bsplit, cudaStream_t st);
 
+// x <- TF32(x) rounded to nearest, in place (count floats)
+void round_tf32(float* x, int64_t count, cudaStream_t st);
+
 // Workspace for in-place inversion of an n x n matrix by blocked Gauss-Jordan
 // elimination without row interchanges.
 template <typename R>
 struct GJWork {
   DevBuf ccol, rrow, ncol, xblk, status;
   int nb = 64;
+  bool round_a = true;               // round the A operand of the tensor-core updates to TF32 (nearest)
   bool nested = false;               // inner level: the outer level reads the pivot status
   std::unique_ptr<GJWork<R>> inner;  // Gauss-Jordan of pivot blocks wider than 64
 };

@@ -208,15 +208,52 @@ def _fact(o):
 def ext_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, order=5, check_chain=False):
     """Adjoint gradient of ext: returns (J, dJ/dverts [nv, 3], dJ/deps_in as
     dJ/dRe(eps) + i dJ/dIm(eps), dict of intermediate pieces)."""
+    return cross_section_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, "ext", None, order,
+                                  check_chain)
+
+
+def sca_rhs(cp, sig, pw, enei):
+    """dJ/dx of the scattering cross section (scattering.m:14-31 with the far
+    fields of farfield.m:15-74): J = sum_d c_d Re(n_d . (e_d x conj(h_d))),
+    c_d = area_d / nb, e_d = sum_i Phi_di (i k0 h2_i - i k dir_d sig2_i),
+    h_d = sum_i Phi_di i k dir_d x h2_i, Phi_di = exp(-i k dir_d . r_i) A_i.
+    dJ = Re(g . dx) with g_h2_i = sum_d c_d Phi_di [i k0 (h_d* x n_d)
+    + i k ((n_d x e_d*) x dir_d)], g_sig2_i = -i k sum_d c_d Phi_di dir_d . (h_d* x n_d).
+    Returns (g_sig2, g_h2, dJ/dpos explicit, dJ/darea explicit)."""
+    pinf = pw.pinfty
+    dirs, ad = pinf.nvec, pinf.area
+    e, h, k = pw.farfield(cp, sig, dirs)
+    e, h = e[:, :, 0], h[:, :, 0]
+    k0 = 2 * np.pi / enei
+    nb = np.sqrt(cp.eps[0](enei)[0])
+    c = ad / nb
+    pos, area = cp.pos, cp.area
+    Phi = np.exp(-1j * k * dirs @ pos.T) * area[None, :]          # [d, i]
+    A1 = np.cross(np.conj(h), dirs)                              # h* x n
+    A2 = np.cross(np.cross(dirs, np.conj(e)), dirs)              # (n x e*) x dir
+    gh2 = np.einsum("d,di,dk->ik", c, Phi, 1j * k0 * A1 + 1j * k * A2)
+    gs2 = -1j * k * np.einsum("d,di,d->i", c, Phi, np.sum(dirs * A1, 1))
+    s2, h2 = sig["sig2"][:, 0], sig["h2"][:, :, 0]
+    # explicit: Phi depends on r_i (phase) and A_i
+    T = Phi * (np.einsum("dk,ik->di", A1, 1j * k0 * h2) - 1j * k * np.sum(dirs * A1, 1)[:, None] * s2[None, :]
+               + np.einsum("dk,dik->di", np.cross(dirs, np.conj(e)), 1j * k * np.cross(dirs[:, None, :], h2[None, :, :])))
+    gpos = np.real(np.einsum("d,di,dk->ik", c * (-1j * k), T, dirs))
+    garea = np.real(np.einsum("d,di->i", c, T)) / area
+    return gs2, gh2, gpos, garea
+
+
+def cross_section_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, which="ext", pinfty=None,
+                           order=5, check_chain=False):
+    """Adjoint gradient of ext or sca (one polarisation): returns (J, dJ/dverts
+    [nv, 3], dJ/dRe(eps) + i dJ/dIm(eps) of the inside medium, intermediates)."""
     cp, bem = make_problem(verts, faces, quad, eps_out, eps_in, None, order)
     p = cp.pc
     n = cp.n
     pol = np.asarray(pol, dtype=float)
     dirv = np.asarray(dirv, dtype=float)
-    pw = R.PlaneWaveRet([pol], [dirv], None)
+    pw = R.PlaneWaveRet([pol], [dirv], pinfty)
     exc = pw.potential(cp, enei)
     sig = bem.solve(exc)
-    J = float(pw.extinction(cp, sig)[0])
     k0 = 2 * np.pi / enei
     kb = cp.eps[0](enei)[1]
     k1 = cp.eps[1](enei)[1]
@@ -225,10 +262,15 @@ def ext_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, order=5, 
     pos, nv, area = cp.pos, cp.nvec, cp.area
     s1, hh1 = sig["sig1"][:, 0], sig["h1"][:, :, 0]
     s2, hh2 = sig["sig2"][:, 0], sig["h2"][:, :, 0]
-    # ---- J = Re(ah . h2 + as . sig2) on faces outside in the excitation medium
-    Phi = np.exp(-1j * kb * pos @ dirv) * area
-    ah = (4 * np.pi * k0 / kb) * Phi[:, None] * pol[None, :]
-    as_ = -4 * np.pi * Phi * np.dot(pol, dirv)
+    if which == "ext":
+        J = float(pw.extinction(cp, sig)[0])
+        # J = Re(ah . h2 + as . sig2) on faces outside in the excitation medium
+        Phi = np.exp(-1j * kb * pos @ dirv) * area
+        ah = (4 * np.pi * k0 / kb) * Phi[:, None] * pol[None, :]
+        as_ = -4 * np.pi * Phi * np.dot(pol, dirv)
+    else:
+        J = float(pw.scattering(cp, sig)[0])
+        as_, ah, gpos_sca, garea_sca = sca_rhs(cp, sig, pw, enei)
     # ---- adjoint solve A^T lam = w
     A = afun_matrix(bem, enei)
     w = pack_x(np.zeros(n), np.zeros((n, 3)), as_, ah)
@@ -246,9 +288,13 @@ def ext_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, order=5, 
     gv = np.zeros_like(p.verts)
     g_k1 = 0j                          # d(lam^T A x)/dk1 (holomorphic)
     # ---- explicit J dependence (farfield phase and area)
-    Jt = np.sum(ah * hh2, 1) + as_ * s2
-    g_pos += np.real(-1j * kb * Jt)[:, None] * dirv[None, :]
-    g_area += np.real(Jt / area)
+    if which == "ext":
+        Jt = np.sum(ah * hh2, 1) + as_ * s2
+        g_pos += np.real(-1j * kb * Jt)[:, None] * dirv[None, :]
+        g_area += np.real(Jt / area)
+    else:
+        g_pos += gpos_sca
+        g_area += garea_sca
     # ---- excitation b (planewaveret/potential.m + excitation.m), times lam
     ph = np.exp(1j * kb * pos @ dirv)
     la_p = la @ pol
@@ -468,13 +514,24 @@ def ext_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, order=5, 
     return J, gv, grad_eps, {"lam": lam, "x": (s1, hh1, s2, hh2)}
 
 
-def fd_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, coords, h=1e-4):
+def scattering(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, pinfty, pattern=None):
+    """J = sca for one polarisation (forward oracle)."""
+    cp, bem = make_problem(verts, faces, quad, eps_out, eps_in, pattern)
+    pw = R.PlaneWaveRet([pol], [dirv], pinfty)
+    sig = bem.solve(pw.potential(cp, enei))
+    return float(pw.scattering(cp, sig)[0])
+
+
+def fd_gradient(verts, faces, quad, eps_out, eps_in, enei, pol, dirv, coords, h=1e-4, which="ext",
+                pinfty=None):
     """Central finite differences of J at fixed refinement pattern for the
     vertex coordinates ``coords`` [(vertex, axis)] and for eps_in (Re, Im)."""
     cp, bem = make_problem(verts, faces, quad, eps_out, eps_in)
     pat = bem.g.g.pattern
 
     def J(v, e):
+        if which == "sca":
+            return scattering(v, faces, quad, eps_out, e, enei, pol, dirv, pinfty, pattern=pat)
         return extinction(v, faces, quad, eps_out, e, enei, pol, dirv, pattern=pat)
     out = []
     for (iv, ax) in coords:

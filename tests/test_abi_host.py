@@ -66,6 +66,9 @@ def test_invalid_arguments_rejected_before_any_device_call(lib):
     assert st == 1 and b"vertex" in lib.mnpbem_last_error()
     assert lib.mnpbem_geom_destroy(None) == 0
     assert lib.mnpbem_solve(None, None, 0, None, None, 0, 0, None, None) == 1
+    assert lib.mnpbem_solve_batch(None, 0, 0, None) == 1
+    assert lib.mnpbem_geom_set_lanes(None, 2) == 1
+    assert lib.mnpbem_ext_gradient(None, None, 0, 500.0, None, 0, 0, None, None, None) == 1
 
 
 def test_materials():

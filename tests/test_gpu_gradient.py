@@ -2,8 +2,8 @@
 
 1. The CUDA adjoint equals the FP64 oracle adjoint (oracle/adjoint_ref.py,
    itself checked against central finite differences on the CPU) on a sphere
-   and a triangulated rod: vertex gradient and d/d eps to 1e-8 relative
-   (max |diff| / max |ref|).
+   and a triangulated rod, for the extinction and the scattering cross
+   section: vertex gradient and d/d eps to 1e-8 relative (max |diff| / max |ref|).
 2. On the capped rod 10 x 40 nm with ~2000 triangles at 650 nm, polarised
    along the axis: directional derivatives along random vertex displacements
    agree with central finite differences of the library's own FP64 solve
@@ -26,8 +26,8 @@ def solver(v, f, eps=EPS_IN):
     return m.bemsolver(cp, m.bemoptions(precision="fp64"))
 
 
-@pytest.mark.parametrize("shape", ["sphere", "rod"])
-def test_gradient_matches_oracle_adjoint(gpu_lib, shape):
+@pytest.mark.parametrize("shape,which", [("sphere", "ext"), ("rod", "ext"), ("sphere", "sca"), ("rod", "sca")])
+def test_gradient_matches_oracle_adjoint(gpu_lib, shape, which):
     from oracle import adjoint_ref as A
     from oracle import mnpbem_ref as R
     if shape == "sphere":
@@ -38,9 +38,11 @@ def test_gradient_matches_oracle_adjoint(gpu_lib, shape):
         pol, dirv = [0, 0, 1.0], [1.0, 0, 0]
     t = shapes.tables()
     q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
-    J0, gv0, ge0, _ = A.ext_gradient(v, f, q, 1.77, EPS_IN, 520.0, pol, dirv)
-    ext, gv, ge = solver(v, f).ext_gradient(m.planewave([pol], [dirv]), 520.0)
-    assert abs(ext - J0) / abs(J0) < 1e-10
+    vi, fi = shapes.trisphere(256, 2.0)
+    J0, gv0, ge0, _ = A.cross_section_gradient(v, f, q, 1.77, EPS_IN, 520.0, pol, dirv, which,
+                                               R.Particle(vi, fi, q))
+    val, gv, ge = solver(v, f).cross_section_gradient(m.planewave([pol], [dirv]), 520.0, 0, which)
+    assert abs(val - J0) / abs(J0) < 1e-10
     assert np.max(np.abs(gv - gv0)) / np.max(np.abs(gv0)) < 1e-8
     assert abs(ge - ge0) / abs(ge0) < 1e-8
 
@@ -67,6 +69,21 @@ def test_gradient_rod_2000_faces_vs_finite_differences(gpu_lib):
     fi = (solver(v, f, EPS_IN + 1j * he).spectrum(exc, [enei])["ext"][0, 0]
           - solver(v, f, EPS_IN - 1j * he).spectrum(exc, [enei])["ext"][0, 0]) / (2 * he)
     assert abs(ge.real - fr) / abs(fr) < 1e-4 and abs(ge.imag - fi) / abs(fi) < 1e-4, (ge, fr, fi)
+
+
+def test_scattering_gradient_rod_vs_finite_differences(gpu_lib):
+    v, f = shapes.trirod(10.0, 40.0, (25, 7, 32), triangles=True)
+    pol, dirv, enei = [0, 0, 1.0], [1.0, 0, 0], 650.0
+    exc = m.planewave([pol], [dirv])
+    sca, gv, ge = solver(v, f).cross_section_gradient(exc, enei, 0, "sca")
+    rng = np.random.default_rng(11)
+    dv = rng.standard_normal(v.shape)
+    dv /= np.linalg.norm(dv)
+    h = 1e-4
+    jp = solver(v + h * dv, f).spectrum(exc, [enei])["sca"][0, 0]
+    jm = solver(v - h * dv, f).spectrum(exc, [enei])["sca"][0, 0]
+    fd = (jp - jm) / (2 * h)
+    assert abs(float(np.sum(gv * dv)) - fd) / abs(fd) < 1e-4
 
 
 def test_autograd_gradcheck(gpu_lib):
