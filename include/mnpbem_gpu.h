@@ -106,7 +106,9 @@ MNPBEM_API mnpbem_status mnpbem_geom_export(const mnpbem_geom* g, double* pos, d
 /* compgreenret matrices of bemret (BEM/@bemret/private/initmat.m:27-31):
  *   G1 = G{1,1} - G{2,1}, H1 = H1{1,1} - H1{2,1}, G2 = G{2,2} - G{1,2}, H2 = H2{2,2} - H2{1,2}
  * for wavenumbers k_media [nmed] (complex, interleaved) of the media.
- * precision MNPBEM_FP64 -> complex128 [n][n] outputs, MNPBEM_FP32 -> complex64.
+ * precision MNPBEM_FP64 -> complex128 [n][n] outputs, MNPBEM_FP32 -> complex64,
+ * MNPBEM_MIXED -> complex128 hi + lo of the mixed-precision pass (far field in
+ * double-single FP32 arithmetic, refined entries in FP64).
  * Outputs are host pointers (NULL to skip).                                     */
 MNPBEM_API mnpbem_status mnpbem_assemble(mnpbem_geom* g, const double* k_media, int32_t nmed,
                               int32_t precision, void* G1, void* H1, void* G2, void* H2);
@@ -261,6 +263,15 @@ MNPBEM_API mnpbem_status mnpbem_cross_sections_noalloc(
  * count.  No counterpart in the reference, which solves one wavelength at a
  * time (Simulation/retarded/@spectrumret and the demo loops over enei).      */
 MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
+
+/* Tuning options of a handle (the autotuner of mnpbem_gb300/autotune.py picks
+ * them per problem size): "lanes" (0..16), "gj_block" (Gauss-Jordan step of
+ * the tensor-core inversions: 256 or 512), "tc_stages" (TMA pipeline depth of
+ * the tensor-core GEMM: 3 or 4), "tf32_round" (round A operands to nearest
+ * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
+ * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
+ * No counterpart in the reference.                                          */
+MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t value);
 
 /* The handle's CUDA stream (cudaStream_t).  mnpbem_solve runs lane 0 on it
  * and makes it wait for the other lanes before returning, so work queued on

@@ -157,6 +157,10 @@ class bemret:
             ctypes.byref(h)))
         self._h = h
         self._lib = lib
+        if self.op.get("tuned", True):
+            from . import autotune
+            for key, val in autotune.settings_for(p.n, prec).items():
+                self.set_option(key, val)
         if "lanes" in self.op:
             self.set_lanes(int(self.op["lanes"]))
 
@@ -168,6 +172,10 @@ class bemret:
             except Exception:
                 pass
             self._h = None
+
+    def set_option(self, key, value):
+        """Tuning option of the handle (``mnpbem_geom_set_option``)."""
+        _lib.check(self._lib.mnpbem_geom_set_option(self._h, key.encode(), int(value)))
 
     def set_lanes(self, lanes):
         """Wavelengths kept in flight at once by ``spectrum`` (0 = automatic)."""
@@ -207,11 +215,11 @@ class bemret:
         em = self._eps(enei)[0]
         k = np.ascontiguousarray(2 * np.pi / enei * np.sqrt(em))
         n = self.p.n
-        dt = np.complex128 if precision == "fp64" else np.complex64
+        dt = np.complex64 if precision == "fp32" else np.complex128
+        code = {"fp64": _lib.FP64, "fp32": _lib.FP32, "mixed": _lib.MIXED}[precision]
         mats = [np.zeros((n, n), dtype=dt) for _ in range(4)]
         _lib.check(self._lib.mnpbem_assemble(self._h, k.view(np.float64).ctypes.data_as(_lib.c_double_p),
-                                             k.size, _lib.FP64 if precision == "fp64" else _lib.FP32,
-                                             *[_lib.vptr(m) for m in mats]))
+                                             k.size, code, *[_lib.vptr(m) for m in mats]))
         return tuple(mats)
 
     def bem_matrices(self, enei, precision=None):

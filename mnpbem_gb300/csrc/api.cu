@@ -130,7 +130,7 @@ struct mnpbem_geom {
   int max_medium = 0;
   int64_t nverts = 0;
   bool all_closed = true;
-  DevBuf d_part, d_src, d_nrm, face_med, exbuf;
+  DevBuf d_part, d_src, d_nrm, d_srcf, d_nrmf, face_med, exbuf;
   DevBuf adj, adj_mats, adj_off;   // adjoint gradient workspace
   int adj_noff = -1;
   int64_t ld = 0;
@@ -138,6 +138,8 @@ struct mnpbem_geom {
   int lanes_req = 0;        // 0: automatic
   int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
   bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
+  bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
+  int tc_stages = 0;        // pipeline depth of the tensor-core GEMM (0: its default)
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -197,6 +199,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
     return s;
   }
   L->status_host[0] = L->status_host[1] = 0;
+  if (G->tc_stages) L->tc.stages = G->tc_stages;
   G->lanes.push_back(std::move(L));
   return MNPBEM_OK;
 }
@@ -230,6 +233,9 @@ AsmParams base_params(mnpbem_geom* G, const LamParams* lp) {
   p.part = G->d_part.as<int>();
   p.src = G->d_src.as<double4_32a>();
   p.nrm = G->d_nrm.as<double4_32a>();
+  p.srcf = G->d_srcf.as<float4>();
+  p.nrmf = G->d_nrmf.as<float4>();
+  p.nmed = G->max_medium;
   p.ref_row = G->g.ref_row;
   p.ref_col = G->g.ref_col;
   p.ref_g = G->g.ref_g;
@@ -336,6 +342,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (s == MNPBEM_OK) s = G->d_part.ensure(sizeof(int) * nfaces);
   if (s == MNPBEM_OK) s = G->d_src.ensure(sizeof(double4_32a) * nfaces);
   if (s == MNPBEM_OK) s = G->d_nrm.ensure(sizeof(double4_32a) * nfaces);
+  if (s == MNPBEM_OK) s = G->d_srcf.ensure(sizeof(float4) * 2 * nfaces);
+  if (s == MNPBEM_OK) s = G->d_nrmf.ensure(sizeof(float4) * 2 * nfaces);
   if (s == MNPBEM_OK) {
     if (cudaMemcpyAsync(G->d_part.ptr, G->face_part.data(), sizeof(int) * nfaces,
                         cudaMemcpyHostToDevice, G->st) != cudaSuccess) {
@@ -343,7 +351,7 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
       s = MNPBEM_ERR_CUDA;
     } else {
       pack_sources((int)nfaces, G->g.pos, G->g.area, G->g.nvec, G->d_src.as<double4_32a>(),
-                   G->d_nrm.as<double4_32a>(), G->st);
+                   G->d_nrm.as<double4_32a>(), G->d_srcf.as<float4>(), G->d_nrmf.as<float4>(), G->st);
       if (cudaStreamSynchronize(G->st) != cudaSuccess) {
         set_error("geometry set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
         s = MNPBEM_ERR_CUDA;
@@ -361,6 +369,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (env && env[0] == '0') G->tc_enabled = false;
   const char* genv = getenv("MNPBEM_GRAPHS");
   if (genv && genv[0] == '0') G->use_graphs = false;
+  const char* dsenv = getenv("MNPBEM_ASM_DS");
+  if (dsenv && dsenv[0] == '0') G->asm_ds = false;
   const char* rnaenv = getenv("MNPBEM_TF32_RNA");
   if (rnaenv && rnaenv[0] == '0') G->tf32_rna = false;
   const char* nbenv = getenv("MNPBEM_GJ_NB");
@@ -392,6 +402,23 @@ mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes) {
   }
   g->lanes_req = lanes;
   return MNPBEM_OK;
+}
+
+mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t value) {
+  MNP_TRY(check_geom(g));
+  if (!key) { set_error("null option name"); return MNPBEM_ERR_INVALID_ARG; }
+  const std::string k(key);
+  if (k == "lanes") return mnpbem_geom_set_lanes(g, value);
+  if (k == "gj_block" && (value == 256 || value == 512)) { g->gj_nb = value; return MNPBEM_OK; }
+  if (k == "tc_stages" && (value == 3 || value == 4)) {
+    g->tc_stages = value;
+    for (auto& L : g->lanes) L->tc.stages = value;
+    return MNPBEM_OK;
+  }
+  if (k == "tf32_round" && (value == 0 || value == 1)) { g->tf32_rna = value != 0; return MNPBEM_OK; }
+  if (k == "assembly_ds" && (value == 0 || value == 1)) { g->asm_ds = value != 0; return MNPBEM_OK; }
+  set_error("unknown option '%s' or value %d out of range", key, value);
+  return MNPBEM_ERR_INVALID_ARG;
 }
 
 mnpbem_status mnpbem_geom_size(const mnpbem_geom* g, int64_t* nfaces, int64_t* nref) {
@@ -436,7 +463,7 @@ mnpbem_status mnpbem_assemble(mnpbem_geom* G, const double* k_media, int32_t nme
                               int32_t precision, void* G1, void* H1, void* G2, void* H2) {
   MNP_TRY(check_geom(G));
   if (!k_media || nmed < G->max_medium || nmed > ASM_MAXMED ||
-      (precision != MNPBEM_FP64 && precision != MNPBEM_FP32)) {
+      (precision != MNPBEM_FP64 && precision != MNPBEM_FP32 && precision != MNPBEM_MIXED)) {
     set_error("mnpbem_assemble: invalid arguments");
     return MNPBEM_ERR_INVALID_ARG;
   }
@@ -451,6 +478,30 @@ mnpbem_status mnpbem_assemble(mnpbem_geom* G, const double* k_media, int32_t nme
   }
   AsmParams p = base_params(G, L.lp_dev.as<LamParams>());
   const int64_t n = G->g.n;
+  if (precision == MNPBEM_MIXED) {
+    // the mixed-precision pass (double-single far field, hi / lo planes), returned as hi + lo
+    DevBuf work, planes, out;
+    MNP_TRY(work.ensure(sizeof(float2) * 4 * n * n));
+    MNP_TRY(planes.ensure(sizeof(float2) * 8 * n * n));
+    MNP_TRY(out.ensure(sizeof(double2) * n * n));
+    float2* w = work.as<float2>();
+    float2* pl = planes.as<float2>();
+    p.ld32 = n;
+    p.g1 = w; p.h1 = w + n * n; p.g2 = w + 2 * n * n; p.h2 = w + 3 * n * n;
+    p.G1hi = pl; p.G1lo = pl + n * n; p.H1hi = pl + 2 * n * n; p.H1lo = pl + 3 * n * n;
+    p.G2hi = pl + 4 * n * n; p.G2lo = pl + 5 * n * n; p.H2hi = pl + 6 * n * n; p.H2lo = pl + 7 * n * n;
+    p.ds = G->asm_ds;
+    MNP_TRY(assemble_launch(p, true, true, G->st));
+    void* hosts[4] = {G1, H1, G2, H2};
+    for (int q = 0; q < 4; ++q) {
+      if (!hosts[q]) continue;
+      hilo_to_c128(pl + 2 * q * n * n, pl + (2 * q + 1) * n * n, out.as<double2>(), n * n, G->st);
+      MNP_CHECK_LAUNCH();
+      MNP_CUDA(cudaMemcpyAsync(hosts[q], out.ptr, sizeof(double2) * n * n, cudaMemcpyDeviceToHost, G->st));
+      MNP_CUDA(cudaStreamSynchronize(G->st));
+    }
+    return MNPBEM_OK;
+  }
   const bool w64 = precision == MNPBEM_FP64;
   const size_t es = w64 ? sizeof(double2) : sizeof(float2);
   void* hosts[4] = {G1, H1, G2, H2};
@@ -718,6 +769,7 @@ mnpbem_status stage_assemble(mnpbem_geom* G, Lane& L, int precision) {
   p.H1hi = hl[1]; p.H1lo = hl[1] + n * ld;
   p.G2hi = hl[2]; p.G2lo = hl[2] + n * ld;
   p.H2hi = hl[3]; p.H2lo = hl[3] + n * ld;
+  p.ds = G->asm_ds;
   return assemble_launch(p, true, true, L.st);
 }
 

@@ -156,6 +156,7 @@ __device__ __forceinline__ void store4(const AsmParams& p, int64_t i, int64_t j,
 
 constexpr int ASM_COLS = 128;
 constexpr int ASM_ROWS = 4;
+constexpr int ASM_DS_ROWS = 8;
 
 template <bool W64, bool W32>
 __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
@@ -189,6 +190,234 @@ __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
     store4<W64, W32>(p, i, j, g1, h1, g2, h2);
   }
 }
+
+// ------------------------------------------------- double-single assembly
+// Mixed precision needs G1, H1, G2, H2 twice: as complex64 working matrices
+// and, for the refinement residual, to ~48 bits as hi / lo complex64 planes.
+// On GB300 FP64 runs at 1/64 of the FP32 rate, so the FP64 pass above is
+// FP64-pipe bound.  This pass computes every entry in double-single
+// arithmetic (value = hi + lo, two floats; error-free transformations of
+// Dekker and Knuth: TwoSum, TwoProduct by FMA) and writes hi / lo directly.
+// exp(ikd) uses the same table-driven reduction as the FP64 pass, with the
+// 2 pi / 256 and ln 2 / 64 constants split in three floats and Taylor series
+// of the reduced arguments whose small tails are kept in float.
+// Accuracy: ~1e-14 relative per entry (tests compare with the FP64 pass).
+struct dsf { float hi, lo; };
+
+__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dsf ds_quick(float a, float b) {   // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ dsf ds_from(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ dsf ds_add(dsf a, dsf b) {
+  dsf s = ds_two_sum(a.hi, b.hi);
+  const dsf t = ds_two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = ds_quick(s.hi, s.lo);
+  s.lo += t.lo;
+  return ds_quick(s.hi, s.lo);
+}
+__device__ __forceinline__ dsf ds_neg(dsf a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dsf ds_sub(dsf a, dsf b) { return ds_add(a, ds_neg(b)); }
+__device__ __forceinline__ dsf ds_mul(dsf a, dsf b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ds_quick(p, e);
+}
+__device__ __forceinline__ dsf ds_mulf(dsf a, float b) {
+  const float p = a.hi * b;
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  return ds_quick(p, e);
+}
+__device__ __forceinline__ dsf ds_sqrt(dsf a) {            // a > 0
+  const float q = sqrtf(a.hi);
+  const float p = q * q;
+  const float pe = fmaf(q, q, -p);
+  const float r = ((a.hi - p) - pe) + a.lo;               // a - q^2 (a.hi - p is exact near q^2)
+  return ds_quick(q, r / (2.0f * q));
+}
+__device__ __forceinline__ dsf ds_recip(dsf a) {           // 1 / a
+  const float q1 = 1.0f / a.hi;
+  const dsf r = ds_sub(dsf{1.0f, 0.0f}, ds_mulf(a, q1));
+  return ds_quick(q1, r.hi * q1);
+}
+struct dsc { dsf re, im; };
+__device__ __forceinline__ dsc dsc_mul(dsc a, dsc b) {
+  return {ds_sub(ds_mul(a.re, b.re), ds_mul(a.im, b.im)), ds_add(ds_mul(a.re, b.im), ds_mul(a.im, b.re))};
+}
+__device__ __forceinline__ dsc dsc_scale(dsc a, dsf s) { return {ds_mul(a.re, s), ds_mul(a.im, s)}; }
+
+// reduction constants: three-float splits (heads with trailing zero bits so
+// that j * head is exact for |j| < 2^12)
+constexpr float CIS_F1 = 0.0245361328125f;           // 2 pi / 256 = F1 + F2 + F3 (F1: 12 bits)
+constexpr float CIS_F2 = 7.55979363e-06f;
+constexpr float CIS_F3 = 4.00522511e-14f;
+constexpr float EXP_F1 = 0.010829925537109375f;      // ln 2 / 64 = F1 + F2 + F3 (F1: 12 bits)
+constexpr float EXP_F2 = 4.99159114e-07f;
+constexpr float EXP_F3 = 2.57280464e-14f;
+
+struct CisTableF {
+  float c_hi[CIS_N], c_lo[CIS_N], s_hi[CIS_N], s_lo[CIS_N];
+  float e_hi[64], e_lo[64];
+};
+__device__ CisTableF g_cisf;
+__global__ void k_cisf_init() {
+  const int j = threadIdx.x;
+  double sn, cs;
+  sincospi(2.0 * j / CIS_N, &sn, &cs);
+  dsf c = ds_from(cs), s = ds_from(sn);
+  g_cisf.c_hi[j] = c.hi; g_cisf.c_lo[j] = c.lo;
+  g_cisf.s_hi[j] = s.hi; g_cisf.s_lo[j] = s.lo;
+  if (j < 64) {
+    dsf e = ds_from(exp2(-j / 64.0));
+    g_cisf.e_hi[j] = e.hi; g_cisf.e_lo[j] = e.lo;
+  }
+}
+
+// x - j * (c1 + c2 + c3) for x in double-single, |j| < 2^12 integral:
+// j c1 is exact (c1 has 12 significant bits) and cancels exactly against x.hi,
+// j c2 is taken exactly as a TwoProduct, j c3 is below the double-single ulp
+__device__ __forceinline__ dsf ds_reduce(dsf x, float j, float c1, float c2, float c3) {
+  const float a = fmaf(-j, c1, x.hi);
+  dsf t = ds_two_sum(a, x.lo);
+  const float p2 = j * c2;
+  t = ds_sub(t, dsf{p2, fmaf(j, c2, -p2)});
+  return ds_sub(t, dsf{j * c3, 0.0f});
+}
+
+// exp(i k d) in double-single; k = (kr, ki) as double-single
+__device__ __forceinline__ dsc ds_cis_exp(const CisTableF& T, dsf kr, dsf ki, bool lossy, dsf d) {
+  const dsf th = ds_mul(kr, d);
+  const float jf = rintf(th.hi * (float)CIS_INV);
+  const dsf t = ds_reduce(th, jf, CIS_F1, CIS_F2, CIS_F3);
+  // sin t = t - t^3/6 + [t^5/120 (1 - t^2/42 + t^4/3024)]
+  // cos t = 1 - t^2/2 + [t^4/24 (1 - t^2/30 + t^4/1680)]
+  // (|t| <= pi/256: the bracketed tails, < 1e-9, are accurate enough in float;
+  //  the leading terms are kept in double-single)
+  const float tf = t.hi, t2f = tf * tf;
+  const dsf t2 = ds_mul(t, t);
+  const dsf sixth = {0.16666667163372040f, -4.96705388e-09f};   // 1/6 split
+  const dsf t3_6 = ds_mul(ds_mul(t2, t), sixth);
+  const float s5 = (t2f * t2f * tf) * (1.0f / 120.0f) * fmaf(t2f, fmaf(t2f, 1.0f / 3024.0f, -1.0f / 42.0f), 1.0f);
+  const dsf sn = ds_add(ds_sub(t, t3_6), dsf{s5, 0.0f});
+  const float c4 = (t2f * t2f) * (1.0f / 24.0f) * fmaf(t2f, fmaf(t2f, 1.0f / 1680.0f, -1.0f / 30.0f), 1.0f);
+  const dsf cn = ds_add(ds_sub(dsf{1.0f, 0.0f}, dsf{t2.hi * 0.5f, t2.lo * 0.5f}), dsf{c4, 0.0f});
+  const int jj = ((int)jf) & (CIS_N - 1);
+  const dsf tc = {T.c_hi[jj], T.c_lo[jj]}, ts = {T.s_hi[jj], T.s_lo[jj]};
+  dsc r = {ds_sub(ds_mul(tc, cn), ds_mul(ts, sn)), ds_add(ds_mul(ts, cn), ds_mul(tc, sn))};
+  if (lossy) {
+    const dsf x = ds_mul(ki, d);
+    if (x.hi > 80.0f) return {dsf{0, 0}, dsf{0, 0}};
+    const float yf = rintf(x.hi * (float)EXP_INV);
+    const dsf u = ds_reduce(x, yf, EXP_F1, EXP_F2, EXP_F3);
+    // exp(-u) = (1 - u) + u^2/2 - [u^3/6 (1 - u/4 + u^2/20 - u^3/120)],  |u| <= ln2/128
+    const float uf = u.hi;
+    const dsf q = ds_mul(u, u);
+    const float c3 = (uf * uf * uf) * (1.0f / 6.0f) * fmaf(uf, fmaf(uf, fmaf(uf, -1.0f / 120.0f, 1.0f / 20.0f), -0.25f), 1.0f);
+    const dsf ex = ds_sub(ds_add(ds_sub(dsf{1.0f, 0.0f}, u), dsf{q.hi * 0.5f, q.lo * 0.5f}), dsf{c3, 0.0f});
+    const int yi = (int)yf;
+    const int nn = yi >> 6, m = yi - (nn << 6);
+    dsf e = ds_mul(ex, dsf{T.e_hi[m], T.e_lo[m]});
+    const float sc = ldexpf(1.0f, -nn);
+    e.hi *= sc;
+    e.lo *= sc;
+    r = dsc_scale(r, e);
+  }
+  return r;
+}
+
+struct DsPair { dsc G, F; };
+__device__ __forceinline__ DsPair ds_far_pair(const CisTableF& T, dsf kr, dsf ki, bool lossy, dsf d, dsf inv,
+                                              dsf in, dsf area) {
+  const dsc ph = ds_cis_exp(T, kr, ki, lossy, d);
+  DsPair v;
+  v.G = dsc_scale(ph, ds_mul(area, inv));
+  // (ik - 1/d) / d^2 (n . r) area = ((-ki - inv) + i kr) inv^2 in area
+  const dsf s = ds_mul(ds_mul(inv, inv), ds_mul(in, area));
+  const dsc tf = {ds_mul(ds_sub(ds_neg(ki), inv), s), ds_mul(kr, s)};
+  v.F = dsc_mul(tf, ph);
+  return v;
+}
+
+__device__ __forceinline__ void ds_store(float2* hi, float2* lo, float2* w, int64_t o, dsc v) {
+  const float2 h = make_float2(v.re.hi, v.im.hi);
+  w[o] = h;
+  hi[o] = h;
+  lo[o] = make_float2(v.re.lo, v.im.lo);
+}
+
+template <int ROWS>
+__global__ void __launch_bounds__(ASM_COLS) k_asm_far_ds(AsmParams p) {
+  __shared__ CisTableF T;
+  for (int q = threadIdx.x; q < CIS_N; q += blockDim.x) {
+    T.c_hi[q] = g_cisf.c_hi[q]; T.c_lo[q] = g_cisf.c_lo[q];
+    T.s_hi[q] = g_cisf.s_hi[q]; T.s_lo[q] = g_cisf.s_lo[q];
+  }
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) { T.e_hi[q] = g_cisf.e_hi[q]; T.e_lo[q] = g_cisf.e_lo[q]; }
+  __syncthreads();
+  const int64_t j = (int64_t)blockIdx.x * ASM_COLS + threadIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.y * ROWS;
+  if (j >= p.n) return;
+  const float4 sjh = p.srcf[2 * j], sjl = p.srcf[2 * j + 1];
+  const dsf xj = {sjh.x, sjl.x}, yj = {sjh.y, sjl.y}, zj = {sjh.z, sjl.z}, aj = {sjh.w, sjl.w};
+  const int pj = p.part[j];
+  // wavenumbers of the media in double-single (once per thread)
+  dsf kr[ASM_MAXMED], ki[ASM_MAXMED];
+  bool lossy[ASM_MAXMED];
+  const int nmed = p.nmed;
+  for (int m = 0; m < nmed; ++m) {
+    kr[m] = ds_from(p.lp->k[m].x);
+    ki[m] = ds_from(p.lp->k[m].y);
+    lossy[m] = p.lp->k[m].y != 0.0;
+  }
+  const dsc zero = {dsf{0, 0}, dsf{0, 0}};
+  for (int r = 0; r < ROWS; ++r) {
+    const int64_t i = i0 + r;
+    if (i >= p.n) break;
+    const int64_t o = i * p.ld32 + j;
+    if (i == j) {
+      // self element: refined (and given its +-2 pi) by the near pass
+      const float2 z = make_float2(0.f, 0.f);
+      p.g1[o] = p.h1[o] = p.g2[o] = p.h2[o] = z;
+      p.G1hi[o] = p.G1lo[o] = p.H1hi[o] = p.H1lo[o] = z;
+      p.G2hi[o] = p.G2lo[o] = p.H2hi[o] = p.H2lo[o] = z;
+      continue;
+    }
+    const float4 sih = p.srcf[2 * i], sil = p.srcf[2 * i + 1];
+    const float4 nih = p.nrmf[2 * i], nil = p.nrmf[2 * i + 1];
+    const dsf x = ds_sub(dsf{sih.x, sil.x}, xj), y = ds_sub(dsf{sih.y, sil.y}, yj), z = ds_sub(dsf{sih.z, sil.z}, zj);
+    const dsf d2 = ds_add(ds_add(ds_mul(x, x), ds_mul(y, y)), ds_mul(z, z));
+    const dsf d = ds_sqrt(d2);
+    const dsf inv = ds_recip(d);
+    const dsf in = ds_add(ds_add(ds_mul(x, dsf{nih.x, nil.x}), ds_mul(y, dsf{nih.y, nil.y})), ds_mul(z, dsf{nih.z, nil.z}));
+    const int pi = p.part[i];
+    const int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
+    dsc g1 = zero, h1 = zero, g2 = zero, h2 = zero;
+    if (m11) { DsPair v = ds_far_pair(T, kr[m11 - 1], ki[m11 - 1], lossy[m11 - 1], d, inv, in, aj); g1 = v.G; h1 = v.F; }
+    if (m21) { DsPair v = ds_far_pair(T, kr[m21 - 1], ki[m21 - 1], lossy[m21 - 1], d, inv, in, aj);
+               g1 = {ds_sub(g1.re, v.G.re), ds_sub(g1.im, v.G.im)}; h1 = {ds_sub(h1.re, v.F.re), ds_sub(h1.im, v.F.im)}; }
+    if (m22) { DsPair v = ds_far_pair(T, kr[m22 - 1], ki[m22 - 1], lossy[m22 - 1], d, inv, in, aj); g2 = v.G; h2 = v.F; }
+    if (m12) { DsPair v = ds_far_pair(T, kr[m12 - 1], ki[m12 - 1], lossy[m12 - 1], d, inv, in, aj);
+               g2 = {ds_sub(g2.re, v.G.re), ds_sub(g2.im, v.G.im)}; h2 = {ds_sub(h2.re, v.F.re), ds_sub(h2.im, v.F.im)}; }
+    ds_store(p.G1hi, p.G1lo, p.g1, o, g1);
+    ds_store(p.H1hi, p.H1lo, p.h1, o, h1);
+    ds_store(p.G2hi, p.G2lo, p.g2, o, g2);
+    ds_store(p.H2hi, p.H2lo, p.h2, o, h2);
+  }
+}
+
+static bool g_cisf_ready[64];
 
 // refined value for wavenumber k
 __device__ __forceinline__ PairVal near_pair(const AsmParams& p, int64_t e, double2 k, double dd,
@@ -238,16 +467,34 @@ __global__ void k_asm_near(AsmParams p) {
 }
 
 __global__ void k_pack_src(int n, const double* pos, const double* area, const double* nvec,
-                           double4_32a* src, double4_32a* nrm) {
+                           double4_32a* src, double4_32a* nrm, float4* srcf, float4* nrmf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   src[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], area[i]);
   nrm[i] = make_double4_32a(nvec[3 * i], nvec[3 * i + 1], nvec[3 * i + 2], 0.0);
+  if (srcf) {
+    const dsf a = ds_from(pos[3 * i]), b = ds_from(pos[3 * i + 1]), c = ds_from(pos[3 * i + 2]), w = ds_from(area[i]);
+    srcf[2 * i] = make_float4(a.hi, b.hi, c.hi, w.hi);
+    srcf[2 * i + 1] = make_float4(a.lo, b.lo, c.lo, w.lo);
+    const dsf u = ds_from(nvec[3 * i]), v = ds_from(nvec[3 * i + 1]), t = ds_from(nvec[3 * i + 2]);
+    nrmf[2 * i] = make_float4(u.hi, v.hi, t.hi, 0.f);
+    nrmf[2 * i + 1] = make_float4(u.lo, v.lo, t.lo, 0.f);
+  }
 }
 
 void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
-                  double4_32a* nrm, cudaStream_t st) {
-  k_pack_src<<<(n + 255) / 256, 256, 0, st>>>(n, pos, area, nvec, src, nrm);
+                  double4_32a* nrm, float4* srcf, float4* nrmf, cudaStream_t st) {
+  k_pack_src<<<(n + 255) / 256, 256, 0, st>>>(n, pos, area, nvec, src, nrm, srcf, nrmf);
+}
+
+__global__ void k_hilo_c128(const float2* hi, const float2* lo, double2* out, int64_t count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  out[i] = make_double2((double)hi[i].x + (double)lo[i].x, (double)hi[i].y + (double)lo[i].y);
+}
+
+void hilo_to_c128(const float2* hi, const float2* lo, double2* out, int64_t count, cudaStream_t st) {
+  if (count > 0) k_hilo_c128<<<(unsigned)cdiv_up(count, 256), 256, 0, st>>>(hi, lo, out, count);
 }
 
 mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st) {
@@ -257,7 +504,17 @@ mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream
   ProfScope ps(PH_ASSEMBLE, st, 0.0, nn * 4.0 * ((w64 ? 16.0 : 0.0) + (w32 ? 8.0 : 0.0)),
                p.nref > 0 ? 2 : 1);
   dim3 grid((unsigned)cdiv_up(p.n, ASM_COLS), (unsigned)cdiv_up(p.n, ASM_ROWS));
-  if (w64 && w32) k_asm_far<true, true><<<grid, ASM_COLS, 0, st>>>(p);
+  if (w64 && w32 && p.ds) {
+    int dev = 0;
+    MNP_CUDA(cudaGetDevice(&dev));
+    if (!g_cisf_ready[dev]) {
+      k_cisf_init<<<1, CIS_N, 0, st>>>();
+      MNP_CHECK_LAUNCH();
+      if (!capturing_now()) g_cisf_ready[dev] = true;
+    }
+    dim3 g2((unsigned)cdiv_up(p.n, ASM_COLS), (unsigned)cdiv_up(p.n, ASM_DS_ROWS));
+    k_asm_far_ds<ASM_DS_ROWS><<<g2, ASM_COLS, 0, st>>>(p);
+  } else if (w64 && w32) k_asm_far<true, true><<<grid, ASM_COLS, 0, st>>>(p);
   else if (w64) k_asm_far<true, false><<<grid, ASM_COLS, 0, st>>>(p);
   else k_asm_far<false, true><<<grid, ASM_COLS, 0, st>>>(p);
   MNP_CHECK_LAUNCH();

@@ -15,11 +15,15 @@ struct AsmParams {
   const int* part = nullptr;      // [n] particle index of each face
   const double4_32a* src = nullptr;   // [n] (x, y, z, area)
   const double4_32a* nrm = nullptr;   // [n] (nx, ny, nz, 0)
+  const float4* srcf = nullptr;   // [n][2] double-single splits of src: (hi x, y, z, area), (lo ...)
+  const float4* nrmf = nullptr;   // [n][2] double-single splits of nrm
   const int* ref_row = nullptr;
   const int* ref_col = nullptr;
   const double* ref_g = nullptr;
   const double* ref_f = nullptr;
   const LamParams* lp = nullptr;   // wavenumbers of the media (device)
+  int nmed = 1;                    // media used by the blocks (1-based indices <= nmed)
+  bool ds = false;                 // mixed outputs from the double-single pass
   // media (1-based, 0 = block not connected) of the four connectivity
   // blocks: 0 -> con{1,1} (+G1), 1 -> con{2,1} (-G1), 2 -> con{2,2} (+G2), 3 -> con{1,2} (-G2)
   signed char med[4][ASM_MAXP][ASM_MAXP];
@@ -32,9 +36,11 @@ struct AsmParams {
 };
 
 void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
-                  double4_32a* nrm, cudaStream_t st);
+                  double4_32a* nrm, float4* srcf, float4* nrmf, cudaStream_t st);
 // w64 && !w32: complex128 outputs; !w64 && w32: complex64 outputs;
 // w64 && w32: complex64 working matrices plus hi / lo planes
 mnpbem_status assemble_launch(const AsmParams& p, bool w64, bool w32, cudaStream_t st);
+// out = hi + lo in FP64 (count complex values)
+void hilo_to_c128(const float2* hi, const float2* lo, double2* out, int64_t count, cudaStream_t st);
 
 }  // namespace mnpbem

@@ -418,6 +418,7 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
     if (!c.usable) cudaGetLastError();
     const char* env = getenv("MNPBEM_TC_STAGES");
     if (env && (env[0] == '3' || env[0] == '4')) c.stages = env[0] - '0';
+    if (c.stages != 3 && c.stages != 4) c.stages = 4;
   }
   if (!c.usable || !c.enabled) return false;
   if ((lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||

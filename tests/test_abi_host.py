@@ -113,3 +113,20 @@ def test_fibsphere_counts():
         cen = v[f[:, :3]].mean(1)
         nv = np.cross(v[f[:, 0]] - v[f[:, 1]], v[f[:, 2]] - v[f[:, 1]])
         assert np.all(np.sum(nv * cen, 1) > 0)
+
+
+def test_autotune_settings_lookup(tmp_path, monkeypatch):
+    import json
+    from mnpbem_gb300 import autotune
+    f = tmp_path / "tuned.json"
+    f.write_text(json.dumps({"4000": {"options": {"lanes": 6, "tc_stages": 4, "gj_block": 256}},
+                             "24000": {"options": {"lanes": 3}}}))
+    monkeypatch.setattr(autotune, "TUNED", str(f))
+    assert autotune.settings_for(3000, "mixed") == {"lanes": 6, "tc_stages": 4, "gj_block": 256}
+    assert autotune.settings_for(20000, "mixed") == {"lanes": 3}
+    assert autotune.settings_for(500, "mixed") == {}          # nothing within a factor of 2
+    assert autotune.settings_for(4000, "fp64") == {}
+
+
+def test_set_option_validation(lib):
+    assert lib.mnpbem_geom_set_option(None, b"lanes", 2) == 1

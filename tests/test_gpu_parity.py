@@ -9,8 +9,9 @@ max |ref| unless stated):
   centroid, where r = |centroid - point| loses ~9 digits to cancellation in any
   FP64 evaluation of the reference formula); FP64 matrices 1e-10; FP64 bemret
   matrices 1e-9; FP64 solution fields 1e-9 and cross sections 1e-10;
-  complex64 assembly 2e-6; mixed precision (complex64 inversion + FP64
-  refinement) cross sections 1e-8.
+  complex64 assembly 2e-6; double-single assembly (hi + lo) against the FP64
+  pass 1e-13; mixed precision (complex64 inversion + FP64 refinement) cross
+  sections 1e-8.
 Measured errors are appended to ``gpurun_out/parity.jsonl`` when that folder
 exists.
 """
@@ -108,6 +109,12 @@ def test_assembly_parity(c1, enei):
         assert v < 1e-10, (nm, v)
     for (nm, v), a in zip(e32.items(), got32):
         assert a.dtype == np.complex64 and v < 2e-6, (nm, v)
+    # mixed-precision pass (double-single far field): hi + lo against the FP64 pass
+    gotmx = bem.matrices(enei, "mixed")
+    emx = {nm + "_ds": rel(a, b) for nm, a, b in zip(names, gotmx, got)}
+    record("assembly_ds_%g" % enei, **emx)
+    for nm, v in emx.items():
+        assert v < 1e-13, (nm, v)
 
 
 def test_bem_matrices_fp64(c1):
