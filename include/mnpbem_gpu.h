@@ -182,7 +182,9 @@ MNPBEM_API mnpbem_status mnpbem_solve_batch(const mnpbem_job* jobs, int32_t njob
  * surface charges, chained to the vertices through norm_flat.m.  No
  * counterpart in the reference (MNPBEM has no derivatives).  The refinement
  * pattern is held fixed.  Scope: one closed particle excited from its outside
- * medium; precision MNPBEM_FP64.
+ * medium.  precision MNPBEM_FP64: FP64 solves; MNPBEM_MIXED: complex64
+ * (TF32) forward and transposed solves, each refined on the FP64-class
+ * operator (double-single products of the hi / lo planes).
  *   ext: the cross section (may be NULL); verts_grad [nverts][3] (host):
  *   dext / dvertex; eps_grad [2] (host): dext / dRe(eps), dext / dIm(eps) of
  *   the medium inside the particle.                                          */

@@ -284,10 +284,11 @@ class bemret:
         outside medium; the refinement pattern is held fixed."""
         return self.cross_section_gradient(exc, enei, ipol, "ext")
 
-    def cross_section_gradient(self, exc, enei, ipol=0, which="ext"):
+    def cross_section_gradient(self, exc, enei, ipol=0, which="ext", precision="fp64"):
         """``which`` = 'ext' or 'sca': the cross section and its gradient
         (see ``ext_gradient``); 'sca' integrates over ``exc``'s sphere at
-        infinity as ``scattering.m``."""
+        infinity as ``scattering.m``.  ``precision`` 'mixed': complex64
+        forward and transposed solves with FP64-class refinement."""
         em = np.ascontiguousarray(self._eps(float(enei))[0])
         pw = exc._struct()
         val = np.zeros(1)
@@ -295,7 +296,8 @@ class bemret:
         ge = np.zeros(2)
         _lib.check(self._lib.mnpbem_cross_section_gradient(
             self._h, ctypes.byref(pw), int(ipol), {"ext": 0, "sca": 1}[which], float(enei),
-            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, _lib.FP64,
+            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size,
+            _lib.MIXED if precision == "mixed" else _lib.FP64,
             _lib.vptr(val), _lib.vptr(gv), _lib.vptr(ge)))
         return float(val[0]), gv, complex(ge[0], ge[1])
 

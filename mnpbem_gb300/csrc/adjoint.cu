@@ -630,17 +630,18 @@ __global__ void k_adj_norm_flat(AdjParams p) {
 
 // --------------------------------------------- transposed chain helpers
 // in-place transpose of an n x n complex128 matrix (leading dimension ld)
-__global__ void k_transpose_sq(double2* A, int64_t n, int64_t ld) {
-  __shared__ double2 t1[32][33], t2[32][33];
+template <typename C>
+__global__ void k_transpose_sq(C* A, int64_t n, int64_t ld) {
+  __shared__ C t1[32][33], t2[32][33];
   const int bx = blockIdx.x, by = blockIdx.y;
   if (bx < by) return;
   const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
   const int64_t r1 = (int64_t)by * 32, c1 = (int64_t)bx * 32;
   for (int k = ty; k < 32; k += 8) {
     const int64_t r = r1 + k, c = c1 + tx;
-    t1[k][tx] = (r < n && c < n) ? A[r * ld + c] : make_double2(0, 0);
+    t1[k][tx] = (r < n && c < n) ? A[r * ld + c] : C{};
     const int64_t r2 = c1 + k, c2 = r1 + tx;
-    t2[k][tx] = (r2 < n && c2 < n) ? A[r2 * ld + c2] : make_double2(0, 0);
+    t2[k][tx] = (r2 < n && c2 < n) ? A[r2 * ld + c2] : C{};
   }
   __syncthreads();
   for (int k = ty; k < 32; k += 8) {
@@ -772,11 +773,135 @@ __global__ void k_adj_chain(AdjParams p, int mode, const double2* a_in, const do
   }
 }
 
+// elementwise steps of the transposed chain for complex type C (per face):
+//   mode 0: o1 += i k0 (L1 - L2) (n . a)               a [n][3], o1 [n]
+//   mode 1: o1  = i k0 (L1 - L2) n a                    a [n],    o1 [n][3]
+//   mode 2: o1 += -L1 a + i k0 L1 (n . b)               (gphi)
+//           o2  = d + i k0 L1 n c - o2                  (ga; o2 holds Sigma1^T gal, d = G1i^T gh1 or 0)
+template <typename C>
+__global__ void k_chainT(AdjParams p, int mode, const C* a, const C* b, C* o1, C* o2, const C* c, const C* d) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const double3 n = vld(p.nvec, i);
+  const double nc[3] = {n.x, n.y, n.z};
+  const double2 L1 = p.eps1[i], L2 = p.eps2[i];
+  const double2 ik = cx(0.0, p.k0);
+  const double2 ikL = cmul(ik, csub(L1, L2)), ikL1 = cmul(ik, L1);
+  if (mode == 0) {
+    double2 sm = cx(0, 0);
+    for (int q = 0; q < 3; ++q) sm = cadd(sm, cscl(to_d(a[3 * i + q]), nc[q]));
+    o1[i] = from_d<C>(cadd(to_d(o1[i]), cmul(ikL, sm)));
+  } else if (mode == 1) {
+    const double2 t = cmul(ikL, to_d(a[i]));
+    for (int q = 0; q < 3; ++q) o1[3 * i + q] = from_d<C>(cscl(t, nc[q]));
+  } else {
+    double2 nb = cx(0, 0);
+    for (int q = 0; q < 3; ++q) nb = cadd(nb, cscl(to_d(b[3 * i + q]), nc[q]));
+    o1[i] = from_d<C>(cadd(to_d(o1[i]), csub(cmul(ikL1, nb), cmul(L1, to_d(a[i])))));
+    const double2 t = cmul(ikL1, to_d(c[i]));
+    for (int q = 0; q < 3; ++q) {
+      const double2 dv = d ? to_d(d[3 * i + q]) : cx(0, 0);
+      o2[3 * i + q] = from_d<C>(csub(cadd(dv, cscl(t, nc[q])), to_d(o2[3 * i + q])));
+    }
+  }
+}
+
+// y[N cols] partial sums of (Ahi + Alo)^T V over row chunk blockIdx.y:
+// thread = column j (coalesced row reads), double-single accumulation
+// (error-free products, TwoSum), partial [chunks][n][N] in FP64
+struct DSa { float hi, lo; };
+__device__ __forceinline__ void dsa_acc(DSa& s, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float t = s.hi + p;
+  const float bp = t - s.hi;
+  const float err = (s.hi - (t - bp)) + (p - bp);
+  s.hi = t;
+  s.lo += err + e;
+}
+template <int N>
+__global__ void __launch_bounds__(128) k_gemm_t_ds(int64_t n, int64_t rows_per_chunk, const float2* __restrict__ Ahi,
+                                                   const float2* __restrict__ Alo, int64_t lda,
+                                                   const float2* __restrict__ Vh, const float2* __restrict__ Vl,
+                                                   double2* __restrict__ part) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per_chunk, r1 = min(n, r0 + rows_per_chunk);
+  DSa re[N], im[N];
+  for (int c = 0; c < N; ++c) re[c] = im[c] = DSa{0.f, 0.f};
+  for (int64_t i = r0; i < r1; ++i) {
+    const float2 ah = Ahi[i * lda + j], al = Alo[i * lda + j];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const float2 vh = Vh[i * N + c], vl = Vl[i * N + c];
+      dsa_acc(re[c], ah.x, vh.x);
+      dsa_acc(re[c], -ah.y, vh.y);
+      dsa_acc(im[c], ah.x, vh.y);
+      dsa_acc(im[c], ah.y, vh.x);
+      re[c].lo += (ah.x * vl.x - ah.y * vl.y) + (al.x * vh.x - al.y * vh.y);
+      im[c].lo += (ah.x * vl.y + ah.y * vl.x) + (al.x * vh.y + al.y * vh.x);
+    }
+  }
+  for (int c = 0; c < N; ++c)
+    part[((int64_t)blockIdx.y * n + j) * N + c] =
+        make_double2((double)re[c].hi + (double)re[c].lo, (double)im[c].hi + (double)im[c].lo);
+}
+
+__global__ void k_parts_sum(const double2* part, int chunks, int64_t count, double2* y, int accumulate) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  double2 sm = accumulate ? y[i] : cx(0, 0);
+  for (int q = 0; q < chunks; ++q) sm = cadd(sm, part[q * count + i]);
+  y[i] = sm;
+}
+
+// hi / lo complex64 planes of a strided complex128 source: dst[i][c] = src[i * stride + off + c]
+__global__ void k_split_strided(const double2* src, int64_t n, int stride, int off, int N, float2* hi, float2* lo) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * N) return;
+  const int64_t i = t / N;
+  const int c = (int)(t % N);
+  const double2 v = src[i * stride + off + c];
+  const float2 h = make_float2((float)v.x, (float)v.y);
+  hi[t] = h;
+  lo[t] = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
+}
+
+// r = w - [y1 ; y2] in the unknown layout (sig1 [n], h1 [n][3], sig2 [n], h2 [n][3]);
+// y1, y2 [n][4] = (sig, h); w has zero sig1 / h1; norms[0] += |r|^2
+__global__ void k_adj_resid(int64_t n, const double2* y1, const double2* y2, const double2* ws2, const double2* wh2,
+                            double2* rs1, double2* rh1, double2* rs2, double2* rh2, double* norms) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (i < n) {
+    double2 v = cscl(y1[4 * i], -1.0);
+    rs1[i] = v;
+    acc += cabs2(v);
+    v = csub(ws2[i], y2[4 * i]);
+    rs2[i] = v;
+    acc += cabs2(v);
+    for (int c = 0; c < 3; ++c) {
+      v = cscl(y1[4 * i + 1 + c], -1.0);
+      rh1[3 * i + c] = v;
+      acc += cabs2(v);
+      v = csub(wh2[3 * i + c], y2[4 * i + 1 + c]);
+      rh2[3 * i + c] = v;
+      acc += cabs2(v);
+    }
+  }
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(norms, acc);
+}
+
 }  // namespace
 
 void adj_transpose(double2* A, int64_t n, int64_t ld, cudaStream_t st) {
   dim3 g((unsigned)cdiv_up(n, 32), (unsigned)cdiv_up(n, 32));
-  k_transpose_sq<<<g, dim3(32, 8), 0, st>>>(A, n, ld);
+  k_transpose_sq<double2><<<g, dim3(32, 8), 0, st>>>(A, n, ld);
+}
+void adj_transpose(float2* A, int64_t n, int64_t ld, cudaStream_t st) {
+  dim3 g((unsigned)cdiv_up(n, 32), (unsigned)cdiv_up(n, 32));
+  k_transpose_sq<float2><<<g, dim3(32, 8), 0, st>>>(A, n, ld);
 }
 
 void adj_rhs(const AdjParams& p, const double* pol, const double* dir, double2* gs2, double2* gh2, cudaStream_t st) {
@@ -792,6 +917,33 @@ void adj_rhs_sca(const AdjParams& p, const double2* fields, const double* inf_nv
 void adj_chain_step(const AdjParams& p, int mode, const double2* a, const double2* b, double2* o1, double2* o2,
                     const double2* c, cudaStream_t st) {
   k_adj_chain<<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, mode, a, b, o1, o2, c);
+}
+
+template <typename C>
+void adj_chainT(const AdjParams& p, int mode, const C* a, const C* b, C* o1, C* o2, const C* c, const C* d,
+                cudaStream_t st) {
+  k_chainT<C><<<(unsigned)cdiv_up(p.n, 128), 128, 0, st>>>(p, mode, a, b, o1, o2, c, d);
+}
+template void adj_chainT<float2>(const AdjParams&, int, const float2*, const float2*, float2*, float2*,
+                                 const float2*, const float2*, cudaStream_t);
+template void adj_chainT<double2>(const AdjParams&, int, const double2*, const double2*, double2*, double2*,
+                                  const double2*, const double2*, cudaStream_t);
+
+void adj_gemm_t_ds(int64_t n, const float2* Ahi, const float2* Alo, int64_t lda, const double2* V, int stride,
+                   int off, float2* vsplit, double2* part, int chunks, double2* y, cudaStream_t st, bool accumulate) {
+  const int N = 4;
+  float2* Vh = vsplit;
+  float2* Vl = vsplit + n * N;
+  k_split_strided<<<(unsigned)cdiv_up(n * N, 256), 256, 0, st>>>(V, n, stride, off, N, Vh, Vl);
+  const int64_t rpc = cdiv_up(n, (int64_t)chunks);
+  dim3 g((unsigned)cdiv_up(n, 128), (unsigned)chunks);
+  k_gemm_t_ds<4><<<g, 128, 0, st>>>(n, rpc, Ahi, Alo, lda, Vh, Vl, part);
+  k_parts_sum<<<(unsigned)cdiv_up(n * N, 256), 256, 0, st>>>(part, chunks, n * N, y, accumulate ? 1 : 0);
+}
+
+void adj_resid(int64_t n, const double2* y1, const double2* y2, const double2* ws2, const double2* wh2, double2* rs1,
+               double2* rh1, double2* rs2, double2* rh2, double* norms, cudaStream_t st) {
+  k_adj_resid<<<(unsigned)cdiv_up(n, 128), 128, 0, st>>>(n, y1, y2, ws2, wh2, rs1, rh1, rs2, rh2, norms);
 }
 
 void adj_weights(const AdjParams& p, const double2* lphi, const double2* la, const double2* lDe,

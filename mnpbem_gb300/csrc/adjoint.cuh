@@ -44,6 +44,18 @@ struct AdjParams {
 };
 
 void adj_transpose(double2* A, int64_t n, int64_t ld, cudaStream_t st);
+void adj_transpose(float2* A, int64_t n, int64_t ld, cudaStream_t st);
+// general elementwise steps of the transposed chain (see adjoint.cu)
+template <typename C>
+void adj_chainT(const AdjParams& p, int mode, const C* a, const C* b, C* o1, C* o2, const C* c, const C* d,
+                cudaStream_t st);
+// y [n][4] = (Ahi + Alo)^T V in double-single arithmetic, V[i][c] = src[i * stride + off + c]
+// (vsplit: 8 n complex64 scratch, part: chunks * 4 n complex128 scratch)
+void adj_gemm_t_ds(int64_t n, const float2* Ahi, const float2* Alo, int64_t lda, const double2* V, int stride,
+                   int off, float2* vsplit, double2* part, int chunks, double2* y, cudaStream_t st, bool accumulate);
+// r = w - A^T lam from the two sides' products y1, y2 ([n][4]); norms[0] += |r|^2
+void adj_resid(int64_t n, const double2* y1, const double2* y2, const double2* ws2, const double2* wh2, double2* rs1,
+               double2* rh1, double2* rs2, double2* rh2, double* norms, cudaStream_t st);
 // dJ/dx of ext (adj_rhs) or sca (adj_rhs_sca, which also adds the explicit
 // far-field terms of sca to the position / area accumulators)
 void adj_rhs(const AdjParams& p, const double* pol, const double* dir, double2* gs2, double2* gh2, cudaStream_t st);

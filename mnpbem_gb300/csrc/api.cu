@@ -131,7 +131,7 @@ struct mnpbem_geom {
   int64_t nverts = 0;
   bool all_closed = true;
   DevBuf d_part, d_src, d_nrm, d_srcf, d_nrmf, face_med, exbuf;
-  DevBuf adj, adj_mats, adj_off;   // adjoint gradient workspace
+  DevBuf adj, adj2, adj_mats, adj_off;   // adjoint gradient workspace
   int adj_noff = -1;
   int64_t ld = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
@@ -1498,6 +1498,43 @@ mnpbem_status run_jobs(std::vector<Job>& jobs) {
   return MNPBEM_OK;
 }
 
+// A^{-T} applied through the transposed chain of mldivide.m (matrices M
+// already transposed in place: G1i^T, G2i^T, Sigmai^T, Deltai^T, Sigma1^T):
+// unknown-space input (gs1, gh1 may be null: zero), equation-space output
+// lam = [phi (n) | a (3n) | De (n) | alpha (3n)]; work holds 11 n values
+template <typename R>
+mnpbem_status chain_transpose(const AdjParams& p, cplx<R>* const* M, int64_t ld, const cplx<R>* gs1,
+                              const cplx<R>* gh1, const cplx<R>* gs2, const cplx<R>* gh2, cplx<R>* lam,
+                              cplx<R>* work, cudaStream_t st) {
+  using Cx = cplx<R>;
+  const int64_t n = p.n;
+  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
+  Cx *lphi = lam, *la = lam + n, *lDe = lam + 4 * n, *lal = lam + 5 * n;
+  Cx *gS2 = work, *gH2p = work + n, *v3 = work + 4 * n, *tS1 = work + 7 * n, *ga0 = work + 8 * n;
+  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[1], ld, gs2, 1, zero, gS2, 1, st));        // G2i^T w_sig2
+  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[1], ld, gh2, 3, zero, gH2p, 3, st));       // G2i^T w_h2
+  if (gs1) {
+    MNP_TRY(gemm_simt<R>(n, 1, n, one, M[0], ld, gs1, 1, zero, lphi, 1, st));     // G1i^T w_sig1
+    MNP_TRY(gemm_simt<R>(n, 1, n, one, M[0], ld, gs1, 1, one, gS2, 1, st));
+  } else {
+    MNP_CUDA(cudaMemsetAsync(lphi, 0, sizeof(Cx) * n, st));
+  }
+  if (gh1) {
+    MNP_TRY(gemm_simt<R>(n, 3, n, one, M[0], ld, gh1, 3, zero, ga0, 3, st));      // G1i^T w_h1
+    MNP_TRY(gemm_simt<R>(n, 3, n, one, M[0], ld, gh1, 3, one, gH2p, 3, st));
+  }
+  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[3], ld, gH2p, 3, zero, lal, 3, st));       // Deltai^T
+  adj_chainT<Cx>(p, 0, lal, nullptr, gS2, nullptr, nullptr, nullptr, st);
+  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[2], ld, gS2, 1, zero, lDe, 1, st));        // Sigmai^T
+  adj_chainT<Cx>(p, 1, lDe, nullptr, v3, nullptr, nullptr, nullptr, st);
+  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[3], ld, v3, 3, one, lal, 3, st));          // += Deltai^T v
+  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[4], ld, lDe, 1, zero, tS1, 1, st));        // Sigma1^T
+  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[4], ld, lal, 3, zero, la, 3, st));
+  adj_chainT<Cx>(p, 2, tS1, lal, lphi, la, lDe, gh1 ? ga0 : nullptr, st);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1559,10 +1596,6 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
     set_error("mnpbem_cross_section_gradient: invalid arguments");
     return MNPBEM_ERR_INVALID_ARG;
   }
-  if (precision != MNPBEM_FP64) {
-    set_error("mnpbem_ext_gradient: only MNPBEM_FP64 is implemented");
-    return MNPBEM_ERR_UNSUPPORTED;
-  }
   if (G->nparts != 1 || !G->all_closed || G->inout[0] == G->inout[1] || exc->medium != G->inout[1]) {
     set_error("mnpbem_ext_gradient: one closed particle excited from its outside medium is required");
     return MNPBEM_ERR_UNSUPPORTED;
@@ -1580,7 +1613,7 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
   MNP_TRY(job_setup(j, exc, 1, &enei, eps_media, nmed, precision, nullptr, &sol));
   Lane& L = *G->lanes[0];
   cudaStream_t st = L.st;
-  // forward solve (FP64, direct) on lane 0
+  // forward solve (direct) on lane 0: FP64, or complex64 with FP64-class refinement
   MNP_TRY(upload_lp(G, L, j.s, 0));
   L.w = 0;
   MNP_TRY(solve_one(G, L, j.c, j.s.ref, false, &L.iters, &L.res));
@@ -1607,9 +1640,9 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
   MNP_TRY(G->adj.ensure(cs * (nvec_c + 24 * (size_t)n) + sizeof(double) * (nacc + (size_t)n) + 256));
   MNP_TRY(G->adj_mats.ensure(cs * 3 * (size_t)n * ld));
   double2* V = G->adj.as<double2>();
-  double2 *gs2 = V, *gh2 = gs2 + n, *gS2 = gh2 + 3 * n, *gH2p = gS2 + n, *gAl = gH2p + 3 * n, *gDe = gAl + 3 * n;
-  double2 *v3b = gDe + n, *tS1 = v3b + 3 * n, *ga = tS1 + n, *gphi = ga + 3 * n;
-  double2 *GX1 = gphi + n, *GX2 = GX1 + 4 * n, *HX1 = GX2 + 4 * n;   // 40 n in total
+  double2 *gs2 = V, *gh2 = gs2 + n, *lam = gh2 + 3 * n, *work = lam + 8 * n;     // 1 + 3 + 8 + 11 n
+  double2 *GX1 = work + 11 * n, *GX2 = GX1 + 4 * n, *HX1 = GX2 + 4 * n;          // 32 n
+  double2 *gphi = lam, *ga = lam + n, *gDe = lam + 4 * n, *gAl = lam + 5 * n;
   double2* Ub = V + nvec_c;
   double2* Xb = Ub + 16 * n;
   double* acc = reinterpret_cast<double*>(Xb + 8 * n);
@@ -1634,38 +1667,82 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
   double* geps = p.gk1 + 2;
   const double* pol_d = G->exbuf.as<double>() + 3 * ipol;
   const double* dir_d = G->exbuf.as<double>() + 3 * P + 3 * ipol;
-  // ---- adjoint solve A^T lam = dJ/dx through the transposed chain of mldivide.m
-  double2* M[5];
-  for (int q = 0; q < 5; ++q) {
-    M[q] = L.mat[q].as<double2>();
-    adj_transpose(M[q], n, ld, st);   // G1i, G2i, Sigmai, Deltai, Sigma1 -> transposes
-  }
-  MNP_CHECK_LAUNCH();
+  Vec64 vv = vec64(G, L, P);
+  // ---- right-hand side w = dJ/dx (sig2, h2; zero on sig1, h1)
   if (which == 0) {
     adj_rhs(p, pol_d, dir_d, gs2, gh2, st);
   } else {
     const double* inf_nvec = G->exbuf.as<double>() + 6 * P;
     const double* inf_area = inf_nvec + 3 * exc->ninf;
-    adj_rhs_sca(p, L.fields.as<double2>(), inf_nvec, inf_area, exc->ninf, P, ipol, lp.nb1.x, vec64(G, L, P).x2,
-                gs2, gh2, st);
+    adj_rhs_sca(p, L.fields.as<double2>(), inf_nvec, inf_area, exc->ninf, P, ipol, lp.nb1.x, vv.x2, gs2, gh2, st);
   }
-  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
-  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[1], ld, gs2, 1, zero, gS2, 1, st));     // G2i^T w_sig2
-  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[1], ld, gh2, 3, zero, gH2p, 3, st));    // G2i^T w_h2
-  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[3], ld, gH2p, 3, zero, gAl, 3, st));    // Deltai^T
-  adj_chain_step(p, 0, gAl, nullptr, gS2, nullptr, nullptr, st);
-  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[2], ld, gS2, 1, zero, gDe, 1, st));     // Sigmai^T
-  adj_chain_step(p, 1, gDe, nullptr, v3b, nullptr, nullptr, st);
-  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[3], ld, v3b, 3, one, gAl, 3, st));      // += Deltai^T v
-  MNP_TRY(gemm_simt<double>(n, 1, n, one, M[4], ld, gDe, 1, zero, tS1, 1, st));     // Sigma1^T
-  MNP_TRY(gemm_simt<double>(n, 3, n, one, M[4], ld, gAl, 3, zero, ga, 3, st));
-  adj_chain_step(p, 2, tS1, gAl, gphi, ga, gDe, st);
   MNP_CHECK_LAUNCH();
+  // ---- adjoint solve A^T lam = w through the transposed chain of mldivide.m
+  if (precision == MNPBEM_FP64) {
+    double2* M[5];
+    for (int q = 0; q < 5; ++q) {
+      M[q] = L.mat[q].as<double2>();
+      adj_transpose(M[q], n, ld, st);   // G1i, G2i, Sigmai, Deltai, Sigma1 -> transposes
+    }
+    MNP_CHECK_LAUNCH();
+    MNP_TRY(chain_transpose<double>(p, M, ld, nullptr, nullptr, gs2, gh2, lam, work, st));
+  } else {
+    // complex64 transposed chain as the preconditioner of a refinement on the
+    // FP64-class operator: r = w - A^T lam with A^T lam = [G1^T U_G1 + H1^T U_H1 ;
+    // G2^T U_G2 + H2^T U_H2] (the weights U of lam), products of the hi / lo
+    // planes in double-single arithmetic
+    float2* M[5];
+    for (int q = 0; q < 5; ++q) {
+      M[q] = L.mat[q].as<float2>();
+      adj_transpose(M[q], n, ld, st);
+    }
+    const int chunks = 32;
+    MNP_TRY(G->adj2.ensure(cs * (8 * (size_t)n + 8 * (size_t)n + chunks * 4 * (size_t)n) +
+                           sizeof(float2) * (8 * (size_t)n + 8 * (size_t)n + 11 * (size_t)n + 8 * (size_t)n) +
+                           sizeof(double) * 4 + 256));
+    double2* r64 = G->adj2.as<double2>();                 // unknown layout: sig1 | h1 | sig2 | h2
+    double2* y12 = r64 + 8 * n;                            // y1 [n][4], y2 [n][4]
+    double2* part = y12 + 8 * n;
+    float2* r32 = reinterpret_cast<float2*>(part + chunks * 4 * n);
+    float2* dl32 = r32 + 8 * n;
+    float2* w32 = dl32 + 8 * n;
+    float2* vsplit = w32 + 11 * n;
+    double* nrm = reinterpret_cast<double*>(vsplit + 8 * n);
+    const float2* hl[4];
+    for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
+    MNP_CUDA(cudaMemsetAsync(lam, 0, cs * 8 * n, st));
+    MNP_CUDA(cudaMemsetAsync(r64, 0, cs * 4 * n, st));
+    MNP_CUDA(cudaMemcpyAsync(r64 + 4 * n, gs2, cs * n, cudaMemcpyDeviceToDevice, st));
+    MNP_CUDA(cudaMemcpyAsync(r64 + 5 * n, gh2, cs * 3 * n, cudaMemcpyDeviceToDevice, st));
+    const double tol = 1e-10;
+    for (int it = 0; it < 20; ++it) {
+      launch_cvt_d2f(r64, r32, 8 * n, st);
+      MNP_CHECK_LAUNCH();
+      MNP_TRY(chain_transpose<float>(p, M, ld, r32, r32 + n, r32 + 4 * n, r32 + 5 * n, dl32, w32, st));
+      MNP_CUDA(cudaMemsetAsync(nrm, 0, sizeof(double) * 4, st));
+      launch_axpy_norm(lam, dl32, 8 * n, nrm, st);
+      MNP_CHECK_LAUNCH();
+      double hn[4];
+      MNP_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+      MNP_CUDA(cudaStreamSynchronize(st));
+      if (!(hn[0] == hn[0])) { set_error("adjoint refinement produced NaN"); return MNPBEM_ERR_NOT_CONVERGED; }
+      if (sqrt(hn[0]) <= tol * sqrt(hn[1])) break;
+      // residual with the weights of the current lam
+      adj_weights(p, gphi, ga, gDe, gAl, vv.x1, vv.x2, P, ipol, st);
+      adj_gemm_t_ds(n, hl[0], hl[0] + n * ld, ld, Ub, 16, 0, vsplit, part, chunks, y12, st, false);
+      adj_gemm_t_ds(n, hl[1], hl[1] + n * ld, ld, Ub, 16, 4, vsplit, part, chunks, y12, st, true);
+      adj_gemm_t_ds(n, hl[2], hl[2] + n * ld, ld, Ub, 16, 8, vsplit, part, chunks, y12 + 4 * n, st, false);
+      adj_gemm_t_ds(n, hl[3], hl[3] + n * ld, ld, Ub, 16, 12, vsplit, part, chunks, y12 + 4 * n, st, true);
+      adj_resid(n, y12, y12 + 4 * n, gs2, gh2, r64, r64 + n, r64 + 4 * n, r64 + 5 * n, nrm + 2, st);
+      MNP_CHECK_LAUNCH();
+    }
+    MNP_TRY(tc_check_error(L.tc, st));
+  }
   // ---- weights, then G1 [sig1 h1], G2 [sig2 h2], H1 sig1 from freshly assembled FP64 matrices
-  Vec64 vv = vec64(G, L, P);
   adj_weights(p, gphi, ga, gDe, gAl, vv.x1, vv.x2, P, ipol, st);
   MNP_CHECK_LAUNCH();
   {
+    const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
     AsmParams ap = base_params(G, L.lp_dev.as<LamParams>());
     double2* AM = G->adj_mats.as<double2>();
     ap.ld64 = ld;

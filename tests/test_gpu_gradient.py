@@ -94,3 +94,17 @@ def test_autograd_gradcheck(gpu_lib):
     eps = torch.tensor([EPS_IN.real, EPS_IN.imag], dtype=torch.float64, requires_grad=True)
     fn = lambda vv, ee: extinction(vv, ee, f, 520.0)
     assert torch.autograd.gradcheck(fn, (verts, eps), eps=1e-5, atol=1e-6, rtol=1e-4, nondet_tol=1e-12)
+
+
+@pytest.mark.parametrize("which", ["ext", "sca"])
+def test_mixed_precision_gradient_matches_fp64(gpu_lib, which):
+    """complex64 forward / transposed solves with FP64-class refinement give
+    the FP64 gradient on the 2016-face rod to 1e-7 (max |diff| / max |ref|)."""
+    v, f = shapes.trirod(10.0, 40.0, (25, 7, 32), triangles=True)
+    exc = m.planewave([[0, 0, 1.0]], [[1.0, 0, 0]])
+    b = solver(v, f)
+    v64, g64, e64 = b.cross_section_gradient(exc, 650.0, 0, which, "fp64")
+    vmx, gmx, emx = b.cross_section_gradient(exc, 650.0, 0, which, "mixed")
+    assert abs(vmx - v64) / abs(v64) < 1e-9
+    assert np.max(np.abs(gmx - g64)) / np.max(np.abs(g64)) < 1e-7
+    assert abs(emx - e64) / abs(e64) < 1e-7
