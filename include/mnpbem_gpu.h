@@ -269,7 +269,9 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
 /* Tuning options of a handle (the autotuner of mnpbem_gb300/autotune.py picks
  * them per problem size): "lanes" (0..16), "gj_block" (Gauss-Jordan step of
  * the tensor-core inversions: 256 or 512), "tc_stages" (TMA pipeline depth of
- * the tensor-core GEMM: 3 or 4), "tf32_round" (round A operands to nearest
+ * the tensor-core GEMM: 3 or 4), "tc_ctas" (CTAs of the persistent
+ * tensor-core GEMM, 0 = one per SM; fewer leave SMs to the pivot-block
+ * clusters of other lanes), "tf32_round" (round A operands to nearest
  * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
  * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
  * No counterpart in the reference.                                          */

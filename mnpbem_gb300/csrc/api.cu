@@ -140,6 +140,7 @@ struct mnpbem_geom {
   bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
   bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
   int tc_stages = 0;        // pipeline depth of the tensor-core GEMM (0: its default)
+  int tc_ctas = 0;          // CTAs of the persistent tensor-core GEMM (0: one per SM)
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -200,6 +201,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
   }
   L->status_host[0] = L->status_host[1] = 0;
   if (G->tc_stages) L->tc.stages = G->tc_stages;
+  L->tc.max_ctas = G->tc_ctas;
   G->lanes.push_back(std::move(L));
   return MNPBEM_OK;
 }
@@ -413,6 +415,11 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
   if (k == "tc_stages" && (value == 3 || value == 4)) {
     g->tc_stages = value;
     for (auto& L : g->lanes) L->tc.stages = value;
+    return MNPBEM_OK;
+  }
+  if (k == "tc_ctas" && value >= 0 && value <= 4096) {
+    g->tc_ctas = value;
+    for (auto& L : g->lanes) L->tc.max_ctas = value;
     return MNPBEM_OK;
   }
   if (k == "tf32_round" && (value == 0 || value == 1)) { g->tf32_rna = value != 0; return MNPBEM_OK; }
@@ -675,6 +682,11 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   gj(L.gj64);
   mix(L.status_host, 0);
   mix(L.norms_host, 0);
+  // tuning options baked into the captured launches
+  mix(nullptr, (size_t)L.tc.stages);
+  mix(nullptr, (size_t)L.tc.max_ctas);
+  mix(nullptr, (size_t)G->tf32_rna);
+  mix(nullptr, (size_t)G->asm_ds);
   return h;
 }
 

@@ -462,7 +462,9 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
   if (MT * NT >= (1ll << 31)) { set_error("tc_gemm_c64: too many tiles"); return MNPBEM_ERR_INVALID_ARG; }
   MNP_TRY(c.ctr.ensure(sizeof(int)));
   MNP_CUDA(cudaMemsetAsync(c.ctr.ptr, 0, sizeof(int), st));
-  const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, c.num_sms > 0 ? c.num_sms : 148);
+  int ctas = c.num_sms > 0 ? c.num_sms : 148;
+  if (c.max_ctas > 0 && c.max_ctas < ctas) ctas = c.max_ctas;
+  const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, ctas);
   {
     ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));

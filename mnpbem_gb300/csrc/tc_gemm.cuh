@@ -14,6 +14,8 @@ struct TcGemmCtx {
   DevBuf ctr;             // tile counter of the persistent kernel (zeroed before each launch)
   int num_sms = 0;
   int stages = 4;         // pipeline depth of the persistent kernel (3 or 4)
+  int max_ctas = 0;       // CTAs of the persistent kernel (0: one per SM); fewer leave SMs
+                          // to the pivot-block clusters of other wavelengths in flight
   void* encode_fn = nullptr;
 };
 
