@@ -224,9 +224,12 @@ MNPBEM_API mnpbem_status mnpbem_profile_read(mnpbem_geom* g, int32_t phase, doub
 
 /* Complex64 GEMM C = alpha A B + beta C on host buffers (row-major, interleaved
  * complex, leading dimensions in elements): path 0 = CUDA-core kernel, path 1 =
- * tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation).  The building
- * block of the inversions and products of initmat.m (MATLAB mtimes on complex
- * matrices); beta must be real for path 1.                                   */
+ * tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation), path 2 = the
+ * same on CTA pairs (cta_group::2, 256 x 256 tiles; M >= 256, else path 1)
+ * with a TMA store / reduce-add epilogue, path 3 = CTA pairs with vector
+ * stores / reductions from the load-store path.
+ * The building block of the inversions and products of initmat.m (MATLAB
+ * mtimes on complex matrices); beta must be real for paths 1 and 2.          */
 MNPBEM_API mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N,
                                          int64_t K, const float* alpha, const float* A,
                                          int64_t lda, const float* B, int64_t ldb,
@@ -271,7 +274,9 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
  * the tensor-core inversions: 256 or 512), "tc_stages" (TMA pipeline depth of
  * the tensor-core GEMM: 3 or 4), "tc_ctas" (CTAs of the persistent
  * tensor-core GEMM, 0 = one per SM; fewer leave SMs to the pivot-block
- * clusters of other lanes), "tf32_round" (round A operands to nearest
+ * clusters of other lanes), "tc_pair" (CTA-pair tensor-core GEMM with
+ * 256 x 256 tiles for products of at least 256 rows: 0 never (default),
+ * 1 always, -1 products with K >= 1024), "tf32_round" (round A operands to nearest
  * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
  * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
  * No counterpart in the reference.                                          */

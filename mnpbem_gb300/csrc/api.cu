@@ -141,6 +141,7 @@ struct mnpbem_geom {
   bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
   int tc_stages = 0;        // pipeline depth of the tensor-core GEMM (0: its default)
   int tc_ctas = 0;          // CTAs of the persistent tensor-core GEMM (0: one per SM)
+  int tc_pair = 0;          // CTA-pair tensor-core GEMM: 1 always, 0 off, -1 long-K products
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -202,6 +203,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
   L->status_host[0] = L->status_host[1] = 0;
   if (G->tc_stages) L->tc.stages = G->tc_stages;
   L->tc.max_ctas = G->tc_ctas;
+  L->tc.pair = G->tc_pair;
   G->lanes.push_back(std::move(L));
   return MNPBEM_OK;
 }
@@ -417,6 +419,11 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
     for (auto& L : g->lanes) L->tc.stages = value;
     return MNPBEM_OK;
   }
+  if (k == "tc_pair" && value >= -1 && value <= 1) {
+    g->tc_pair = value;
+    for (auto& L : g->lanes) L->tc.pair = value;
+    return MNPBEM_OK;
+  }
   if (k == "tc_ctas" && value >= 0 && value <= 4096) {
     g->tc_ctas = value;
     for (auto& L : g->lanes) L->tc.max_ctas = value;
@@ -564,7 +571,7 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
                               const float* alpha, const float* A, int64_t lda, const float* B,
                               int64_t ldb, const float* beta, float* C, int64_t ldc) {
   if (M <= 0 || N <= 0 || K <= 0 || !alpha || !beta || !A || !B || !C || lda < K || ldb < N ||
-      ldc < N || (path != 0 && path != 1)) {
+      ldc < N || path < 0 || path > 3) {
     set_error("mnpbem_gemm_c64: invalid arguments");
     return MNPBEM_ERR_INVALID_ARG;
   }
@@ -582,7 +589,9 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
   MNP_CUDA(cudaMemcpyAsync(dB.ptr, B, sizeof(float2) * K * ldb, cudaMemcpyHostToDevice, st));
   MNP_CUDA(cudaMemcpyAsync(dC.ptr, C, sizeof(float2) * M * ldc, cudaMemcpyHostToDevice, st));
   const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
-  if (path == 1) {
+  if (path >= 1) {
+    tc[device].pair = path >= 2 ? 1 : 0;
+    tc[device].pair_epi = path == 3 ? 1 : 0;
     if (!tc_gemm_eligible(tc[device], M, N, K, dA.ptr, lda, dC.ptr, ldc, be)) {
       set_error("tensor-core GEMM not available for this device or shape");
       return MNPBEM_ERR_UNSUPPORTED;
@@ -685,6 +694,7 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   // tuning options baked into the captured launches
   mix(nullptr, (size_t)L.tc.stages);
   mix(nullptr, (size_t)L.tc.max_ctas);
+  mix(nullptr, (size_t)(L.tc.pair + 1));
   mix(nullptr, (size_t)G->tf32_rna);
   mix(nullptr, (size_t)G->asm_ds);
   return h;
@@ -819,6 +829,7 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   MNP_CHECK_LAUNCH();
   MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
   if (direct && ctx) MNP_TRY(tc_check_error(L.tc, L.st));
+  if (direct) MNP_TRY(thin_stream_check(L.st));
   return MNPBEM_OK;
 }
 
@@ -1488,6 +1499,7 @@ mnpbem_status job_finish(Job& j, bool failed) {
     MNP_TRY(check_pivots(L));
     if (j.c.precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(L.tc, L.st));
   }
+  MNP_TRY(thin_stream_check(G->st));
   return MNPBEM_OK;
 }
 
@@ -1749,6 +1761,7 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
       MNP_CHECK_LAUNCH();
     }
     MNP_TRY(tc_check_error(L.tc, st));
+    MNP_TRY(thin_stream_check(st));
   }
   // ---- weights, then G1 [sig1 h1], G2 [sig2 h2], H1 sig1 from freshly assembled FP64 matrices
   adj_weights(p, gphi, ga, gDe, gAl, vv.x1, vv.x2, P, ipol, st);

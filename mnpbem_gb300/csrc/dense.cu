@@ -11,6 +11,7 @@
 #include <cooperative_groups.h>
 
 #include "dense.cuh"
+#include "mbarrier.cuh"
 #include "profile.cuh"
 
 namespace mnpbem {
@@ -379,6 +380,225 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_hi(int64_t M, int64
   }
 }
 
+// ------------------------------------------- streamed thin GEMM (bulk copies)
+// C[M x N] = A[M x K] * B[K x N], N <= 4, for a complex64 A far larger than
+// L2 (the chain products and FP32 residuals of the refinement read a whole
+// n x n matrix for a few right-hand sides: pure HBM streaming).  One CTA per
+// SM owns a contiguous, balanced share of the rows.  A producer warp streams
+// row segments of TS_KC complex values with bulk copies (cp.async.bulk: long
+// sequential requests, TS_ST stages in flight) into shared memory; eight
+// consumer warps take the chunk's k range in parallel (lane = k), read B
+// through L1 and accumulate TS_TR rows x N in registers; at the end of a row
+// block the warps' partial sums are added in a fixed order (deterministic).
+// Waits are bounded; after a timeout every role skips the remaining waits
+// (the result is then garbage and the error word is set) so that no barrier
+// is left waiting.
+constexpr int TS_TR = 8, TS_KC = 512, TS_ST = 4, TS_CW = 8;
+constexpr int TS_THREADS = 32 * (TS_CW + 1);
+constexpr int TS_STAGE = TS_TR * TS_KC * 8;               // 32 KB
+constexpr int TS_SMEM = TS_ST * TS_STAGE;
+__device__ int g_thin_stream_err;
+
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(32 * TS_CW) : "memory");
+}
+
+// MODE 0: C (complex64) = alpha A B + beta C;  MODE 1: C (complex128) = A B
+template <int N, int MODE>
+__global__ void __launch_bounds__(TS_THREADS, 1)
+    k_gemm_thin_stream(int64_t M, int64_t K, const float2* __restrict__ A, int64_t lda, const float2* __restrict__ B,
+                       int64_t ldb, float2 alpha, float2 beta, void* __restrict__ Cv, int64_t ldc) {
+  extern __shared__ __align__(128) unsigned char ts_smem[];
+  __shared__ __align__(8) unsigned long long bars[2 * TS_ST];
+  __shared__ float2 red[TS_CW][TS_TR][N];
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rb = M * blockIdx.x / gridDim.x, re = M * (blockIdx.x + 1) / gridDim.x;
+  const int64_t nchunk = (K + TS_KC - 1) / TS_KC;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[TS_ST]);
+  const uint32_t sbase = smem_u32(ts_smem);
+  int* err = &g_thin_stream_err;
+  volatile int* abort_v = &abort_flag;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TS_ST; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, TS_CW);
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (warp == TS_CW) {
+    // ---------------- producer: row segments of the CTA's rows, block by block
+    if (lane == 0) {
+      int it = 0;
+      for (int64_t r0 = rb; r0 < re && !*abort_v; r0 += TS_TR) {
+        const int nr = (int)min((int64_t)TS_TR, re - r0);
+        for (int64_t ch = 0; ch < nchunk; ++ch, ++it) {
+          const int s = it % TS_ST;
+          if (it >= TS_ST && !*abort_v && !mbar_wait(empty0 + 8 * s, ((it / TS_ST) - 1) & 1, err, 1)) *abort_v = 1;
+          if (*abort_v) break;
+          const int64_t k0 = ch * TS_KC;
+          const uint32_t bytes = (uint32_t)min((int64_t)TS_KC, K - k0) * 8u;
+          mbar_expect_tx(full0 + 8 * s, bytes * (uint32_t)nr);
+          for (int r = 0; r < nr; ++r)
+            bulk_copy_g2s(sbase + (uint32_t)(s * TS_STAGE + r * TS_KC * 8), A + (r0 + r) * lda + k0, bytes,
+                          full0 + 8 * s);
+        }
+      }
+      if (*abort_v) {
+        // copies may still be landing: give them time before the CTA exits
+        const unsigned long long t0 = gtimer();
+        while (gtimer() - t0 < 200000ull) {
+        }
+      }
+    }
+  } else {
+    // ---------------- consumers
+    const float2* As = reinterpret_cast<const float2*>(ts_smem);
+    int it = 0;
+    for (int64_t r0 = rb; r0 < re; r0 += TS_TR) {
+      const int nr = (int)min((int64_t)TS_TR, re - r0);
+      float2 acc[TS_TR][N];
+#pragma unroll
+      for (int r = 0; r < TS_TR; ++r)
+#pragma unroll
+        for (int c = 0; c < N; ++c) acc[r][c] = make_float2(0.f, 0.f);
+      for (int64_t ch = 0; ch < nchunk; ++ch, ++it) {
+        const int s = it % TS_ST;
+        if (!*abort_v && !mbar_wait(full0 + 8 * s, (it / TS_ST) & 1, err, 2)) *abort_v = 1;
+        const int64_t k0 = ch * TS_KC;
+        const int kl = (int)min((int64_t)TS_KC, K - k0);
+        const float2* Ast = As + s * (TS_TR * TS_KC);
+#pragma unroll
+        for (int j = 0; j < TS_KC / (32 * TS_CW); ++j) {
+          const int kk = warp * (TS_KC / TS_CW) + 32 * j + lane;
+          if (kk < kl) {
+            float2 b[N];
+#pragma unroll
+            for (int c = 0; c < N; ++c) b[c] = __ldg(B + (k0 + kk) * ldb + c);
+#pragma unroll
+            for (int r = 0; r < TS_TR; ++r) {
+              if (r < nr) {
+                const float2 a = Ast[r * TS_KC + kk];
+#pragma unroll
+                for (int c = 0; c < N; ++c) cfma(acc[r][c], a, b[c]);
+              }
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8 * s);
+      }
+#pragma unroll
+      for (int r = 0; r < TS_TR; ++r)
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          float2 v = acc[r][c];
+#pragma unroll
+          for (int o = 16; o; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+          }
+          if (lane == 0) red[warp][r][c] = v;
+        }
+      consumer_sync();
+      for (int t = threadIdx.x; t < nr * N; t += 32 * TS_CW) {
+        const int r = t / N, c = t % N;
+        float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int w = 0; w < TS_CW; ++w) v = cadd(v, red[w][r][c]);
+        const int64_t row = r0 + r;
+        if (MODE == 0) {
+          float2* C = reinterpret_cast<float2*>(Cv);
+          float2 out = cmul(alpha, v);
+          if (beta.x != 0.f || beta.y != 0.f) out = cadd(out, cmul(beta, C[row * ldc + c]));
+          C[row * ldc + c] = out;
+        } else {
+          reinterpret_cast<double2*>(Cv)[row * ldc + c] = make_double2(v.x, v.y);
+        }
+      }
+      consumer_sync();
+    }
+  }
+  __syncthreads();
+}
+
+static int stream_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+      cudaGetLastError();
+      sms = 148;
+    }
+  }
+  return sms;
+}
+
+// the streamed kernel applies: N <= 4, even K and lda (16-byte row segments),
+// a 16-byte aligned A, and a matrix of at least 2^22 entries.  Measured on
+// GB300 (standalone, complex64): equal to the register-tiled kernel for N = 1,
+// faster for N = 3 at n = 4000 (44 against 61 us), slower for N = 4 at
+// n = 12000 (417 against 305 us); inside the multi-lane sweep at n = 4000 it
+// shortens the thin-product phase by 15 %.  N = 4 uses it up to 2^26 entries.
+static bool thin_stream_ok(int64_t M, int64_t N, int64_t K, const void* A, int64_t lda) {
+  static int enabled = -1;
+  if (enabled < 0) {
+    const char* e = getenv("MNPBEM_THIN_STREAM");
+    enabled = (e && e[0] == '0') ? 0 : 1;
+  }
+  const int64_t mk = M * K;
+  return enabled && N >= 1 && N <= 4 && !(K & 1) && !(lda & 1) && !(reinterpret_cast<uintptr_t>(A) & 15) &&
+         mk >= (int64_t(1) << 22) && (N <= 3 || mk <= (int64_t(1) << 26));
+}
+
+template <int MODE>
+static mnpbem_status launch_thin_stream(int64_t M, int64_t N, int64_t K, const float2* A, int64_t lda,
+                                        const float2* B, int64_t ldb, float2 alpha, float2 beta, void* C,
+                                        int64_t ldc, cudaStream_t st) {
+  static bool attr[2][5] = {};
+  const unsigned grid = (unsigned)std::min<int64_t>(M, stream_sms());
+#define TS_CASE(NN)                                                                                       \
+  case NN:                                                                                                \
+    if (!attr[MODE][NN]) {                                                                                \
+      MNP_CUDA(cudaFuncSetAttribute(k_gemm_thin_stream<NN, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                    TS_SMEM));                                                            \
+      attr[MODE][NN] = true;                                                                              \
+    }                                                                                                     \
+    k_gemm_thin_stream<NN, MODE><<<grid, TS_THREADS, TS_SMEM, st>>>(M, K, A, lda, B, ldb, alpha, beta, C, ldc); \
+    break;
+  switch (N) {
+    TS_CASE(1) TS_CASE(2) TS_CASE(3) TS_CASE(4)
+    default:
+      set_error("thin stream GEMM: N must be 1..4");
+      return MNPBEM_ERR_INVALID_ARG;
+  }
+#undef TS_CASE
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+mnpbem_status thin_stream_check(cudaStream_t st) {
+  int* p = nullptr;
+  MNP_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_thin_stream_err));
+  int h = 0;
+  MNP_CUDA(cudaMemcpyAsync(&h, p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    MNP_CUDA(cudaMemsetAsync(p, 0, sizeof(int), st));
+    set_error("streamed thin GEMM: a bounded pipeline wait expired (code %d)", h);
+    return MNPBEM_ERR_TIMEOUT;
+  }
+  return MNPBEM_OK;
+}
+
 mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
                            float2* bsplit, cudaStream_t st) {
@@ -394,6 +614,8 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
   const unsigned nblk = (unsigned)cdiv_up(M, (int64_t)DS_TR);
   if (!Alo) {
     ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 8.0 * M * K + 8.0 * K * N + 16.0 * M * N);
+    if (thin_stream_ok(M, N, K, Ahi, lda))
+      return launch_thin_stream<1>(M, N, K, Ahi, lda, Bh, N, make_float2(1.f, 0.f), make_float2(0.f, 0.f), C, ldc, st);
 #define HI_CASE(NN)                                                                                \
   case NN:                                                                                         \
     k_gemm_thin_hi<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, lda, Bh, N, C, ldc);            \
@@ -434,6 +656,8 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
     const float2* Bf = reinterpret_cast<const float2*>(B);
     float2* Cf = reinterpret_cast<float2*>(C);
     const float2 al = make_float2((float)alpha.x, (float)alpha.y), be = make_float2((float)beta.x, (float)beta.y);
+    if (N <= 4 && thin_stream_ok(M, N, K, Af, lda))
+      return launch_thin_stream<0>(M, N, K, Af, lda, Bf, ldb, al, be, Cf, ldc, st);
 #define C64_CASE(NN)                                                                                    \
   case NN:                                                                                              \
     k_gemm_thin_c64<NN, 4><<<(unsigned)cdiv_up(M, 4), 32 * THIN_WARPS, 0, st>>>(M, K, al, Af, lda, Bf, ldb, be, Cf, ldc); \

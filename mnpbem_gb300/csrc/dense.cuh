@@ -21,6 +21,10 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
                            float2* bsplit, cudaStream_t st);
 
+// MNPBEM_ERR_TIMEOUT (and the word cleared) if a bounded wait of the streamed
+// thin GEMM expired since the last check; synchronises st
+mnpbem_status thin_stream_check(cudaStream_t st);
+
 // x <- TF32(x) rounded to nearest, in place (count floats)
 void round_tf32(float* x, int64_t count, cudaStream_t st);
 

@@ -21,6 +21,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include "mbarrier.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
 
@@ -33,58 +34,24 @@ constexpr int TC_A_BYTES = TC_BM * TC_BK * 4;   // 16 KB
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 4;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr uint32_t TC_TMEM_COLS = 256;
-constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long TC_WAIT_NS = MBAR_WAIT_NS;
 
 // instruction descriptor: D f32, A/B tf32, K-major A and B, N = 256, M = 128
 constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
                               ((uint32_t)(TC_BM >> 4) << 24);
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  uint64_t state;
-  asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(bar) : "memory");
-  (void)state;
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait; false (and err |= code) when the limit expires
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = gtimer();
-  while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (gtimer() - t0 > TC_WAIT_NS) {
-      atomicOr(err, code);
-      return false;
-    }
-  }
-}
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
       ::"r"(dst), "l"((unsigned long long)map), "r"(bar), "r"(x), "r"(y)
       : "memory");
+}
+// L2 prefetch of one C tile (128 rows x 256 floats, unswizzled map) so that the
+// epilogue's reduce-add finds C in L2 instead of waiting for HBM
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];"
+               ::"l"((unsigned long long)map), "r"(x), "r"(y)
+               : "memory");
 }
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
 __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
@@ -145,11 +112,50 @@ constexpr int TC_STAGE_SMEM = TC_EPI_WARPS * 2 * 4096;   // two 32 x 32 float st
 constexpr int tc_psmem(int stages) { return stages * TC_STAGE_BYTES + TC_STAGE_SMEM + 1024; }
 constexpr int TC_TQ = 4;                                  // tile-index ring slots
 
-template <int ST>
+// One 32 x 32 accumulator chunk (row = lane, r = its 32 columns) stored from
+// the SM's load-store path: transposed through the warp's 4 KB staging tile
+// (row per lane in, eight lanes per 128-byte row out) and written with
+// coalesced vector stores (beta = 0) or vector reductions (beta = 1).  Used
+// where the TMA store cannot be: a row length of 2N floats that is not a
+// multiple of 16 bytes (TMA writes whole 16-byte granules at the right edge).
+__device__ __forceinline__ void epi_chunk_lsu(const uint32_t (&r)[32], float* stage, int lane, float* __restrict__ Cp,
+                                              long long ldcf, int row0, int col0, int M, int N2, int accumulate) {
+  float4* st = reinterpret_cast<float4*>(stage) + lane * 8;
+#pragma unroll
+  for (int c4 = 0; c4 < 8; ++c4)
+    st[c4 ^ (lane & 7)] = make_float4(__uint_as_float(r[4 * c4]), __uint_as_float(r[4 * c4 + 1]),
+                                      __uint_as_float(r[4 * c4 + 2]), __uint_as_float(r[4 * c4 + 3]));
+  __syncwarp();
+  const int q4 = lane & 7, col = col0 + 4 * q4;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int rr = 4 * i + (lane >> 3), grow = row0 + rr;
+    const float4 v = reinterpret_cast<const float4*>(stage)[rr * 8 + (q4 ^ (rr & 7))];
+    if (grow < M && col < N2) {
+      float* dst = Cp + (long long)grow * ldcf + col;
+      if (col + 4 <= N2) {
+        if (accumulate)
+          asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(v.x), "f"(v.y), "f"(v.z),
+                       "f"(v.w)
+                       : "memory");
+        else
+          *reinterpret_cast<float4*>(dst) = v;
+      } else {                                          // N2 is even: a last pair of columns
+        if (accumulate)
+          asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(dst), "f"(v.x), "f"(v.y) : "memory");
+        else
+          *reinterpret_cast<float2*>(dst) = make_float2(v.x, v.y);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+template <int ST, int EPI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-              const __grid_constant__ CUtensorMap mapC, int M, int N2, int K2, int accumulate,
-              int* tile_ctr, int* err) {
+              const __grid_constant__ CUtensorMap mapC, const __grid_constant__ CUtensorMap mapP,
+              float* __restrict__ Cp, long long ldcf, int M, int N2, int K2, int accumulate, int* tile_ctr, int* err) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bars[2 * ST + 4 + 2 * TC_TQ];
   __shared__ int tq[TC_TQ];
@@ -196,15 +202,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       // ---------------- tile scheduler + TMA producer
       int it = 0;
+      // the tile counter is read one tile ahead: the atomic's round trip
+      // overlaps the current tile's copies instead of stalling the pipeline
+      int t_next = atomicAdd(tile_ctr, 1);
       for (int j = 0;; ++j) {
         const int q = j % TC_TQ;
         if (j >= TC_TQ && !mbar_wait(tqe0 + 8 * q, ((j / TC_TQ) - 1) & 1, err, 16)) break;
-        int t = *(volatile int*)err ? -1 : atomicAdd(tile_ctr, 1);
+        int t = *(volatile int*)err ? -1 : t_next;
         if (t >= ntiles) t = -1;
+        if (t >= 0) t_next = atomicAdd(tile_ctr, 1);
         tq[q] = t;
         mbar_arrive(tqf0 + 8 * q);
         if (t < 0) break;
         const int m0 = (t % MT) * TC_BM, n0 = (t / MT) * TC_BN;
+        if (accumulate) tma_prefetch_2d(&mapP, n0, m0);
         bool ok = true;
         for (int kt = 0; kt < KT; ++kt, ++it) {
           const int s = it % ST;
@@ -284,6 +295,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * TC_TMEM_COLS + c * 32), r);
         if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
+        if constexpr (EPI == 1) {
+          epi_chunk_lsu(r, stage_gen, lane, Cp, ldcf, row0, col0, M, N2, accumulate);
+          continue;
+        }
         const int buf = nstores & 1;
         if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
         __syncwarp();
@@ -331,6 +346,332 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_TMEM_COLS) : "memory");
+  }
+}
+
+// ------------------------------------------------------------- CTA-pair kernel
+// The same product with a cluster of two CTAs per 256 x 256 output tile:
+// tcgen05.mma.cta_group::2 (M = 256, N = 256), issued by the even CTA, reads
+// 128 rows of A and 128 rows of B' from the shared memory of each CTA, so a CTA
+// streams 32 KB per K chunk for the tensor work that costs 48 KB in the
+// single-CTA kernel, and 5 or 6 chunks fit in flight.  Each CTA's tensor memory
+// holds its 128 rows of the tile (two 256-column accumulators, allocated for
+// the pair) and its four epilogue warps store them.
+// Signalling across the pair:
+//   full[s]   even CTA, 1 arrival + 64 KB: the TMA copies of both CTAs complete
+//             on the even CTA's barrier (cta_group::2 copies);
+//   empty[s]  each CTA: MMA completion, committed to both CTAs (multicast);
+//   accf[b]   each CTA: accumulator complete, committed to both CTAs;
+//   acce[b]   even CTA, 8 arrivals: the epilogue warps of both CTAs;
+//   tile ring the even CTA's producer takes a tile index from the counter and
+//             writes it into both CTAs' slot; the consumers of both CTAs
+//             release the slot on the even CTA's barrier (10 arrivals).
+// Waits are bounded as in the single-CTA kernel.  Before exiting, each producer
+// waits for the MMA completions of its last stages (so that no commit arrives in
+// shared memory of an exited CTA), and both CTAs meet at a cluster barrier.
+constexpr int TP_ROWS = 128;                          // A and B' rows per CTA and K chunk
+constexpr int TP_A_BYTES = TP_ROWS * TC_BK * 4;       // 16 KB
+constexpr int TP_B_BYTES = TP_ROWS * TC_BK * 4;       // 16 KB
+constexpr int TP_STAGE_BYTES = TP_A_BYTES + TP_B_BYTES;
+constexpr int TP_TILE = 2 * TP_ROWS;
+constexpr uint32_t TP_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TP_TILE >> 3) << 17) |
+                              ((uint32_t)(TP_TILE >> 4) << 24);
+constexpr int tp_psmem(int stages, int nbuf) { return stages * TP_STAGE_BYTES + TC_EPI_WARPS * nbuf * 4096 + 1024; }
+static_assert(tp_psmem(6, 2) <= 232448 && tp_psmem(5, 4) <= 232448, "pair kernel shared memory");
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared::cluster address of the same shared-memory offset in CTA `rank`
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t caddr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+__device__ __forceinline__ void st_cluster_u32(uint32_t caddr, uint32_t v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(caddr), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cl(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait on a barrier that receives arrivals from the other CTA
+__device__ __forceinline__ bool mbar_wait_cl(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try_wait_cl(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    if (mbar_try_wait_cl(bar, parity)) return true;
+    if (gtimer() - t0 > TC_WAIT_NS) {
+      atomicOr(err, code);
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// TMA copy into this CTA's shared memory, completing on the even CTA's barrier
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, uint32_t cbar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(dst), "l"((unsigned long long)map), "r"(cbar), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void mma_tf32_pair(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// arrive on the barrier at this offset in both CTAs when the MMAs issued so far complete
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+  const uint16_t mask = 3;
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+               ::"r"(bar), "h"(mask)
+               : "memory");
+}
+
+template <int ST, int NB, int EPI>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm_pair(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const __grid_constant__ CUtensorMap mapC, const __grid_constant__ CUtensorMap mapP,
+                   float* __restrict__ Cp, long long ldcf, int M, int N2, int K2, int accumulate,
+                   int* tile_ctr, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[2 * ST + 4 + 2 * TC_TQ];
+  __shared__ int tq[TC_TQ];
+  __shared__ uint32_t tmem_slot;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t crank = cluster_rank();
+  const bool lead = crank == 0;
+  const int KT = (K2 + TC_BK - 1) / TC_BK;
+  const int MT = (M + TP_TILE - 1) / TP_TILE, NT = (N2 + TP_TILE - 1) / TP_TILE;
+  const int ntiles = MT * NT;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[ST]);
+  const uint32_t accf0 = smem_u32(&bars[2 * ST]), acce0 = smem_u32(&bars[2 * ST + 2]);
+  const uint32_t tqf0 = smem_u32(&bars[2 * ST + 4]), tqe0 = smem_u32(&bars[2 * ST + 4 + TC_TQ]);
+  const uint32_t stage_base = base + ST * TP_STAGE_BYTES;
+  // the even CTA's barriers, the odd CTA's ring (cluster addresses)
+  const uint32_t full0_l = mapa_rank(full0, 0), acce0_l = mapa_rank(acce0, 0), tqe0_l = mapa_rank(tqe0, 0);
+  const uint32_t tq_p = mapa_rank(smem_u32(&tq[0]), 1), tqf0_p = mapa_rank(tqf0, 1);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, 2 * TC_EPI_WARPS);
+    }
+    for (int q = 0; q < TC_TQ; ++q) {
+      mbar_init(tqf0 + 8 * q, 1);
+      mbar_init(tqe0 + 8 * q, 2 + 2 * TC_EPI_WARPS);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    // one warp of each CTA allocates the pair's tensor memory collectively
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(2 * TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  cluster_sync_all();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- tile scheduler (even CTA) + TMA producer (both CTAs)
+      int it = 0, issued = 0;
+      int t_next = lead ? atomicAdd(tile_ctr, 1) : -1;   // one tile ahead (see the single-CTA kernel)
+      for (int j = 0;; ++j) {
+        const int q = j % TC_TQ;
+        int t;
+        if (lead) {
+          if (j >= TC_TQ && !mbar_wait_cl(tqe0 + 8 * q, ((j / TC_TQ) - 1) & 1, err, 16)) break;
+          t = *(volatile int*)err ? -1 : t_next;
+          if (t >= ntiles) t = -1;
+          if (t >= 0) t_next = atomicAdd(tile_ctr, 1);
+          tq[q] = t;
+          st_cluster_u32(tq_p + 4 * q, (uint32_t)t);
+          mbar_arrive(tqf0 + 8 * q);
+          mbar_arrive_cluster(tqf0_p + 8 * q);
+        } else {
+          if (!mbar_wait_cl(tqf0 + 8 * q, (j / TC_TQ) & 1, err, 16)) break;
+          t = *(volatile int*)&tq[q];
+          mbar_arrive_cluster(tqe0_l + 8 * q);
+        }
+        if (t < 0) break;
+        const int m0 = (t % MT) * TP_TILE + (int)crank * TP_ROWS;
+        const int n0 = (t / MT) * TP_TILE + (int)crank * TP_ROWS;
+        if (accumulate) tma_prefetch_2d(&mapP, (t / MT) * TP_TILE, m0);
+        bool ok = true;
+        for (int kt = 0; kt < KT; ++kt, ++it) {
+          const int s = it % ST;
+          if (it >= ST && !mbar_wait(empty0 + 8 * s, ((it / ST) - 1) & 1, err, 1)) { ok = false; break; }
+          const uint32_t sa = base + s * TP_STAGE_BYTES, sb = sa + TP_A_BYTES;
+          if (lead) mbar_expect_tx(full0 + 8 * s, 2 * TP_STAGE_BYTES);
+          tma_load_2d_pair(sa, &mapA, full0_l + 8 * s, kt * TC_BK, m0);
+          tma_load_2d_pair(sb, &mapB, full0_l + 8 * s, kt * TC_BK, n0);
+          issued = it + 1;
+        }
+        if (!ok) {
+          if (lead) {
+            // hand out an end marker in the next slot so that the other roles stop
+            const int j2 = j + 1, q2 = j2 % TC_TQ;
+            if (j2 < TC_TQ || mbar_wait_cl(tqe0 + 8 * q2, ((j2 / TC_TQ) - 1) & 1, err, 16)) {
+              tq[q2] = -1;
+              st_cluster_u32(tq_p + 4 * q2, 0xffffffffu);
+              mbar_arrive(tqf0 + 8 * q2);
+              mbar_arrive_cluster(tqf0_p + 8 * q2);
+            }
+          }
+          break;
+        }
+      }
+      if (!*(volatile int*)err) {
+        for (int i = issued - ST > 0 ? issued - ST : 0; i < issued; ++i)
+          mbar_wait(empty0 + 8 * (i % ST), (i / ST) & 1, err, 8);
+      } else {
+        // copies may still be in flight towards a barrier that never completes:
+        // give them time to land before the shared memory is released
+        const unsigned long long t0 = gtimer();
+        while (gtimer() - t0 < 200000ull) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      // ---------------- MMA issuer (even CTA)
+      int it = 0;
+      for (int j = 0;; ++j) {
+        const int q = j % TC_TQ;
+        if (!mbar_wait(tqf0 + 8 * q, (j / TC_TQ) & 1, err, 32)) break;
+        const int t = *(volatile int*)&tq[q];
+        mbar_arrive(tqe0 + 8 * q);
+        if (t < 0) break;
+        const int b = j & 1;
+        if (j >= 2 && !mbar_wait_cl(acce0 + 8 * b, ((j >> 1) - 1) & 1, err, 64)) break;
+        tc_fence_after();
+        const uint32_t dt = tmem + (uint32_t)(b * TC_TMEM_COLS);
+        bool ok = true;
+        for (int kt = 0; kt < KT; ++kt, ++it) {
+          const int s = it % ST;
+          if (!mbar_wait(full0 + 8 * s, (it / ST) & 1, err, 2)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = base + s * TP_STAGE_BYTES, sb = sa + TP_A_BYTES;
+          const uint64_t da = desc_sw128(sa), db = desc_sw128(sb);
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 8; ++kk)
+            mma_tf32_pair(dt, da + 2 * kk, db + 2 * kk, TP_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
+          mma_commit_pair(empty0 + 8 * s);
+        }
+        if (!ok) break;
+        mma_commit_pair(accf0 + 8 * b);
+      }
+    }
+  } else {
+    // ---------------- epilogue warps (both CTAs): TMEM lane quarter = 32 rows
+    const int ew = warp - 2;
+    const int quarter = warp & 3;
+    const uint32_t stage0 = stage_base + (uint32_t)ew * (uint32_t)NB * 4096u;
+    float* stage_gen = reinterpret_cast<float*>(smem_raw + (stage_base - smem_u32(smem_raw))) + ew * NB * 1024;
+    int nstores = 0;
+    for (int j = 0;; ++j) {
+      const int q = j % TC_TQ;
+      int t = -1;
+      const bool okq = __all_sync(0xffffffffu, mbar_wait_cl(tqf0 + 8 * q, (j / TC_TQ) & 1, err, 128) ? 1 : 0) != 0;
+      if (okq) t = *(volatile int*)&tq[q];
+      __syncwarp();
+      if (lane == 0 && okq) {
+        if (lead) mbar_arrive(tqe0 + 8 * q);
+        else mbar_arrive_cluster(tqe0_l + 8 * q);
+      }
+      if (!okq || t < 0) break;
+      const int b = j & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (j >> 1) & 1, err, 4) ? 1 : 0) != 0;
+      if (!ok) break;
+      tc_fence_after();
+      const int m0 = (t % MT) * TP_TILE + (int)crank * TP_ROWS, n0 = (t / MT) * TP_TILE;
+      const int row0 = m0 + quarter * 32;
+      for (int c = 0; c < TP_TILE / 32; ++c) {
+        const int col0 = n0 + c * 32;
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * TC_TMEM_COLS + c * 32), r);
+        if constexpr (EPI == 1) {
+          if (c == TP_TILE / 32 - 1) {
+            // the accumulator has been read: the MMA warp may overwrite it
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+              if (lead) mbar_arrive(acce0 + 8 * b);
+              else mbar_arrive_cluster(acce0_l + 8 * b);
+            }
+          }
+          if (col0 >= N2 || row0 >= M) continue;          // warp-uniform
+          epi_chunk_lsu(r, stage_gen, lane, Cp, ldcf, row0, col0, M, N2, accumulate);
+          continue;
+        }
+        if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
+        const int buf = nstores % NB;
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(NB - 1) : "memory");
+        __syncwarp();
+        float4* st = reinterpret_cast<float4*>(stage_gen + buf * 1024) + lane * 8;
+#pragma unroll
+        for (int c4 = 0; c4 < 8; ++c4)
+          st[c4 ^ (lane & 7)] = make_float4(__uint_as_float(r[4 * c4]), __uint_as_float(r[4 * c4 + 1]),
+                                            __uint_as_float(r[4 * c4 + 2]), __uint_as_float(r[4 * c4 + 3]));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          const uint32_t src = stage0 + (uint32_t)buf * 4096u;
+          if (accumulate)
+            asm volatile(
+                "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%1, %2}], [%3];"
+                ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+                : "memory");
+          else
+            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                         ::"l"((unsigned long long)&mapC), "r"(col0), "r"(row0), "r"(src)
+                         : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
+        ++nstores;
+      }
+      if constexpr (EPI == 0) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          if (lead) mbar_arrive(acce0 + 8 * b);
+          else mbar_arrive_cluster(acce0_l + 8 * b);
+        }
+      }
+    }
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+  __syncwarp();
+  tc_fence_before();
+  cluster_sync_all();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_TMEM_COLS) : "memory");
   }
 }
 
@@ -392,10 +733,11 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode(TcGemmCtx& c) {
 }
 
 static bool make_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, const void* ptr, uint64_t inner,
-                     uint64_t rows, uint64_t row_bytes, uint32_t box_rows, bool swizzle = true) {
+                     uint64_t rows, uint64_t row_bytes, uint32_t box_rows, bool swizzle = true,
+                     uint32_t box_inner = TC_BK) {
   cuuint64_t dims[2] = {inner, rows};
   cuuint64_t strides[1] = {row_bytes};
-  cuuint32_t box[2] = {(cuuint32_t)TC_BK, box_rows};
+  cuuint32_t box[2] = {box_inner, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -412,13 +754,20 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     c.usable = (major == 10 && minor == 3) && get_encode(c) != nullptr &&
-               cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
-               cudaFuncSetAttribute(k_tc_gemm<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm_pair<5, 4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(5, 4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm_pair<6, 2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(6, 2)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm_pair<6, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(6, 2)) == cudaSuccess &&
                cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess;
     if (!c.usable) cudaGetLastError();
     const char* env = getenv("MNPBEM_TC_STAGES");
     if (env && (env[0] == '3' || env[0] == '4')) c.stages = env[0] - '0';
     if (c.stages != 3 && c.stages != 4) c.stages = 4;
+    const char* penv = getenv("MNPBEM_TC_PAIR");
+    if (penv && (penv[0] == '0' || penv[0] == '1')) c.pair = penv[0] - '0';
   }
   if (!c.usable || !c.enabled) return false;
   if ((lda & 1) || (ldc & 1) || (reinterpret_cast<uintptr_t>(A) & 15) ||
@@ -447,10 +796,16 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     MNP_CHECK_LAUNCH();
   }
   auto enc = get_encode(c);
-  CUtensorMap ma, mb, mc;
-  if (!make_map(enc, &ma, A, (uint64_t)K2, (uint64_t)M, (uint64_t)lda * 8, TC_BM) ||
-      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, TC_BN) ||
-      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, true)) {
+  // CTA pairs for products with at least 256 rows (the pair tile is 256 x 256)
+  // measured on GB300 (complex 4000 x 4000 products): the pair kernel reaches
+  // 870 TFLOP/s at K = 4000 against 745 for the single-CTA kernel, and ties or
+  // trails it at K = 256 (rank updates, panel products)
+  const bool pair = M >= TP_TILE && (c.pair == 1 || (c.pair < 0 && K >= 1024));
+  CUtensorMap ma, mb, mc, mp;
+  if (!make_map(enc, &ma, A, (uint64_t)K2, (uint64_t)M, (uint64_t)lda * 8, pair ? TP_ROWS : TC_BM) ||
+      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 4, pair ? TP_ROWS : TC_BN) ||
+      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, true) ||
+      !make_map(enc, &mp, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, TC_BM, false, TC_BN)) {
     set_error("cuTensorMapEncodeTiled failed");
     return MNPBEM_ERR_CUDA;
   }
@@ -458,22 +813,39 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     MNP_CUDA(cudaMemsetAsync(c.err.ptr, 0, sizeof(int), st));
     c.err_cleared = true;
   }
-  const int64_t MT = cdiv_up(M, TC_BM), NT = cdiv_up(N2, TC_BN);
+  const int64_t MT = cdiv_up(M, pair ? TP_TILE : TC_BM), NT = cdiv_up(N2, pair ? TP_TILE : TC_BN);
   if (MT * NT >= (1ll << 31)) { set_error("tc_gemm_c64: too many tiles"); return MNPBEM_ERR_INVALID_ARG; }
   MNP_TRY(c.ctr.ensure(sizeof(int)));
   MNP_CUDA(cudaMemsetAsync(c.ctr.ptr, 0, sizeof(int), st));
+  // 2N floats per row that are not a multiple of 16 bytes: vector stores, not TMA
+  const bool lsu = c.pair_epi == 1 || (N2 & 3) != 0;
+  float* Cf = reinterpret_cast<float*>(C);
+  const long long ldcf = 2ll * ldc;
+  const int acc = beta.x != 0.0f ? 1 : 0;
   int ctas = c.num_sms > 0 ? c.num_sms : 148;
   if (c.max_ctas > 0 && c.max_ctas < ctas) ctas = c.max_ctas;
-  const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, ctas);
   {
     ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
                  8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
-    if (c.stages == 3)
-      k_tc_gemm<3><<<grid, TC_THREADS, tc_psmem(3), st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2,
-                                                          beta.x != 0.0f ? 1 : 0, c.ctr.as<int>(), c.err.as<int>());
-    else
-      k_tc_gemm<4><<<grid, TC_THREADS, tc_psmem(4), st>>>(ma, mb, mc, (int)M, (int)N2, (int)K2,
-                                                          beta.x != 0.0f ? 1 : 0, c.ctr.as<int>(), c.err.as<int>());
+    if (pair) {
+      // one cluster of two CTAs per pair tile, at most one CTA per SM
+      const unsigned grid = 2u * (unsigned)std::min<int64_t>(MT * NT, std::max(1, ctas / 2));
+      if (c.pair_nb == 4 && !lsu)
+        k_tc_gemm_pair<5, 4, 0><<<grid, TC_THREADS, tp_psmem(5, 4), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2,
+                                                                          (int)K2, acc, c.ctr.as<int>(), c.err.as<int>());
+      else if (lsu)
+        k_tc_gemm_pair<6, 2, 1><<<grid, TC_THREADS, tp_psmem(6, 2), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2,
+                                                                          (int)K2, acc, c.ctr.as<int>(), c.err.as<int>());
+      else
+        k_tc_gemm_pair<6, 2, 0><<<grid, TC_THREADS, tp_psmem(6, 2), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2,
+                                                                          (int)K2, acc, c.ctr.as<int>(), c.err.as<int>());
+      MNP_CHECK_LAUNCH();
+      return MNPBEM_OK;
+    }
+    const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, ctas);
+    auto kern = c.stages == 3 ? (lsu ? k_tc_gemm<3, 1> : k_tc_gemm<3, 0>) : (lsu ? k_tc_gemm<4, 1> : k_tc_gemm<4, 0>);
+    kern<<<grid, TC_THREADS, tc_psmem(c.stages == 3 ? 3 : 4), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2, (int)K2,
+                                                                    acc, c.ctr.as<int>(), c.err.as<int>());
     MNP_CHECK_LAUNCH();
   }
   return MNPBEM_OK;

@@ -14,6 +14,10 @@ struct TcGemmCtx {
   DevBuf ctr;             // tile counter of the persistent kernel (zeroed before each launch)
   int num_sms = 0;
   int stages = 4;         // pipeline depth of the persistent kernel (3 or 4)
+  int pair = 0;           // CTA-pair kernel (tcgen05 cta_group::2, 256 x 256 tiles) for M >= 256:
+                          // 1 always, 0 never, -1 for long K (at least 1024), where it is faster
+  int pair_epi = 0;       // epilogue of the pair kernel: 0 TMA store / reduce-add, 1 vector stores / reductions
+  int pair_nb = 2;        // epilogue staging buffers per warp of the pair kernel (2: 6 stages, 4: 5 stages)
   int max_ctas = 0;       // CTAs of the persistent kernel (0: one per SM); fewer leave SMs
                           // to the pivot-block clusters of other wavelengths in flight
   void* encode_fn = nullptr;
