@@ -139,6 +139,7 @@ struct mnpbem_geom {
   int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
   bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
   bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
+  bool gj_fused = true;     // fused Gauss-Jordan steps on the tensor-core path
   int tc_stages = 0;        // pipeline depth of the tensor-core GEMM (0: its default)
   int tc_ctas = 0;          // CTAs of the persistent tensor-core GEMM (0: one per SM)
   int tc_pair = 0;          // CTA-pair tensor-core GEMM: 1 always, 0 off, -1 long-K products
@@ -377,6 +378,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (dsenv && dsenv[0] == '0') G->asm_ds = false;
   const char* rnaenv = getenv("MNPBEM_TF32_RNA");
   if (rnaenv && rnaenv[0] == '0') G->tf32_rna = false;
+  const char* gjfenv = getenv("MNPBEM_GJ_FUSED");
+  if (gjfenv && gjfenv[0] == '0') G->gj_fused = false;
   const char* nbenv = getenv("MNPBEM_GJ_NB");
   if (nbenv && atoi(nbenv) == 512) G->gj_nb = 512;
   const char* lenv = getenv("MNPBEM_LANES");
@@ -697,6 +700,7 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   mix(nullptr, (size_t)(L.tc.pair + 1));
   mix(nullptr, (size_t)G->tf32_rna);
   mix(nullptr, (size_t)G->asm_ds);
+  mix(nullptr, (size_t)G->gj_fused);
   return h;
 }
 
@@ -807,6 +811,7 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   // fewer passes over the n x n matrix (each step reads and writes it once)
   gjw<R>(L).nb = (ctx && n >= 1024) ? G->gj_nb : 64;
   gjw<R>(L).round_a = G->tf32_rna;
+  gjw<R>(L).fused = G->gj_fused;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
   const FaceData fd = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();

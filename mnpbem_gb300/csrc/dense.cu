@@ -13,6 +13,7 @@
 #include "dense.cuh"
 #include "mbarrier.cuh"
 #include "profile.cuh"
+#include "tc_gemm.cuh"
 
 namespace mnpbem {
 
@@ -951,6 +952,28 @@ void round_tf32(float* x, int64_t count, cudaStream_t st) {
   k_round_tf32<<<(unsigned)cdiv_up(count, 256), 256, 0, st>>>(x, count);
 }
 
+// Ccol[n][bw] <- A[:, k0 .. k0 + bw) with the rows k0 .. k0 + bw zeroed and,
+// if rna, rounded to TF32 (nearest): the A operand of the column-panel product
+// and of the rank update of one fused Gauss-Jordan step.
+__global__ void k_gj_take_col(const float2* __restrict__ A, int64_t lda, int64_t n, int64_t k0, int bw,
+                              float2* __restrict__ Ccol, int rna) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * bw) return;
+  const int64_t i = idx / bw;
+  const int c = (int)(idx - i * bw);
+  float2 v = make_float2(0.f, 0.f);
+  if (i < k0 || i >= k0 + bw) {
+    v = A[i * lda + k0 + c];
+    if (rna) {
+      uint32_t x, y;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(x) : "f"(v.x));
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(v.y));
+      v = make_float2(__uint_as_float(x), __uint_as_float(y));
+    }
+  }
+  Ccol[idx] = v;
+}
+
 // --------------------------------------------------- blocked Gauss-Jordan
 template <typename R>
 mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st) {
@@ -993,6 +1016,43 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
   for (int64_t k0 = 0; k0 < n; k0 += nb) {
     const int bw = (int)std::min<int64_t>(nb, n - k0);
+    if constexpr (sizeof(R) == 4) {
+      // Fused step on the tensor-core path (all three products eligible):
+      //   X <- inv(A_kk) read in place; Ccol <- TF32(A[:, k]) with rows k zeroed;
+      //   A[k, :] <- X A[k, :] in place (the product copies its B operand before it
+      //   runs); A[:, k] <- -Ccol X (rows k become 0); A <- A - Ccol A[k, :] with the
+      //   k columns of the B operand read as zero (rows and columns k unchanged);
+      //   A_kk <- X.  The same products as the general step below, without its
+      //   panel copies and write-backs.
+      TcGemmCtx* tc = reinterpret_cast<TcGemmCtx*>(ctx);
+      const float2 b0 = make_float2(0.f, 0.f), b1 = make_float2(1.f, 0.f);
+      float2* Af = reinterpret_cast<float2*>(A);
+      float2* Cf = reinterpret_cast<float2*>(Ccol);
+      float2* Xf = reinterpret_cast<float2*>(X);
+      if (tc && w.fused && bw <= PB_W && tc_gemm_eligible(*tc, bw, n, bw, Xf, bw, Af + k0 * lda, lda, b0) &&
+          tc_gemm_eligible(*tc, n, bw, bw, Cf, bw, Af + k0, lda, b0) &&
+          tc_gemm_eligible(*tc, n, n, bw, Cf, bw, Af, lda, b1)) {
+        if (bw <= 64) {
+          ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
+          k_block_inv<R><<<1, 256, 0, st>>>(A + k0 * lda + k0, lda, bw, X, bw, w.status.template as<int>());
+          MNP_CHECK_LAUNCH();
+        } else {
+          MNP_TRY(launch_block_inv_cluster(Af + k0 * lda + k0, lda, bw, Xf, bw, w.status.template as<int>(), st));
+        }
+        {
+          ProfScope ps(PH_ELEMWISE, st, 0.0, 16.0 * n * bw, 1);
+          k_gj_take_col<<<(unsigned)cdiv_up(n * bw, (int64_t)256), 256, 0, st>>>(Af, lda, n, k0, bw, Cf,
+                                                                                 w.round_a ? 1 : 0);
+          MNP_CHECK_LAUNCH();
+        }
+        MNP_TRY(tc_gemm_c64(*tc, bw, n, bw, b1, Xf, bw, Af + k0 * lda, lda, b0, Af + k0 * lda, lda, st));
+        MNP_TRY(tc_gemm_c64(*tc, n, bw, bw, make_float2(-1.f, 0.f), Cf, bw, Xf, bw, b0, Af + k0, lda, st));
+        MNP_TRY(tc_gemm_c64(*tc, n, n, bw, make_float2(-1.f, 0.f), Cf, bw, Af + k0 * lda, lda, b1, Af, lda, st,
+                            k0, k0 + bw));
+        MNP_CUDA(cudaMemcpy2DAsync(A + k0 * lda + k0, cs * lda, X, cs * bw, cs * bw, bw, cudaMemcpyDeviceToDevice, st));
+        continue;
+      }
+    }
     // 1. Ccol <- A[:, k-block]
     MNP_CUDA(cudaMemcpy2DAsync(Ccol, cs * bw, A + k0, cs * lda, cs * bw, n, cudaMemcpyDeviceToDevice, st));
     // 2. X <- inv(A_kk): one shared-memory kernel for blocks up to 64, else

@@ -35,6 +35,7 @@ struct GJWork {
   DevBuf ccol, rrow, ncol, xblk, status;
   int nb = 64;
   bool round_a = true;               // round the A operand of the tensor-core updates to TF32 (nearest)
+  bool fused = true;                 // tensor-core path: products written in place (no panel copies)
   bool nested = false;               // inner level: the outer level reads the pivot status
   std::unique_ptr<GJWork<R>> inner;  // Gauss-Jordan of pivot blocks wider than 64
 };

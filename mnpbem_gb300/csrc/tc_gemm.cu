@@ -683,14 +683,14 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 __global__ void k_expand_b(int K, int N, float2 alpha, const float2* __restrict__ B, int64_t ldb, float* __restrict__ Bp,
-                           int K2p) {
+                           int K2p, int bz0, int bz1) {
   __shared__ float2 tile[32][33];
   const int l0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
   for (int r = ty; r < 32; r += 8) {
     int l = l0 + r, j = j0 + tx;
     float2 v = make_float2(0.f, 0.f);
-    if (l < K && j < N) {
+    if (l < K && j < N && (j < bz0 || j >= bz1)) {
       float2 b = B[(int64_t)l * ldb + j];
       v = make_float2(alpha.x * b.x - alpha.y * b.y, alpha.x * b.y + alpha.y * b.x);
     }
@@ -778,7 +778,7 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
 
 mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
                           int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc,
-                          cudaStream_t st) {
+                          cudaStream_t st, int64_t bz0, int64_t bz1) {
   if (beta.y != 0.0f || (beta.x != 0.0f && beta.x != 1.0f) || (lda & 1) || (ldc & 1) ||
       (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(C) & 15)) {
     set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base, beta not 0 or 1)");
@@ -792,7 +792,7 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
   {
     ProfScope ps(PH_ELEMWISE, st, 0.0, 8.0 * K * N + 16.0 * K * N);
     dim3 g((unsigned)cdiv_up(N, 32), (unsigned)cdiv_up(K2p / 2, 32));
-    k_expand_b<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p);
+    k_expand_b<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p, (int)bz0, (int)bz1);
     MNP_CHECK_LAUNCH();
   }
   auto enc = get_encode(c);

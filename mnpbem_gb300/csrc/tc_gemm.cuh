@@ -27,9 +27,11 @@ struct TcGemmCtx {
 // even leading dimensions and 16-byte aligned A and C, real beta)
 bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
                       const void* C, int64_t ldc, float2 beta);
+// B's columns [bz0, bz1) are read as zero (the B operand is copied, expanded,
+// before the product runs, so C may overlap B)
 mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha,
                           const float2* A, int64_t lda, const float2* B, int64_t ldb, float2 beta,
-                          float2* C, int64_t ldc, cudaStream_t st);
+                          float2* C, int64_t ldc, cudaStream_t st, int64_t bz0 = 0, int64_t bz1 = 0);
 // reads (and clears) the device error word; MNPBEM_ERR_TIMEOUT if a wait expired
 mnpbem_status tc_check_error(TcGemmCtx& c, cudaStream_t st);
 void tc_release(TcGemmCtx& c);
