@@ -1029,15 +1029,20 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
       float2* Af = reinterpret_cast<float2*>(A);
       float2* Cf = reinterpret_cast<float2*>(Ccol);
       float2* Xf = reinterpret_cast<float2*>(X);
-      if (tc && w.fused && bw <= PB_W && tc_gemm_eligible(*tc, bw, n, bw, Xf, bw, Af + k0 * lda, lda, b0) &&
+      if (tc && w.fused && (bw <= PB_W || w.inner) && tc_gemm_eligible(*tc, bw, n, bw, Xf, bw, Af + k0 * lda, lda, b0) &&
           tc_gemm_eligible(*tc, n, bw, bw, Cf, bw, Af + k0, lda, b0) &&
           tc_gemm_eligible(*tc, n, n, bw, Cf, bw, Af, lda, b1)) {
         if (bw <= 64) {
           ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
           k_block_inv<R><<<1, 256, 0, st>>>(A + k0 * lda + k0, lda, bw, X, bw, w.status.template as<int>());
           MNP_CHECK_LAUNCH();
-        } else {
+        } else if (bw <= PB_W) {
           MNP_TRY(launch_block_inv_cluster(Af + k0 * lda + k0, lda, bw, Xf, bw, w.status.template as<int>(), st));
+        } else {
+          // wider pivot blocks: inner Gauss-Jordan (256-wide steps) on a copy
+          MNP_CUDA(cudaMemcpy2DAsync(X, cs * bw, A + k0 * lda + k0, cs * lda, cs * bw, bw, cudaMemcpyDeviceToDevice,
+                                     st));
+          MNP_TRY(gj_invert<R>(X, bw, bw, *w.inner, big_gemm, ctx, st));
         }
         {
           ProfScope ps(PH_ELEMWISE, st, 0.0, 16.0 * n * bw, 1);
