@@ -391,10 +391,14 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_hi(int64_t M, int64
 // consumer warps take the chunk's k range in parallel (lane = k), read B
 // through L1 and accumulate TS_TR rows x N in registers; at the end of a row
 // block the warps' partial sums are added in a fixed order (deterministic).
+// Sixteen consumer warps: TS_KG k groups x TS_RG row groups (TS_RPW rows each),
+// so that each warp keeps few accumulators and each scheduler has four warps
+// to hide the L1 / shared-memory latencies (eight warps with all rows each
+// were latency bound: 29 % issue, 32 % of HBM).
 // Waits are bounded; after a timeout every role skips the remaining waits
 // (the result is then garbage and the error word is set) so that no barrier
 // is left waiting.
-constexpr int TS_TR = 8, TS_KC = 512, TS_ST = 4, TS_CW = 8;
+constexpr int TS_TR = 8, TS_KC = 512, TS_ST = 4, TS_RG = 2, TS_KG = 8, TS_CW = TS_RG * TS_KG, TS_RPW = TS_TR / TS_RG;
 constexpr int TS_THREADS = 32 * (TS_CW + 1);
 constexpr int TS_STAGE = TS_TR * TS_KC * 8;               // 32 KB
 constexpr int TS_SMEM = TS_ST * TS_STAGE;
@@ -416,7 +420,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
                        int64_t ldb, float2 alpha, float2 beta, void* __restrict__ Cv, int64_t ldc) {
   extern __shared__ __align__(128) unsigned char ts_smem[];
   __shared__ __align__(8) unsigned long long bars[2 * TS_ST];
-  __shared__ float2 red[TS_CW][TS_TR][N];
+  __shared__ float2 red[TS_KG][TS_TR][N];
   __shared__ int abort_flag;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t rb = M * blockIdx.x / gridDim.x, re = M * (blockIdx.x + 1) / gridDim.x;
@@ -462,12 +466,14 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
   } else {
     // ---------------- consumers
     const float2* As = reinterpret_cast<const float2*>(ts_smem);
+    const int rg = warp / TS_KG, kg = warp % TS_KG;
     int it = 0;
     for (int64_t r0 = rb; r0 < re; r0 += TS_TR) {
       const int nr = (int)min((int64_t)TS_TR, re - r0);
-      float2 acc[TS_TR][N];
+      const int nrw = max(0, min(TS_RPW, nr - rg * TS_RPW));   // this warp's rows in the block
+      float2 acc[TS_RPW][N];
 #pragma unroll
-      for (int r = 0; r < TS_TR; ++r)
+      for (int r = 0; r < TS_RPW; ++r)
 #pragma unroll
         for (int c = 0; c < N; ++c) acc[r][c] = make_float2(0.f, 0.f);
       for (int64_t ch = 0; ch < nchunk; ++ch, ++it) {
@@ -475,17 +481,17 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         if (!*abort_v && !mbar_wait(full0 + 8 * s, (it / TS_ST) & 1, err, 2)) *abort_v = 1;
         const int64_t k0 = ch * TS_KC;
         const int kl = (int)min((int64_t)TS_KC, K - k0);
-        const float2* Ast = As + s * (TS_TR * TS_KC);
+        const float2* Ast = As + s * (TS_TR * TS_KC) + rg * TS_RPW * TS_KC;
 #pragma unroll
-        for (int j = 0; j < TS_KC / (32 * TS_CW); ++j) {
-          const int kk = warp * (TS_KC / TS_CW) + 32 * j + lane;
+        for (int j = 0; j < TS_KC / (32 * TS_KG); ++j) {
+          const int kk = kg * (TS_KC / TS_KG) + 32 * j + lane;
           if (kk < kl) {
             float2 b[N];
 #pragma unroll
             for (int c = 0; c < N; ++c) b[c] = __ldg(B + (k0 + kk) * ldb + c);
 #pragma unroll
-            for (int r = 0; r < TS_TR; ++r) {
-              if (r < nr) {
+            for (int r = 0; r < TS_RPW; ++r) {
+              if (r < nrw) {
                 const float2 a = Ast[r * TS_KC + kk];
 #pragma unroll
                 for (int c = 0; c < N; ++c) cfma(acc[r][c], a, b[c]);
@@ -497,7 +503,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
         if (lane == 0) mbar_arrive(empty0 + 8 * s);
       }
 #pragma unroll
-      for (int r = 0; r < TS_TR; ++r)
+      for (int r = 0; r < TS_RPW; ++r)
 #pragma unroll
         for (int c = 0; c < N; ++c) {
           float2 v = acc[r][c];
@@ -506,14 +512,14 @@ __global__ void __launch_bounds__(TS_THREADS, 1)
             v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
             v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
           }
-          if (lane == 0) red[warp][r][c] = v;
+          if (lane == 0) red[kg][rg * TS_RPW + r][c] = v;
         }
       consumer_sync();
       for (int t = threadIdx.x; t < nr * N; t += 32 * TS_CW) {
         const int r = t / N, c = t % N;
         float2 v = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int w = 0; w < TS_CW; ++w) v = cadd(v, red[w][r][c]);
+        for (int w = 0; w < TS_KG; ++w) v = cadd(v, red[w][r][c]);
         const int64_t row = r0 + r;
         if (MODE == 0) {
           float2* C = reinterpret_cast<float2*>(Cv);
