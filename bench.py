@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=20, help="wavelengths per step per GPU")
     ap.add_argument("--lanes", type=int, default=0, help="wavelengths in flight at once (0: library default)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--refine-tol", type=float, default=1e-8,
+                    help="mixed precision: refinement stops at ||dx|| <= tol ||x|| (the metric asks for an "
+                         "extinction error <= 1e-6 against FP64; the library default is 1e-10)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (default: workload)")
@@ -147,6 +150,7 @@ def make_problem(a, device, precision):
     p = m.particle(v, f)
     cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
     bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device, lanes=a.lanes))
+    bem.refine_tol = a.refine_tol
     exc = m.planewave([1, 0, 0], [0, 0, 1])
     return cp, bem, exc
 
@@ -247,6 +251,22 @@ def run_ours(a, rank, world, dist, torch):
     ms = e0.elapsed_time(e1)
     launches_timed = read_profile(bem)
     iters = sweep.iters.copy()
+    # ---------------- the same steps at the library's default tolerance (1e-10)
+    tol_default = None
+    if a.precision == "mixed" and a.refine_tol != 1e-10:
+        from mnpbem_gb300 import _lib as L_
+        sweep_d = DeviceSweep(bem, exc, a.batch, torch)
+        sweep_d.ref = L_.Refine(bem.refine_iters, 1e-10)
+        sweep_d.run(step_wavelengths(0, rank, world, a.batch))
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for s in range(a.steps):
+            sweep_d.run(step_wavelengths(a.warmup + s, rank, world, a.batch))
+        g1.record(stream)
+        torch.cuda.synchronize()
+        tol_default = {"refine_tol": 1e-10, "value": a.batch * a.steps / (g0.elapsed_time(g1) / 1e3),
+                       "refinement_iterations": sweep_d.iters.tolist()}
     # ---------------- profiled repeat of the same steps: CUDA events on the
     # library stream around every launch give per-kernel-class durations
     bem_lib.mnpbem_profile_enable(bem.handle, 1)
@@ -313,7 +333,7 @@ def run_ours(a, rank, world, dist, torch):
     extra = {"phases_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "phases_roofline": phases_roof,
              "assembly_hbm_gbs": asm["bytes"] / (asm["ms"] / 1e3) / 1e9 if asm["ms"] > 0 else None,
              "assembled_pairs_per_s": (n * n * a.batch * a.steps) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
-             "refinement_iterations": iters.tolist()}
+             "refinement_iterations": iters.tolist(), "at_default_tolerance": tol_default}
     launches = int(sum(v["launches"] for k, v in launches_timed.items() if k != "geometry"))
     out = {"value": value, "ms": ms, "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                                              "d2h_bytes_per_step": int(d2h), "ms": e2e_ms,
@@ -328,18 +348,19 @@ def fp64_comparison(a, cp, exc, torch, mixed_bem):
     import mnpbem_gb300 as m
     device = torch.cuda.current_device()
     bem64 = m.bemsolver(cp, m.bemoptions(precision="fp64", device=device))
-    lam = [600.0]
-    bem64.spectrum(exc, [450.0])          # warm-up (kernel loading)
+    lam = [450.0, 600.0, 750.0]
+    bem64.spectrum(exc, [500.0])          # warm-up (kernel loading)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     r64 = bem64.spectrum(exc, lam)
     torch.cuda.synchronize()
-    t64 = time.perf_counter() - t0
+    t64 = (time.perf_counter() - t0) / len(lam)
     rmx = mixed_bem.spectrum(exc, lam)
     err_ext = float(np.max(np.abs(rmx["ext"] - r64["ext"]) / np.abs(r64["ext"])))
     err_sca = float(np.max(np.abs(rmx["sca"] - r64["sca"]) / np.abs(r64["sca"])))
-    return {"value": 1.0 / t64, "unit": UNIT, "sample": "1 wavelength (600 nm), same workload",
-            "ext_rel_err_mixed_vs_fp64": err_ext, "sca_rel_err_mixed_vs_fp64": err_sca}
+    return {"value": 1.0 / t64, "unit": UNIT, "sample": "3 wavelengths (450, 600, 750 nm), same workload",
+            "ext_rel_err_mixed_vs_fp64": err_ext, "sca_rel_err_mixed_vs_fp64": err_sca,
+            "mixed_refine_tol": mixed_bem.refine_tol}
 
 
 # ------------------------------------------------- secondary workloads
@@ -370,6 +391,8 @@ def run_batch3(a, torch):
         for v, f in geo:
             cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
             out.append(m.bemsolver(cp, m.bemoptions(precision=prec, device=dev, lanes=lanes)))
+            if prec == "mixed":
+                out[-1].refine_tol = a.refine_tol
         return out
     bems = solvers("mixed", a.lanes)
     for _ in range(max(1, a.warmup)):
@@ -395,7 +418,8 @@ def run_batch3(a, torch):
                                    "quadrilaterals, rounded cube 40 nm / 4 nm rounding 2904 faces), Drude metal in "
                                    "eps=1.77, x and y polarisation along +z, 128 wavelengths 400-900 nm per particle",
                        "faces": [int(b.p.n) for b in bems], "wavelength_solves_per_step": nsol,
-                       "timing": "host wall clock around mnpbem_solve_batch (public API, ext/sca to host)"},
+                       "timing": "host wall clock around mnpbem_solve_batch (public API, ext/sca to host)",
+                       "refine_tol": a.refine_tol},
             "fp64_gpu": {"value": v64, "unit": UNIT, "sample": "2 wavelengths x 3 particles, FP64 path"},
             "speedup_vs_fp64_gpu": value / v64, "ext_rel_err_mixed_vs_fp64": err,
             "refinement_iterations_max": int(max(int(r["ir_iters"].max()) for r in res)),
@@ -424,6 +448,7 @@ def run_dimer(a, torch):
     enei = np.linspace(500.0, 900.0, 32)
     bem = dimer_problem(24000, "mixed", dev, a.lanes)
     bem.refine_iters = 20
+    bem.refine_tol = a.refine_tol
     bem.spectrum(exc, enei[:max(1, a.lanes or 3)])        # warm-up: sizes and captures every lane
     res, dt = _timed(lambda: bem.spectrum(exc, enei), torch)
     value = enei.size / dt
@@ -431,6 +456,7 @@ def run_dimer(a, torch):
     b64.spectrum(exc, [700.0])
     r64, t64 = _timed(lambda: b64.spectrum(exc, [700.0]), torch)
     bmx = dimer_problem(a.fp64_faces, "mixed", dev, 1)
+    bmx.refine_iters, bmx.refine_tol = 20, a.refine_tol
     rmx = bmx.spectrum(exc, [700.0])
     err = float(abs(rmx["ext"][0, 0] - r64["ext"][0, 0]) / abs(r64["ext"][0, 0]))
     scale = (24000.0 / a.fp64_faces) ** 3
@@ -440,7 +466,8 @@ def run_dimer(a, torch):
             "dtype": "c64(tf32)+f64", "data": "synthetic",
             "config": {"workload": "dimer of two d=50 nm spheres, 2 nm gap, 2 x 12000 faces, Drude metal in "
                                    "eps=1.77, x-pol along +z, 32 wavelengths 500-900 nm", "faces": 24000,
-                       "timing": "host wall clock around bemsolver.spectrum (public API, ext/sca to host)"},
+                       "timing": "host wall clock around bemsolver.spectrum (public API, ext/sca to host)",
+                       "refine_tol": a.refine_tol},
             "fp64_gpu": {"value": v64, "unit": UNIT,
                          "sample": "1 wavelength (700 nm) of a %d-face dimer, %.3f s, scaled by (24000/%d)^3"
                                    % (a.fp64_faces, t64, a.fp64_faces)},
@@ -563,6 +590,7 @@ def main():
                 "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": workload_desc(a), "faces": n, "wavelengths_per_step": a.batch,
                            "precision": a.precision, "lanes": a.lanes or "auto",
+                           "refine_tol": a.refine_tol if a.precision == "mixed" else None,
                            "l2": "no flush: per-wavelength working set %.2f GB > 129 MB L2" % (wset / 1e9)},
                 "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],
                 "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64}

@@ -1077,13 +1077,15 @@ struct Refine {
 //   step 1      full residual b - A x with FP32 products of the hi planes (5)
 //   then        incremental residuals r - A dx, FP32 products (6)
 //   once        a full double-single residual (3), when the relative residual
-//               is below 1e-5 or after three steps: it removes the FP32
-//               rounding of the first residual (~1e-7 of |A| |x|)
+//               is below 1e-3 or after three steps: it removes the FP32
+//               rounding of the first residual (~1e-7 of |A| |x|); taken as
+//               early as the FP32 chain's contraction allows, it saves one
+//               step against an anchor at 1e-5
 //   then        incremental residuals again, whose rounding (~1e-7 of |A| |dx|)
 //               is far below the 1e-10 tolerance once dx is small.
 // The stopping test (||dx|| <= tol ||x||) counts only after the double-single
 // residual.  Relative residuals are measured against ||b|| of the last full one.
-constexpr double DS_SWITCH = 1e-5;
+constexpr double DS_SWITCH = 1e-3;
 constexpr int STEP_DS = 3, STEP_FP32 = 5, STEP_INCR = 6;
 int next_step(const Lane& L) {
   if (L.iters == 0) return STEP_FP32;
