@@ -89,6 +89,20 @@ MNPBEM_API mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts,
                                  const int32_t* inout, const int32_t* closed,
                                  const mnpbem_quad* quad, const mnpbem_options* opts,
                                  mnpbem_geom** out);
+/* Same for curved boundary elements (particle with interp = 'curv'): 6-node
+ * triangles and 9-node quadrilaterals (Particles/@particle/private/norm_curv.m:8-62,
+ * quad_curv.m:13-59, quadpol_curv.m:15-88, totriangles_curv.m:14-31).
+ *   verts2 [nverts2][3]: corners and the extra nodes (p.verts2)
+ *   faces2 [nfaces][9] (p.faces2, 0-based, -1 for NaN): corners 0-3 (3 = -1 for
+ *   triangles), midpoints of edges 12, 23, 34 (31 for triangles), 41 in 4-7,
+ *   quadrilateral centre in 8.  Gradients (mnpbem_cross_section_gradient)
+ *   return MNPBEM_ERR_UNSUPPORTED on curved handles.                           */
+MNPBEM_API mnpbem_status mnpbem_geom_create_curved(const double* verts2, int64_t nverts2,
+                                        const int64_t* faces2, int64_t nfaces,
+                                        int32_t nparts, const int64_t* part_nfaces,
+                                        const int32_t* inout, const int32_t* closed,
+                                        const mnpbem_quad* quad, const mnpbem_options* opts,
+                                        mnpbem_geom** out);
 MNPBEM_API mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g);
 
 /* Sizes: number of faces and of refined (near + self) elements. */

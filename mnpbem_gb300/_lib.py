@@ -67,6 +67,10 @@ SIGNATURES = {
                                           ctypes.c_int32, c_int64_p, c_int32_p, c_int32_p,
                                           ctypes.POINTER(Quad), ctypes.POINTER(Options),
                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_geom_create_curved": (ctypes.c_int, [c_double_p, ctypes.c_int64, c_int64_p, ctypes.c_int64,
+                                                 ctypes.c_int32, c_int64_p, c_int32_p, c_int32_p,
+                                                 ctypes.POINTER(Quad), ctypes.POINTER(Options),
+                                                 ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_geom_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "mnpbem_geom_size": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p]),
     "mnpbem_geom_export": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 9),

@@ -150,11 +150,19 @@ class bemret:
         inout = np.ascontiguousarray(p.inout, dtype=np.int32)
         closed = np.ascontiguousarray(p.closed, dtype=np.int32)
         h = ctypes.c_void_p()
-        _lib.check(lib.mnpbem_geom_create(
-            _lib.dptr(p.verts), p.verts.shape[0], p.faces.ctypes.data_as(_lib.c_int64_p), p.n,
-            len(p.p), part_n.ctypes.data_as(_lib.c_int64_p), inout.ctypes.data_as(_lib.c_int32_p),
-            closed.ctypes.data_as(_lib.c_int32_p), ctypes.byref(quad), ctypes.byref(opts),
-            ctypes.byref(h)))
+        if getattr(p, "curved", False):
+            # curved boundary elements (interp = 'curv')
+            _lib.check(lib.mnpbem_geom_create_curved(
+                _lib.dptr(p.verts2), p.verts2.shape[0], p.faces2.ctypes.data_as(_lib.c_int64_p), p.n,
+                len(p.p), part_n.ctypes.data_as(_lib.c_int64_p), inout.ctypes.data_as(_lib.c_int32_p),
+                closed.ctypes.data_as(_lib.c_int32_p), ctypes.byref(quad), ctypes.byref(opts),
+                ctypes.byref(h)))
+        else:
+            _lib.check(lib.mnpbem_geom_create(
+                _lib.dptr(p.verts), p.verts.shape[0], p.faces.ctypes.data_as(_lib.c_int64_p), p.n,
+                len(p.p), part_n.ctypes.data_as(_lib.c_int64_p), inout.ctypes.data_as(_lib.c_int32_p),
+                closed.ctypes.data_as(_lib.c_int32_p), ctypes.byref(quad), ctypes.byref(opts),
+                ctypes.byref(h)))
         self._h = h
         self._lib = lib
         if self.op.get("tuned", True):

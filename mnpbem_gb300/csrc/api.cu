@@ -130,6 +130,7 @@ struct mnpbem_geom {
   int max_medium = 0;
   int64_t nverts = 0;
   bool all_closed = true;
+  bool curved = false;       // curved (6-node / 9-node) elements: interp = 'curv'
   DevBuf d_part, d_src, d_nrm, d_srcf, d_nrmf, face_med, exbuf;
   DevBuf adj, adj2, adj_mats, adj_off;   // adjoint gradient workspace
   int adj_noff = -1;
@@ -257,11 +258,11 @@ extern "C" {
 const char* mnpbem_last_error(void) { return get_error(); }
 const char* mnpbem_version(void) { return "mnpbem-gb300 0.2 (sm_103a)"; }
 
-mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int64_t* faces,
-                                 int64_t nfaces, int32_t nparts, const int64_t* part_nfaces,
-                                 const int32_t* inout, const int32_t* closed,
-                                 const mnpbem_quad* quad, const mnpbem_options* opts,
-                                 mnpbem_geom** out) {
+static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const int64_t* faces,
+                                      const int64_t* faces2, int64_t nfaces, int32_t nparts,
+                                      const int64_t* part_nfaces, const int32_t* inout,
+                                      const int32_t* closed, const mnpbem_quad* quad,
+                                      const mnpbem_options* opts, mnpbem_geom** out) {
   if (!out || !verts || !faces || !part_nfaces || !inout || !quad || nverts <= 0 || nfaces <= 0 ||
       nparts <= 0) {
     set_error("mnpbem_geom_create: invalid arguments");
@@ -328,7 +329,8 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   G->nverts = nverts;
   G->all_closed = (int)cs.size() == nparts;
   G->g.order = op.order;
-  mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, nfaces, cs.data(), ce.data(),
+  G->curved = faces2 != nullptr;
+  mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, faces2, nfaces, cs.data(), ce.data(),
                                    (int)cs.size(), quad, op.rel_cutoff, op.abs_cutoff, G->st);
   if (s == MNPBEM_OK) s = G->face_med.ensure(sizeof(int) * 2 * nfaces);
   if (s == MNPBEM_OK) {
@@ -386,6 +388,44 @@ mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int6
   if (lenv && atoi(lenv) > 0) G->lanes_req = std::min(MAX_LANES, atoi(lenv));
   *out = G;
   return MNPBEM_OK;
+}
+
+mnpbem_status mnpbem_geom_create(const double* verts, int64_t nverts, const int64_t* faces,
+                                 int64_t nfaces, int32_t nparts, const int64_t* part_nfaces,
+                                 const int32_t* inout, const int32_t* closed,
+                                 const mnpbem_quad* quad, const mnpbem_options* opts,
+                                 mnpbem_geom** out) {
+  return geom_create_impl(verts, nverts, faces, nullptr, nfaces, nparts, part_nfaces, inout, closed, quad,
+                          opts, out);
+}
+
+mnpbem_status mnpbem_geom_create_curved(const double* verts2, int64_t nverts2, const int64_t* faces2,
+                                        int64_t nfaces, int32_t nparts, const int64_t* part_nfaces,
+                                        const int32_t* inout, const int32_t* closed,
+                                        const mnpbem_quad* quad, const mnpbem_options* opts,
+                                        mnpbem_geom** out) {
+  if (!faces2 || nfaces <= 0 || nverts2 <= 0) {
+    set_error("mnpbem_geom_create_curved: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  // corners for the flat-element bookkeeping (bradius, face lists); the curved
+  // nodes must all exist: triangles use columns 0-2 and 4-6, quadrilaterals 0-8
+  std::vector<int64_t> corners(4 * (size_t)nfaces);
+  for (int64_t k = 0; k < nfaces; ++k) {
+    const int64_t* f = faces2 + 9 * k;
+    const bool quad4 = f[3] >= 0;
+    for (int c = 0; c < 9; ++c) {
+      const bool used = c < 3 || (c >= 4 && c <= 6) || (quad4 && (c == 3 || c == 7 || c == 8));
+      const int64_t v = f[c];
+      if ((used && (v < 0 || v >= nverts2)) || (!used && v != -1 && (v < 0 || v >= nverts2))) {
+        set_error("curved face %lld has an invalid node index in column %d", (long long)k, c);
+        return MNPBEM_ERR_INVALID_ARG;
+      }
+    }
+    for (int c = 0; c < 4; ++c) corners[4 * k + c] = f[c];
+  }
+  return geom_create_impl(verts2, nverts2, corners.data(), faces2, nfaces, nparts, part_nfaces, inout, closed,
+                          quad, opts, out);
 }
 
 mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g) {
@@ -1629,6 +1669,10 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
   }
   if (G->nparts != 1 || !G->all_closed || G->inout[0] == G->inout[1] || exc->medium != G->inout[1]) {
     set_error("mnpbem_ext_gradient: one closed particle excited from its outside medium is required");
+    return MNPBEM_ERR_UNSUPPORTED;
+  }
+  if (G->curved) {
+    set_error("cross-section gradients are implemented for flat elements (norm_flat.m) only");
     return MNPBEM_ERR_UNSUPPORTED;
   }
   double sol_ext[4] = {0, 0, 0, 0}, sol_sca[4] = {0, 0, 0, 0};

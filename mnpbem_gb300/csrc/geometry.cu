@@ -1,6 +1,7 @@
 // Geometry set-up of the retarded Green function, once per particle (FP64).
 //
 //  k_norm_flat      Particles/@particle/private/norm_flat.m:8-62 (+ Misc/+misc/bradius.m:11-32)
+//  k_norm_curv      Particles/@particle/private/norm_curv.m:8-62, quad_curv.m:13-59 (curved elements)
 //  k_ref_count /    Greenfun/+green/refinematrix.m:28-68 with Misc/+misc/pdist2.m:13-17
 //  k_ref_fill       (pattern 2 = self element, 1 = near pair), in MATLAB find() order
 //  k_ref_diag_*     Greenfun/@greenret/private/init.m:42-95   (polar integration, 'cart')
@@ -19,6 +20,54 @@ __device__ __forceinline__ double3 cross3(double3 a, double3 b) {
 }
 __device__ __forceinline__ double3 ld3(const double* p, int64_t i) { return d3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 __device__ __forceinline__ void st3(double* p, int64_t i, double3 v) { p[3 * i] = v.x; p[3 * i + 1] = v.y; p[3 * i + 2] = v.z; }
+
+// ------------------------------------------------- curved element helpers
+// 6-node triangle (Misc/+shape/@tri/eval.m:16-22, deriv.m:45-56): corners 1-3,
+// midpoints of edges 12, 23, 31
+__device__ __forceinline__ void shape6(double x, double y, double* s, double* sx, double* sy) {
+  const double z = 1 - x - y;
+  s[0] = x * (2 * x - 1); s[1] = y * (2 * y - 1); s[2] = z * (2 * z - 1);
+  s[3] = 4 * x * y; s[4] = 4 * y * z; s[5] = 4 * z * x;
+  sx[0] = 4 * x - 1; sx[1] = 0; sx[2] = 1 - 4 * z; sx[3] = 4 * y; sx[4] = -4 * y; sx[5] = 4 * (z - x);
+  sy[0] = 0; sy[1] = 4 * y - 1; sy[2] = 1 - 4 * z; sy[3] = 4 * x; sy[4] = 4 * (z - y); sy[5] = -4 * x;
+}
+// 9-node quadrilateral (Misc/+shape/@quad/eval.m:19-27, deriv.m:47-66): corners
+// 1-4, midpoints of edges 12, 23, 34, 41, centre
+__device__ __forceinline__ void shape9(double x, double y, double* s, double* sx, double* sy) {
+  const double a0 = 0.5 * x * (x - 1), a1 = 1 - x * x, a2 = 0.5 * x * (1 + x);
+  const double b0 = 0.5 * y * (y - 1), b1 = 1 - y * y, b2 = 0.5 * y * (1 + y);
+  const double da0 = x - 0.5, da1 = -2 * x, da2 = x + 0.5;
+  const double db0 = y - 0.5, db1 = -2 * y, db2 = y + 0.5;
+  s[0] = a0 * b0; s[1] = a2 * b0; s[2] = a2 * b2; s[3] = a0 * b2; s[4] = a1 * b0;
+  s[5] = a2 * b1; s[6] = a1 * b2; s[7] = a0 * b1; s[8] = a1 * b1;
+  sx[0] = da0 * b0; sx[1] = da2 * b0; sx[2] = da2 * b2; sx[3] = da0 * b2; sx[4] = da1 * b0;
+  sx[5] = da2 * b1; sx[6] = da1 * b2; sx[7] = da0 * b1; sx[8] = da1 * b1;
+  sy[0] = a0 * db0; sy[1] = a2 * db0; sy[2] = a2 * db2; sy[3] = a0 * db2; sy[4] = a1 * db0;
+  sy[5] = a2 * db1; sy[6] = a1 * db2; sy[7] = a0 * db1; sy[8] = a1 * db1;
+}
+// 6-node triangles of a curved element (totriangles_curv.m:22-30): a triangle,
+// or the halves (1,2,3,5,6,9) and (3,4,1,7,8,9) of a quadrilateral
+__device__ __forceinline__ void curv_tri_nodes(const int* f2, int t, int* nd) {
+  if (f2[3] < 0) { nd[0] = f2[0]; nd[1] = f2[1]; nd[2] = f2[2]; nd[3] = f2[4]; nd[4] = f2[5]; nd[5] = f2[6]; }
+  else if (t == 0) { nd[0] = f2[0]; nd[1] = f2[1]; nd[2] = f2[2]; nd[3] = f2[4]; nd[4] = f2[5]; nd[5] = f2[8]; }
+  else { nd[0] = f2[2]; nd[1] = f2[3]; nd[2] = f2[0]; nd[3] = f2[6]; nd[4] = f2[7]; nd[5] = f2[8]; }
+}
+// point and weight 0.5 w |dp/dx x dp/dy| of a 6-node triangle (quad_curv.m:39-54)
+__device__ __forceinline__ void curv_tri_point(const double* verts, const int* nd, double x, double y, double w,
+                                               double3& p, double& wt) {
+  double s[6], sx[6], sy[6];
+  shape6(x, y, s, sx, sy);
+  double3 px = d3(0, 0, 0), py = d3(0, 0, 0);
+  p = d3(0, 0, 0);
+  for (int k = 0; k < 6; ++k) {
+    const double3 v = ld3(verts, nd[k]);
+    p.x += s[k] * v.x; p.y += s[k] * v.y; p.z += s[k] * v.z;
+    px.x += sx[k] * v.x; px.y += sx[k] * v.y; px.z += sx[k] * v.z;
+    py.x += sy[k] * v.x; py.y += sy[k] * v.y; py.z += sy[k] * v.z;
+  }
+  const double3 nv = cross3(px, py);
+  wt = 0.5 * w * sqrt(dot3(nv, nv));
+}
 
 // ------------------------------------------------------------------ norm_flat
 __global__ void k_norm_flat(int n, const double* __restrict__ verts, const int* __restrict__ faces,
@@ -64,6 +113,67 @@ __global__ void k_norm_flat(int n, const double* __restrict__ verts, const int* 
   for (int k = 0; k < nvx; ++k) {
     double3 d = sub3(p, ld3(verts, f[k]));
     r = fmax(r, sqrt(d.x * d.x + d.y * d.y + d.z * d.z));
+  }
+  rad[i] = r;
+}
+
+// ------------------------------------------------------------------ norm_curv
+// Curved elements: area = sum of the boundary-element weights of quad_curv.m
+// over the element's 6-node triangles; centroid and tangent vectors from the
+// shape functions at the centre (norm_curv.m:22-51); orthonormal basis as in
+// norm_curv.m:54-59.  bradius uses the corner vertices.
+__global__ void k_norm_curv(int n, const double* __restrict__ verts, const int* __restrict__ faces2,
+                            const double* __restrict__ xt, const double* __restrict__ yt,
+                            const double* __restrict__ wt, int ntri, double* pos, double* nvec, double* tvec1,
+                            double* tvec2, double* area, double* rad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int* f2 = faces2 + 9 * i;
+  const bool quad = f2[3] >= 0;
+  double ar = 0.0;
+  for (int t = 0; t < (quad ? 2 : 1); ++t) {
+    int nd[6];
+    curv_tri_nodes(f2, t, nd);
+    for (int q = 0; q < ntri; ++q) {
+      double3 p;
+      double w;
+      curv_tri_point(verts, nd, xt[q], yt[q], wt[q], p, w);
+      ar += w;
+    }
+  }
+  int nd[6];
+  curv_tri_nodes(f2, 0, nd);
+  double3 p = d3(0, 0, 0), a = d3(0, 0, 0), b = d3(0, 0, 0);
+  if (!quad) {
+    const double c[6] = {-1.0 / 9, -1.0 / 9, -1.0 / 9, 4.0 / 9, 4.0 / 9, 4.0 / 9};
+    const double cx[6] = {1.0 / 3, 0.0, -1.0 / 3, 4.0 / 3, -4.0 / 3, 0.0};
+    const double cy[6] = {0.0, 1.0 / 3, -1.0 / 3, 4.0 / 3, 0.0, -4.0 / 3};
+    for (int k = 0; k < 6; ++k) {
+      const double3 v = ld3(verts, nd[k]);
+      p.x += c[k] * v.x; p.y += c[k] * v.y; p.z += c[k] * v.z;
+      a.x += cy[k] * v.x; a.y += cy[k] * v.y; a.z += cy[k] * v.z;
+      b.x += cx[k] * v.x; b.y += cx[k] * v.y; b.z += cx[k] * v.z;
+    }
+  } else {
+    p = ld3(verts, nd[5]);   // quadrilateral centre
+    const double cx[6] = {1.0, 0.0, -1.0, 0.0, 0.0, 0.0};
+    const double cy[6] = {0.0, -1.0, -1.0, 2.0, 2.0, -2.0};
+    for (int k = 0; k < 6; ++k) {
+      const double3 v = ld3(verts, nd[k]);
+      a.x += cy[k] * v.x; a.y += cy[k] * v.y; a.z += cy[k] * v.z;
+      b.x += cx[k] * v.x; b.y += cx[k] * v.y; b.z += cx[k] * v.z;
+    }
+  }
+  double3 nn = cross3(a, b);
+  const double ln = sqrt(dot3(nn, nn)), la = sqrt(dot3(a, a));
+  nn = d3(nn.x / ln, nn.y / ln, nn.z / ln);
+  const double3 t1 = d3(a.x / la, a.y / la, a.z / la);
+  st3(pos, i, p); st3(nvec, i, nn); st3(tvec1, i, t1); st3(tvec2, i, cross3(nn, t1));
+  area[i] = ar;
+  double r = 0.0;
+  for (int k = 0; k < (quad ? 4 : 3); ++k) {
+    const double3 d = sub3(p, ld3(verts, f2[k]));
+    r = fmax(r, sqrt(dot3(d, d)));
   }
   rad[i] = r;
 }
@@ -135,6 +245,29 @@ struct PolPoint { double3 p; double w; };
 __device__ __forceinline__ PolPoint polar_point(const GeomDev& g, int j, int q) {
   const int* f = g.faces + 4 * j;
   PolPoint r;
+  if (g.faces2) {
+    // curved elements (quadpol_curv.m:34-85)
+    const int* f2 = g.faces2 + 9 * j;
+    if (f2[3] < 0) {
+      int nd[6];
+      curv_tri_nodes(f2, 0, nd);
+      curv_tri_point(g.verts, nd, g.x3[q], g.y3[q], g.w3[q], r.p, r.w);
+    } else {
+      double s[9], sx[9], sy[9];
+      shape9(g.x4[q], g.y4[q], s, sx, sy);
+      double3 p = d3(0, 0, 0), px = d3(0, 0, 0), py = d3(0, 0, 0);
+      for (int k = 0; k < 9; ++k) {
+        const double3 v = ld3(g.verts, f2[k]);
+        p.x += s[k] * v.x; p.y += s[k] * v.y; p.z += s[k] * v.z;
+        px.x += sx[k] * v.x; px.y += sx[k] * v.y; px.z += sx[k] * v.z;
+        py.x += sy[k] * v.x; py.y += sy[k] * v.y; py.z += sy[k] * v.z;
+      }
+      const double3 nv = cross3(px, py);
+      r.p = p;
+      r.w = g.w4[q] * sqrt(dot3(nv, nv));
+    }
+    return r;
+  }
   if (f[3] < 0) {
     double x = g.x3[q], y = g.y3[q];
     double3 v1 = ld3(g.verts, f[0]), v2 = ld3(g.verts, f[1]), v3 = ld3(g.verts, f[2]);
@@ -269,11 +402,19 @@ __global__ void k_ref_offdiag(GeomDev g, const int* __restrict__ off_idx, int no
     double3 va = ld3(g.verts, a), vb = ld3(g.verts, b), vc = ld3(g.verts, c);
     double3 nv = cross3(sub3(vb, va), sub3(vc, va));
     double atri = 0.5 * sqrt(dot3(nv, nv));
+    int nd[6];
+    if (g.faces2) curv_tri_nodes(g.faces2 + 9 * j, tr, nd);
     for (int q = 0; q < g.ntri; ++q) {
       double x = g.xt[q], y = g.yt[q], z = 1 - x - y;
-      double3 pt = d3(x * va.x + y * vb.x + z * vc.x, x * va.y + y * vb.y + z * vc.y,
-                      x * va.z + y * vb.z + z * vc.z);
-      double w = g.wt[q] * atri;
+      double3 pt;
+      double w;
+      if (g.faces2) {
+        // curved elements: quad_curv.m:39-54
+        curv_tri_point(g.verts, nd, x, y, g.wt[q], pt, w);
+      } else {
+        pt = d3(x * va.x + y * vb.x + z * vc.x, x * va.y + y * vb.y + z * vc.y, x * va.z + y * vb.z + z * vc.z);
+        w = g.wt[q] * atri;
+      }
       double3 v = sub3(pi, pt);
       double r = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
       double dr = r - r0;
@@ -357,7 +498,8 @@ __global__ void k_closed_sum(GeomDev g, int s, int e, const int64_t* __restrict_
 
 // ============================================================== host driver
 mnpbem_status geometry_build(GeomDev& g, DevBufSet& b, const double* verts, int64_t nverts,
-                             const int64_t* faces, int64_t nfaces, const int* closed_part_start,
+                             const int64_t* faces, const int64_t* faces2, int64_t nfaces,
+                             const int* closed_part_start,
                              const int* closed_part_end, int nclosed, const mnpbem_quad* quad,
                              double rel_cut, double abs_cut, cudaStream_t st) {
   const int n = (int)nfaces;
@@ -372,6 +514,15 @@ mnpbem_status geometry_build(GeomDev& g, DevBufSet& b, const double* verts, int6
     MNP_TRY(b.faces.ensure(sizeof(int) * 4 * n));
     MNP_CUDA(cudaMemcpyAsync(b.faces.ptr, f32.data(), sizeof(int) * 4 * n, cudaMemcpyHostToDevice, st));
     MNP_CUDA(cudaStreamSynchronize(st));
+  }
+  g.faces2 = nullptr;
+  if (faces2) {
+    std::vector<int> f9(9 * (size_t)n);
+    for (int64_t k = 0; k < 9 * nfaces; ++k) f9[k] = (int)faces2[k];
+    MNP_TRY(b.faces2.ensure(sizeof(int) * 9 * n));
+    MNP_CUDA(cudaMemcpyAsync(b.faces2.ptr, f9.data(), sizeof(int) * 9 * n, cudaMemcpyHostToDevice, st));
+    MNP_CUDA(cudaStreamSynchronize(st));
+    g.faces2 = b.faces2.as<int>();
   }
   {
     std::vector<double> q;
@@ -398,8 +549,12 @@ mnpbem_status geometry_build(GeomDev& g, DevBufSet& b, const double* verts, int6
   g.pos = G; g.nvec = G + 3 * n; g.tvec1 = G + 6 * n; g.tvec2 = G + 9 * n; g.area = G + 12 * n;
   g.rad = G + 13 * n;
   if (ps.p) ps.p->acc[PH_GEOMETRY].launches += 1;
-  k_norm_flat<<<(n + 127) / 128, 128, 0, st>>>(n, g.verts, g.faces, g.pos, g.nvec, g.tvec1, g.tvec2,
-                                                 g.area, g.rad);
+  if (g.faces2)
+    k_norm_curv<<<(n + 127) / 128, 128, 0, st>>>(n, g.verts, g.faces2, g.xt, g.yt, g.wt, g.ntri, g.pos, g.nvec,
+                                                   g.tvec1, g.tvec2, g.area, g.rad);
+  else
+    k_norm_flat<<<(n + 127) / 128, 128, 0, st>>>(n, g.verts, g.faces, g.pos, g.nvec, g.tvec1, g.tvec2,
+                                                   g.area, g.rad);
   MNP_CHECK_LAUNCH();
   // ---- refinement pattern
   DevBuf counts;

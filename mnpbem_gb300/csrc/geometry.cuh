@@ -15,6 +15,7 @@ struct GeomDev {
   // geometry [n][3] / [n]
   const double* verts = nullptr;
   const int* faces = nullptr;   // [n][4], -1 = triangle
+  const int* faces2 = nullptr;  // [n][9] curved elements (corners, edge midpoints, quad centre), or null
   double *pos = nullptr, *nvec = nullptr, *tvec1 = nullptr, *tvec2 = nullptr, *area = nullptr,
          *rad = nullptr;
   // quadrature rules
@@ -32,11 +33,14 @@ struct GeomDev {
 };
 
 struct DevBufSet {
-  DevBuf verts, faces, quad, geo, col_off, ref_idx, ref_coef, part;
+  DevBuf verts, faces, faces2, quad, geo, col_off, ref_idx, ref_coef, part;
 };
 
+// faces2: NULL for flat elements, else [nfaces][9] curved connectivity into
+// verts (interp = 'curv'; faces then holds the corners, faces2[:, 0:4])
 mnpbem_status geometry_build(GeomDev& g, DevBufSet& b, const double* verts, int64_t nverts,
-                             const int64_t* faces, int64_t nfaces, const int* closed_part_start,
+                             const int64_t* faces, const int64_t* faces2, int64_t nfaces,
+                             const int* closed_part_start,
                              const int* closed_part_end, int nclosed, const mnpbem_quad* quad,
                              double rel_cut, double abs_cut, cudaStream_t st);
 

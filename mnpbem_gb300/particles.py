@@ -98,27 +98,84 @@ def _norm_flat(verts, faces):
     return pos, nn, np.cross(nn, t1), t1, area[:n]
 
 
+def _tri6(x, y):
+    z = 1 - x - y
+    s = np.stack([x * (2 * x - 1), y * (2 * y - 1), z * (2 * z - 1), 4 * x * y, 4 * y * z, 4 * z * x], 1)
+    sx = np.stack([4 * x - 1, 0 * y, 1 - 4 * z, 4 * y, -4 * y, 4 * (z - x)], 1)
+    sy = np.stack([0 * x, 4 * y - 1, 1 - 4 * z, 4 * x, 4 * (z - y), -4 * x], 1)
+    return s, sx, sy
+
+
+def _norm_curv(verts2, faces2, quad):
+    """Curved elements (norm_curv.m:8-62): area from the quad_curv.m weights,
+    centroid and basis from the 6-node shape functions at the centre."""
+    tri = faces2[:, 3] < 0
+    n = faces2.shape[0]
+    t1 = np.where(tri[:, None], faces2[:, [0, 1, 2, 4, 5, 6]], faces2[:, [0, 1, 2, 4, 5, 8]])
+    s, sx, sy = _tri6(quad.x, quad.y)
+
+    def tri_area(nodes):
+        vv = verts2[nodes]
+        nv = np.cross(np.einsum("pk,tkc->tpc", sx, vv), np.einsum("pk,tkc->tpc", sy, vv))
+        return np.sum(0.5 * quad.w[None, :] * np.linalg.norm(nv, axis=2), 1)
+    area = tri_area(t1)
+    q = np.nonzero(~tri)[0]
+    if q.size:
+        area[q] += tri_area(faces2[q][:, [2, 3, 0, 6, 7, 8]])
+    vv = verts2[t1]
+    c = np.array([-1, -1, -1, 4, 4, 4]) / 9
+    cx, cy = np.array([1, 0, -1, 4, -4, 0]) / 3, np.array([0, 1, -1, 4, 0, -4]) / 3
+    qx, qy = np.array([1, 0, -1, 0, 0, 0], float), np.array([0, -1, -1, 2, 2, -2], float)
+    pos = np.where(tri[:, None], np.einsum("k,tkc->tc", c, vv), verts2[t1[:, 5]])
+    a = np.where(tri[:, None], np.einsum("k,tkc->tc", cy, vv), np.einsum("k,tkc->tc", qy, vv))
+    b = np.where(tri[:, None], np.einsum("k,tkc->tc", cx, vv), np.einsum("k,tkc->tc", qx, vv))
+    nn = np.cross(a, b)
+    nn /= np.linalg.norm(nn, axis=1)[:, None]
+    t1v = a / np.linalg.norm(a, axis=1)[:, None]
+    return pos, nn, np.cross(nn, t1v), t1v, area
+
+
 class particle:
-    """Flat-faced discretised surface: ``verts [nv, 3]``, ``faces [n, 4]``
-    (-1 in the 4th column for triangles; a ``[n, 3]`` array is accepted)."""
+    """Discretised surface: ``verts [nv, 3]``, ``faces [n, 4]`` (-1 in the 4th
+    column for triangles; a ``[n, 3]`` array is accepted).  As in MNPBEM
+    (Particles/@particle/init.m:17-38), ``faces [n, 9]`` gives the nodes of
+    curved elements (``verts2`` / ``faces2``: corners, edge midpoints,
+    quadrilateral centre; -1 or NaN where unused); ``op['interp']`` selects
+    flat (default, the corners) or curved ('curv') elements."""
 
     def __init__(self, verts, faces, op=None):
         verts = np.ascontiguousarray(verts, dtype=np.float64)
         faces = np.asarray(faces)
-        if faces.ndim != 2 or faces.shape[1] not in (3, 4):
-            raise ValueError("faces must be [n, 3] or [n, 4]")
-        if faces.shape[1] == 3:
-            faces = np.hstack([faces, -np.ones((faces.shape[0], 1), dtype=np.int64)])
+        if faces.ndim != 2 or faces.shape[1] not in (3, 4, 9):
+            raise ValueError("faces must be [n, 3], [n, 4] or [n, 9]")
         if np.issubdtype(faces.dtype, np.floating):
             faces = np.where(np.isnan(faces), -1, faces)
+        faces = faces.astype(np.int64)
+        if faces.shape[1] == 3:
+            faces = np.hstack([faces, -np.ones((faces.shape[0], 1), dtype=np.int64)])
+        self.verts2 = self.faces2 = None
+        if faces.shape[1] == 9:
+            self.verts2, self.faces2 = verts, np.ascontiguousarray(faces)
+            faces = faces[:, :4]
         self.verts = verts
         self.faces = np.ascontiguousarray(faces, dtype=np.int64)
         op = op or {}
+        self.op = dict(op)
         self.interp = op.get("interp", "flat")
-        if self.interp != "flat":
-            raise NotImplementedError("only interp='flat' boundaries are implemented")
+        if self.interp not in ("flat", "curv"):
+            raise ValueError("interp must be 'flat' or 'curv'")
         self.quad = quadface(op.get("npol", (7, 5)))
-        self.pos, self.nvec, self.tvec2, self.tvec1, self.area = _norm_flat(self.verts, self.faces)
+        if self.interp == "curv":
+            if self.faces2 is None:
+                # curved elements through flat midpoints (midpoints.m, key 'flat')
+                self.verts2, self.faces2 = shapes.midpoints_flat(self.verts, self.faces)
+            self.pos, self.nvec, self.tvec2, self.tvec1, self.area = _norm_curv(self.verts2, self.faces2, self.quad)
+        else:
+            self.pos, self.nvec, self.tvec2, self.tvec1, self.area = _norm_flat(self.verts, self.faces)
+
+    @property
+    def curved(self):
+        return self.interp == "curv"
 
     @property
     def n(self):
@@ -127,12 +184,19 @@ class particle:
     nfaces = n
 
     def shift(self, vec):
-        return particle(self.verts + np.asarray(vec, dtype=np.float64)[None, :], self.faces,
-                        {"npol": self.quad.npol})
+        d = np.asarray(vec, dtype=np.float64)[None, :]
+        if self.faces2 is not None:
+            return particle(self.verts2 + d, self.faces2, self.op)
+        return particle(self.verts + d, self.faces, self.op)
 
 
 def trisphere(n, diameter=1.0, op=None):
-    """Sphere triangulated from the stored point set closest to ``n`` points."""
+    """Sphere triangulated from the stored point set closest to ``n`` points;
+    with ``op['interp'] = 'curv'`` the curved elements of trisphere.m:54-61
+    (edge midpoints on the sphere)."""
+    if (op or {}).get("interp", "flat") == "curv":
+        v2, f2 = shapes.trisphere_curved(n, diameter)
+        return particle(v2, f2, op)
     v, f = shapes.trisphere(n, diameter)
     return particle(v, f, op)
 
@@ -174,6 +238,24 @@ class comparticle:
             voff += q.verts.shape[0]
         self.verts = np.ascontiguousarray(np.vstack(verts))
         self.faces = np.ascontiguousarray(np.vstack(faces))
+        # a compound with a curved particle is curved as a whole; flat members
+        # enter with flat midpoints, which reproduce their flat elements
+        self.curved = any(q.curved for q in self.p)
+        self.verts2 = self.faces2 = None
+        if self.curved:
+            v2s, f2s, voff = [], [], 0
+            for q in self.p:
+                if q.curved:
+                    v2, f2 = q.verts2, q.faces2
+                else:
+                    v2, f2 = shapes.midpoints_flat(q.verts, q.faces)
+                f2 = f2.copy()
+                f2[f2 >= 0] += voff
+                v2s.append(v2)
+                f2s.append(f2)
+                voff += v2.shape[0]
+            self.verts2 = np.ascontiguousarray(np.vstack(v2s))
+            self.faces2 = np.ascontiguousarray(np.vstack(f2s))
         self.pos = np.vstack([q.pos for q in self.p])
         self.nvec = np.vstack([q.nvec for q in self.p])
         self.area = np.concatenate([q.area for q in self.p])

@@ -60,6 +60,52 @@ def trisphere(n, diameter=1.0):
     return verts, faces
 
 
+def midpoints_flat(verts, faces):
+    """Nodes of curved elements from flat ones (Particles/@particle/midpoints.m,
+    key 'flat'): every edge gets its midpoint and every quadrilateral its
+    centroid.  Returns ``verts2`` (the corners, then the new nodes) and
+    ``faces2 [n, 9]`` (corners 0-3 with -1 for triangles, midpoints of edges
+    12, 23, 34 (31), 41 in 4-7, quadrilateral centre in 8; -1 where unused)."""
+    verts = np.asarray(verts, dtype=np.float64)
+    faces = np.asarray(faces, dtype=np.int64)
+    if faces.shape[1] == 3:
+        faces = np.hstack([faces, -np.ones((faces.shape[0], 1), np.int64)])
+    n, nv = faces.shape[0], verts.shape[0]
+    quad = faces[:, 3] >= 0
+    # edges of every face in order, as (min, max) vertex pairs
+    k = np.where(quad, 4, 3)
+    a_list, b_list, slot = [], [], []
+    for e in range(4):
+        m = e < k
+        a = faces[m, e]
+        b = np.where(e + 1 < k[m], faces[m, (e + 1) % 4], faces[m, 0])
+        a_list.append(a); b_list.append(b); slot.append((np.nonzero(m)[0], e))
+    lo = np.concatenate([np.minimum(a, b) for a, b in zip(a_list, b_list)])
+    hi = np.concatenate([np.maximum(a, b) for a, b in zip(a_list, b_list)])
+    uniq, inv = np.unique(lo * (nv + 1) + hi, return_inverse=True)
+    ulo, uhi = uniq // (nv + 1), uniq % (nv + 1)
+    faces2 = -np.ones((n, 9), np.int64)
+    faces2[:, :4] = faces
+    off = 0
+    for (rows, e) in slot:
+        faces2[rows, 4 + e] = nv + inv[off:off + rows.size]
+        off += rows.size
+    mids = 0.5 * (verts[ulo] + verts[uhi])
+    iq = np.nonzero(quad)[0]
+    faces2[iq, 8] = nv + uniq.size + np.arange(iq.size)
+    cents = 0.25 * verts[faces[iq, :4]].sum(1) if iq.size else np.zeros((0, 3))
+    return np.vstack([verts, mids, cents]), faces2
+
+
+def trisphere_curved(n, diameter=1.0):
+    """``trisphere`` with the curved-element nodes of trisphere.m:54-61: edge
+    midpoints projected onto the sphere.  Returns ``verts2, faces2``."""
+    v, f = trisphere(n, diameter)
+    v2, f2 = midpoints_flat(v, f)
+    v2 = 0.5 * diameter * v2 / np.sqrt(np.sum(v2 * v2, 1))[:, None]
+    return v2, f2
+
+
 def fibsphere(n_faces, diameter=1.0, center=(0.0, 0.0, 0.0)):
     """Deterministic sphere with ``n_faces`` (even) flat triangles."""
     npts = n_faces // 2 + 2

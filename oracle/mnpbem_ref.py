@@ -123,10 +123,77 @@ def _quad_shape(x, y):
     return s, sx, sy
 
 
-class Particle:
-    """Flat-faced particle: ``pos``, ``area``, ``tvec1``, ``tvec2``, ``nvec``."""
+def _tri6_shape(x, y):
+    """6-node triangle shape functions and first derivatives
+    (Misc/+shape/@tri/eval.m:16-22, deriv.m:45-56): nodes 1-3 corners,
+    4-6 the midpoints of edges 12, 23, 31."""
+    x, y = np.asarray(x, float), np.asarray(y, float)
+    z = 1 - x - y
+    s = np.stack([x * (2 * x - 1), y * (2 * y - 1), z * (2 * z - 1), 4 * x * y, 4 * y * z, 4 * z * x], 1)
+    sx = np.stack([4 * x - 1, 0 * y, 1 - 4 * z, 4 * y, -4 * y, 4 * (z - x)], 1)
+    sy = np.stack([0 * x, 4 * y - 1, 1 - 4 * z, 4 * x, 4 * (z - y), -4 * x], 1)
+    return s, sx, sy
 
-    def __init__(self, verts, faces, quad):
+
+def _quad9_shape(x, y):
+    """9-node quadrilateral shape functions and first derivatives
+    (Misc/+shape/@quad/eval.m:19-27, deriv.m:47-66): corners 1-4, edge
+    midpoints 5-8 (edges 12, 23, 34, 41), centre 9."""
+    x, y = np.asarray(x, float), np.asarray(y, float)
+
+    def asm(a, b):
+        return np.stack([a[0] * b[0], a[2] * b[0], a[2] * b[2], a[0] * b[2], a[1] * b[0], a[2] * b[1],
+                         a[1] * b[2], a[0] * b[1], a[1] * b[1]], 1)
+    sx0 = [0.5 * x * (x - 1), 1 - x ** 2, 0.5 * x * (1 + x)]
+    sy0 = [0.5 * y * (y - 1), 1 - y ** 2, 0.5 * y * (1 + y)]
+    sx1 = [x - 0.5, -2 * x, x + 0.5]
+    sy1 = [y - 0.5, -2 * y, y + 0.5]
+    return asm(sx0, sy0), asm(sx1, sy0), asm(sx0, sy1)
+
+
+def midpoints_flat(verts, faces):
+    """Edge midpoints and quadrilateral centroids for curved interpolation
+    (Particles/@particle/midpoints.m:16-45, key 'flat'): returns ``verts2``
+    (the corner vertices followed by the new points) and ``faces2 [n, 9]``
+    (corners 0-3, -1 for triangles; edge midpoints 4-7; quadrilateral centre 8).
+    The numbering of the new points follows this function's own edge order."""
+    verts = np.asarray(verts, float)
+    faces = np.asarray(faces, np.int64)
+    if faces.shape[1] == 3:
+        faces = np.hstack([faces, -np.ones((faces.shape[0], 1), np.int64)])
+    n, nv = faces.shape[0], verts.shape[0]
+    edge_id, new = {}, []
+    faces2 = -np.ones((n, 9), np.int64)
+    faces2[:, :4] = faces
+    for i in range(n):
+        k = 3 if faces[i, 3] < 0 else 4
+        for e in range(k):
+            a, b = int(faces[i, e]), int(faces[i, (e + 1) % k])
+            key = (min(a, b), max(a, b))
+            if key not in edge_id:
+                edge_id[key] = nv + len(new)
+                new.append(0.5 * (verts[a] + verts[b]))
+            faces2[i, 4 + e] = edge_id[key]
+    ind4 = np.nonzero(faces[:, 3] >= 0)[0]
+    for i in ind4:
+        faces2[i, 8] = nv + len(new)
+        new.append(0.25 * verts[faces[i, :4]].sum(0))
+    verts2 = np.vstack([verts] + ([np.asarray(new)] if new else []))
+    return verts2, faces2
+
+
+class Particle:
+    """Particle boundary: ``pos``, ``area``, ``tvec1``, ``tvec2``, ``nvec``.
+
+    Flat faces (``interp = 'flat'``, norm_flat.m) by default; with
+    ``verts2, faces2`` (9-node connectivity, midpoints.m) and
+    ``interp = 'curv'`` the elements are the quadratic (6-node triangle,
+    9-node quadrilateral) interpolations of norm_curv.m, quad_curv.m and
+    quadpol_curv.m.  ``verts`` / ``faces`` hold the corner vertices (the
+    flat particle and bradius.m use them).
+    """
+
+    def __init__(self, verts, faces, quad, verts2=None, faces2=None, interp="flat"):
         self.verts = np.asarray(verts, dtype=float)
         faces = np.asarray(faces, dtype=np.int64)
         if faces.shape[1] == 3:
@@ -134,7 +201,21 @@ class Particle:
         self.faces = faces
         self.quad = quad
         self.n = faces.shape[0]
-        self._norm_flat()
+        self.interp = interp
+        self.verts2 = None if verts2 is None else np.asarray(verts2, float)
+        self.faces2 = None if faces2 is None else np.asarray(faces2, np.int64)
+        if interp == "curv":
+            if self.verts2 is None:
+                raise ValueError("interp='curv' needs verts2 / faces2")
+            self._norm_curv()
+        else:
+            self._norm_flat()
+
+    @classmethod
+    def curved(cls, verts2, faces2, quad):
+        """Curved particle from 9-node connectivity into ``verts2``."""
+        faces2 = np.asarray(faces2, np.int64)
+        return cls(verts2, faces2[:, :4], quad, verts2, faces2, "curv")
 
     # index34.m
     def index34(self, ind=None):
@@ -179,12 +260,70 @@ class Particle:
         self.pos = pos
         self.tvec1, self.tvec2, self.nvec = vec1[:n], vec2[:n], nvec[:n]
 
+    # totriangles_curv.m:14-31 (6-node triangles; quads split into (1,2,3,5,6,9), (3,4,1,7,8,9))
+    def totriangles_curv(self, ind=None):
+        ind = np.arange(self.n) if ind is None else np.asarray(ind)
+        _, i4 = self.index34(ind)
+        f2 = self.faces2[ind]
+        faces = f2[:, [0, 1, 2, 4, 5, 6]].copy()
+        if i4.size:
+            faces[i4] = f2[i4][:, [0, 1, 2, 4, 5, 8]]
+            faces = np.vstack([faces, f2[i4][:, [2, 3, 0, 6, 7, 8]]])
+            i4 = np.stack([i4, ind.size + np.arange(i4.size)], 1)
+        else:
+            i4 = np.zeros((0, 2), np.int64)
+        return faces, i4
+
+    def _norm_curv(self):
+        """Centroids, areas and bases of curved elements (norm_curv.m:8-62)."""
+        n, v2 = self.n, self.verts2
+        _, w, row = self.quad_points(np.arange(n))
+        self.area = np.bincount(row, weights=w, minlength=n)
+        i3, i4 = self.index34()
+        faces, _ = self.totriangles_curv()
+        pos, vec1, vec2 = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+        if i3.size:
+            tri = np.array([-1, -1, -1, 4, 4, 4]) / 9
+            trix = np.array([1, 0, -1, 4, -4, 0]) / 3
+            triy = np.array([0, 1, -1, 4, 0, -4]) / 3
+            vv = v2[faces[i3]]
+            pos[i3] = np.einsum("k,fkc->fc", tri, vv)
+            vec1[i3] = np.einsum("k,fkc->fc", triy, vv)
+            vec2[i3] = np.einsum("k,fkc->fc", trix, vv)
+        if i4.size:
+            pos[i4] = v2[faces[i4, 5]]
+            trix = np.array([1, 0, -1, 0, 0, 0], float)
+            triy = np.array([0, -1, -1, 2, 2, -2], float)
+            vv = v2[faces[i4]]
+            vec1[i4] = np.einsum("k,fkc->fc", triy, vv)
+            vec2[i4] = np.einsum("k,fkc->fc", trix, vv)
+        nrm = lambda x: x / np.sqrt(np.sum(x * x, 1))[:, None]
+        nvec = nrm(np.cross(vec1, vec2))
+        vec1 = nrm(vec1)
+        self.pos, self.tvec1, self.tvec2, self.nvec = pos, vec1, np.cross(nvec, vec1), nvec
+
     def quad_points(self, ind):
-        """Boundary-element points/weights for faces ``ind`` (quad_flat.m:13-56).
+        """Boundary-element points/weights for faces ``ind`` (quad_flat.m:13-56,
+        quad_curv.m:13-59 for curved elements).
 
         Returns ``pos [m, 3]``, ``w [m]`` and ``row [m]`` (index into ``ind``).
         """
         ind = np.asarray(ind)
+        if self.interp == "curv":
+            faces, ind4 = self.totriangles_curv(ind)
+            ind3 = np.arange(ind.size)
+            if ind4.shape[0]:
+                ind3 = np.concatenate([ind3, ind4[:, 0]])
+            q = self.quad
+            s, sx, sy = _tri6_shape(q.x, q.y)
+            vv = self.verts2[faces]                     # [t, 6, 3]
+            pos = np.einsum("pk,tkc->tpc", s, vv).reshape(-1, 3)
+            px = np.einsum("pk,tkc->tpc", sx, vv)
+            py = np.einsum("pk,tkc->tpc", sy, vv)
+            nv = np.cross(px, py)
+            w = (0.5 * q.w[None, :] * np.sqrt(np.sum(nv * nv, 2))).ravel()
+            row = np.repeat(ind3, q.w.size)
+            return pos, w, row
         faces, ind4 = self.totriangles(ind)
         ind3 = np.arange(ind.size)
         if ind4.shape[0]:
@@ -200,11 +339,31 @@ class Particle:
         return pos, w, row
 
     def quadpol_points(self, ind):
-        """Polar points/weights around centroids (quadpol_flat.m:15-78)."""
+        """Polar points/weights around centroids (quadpol_flat.m:15-78,
+        quadpol_curv.m:15-88 for curved elements)."""
         ind = np.asarray(ind)
         i3, i4 = self.index34(ind)
         q, v = self.quad, self.verts
         pos, w, row = [], [], []
+        if self.interp == "curv":
+            f2, v2 = self.faces2, self.verts2
+            if i3.size:
+                s, sx, sy = _tri6_shape(q.x3, q.y3)
+                for i in i3:
+                    vv = v2[f2[ind[i], [0, 1, 2, 4, 5, 6]]]
+                    nv = np.cross(sx @ vv, sy @ vv)
+                    pos.append(s @ vv)
+                    w.append(0.5 * q.w3 * np.sqrt(np.sum(nv * nv, 1)))
+                    row.append(np.full(q.w3.size, i))
+            if i4.size:
+                s, sx, sy = _quad9_shape(q.x4, q.y4)
+                for i in i4:
+                    vv = v2[f2[ind[i], :9]]
+                    nv = np.cross(sx @ vv, sy @ vv)
+                    pos.append(s @ vv)
+                    w.append(q.w4 * np.sqrt(np.sum(nv * nv, 1)))
+                    row.append(np.full(q.w4.size, i))
+            return np.vstack(pos), np.concatenate(w), np.concatenate(row)
         if i3.size:
             tri = np.stack([q.x3, q.y3, 1 - q.x3 - q.y3], 1)
             for i in i3:
@@ -252,15 +411,32 @@ class ComParticle:
         offs = np.cumsum([0] + [p.n for p in parts])
         self.offsets = offs
         self.n = int(offs[-1])
+        curved = any(p.interp == "curv" for p in parts)
         verts, faces = [], []
         voff = 0
         for p in parts:
-            verts.append(p.verts)
-            f = p.faces.copy()
-            f[f >= 0] += voff
-            faces.append(f)
-            voff += p.verts.shape[0]
-        self.pc = Particle(np.vstack(verts), np.vstack(faces), parts[0].quad)
+            if curved:
+                # a compound is curved as a whole; flat members get flat midpoints
+                # (which reproduce their flat elements exactly)
+                if p.interp == "curv":
+                    v2, f2 = p.verts2, p.faces2
+                else:
+                    v2, f2 = midpoints_flat(p.verts, p.faces)
+                verts.append(v2)
+                f = f2.copy()
+                f[f >= 0] += voff
+                faces.append(f)
+                voff += v2.shape[0]
+            else:
+                verts.append(p.verts)
+                f = p.faces.copy()
+                f[f >= 0] += voff
+                faces.append(f)
+                voff += p.verts.shape[0]
+        if curved:
+            self.pc = Particle.curved(np.vstack(verts), np.vstack(faces), parts[0].quad)
+        else:
+            self.pc = Particle(np.vstack(verts), np.vstack(faces), parts[0].quad)
         self.pos, self.area, self.nvec = self.pc.pos, self.pc.area, self.pc.nvec
         self.tvec1, self.tvec2 = self.pc.tvec1, self.pc.tvec2
 
