@@ -301,6 +301,22 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key,
  * this stream after a call is ordered after all of the call's kernels.       */
 MNPBEM_API mnpbem_status mnpbem_geom_stream(const mnpbem_geom* g, void** stream);
 
+/* Electric and magnetic fields at points off the particle boundary
+ * (Greenfun/@compgreenret/field.m:17-38 on the Green function between a
+ * compoint and the particle; Simulation/misc/@meshfield): for a point in
+ * medium m, the faces whose inside (outside) medium is m contribute through
+ * sig1 / h1 (sig2 / h2); points within RelCutoff element radii of a face use
+ * the refined Taylor coefficients of the pair (refinematrix.m with the face's
+ * radius, greenret/private/init.m:98-177).
+ *   pts [npts][3]; pt_medium [npts] 1-based (compoint's inout)
+ *   eps_media [nmed] complex; sig1, sig2 [n][npol], h1, h2 [n][3][npol]
+ *   complex (mnpbem_solve's outputs for wavelength enei), host
+ *   e, h [npts][3][npol] complex (host; either may be NULL)                  */
+MNPBEM_API mnpbem_status mnpbem_fields(mnpbem_geom* g, int64_t npts, const double* pts,
+                                       const int32_t* pt_medium, double enei, const double* eps_media,
+                                       int32_t nmed, int32_t npol, const double* sig1, const double* sig2,
+                                       const double* h1, const double* h2, double* e, double* h);
+
 /* Message of the last failure on the calling thread ("" if none). */
 MNPBEM_API const char* mnpbem_last_error(void);
 

@@ -320,6 +320,66 @@ class bemret:
     solve = mldivide
 
 
+def point_media(p, pts):
+    """Medium of each point (compoint, Particles/@compoint/init.m:20-35): the
+    point is inside (outside) the face nearest to it when it lies behind (in
+    front of) that face's plane, and takes the face's inside (outside) medium.
+    The nearest face is the one with the nearest centroid (compoint measures
+    the distance to the element itself; the two agree away from the surface)."""
+    pts = np.asarray(pts, dtype=np.float64).reshape(-1, 3)
+    med = np.zeros(pts.shape[0], dtype=np.int32)
+    fmed = np.repeat(p.inout, [q.n for q in p.p], axis=0)
+    for s0 in range(0, pts.shape[0], 2048):
+        q = pts[s0:s0 + 2048]
+        d2 = np.sum((q[:, None, :] - p.pos[None, :, :]) ** 2, 2)
+        j = np.argmin(d2, 1)
+        side = np.sum((q - p.pos[j]) * p.nvec[j], 1) >= 0
+        med[s0:s0 + 2048] = np.where(side, fmed[j, 1], fmed[j, 0])
+    return med
+
+
+class meshfield:
+    """Electric and magnetic fields on a set of points (Simulation/misc/@meshfield).
+
+    ``meshfield(bem, x, y, z)`` with arrays of equal shape (or ``pts [m, 3]``
+    as ``x``); ``e, h = emesh(sig)`` for surface charges ``sig`` from
+    ``bem.mldivide`` (or ``bem \\ exc``), each shaped ``x.shape + (3, npol)``.
+    ``medium`` overrides the media of the points (1-based, compoint's inout).
+    Computed by ``mnpbem_fields`` on the GPU.
+    """
+
+    def __init__(self, bem, x, y=None, z=None, medium=None):
+        self.bem = bem
+        if y is None:
+            pts = np.asarray(x, dtype=np.float64).reshape(-1, 3)
+            self.shape = pts.shape[:1]
+        else:
+            x, y, z = np.broadcast_arrays(np.asarray(x, float), np.asarray(y, float), np.asarray(z, float))
+            self.shape = x.shape
+            pts = np.stack([x.ravel(), y.ravel(), z.ravel()], 1)
+        self.pts = np.ascontiguousarray(pts)
+        self.medium = (point_media(bem.p, self.pts) if medium is None
+                       else np.ascontiguousarray(np.broadcast_to(medium, self.pts.shape[0]), dtype=np.int32))
+
+    def __call__(self, sig):
+        b = self.bem
+        enei = float(sig.enei)
+        em = np.ascontiguousarray(b.p.eps_media(enei)[0])
+        s1 = np.ascontiguousarray(sig.sig1, dtype=np.complex128)
+        P = s1.shape[1]
+        s2 = np.ascontiguousarray(sig.sig2, dtype=np.complex128)
+        q1 = np.ascontiguousarray(sig.h1, dtype=np.complex128)
+        q2 = np.ascontiguousarray(sig.h2, dtype=np.complex128)
+        m = self.pts.shape[0]
+        e = np.zeros((m, 3, P), np.complex128)
+        h = np.zeros((m, 3, P), np.complex128)
+        _lib.check(b._lib.mnpbem_fields(
+            b._h, m, _lib.dptr(self.pts), self.medium.ctypes.data_as(_lib.c_int32_p), enei,
+            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, P,
+            s1.ctypes.data, s2.ctypes.data, q1.ctypes.data, q2.ctypes.data, e.ctypes.data, h.ctypes.data))
+        return e.reshape(self.shape + (3, P)), h.reshape(self.shape + (3, P))
+
+
 def spectrum_batch(items, fields=False):
     """Sweeps of several particles in one library call (``mnpbem_solve_batch``).
 

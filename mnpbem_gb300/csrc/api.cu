@@ -25,6 +25,7 @@
 #include "bem.cuh"
 #include "dense.cuh"
 #include "geometry.cuh"
+#include "field.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
 
@@ -131,6 +132,7 @@ struct mnpbem_geom {
   int64_t nverts = 0;
   bool all_closed = true;
   bool curved = false;       // curved (6-node / 9-node) elements: interp = 'curv'
+  double rel_cut = 3.0, abs_cut = 0.0;   // refinement cutoffs (RelCutoff, AbsCutoff)
   DevBuf d_part, d_src, d_nrm, d_srcf, d_nrmf, face_med, exbuf;
   DevBuf adj, adj2, adj_mats, adj_off;   // adjoint gradient workspace
   int adj_noff = -1;
@@ -330,6 +332,8 @@ static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const
   G->all_closed = (int)cs.size() == nparts;
   G->g.order = op.order;
   G->curved = faces2 != nullptr;
+  G->rel_cut = op.rel_cutoff;
+  G->abs_cut = op.abs_cutoff;
   mnpbem_status s = geometry_build(G->g, G->b, verts, nverts, faces, faces2, nfaces, cs.data(), ce.data(),
                                    (int)cs.size(), quad, op.rel_cutoff, op.abs_cutoff, G->st);
   if (s == MNPBEM_OK) s = G->face_med.ensure(sizeof(int) * 2 * nfaces);
@@ -1886,3 +1890,43 @@ mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps
 }
 
 }  // extern "C"
+
+mnpbem_status mnpbem_fields(mnpbem_geom* G, int64_t npts, const double* pts, const int32_t* pt_medium,
+                            double enei, const double* eps_media, int32_t nmed, int32_t npol,
+                            const double* sig1, const double* sig2, const double* h1, const double* h2,
+                            double* e, double* h) {
+  MNP_TRY(check_geom(G));
+  if (npts <= 0 || !pts || !pt_medium || !(enei > 0) || !eps_media || nmed < G->max_medium || npol < 1 ||
+      !sig1 || !sig2 || !h1 || !h2 || (!e && !h)) {
+    set_error("mnpbem_fields: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  const int64_t n = G->g.n;
+  const double k0 = 2 * M_PI / enei;
+  std::vector<double2> km(nmed);
+  for (int m = 0; m < nmed; ++m) {
+    const std::complex<double> kk = k0 * std::sqrt(std::complex<double>(eps_media[2 * m], eps_media[2 * m + 1]));
+    km[m] = make_double2(kk.real(), kk.imag());
+  }
+  DevBuf ds, dout;
+  MNP_TRY(ds.ensure(sizeof(double2) * 8 * n * npol));
+  MNP_TRY(dout.ensure(sizeof(double2) * 6 * npts * npol));
+  double2* S = ds.as<double2>();
+  double2 *s1 = S, *s2 = S + n * npol, *q1 = S + 2 * n * npol, *q2 = S + 5 * n * npol;
+  cudaStream_t st = G->st;
+  MNP_CUDA(cudaMemcpyAsync(s1, sig1, sizeof(double2) * n * npol, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(s2, sig2, sizeof(double2) * n * npol, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q1, h1, sizeof(double2) * 3 * n * npol, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q2, h2, sizeof(double2) * 3 * n * npol, cudaMemcpyHostToDevice, st));
+  double2* de = dout.as<double2>();
+  double2* dh = de + 3 * npts * npol;
+  MNP_TRY(point_fields(G->g, G->face_med.as<int>(), npts, pts, pt_medium, km.data(), nmed, k0, npol, s1, s2, q1, q2,
+                       de, dh, G->rel_cut, G->abs_cut, st));
+  if (e) MNP_CUDA(cudaMemcpyAsync(e, de, sizeof(double2) * 3 * npts * npol, cudaMemcpyDeviceToHost, st));
+  if (h) MNP_CUDA(cudaMemcpyAsync(h, dh, sizeof(double2) * 3 * npts * npol, cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  G->prof.flush();
+  return MNPBEM_OK;
+}

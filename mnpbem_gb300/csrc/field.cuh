@@ -1,0 +1,17 @@
+// Fields at points off the particle boundary.
+#pragma once
+#include "geometry.cuh"
+
+namespace mnpbem {
+
+// E and H [npts][3][npol] (complex128, device) at the points pts [npts][3]
+// (host) lying in the 1-based media pt_med (host) from the surface charges
+// sig1, sig2 [n][npol] and currents h1, h2 [n][3][npol] (device).  face_med:
+// device [2][n] 0-based inside / outside media of the faces; kmed [nmed]: the
+// media's wavenumbers; k0 = 2 pi / enei.
+mnpbem_status point_fields(const GeomDev& g, const int* face_med, int64_t npts, const double* pts,
+                           const int* pt_med, const double2* kmed, int nmed, double k0, int npol,
+                           const double2* sig1, const double2* sig2, const double2* h1, const double2* h2,
+                           double2* e, double2* h, double rel_cut, double abs_cut, cudaStream_t st);
+
+}  // namespace mnpbem

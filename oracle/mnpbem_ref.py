@@ -932,3 +932,99 @@ def solve_spectrum(cp, pw, eneis, order=5, rel_cutoff=3.0):
         sca.append(pw.scattering(cp, sig))
         sols.append(sig)
     return np.array(ext), np.array(sca), sols, bem
+
+
+# --------------------------------------------------------------------------
+# fields at points off the boundary (Greenfun/@compgreenret/field.m:17-38
+# with the Green function between a compoint and the particle:
+# refinematrix.m:27-67 for points (radius of the boundary element, no self
+# elements), greenret/private/init.m:98-177 near coefficients with the points
+# as first argument, eval1.m:18-40,110-124 for G and its Cartesian derivative)
+# --------------------------------------------------------------------------
+def point_refinement(cp, pts, rel_cutoff=3.0, abs_cutoff=0.0, order=5):
+    """Refined (point, face) pairs and their Taylor coefficients.
+
+    Returns ``rows, cols`` (point, face) in row-major order and ``g [m,
+    order+1]``, ``f [m, 3, order+1]``.
+    """
+    pts = np.asarray(pts, float)
+    rad2 = cp.bradius()
+    d = np.sqrt(np.sum((pts[:, None, :] - cp.pos[None, :, :]) ** 2, 2))
+    d2 = d - rad2[None, :]
+    ir = (d2 < abs_cutoff) | (d2 / rad2[None, :] < rel_cutoff)
+    rows, cols = np.nonzero(ir)
+    g = np.zeros((rows.size, order + 1))
+    f = np.zeros((rows.size, 3, order + 1))
+    faces = np.unique(cols)
+    if faces.size:
+        postab, wtab, rowtab = cp.quad_points(faces)
+        for k2, face in enumerate(faces):
+            sel_pairs = np.nonzero(cols == face)[0]
+            nb = rows[sel_pairs]
+            sel = rowtab == k2
+            q, w = postab[sel], wtab[sel]
+            x = pts[nb, 0][:, None] - q[None, :, 0]
+            y = pts[nb, 1][:, None] - q[None, :, 1]
+            z = pts[nb, 2][:, None] - q[None, :, 2]
+            r = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+            r0 = np.sqrt(np.sum((pts[nb] - cp.pos[face]) ** 2, 1))
+            dr = r - r0[:, None]
+            for o in range(order + 1):
+                g[sel_pairs, o] = (dr ** o / r / math.factorial(o)) @ w
+
+            def fun(ff):
+                return np.stack([(x * ff) @ w, (y * ff) @ w, (z * ff) @ w], 1)
+            f[sel_pairs, :, 0] = -fun(1.0 / r ** 3)
+            for o in range(1, order + 1):
+                f[sel_pairs, :, o] = fun(-dr ** o / (r ** 3 * math.factorial(o))
+                                         + dr ** (o - 1) / (r ** 2 * math.factorial(o - 1)))
+    return rows, cols, g, f
+
+
+def point_fields(cp, pts, pt_medium, enei, sig1, sig2, h1, h2, rel_cutoff=3.0, abs_cutoff=0.0, order=5):
+    """E and H at points ``pts`` lying in media ``pt_medium`` (1-based) from the
+    surface charges ``sig1, sig2 [n, npol]`` and currents ``h1, h2 [n, 3, npol]``
+    (field.m:17-38): faces whose inside (outside) medium is the point's medium
+    contribute with sig1 / h1 (sig2 / h2); the Green function takes
+    k = k0 sqrt(eps(medium)), the vector-potential term E = i k0 A the vacuum k0.
+    Returns ``e, h [m, 3, npol]``."""
+    pts = np.asarray(pts, float)
+    pt_medium = np.asarray(pt_medium, int)
+    m, n = pts.shape[0], cp.n
+    k0 = 2 * np.pi / enei
+    rows, cols, gc, fc = point_refinement(cp, pts, rel_cutoff, abs_cutoff, order)
+    med = cp.face_media()                       # [n, 2] inside, outside
+    x = pts[:, None, 0] - cp.pos[None, :, 0]
+    y = pts[:, None, 1] - cp.pos[None, :, 1]
+    z = pts[:, None, 2] - cp.pos[None, :, 2]
+    d = np.maximum(np.sqrt(x ** 2 + y ** 2 + z ** 2), EPS)
+    P = sig1.shape[1]
+    e = np.zeros((m, 3, P), complex)
+    h = np.zeros((m, 3, P), complex)
+    for mm in np.unique(pt_medium):
+        ip = np.nonzero(pt_medium == mm)[0]
+        k = k0 * np.sqrt(complex(cp.eps[mm - 1](enei)[0]))
+        area = cp.area[None, :]
+        G = (1.0 / d[ip] * area).astype(complex)
+        ff = (1j * k - 1.0 / d[ip]) / d[ip] ** 2 * area
+        Gp = np.stack([ff * x[ip], ff * y[ip], ff * z[ip]], 1)     # [mi, 3, n]
+        # refined pairs of these points
+        fr = (1j * k) ** np.arange(order + 1)
+        pos_in = np.full(m, -1)
+        pos_in[ip] = np.arange(ip.size)
+        sel = pos_in[rows] >= 0
+        ri, ci = pos_in[rows[sel]], cols[sel]
+        G[ri, ci] = gc[sel] @ fr
+        Gp[ri, :, ci] = fc[sel] @ fr
+        ph = np.exp(1j * k * d[ip])
+        G, Gp = G * ph, Gp * ph[:, None, :]
+        for side, (s, hh) in enumerate(((sig1, h1), (sig2, h2))):
+            mask = (med[:, side] == mm).astype(float)         # faces of this side facing medium mm
+            Gs, Gps = G * mask[None, :], Gp * mask[None, None, :]
+            # E = i k0 A - grad(phi) with the vacuum wavenumber (field.m:17-21)
+            e[ip] += 1j * k0 * np.einsum("ij,jcp->icp", Gs, hh) - np.einsum("icj,jp->icp", Gps, s)
+            hx = np.einsum("ij,jp->ip", Gps[:, 1], hh[:, 2]) - np.einsum("ij,jp->ip", Gps[:, 2], hh[:, 1])
+            hy = np.einsum("ij,jp->ip", Gps[:, 2], hh[:, 0]) - np.einsum("ij,jp->ip", Gps[:, 0], hh[:, 2])
+            hz = np.einsum("ij,jp->ip", Gps[:, 0], hh[:, 1]) - np.einsum("ij,jp->ip", Gps[:, 1], hh[:, 0])
+            h[ip] += np.stack([hx, hy, hz], 1)
+    return e, h
