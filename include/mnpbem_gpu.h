@@ -301,6 +301,25 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key,
  * this stream after a call is ordered after all of the call's kernels.       */
 MNPBEM_API mnpbem_status mnpbem_geom_stream(const mnpbem_geom* g, void** stream);
 
+/* External potentials of one wavelength (MNPBEM's compstruct exc of any
+ * excitation, e.g. dipoleret.potential): scalar potentials phi1, phi2 and
+ * their surface derivatives phi1p, phi2p [n][npol] complex, vector potentials
+ * a1, a2 and derivatives a1p, a2p [n][3][npol] complex (index 1: inside
+ * of the faces, 2: outside); NULL = 0.                                      */
+typedef struct mnpbem_potentials {
+  int32_t npol;
+  const double *phi1, *phi1p, *phi2, *phi2p;
+  const double *a1, *a1p, *a2, *a2p;
+} mnpbem_potentials;
+
+/* sig = bem \ exc for external potentials at one wavelength: the excitation
+ * variables of BEM/@bemret/private/excitation.m, then the solve of
+ * mnpbem_solve (same precision and refinement).  out->sig1, sig2, h1, h2,
+ * ir_iters, ir_resid are filled (ext, sca are not: no plane wave).          */
+MNPBEM_API mnpbem_status mnpbem_solve_potentials(mnpbem_geom* g, const mnpbem_potentials* pot, double enei,
+                                                 const double* eps_media, int32_t nmed, int32_t precision,
+                                                 const mnpbem_refine* refine, mnpbem_solution* out);
+
 /* Electric and magnetic fields at points off the particle boundary
  * (Greenfun/@compgreenret/field.m:17-38 on the Green function between a
  * compoint and the particle; Simulation/misc/@meshfield): for a point in

@@ -8,7 +8,7 @@ MATLAB calling surface on top of that library.
 """
 from .materials import EV2NM, epsconst, epsdrude, epsfun  # noqa: F401
 from .particles import comparticle, lglnodes, particle, quadface, trisphere  # noqa: F401
-from .bem import (bemoptions, bemret, bemsolver, compstruct, meshfield, planewave,  # noqa: F401
+from .bem import (bemoptions, bemret, bemsolver, compstruct, dipoleret, meshfield, planewave,  # noqa: F401
                   planewaveret, point_media, spectrum_batch, spectrumret)
 
 __version__ = "0.1.0"

@@ -51,6 +51,11 @@ class Solution(ctypes.Structure):
                 ("outputs_on_device", ctypes.c_int32)]
 
 
+class Potentials(ctypes.Structure):
+    _fields_ = [("npol", ctypes.c_int32)] + [(k, ctypes.c_void_p) for k in
+                                             ("phi1", "phi1p", "phi2", "phi2p", "a1", "a1p", "a2", "a2p")]
+
+
 class Refine(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int32), ("tol", ctypes.c_double)]
 
@@ -72,6 +77,9 @@ SIGNATURES = {
                                                  ctypes.POINTER(Quad), ctypes.POINTER(Options),
                                                  ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_geom_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "mnpbem_solve_potentials": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Potentials), ctypes.c_double,
+                                               c_double_p, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.POINTER(Refine), ctypes.POINTER(Solution)]),
     "mnpbem_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_double_p, c_int32_p, ctypes.c_double,
                                      c_double_p, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 6),
     "mnpbem_geom_size": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p]),

@@ -310,7 +310,14 @@ class bemret:
         return float(val[0]), gv, complex(ge[0], ge[1])
 
     def mldivide(self, exc):
-        """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m)."""
+        """sig = bem \\ exc(p, enei): surface charges and currents (mldivide.m).
+
+        ``exc`` from a plane wave (``planewave(...)(p, enei)``) or with
+        external potentials ``phi1, phi1p, phi2, phi2p [n, P]``, ``a1, a1p, a2,
+        a2p [n, 3, P]`` (e.g. ``dipoleret.potential``), solved in groups of at
+        most four columns by ``mnpbem_solve_potentials``."""
+        if not hasattr(exc, "exc"):
+            return self._solve_potentials(exc)
         pw = exc.exc
         r = self.spectrum(pw, exc.enei, fields=True)
         return compstruct(self.p, exc.enei, sig1=r["sig1"][0], sig2=r["sig2"][0], h1=r["h1"][0],
@@ -318,6 +325,172 @@ class bemret:
                           ir_iters=int(r["ir_iters"][0]), ir_resid=float(r["ir_resid"][0]))
 
     solve = mldivide
+
+    def _solve_potentials(self, exc):
+        enei = float(exc.enei)
+        n = self.p.n
+        keys1, keys3 = ("phi1", "phi1p", "phi2", "phi2p"), ("a1", "a1p", "a2", "a2p")
+        P = next(np.asarray(getattr(exc, k)).shape[-1] for k in keys1 + keys3 if hasattr(exc, k))
+        em = np.ascontiguousarray(self.p.eps_media(enei)[0])
+        out = {k: np.zeros((n, P), np.complex128) for k in ("sig1", "sig2")}
+        out.update({k: np.zeros((n, 3, P), np.complex128) for k in ("h1", "h2")})
+        iters = []
+        for c0 in range(0, P, 4):
+            cols = slice(c0, min(P, c0 + 4))
+            w = cols.stop - cols.start
+            keep = []
+            pot = _lib.Potentials()
+            pot.npol = w
+            for k in keys1 + keys3:
+                if hasattr(exc, k):
+                    arr = np.ascontiguousarray(np.asarray(getattr(exc, k))[..., cols], dtype=np.complex128)
+                    keep.append(arr)
+                    setattr(pot, k, arr.ctypes.data)
+            part = {k: np.zeros((n, w) if k.startswith("sig") else (n, 3, w), np.complex128)
+                    for k in ("sig1", "sig2", "h1", "h2")}
+            it, res = np.zeros(1, np.int32), np.zeros(1)
+            sol = _lib.Solution()
+            sol.sig1, sol.sig2 = part["sig1"].ctypes.data, part["sig2"].ctypes.data
+            sol.h1, sol.h2 = part["h1"].ctypes.data, part["h2"].ctypes.data
+            sol.ir_iters, sol.ir_resid = it.ctypes.data, res.ctypes.data
+            ref = _lib.Refine(self.refine_iters, self.refine_tol)
+            _lib.check(self._lib.mnpbem_solve_potentials(
+                self._h, ctypes.byref(pot), enei, em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size,
+                self.precision, ctypes.byref(ref), ctypes.byref(sol)))
+            for k in part:
+                out[k][..., cols] = part[k]
+            iters.append(int(it[0]))
+        return compstruct(self.p, enei, ir_iters=max(iters), **out)
+
+
+class dipoleret:
+    """Oscillating dipoles for the retarded solver (Simulation/retarded/@dipoleret).
+
+    ``dipoleret(p, pos, dip=None)``: dipoles at ``pos [npt, 3]`` near the
+    comparticle ``p`` with moments ``dip`` ([3] or [ndip, 3] for every
+    position, default the unit vectors; ``[npt, 3, ndip]`` with ``full=True``).
+    The media of the positions follow compoint (``medium`` overrides them).
+    ``exc = dip(p, enei)`` holds the potentials of potential.m:14-117 (columns
+    = (position, orientation), position-major); ``sig = bem \\ exc``;
+    ``tot, rad, rad0 = dip.decayrate(bem, sig)`` (decayrate.m:13-62): the
+    induced field at the dipoles comes from ``mnpbem_fields``, the radiated
+    power from the far fields of the charges (spectrumret/farfield.m) and of
+    the dipoles (farfield.m:11-55) on the unit sphere at infinity.
+    """
+
+    def __init__(self, p, pos, dip=None, full=False, medium=None, pinfty=None, spec_medium=1):
+        self.p = p
+        self.pos = np.ascontiguousarray(np.asarray(pos, dtype=np.float64).reshape(-1, 3))
+        npt = self.pos.shape[0]
+        if full:
+            d = np.asarray(dip, dtype=np.float64)
+            self.dip = d.reshape(npt, 3, -1)
+        else:
+            d = np.eye(3) if dip is None else np.atleast_2d(np.asarray(dip, dtype=np.float64))
+            self.dip = np.repeat(d.T[None, :, :], npt, axis=0)       # [npt, 3, ndip]
+        self.medium = (point_media(p, self.pos) if medium is None
+                       else np.ascontiguousarray(np.broadcast_to(medium, npt), dtype=np.int32))
+        self.spec = spectrumret(pinfty, spec_medium)
+
+    @property
+    def ncol(self):
+        return self.dip.shape[0] * self.dip.shape[2]
+
+    def __call__(self, p, enei):
+        return self.potential(p, enei)
+
+    def potential(self, p, enei):
+        """Potentials at the faces (potential.m:14-117)."""
+        enei = float(enei)
+        npt, ndip = self.dip.shape[0], self.dip.shape[2]
+        n, P = p.n, self.ncol
+        f = {k: np.zeros((n, P), np.complex128) for k in ("phi1", "phi1p", "phi2", "phi2p")}
+        f.update({k: np.zeros((n, 3, P), np.complex128) for k in ("a1", "a1p", "a2", "a2p")})
+        fmed = np.repeat(p.inout, [q.n for q in p.p], axis=0)
+        eps = p.eps_media(enei)[0]
+        k0 = 2 * np.pi / enei
+        for ipt in range(npt):
+            mm = int(self.medium[ipt])
+            e = eps[mm - 1]
+            k = k0 * np.sqrt(e)
+            for side, sfx in ((0, "1"), (1, "2")):
+                ind = np.nonzero(fmed[:, side] == mm)[0]
+                if ind.size == 0:
+                    continue
+                v = p.pos[ind] - self.pos[ipt][None, :]
+                r = np.sqrt(np.sum(v * v, 1))
+                u = v / r[:, None]
+                G = np.exp(1j * k * r) / r
+                F = (1j * k - 1 / r) * G
+                nv = p.nvec[ind]
+                en = np.sum(nv * u, 1)
+                for idip in range(ndip):
+                    d = self.dip[ipt, :, idip]
+                    col = ipt * ndip + idip
+                    ep, npd = u @ d, nv @ d
+                    f["phi" + sfx][ind, col] = -ep * F / e
+                    f["phi" + sfx + "p"][ind, col] = ((npd - 3 * en * ep) / r ** 2 * (1 - 1j * k * r) * G / e
+                                                       + k ** 2 * ep * en * G / e)
+                    f["a" + sfx][ind, :, col] = -1j * k0 * d[None, :] * G[:, None]
+                    f["a" + sfx + "p"][ind, :, col] = -1j * k0 * d[None, :] * (en * F)[:, None]
+        return compstruct(p, enei, **f)
+
+    def _farfields(self, p, sig):
+        """Far fields of the induced charges and of the dipoles on the unit
+        sphere at infinity."""
+        enei = float(sig.enei)
+        dirs, med = self.spec.nvec, self.spec.medium
+        eps = p.eps_media(enei)[0][med - 1]
+        k0 = 2 * np.pi / enei
+        k = k0 * np.sqrt(eps)
+        fmed = np.repeat(p.inout, [q.n for q in p.p], axis=0)
+        phase = np.exp(-1j * k * dirs @ p.pos.T) * p.area[None, :]
+        P = sig.sig1.shape[1]
+        e = np.zeros((dirs.shape[0], 3, P), np.complex128)
+        h = np.zeros_like(e)
+        for side, (ks, kh) in enumerate((("sig1", "h1"), ("sig2", "h2"))):
+            ind = np.nonzero(fmed[:, side] == med)[0]
+            if ind.size == 0:
+                continue
+            ph = phase[:, ind]
+            Ph = np.einsum("dn,nkp->dkp", ph, getattr(sig, kh)[ind])
+            Ps = ph @ getattr(sig, ks)[ind]
+            e += 1j * k0 * Ph - 1j * k * dirs[:, :, None] * Ps[:, None, :]
+            h += 1j * k * np.cross(np.broadcast_to(dirs[:, :, None], Ph.shape), Ph, axis=1)
+        npt, ndip = self.dip.shape[0], self.dip.shape[2]
+        for ipt in range(npt):
+            if self.medium[ipt] != med:
+                continue
+            g = np.exp(-1j * k * dirs @ self.pos[ipt])
+            for idip in range(ndip):
+                hh = np.cross(dirs, self.dip[ipt, :, idip][None, :]) * g[:, None]
+                col = ipt * ndip + idip
+                e[:, :, col] += k ** 2 * np.cross(hh, dirs) / eps
+                h[:, :, col] += k ** 2 * hh / np.sqrt(eps)
+        return e, h
+
+    def decayrate(self, bem, sig):
+        """``tot, rad, rad0 [npt, ndip]``: total and radiative decay rates in
+        units of the free-space rate, and the free-space rate nb * 4/3 k0^3."""
+        p = self.p
+        enei = float(sig.enei)
+        k0 = 2 * np.pi / enei
+        gamma = 4.0 / 3.0 * k0 ** 3
+        e, _ = meshfield(bem, self.pos, medium=self.medium)(sig)              # [npt, 3, P]
+        ef, hf = self._farfields(p, sig)
+        flux = 0.5 * np.real(np.einsum("dc,dcp->dp", self.spec.nvec, np.cross(ef, np.conj(hf), axis=1)))
+        sca = self.spec.area @ flux
+        npt, ndip = self.dip.shape[0], self.dip.shape[2]
+        eps = p.eps_media(enei)[0]
+        tot, rad, rad0 = np.zeros((npt, ndip)), np.zeros((npt, ndip)), np.zeros((npt, ndip))
+        for ipt in range(npt):
+            nb = np.sqrt(eps[int(self.medium[ipt]) - 1]).real
+            for idip in range(ndip):
+                col = ipt * ndip + idip
+                tot[ipt, idip] = 1 + np.imag(e[ipt, :, col] @ np.conj(self.dip[ipt, :, idip])) / (0.5 * nb * gamma)
+                rad[ipt, idip] = sca[col] / (2 * np.pi * k0) / (0.5 * nb * gamma)
+                rad0[ipt, idip] = nb * gamma
+        return tot, rad, rad0
 
 
 def point_media(p, pts):

@@ -683,6 +683,8 @@ struct SolveCtx {
   int P;
   int precision;
   const mnpbem_planewave* exc;
+  const double2* ext_pot = nullptr;   // external potentials instead of the plane wave (device)
+  bool spectra = true;                // far fields and cross sections of the plane wave
 };
 
 size_t lane_bytes_estimate(const mnpbem_geom* G, int precision, int P, int ninf) {
@@ -930,7 +932,10 @@ mnpbem_status stage_first(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   const double* dirs = pol + 3 * P;
   const LamParams* lp = L.lp_dev.as<LamParams>();
   const FaceData fd = face_data(G, L);
-  launch_excitation(fd, P, pol, dirs, lp, v.phi, v.a, v.alpha, v.De, L.st);
+  if (c.ext_pot)
+    launch_excitation_ext(fd, P, c.ext_pot, lp, v.phi, v.a, v.alpha, v.De, L.st);
+  else
+    launch_excitation(fd, P, pol, dirs, lp, v.phi, v.a, v.alpha, v.De, L.st);
   MNP_CHECK_LAUNCH();
   if (c.precision == MNPBEM_FP64)
     return apply_mldivide<double>(fd, P, lp, chain_mats<double>(G, L), v.phi, v.a, v.alpha, v.De, v.x1, v.x2,
@@ -1179,7 +1184,7 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
       if (step_converged(L, hn, ref.tol)) break;
     }
   }
-  MNP_TRY(launch_stage(G, L, c, 4, graphs));
+  if (c.spectra) MNP_TRY(launch_stage(G, L, c, 4, graphs));
   MNP_CUDA(cudaStreamSynchronize(st));
   G->prof.flush();
   MNP_TRY(check_pivots(L));
@@ -1431,6 +1436,17 @@ mnpbem_status job_prepare(Job& j) {
   ProfBind pb_(&G->prof);
   const SolveCtx& c = j.c;
   const Sweep& s = j.s;
+  if (c.ext_pot) {
+    // external potentials: direct solves on lane 0 (no captured graphs)
+    Lane& L = *G->lanes[0];
+    for (; j.next < s.nenei; ++j.next) {
+      MNP_TRY(upload_lp(G, L, s, j.next));
+      L.w = j.next;
+      MNP_TRY(solve_one(G, L, c, s.ref, false, &L.iters, &L.res));
+      MNP_TRY(write_outputs(G, L, c, s, j.next));
+    }
+    return MNPBEM_OK;
+  }
   std::vector<int> fresh;
   for (int l = 0; l < j.nl && j.next < s.nenei; ++l) {
     Lane& L = *G->lanes[l];
@@ -1929,4 +1945,44 @@ mnpbem_status mnpbem_fields(mnpbem_geom* G, int64_t npts, const double* pts, con
   MNP_CUDA(cudaStreamSynchronize(st));
   G->prof.flush();
   return MNPBEM_OK;
+}
+
+mnpbem_status mnpbem_solve_potentials(mnpbem_geom* G, const mnpbem_potentials* pot, double enei,
+                                      const double* eps_media, int32_t nmed, int32_t precision,
+                                      const mnpbem_refine* refine, mnpbem_solution* out) {
+  MNP_TRY(check_geom(G));
+  if (!pot || pot->npol < 1 || pot->npol > 4 || !out || !(enei > 0)) {
+    set_error("mnpbem_solve_potentials: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  const int P = pot->npol;
+  const double* src[8] = {pot->phi1, pot->phi1p, pot->phi2, pot->phi2p, pot->a1, pot->a1p, pot->a2, pot->a2p};
+  // a plane wave without directions stands in for the job's excitation; the
+  // potentials replace its excitation and no spectra are computed
+  std::vector<double> zero(3 * P, 0.0);
+  mnpbem_planewave pw{P, zero.data(), zero.data(), 1, 0, nullptr, nullptr};
+  mnpbem_solution o = *out;
+  o.ext = o.sca = nullptr;
+  MNP_TRY(validate_job(G, &pw, 1, &enei, eps_media, nmed, precision, &o));
+  MNP_CUDA(cudaSetDevice(G->device));
+  const int64_t n = G->g.n;
+  DevBuf dpot;
+  MNP_TRY(dpot.ensure(sizeof(double2) * 16 * n * P));
+  double2* D = dpot.as<double2>();
+  for (int q = 0; q < 8; ++q) {
+    const int64_t cnt = (q < 4 ? 1 : 3) * n * P;
+    double2* dst = D + (q < 4 ? q * n * P : 4 * n * P + (q - 4) * 3 * n * P);
+    if (src[q])
+      MNP_CUDA(cudaMemcpyAsync(dst, src[q], sizeof(double2) * cnt, cudaMemcpyHostToDevice, G->st));
+    else
+      MNP_CUDA(cudaMemsetAsync(dst, 0, sizeof(double2) * cnt, G->st));
+  }
+  MNP_CUDA(cudaStreamSynchronize(G->st));
+  std::vector<Job> jobs(1);
+  jobs[0].G = G;
+  MNP_TRY(job_setup(jobs[0], &pw, 1, &enei, eps_media, nmed, precision, refine, &o));
+  jobs[0].c.ext_pot = D;
+  jobs[0].c.spectra = false;
+  jobs[0].nl = 1;
+  return run_jobs(jobs);
 }

@@ -59,6 +59,49 @@ void launch_excitation(const FaceData& f, int P, const double* pol, const double
   k_excitation<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, pol, dir, lp, phi, a, alpha, De);
 }
 
+// External potentials (compstruct exc of any excitation, e.g. dipoleret)
+// -> excitation variables (BEM/@bemret/private/excitation.m, Garcia de Abajo
+// and Howie Eqs. 10, 11, 15, 18):
+//   phi = phi2 - phi1,  a = a2 - a1,
+//   alpha = a2p - a1p - i k0 (n eps2 phi2 - n eps1 phi1),
+//   De = eps2 phi2p - eps1 phi1p - i k0 (n . eps2 a2 - n . eps1 a1).
+// pot: phi1, phi1p, phi2, phi2p [n][P] then a1, a1p, a2, a2p [n][3][P].
+__global__ void k_excitation_ext(FaceData f, int P, const double2* __restrict__ pot,
+                                 const LamParams* __restrict__ lp, double2* phi, double2* a, double2* alpha,
+                                 double2* De) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.n) return;
+  const int64_t n = f.n;
+  const double k0 = lp->k0;
+  const double2 e1 = f.eps1[i], e2 = f.eps2[i];
+  const double nv[3] = {f.nvec[3 * i], f.nvec[3 * i + 1], f.nvec[3 * i + 2]};
+  const double2 *p1 = pot, *p1p = pot + n * P, *p2 = pot + 2 * n * P, *p2p = pot + 3 * n * P;
+  const double2 *a1 = pot + 4 * n * P, *a1p = a1 + 3 * n * P, *a2 = a1 + 6 * n * P, *a2p = a1 + 9 * n * P;
+  for (int p = 0; p < P; ++p) {
+    const int64_t s = i * P + p;
+    phi[s] = csub(p2[s], p1[s]);
+    const double2 ep2 = cmul(e2, p2[s]), ep1 = cmul(e1, p1[s]);
+    double2 na1 = make_double2(0, 0), na2 = make_double2(0, 0);
+    for (int c = 0; c < 3; ++c) {
+      const int64_t v = (i * 3 + c) * P + p;
+      a[v] = csub(a2[v], a1[v]);
+      // - i k0 n_c (eps2 phi2 - eps1 phi1)
+      const double2 t = cscale(csub(ep2, ep1), nv[c]);
+      alpha[v] = cadd(csub(a2p[v], a1p[v]), make_double2(k0 * t.y, -k0 * t.x));
+      na1 = cadd(na1, cscale(a1[v], nv[c]));
+      na2 = cadd(na2, cscale(a2[v], nv[c]));
+    }
+    const double2 t = csub(cmul(e2, na2), cmul(e1, na1));
+    De[s] = cadd(csub(cmul(e2, p2p[s]), cmul(e1, p1p[s])), make_double2(k0 * t.y, -k0 * t.x));
+  }
+}
+
+void launch_excitation_ext(const FaceData& f, int P, const double2* pot, const LamParams* lp, double2* phi,
+                           double2* a, double2* alpha, double2* De, cudaStream_t st) {
+  ProfScope ps_(PH_ELEMWISE, st, 0.0, 0.0, 1);
+  k_excitation_ext<<<(unsigned)cdiv_up(f.n, 128), 128, 0, st>>>(f, P, pot, lp, phi, a, alpha, De);
+}
+
 __global__ void k_face_eps(int64_t n, const int* __restrict__ med_in, const int* __restrict__ med_out,
                            const LamParams* __restrict__ lp, const double* __restrict__ nvec, double2* eps1,
                            double2* eps2, float2* eps1f, float2* eps2f, float2* Lf, float* nvecf) {

@@ -33,6 +33,10 @@ struct Fields {
 void launch_excitation(const FaceData& f, int P, const double* pol, const double* dir,
                        const LamParams* lp, double2* phi, double2* a, double2* alpha,
                        double2* De, cudaStream_t st);
+// external potentials [4][n][P] + [4][n][3][P] (phi1, phi1p, phi2, phi2p, a1,
+// a1p, a2, a2p) -> phi, a, alpha, De (BEM/@bemret/private/excitation.m)
+void launch_excitation_ext(const FaceData& f, int P, const double2* pot, const LamParams* lp, double2* phi,
+                           double2* a, double2* alpha, double2* De, cudaStream_t st);
 
 // per-face dielectric functions eps1 (inside) / eps2 (outside) of this wavelength,
 // plus their complex64 copies, L = eps1 - eps2 and the normals in FP32

@@ -760,16 +760,24 @@ class BemRet:
         self.G1, self.H1, self.G2, self.H2 = G1, H1, G2, H2
 
     def excitation(self, exc):
-        """excitation.m:4-29 for potentials a1, a1p, a2, a2p (no scalar phi)."""
+        """excitation.m:4-29 (Garcia de Abajo and Howie Eqs. 10, 11, 15, 18);
+        missing potentials are zero."""
         k = 2 * np.pi / exc["enei"]
         eps1 = self.p.eps_faces(exc["enei"], 0)
         eps2 = self.p.eps_faces(exc["enei"], 1)
         nvec = self.nvec
-        a1, a1p, a2, a2p = exc["a1"], exc["a1p"], exc["a2"], exc["a2p"]
-        phi = np.zeros((nvec.shape[0], a1.shape[2]), dtype=complex)
+        n = nvec.shape[0]
+        P = next(v.shape[-1] for key, v in exc.items() if key != "enei")
+        z1, z3 = np.zeros((n, P), complex), np.zeros((n, 3, P), complex)
+        get = lambda key, z: exc.get(key, z)
+        phi1, phi1p, phi2, phi2p = get("phi1", z1), get("phi1p", z1), get("phi2", z1), get("phi2p", z1)
+        a1, a1p, a2, a2p = get("a1", z3), get("a1p", z3), get("a2", z3), get("a2p", z3)
+        phi = phi2 - phi1
         a = a2 - a1
-        alpha = a2p - a1p
-        De = -1j * k * (eps2[:, None] * _inner(nvec, a2) - eps1[:, None] * _inner(nvec, a1))
+        alpha = a2p - a1p - 1j * k * (nvec[:, :, None] * (eps2[:, None] * phi2)[:, None, :]
+                                      - nvec[:, :, None] * (eps1[:, None] * phi1)[:, None, :])
+        De = (eps2[:, None] * phi2p - eps1[:, None] * phi1p
+              - 1j * k * (eps2[:, None] * _inner(nvec, a2) - eps1[:, None] * _inner(nvec, a1)))
         return phi, a, alpha, De
 
     def solve(self, exc):
@@ -1028,3 +1036,106 @@ def point_fields(cp, pts, pt_medium, enei, sig1, sig2, h1, h2, rel_cutoff=3.0, a
             hz = np.einsum("ij,jp->ip", Gps[:, 0], hh[:, 1]) - np.einsum("ij,jp->ip", Gps[:, 1], hh[:, 0])
             h[ip] += np.stack([hx, hy, hz], 1)
     return e, h
+
+
+
+# --------------------------------------------------------------------------
+# dipole excitation (Simulation/retarded/@dipoleret: potential.m:14-117,
+# farfield.m:11-55, scattering.m, decayrate.m:13-62)
+# --------------------------------------------------------------------------
+class DipoleRet:
+    """Oscillating dipoles at ``pos [npt, 3]`` in media ``medium [npt]``
+    (1-based) with moments ``dip [npt, 3, ndip]``; ``pinfty`` the unit sphere
+    at infinity of the radiative rate.  Columns of the potentials are the
+    (position, orientation) pairs, position-major."""
+
+    def __init__(self, pos, dip, medium, pinfty, spec_medium=1):
+        self.pos = np.asarray(pos, float).reshape(-1, 3)
+        self.dip = np.asarray(dip, float)
+        self.medium = np.asarray(medium, int)
+        self.pinfty = pinfty
+        self.spec_medium = spec_medium
+
+    def potential(self, cp, enei):
+        npt, ndip = self.pos.shape[0], self.dip.shape[2]
+        P = npt * ndip
+        n = cp.n
+        out = {"enei": enei}
+        for key in ("phi1", "phi1p", "phi2", "phi2p"):
+            out[key] = np.zeros((n, P), complex)
+        for key in ("a1", "a1p", "a2", "a2p"):
+            out[key] = np.zeros((n, 3, P), complex)
+        media = cp.face_media()
+        k0 = 2 * np.pi / enei
+        for ipt in range(npt):
+            mm = self.medium[ipt]
+            eps = complex(cp.eps[mm - 1](enei)[0])
+            k = k0 * np.sqrt(eps)
+            for side, sfx in ((0, "1"), (1, "2")):
+                ind = np.nonzero(media[:, side] == mm)[0]
+                if ind.size == 0:
+                    continue
+                v = cp.pos[ind] - self.pos[ipt][None, :]
+                r = np.sqrt(np.sum(v * v, 1))
+                u = v / r[:, None]
+                G = np.exp(1j * k * r) / r
+                F = (1j * k - 1 / r) * G
+                nv = cp.nvec[ind]
+                en = np.sum(nv * u, 1)
+                for idip in range(ndip):
+                    d = self.dip[ipt, :, idip]
+                    col = ipt * ndip + idip
+                    ep, npd = u @ d, nv @ d
+                    out["phi" + sfx][ind, col] = -ep * F / eps
+                    out["phi" + sfx + "p"][ind, col] = ((npd - 3 * en * ep) / r ** 2 * (1 - 1j * k * r) * G / eps
+                                                         + k ** 2 * ep * en * G / eps)
+                    out["a" + sfx][ind, :, col] = -1j * k0 * d[None, :] * G[:, None]
+                    out["a" + sfx + "p"][ind, :, col] = -1j * k0 * d[None, :] * (en * F)[:, None]
+        return out
+
+    def farfield(self, cp, enei):
+        """Far fields of the dipoles themselves (farfield.m:11-55)."""
+        dirs = self.pinfty.nvec
+        eps = complex(cp.eps[self.spec_medium - 1](enei)[0])
+        k = 2 * np.pi / enei * np.sqrt(eps)
+        npt, ndip = self.pos.shape[0], self.dip.shape[2]
+        e = np.zeros((dirs.shape[0], 3, npt * ndip), complex)
+        h = np.zeros_like(e)
+        for ipt in range(npt):
+            if self.medium[ipt] != self.spec_medium:
+                continue
+            g = np.exp(-1j * k * dirs @ self.pos[ipt])
+            for idip in range(ndip):
+                hh = np.cross(dirs, self.dip[ipt, :, idip][None, :]) * g[:, None]
+                ee = np.cross(hh, dirs)
+                e[:, :, ipt * ndip + idip] = k ** 2 * ee / eps
+                h[:, :, ipt * ndip + idip] = k ** 2 * hh / np.sqrt(eps)
+        return e, h
+
+    def decayrate(self, cp, sig):
+        """Total and radiative decay rates in units of the free-space rate
+        (decayrate.m:13-62): tot = 1 + Im(e_ind . dip*) / (nb gamma / 2) with
+        gamma = 4/3 k0^3 and e_ind the induced field at the dipole; rad = the
+        power scattered by dipole + induced far fields / (2 pi k0), in the same
+        units."""
+        enei = sig["enei"]
+        k0 = 2 * np.pi / enei
+        gamma = 4.0 / 3.0 * k0 ** 3
+        npt, ndip = self.pos.shape[0], self.dip.shape[2]
+        e, _ = point_fields(cp, self.pos, self.medium, enei, sig["sig1"], sig["sig2"], sig["h1"], sig["h2"])
+        # far fields: induced charges (spectrumret/farfield.m, as PlaneWaveRet.farfield) + dipoles
+        pw = PlaneWaveRet([1, 0, 0], [0, 0, 1], self.pinfty, self.spec_medium)
+        ef, hf, _ = pw.farfield(cp, sig, self.pinfty.nvec)
+        ed, hd = self.farfield(cp, enei)
+        et, ht = ef + ed, hf + hd
+        flux = 0.5 * np.real(np.einsum("dc,dcp->dp", self.pinfty.nvec, np.cross(et, np.conj(ht), axis=1)))
+        sca = self.pinfty.area @ flux
+        tot = np.zeros((npt, ndip))
+        rad = np.zeros((npt, ndip))
+        for ipt in range(npt):
+            nb = np.sqrt(complex(cp.eps[self.medium[ipt] - 1](enei)[0])).real
+            for idip in range(ndip):
+                col = ipt * ndip + idip
+                tot[ipt, idip] = 1 + np.imag(e[ipt, :, col] @ np.conj(self.dip[ipt, :, idip])) / (0.5 * nb * gamma)
+                rad[ipt, idip] = sca[col] / (2 * np.pi * k0) / (0.5 * nb * gamma)
+        return tot, rad
