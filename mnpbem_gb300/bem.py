@@ -546,10 +546,18 @@ class meshfield:
         m = self.pts.shape[0]
         e = np.zeros((m, 3, P), np.complex128)
         h = np.zeros((m, 3, P), np.complex128)
-        _lib.check(b._lib.mnpbem_fields(
-            b._h, m, _lib.dptr(self.pts), self.medium.ctypes.data_as(_lib.c_int32_p), enei,
-            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, P,
-            s1.ctypes.data, s2.ctypes.data, q1.ctypes.data, q2.ctypes.data, e.ctypes.data, h.ctypes.data))
+        for c0 in range(0, P, 4):        # mnpbem_fields takes up to four columns per call
+            cols = slice(c0, min(P, c0 + 4))
+            w = cols.stop - cols.start
+            part = [np.ascontiguousarray(a[..., cols]) for a in (s1, s2, q1, q2)]
+            ec = np.zeros((m, 3, w), np.complex128)
+            hc = np.zeros((m, 3, w), np.complex128)
+            _lib.check(b._lib.mnpbem_fields(
+                b._h, m, _lib.dptr(self.pts), self.medium.ctypes.data_as(_lib.c_int32_p), enei,
+                em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, w,
+                part[0].ctypes.data, part[1].ctypes.data, part[2].ctypes.data, part[3].ctypes.data,
+                ec.ctypes.data, hc.ctypes.data))
+            e[..., cols], h[..., cols] = ec, hc
         return e.reshape(self.shape + (3, P)), h.reshape(self.shape + (3, P))
 
 

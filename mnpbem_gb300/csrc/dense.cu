@@ -606,16 +606,29 @@ mnpbem_status thin_stream_check(cudaStream_t st) {
   return MNPBEM_OK;
 }
 
-mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
-                           int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
-                           float2* bsplit, cudaStream_t st) {
-  if (M <= 0 || N <= 0) return MNPBEM_OK;
-  if (N > 8 || K <= 0 || ldb != N) { set_error("gemm_thin_ds: N must be 1..8 and B packed"); return MNPBEM_ERR_INVALID_ARG; }
+// B[:, 0:N] (row stride ldb) -> packed hi / lo planes [K][N]
+__global__ void k_split_hi_lo_cols(const double2* __restrict__ B, int64_t ldb, int64_t K, int N, float2* hi,
+                                   float2* lo) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K * N) return;
+  const int64_t k = i / N;
+  const double2 b = B[k * ldb + (i - k * N)];
+  const float2 h = make_float2((float)b.x, (float)b.y);
+  hi[i] = h;
+  lo[i] = make_float2((float)(b.x - (double)h.x), (float)(b.y - (double)h.y));
+}
+
+static mnpbem_status gemm_thin_ds_block(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
+                                        int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
+                                        float2* bsplit, cudaStream_t st) {
   float2* Bh = bsplit;
   float2* Bl = bsplit + K * N;
   {
     ProfScope ps(PH_ELEMWISE, st, 0.0, 0.0, 1);
-    k_split_hi_lo<<<(unsigned)cdiv_up(K * N, 256), 256, 0, st>>>(B, K * N, Bh, Bl);
+    if (ldb == N)
+      k_split_hi_lo<<<(unsigned)cdiv_up(K * N, 256), 256, 0, st>>>(B, K * N, Bh, Bl);
+    else
+      k_split_hi_lo_cols<<<(unsigned)cdiv_up(K * N, 256), 256, 0, st>>>(B, ldb, K, (int)N, Bh, Bl);
     MNP_CHECK_LAUNCH();
   }
   const unsigned nblk = (unsigned)cdiv_up(M, (int64_t)DS_TR);
@@ -648,6 +661,19 @@ mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, c
   }
 #undef DS_CASE
   MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+// columns in blocks of at most 8 (the kernels' register-tiled widths)
+mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
+                           int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
+                           float2* bsplit, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return MNPBEM_OK;
+  if (K <= 0 || ldb < N) { set_error("gemm_thin_ds: invalid sizes"); return MNPBEM_ERR_INVALID_ARG; }
+  for (int64_t c0 = 0; c0 < N; c0 += 8) {
+    const int64_t w = std::min<int64_t>(8, N - c0);
+    MNP_TRY(gemm_thin_ds_block(M, w, K, Ahi, Alo, lda, B + c0, ldb, C + c0, ldc, bsplit, st));
+  }
   return MNPBEM_OK;
 }
 

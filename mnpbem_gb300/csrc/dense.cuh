@@ -11,11 +11,11 @@ mnpbem_status gemm_simt(int64_t M, int64_t N, int64_t K, cplx<R> alpha, const cp
                         int64_t lda, const cplx<R>* B, int64_t ldb, cplx<R> beta, cplx<R>* C,
                         int64_t ldc, cudaStream_t st);
 
-// C[M x N] = (A_hi + A_lo)[M x K] * B[K x N] for N <= 8 with the product
+// C[M x N] = (A_hi + A_lo)[M x K] * B[K x N] (columns in blocks of 8) with the product
 // evaluated in double-single FP32 arithmetic (error-free products and
 // TwoSum accumulation, ~48-bit accuracy): A_hi = fl32(A), A_lo = fl32(A - A_hi)
-// are complex64 planes, B (packed, ldb = N) and C are complex128.
-// bsplit: workspace of 2 K N complex64 (hi / lo planes of B).
+// are complex64 planes, B (row stride ldb) and C are complex128.
+// bsplit: workspace of 2 K min(N, 8) complex64 (hi / lo planes of a block of B).
 // Alo == NULL: FP32 product of the hi planes (FMA accumulation, ~24 bits).
 mnpbem_status gemm_thin_ds(int64_t M, int64_t N, int64_t K, const float2* Ahi, const float2* Alo,
                            int64_t lda, const double2* B, int64_t ldb, double2* C, int64_t ldc,
