@@ -199,7 +199,8 @@ def lib_stream(bem, torch):
 
 def read_profile(bem):
     from mnpbem_gb300 import _lib
-    names = ["assembly", "gemm_n3", "gemm_thin", "block_inverse", "elementwise", "spectra", "geometry"]
+    names = ["assembly", "gemm_n3", "gemm_thin", "block_inverse", "elementwise", "spectra", "geometry",
+             "hmat_build", "hmat_matvec"]
     out = {}
     for ph, nm in enumerate(names):
         ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -227,7 +227,8 @@ MNPBEM_API mnpbem_status mnpbem_bem_matrices(mnpbem_geom* g, double enei, const 
 /* Per-phase accounting of the library's kernels on a handle (the tracing that
  * the reference does with named timer maps, mex/hlib/hoptions.h:65-72, and
  * BEM/@bemiter/tocout.m).  Phases: 0 assembly, 1 O(n^3) GEMMs, 2 thin/panel GEMMs,
- * 3 pivot-block inversions, 4 element-wise kernels, 5 spectra, 6 geometry set-up.
+ * 3 pivot-block inversions, 4 element-wise kernels, 5 spectra, 6 geometry set-up,
+ * 7 H-matrix construction (full blocks + ACA), 8 H-matrix products.
  * Launch counts are always kept; with profiling enabled each launch is also
  * bracketed by CUDA events on the handle's stream (durations in ms) and the
  * algorithmic FLOPs / bytes of the launches are accumulated.                */
@@ -335,6 +336,76 @@ MNPBEM_API mnpbem_status mnpbem_fields(mnpbem_geom* g, int64_t npts, const doubl
                                        const int32_t* pt_medium, double enei, const double* eps_media,
                                        int32_t nmed, int32_t npol, const double* sig1, const double* sig2,
                                        const double* h1, const double* h2, double* e, double* h);
+
+/* Cluster tree and block partition of an H-matrix (the arguments
+ * Greenfun/hmatrices/@hmatrix/treemex.m hands to the H-matrix MEX functions,
+ * mex/hmatgreenret.cpp:21-61, 0-based): clusters in the order of
+ * @clustertree/private/bisection.m, positions in cluster order.
+ *   son [ncluster][2]   sons, -1 for leaves
+ *   cind [ncluster][2]  first and last cluster-order position (inclusive)
+ *   ipart [ncluster]    particle of the cluster (0-based), -1 if several
+ *   perm [n]            face at each cluster-order position (tree.ind(:,1) - 1)
+ *   full [nfull][2]     (row, column) clusters of the full blocks (leaf pairs)
+ *   low [nlow][2]       (row, column) clusters of the low-rank blocks        */
+typedef struct mnpbem_cluster_tree {
+  int32_t ncluster;
+  const int32_t* son;
+  const int32_t* cind;
+  const int32_t* ipart;
+  const int32_t* perm;
+  int32_t nfull;
+  const int32_t* full;
+  int32_t nlow;
+  const int32_t* low;
+} mnpbem_cluster_tree;
+
+/* Options of the iterative solver (BEM/@bemiter/options.m; defaults in
+ * brackets).  solver: 0 GMRES [0] (cgs / bicgstab are not built);
+ * precond: 0 none, 1 'full' [1] (the dense inverses of bemret in the
+ * solve's precision: FP64, or complex64 on the tensor cores for MIXED);
+ * restart 0 = no restarts (one cycle of up to maxit steps).                 */
+typedef struct mnpbem_iter_options {
+  int32_t solver;
+  double tol;        /* [1e-6] on ||M (b - A x)|| / ||M b||  */
+  int32_t maxit;     /* [100] */
+  int32_t restart;   /* [0]   */
+  int32_t precond;   /* [1]   */
+  double htol;       /* [1e-6] ACA tolerance */
+  int32_t kmax;      /* [100] largest rank of a low-rank block (<= 512) */
+} mnpbem_iter_options;
+
+/* Statistics of one iterative solve. */
+typedef struct mnpbem_iter_info {
+  int32_t flag;          /* 0 converged, 1 maxit reached */
+  int32_t iter;          /* GMRES steps */
+  double relres;         /* ||M (b - A x)|| / ||M b|| */
+  double true_relres;    /* ||b - A x|| / ||b|| with the H-matrix operator */
+  int32_t rank_max;      /* largest ACA rank over the four matrices */
+  double rank_mean;
+  double compression;    /* stored entries of the four H-matrices / 4 n^2 */
+} mnpbem_iter_info;
+
+/* sig = bem \ exc with the iterative solver (BEM/@bemretiter/solve.m:11-36,
+ * @bemiter/solve.m): H-matrices of G1, H1, G2, H2 (full blocks of the
+ * complete Green function on leaf pairs, low-rank blocks by ACA of the far
+ * field kernel, Greenfun/+aca/@compgreenret/eval.m), the operator of
+ * afun.m with H-matrix products in FP64, GMRES preconditioned by mfun.m.
+ * Excitation: the plane wave exc (ext / sca filled when exc->ninf > 0 for
+ * sca), or the potentials pot when pot is not NULL (exc ignored).  One
+ * wavelength; out as mnpbem_solve (ir_iters: GMRES steps, ir_resid: true
+ * relative residual); info may be NULL.                                     */
+MNPBEM_API mnpbem_status mnpbem_solve_iter(mnpbem_geom* g, const mnpbem_cluster_tree* tree,
+                                           const mnpbem_iter_options* op, const mnpbem_planewave* exc,
+                                           const mnpbem_potentials* pot, double enei, const double* eps_media,
+                                           int32_t nmed, int32_t precision, mnpbem_solution* out,
+                                           mnpbem_iter_info* info);
+
+/* H-matrix `which` (0 G1, 1 H1, 2 G2, 3 H2) of wavelength enei expanded to a
+ * dense [n][n] complex host array (Greenfun/hmatrices/@hmatrix/full.m).
+ * ranks [4][nlow] (may be NULL) receives the ACA ranks.                     */
+MNPBEM_API mnpbem_status mnpbem_hmat_full(mnpbem_geom* g, const mnpbem_cluster_tree* tree,
+                                          const mnpbem_iter_options* op, double enei, const double* eps_media,
+                                          int32_t nmed, int32_t which, double* out, int32_t* ranks);
 
 /* Message of the last failure on the calling thread ("" if none). */
 MNPBEM_API const char* mnpbem_last_error(void);

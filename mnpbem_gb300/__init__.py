@@ -8,7 +8,8 @@ MATLAB calling surface on top of that library.
 """
 from .materials import EV2NM, epsconst, epsdrude, epsfun  # noqa: F401
 from .particles import comparticle, lglnodes, particle, quadface, trisphere  # noqa: F401
-from .bem import (bemoptions, bemret, bemsolver, compstruct, dipoleret, meshfield, planewave,  # noqa: F401
-                  planewaveret, point_media, spectrum_batch, spectrumret)
+from .bem import (bemiter_options, bemoptions, bemret, bemretiter, bemsolver, compstruct, dipoleret,  # noqa: F401
+                  meshfield, planewave, planewaveret, point_media, spectrum_batch, spectrumret)
+from .hmatrix import clustertree, hmatrix_blocks, hpartition  # noqa: F401
 
 __version__ = "0.1.0"

@@ -56,6 +56,24 @@ class Potentials(ctypes.Structure):
                                              ("phi1", "phi1p", "phi2", "phi2p", "a1", "a1p", "a2", "a2p")]
 
 
+class ClusterTree(ctypes.Structure):
+    _fields_ = [("ncluster", ctypes.c_int32), ("son", ctypes.c_void_p), ("cind", ctypes.c_void_p),
+                ("ipart", ctypes.c_void_p), ("perm", ctypes.c_void_p), ("nfull", ctypes.c_int32),
+                ("full", ctypes.c_void_p), ("nlow", ctypes.c_int32), ("low", ctypes.c_void_p)]
+
+
+class IterOptions(ctypes.Structure):
+    _fields_ = [("solver", ctypes.c_int32), ("tol", ctypes.c_double), ("maxit", ctypes.c_int32),
+                ("restart", ctypes.c_int32), ("precond", ctypes.c_int32), ("htol", ctypes.c_double),
+                ("kmax", ctypes.c_int32)]
+
+
+class IterInfo(ctypes.Structure):
+    _fields_ = [("flag", ctypes.c_int32), ("iter", ctypes.c_int32), ("relres", ctypes.c_double),
+                ("true_relres", ctypes.c_double), ("rank_max", ctypes.c_int32), ("rank_mean", ctypes.c_double),
+                ("compression", ctypes.c_double)]
+
+
 class Refine(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int32), ("tol", ctypes.c_double)]
 
@@ -80,6 +98,13 @@ SIGNATURES = {
     "mnpbem_solve_potentials": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Potentials), ctypes.c_double,
                                                c_double_p, ctypes.c_int32, ctypes.c_int32,
                                                ctypes.POINTER(Refine), ctypes.POINTER(Solution)]),
+    "mnpbem_solve_iter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ClusterTree), ctypes.POINTER(IterOptions),
+                                         ctypes.POINTER(PlaneWave), ctypes.POINTER(Potentials), ctypes.c_double,
+                                         c_double_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Solution),
+                                         ctypes.POINTER(IterInfo)]),
+    "mnpbem_hmat_full": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ClusterTree), ctypes.POINTER(IterOptions),
+                                        ctypes.c_double, c_double_p, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_void_p]),
     "mnpbem_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_double_p, c_int32_p, ctypes.c_double,
                                      c_double_p, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 6),
     "mnpbem_geom_size": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p]),

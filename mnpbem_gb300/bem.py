@@ -591,9 +591,125 @@ def spectrum_batch(items, fields=False):
     return [a["res"] for a in args]
 
 
+def bemiter_options(**kw):
+    """Options of the iterative solver (BEM/@bemiter/options.m:19-44)."""
+    op = {"solver": "gmres", "tol": 1e-6, "maxit": 100, "restart": None, "precond": "full", "output": 0,
+          "cleaf": 200, "htol": 1e-6, "kmax": [4, 100], "eta": 2.5}
+    op.update(kw)
+    return op
+
+
+class bemretiter(bemret):
+    """Iterative retarded solver (BEM/@bemretiter) on one GPU.
+
+    H-matrices of G1, H1, G2, H2 on a cluster tree of the faces: full blocks
+    hold the complete Green function (refinement included), far blocks are
+    compressed by adaptive cross approximation (tolerance ``htol``, rank at
+    most ``max(kmax)``).  ``sig = bem.mldivide(exc(p, enei))`` runs GMRES on
+    the operator of afun.m with H-matrix products, preconditioned by the dense
+    inverses of bemret (``precond='full'``, in the solver's precision) or not
+    at all (``precond=None``).  After a solve ``bem.info`` holds flag, iter,
+    relres, true_relres, rank_max, rank_mean and compression.
+
+    Restrictions: solver 'gmres' only; the 'hmat' preconditioner (H-matrix LU
+    of hmatlu / hmatsolve) is not built.
+    """
+
+    def __init__(self, p, op=None):
+        op = bemoptions(op)
+        it = bemiter_options(**op.get("iter", {}))
+        for k in ("solver", "tol", "maxit", "restart", "precond", "cleaf", "htol", "kmax", "eta"):
+            if k in op:
+                it[k] = op[k]
+        if it["solver"] != "gmres":
+            raise NotImplementedError("only the GMRES iterative solver is built")
+        if it["precond"] not in ("full", None, ""):
+            raise NotImplementedError("precond must be 'full' or None (the 'hmat' preconditioner is not built)")
+        super().__init__(p, op)
+        from .hmatrix import hpartition
+        self.iter_op = it
+        self.hpart = hpartition(p, it["cleaf"], it["eta"])
+        self.info = None
+
+    def _opts(self):
+        it = self.iter_op
+        o = _lib.IterOptions()
+        o.solver = 0
+        o.tol = float(it["tol"])
+        o.maxit = int(it["maxit"])
+        o.restart = int(it["restart"] or 0)
+        o.precond = 1 if it["precond"] == "full" else 0
+        o.htol = float(np.min(it["htol"]))
+        o.kmax = int(np.max(it["kmax"]))
+        return o
+
+    def hmat_full(self, enei, which):
+        """H-matrix ``which`` ('G1', 'H1', 'G2', 'H2') expanded to a dense
+        [n, n] array (@hmatrix/full.m) and the ACA ranks [4, nlow]."""
+        q = ("G1", "H1", "G2", "H2").index(which)
+        em = np.ascontiguousarray(self._eps(float(enei))[0])
+        n = self.p.n
+        out = np.zeros((n, n), np.complex128)
+        ranks = np.zeros((4, max(1, self.hpart.low.shape[0])), np.int32)
+        o = self._opts()
+        _lib.check(self._lib.mnpbem_hmat_full(
+            self._h, ctypes.byref(self.hpart.c), ctypes.byref(o), float(enei),
+            em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, q, out.ctypes.data, ranks.ctypes.data))
+        return out, ranks[:, :self.hpart.low.shape[0]]
+
+    def mldivide(self, exc):
+        """sig = bem \\ exc(p, enei) with preconditioned GMRES (bemretiter/solve.m)."""
+        enei = float(exc.enei)
+        n = self.p.n
+        em = np.ascontiguousarray(self._eps(enei)[0])
+        o = self._opts()
+        info = _lib.IterInfo()
+        keep = []
+        if hasattr(exc, "exc"):
+            pw = exc.exc._struct()
+            P = exc.exc.npol
+            pot_ptr = None
+        else:
+            keys1, keys3 = ("phi1", "phi1p", "phi2", "phi2p"), ("a1", "a1p", "a2", "a2p")
+            P = next(np.asarray(getattr(exc, k)).shape[-1] for k in keys1 + keys3 if hasattr(exc, k))
+            if P > 4:
+                raise ValueError("bemretiter: at most 4 excitation columns per solve")
+            pot = _lib.Potentials()
+            pot.npol = P
+            for k in keys1 + keys3:
+                if hasattr(exc, k):
+                    arr = np.ascontiguousarray(np.asarray(getattr(exc, k)), dtype=np.complex128)
+                    keep.append(arr)
+                    setattr(pot, k, arr.ctypes.data)
+            pw = None
+            pot_ptr = ctypes.byref(pot)
+        sig = {k: np.zeros((n, P) if k.startswith("sig") else (n, 3, P), np.complex128)
+               for k in ("sig1", "sig2", "h1", "h2")}
+        ext, sca = np.zeros(P), np.zeros(P)
+        it, res = np.zeros(1, np.int32), np.zeros(1)
+        sol = _lib.Solution()
+        sol.sig1, sol.sig2 = sig["sig1"].ctypes.data, sig["sig2"].ctypes.data
+        sol.h1, sol.h2 = sig["h1"].ctypes.data, sig["h2"].ctypes.data
+        sol.ir_iters, sol.ir_resid = it.ctypes.data, res.ctypes.data
+        if pw is not None:
+            sol.ext, sol.sca = ext.ctypes.data, sca.ctypes.data
+        _lib.check(self._lib.mnpbem_solve_iter(
+            self._h, ctypes.byref(self.hpart.c), ctypes.byref(o), ctypes.byref(pw) if pw is not None else None,
+            pot_ptr, enei, em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, self.precision, ctypes.byref(sol),
+            ctypes.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in _lib.IterInfo._fields_}
+        extra = {"ext": ext, "sca": sca} if pw is not None else {}
+        return compstruct(self.p, enei, iter=int(it[0]), relres=float(res[0]), **sig, **extra)
+
+    solve = mldivide
+
+
 def bemsolver(p, op=None, **kw):
-    """Factory of Base/bemsolver.m: picks the solver class whose needs match op."""
+    """Factory of Base/bemsolver.m: picks the solver class whose needs match op
+    (``'iter'`` in the options selects bemretiter, as its needs = {'iter'})."""
     op = bemoptions(op, **kw)
     if op.get("sim", "ret") != "ret":
         raise NotImplementedError("only the retarded solver (sim='ret') is implemented")
+    if "iter" in op:
+        return bemretiter(p, op)
     return bemret(p, op)

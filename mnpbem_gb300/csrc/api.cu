@@ -26,6 +26,7 @@
 #include "dense.cuh"
 #include "geometry.cuh"
 #include "field.cuh"
+#include "hmat.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
 
@@ -1985,4 +1986,566 @@ mnpbem_status mnpbem_solve_potentials(mnpbem_geom* G, const mnpbem_potentials* p
   jobs[0].c.spectra = false;
   jobs[0].nl = 1;
   return run_jobs(jobs);
+}
+
+// ======================================================================
+// iterative solver: H-matrices + preconditioned GMRES
+// ======================================================================
+namespace {
+
+// index arrays, values and factors of the H-matrices of one cluster tree
+struct HmatHost {
+  DevBuf idx, vals, fac, used, tbuf;
+  HmatDev d;
+  LeafAsm la;
+  std::vector<int4> lblk;   // host copy of the low-rank blocks
+  std::vector<int> ranks;   // [4][nlow] ACA ranks of the current wavelength
+  double mv_bytes = 0.0;    // algorithmic bytes of one product of the four matrices
+};
+
+template <typename T>
+T* carve(char*& p, size_t count) {
+  T* r = reinterpret_cast<T*>(p);
+  p += ((sizeof(T) * count + 255) / 256) * 256;
+  return r;
+}
+size_t carve_size(size_t bytes) { return ((bytes + 255) / 256) * 256; }
+
+mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax, double htol, HmatHost& H,
+                         cudaStream_t st) {
+  const int n = (int)G->g.n;
+  const int nc = t ? t->ncluster : 0;
+  auto bad = [](const char* why) {
+    set_error("cluster tree: %s", why);
+    return MNPBEM_ERR_INVALID_ARG;
+  };
+  if (!t || nc < 1 || !t->son || !t->cind || !t->ipart || !t->perm || t->nfull < 0 || t->nlow < 0 ||
+      (t->nfull > 0 && !t->full) || (t->nlow > 0 && !t->low))
+    return bad("missing arrays");
+  if (kmax < 1 || kmax > ACA_KMAX || !(htol > 0)) {
+    set_error("iterative solver: kmax must be 1..%d and htol > 0", ACA_KMAX);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  std::vector<int> iperm(n, -1);
+  for (int c = 0; c < n; ++c) {
+    const int f = t->perm[c];
+    if (f < 0 || f >= n || iperm[f] >= 0) return bad("perm is not a permutation of the faces");
+    iperm[f] = c;
+  }
+  for (int c = 0; c < nc; ++c) {
+    const int a = t->cind[2 * c], b = t->cind[2 * c + 1];
+    if (a < 0 || b < a || b >= n) return bad("cluster range out of bounds");
+    for (int s = 0; s < 2; ++s)
+      if (t->son[2 * c + s] < -1 || t->son[2 * c + s] >= nc) return bad("son index out of range");
+  }
+  // leaves tile [0, n)
+  std::vector<int> leaves;
+  for (int c = 0; c < nc; ++c)
+    if (t->son[2 * c] < 0) leaves.push_back(c);
+  std::sort(leaves.begin(), leaves.end(), [&](int a, int b) { return t->cind[2 * a] < t->cind[2 * b]; });
+  const int nleaf = (int)leaves.size();
+  std::vector<int> leaf_id(nc, -1), leaf_of(n, -1);
+  {
+    int pos = 0;
+    for (int l = 0; l < nleaf; ++l) {
+      const int c = leaves[l];
+      if (t->cind[2 * c] != pos) return bad("leaves do not tile the faces");
+      for (int i = t->cind[2 * c]; i <= t->cind[2 * c + 1]; ++i) leaf_of[i] = l;
+      pos = t->cind[2 * c + 1] + 1;
+      leaf_id[c] = l;
+    }
+    if (pos != n) return bad("leaves do not tile the faces");
+  }
+  auto rows = [&](int c) { return t->cind[2 * c + 1] - t->cind[2 * c] + 1; };
+  const int nf = t->nfull, nlow = t->nlow;
+  std::vector<int4> fblk(nf), lblk(nlow);
+  std::vector<int64_t> foff(nf), aoff(nlow), boff(nlow), uoff(nlow), toff(nlow);
+  std::vector<int> kcap(nlow), fidx((size_t)nleaf * nleaf, -1);
+  double area = 0.0;
+  int64_t nvals = 0, asz = 0, bsz = 0, usz = 0, tsz = 0;
+  for (int b = 0; b < nf; ++b) {
+    const int r = t->full[2 * b], c = t->full[2 * b + 1];
+    if (r < 0 || r >= nc || c < 0 || c >= nc || leaf_id[r] < 0 || leaf_id[c] < 0)
+      return bad("full blocks must be leaf pairs");
+    fblk[b] = make_int4(t->cind[2 * r], rows(r), t->cind[2 * c], rows(c));
+    foff[b] = nvals;
+    nvals += (int64_t)rows(r) * rows(c);
+    fidx[(size_t)leaf_id[r] * nleaf + leaf_id[c]] = b;
+    area += (double)rows(r) * rows(c);
+  }
+  for (int b = 0; b < nlow; ++b) {
+    const int r = t->low[2 * b], c = t->low[2 * b + 1];
+    if (r < 0 || r >= nc || c < 0 || c >= nc) return bad("low-rank block cluster out of range");
+    const int m = rows(r), nb = rows(c);
+    lblk[b] = make_int4(t->cind[2 * r], m, t->cind[2 * c], nb);
+    kcap[b] = std::min(kmax, std::min(m, nb));
+    aoff[b] = asz; asz += (int64_t)m * kcap[b];
+    boff[b] = bsz; bsz += (int64_t)nb * kcap[b];
+    uoff[b] = usz; usz += m;
+    toff[b] = tsz; tsz += (int64_t)kcap[b] * HMV_NMAX;
+    area += (double)m * nb;
+  }
+  if (area != (double)n * n) return bad("blocks do not partition the matrix");
+  // blocks covering each leaf's rows: full blocks of the leaf, then low-rank
+  // blocks whose row cluster contains it
+  std::vector<std::vector<int>> cover(nleaf);
+  for (int b = 0; b < nf; ++b) cover[leaf_id[t->full[2 * b]]].push_back(b);
+  for (int b = 0; b < nlow; ++b)
+    for (int i = lblk[b].x; i < lblk[b].x + lblk[b].y;) {
+      const int l = leaf_of[i];
+      cover[l].push_back(~b);
+      i = t->cind[2 * leaves[l] + 1] + 1;
+    }
+  std::vector<int> lptr(nleaf + 1, 0), lent;
+  std::vector<int2> leaf(nleaf);
+  for (int l = 0; l < nleaf; ++l) {
+    leaf[l] = make_int2(t->cind[2 * leaves[l]], rows(leaves[l]));
+    lent.insert(lent.end(), cover[l].begin(), cover[l].end());
+    lptr[l + 1] = (int)lent.size();
+  }
+  // device copies
+  const size_t bytes = carve_size(sizeof(int) * 3 * n) + carve_size(sizeof(int) * fidx.size()) +
+                       carve_size(sizeof(int4) * (nf + nlow)) + carve_size(sizeof(int64_t) * (nf + 4 * nlow)) +
+                       carve_size(sizeof(int) * (2 * nlow + 4 * nlow)) + carve_size(sizeof(int2) * nleaf) +
+                       carve_size(sizeof(int) * (nleaf + 1 + lent.size())) + 4096;
+  MNP_TRY(H.idx.ensure(bytes));
+  char* p = static_cast<char*>(H.idx.ptr);
+  std::vector<char> host(bytes, 0);
+  char* hp = host.data();
+  auto put = [&](const void* src, size_t nbytes) -> void* {
+    const size_t off = (size_t)(hp - host.data());
+    if (nbytes) memcpy(hp, src, nbytes);
+    hp += carve_size(nbytes);
+    return p + off;
+  };
+  std::vector<int> perm(t->perm, t->perm + n);
+  H.la.perm = H.d.perm = static_cast<const int*>(put(perm.data(), sizeof(int) * n));
+  H.la.iperm = static_cast<const int*>(put(iperm.data(), sizeof(int) * n));
+  H.la.leaf_of = static_cast<const int*>(put(leaf_of.data(), sizeof(int) * n));
+  H.la.fidx = static_cast<const int*>(put(fidx.data(), sizeof(int) * fidx.size()));
+  H.la.fblk = H.d.fblk = static_cast<const int4*>(put(fblk.data(), sizeof(int4) * nf));
+  H.la.foff = H.d.foff = static_cast<const int64_t*>(put(foff.data(), sizeof(int64_t) * nf));
+  H.d.lblk = static_cast<const int4*>(put(lblk.data(), sizeof(int4) * nlow));
+  H.d.kcap = static_cast<const int*>(put(kcap.data(), sizeof(int) * nlow));
+  H.d.aoff = static_cast<const int64_t*>(put(aoff.data(), sizeof(int64_t) * nlow));
+  H.d.boff = static_cast<const int64_t*>(put(boff.data(), sizeof(int64_t) * nlow));
+  H.d.uoff = static_cast<const int64_t*>(put(uoff.data(), sizeof(int64_t) * nlow));
+  H.d.toff = static_cast<const int64_t*>(put(toff.data(), sizeof(int64_t) * nlow));
+  std::vector<int> zr(4 * (size_t)nlow, 0);
+  H.d.rank = static_cast<int*>(put(zr.data(), sizeof(int) * zr.size()));
+  H.d.leaf = static_cast<const int2*>(put(leaf.data(), sizeof(int2) * nleaf));
+  H.d.lptr = static_cast<const int*>(put(lptr.data(), sizeof(int) * lptr.size()));
+  H.d.lent = static_cast<const int*>(put(lent.data(), sizeof(int) * lent.size()));
+  if ((size_t)(hp - host.data()) > bytes) return bad("internal: index buffer size");
+  MNP_CUDA(cudaMemcpyAsync(H.idx.ptr, host.data(), (size_t)(hp - host.data()), cudaMemcpyHostToDevice, st));
+  // values, factors, scratch
+  MNP_TRY(H.vals.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, nvals)));
+  MNP_TRY(H.fac.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, asz + bsz)));
+  MNP_TRY(H.used.ensure(4 * std::max<int64_t>(1, usz)));
+  MNP_TRY(H.tbuf.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, tsz)));
+  for (int q = 0; q < 4; ++q) {
+    H.la.val[q] = H.d.val[q] = H.vals.as<double2>() + q * nvals;
+    H.d.A[q] = H.fac.as<double2>() + q * (asz + bsz);
+    H.d.B[q] = H.d.A[q] + asz;
+  }
+  H.d.used = H.used.as<unsigned char>();
+  H.d.T = H.tbuf.as<double2>();
+  H.d.n = n; H.d.nfull = nf; H.d.nlow = nlow; H.d.nleaf = nleaf;
+  H.d.tol = htol;
+  H.d.usz = usz; H.d.tsz = tsz;
+  H.la.nfull = nf; H.la.nleaf = nleaf; H.la.nvals = nvals;
+  H.lblk = lblk;
+  MNP_CUDA(cudaStreamSynchronize(st));
+  return MNPBEM_OK;
+}
+
+// full blocks and ACA of one wavelength (lane parameters lp_dev); ranks to
+// the host, bytes of a product with N columns
+mnpbem_status hmat_fill(mnpbem_geom* G, Lane& L, HmatHost& H, int N) {
+  AsmParams p = base_params(G, L.lp_dev.as<LamParams>());
+  MNP_TRY(assemble_leaves(p, H.la, L.st));
+  MNP_TRY(hmat_aca(p, H.d, L.st));
+  H.ranks.assign((size_t)4 * H.d.nlow, 0);
+  if (!H.ranks.empty())
+    MNP_CUDA(cudaMemcpyAsync(H.ranks.data(), H.d.rank, sizeof(int) * H.ranks.size(), cudaMemcpyDeviceToHost, L.st));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
+  double entries = 4.0 * (double)H.la.nvals;
+  for (int q = 0; q < 4; ++q)
+    for (int b = 0; b < H.d.nlow; ++b)
+      entries += (double)H.ranks[(size_t)q * H.d.nlow + b] * (H.lblk[b].y + H.lblk[b].w);
+  H.mv_bytes = 16.0 * (entries + 4.0 * 2.0 * (double)H.d.n * N);
+  return MNPBEM_OK;
+}
+
+void face_eps(mnpbem_geom* G, Lane& L) {
+  const int* fm = G->face_med.as<int>();
+  FaceData f = face_data(G, L);
+  launch_face_eps(G->g.n, fm, fm + G->g.n, L.lp_dev.as<LamParams>(), G->g.nvec, const_cast<double2*>(f.eps1),
+                  const_cast<double2*>(f.eps2), const_cast<float2*>(f.eps1f), const_cast<float2*>(f.eps2f),
+                  const_cast<float2*>(f.Lf), const_cast<float*>(f.nvecf), L.st);
+}
+
+struct IterOpts {
+  double tol = 1e-6, htol = 1e-6;
+  int maxit = 100, restart = 0, precond = 1, kmax = 100;
+};
+
+mnpbem_status iter_opts(const mnpbem_iter_options* op, IterOpts& o) {
+  if (op) {
+    if (op->solver != 0) {
+      set_error("iterative solver: only GMRES (solver 0) is built");
+      return MNPBEM_ERR_UNSUPPORTED;
+    }
+    if (op->tol > 0) o.tol = op->tol;
+    if (op->maxit > 0) o.maxit = op->maxit;
+    if (op->restart > 0) o.restart = op->restart;
+    if (op->precond == 0 || op->precond == 1) o.precond = op->precond;
+    else { set_error("iterative solver: precond must be 0 or 1"); return MNPBEM_ERR_INVALID_ARG; }
+    if (op->htol > 0) o.htol = op->htol;
+    if (op->kmax > 0) o.kmax = op->kmax;
+  }
+  return MNPBEM_OK;
+}
+
+// Restarted, left-preconditioned GMRES on M A x = M b (@bemiter/solve.m with
+// the afun / mfun of bemretiter), x-space vectors [x1 | x2] of 8 n P complex:
+// classical Gram-Schmidt applied twice, complex Givens rotations, stop when
+// ||M (b - A x)|| <= tol ||M b|| (estimated in the cycle, confirmed with the
+// true preconditioned residual after it).
+struct Gmres {
+  mnpbem_geom* G;
+  Lane& L;
+  const SolveCtx& c;
+  HmatHost& H;
+  const IterOpts& o;
+  int64_t n, len;
+  int P;
+  DevBuf V, part, hdev, zero, rvec;
+  std::vector<double2> hpart;
+  std::vector<double> npart;
+
+  Gmres(mnpbem_geom* G_, Lane& L_, const SolveCtx& c_, HmatHost& H_, const IterOpts& o_)
+      : G(G_), L(L_), c(c_), H(H_), o(o_), n(G_->g.n), len(8 * G_->g.n * c_.P), P(c_.P) {}
+
+  // (rphi, ra, ral, rDe) = b - A x with b = (bphi, ba, bal, bDe); norms[0..1] += ||r||^2, ||b||^2
+  mnpbem_status residual(const double2* x, const double2* bphi, const double2* ba, const double2* bal,
+                         const double2* bDe) {
+    Vec64 v = vec64(G, L, P);
+    double2* y[4] = {v.Y1, v.Z1, v.Y2, v.Z2};
+    MNP_TRY(hmat_mv(H.d, 4 * P, x, x + 4 * n * P, y, H.mv_bytes, L.st));
+    launch_residual(face_data(G, L), P, L.lp_dev.as<LamParams>(), v.Y1, v.Y2, v.Z1, v.Z2, bphi, ba, bal, bDe,
+                    v.rphi, v.ra, v.ral, v.rDe, L.norms.as<double>(), L.st);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  // dst (x-space) = M applied to the b-space vector (phi, a, alpha, De)
+  mnpbem_status precond(const double2* phi, const double2* a, const double2* al, const double2* De, double2* dst) {
+    Vec64 v = vec64(G, L, P);
+    if (!o.precond) {
+      kv_pack_bx(n, P, phi, a, al, De, dst, L.st);
+    } else if (c.precision == MNPBEM_FP64) {
+      MNP_TRY(apply_mldivide<double>(face_data(G, L), P, L.lp_dev.as<LamParams>(), chain_mats<double>(G, L), phi, a,
+                                     al, De, dst, dst + 4 * n * P, v.work, gemm_w<double>, nullptr, L.st));
+    } else {
+      MNP_TRY(apply32(G, L, P, phi, a, al, De));
+      launch_cvt_f2d(fx_ptr(G, L, P, 0), dst, 4 * n * P, L.st);
+      launch_cvt_f2d(fx_ptr(G, L, P, 1), dst + 4 * n * P, 4 * n * P, L.st);
+    }
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  // dst = M A x
+  mnpbem_status op(const double2* x, double2* dst) {
+    const double2* z = zero.as<double2>();
+    MNP_TRY(residual(x, z, z + n * P, z + 4 * n * P, z + 7 * n * P));   // -A x
+    Vec64 v = vec64(G, L, P);
+    MNP_TRY(precond(v.rphi, v.ra, v.ral, v.rDe, dst));
+    kv_scale(dst, len, -1.0, dst, L.st);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  mnpbem_status norm(const double2* w, double& out) {
+    kv_norm2(w, len, part.as<double>(), L.st);
+    MNP_CHECK_LAUNCH();
+    npart.resize(KV_BLOCKS);
+    MNP_CUDA(cudaMemcpyAsync(npart.data(), part.ptr, sizeof(double) * KV_BLOCKS, cudaMemcpyDeviceToHost, L.st));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
+    double s = 0.0;
+    for (double q : npart) s += q;
+    out = sqrt(s);
+    return MNPBEM_OK;
+  }
+  mnpbem_status dots(int nv, const double2* w, std::vector<std::complex<double>>& h) {
+    kv_dots(V.as<double2>(), nv, len, w, part.as<double2>(), L.st);
+    MNP_CHECK_LAUNCH();
+    hpart.resize((size_t)nv * KV_BLOCKS);
+    MNP_CUDA(cudaMemcpyAsync(hpart.data(), part.ptr, sizeof(double2) * hpart.size(), cudaMemcpyDeviceToHost, L.st));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
+    h.assign(nv, 0.0);
+    for (int i = 0; i < nv; ++i) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int b = 0; b < KV_BLOCKS; ++b) s = cadd(s, hpart[(size_t)i * KV_BLOCKS + b]);
+      h[i] = std::complex<double>(s.x, s.y);
+    }
+    return MNPBEM_OK;
+  }
+  // w -= sum_i h_i V_i
+  mnpbem_status update(int nv, const std::vector<std::complex<double>>& h, double2* w) {
+    MNP_CUDA(cudaMemcpyAsync(hdev.ptr, h.data(), sizeof(double2) * nv, cudaMemcpyHostToDevice, L.st));
+    kv_update(V.as<double2>(), nv, len, hdev.as<double2>(), w, L.st);
+    MNP_CHECK_LAUNCH();
+    MNP_CUDA(cudaStreamSynchronize(L.st));   // h lives in pageable host memory
+    return MNPBEM_OK;
+  }
+
+  mnpbem_status run(int& flag, int& steps, double& relres) {
+    using cd = std::complex<double>;
+    // restart 0: cycles of up to maxit steps, maxit steps in all; else cycles
+    // of restart steps, at most maxit cycles.  A cycle whose estimated
+    // residual reached the tolerance while the true one did not (an inexact
+    // complex64 preconditioner) is followed by another within the budget.
+    const int inner = o.restart > 0 ? o.restart : o.maxit;
+    const int64_t budget = o.restart > 0 ? (int64_t)o.maxit * o.restart : o.maxit;
+    MNP_TRY(V.ensure(sizeof(double2) * (size_t)(inner + 1) * len));
+    MNP_TRY(part.ensure(sizeof(double2) * (size_t)(inner + 1) * KV_BLOCKS));
+    MNP_TRY(hdev.ensure(sizeof(double2) * (size_t)(inner + 1)));
+    MNP_TRY(zero.ensure(sizeof(double2) * len));
+    MNP_TRY(rvec.ensure(sizeof(double2) * len));
+    MNP_CUDA(cudaMemsetAsync(zero.ptr, 0, sizeof(double2) * len, L.st));
+    Vec64 v = vec64(G, L, P);
+    double2* x = v.x1;                     // x2 follows x1
+    double2* r = rvec.as<double2>();
+    double2* Vb = V.as<double2>();
+    MNP_CUDA(cudaMemsetAsync(x, 0, sizeof(double2) * len, L.st));
+    MNP_TRY(precond(v.phi, v.a, v.alpha, v.De, r));
+    double nmb = 0.0;
+    MNP_TRY(norm(r, nmb));
+    flag = 1;
+    steps = 0;
+    relres = 0.0;
+    if (!(nmb > 0)) {
+      flag = nmb == 0 ? 0 : 1;
+      if (nmb != 0) { set_error("GMRES: non-finite right-hand side"); return MNPBEM_ERR_NOT_CONVERGED; }
+      return MNPBEM_OK;
+    }
+    const double tolb = o.tol * nmb;
+    std::vector<cd> h, h2, g(inner + 1), sn(inner), y;
+    std::vector<double> cs(inner);
+    std::vector<std::vector<cd>> Hc(inner, std::vector<cd>(inner + 1));
+    double rn = nmb;
+    while (steps < budget) {
+      const double beta = rn;
+      if (beta <= tolb) { flag = 0; break; }
+      const int inner_c = (int)std::min<int64_t>(inner, budget - steps);
+      kv_scale(r, len, 1.0 / beta, Vb, L.st);
+      std::fill(g.begin(), g.end(), cd(0.0));
+      g[0] = beta;
+      int m = 0;
+      for (int j = 0; j < inner_c; ++j) {
+        double2* w = Vb + (size_t)(j + 1) * len;
+        MNP_TRY(op(Vb + (size_t)j * len, w));
+        ++steps;
+        MNP_TRY(dots(j + 1, w, h));
+        MNP_TRY(update(j + 1, h, w));
+        MNP_TRY(dots(j + 1, w, h2));
+        MNP_TRY(update(j + 1, h2, w));
+        for (int i = 0; i <= j; ++i) h[i] += h2[i];
+        double hn = 0.0;
+        MNP_TRY(norm(w, hn));
+        if (!(hn == hn)) { set_error("GMRES: non-finite Krylov vector"); return MNPBEM_ERR_NOT_CONVERGED; }
+        std::vector<cd>& col = Hc[j];
+        std::fill(col.begin(), col.end(), cd(0.0));
+        for (int i = 0; i <= j; ++i) col[i] = h[i];
+        col[j + 1] = hn;
+        for (int i = 0; i < j; ++i) {
+          const cd a0 = col[i], a1 = col[i + 1];
+          col[i] = cs[i] * a0 + sn[i] * a1;
+          col[i + 1] = -std::conj(sn[i]) * a0 + cs[i] * a1;
+        }
+        const cd a = col[j], bb = col[j + 1];
+        const double t = std::hypot(std::abs(a), std::abs(bb));
+        if (std::abs(a) == 0.0) {
+          cs[j] = 0.0;
+          sn[j] = 1.0;
+        } else {
+          cs[j] = std::abs(a) / t;
+          sn[j] = (a / std::abs(a)) * std::conj(bb) / t;
+        }
+        col[j] = cs[j] * a + sn[j] * bb;
+        col[j + 1] = 0.0;
+        g[j + 1] = -std::conj(sn[j]) * g[j];
+        g[j] = cs[j] * g[j];
+        m = j + 1;
+        if (hn == 0.0 || std::abs(g[j + 1]) <= tolb) break;
+        kv_scale(w, len, 1.0 / hn, w, L.st);
+      }
+      // x += V y with H y = g (upper triangular)
+      y.assign(m, 0.0);
+      for (int i = m - 1; i >= 0; --i) {
+        cd s = g[i];
+        for (int k = i + 1; k < m; ++k) s -= Hc[k][i] * y[k];
+        y[i] = s / Hc[i][i];
+      }
+      for (int i = 0; i < m; ++i) y[i] = -y[i];
+      MNP_TRY(update(m, y, x));
+      // true preconditioned residual
+      MNP_TRY(residual(x, v.phi, v.a, v.alpha, v.De));
+      MNP_TRY(precond(v.rphi, v.ra, v.ral, v.rDe, r));
+      MNP_TRY(norm(r, rn));
+      if (rn <= tolb) { flag = 0; break; }
+    }
+    if (rn <= tolb) flag = 0;
+    relres = rn / nmb;
+    return MNPBEM_OK;
+  }
+};
+
+// one wavelength on lane 0: excitation, H-matrices, optional preconditioner
+mnpbem_status iter_prepare(mnpbem_geom* G, Job& j, const double2* ext_pot, HmatHost& H, const IterOpts& o,
+                           const mnpbem_cluster_tree* tree) {
+  Lane& L = *G->lanes[0];
+  MNP_TRY(upload_lp(G, L, j.s, 0));
+  L.w = 0;
+  MNP_TRY(hmat_setup(G, tree, o.kmax, o.htol, H, L.st));
+  if (o.precond) {
+    MNP_TRY(run_stage(G, L, j.c, 0, true));   // per-face eps + dense matrices
+    MNP_TRY(run_stage(G, L, j.c, 1, true));   // dense inverses of bemret (initmat.m)
+  } else {
+    face_eps(G, L);
+    MNP_CHECK_LAUNCH();
+  }
+  const int P = j.c.P;
+  MNP_TRY(hmat_fill(G, L, H, 4 * P));
+  Vec64 v = vec64(G, L, P);
+  const FaceData fd = face_data(G, L);
+  const LamParams* lp = L.lp_dev.as<LamParams>();
+  if (ext_pot) {
+    launch_excitation_ext(fd, P, ext_pot, lp, v.phi, v.a, v.alpha, v.De, L.st);
+  } else {
+    const double* pol = G->exbuf.as<double>();
+    launch_excitation(fd, P, pol, pol + 3 * P, lp, v.phi, v.a, v.alpha, v.De, L.st);
+  }
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
+// ranks and the stored entries of the four H-matrices against 4 n^2
+void hmat_stats(const HmatHost& H, const std::vector<int>& ranks, int64_t n, mnpbem_iter_info* info) {
+  int rmax = 0;
+  double rs = 0.0, stored = 4.0 * (double)H.la.nvals;
+  for (int q = 0; q < 4; ++q)
+    for (int b = 0; b < H.d.nlow; ++b) {
+      const int r = ranks[(size_t)q * H.d.nlow + b];
+      rmax = std::max(rmax, r);
+      rs += r;
+      stored += (double)r * (H.lblk[b].y + H.lblk[b].w);
+    }
+  info->rank_max = rmax;
+  info->rank_mean = ranks.empty() ? 0.0 : rs / ranks.size();
+  info->compression = stored / (4.0 * (double)n * n);
+}
+
+}  // namespace
+
+mnpbem_status mnpbem_solve_iter(mnpbem_geom* G, const mnpbem_cluster_tree* tree, const mnpbem_iter_options* op,
+                                const mnpbem_planewave* exc, const mnpbem_potentials* pot, double enei,
+                                const double* eps_media, int32_t nmed, int32_t precision, mnpbem_solution* out,
+                                mnpbem_iter_info* info) {
+  MNP_TRY(check_geom(G));
+  IterOpts o;
+  MNP_TRY(iter_opts(op, o));
+  if (!out || !(enei > 0) || (!exc && !pot) || (pot && (pot->npol < 1 || pot->npol > 4))) {
+    set_error("mnpbem_solve_iter: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  const int P = pot ? pot->npol : exc->npol;
+  std::vector<double> zero(3 * P, 0.0);
+  mnpbem_planewave pw{P, zero.data(), zero.data(), 1, 0, nullptr, nullptr};
+  mnpbem_solution so = *out;
+  if (pot) so.ext = so.sca = nullptr;
+  const mnpbem_planewave* ex = pot ? &pw : exc;
+  MNP_TRY(validate_job(G, ex, 1, &enei, eps_media, nmed, precision, &so));
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  const int64_t n = G->g.n;
+  DevBuf dpot;
+  if (pot) {
+    const double* src[8] = {pot->phi1, pot->phi1p, pot->phi2, pot->phi2p, pot->a1, pot->a1p, pot->a2, pot->a2p};
+    MNP_TRY(dpot.ensure(sizeof(double2) * 16 * n * P));
+    double2* D = dpot.as<double2>();
+    for (int q = 0; q < 8; ++q) {
+      const int64_t cnt = (q < 4 ? 1 : 3) * n * P;
+      double2* dst = D + (q < 4 ? q * n * P : 4 * n * P + (q - 4) * 3 * n * P);
+      if (src[q]) MNP_CUDA(cudaMemcpy(dst, src[q], sizeof(double2) * cnt, cudaMemcpyHostToDevice));
+      else MNP_CUDA(cudaMemset(dst, 0, sizeof(double2) * cnt));
+    }
+  }
+  std::vector<Job> jobs(1);
+  Job& j = jobs[0];
+  j.G = G;
+  MNP_TRY(job_setup(j, ex, 1, &enei, eps_media, nmed, precision, nullptr, &so));
+  j.c.spectra = !pot;
+  Lane& L = *G->lanes[0];
+  HmatHost H;
+  MNP_TRY(iter_prepare(G, j, pot ? dpot.as<double2>() : nullptr, H, o, tree));
+  Gmres gm(G, L, j.c, H, o);
+  int flag = 1, steps = 0;
+  double relres = 0.0;
+  MNP_TRY(gm.run(flag, steps, relres));
+  // true relative residual ||b - A x|| / ||b|| with the H-matrix operator
+  Vec64 v = vec64(G, L, P);
+  MNP_CUDA(cudaMemsetAsync(L.norms.ptr, 0, sizeof(double) * 4, L.st));
+  MNP_TRY(gm.residual(v.x1, v.phi, v.a, v.alpha, v.De));
+  double hn[4];
+  MNP_CUDA(cudaMemcpyAsync(hn, L.norms.ptr, sizeof(double) * 4, cudaMemcpyDeviceToHost, L.st));
+  if (j.c.spectra) MNP_TRY(run_stage(G, L, j.c, 4, true));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
+  L.iters = steps;
+  L.res = hn[1] > 0 ? sqrt(hn[0] / hn[1]) : 0.0;
+  MNP_TRY(write_outputs(G, L, j.c, j.s, 0));
+  G->prof.flush();
+  if (info) {
+    info->flag = flag;
+    info->iter = steps;
+    info->relres = relres;
+    info->true_relres = L.res;
+    hmat_stats(H, H.ranks, n, info);
+  }
+  return MNPBEM_OK;
+}
+
+mnpbem_status mnpbem_hmat_full(mnpbem_geom* G, const mnpbem_cluster_tree* tree, const mnpbem_iter_options* op,
+                               double enei, const double* eps_media, int32_t nmed, int32_t which, double* out,
+                               int32_t* ranks) {
+  MNP_TRY(check_geom(G));
+  IterOpts o;
+  MNP_TRY(iter_opts(op, o));
+  if (!out || which < 0 || which > 3 || !(enei > 0)) {
+    set_error("mnpbem_hmat_full: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  const double pol[3] = {1, 0, 0}, dir[3] = {0, 0, 1};
+  mnpbem_planewave pw{1, pol, dir, 1, 0, nullptr, nullptr};
+  mnpbem_solution so{};
+  MNP_TRY(validate_job(G, &pw, 1, &enei, eps_media, nmed, MNPBEM_FP64, &so));
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  std::vector<Job> jobs(1);
+  Job& j = jobs[0];
+  j.G = G;
+  MNP_TRY(job_setup(j, &pw, 1, &enei, eps_media, nmed, MNPBEM_FP64, nullptr, &so));
+  Lane& L = *G->lanes[0];
+  MNP_TRY(upload_lp(G, L, j.s, 0));
+  HmatHost H;
+  MNP_TRY(hmat_setup(G, tree, o.kmax, o.htol, H, L.st));
+  MNP_TRY(hmat_fill(G, L, H, 4));
+  const int64_t n = G->g.n;
+  DevBuf full;
+  MNP_TRY(full.ensure(sizeof(double2) * n * n));
+  MNP_TRY(hmat_full(H.d, which, full.as<double2>(), L.st));
+  MNP_CUDA(cudaMemcpyAsync(out, full.ptr, sizeof(double2) * n * n, cudaMemcpyDeviceToHost, L.st));
+  if (ranks && H.d.nlow > 0)
+    MNP_CUDA(cudaMemcpyAsync(ranks, H.d.rank, sizeof(int) * 4 * H.d.nlow, cudaMemcpyDeviceToHost, L.st));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
+  return MNPBEM_OK;
 }

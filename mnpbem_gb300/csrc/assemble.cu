@@ -158,6 +158,30 @@ constexpr int ASM_COLS = 128;
 constexpr int ASM_ROWS = 4;
 constexpr int ASM_DS_ROWS = 8;
 
+struct Val4 { double2 g1, h1, g2, h2; };
+
+// G1, H1, G2, H2 of the pair (i, j) by the far-field formula
+__device__ __forceinline__ Val4 far4(const AsmParams& p, const CisShared& T, int64_t i, const double4_32a& sj,
+                                     int pj) {
+  const double4_32a si = p.src[i];
+  const double4_32a ni = p.nrm[i];
+  const double x = si.x - sj.x, y = si.y - sj.y, z = si.z - sj.z;
+  const double dist = sqrt(x * x + y * y + z * z);
+  const double dd = fmax(dist, DBL_EPS_ASM);
+  const double delta = (dd == DBL_EPS_ASM) ? 2.0 * M_PI : 0.0;
+  const double inv = 1.0 / dd;
+  const double in = x * ni.x + y * ni.y + z * ni.z;
+  const int pi = p.part[i];
+  const int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
+  Val4 o;
+  o.g1 = make_double2(0, 0); o.h1 = o.g1; o.g2 = o.g1; o.h2 = o.g1;
+  if (m11) { PairVal v = far_pair(T, p.lp->k[m11 - 1], dd, inv, in, sj.w); o.g1 = v.G; o.h1 = make_double2(v.F.x + delta, v.F.y); }
+  if (m21) { PairVal v = far_pair(T, p.lp->k[m21 - 1], dd, inv, in, sj.w); o.g1 = csub(o.g1, v.G); o.h1 = csub(o.h1, make_double2(v.F.x + delta, v.F.y)); }
+  if (m22) { PairVal v = far_pair(T, p.lp->k[m22 - 1], dd, inv, in, sj.w); o.g2 = v.G; o.h2 = make_double2(v.F.x - delta, v.F.y); }
+  if (m12) { PairVal v = far_pair(T, p.lp->k[m12 - 1], dd, inv, in, sj.w); o.g2 = csub(o.g2, v.G); o.h2 = csub(o.h2, make_double2(v.F.x - delta, v.F.y)); }
+  return o;
+}
+
 template <bool W64, bool W32>
 __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
   __shared__ CisShared T;
@@ -167,27 +191,31 @@ __global__ void __launch_bounds__(ASM_COLS) k_asm_far(AsmParams p) {
   if (j >= p.n) return;
   double4_32a sj = p.src[j];
   int pj = p.part[j];
-  const double twopi = 2.0 * M_PI;
 #pragma unroll
   for (int r = 0; r < ASM_ROWS; ++r) {
     int64_t i = i0 + r;
     if (i >= p.n) break;
-    double4_32a si = p.src[i];
-    double4_32a ni = p.nrm[i];
-    double x = si.x - sj.x, y = si.y - sj.y, z = si.z - sj.z;
-    double dist = sqrt(x * x + y * y + z * z);
-    double dd = fmax(dist, DBL_EPS_ASM);
-    double delta = (dd == DBL_EPS_ASM) ? twopi : 0.0;
-    double inv = 1.0 / dd;
-    double in = x * ni.x + y * ni.y + z * ni.z;
-    int pi = p.part[i];
-    int m11 = p.med[0][pi][pj], m21 = p.med[1][pi][pj], m22 = p.med[2][pi][pj], m12 = p.med[3][pi][pj];
-    double2 g1 = make_double2(0, 0), h1 = g1, g2 = g1, h2 = g1;
-    if (m11) { PairVal v = far_pair(T, p.lp->k[m11 - 1], dd, inv, in, sj.w); g1 = v.G; h1 = make_double2(v.F.x + delta, v.F.y); }
-    if (m21) { PairVal v = far_pair(T, p.lp->k[m21 - 1], dd, inv, in, sj.w); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
-    if (m22) { PairVal v = far_pair(T, p.lp->k[m22 - 1], dd, inv, in, sj.w); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
-    if (m12) { PairVal v = far_pair(T, p.lp->k[m12 - 1], dd, inv, in, sj.w); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
-    store4<W64, W32>(p, i, j, g1, h1, g2, h2);
+    const Val4 v = far4(p, T, i, sj, pj);
+    store4<W64, W32>(p, i, j, v.g1, v.h1, v.g2, v.h2);
+  }
+}
+
+// full (near-field) blocks of the H-matrices: entries of the complete Green
+// function on leaf pairs of the cluster tree, FP64, block b row-major at
+// val[q] + foff[b] (Greenfun/@hmatrix/fillval.m with compgreenret's eval)
+__global__ void __launch_bounds__(256) k_asm_leaf(AsmParams p, LeafAsm la) {
+  __shared__ CisShared T;
+  cis_load(T);
+  const int b = blockIdx.x;
+  const int4 blk = la.fblk[b];   // (r0, m, c0, nb)
+  const int64_t cnt = (int64_t)blk.y * blk.w;
+  const int64_t off = la.foff[b];
+  for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const int r = (int)(e / blk.w), c = (int)(e - (int64_t)r * blk.w);
+    const int i = la.perm[blk.x + r], j = la.perm[blk.z + c];
+    const Val4 v = far4(p, T, i, p.src[j], p.part[j]);
+    la.val[0][off + e] = v.g1; la.val[1][off + e] = v.h1;
+    la.val[2][off + e] = v.g2; la.val[3][off + e] = v.h2;
   }
 }
 
@@ -444,11 +472,7 @@ __device__ __forceinline__ PairVal near_pair(const AsmParams& p, int64_t e, doub
   return v;
 }
 
-template <bool W64, bool W32>
-__global__ void k_asm_near(AsmParams p) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= p.nref) return;
-  int i = p.ref_row[e], j = p.ref_col[e];
+__device__ __forceinline__ Val4 near4(const AsmParams& p, int64_t e, int i, int j) {
   double4_32a si = p.src[i], sj = p.src[j];
   double4_32a nn = p.nrm[i];
   double3 ni = make_double3(nn.x, nn.y, nn.z);
@@ -463,7 +487,45 @@ __global__ void k_asm_near(AsmParams p) {
   if (m21) { PairVal v = near_pair(p, e, p.lp->k[m21 - 1], dd, ni); g1 = csub(g1, v.G); h1 = csub(h1, make_double2(v.F.x + delta, v.F.y)); }
   if (m22) { PairVal v = near_pair(p, e, p.lp->k[m22 - 1], dd, ni); g2 = v.G; h2 = make_double2(v.F.x - delta, v.F.y); }
   if (m12) { PairVal v = near_pair(p, e, p.lp->k[m12 - 1], dd, ni); g2 = csub(g2, v.G); h2 = csub(h2, make_double2(v.F.x - delta, v.F.y)); }
-  store4<W64, W32>(p, i, j, g1, h1, g2, h2);
+  return Val4{g1, h1, g2, h2};
+}
+
+template <bool W64, bool W32>
+__global__ void k_asm_near(AsmParams p) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.nref) return;
+  const int i = p.ref_row[e], j = p.ref_col[e];
+  const Val4 v = near4(p, e, i, j);
+  store4<W64, W32>(p, i, j, v.g1, v.h1, v.g2, v.h2);
+}
+
+// refined entries that fall in full blocks of the H-matrices (refined pairs in
+// low-rank blocks keep the far-field kernel, as ACA does)
+__global__ void k_asm_leaf_near(AsmParams p, LeafAsm la) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.nref) return;
+  const int i = p.ref_row[e], j = p.ref_col[e];
+  const int ci = la.iperm[i], cj = la.iperm[j];
+  const int b = la.fidx[(int64_t)la.leaf_of[ci] * la.nleaf + la.leaf_of[cj]];
+  if (b < 0) return;
+  const int4 blk = la.fblk[b];
+  const int64_t o = la.foff[b] + (int64_t)(ci - blk.x) * blk.w + (cj - blk.z);
+  const Val4 v = near4(p, e, i, j);
+  la.val[0][o] = v.g1; la.val[1][o] = v.h1; la.val[2][o] = v.g2; la.val[3][o] = v.h2;
+}
+
+mnpbem_status assemble_leaves(const AsmParams& p, const LeafAsm& la, cudaStream_t st) {
+  MNP_TRY(ensure_cis(st));
+  if (la.nfull > 0) {
+    ProfScope ps(PH_HMAT_BUILD, st, 0.0, 64.0 * (double)la.nvals, p.nref > 0 ? 2 : 1);
+    k_asm_leaf<<<la.nfull, 256, 0, st>>>(p, la);
+    MNP_CHECK_LAUNCH();
+    if (p.nref > 0) {
+      k_asm_leaf_near<<<(unsigned)cdiv_up(p.nref, 128), 128, 0, st>>>(p, la);
+      MNP_CHECK_LAUNCH();
+    }
+  }
+  return MNPBEM_OK;
 }
 
 __global__ void k_pack_src(int n, const double* pos, const double* area, const double* nvec,

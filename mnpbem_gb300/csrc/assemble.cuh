@@ -35,6 +35,21 @@ struct AsmParams {
   float2 *G1hi = nullptr, *H1hi = nullptr, *G2hi = nullptr, *H2hi = nullptr;
 };
 
+// full blocks of the H-matrices of G1, H1, G2, H2 on the leaf pairs of a
+// cluster tree (cluster order = perm)
+struct LeafAsm {
+  int nfull = 0, nleaf = 0;
+  int64_t nvals = 0;             // sum of the blocks' entries
+  const int4* fblk = nullptr;    // [nfull] (first row, rows, first col, cols) in cluster order
+  const int64_t* foff = nullptr; // [nfull] value offsets
+  const int* perm = nullptr;     // [n] face at each cluster position
+  const int* iperm = nullptr;    // [n] cluster position of each face
+  const int* leaf_of = nullptr;  // [n] leaf index of each cluster position
+  const int* fidx = nullptr;     // [nleaf][nleaf] full block of a leaf pair, -1 if none
+  double2* val[4] = {};          // G1, H1, G2, H2 block values, row-major per block
+};
+mnpbem_status assemble_leaves(const AsmParams& p, const LeafAsm& la, cudaStream_t st);
+
 void pack_sources(int n, const double* pos, const double* area, const double* nvec, double4_32a* src,
                   double4_32a* nrm, float4* srcf, float4* nrmf, cudaStream_t st);
 // w64 && !w32: complex128 outputs; !w64 && w32: complex64 outputs;

@@ -15,6 +15,8 @@ enum Phase {
   PH_ELEMWISE,      // Sigma stage, chain steps, conversions, excitation
   PH_SPECTRA,       // far fields + cross sections
   PH_GEOMETRY,      // one-time geometry / refinement set-up
+  PH_HMAT_BUILD,    // H-matrices: full blocks and ACA of the far blocks
+  PH_HMAT_MV,       // H-matrix products of the iterative solver
   PH_COUNT
 };
 

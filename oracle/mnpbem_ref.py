@@ -784,6 +784,12 @@ class BemRet:
         """mldivide.m:12-49 -> dict with sig1, sig2 [n, npol], h1, h2 [n, 3, npol]."""
         self.initmat(exc["enei"])
         phi, a, alpha, De = self.excitation(exc)
+        out = self.chain(phi, a, alpha, De)
+        out["enei"] = exc["enei"]
+        return out
+
+    def chain(self, phi, a, alpha, De):
+        """mldivide.m:20-49 on excitation variables (after initmat)."""
         k, nvec = self.k, self.nvec
         G1i, G2i, L1, L2 = self.G1i, self.G2i, self.L1, self.L2
         Sigma1, Deltai, Sigmai = self.Sigma1, self.Deltai, self.Sigmai
@@ -795,7 +801,7 @@ class BemRet:
         h1 = _matmul(G1i, h2 + a)
         sig2 = _matmul(G2i, sig2)
         h2 = _matmul(G2i, h2)
-        return {"enei": exc["enei"], "sig1": sig1, "sig2": sig2, "h1": h1, "h2": h2}
+        return {"sig1": sig1, "sig2": sig2, "h1": h1, "h2": h2}
 
     def afun(self, sig1, h1, sig2, h2):
         """Full BEM operator (BEM/@bemretiter/private/afun.m:6-35).

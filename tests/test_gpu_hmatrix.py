@@ -1,0 +1,124 @@
+"""GPU iterative solver (BEM/@bemretiter) against the oracle.
+
+Same cluster tree (796-face sphere, leaves of at most 32 faces: 144 low-rank
+blocks) on both sides.  Checks through the C ABI:
+* mnpbem_hmat_full: the four H-matrices expanded (full blocks from the GPU
+  assembly incl. refinement, low-rank blocks from the GPU ACA) equal the
+  oracle's expansions to 1e-9 (max |diff| / max |ref|) and the dense matrices
+  to 1e-5; the ACA ranks equal the oracle's in at least 95 % of the blocks;
+* mnpbem_solve_iter, FP64 with the 'full' preconditioner: charges equal the
+  oracle's iterative solution to 1e-8 with the same number of GMRES steps,
+  and the direct solve to 1e-5; no preconditioner: converged, same step count
+  as the oracle within 2, charges within 1e-6 of the oracle's; MIXED
+  preconditioner (complex64 tensor-core inverses) at tol 1e-10: within 1e-8 of
+  the FP64 iterative solve of the same H-matrix operator and 1e-5 of the
+  direct FP64 solve (the ACA error of the operator); dipole potentials through
+  the same entry.
+"""
+import numpy as np
+import pytest
+
+import mnpbem_gb300 as m
+from mnpbem_gb300 import shapes
+
+from test_gpu_parity import drude, rel, record
+
+pytestmark = pytest.mark.gpu
+
+CLEAF = 32
+ENEI = 600.0
+
+
+@pytest.fixture(scope="module")
+def case(gpu_lib):
+    from oracle import hmatrix_ref as HR
+    from oracle import mnpbem_ref as R
+    t = shapes.tables()
+    q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    v, f = shapes.trisphere(400, 30.0)
+    ocp = R.ComParticle([R.EpsConst(1.77), R.drude_eps()], [R.Particle(v, f, q)], [[2, 1]], [True])
+    cp = m.comparticle([m.epsconst(1.77), drude()], [m.trisphere(400, 30.0)], [[2, 1]], 1)
+    oit = HR.BemRetIter(ocp, cleaf=CLEAF)
+    oit.initmat(ENEI)
+    return cp, ocp, oit
+
+
+def test_hmatrices_match_oracle(case):
+    cp, ocp, oit = case
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=CLEAF)))
+    assert np.array_equal(bem.hpart.low, np.asarray(oit.H[0].low))
+    b = oit.bem
+    errs = {}
+    same = 0
+    for q, (name, D) in enumerate(zip(("G1", "H1", "G2", "H2"), (b.G1, b.H1, b.G2, b.H2))):
+        F, ranks = bem.hmat_full(ENEI, name)
+        OF = oit.H[q].full_matrix()
+        errs[name + "_oracle"] = rel(F, OF)
+        errs[name + "_dense"] = rel(F, D)
+        same += int(np.sum(ranks[q] == np.asarray(oit.H[q].ranks())))
+    record("hmatrix_full", **errs, rank_match=same / (4 * len(oit.H[0].low)))
+    for k, e in errs.items():
+        assert e < (1e-9 if k.endswith("oracle") else 1e-5), (k, e)
+    assert same >= 0.95 * 4 * len(oit.H[0].low)
+
+
+def test_iterative_solve_fp64(case):
+    from oracle import hmatrix_ref as HR
+    from oracle import mnpbem_ref as R
+    cp, ocp, oit = case
+    pw = R.PlaneWaveRet([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]], None)
+    oexc = pw.potential(ocp, ENEI)
+    osig = oit.solve(oexc)
+    direct = R.BemRet(ocp).solve(oexc)
+    exc = m.planewave([[1, 0, 0], [0, 1, 0]], [[0, 0, 1], [0, 0, 1]])
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=CLEAF)))
+    sig = bem.mldivide(exc(cp, ENEI))
+    info = bem.info
+    errs = {k: rel(getattr(sig, k), osig[k]) for k in ("sig1", "sig2", "h1", "h2")}
+    errs.update({k + "_direct": rel(getattr(sig, k), direct[k]) for k in ("sig1", "sig2", "h1", "h2")})
+    dsig = m.bemsolver(cp, m.bemoptions(precision="fp64")).mldivide(exc(cp, ENEI))
+    errs["ext_vs_direct"] = rel(sig.ext, dsig.ext)
+    record("iter_fp64", **errs, iter=info["iter"], oracle_iter=oit.iter, relres=info["relres"],
+           true_relres=info["true_relres"], rank_max=info["rank_max"], compression=info["compression"])
+    assert info["flag"] == 0 and info["iter"] == oit.iter
+    for k, e in errs.items():
+        tol = 1e-8 if k in ("sig1", "sig2", "h1", "h2") else (1e-6 if k == "ext_vs_direct" else 1e-5)
+        assert e < tol, (k, e)
+    # no preconditioner
+    plain = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=CLEAF, precond=None,
+                                                                                   maxit=300)))
+    s2 = plain.mldivide(exc(cp, ENEI))
+    oplain = HR.BemRetIter(ocp, cleaf=CLEAF, precond=None, maxit=300)
+    os2 = oplain.solve(oexc)
+    e2 = {k: rel(getattr(s2, k), os2[k]) for k in ("sig1", "sig2", "h1", "h2")}
+    record("iter_fp64_noprecond", **e2, iter=plain.info["iter"], oracle_iter=oplain.iter)
+    assert plain.info["flag"] == 0 and abs(plain.info["iter"] - oplain.iter) <= 2
+    for k, e in e2.items():
+        assert e < 1e-6, (k, e)
+
+
+def test_iterative_solve_mixed_and_dipole(case):
+    from oracle import mnpbem_ref as R
+    cp, ocp, oit = case
+    exc = m.planewave([[1, 0, 0]], [[0, 0, 1]])
+    direct = m.bemsolver(cp, m.bemoptions(precision="fp64")).mldivide(exc(cp, ENEI))
+    # GMRES with the complex64 tensor-core inverses as preconditioner, to a
+    # tolerance near the FP64 solve of the same H-matrix operator
+    opts = m.bemiter_options(cleaf=CLEAF, tol=1e-10)
+    bem = m.bemsolver(cp, m.bemoptions(precision="mixed", iter=opts))
+    sig = bem.mldivide(exc(cp, ENEI))
+    it64 = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=opts)).mldivide(exc(cp, ENEI))
+    errs = {k: rel(getattr(sig, k), getattr(direct, k)) for k in ("sig1", "sig2", "h1", "h2")}
+    errs["ext"] = rel(sig.ext, direct.ext)
+    errs.update({"fp64iter_" + k: rel(getattr(sig, k), getattr(it64, k)) for k in ("sig1", "sig2", "h1", "h2")})
+    mixed_iter, mixed_flag = bem.info["iter"], bem.info["flag"]
+    # dipole potentials through the iterative solver
+    dip = m.dipoleret(cp, [[0, 0, 25.0]])
+    dexc = dip(cp, ENEI)
+    dsig = bem.mldivide(dexc)
+    ddir = m.bemsolver(cp, m.bemoptions(precision="fp64")).mldivide(dexc)
+    errs.update({"dip_" + k: rel(getattr(dsig, k), getattr(ddir, k)) for k in ("sig1", "sig2", "h1", "h2")})
+    record("iter_mixed", **errs, iter=mixed_iter, dip_iter=bem.info["iter"])
+    assert mixed_flag == 0 and bem.info["flag"] == 0
+    for k, e in errs.items():
+        assert e < (1e-8 if k.startswith("fp64iter") else 1e-5), (k, e)
