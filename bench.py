@@ -58,9 +58,12 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (default: workload)")
-    ap.add_argument("--workload", default="sphere4000", choices=["sphere4000", "batch3", "dimer24k"],
+    ap.add_argument("--workload", default="sphere4000", choices=["sphere4000", "batch3", "dimer24k", "iter24k"],
                     help="sphere4000: the headline sweep; batch3: three particles of uneven size, 128 "
-                         "wavelengths, two polarisations; dimer24k: two 12000-face spheres, 32 wavelengths")
+                         "wavelengths, two polarisations; dimer24k: two 12000-face spheres, 32 wavelengths; "
+                         "iter24k: the same dimer through the iterative H-matrix solver")
+    ap.add_argument("--iter-faces", type=int, default=24000,
+                    help="iter24k: total faces of the dimer (smaller sizes for profiling runs)")
     ap.add_argument("--fp64-faces", type=int, default=12000,
                     help="dimer24k: total faces of the FP64 timing sample (scaled by n^3 to 24000)")
     return ap.parse_args()
@@ -478,6 +481,74 @@ def run_dimer(a, torch):
             "refinement_final_residual_max": float(np.max(res["ir_resid"]))}
 
 
+def run_iter(a, torch):
+    """Iterative solver (bemretiter) on the dimer of run_dimer (--iter-faces,
+    default 24000 faces):
+    H-matrices of G1, H1, G2, H2 (leaves of at most 200 faces, htol 1e-6,
+    kmax 100), GMRES (tol 1e-6) preconditioned by the complex64 tensor-core
+    inverses; wavelengths 600 and 700 nm timed after a warm-up at 650 nm, then
+    a profiled repeat at 600 nm for the H-matrix phases.  The extinction is
+    compared with the direct mixed solve of the same handle."""
+    import mnpbem_gb300 as m
+    from mnpbem_gb300 import _lib, shapes
+    dev = torch.cuda.current_device()
+    nf = a.iter_faces // 2
+    v1, f1 = shapes.fibsphere(nf, 50.0, center=(-26.0, 0.0, 0.0))
+    v2, f2 = shapes.fibsphere(nf, 50.0, center=(26.0, 0.0, 0.0))
+    cp = m.comparticle([m.epsconst(1.77), drude(), drude()], [m.particle(v1, f1), m.particle(v2, f2)],
+                       [[2, 1], [3, 1]], 1, 2)
+    bem = m.bemsolver(cp, m.bemoptions(precision="mixed", device=dev, lanes=1,
+                                       iter=m.bemiter_options(cleaf=200, htol=1e-6, kmax=[4, 100])))
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    bem.mldivide(exc(cp, 650.0))
+    eneis = [600.0, 700.0]
+    infos, ext = [], []
+
+    def sweep():
+        for e in eneis:
+            sig = bem.mldivide(exc(cp, e))
+            infos.append(dict(bem.info))
+            ext.append(float(sig.ext[0]))
+    _, dt = _timed(sweep, torch)
+    lib = bem._lib
+    lib.mnpbem_profile_enable(bem.handle, 1)
+    lib.mnpbem_profile_reset(bem.handle)
+    bem.mldivide(exc(cp, 600.0))
+    lib.mnpbem_profile_enable(bem.handle, 0)
+    prof = read_profile(bem)
+    direct = bemret_spectrum(bem, exc, [600.0])
+    ext_direct = float(direct["ext"][0, 0])
+    hbm, _, src = peaks()
+    mv, hb = prof["hmat_matvec"], prof["hmat_build"]
+    gbs = mv["bytes"] / (mv["ms"] * 1e-3) / 1e9 if mv["ms"] > 0 else None
+    return {"metric": METRIC, "value": len(eneis) / dt, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (H-matrix operator) + c64(tf32) preconditioner", "data": "synthetic",
+            "config": {"workload": "iterative solver (bemretiter, H-matrices + GMRES) on the dimer of two d=50 nm "
+                                   "spheres, 2 nm gap, 2 x %d faces, x-pol along +z, 600 and 700 nm" % nf,
+                       "faces": 2 * nf, "cleaf": 200, "htol": 1e-6, "kmax": 100, "gmres_tol": 1e-6,
+                       "timing": "host wall clock around bemretiter.mldivide (public API, charges and ext/sca "
+                                 "to host)"},
+            "gmres_steps": [i["iter"] for i in infos], "relres": [i["relres"] for i in infos],
+            "true_relres": [i["true_relres"] for i in infos], "rank_max": infos[0]["rank_max"],
+            "rank_mean": infos[0]["rank_mean"], "compression": infos[0]["compression"],
+            "dense_fraction": bem.hpart.dense_fraction(), "low_rank_blocks": int(bem.hpart.low.shape[0]),
+            "full_blocks": int(bem.hpart.full.shape[0]),
+            "ext_rel_err_vs_direct": abs(ext[0] - ext_direct) / abs(ext_direct),
+            "phases_ms_600nm": {k: round(v["ms"], 3) for k, v in prof.items() if v["ms"] > 0},
+            "hmat_matvec": {"launches": mv["launches"], "ms": mv["ms"], "GB/s": gbs,
+                            "hbm_frac": gbs / hbm if gbs else None, "peak_source": src,
+                            "bytes_note": "stored FP64 entries of the four H-matrices (full blocks + used "
+                                          "factor columns) + vectors, per product"},
+            "hmat_build_ms": hb["ms"]}
+
+
+def bemret_spectrum(bem, exc, eneis):
+    """Direct (bemret) sweep on a bemretiter's handle."""
+    import mnpbem_gb300 as m
+    return m.bemret.spectrum(bem, exc, eneis)
+
+
 # ---------------------------------------------------------- CPU / reference
 def cpu_problem(faces):
     from mnpbem_gb300 import shapes
@@ -564,7 +635,7 @@ def main():
     import torch
     if a.workload != "sphere4000":
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        line = run_batch3(a, torch) if a.workload == "batch3" else run_dimer(a, torch)
+        line = {"batch3": run_batch3, "dimer24k": run_dimer, "iter24k": run_iter}[a.workload](a, torch)
         if rank == 0:
             print(json.dumps(line))
         return

@@ -1995,7 +1995,7 @@ namespace {
 
 // index arrays, values and factors of the H-matrices of one cluster tree
 struct HmatHost {
-  DevBuf idx, vals, fac, used, tbuf;
+  DevBuf idx, vals, fac, used, tbuf, xsbuf;
   HmatDev d;
   LeafAsm la;
   std::vector<int4> lblk;   // host copy of the low-rank blocks
@@ -2142,14 +2142,17 @@ mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax,
   MNP_TRY(H.vals.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, nvals)));
   MNP_TRY(H.fac.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, asz + bsz)));
   MNP_TRY(H.used.ensure(4 * std::max<int64_t>(1, usz)));
-  MNP_TRY(H.tbuf.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, tsz)));
+  MNP_TRY(H.tbuf.ensure(sizeof(float4) * 4 * std::max<int64_t>(1, tsz)));
+  MNP_TRY(H.xsbuf.ensure(sizeof(float4) * 2 * (size_t)n * HMV_NMAX));
   for (int q = 0; q < 4; ++q) {
     H.la.val[q] = H.d.val[q] = H.vals.as<double2>() + q * nvals;
     H.d.A[q] = H.fac.as<double2>() + q * (asz + bsz);
     H.d.B[q] = H.d.A[q] + asz;
   }
   H.d.used = H.used.as<unsigned char>();
-  H.d.T = H.tbuf.as<double2>();
+  H.d.T = H.tbuf.as<float4>();
+  H.d.xs = H.xsbuf.as<float4>();
+  H.d.nvals = nvals;
   H.d.n = n; H.d.nfull = nf; H.d.nlow = nlow; H.d.nleaf = nleaf;
   H.d.tol = htol;
   H.d.usz = usz; H.d.tsz = tsz;
@@ -2165,6 +2168,7 @@ mnpbem_status hmat_fill(mnpbem_geom* G, Lane& L, HmatHost& H, int N) {
   AsmParams p = base_params(G, L.lp_dev.as<LamParams>());
   MNP_TRY(assemble_leaves(p, H.la, L.st));
   MNP_TRY(hmat_aca(p, H.d, L.st));
+  MNP_TRY(hmat_split(H.d, L.st));
   H.ranks.assign((size_t)4 * H.d.nlow, 0);
   if (!H.ranks.empty())
     MNP_CUDA(cudaMemcpyAsync(H.ranks.data(), H.d.rank, sizeof(int) * H.ranks.size(), cudaMemcpyDeviceToHost, L.st));

@@ -11,6 +11,7 @@
 #include <cooperative_groups.h>
 
 #include "dense.cuh"
+#include "ds_math.cuh"
 #include "mbarrier.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
@@ -220,31 +221,6 @@ __global__ void __launch_bounds__(32 * THIN_WARPS) k_gemm_thin_c64(int64_t M, in
 }
 
 // ------------------------------------------- double-single thin GEMM (N <= 16)
-// Error-free transformations (Dekker / Knuth): the product a*b = p + e exactly
-// with p = fl(a*b), e = fma(a, b, -p); the sum s + p = t + err exactly with
-// TwoSum.  Each accumulator is a pair (hi, lo) of floats.
-struct DS { float hi, lo; };
-
-__device__ __forceinline__ void ds_acc_prod(DS& s, float a, float b) {
-  const float p = a * b;
-  const float e = fmaf(a, b, -p);
-  const float t = s.hi + p;
-  const float bp = t - s.hi;
-  const float err = (s.hi - (t - bp)) + (p - bp);
-  s.hi = t;
-  s.lo += err + e;
-}
-__device__ __forceinline__ DS ds_add(DS a, DS b) {
-  const float t = a.hi + b.hi;
-  const float bp = t - a.hi;
-  const float err = (a.hi - (t - bp)) + (b.hi - bp);
-  const float lo = a.lo + b.lo + err;
-  DS r;
-  r.hi = t + lo;                 // renormalise (FastTwoSum)
-  r.lo = lo - (r.hi - t);
-  return r;
-}
-
 constexpr int DS_WARPS = 8, DS_TR = 4;
 
 // B (complex128) -> hi / lo complex64 planes

@@ -8,7 +8,11 @@
 //             per row, summing the full blocks of the leaf and the rows of the
 //             low-rank blocks that cover it (no atomics: every row is written
 //             once, in a fixed order)
+// The products run in double-single arithmetic on (hi, lo) float splits of
+// the values, factors and vectors: FP64 runs at a small fraction of the FP32
+// rate on this GPU, and each complex entry feeds 4 N multiply-adds.
 #include "hmat.cuh"
+#include "ds_math.cuh"
 #include "profile.cuh"
 
 namespace mnpbem {
@@ -161,40 +165,47 @@ __global__ void __launch_bounds__(ACA_T) k_aca(AsmParams p, HmatDev h) {
 }
 
 template <int N>
-__device__ __forceinline__ void warp_sum_cols(double2 (&acc)[N]) {
+__device__ __forceinline__ void warp_sum_ds(DS (&re)[N], DS (&im)[N]) {
 #pragma unroll
   for (int c = 0; c < N; ++c)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
-      acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
+      const DS a{__shfl_xor_sync(0xffffffffu, re[c].hi, o), __shfl_xor_sync(0xffffffffu, re[c].lo, o)};
+      const DS b{__shfl_xor_sync(0xffffffffu, im[c].hi, o), __shfl_xor_sync(0xffffffffu, im[c].lo, o)};
+      re[c] = ds_add(re[c], a);
+      im[c] = ds_add(im[c], b);
     }
 }
 
+__device__ __forceinline__ float2 f4hi(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 f4lo(float4 v) { return make_float2(v.z, v.w); }
+
 template <int N>
-__global__ void __launch_bounds__(256) k_hmv_t(HmatDev h, const double2* __restrict__ x1,
-                                               const double2* __restrict__ x2) {
+__global__ void __launch_bounds__(256) k_hmv_t(HmatDev h) {
   const int b = blockIdx.x, q = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int4 blk = h.lblk[b];
   const int rank = h.rank[q * h.nlow + b];
-  const double2* B = h.B[q] + h.boff[b];
-  const double2* x = q < 2 ? x1 : x2;
-  double2* T = h.T + (int64_t)q * h.tsz + h.toff[b];
+  const float4* B = reinterpret_cast<const float4*>(h.B[q] + h.boff[b]);
+  const float4* x = h.xs + (q < 2 ? 0 : (int64_t)h.n * N);
+  float4* T = h.T + (int64_t)q * h.tsz + h.toff[b];
   for (int kk = warp; kk < rank; kk += 8) {
-    double2 acc[N];
+    DS re[N], im[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) acc[c] = make_double2(0.0, 0.0);
+    for (int c = 0; c < N; ++c) re[c] = im[c] = DS{0.f, 0.f};
     for (int j = lane; j < blk.w; j += 32) {
-      const double2 bv = B[(int64_t)kk * blk.w + j];
-      const double2* xr = x + (int64_t)h.perm[blk.z + j] * N;
+      const float4 bv = B[(int64_t)kk * blk.w + j];
+      const float4* xr = x + (int64_t)h.perm[blk.z + j] * N;
 #pragma unroll
-      for (int c = 0; c < N; ++c) cfma(acc[c], bv, xr[c]);
+      for (int c = 0; c < N; ++c) {
+        const float4 xv = xr[c];
+        ds_cfma(re[c], im[c], f4hi(bv), f4lo(bv), f4hi(xv), f4lo(xv));
+      }
     }
-    warp_sum_cols<N>(acc);
+    warp_sum_ds<N>(re, im);
     if (lane == 0)
 #pragma unroll
-      for (int c = 0; c < N; ++c) T[kk * N + c] = acc[c];
+      for (int c = 0; c < N; ++c) T[kk * N + c] = make_float4(re[c].hi, im[c].hi, re[c].lo, im[c].lo);
   }
 }
 
@@ -202,49 +213,57 @@ struct YPtrs {
   double2* y[4];
 };
 
+// rs CTAs share the rows of a leaf (grid.x = nleaf * rs) so that small trees
+// still fill the SMs
 template <int N>
-__global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, const double2* __restrict__ x1,
-                                                  const double2* __restrict__ x2, YPtrs ys) {
-  const int l = blockIdx.x, q = blockIdx.y;
+__global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, YPtrs ys, int rs) {
+  const int l = blockIdx.x / rs, part = blockIdx.x - l * rs, q = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int2 lf = h.leaf[l];
-  const double2* x = q < 2 ? x1 : x2;
+  const float4* x = h.xs + (q < 2 ? 0 : (int64_t)h.n * N);
   double2* y = ys.y[q];
   const int e0 = h.lptr[l], e1 = h.lptr[l + 1];
-  for (int rr = warp; rr < lf.y; rr += 8) {
+  for (int rr = part * 8 + warp; rr < lf.y; rr += 8 * rs) {
     const int i = lf.x + rr;
-    double2 acc[N];
+    DS re[N], im[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) acc[c] = make_double2(0.0, 0.0);
+    for (int c = 0; c < N; ++c) re[c] = im[c] = DS{0.f, 0.f};
     for (int e = e0; e < e1; ++e) {
       const int ent = h.lent[e];
       if (ent >= 0) {
         const int4 fb = h.fblk[ent];
-        const double2* V = h.val[q] + h.foff[ent] + (int64_t)(i - fb.x) * fb.w;
+        const float4* V = reinterpret_cast<const float4*>(h.val[q] + h.foff[ent]) + (int64_t)(i - fb.x) * fb.w;
         for (int j = lane; j < fb.w; j += 32) {
-          const double2 v = V[j];
-          const double2* xr = x + (int64_t)h.perm[fb.z + j] * N;
+          const float4 v = V[j];
+          const float4* xr = x + (int64_t)h.perm[fb.z + j] * N;
 #pragma unroll
-          for (int c = 0; c < N; ++c) cfma(acc[c], v, xr[c]);
+          for (int c = 0; c < N; ++c) {
+            const float4 xv = xr[c];
+            ds_cfma(re[c], im[c], f4hi(v), f4lo(v), f4hi(xv), f4lo(xv));
+          }
         }
       } else {
         const int b = ~ent;
         const int4 lb = h.lblk[b];
         const int rank = h.rank[q * h.nlow + b];
-        const double2* A = h.A[q] + h.aoff[b] + (i - lb.x);
-        const double2* T = h.T + (int64_t)q * h.tsz + h.toff[b];
+        const float4* A = reinterpret_cast<const float4*>(h.A[q] + h.aoff[b]) + (i - lb.x);
+        const float4* T = h.T + (int64_t)q * h.tsz + h.toff[b];
         for (int kk = lane; kk < rank; kk += 32) {
-          const double2 a = A[(int64_t)kk * lb.y];
+          const float4 a = A[(int64_t)kk * lb.y];
 #pragma unroll
-          for (int c = 0; c < N; ++c) cfma(acc[c], a, T[kk * N + c]);
+          for (int c = 0; c < N; ++c) {
+            const float4 tv = T[kk * N + c];
+            ds_cfma(re[c], im[c], f4hi(a), f4lo(a), f4hi(tv), f4lo(tv));
+          }
         }
       }
     }
-    warp_sum_cols<N>(acc);
+    warp_sum_ds<N>(re, im);
     if (lane == 0) {
       double2* yr = y + (int64_t)h.perm[i] * N;
 #pragma unroll
-      for (int c = 0; c < N; ++c) yr[c] = acc[c];
+      for (int c = 0; c < N; ++c)
+        yr[c] = make_double2((double)re[c].hi + (double)re[c].lo, (double)im[c].hi + (double)im[c].lo);
     }
   }
 }
@@ -254,23 +273,54 @@ __global__ void k_hmat_full(HmatDev h, int q, double2* out) {
   const int64_t n = h.n;
   if (b < h.nfull) {
     const int4 fb = h.fblk[b];
-    const double2* V = h.val[q] + h.foff[b];
+    const float4* V = reinterpret_cast<const float4*>(h.val[q] + h.foff[b]);
     for (int64_t e = threadIdx.x; e < (int64_t)fb.y * fb.w; e += blockDim.x) {
       const int r = (int)(e / fb.w), c = (int)(e - (int64_t)r * fb.w);
-      out[(int64_t)h.perm[fb.x + r] * n + h.perm[fb.z + c]] = V[e];
+      out[(int64_t)h.perm[fb.x + r] * n + h.perm[fb.z + c]] = join4(V[e]);
     }
     return;
   }
   const int lb = b - h.nfull;
   const int4 blk = h.lblk[lb];
   const int rank = h.rank[q * h.nlow + lb];
-  const double2* A = h.A[q] + h.aoff[lb];
-  const double2* B = h.B[q] + h.boff[lb];
+  const float4* A = reinterpret_cast<const float4*>(h.A[q] + h.aoff[lb]);
+  const float4* B = reinterpret_cast<const float4*>(h.B[q] + h.boff[lb]);
   for (int64_t e = threadIdx.x; e < (int64_t)blk.y * blk.w; e += blockDim.x) {
     const int r = (int)(e / blk.w), c = (int)(e - (int64_t)r * blk.w);
     double2 s = make_double2(0.0, 0.0);
-    for (int k = 0; k < rank; ++k) cfma(s, A[(int64_t)k * blk.y + r], B[(int64_t)k * blk.w + c]);
+    for (int k = 0; k < rank; ++k) cfma(s, join4(A[(int64_t)k * blk.y + r]), join4(B[(int64_t)k * blk.w + c]));
     out[(int64_t)h.perm[blk.x + r] * n + h.perm[blk.z + c]] = s;
+  }
+}
+
+// complex128 -> float4 (hi, lo) in place
+__device__ __forceinline__ void split_in_place(double2* p, int64_t i) {
+  const double2 v = p[i];
+  reinterpret_cast<float4*>(p)[i] = split4(v);
+}
+
+__global__ void k_split_vals(double2* v0, double2* v1, double2* v2, double2* v3, int64_t count) {
+  double2* v[4] = {v0, v1, v2, v3};
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 4 * count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    split_in_place(v[e / count], e % count);
+}
+
+__global__ void k_split_factors(HmatDev h) {
+  const int b = blockIdx.x, q = blockIdx.y;
+  const int4 blk = h.lblk[b];
+  const int rank = h.rank[q * h.nlow + b];
+  double2* A = h.A[q] + h.aoff[b];
+  double2* B = h.B[q] + h.boff[b];
+  for (int64_t e = threadIdx.x; e < (int64_t)rank * blk.y; e += blockDim.x) split_in_place(A, e);
+  for (int64_t e = threadIdx.x; e < (int64_t)rank * blk.w; e += blockDim.x) split_in_place(B, e);
+}
+
+__global__ void k_split_x(const double2* __restrict__ x1, const double2* __restrict__ x2, int64_t count,
+                          float4* xs) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    xs[e] = split4(x1[e]);
+    xs[count + e] = split4(x2[e]);
   }
 }
 
@@ -357,20 +407,35 @@ mnpbem_status hmat_aca(const AsmParams& p, const HmatDev& h, cudaStream_t st) {
   return MNPBEM_OK;
 }
 
+mnpbem_status hmat_split(const HmatDev& h, cudaStream_t st) {
+  ProfScope ps(PH_HMAT_BUILD, st, 0.0, 0.0, h.nlow > 0 ? 2 : 1);
+  if (h.nvals > 0)
+    k_split_vals<<<(unsigned)std::min<int64_t>(cdiv_up(4 * h.nvals, 256), 8192), 256, 0, st>>>(
+        h.val[0], h.val[1], h.val[2], h.val[3], h.nvals);
+  if (h.nlow > 0) k_split_factors<<<dim3((unsigned)h.nlow, 4), 256, 0, st>>>(h);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 mnpbem_status hmat_mv(const HmatDev& h, int N, const double2* x1, const double2* x2, double2* const* y,
                       double bytes, cudaStream_t st) {
+  if (N != 4 && N != 8 && N != 12 && N != 16) {
+    set_error("hmat_mv: %d columns (4, 8, 12 or 16 supported)", N);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
   YPtrs ys{{y[0], y[1], y[2], y[3]}};
-  ProfScope ps(PH_HMAT_MV, st, 0.0, bytes, h.nlow > 0 ? 2 : 1);
-#define HMV_CASE(NN)                                                                        \
-  case NN:                                                                                  \
-    if (h.nlow > 0) k_hmv_t<NN><<<dim3((unsigned)h.nlow, 4), 256, 0, st>>>(h, x1, x2);      \
-    k_hmv_leaf<NN><<<dim3((unsigned)h.nleaf, 4), 256, 0, st>>>(h, x1, x2, ys);              \
+  ProfScope ps(PH_HMAT_MV, st, 0.0, bytes, h.nlow > 0 ? 3 : 2);
+  const int64_t cnt = (int64_t)h.n * N;
+  // CTAs per leaf: at least two waves of CTAs over the SMs, at least 8 rows per CTA
+  const int rs = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv_up(2 * 152, 4 * (int64_t)h.nleaf), 4));
+  k_split_x<<<(unsigned)std::min<int64_t>(cdiv_up(cnt, 256), 4096), 256, 0, st>>>(x1, x2, cnt, h.xs);
+#define HMV_CASE(NN)                                                                  \
+  case NN:                                                                            \
+    if (h.nlow > 0) k_hmv_t<NN><<<dim3((unsigned)h.nlow, 4), 256, 0, st>>>(h);        \
+    k_hmv_leaf<NN><<<dim3((unsigned)(h.nleaf * rs), 4), 256, 0, st>>>(h, ys, rs);    \
     break;
   switch (N) {
     HMV_CASE(4) HMV_CASE(8) HMV_CASE(12) HMV_CASE(16)
-    default:
-      set_error("hmat_mv: %d columns (4, 8, 12 or 16 supported)", N);
-      return MNPBEM_ERR_INVALID_ARG;
   }
 #undef HMV_CASE
   MNP_CHECK_LAUNCH();

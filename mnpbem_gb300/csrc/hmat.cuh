@@ -25,7 +25,11 @@ struct HmatDev {
   const int64_t* uoff = nullptr;     // [nlow] offsets of the ACA row flags
   const int64_t* toff = nullptr;     // [nlow] offsets of the products R^T x [kcap][HMV_NMAX]
   int64_t usz = 0, tsz = 0;          // per-matrix sizes of the row flags and products
+  int64_t nvals = 0;                 // entries of the full blocks (per matrix)
   int* rank = nullptr;               // [4][nlow] ranks found by ACA
+  // values and factors: complex128 while assembled / compressed, then split
+  // in place into (hi, lo) float pairs, float4 (hi.re, hi.im, lo.re, lo.im),
+  // for the double-single products
   double2* val[4] = {};              // full block values
   double2* A[4] = {};                // left factors, column k of block b at A + aoff + k rows
   double2* B[4] = {};                // right factors
@@ -33,13 +37,17 @@ struct HmatDev {
   const int2* leaf = nullptr;        // [nleaf] (first row, rows) of the leaf clusters
   const int* lptr = nullptr;         // [nleaf + 1] CSR of the blocks that cover each leaf's rows
   const int* lent = nullptr;         // b >= 0: full block b; ~b: low-rank block b
-  double2* T = nullptr;              // [4][tsz] products R^T x of the low-rank blocks
+  float4* T = nullptr;               // [4][tsz] products R^T x of the low-rank blocks (hi / lo)
+  float4* xs = nullptr;              // [2][n * HMV_NMAX] hi / lo split of the product's x1, x2
 };
 
 // low-rank blocks of the four matrices by ACA (mex/hlib/aca.cpp restated,
 // kernel of mex/acagreen/acagreen.cpp greenret::getrow / getcol)
 mnpbem_status hmat_aca(const AsmParams& p, const HmatDev& h, cudaStream_t st);
-// y[q] = H_q x (x = x1 for q = 0, 1; x2 for q = 2, 3); x, y [n][N] in face order, N <= 16
+// values and used factor columns -> (hi, lo) float4 in place (after hmat_aca)
+mnpbem_status hmat_split(const HmatDev& h, cudaStream_t st);
+// y[q] = H_q x (x = x1 for q = 0, 1; x2 for q = 2, 3); x, y [n][N] in face order, N <= 16;
+// double-single arithmetic on the split values (FP32 pipe, ~1e-14 relative)
 // bytes: algorithmic bytes of the product (for the profiler)
 mnpbem_status hmat_mv(const HmatDev& h, int N, const double2* x1, const double2* x2, double2* const* y,
                       double bytes, cudaStream_t st);

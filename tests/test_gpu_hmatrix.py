@@ -122,3 +122,33 @@ def test_iterative_solve_mixed_and_dipole(case):
     assert mixed_flag == 0 and bem.info["flag"] == 0
     for k, e in errs.items():
         assert e < (1e-8 if k.startswith("fp64iter") else 1e-5), (k, e)
+
+
+def test_iterative_solve_dimer_fp64(gpu_lib):
+    # two particles with separate inside media: cross-particle blocks of G1 / G2
+    # vanish (ACA stops on the zero row), G2 couples them through the outside
+    from oracle import hmatrix_ref as HR
+    from oracle import mnpbem_ref as R
+    t = shapes.tables()
+    q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    v1, f1 = shapes.trisphere(256, 20.0)
+    v2 = v1 + np.array([24.0, 0.0, 0.0])
+    ocp = R.ComParticle([R.EpsConst(1.77), R.drude_eps(), R.EpsConst(-6 + 0.5j)],
+                        [R.Particle(v1, f1, q), R.Particle(v2, f1, q)], [[2, 1], [3, 1]], [True, True])
+    cp = m.comparticle([m.epsconst(1.77), drude(), m.epsconst(-6 + 0.5j)],
+                       [m.particle(v1, f1), m.particle(v2, f1)], [[2, 1], [3, 1]], 1, 2)
+    pw = R.PlaneWaveRet([[1, 0, 0]], [[0, 0, 1]], None)
+    oexc = pw.potential(ocp, ENEI)
+    oit = HR.BemRetIter(ocp, cleaf=24)
+    osig = oit.solve(oexc)
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=24)))
+    assert np.array_equal(bem.hpart.low, np.asarray(oit.H[0].low))
+    sig = bem.mldivide(m.planewave([[1, 0, 0]], [[0, 0, 1]])(cp, ENEI))
+    errs = {k: rel(getattr(sig, k), osig[k]) for k in ("sig1", "sig2", "h1", "h2")}
+    F, ranks = bem.hmat_full(ENEI, "G2")
+    errs["G2_oracle"] = rel(F, oit.H[2].full_matrix())
+    record("iter_dimer_fp64", **errs, iter=bem.info["iter"], oracle_iter=oit.iter,
+           rank_match=float(np.mean(ranks == np.array([H.ranks() for H in oit.H]))))
+    assert bem.info["flag"] == 0 and bem.info["iter"] == oit.iter
+    for k, e in errs.items():
+        assert e < 1e-8, (k, e)
