@@ -544,7 +544,8 @@ def run_iter(a, torch):
 
 
 def bemret_spectrum(bem, exc, eneis):
-    """Direct (bemret) sweep on a bemretiter's handle."""
+    """Direct (bemret) sweep on a bemretiter's handle (the parent class's
+    spectrum runs mnpbem_solve)."""
     import mnpbem_gb300 as m
     return m.bemret.spectrum(bem, exc, eneis)
 

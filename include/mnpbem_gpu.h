@@ -389,7 +389,9 @@ typedef struct mnpbem_iter_info {
  * @bemiter/solve.m): H-matrices of G1, H1, G2, H2 (full blocks of the
  * complete Green function on leaf pairs, low-rank blocks by ACA of the far
  * field kernel, Greenfun/+aca/@compgreenret/eval.m), the operator of
- * afun.m with H-matrix products in FP64, GMRES preconditioned by mfun.m.
+ * afun.m with H-matrix products (entries assembled and compressed in FP64,
+ * products in double-single FP32 arithmetic, ~1e-14 relative), GMRES
+ * preconditioned by mfun.m.
  * Excitation: the plane wave exc (ext / sca filled when exc->ninf > 0 for
  * sca), or the potentials pot when pot is not NULL (exc ignored).  One
  * wavelength; out as mnpbem_solve (ir_iters: GMRES steps, ir_resid: true

@@ -703,6 +703,21 @@ class bemretiter(bemret):
 
     solve = mldivide
 
+    def spectrum(self, exc, enei, fields=False, out=None):
+        """Wavelength sweep through the iterative solver (one mnpbem_solve_iter
+        call per wavelength): dict with ext, sca [nenei, npol], GMRES steps
+        ``ir_iters`` and true relative residuals ``ir_resid`` [nenei] (+ sig1,
+        sig2, h1, h2 with ``fields``).  ``out`` is not used."""
+        eneis = np.atleast_1d(np.asarray(enei, dtype=np.float64))
+        sigs = [self.mldivide(exc(self.p, float(e))) for e in eneis]
+        res = {"ext": np.array([s.ext for s in sigs]), "sca": np.array([s.sca for s in sigs]),
+               "ir_iters": np.array([s.iter for s in sigs], dtype=np.int32),
+               "ir_resid": np.array([s.relres for s in sigs])}
+        if fields:
+            for k in ("sig1", "sig2", "h1", "h2"):
+                res[k] = np.array([getattr(s, k) for s in sigs])
+        return res
+
 
 def bemsolver(p, op=None, **kw):
     """Factory of Base/bemsolver.m: picks the solver class whose needs match op

@@ -1995,7 +1995,7 @@ namespace {
 
 // index arrays, values and factors of the H-matrices of one cluster tree
 struct HmatHost {
-  DevBuf idx, vals, fac, used, tbuf, xsbuf;
+  DevBuf idx, vals, fac, fact, used, tbuf, xsbuf;
   HmatDev d;
   LeafAsm la;
   std::vector<int4> lblk;   // host copy of the low-rank blocks
@@ -2141,6 +2141,7 @@ mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax,
   // values, factors, scratch
   MNP_TRY(H.vals.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, nvals)));
   MNP_TRY(H.fac.ensure(sizeof(double2) * 4 * std::max<int64_t>(1, asz + bsz)));
+  MNP_TRY(H.fact.ensure(sizeof(float4) * 4 * std::max<int64_t>(1, asz)));
   MNP_TRY(H.used.ensure(4 * std::max<int64_t>(1, usz)));
   MNP_TRY(H.tbuf.ensure(sizeof(float4) * 4 * std::max<int64_t>(1, tsz)));
   MNP_TRY(H.xsbuf.ensure(sizeof(float4) * 2 * (size_t)n * HMV_NMAX));
@@ -2148,6 +2149,7 @@ mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax,
     H.la.val[q] = H.d.val[q] = H.vals.as<double2>() + q * nvals;
     H.d.A[q] = H.fac.as<double2>() + q * (asz + bsz);
     H.d.B[q] = H.d.A[q] + asz;
+    H.d.At[q] = H.fact.as<float4>() + q * asz;
   }
   H.d.used = H.used.as<unsigned char>();
   H.d.T = H.tbuf.as<float4>();

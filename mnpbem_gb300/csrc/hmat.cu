@@ -132,6 +132,8 @@ __global__ void __launch_bounds__(ACA_T) k_aca(AsmParams p, HmatDev h) {
     const int cp = rr.idx;
     if (cp < 0 || cp >= nb) { rank = k; break; }     // no finite pivot
     const double2 piv = B[(int64_t)k * nb + cp];
+    // every thread holds the pivot before its owner rescales that entry
+    __syncthreads();
     if (piv.x == 0.0 && piv.y == 0.0) { rank = k; break; }
     const double2 sc = cdiv(make_double2(1.0, 0.0), piv);
     Red v1{0.0, 0.0, -1.0, INT_MAX};
@@ -233,6 +235,7 @@ __global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, YPtrs ys, int rs) {
       if (ent >= 0) {
         const int4 fb = h.fblk[ent];
         const float4* V = reinterpret_cast<const float4*>(h.val[q] + h.foff[ent]) + (int64_t)(i - fb.x) * fb.w;
+#pragma unroll 2
         for (int j = lane; j < fb.w; j += 32) {
           const float4 v = V[j];
           const float4* xr = x + (int64_t)h.perm[fb.z + j] * N;
@@ -246,10 +249,10 @@ __global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, YPtrs ys, int rs) {
         const int b = ~ent;
         const int4 lb = h.lblk[b];
         const int rank = h.rank[q * h.nlow + b];
-        const float4* A = reinterpret_cast<const float4*>(h.A[q] + h.aoff[b]) + (i - lb.x);
+        const float4* A = h.At[q] + h.aoff[b] + (int64_t)(i - lb.x) * h.kcap[b];
         const float4* T = h.T + (int64_t)q * h.tsz + h.toff[b];
         for (int kk = lane; kk < rank; kk += 32) {
-          const float4 a = A[(int64_t)kk * lb.y];
+          const float4 a = A[kk];
 #pragma unroll
           for (int c = 0; c < N; ++c) {
             const float4 tv = T[kk * N + c];
@@ -283,12 +286,12 @@ __global__ void k_hmat_full(HmatDev h, int q, double2* out) {
   const int lb = b - h.nfull;
   const int4 blk = h.lblk[lb];
   const int rank = h.rank[q * h.nlow + lb];
-  const float4* A = reinterpret_cast<const float4*>(h.A[q] + h.aoff[lb]);
+  const double2* A = h.A[q] + h.aoff[lb];
   const float4* B = reinterpret_cast<const float4*>(h.B[q] + h.boff[lb]);
   for (int64_t e = threadIdx.x; e < (int64_t)blk.y * blk.w; e += blockDim.x) {
     const int r = (int)(e / blk.w), c = (int)(e - (int64_t)r * blk.w);
     double2 s = make_double2(0.0, 0.0);
-    for (int k = 0; k < rank; ++k) cfma(s, join4(A[(int64_t)k * blk.y + r]), join4(B[(int64_t)k * blk.w + c]));
+    for (int k = 0; k < rank; ++k) cfma(s, A[(int64_t)k * blk.y + r], join4(B[(int64_t)k * blk.w + c]));
     out[(int64_t)h.perm[blk.x + r] * n + h.perm[blk.z + c]] = s;
   }
 }
@@ -310,9 +313,14 @@ __global__ void k_split_factors(HmatDev h) {
   const int b = blockIdx.x, q = blockIdx.y;
   const int4 blk = h.lblk[b];
   const int rank = h.rank[q * h.nlow + b];
-  double2* A = h.A[q] + h.aoff[b];
+  const double2* A = h.A[q] + h.aoff[b];
+  float4* At = h.At[q] + h.aoff[b];
+  const int kc = h.kcap[b];
   double2* B = h.B[q] + h.boff[b];
-  for (int64_t e = threadIdx.x; e < (int64_t)rank * blk.y; e += blockDim.x) split_in_place(A, e);
+  for (int64_t e = threadIdx.x; e < (int64_t)rank * blk.y; e += blockDim.x) {
+    const int64_t k = e / blk.y, i = e - k * blk.y;
+    At[i * kc + k] = split4(A[e]);
+  }
   for (int64_t e = threadIdx.x; e < (int64_t)rank * blk.w; e += blockDim.x) split_in_place(B, e);
 }
 

@@ -31,8 +31,9 @@ struct HmatDev {
   // in place into (hi, lo) float pairs, float4 (hi.re, hi.im, lo.re, lo.im),
   // for the double-single products
   double2* val[4] = {};              // full block values
-  double2* A[4] = {};                // left factors, column k of block b at A + aoff + k rows
-  double2* B[4] = {};                // right factors
+  double2* A[4] = {};                // left factors, column k of block b at A + aoff + k rows (FP64)
+  double2* B[4] = {};                // right factors (split in place)
+  float4* At[4] = {};                // left factors split, row-major [rows][kcap] at At + aoff
   unsigned char* used = nullptr;     // [4][usz] ACA row flags
   const int2* leaf = nullptr;        // [nleaf] (first row, rows) of the leaf clusters
   const int* lptr = nullptr;         // [nleaf + 1] CSR of the blocks that cover each leaf's rows
@@ -44,7 +45,8 @@ struct HmatDev {
 // low-rank blocks of the four matrices by ACA (mex/hlib/aca.cpp restated,
 // kernel of mex/acagreen/acagreen.cpp greenret::getrow / getcol)
 mnpbem_status hmat_aca(const AsmParams& p, const HmatDev& h, cudaStream_t st);
-// values and used factor columns -> (hi, lo) float4 in place (after hmat_aca)
+// values and right factors -> (hi, lo) float4 in place, left factors -> At
+// (row-major, split) (after hmat_aca)
 mnpbem_status hmat_split(const HmatDev& h, cudaStream_t st);
 // y[q] = H_q x (x = x1 for q = 0, 1; x2 for q = 2, 3); x, y [n][N] in face order, N <= 16;
 // double-single arithmetic on the split values (FP32 pipe, ~1e-14 relative)
