@@ -363,7 +363,13 @@ typedef struct mnpbem_cluster_tree {
  * brackets).  solver: 0 GMRES [0] (cgs / bicgstab are not built);
  * precond: 0 none, 1 'full' [1] (the dense inverses of bemret in the
  * solve's precision: FP64, or complex64 on the tensor cores for MIXED);
- * restart 0 = no restarts (one cycle of up to maxit steps).                 */
+ * restart 0 = no restarts (one cycle of up to maxit steps).
+ * reuse_precond 1 (not in the reference, which rebuilds the preconditioner
+ * at every wavelength): keep the 'full' preconditioner of an earlier
+ * iterative solve on this handle (same precision) for this wavelength; it
+ * changes the number of GMRES steps, not the solution (tol).  It is rebuilt
+ * when the previous solve needed more than refresh_steps steps
+ * (refresh_steps 0: never) and after any direct solve on the handle.       */
 typedef struct mnpbem_iter_options {
   int32_t solver;
   double tol;        /* [1e-6] on ||M (b - A x)|| / ||M b||  */
@@ -372,6 +378,8 @@ typedef struct mnpbem_iter_options {
   int32_t precond;   /* [1]   */
   double htol;       /* [1e-6] ACA tolerance */
   int32_t kmax;      /* [100] largest rank of a low-rank block (<= 512) */
+  int32_t reuse_precond;  /* [0] */
+  int32_t refresh_steps;  /* [0] */
 } mnpbem_iter_options;
 
 /* Statistics of one iterative solve. */
@@ -383,6 +391,7 @@ typedef struct mnpbem_iter_info {
   int32_t rank_max;      /* largest ACA rank over the four matrices */
   double rank_mean;
   double compression;    /* stored entries of the four H-matrices / 4 n^2 */
+  double precond_enei;   /* wavelength the preconditioner was built at (0: none) */
 } mnpbem_iter_info;
 
 /* sig = bem \ exc with the iterative solver (BEM/@bemretiter/solve.m:11-36,

@@ -65,13 +65,13 @@ class ClusterTree(ctypes.Structure):
 class IterOptions(ctypes.Structure):
     _fields_ = [("solver", ctypes.c_int32), ("tol", ctypes.c_double), ("maxit", ctypes.c_int32),
                 ("restart", ctypes.c_int32), ("precond", ctypes.c_int32), ("htol", ctypes.c_double),
-                ("kmax", ctypes.c_int32)]
+                ("kmax", ctypes.c_int32), ("reuse_precond", ctypes.c_int32), ("refresh_steps", ctypes.c_int32)]
 
 
 class IterInfo(ctypes.Structure):
     _fields_ = [("flag", ctypes.c_int32), ("iter", ctypes.c_int32), ("relres", ctypes.c_double),
                 ("true_relres", ctypes.c_double), ("rank_max", ctypes.c_int32), ("rank_mean", ctypes.c_double),
-                ("compression", ctypes.c_double)]
+                ("compression", ctypes.c_double), ("precond_enei", ctypes.c_double)]
 
 
 class Refine(ctypes.Structure):

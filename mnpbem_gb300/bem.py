@@ -594,7 +594,8 @@ def spectrum_batch(items, fields=False):
 def bemiter_options(**kw):
     """Options of the iterative solver (BEM/@bemiter/options.m:19-44)."""
     op = {"solver": "gmres", "tol": 1e-6, "maxit": 100, "restart": None, "precond": "full", "output": 0,
-          "cleaf": 200, "htol": 1e-6, "kmax": [4, 100], "eta": 2.5}
+          "cleaf": 200, "htol": 1e-6, "kmax": [4, 100], "eta": 2.5, "reuse_precond": False,
+          "refresh_steps": 0}
     op.update(kw)
     return op
 
@@ -609,7 +610,11 @@ class bemretiter(bemret):
     the operator of afun.m with H-matrix products, preconditioned by the dense
     inverses of bemret (``precond='full'``, in the solver's precision) or not
     at all (``precond=None``).  After a solve ``bem.info`` holds flag, iter,
-    relres, true_relres, rank_max, rank_mean and compression.
+    relres, true_relres, rank_max, rank_mean, compression and precond_enei.
+    ``reuse_precond=True`` (not in the reference) keeps the preconditioner of
+    an earlier wavelength (rebuilt when a solve needed more than
+    ``refresh_steps`` GMRES steps): a sweep then pays the dense inversion
+    once instead of at every wavelength, with the same solutions to ``tol``.
 
     Restrictions: solver 'gmres' only; the 'hmat' preconditioner (H-matrix LU
     of hmatlu / hmatsolve) is not built.
@@ -618,7 +623,8 @@ class bemretiter(bemret):
     def __init__(self, p, op=None):
         op = bemoptions(op)
         it = bemiter_options(**op.get("iter", {}))
-        for k in ("solver", "tol", "maxit", "restart", "precond", "cleaf", "htol", "kmax", "eta"):
+        for k in ("solver", "tol", "maxit", "restart", "precond", "cleaf", "htol", "kmax", "eta", "reuse_precond",
+                  "refresh_steps"):
             if k in op:
                 it[k] = op[k]
         if it["solver"] != "gmres":
@@ -631,8 +637,10 @@ class bemretiter(bemret):
         self.hpart = hpartition(p, it["cleaf"], it["eta"])
         self.info = None
 
-    def _opts(self):
-        it = self.iter_op
+    def _opts(self, reuse=None):
+        it = dict(self.iter_op)
+        if reuse is not None:
+            it["reuse_precond"] = reuse
         o = _lib.IterOptions()
         o.solver = 0
         o.tol = float(it["tol"])
@@ -641,6 +649,8 @@ class bemretiter(bemret):
         o.precond = 1 if it["precond"] == "full" else 0
         o.htol = float(np.min(it["htol"]))
         o.kmax = int(np.max(it["kmax"]))
+        o.reuse_precond = int(bool(it["reuse_precond"]))
+        o.refresh_steps = int(it["refresh_steps"] or 0)
         return o
 
     def hmat_full(self, enei, which):
@@ -657,12 +667,13 @@ class bemretiter(bemret):
             em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, q, out.ctypes.data, ranks.ctypes.data))
         return out, ranks[:, :self.hpart.low.shape[0]]
 
-    def mldivide(self, exc):
-        """sig = bem \\ exc(p, enei) with preconditioned GMRES (bemretiter/solve.m)."""
+    def mldivide(self, exc, reuse=None):
+        """sig = bem \\ exc(p, enei) with preconditioned GMRES (bemretiter/solve.m);
+        ``reuse`` overrides the ``reuse_precond`` option for this call."""
         enei = float(exc.enei)
         n = self.p.n
         em = np.ascontiguousarray(self._eps(enei)[0])
-        o = self._opts()
+        o = self._opts(reuse)
         info = _lib.IterInfo()
         keep = []
         if hasattr(exc, "exc"):
@@ -707,9 +718,15 @@ class bemretiter(bemret):
         """Wavelength sweep through the iterative solver (one mnpbem_solve_iter
         call per wavelength): dict with ext, sca [nenei, npol], GMRES steps
         ``ir_iters`` and true relative residuals ``ir_resid`` [nenei] (+ sig1,
-        sig2, h1, h2 with ``fields``).  ``out`` is not used."""
+        sig2, h1, h2 with ``fields``).  With ``reuse_precond`` the preconditioner
+        is built at the first wavelength and reused (rebuilt when a solve needed
+        more than ``refresh_steps`` steps).  ``out`` is not used."""
         eneis = np.atleast_1d(np.asarray(enei, dtype=np.float64))
-        sigs = [self.mldivide(exc(self.p, float(e))) for e in eneis]
+        # a sweep builds its preconditioner at its first wavelength
+        sigs, self.sweep_info = [], []
+        for i, e in enumerate(eneis):
+            sigs.append(self.mldivide(exc(self.p, float(e)), reuse=False if i == 0 else None))
+            self.sweep_info.append(dict(self.info))
         res = {"ext": np.array([s.ext for s in sigs]), "sca": np.array([s.sca for s in sigs]),
                "ir_iters": np.array([s.iter for s in sigs], dtype=np.int32),
                "ir_resid": np.array([s.relres for s in sigs])}

@@ -118,6 +118,15 @@ struct Lane {
   int last_kind = 0;         // stage of the last refinement step
   bool ds_done = false;      // a double-single residual has been computed for this wavelength
   double bnorm2 = 0.0;       // ||b||^2 of the excitation (from the last full residual)
+  // preconditioner of the iterative solver kept for later wavelengths: the
+  // dense chain matrices in mat[], the per-face data and parameters of the
+  // wavelength it was built at (cleared whenever mat[] is overwritten)
+  DevBuf pc_face, pc_lp;
+  bool pc_valid = false;
+  int pc_precision = -1;
+  double pc_enei = 0.0;
+  int pc_last_steps = 0;
+  const void* pc_mat0 = nullptr;
 };
 
 struct mnpbem_geom {
@@ -751,14 +760,14 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   return h;
 }
 
-FaceData face_data(mnpbem_geom* G, Lane& L) {
+FaceData face_data_in(mnpbem_geom* G, DevBuf& buf) {
   const int64_t n = G->g.n;
   FaceData f;
   f.n = n;
   f.pos = G->g.pos;
   f.nvec = G->g.nvec;
   f.area = G->g.area;
-  double2* e = L.facebuf.as<double2>();
+  double2* e = buf.as<double2>();
   f.eps1 = e;
   f.eps2 = e + n;
   float2* ef = reinterpret_cast<float2*>(e + 2 * n);
@@ -770,6 +779,7 @@ FaceData face_data(mnpbem_geom* G, Lane& L) {
   f.exc_out = f.exc_in + n;
   return f;
 }
+FaceData face_data(mnpbem_geom* G, Lane& L) { return face_data_in(G, L.facebuf); }
 
 mnpbem_status upload_masks(mnpbem_geom* G, Lane& L, const std::vector<unsigned char>& m) {
   unsigned char* dst = const_cast<unsigned char*>(face_data(G, L).exc_in);
@@ -818,6 +828,7 @@ void* tc_ctx(mnpbem_geom* G, Lane& L) { return G->tc_enabled ? (void*)&L.tc : nu
 // ---------------------------------------------------------------- S0
 mnpbem_status stage_assemble(mnpbem_geom* G, Lane& L, int precision) {
   const int64_t n = G->g.n, ld = G->ld;
+  L.pc_valid = false;   // mat[] is about to be overwritten
   const int* fm = G->face_med.as<int>();
   FaceData f = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();
@@ -903,9 +914,10 @@ Vec64 vec64(const mnpbem_geom* G, Lane& L, int P) {
   return v;
 }
 
-// complex64 chain applied to FP64 inputs, result in fx1/fx2
-mnpbem_status apply32(mnpbem_geom* G, Lane& L, int P, const double2* p_, const double2* a_,
-                      const double2* al_, const double2* De_) {
+// complex64 chain applied to FP64 inputs, result in fx1/fx2 (per-face data
+// and parameters fd / lp: those of the wavelength the matrices belong to)
+mnpbem_status apply32_at(mnpbem_geom* G, Lane& L, int P, const FaceData& fd, const LamParams* lp,
+                         const double2* p_, const double2* a_, const double2* al_, const double2* De_) {
   const int64_t n = G->g.n;
   cudaStream_t st = L.st;
   float2* W = L.vecw.as<float2>();
@@ -916,8 +928,12 @@ mnpbem_status apply32(mnpbem_geom* G, Lane& L, int P, const double2* p_, const d
   launch_cvt_d2f(al_, fal, 3 * n * P, st);
   launch_cvt_d2f(De_, fDe, n * P, st);
   MNP_CHECK_LAUNCH();
-  return apply_mldivide<float>(face_data(G, L), P, L.lp_dev.as<LamParams>(), chain_mats<float>(G, L), fphi, fa,
-                               fal, fDe, fx1, fx2, fwork, gemm_w<float>, tc_ctx(G, L), st);
+  return apply_mldivide<float>(fd, P, lp, chain_mats<float>(G, L), fphi, fa, fal, fDe, fx1, fx2, fwork,
+                               gemm_w<float>, tc_ctx(G, L), st);
+}
+mnpbem_status apply32(mnpbem_geom* G, Lane& L, int P, const double2* p_, const double2* a_,
+                      const double2* al_, const double2* De_) {
+  return apply32_at(G, L, P, face_data(G, L), L.lp_dev.as<LamParams>(), p_, a_, al_, De_);
 }
 float2* fx_ptr(const mnpbem_geom* G, Lane& L, int P, int which) {
   const int64_t n = G->g.n;
@@ -1574,6 +1590,8 @@ mnpbem_status job_finish(Job& j, bool failed) {
 mnpbem_status run_jobs(std::vector<Job>& jobs) {
   mnpbem_status st = MNPBEM_OK;
   for (Job& j : jobs)
+    for (auto& L : j.G->lanes) L->pc_valid = false;
+  for (Job& j : jobs)
     if (st == MNPBEM_OK) st = job_prepare(j);
   if (st == MNPBEM_OK) {
     std::vector<Job*> js;
@@ -2194,6 +2212,7 @@ void face_eps(mnpbem_geom* G, Lane& L) {
 struct IterOpts {
   double tol = 1e-6, htol = 1e-6;
   int maxit = 100, restart = 0, precond = 1, kmax = 100;
+  int reuse = 0, refresh = 0;
 };
 
 mnpbem_status iter_opts(const mnpbem_iter_options* op, IterOpts& o) {
@@ -2209,6 +2228,8 @@ mnpbem_status iter_opts(const mnpbem_iter_options* op, IterOpts& o) {
     else { set_error("iterative solver: precond must be 0 or 1"); return MNPBEM_ERR_INVALID_ARG; }
     if (op->htol > 0) o.htol = op->htol;
     if (op->kmax > 0) o.kmax = op->kmax;
+    o.reuse = op->reuse_precond != 0;
+    o.refresh = std::max(0, op->refresh_steps);
   }
   return MNPBEM_OK;
 }
@@ -2229,9 +2250,12 @@ struct Gmres {
   DevBuf V, part, hdev, zero, rvec;
   std::vector<double2> hpart;
   std::vector<double> npart;
+  FaceData fdp;                // per-face data of the preconditioner's wavelength
+  const LamParams* lpp;        // its parameters
 
   Gmres(mnpbem_geom* G_, Lane& L_, const SolveCtx& c_, HmatHost& H_, const IterOpts& o_)
-      : G(G_), L(L_), c(c_), H(H_), o(o_), n(G_->g.n), len(8 * G_->g.n * c_.P), P(c_.P) {}
+      : G(G_), L(L_), c(c_), H(H_), o(o_), n(G_->g.n), len(8 * G_->g.n * c_.P), P(c_.P),
+        fdp(face_data_in(G_, L_.pc_face)), lpp(L_.pc_lp.as<LamParams>()) {}
 
   // (rphi, ra, ral, rDe) = b - A x with b = (bphi, ba, bal, bDe); norms[0..1] += ||r||^2, ||b||^2
   mnpbem_status residual(const double2* x, const double2* bphi, const double2* ba, const double2* bal,
@@ -2250,10 +2274,10 @@ struct Gmres {
     if (!o.precond) {
       kv_pack_bx(n, P, phi, a, al, De, dst, L.st);
     } else if (c.precision == MNPBEM_FP64) {
-      MNP_TRY(apply_mldivide<double>(face_data(G, L), P, L.lp_dev.as<LamParams>(), chain_mats<double>(G, L), phi, a,
-                                     al, De, dst, dst + 4 * n * P, v.work, gemm_w<double>, nullptr, L.st));
+      MNP_TRY(apply_mldivide<double>(fdp, P, lpp, chain_mats<double>(G, L), phi, a, al, De, dst, dst + 4 * n * P,
+                                     v.work, gemm_w<double>, nullptr, L.st));
     } else {
-      MNP_TRY(apply32(G, L, P, phi, a, al, De));
+      MNP_TRY(apply32_at(G, L, P, fdp, lpp, phi, a, al, De));
       launch_cvt_f2d(fx_ptr(G, L, P, 0), dst, 4 * n * P, L.st);
       launch_cvt_f2d(fx_ptr(G, L, P, 1), dst + 4 * n * P, 4 * n * P, L.st);
     }
@@ -2413,12 +2437,26 @@ mnpbem_status iter_prepare(mnpbem_geom* G, Job& j, const double2* ext_pot, HmatH
   MNP_TRY(upload_lp(G, L, j.s, 0));
   L.w = 0;
   MNP_TRY(hmat_setup(G, tree, o.kmax, o.htol, H, L.st));
-  if (o.precond) {
+  const bool keep = o.precond && o.reuse && L.pc_valid && L.pc_precision == j.c.precision &&
+                    L.pc_mat0 == L.mat[0].ptr && !(o.refresh > 0 && L.pc_last_steps > o.refresh);
+  if (o.precond && !keep) {
     MNP_TRY(run_stage(G, L, j.c, 0, true));   // per-face eps + dense matrices
     MNP_TRY(run_stage(G, L, j.c, 1, true));   // dense inverses of bemret (initmat.m)
+    MNP_TRY(L.pc_face.ensure(L.facebuf.bytes));
+    MNP_TRY(L.pc_lp.ensure(sizeof(LamParams)));
+    MNP_CUDA(cudaMemcpyAsync(L.pc_face.ptr, L.facebuf.ptr, L.facebuf.bytes, cudaMemcpyDeviceToDevice, L.st));
+    MNP_CUDA(cudaMemcpyAsync(L.pc_lp.ptr, L.lp_dev.ptr, sizeof(LamParams), cudaMemcpyDeviceToDevice, L.st));
+    L.pc_valid = true;
+    L.pc_precision = j.c.precision;
+    L.pc_enei = j.s.enei[0];
+    L.pc_mat0 = L.mat[0].ptr;
   } else {
     face_eps(G, L);
     MNP_CHECK_LAUNCH();
+    if (!o.precond) {   // the preconditioner's per-face data are the current ones (unused)
+      MNP_TRY(L.pc_face.ensure(L.facebuf.bytes));
+      MNP_TRY(L.pc_lp.ensure(sizeof(LamParams)));
+    }
   }
   const int P = j.c.P;
   MNP_TRY(hmat_fill(G, L, H, 4 * P));
@@ -2498,6 +2536,7 @@ mnpbem_status mnpbem_solve_iter(mnpbem_geom* G, const mnpbem_cluster_tree* tree,
   int flag = 1, steps = 0;
   double relres = 0.0;
   MNP_TRY(gm.run(flag, steps, relres));
+  L.pc_last_steps = steps;
   // true relative residual ||b - A x|| / ||b|| with the H-matrix operator
   Vec64 v = vec64(G, L, P);
   MNP_CUDA(cudaMemsetAsync(L.norms.ptr, 0, sizeof(double) * 4, L.st));
@@ -2515,6 +2554,7 @@ mnpbem_status mnpbem_solve_iter(mnpbem_geom* G, const mnpbem_cluster_tree* tree,
     info->iter = steps;
     info->relres = relres;
     info->true_relres = L.res;
+    info->precond_enei = o.precond ? L.pc_enei : 0.0;
     hmat_stats(H, H.ranks, n, info);
   }
   return MNPBEM_OK;

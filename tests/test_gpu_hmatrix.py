@@ -196,3 +196,38 @@ def test_hmatrix_construction_is_deterministic(case):
         F1, r1 = bem.hmat_full(ENEI, name)
         F2, r2 = bem.hmat_full(ENEI, name)
         assert np.array_equal(r1, r2) and np.array_equal(F1, F2), name
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_preconditioner_reuse_across_wavelengths(case, precision):
+    # reuse_precond: the preconditioner built at the sweep's first wavelength
+    # serves the later ones (more GMRES steps, same solutions to the GMRES
+    # tolerance); a direct solve on the handle invalidates it; refresh_steps
+    # rebuilds it when a solve needed more steps
+    cp, ocp, oit = case
+    exc = m.planewave([[1, 0, 0]], [[0, 0, 1]])
+    eneis = [600.0, 620.0, 680.0]
+    tol = 1e-9
+    ref = m.bemsolver(cp, m.bemoptions(precision=precision, iter=m.bemiter_options(cleaf=CLEAF, tol=tol)))
+    r0 = ref.spectrum(exc, eneis, fields=True)
+    bem = m.bemsolver(cp, m.bemoptions(precision=precision, iter=m.bemiter_options(
+        cleaf=CLEAF, tol=tol, reuse_precond=True)))
+    r1 = bem.spectrum(exc, eneis, fields=True)
+    built = [i["precond_enei"] for i in bem.sweep_info]
+    steps = [i["iter"] for i in bem.sweep_info]
+    errs = {k: rel(r1[k], r0[k]) for k in ("sig1", "sig2", "h1", "h2", "ext")}
+    record("iter_reuse_" + precision, **errs, steps=steps, steps_no_reuse=[int(x) for x in r0["ir_iters"]],
+           built=built)
+    assert built == [600.0, 600.0, 600.0]
+    assert steps[2] > steps[0]
+    for k, e in errs.items():
+        assert e < 1e-6, (k, e)
+    # a direct solve overwrites the dense matrices: the next solve rebuilds
+    m.bemret.spectrum(bem, exc, [650.0])
+    bem.mldivide(exc(cp, 700.0))
+    assert bem.info["precond_enei"] == 700.0
+    # refresh_steps: rebuilt after a solve that needed more than 1 step
+    rf = m.bemsolver(cp, m.bemoptions(precision=precision, iter=m.bemiter_options(
+        cleaf=CLEAF, tol=tol, reuse_precond=True, refresh_steps=1)))
+    rf.spectrum(exc, eneis)
+    assert [i["precond_enei"] for i in rf.sweep_info][2] != 600.0
