@@ -487,7 +487,7 @@ def run_iter(a, torch):
     faces, htol 1e-6, kmax 100), GMRES (tol 1e-6) preconditioned by the
     complex64 tensor-core inverses.  Timed: a sweep of 8 wavelengths 600-740 nm
     that builds the preconditioner at its first wavelength and keeps it while
-    GMRES needs at most 15 steps (reuse_precond), after a warm-up sweep of two
+    GMRES needs at most 30 steps (reuse_precond), after a warm-up sweep of two
     wavelengths; then a profiled repeat at 600 nm (preconditioner rebuilt) for
     the H-matrix phases.  The extinction is compared with the direct mixed
     solve of the same handle at 600 and 740 nm."""
@@ -501,7 +501,7 @@ def run_iter(a, torch):
                        [[2, 1], [3, 1]], 1, 2)
     bem = m.bemsolver(cp, m.bemoptions(precision="mixed", device=dev, lanes=1,
                                        iter=m.bemiter_options(cleaf=200, htol=1e-6, kmax=[4, 100],
-                                                              reuse_precond=True, refresh_steps=15)))
+                                                              reuse_precond=True, refresh_steps=30)))
     exc = m.planewave([1, 0, 0], [0, 0, 1])
     bem.spectrum(exc, [650.0, 660.0])
     eneis = np.linspace(600.0, 740.0, 8)
@@ -525,7 +525,7 @@ def run_iter(a, torch):
             "config": {"workload": "iterative solver (bemretiter, H-matrices + GMRES) on the dimer of two d=50 nm "
                                    "spheres, 2 nm gap, 2 x %d faces, x-pol along +z, 8 wavelengths 600-740 nm" % nf,
                        "faces": 2 * nf, "cleaf": 200, "htol": 1e-6, "kmax": 100, "gmres_tol": 1e-6,
-                       "reuse_precond": True, "refresh_steps": 15,
+                       "reuse_precond": True, "refresh_steps": 30,
                        "timing": "host wall clock around bemretiter.spectrum (public API, one mnpbem_solve_iter "
                                  "per wavelength, charges and ext/sca to host)"},
             "gmres_steps": [i["iter"] for i in infos], "precond_built_at": [i["precond_enei"] for i in infos],

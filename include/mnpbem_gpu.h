@@ -363,7 +363,8 @@ typedef struct mnpbem_cluster_tree {
  * brackets).  solver: 0 GMRES [0] (cgs / bicgstab are not built);
  * precond: 0 none, 1 'full' [1] (the dense inverses of bemret in the
  * solve's precision: FP64, or complex64 on the tensor cores for MIXED);
- * restart 0 = no restarts (one cycle of up to maxit steps).
+ * restart 0 = no restarts (one cycle of up to maxit steps); at most 4096
+ * steps per cycle.
  * reuse_precond 1 (not in the reference, which rebuilds the preconditioner
  * at every wavelength): keep the 'full' preconditioner of an earlier
  * iterative solve on this handle (same precision) for this wavelength; it

@@ -2095,6 +2095,11 @@ mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax,
     const int r = t->low[2 * b], c = t->low[2 * b + 1];
     if (r < 0 || r >= nc || c < 0 || c >= nc) return bad("low-rank block cluster out of range");
     const int m = rows(r), nb = rows(c);
+    // the product walks a block's rows leaf by leaf: its row range must start
+    // and end on leaf boundaries
+    const int r0 = t->cind[2 * r], r1 = t->cind[2 * r + 1];
+    if (t->cind[2 * leaves[leaf_of[r0]]] != r0 || t->cind[2 * leaves[leaf_of[r1]] + 1] != r1)
+      return bad("a low-rank block's rows do not start and end on leaf boundaries");
     lblk[b] = make_int4(t->cind[2 * r], m, t->cind[2 * c], nb);
     kcap[b] = std::min(kmax, std::min(m, nb));
     aoff[b] = asz; asz += (int64_t)m * kcap[b];
@@ -2336,6 +2341,10 @@ struct Gmres {
     // complex64 preconditioner) is followed by another within the budget.
     const int inner = o.restart > 0 ? o.restart : o.maxit;
     const int64_t budget = o.restart > 0 ? (int64_t)o.maxit * o.restart : o.maxit;
+    if (inner > 4096) {
+      set_error("GMRES: at most 4096 steps per cycle (set restart)");
+      return MNPBEM_ERR_INVALID_ARG;
+    }
     MNP_TRY(V.ensure(sizeof(double2) * (size_t)(inner + 1) * len));
     MNP_TRY(part.ensure(sizeof(double2) * (size_t)(inner + 1) * KV_BLOCKS));
     MNP_TRY(hdev.ensure(sizeof(double2) * (size_t)(inner + 1)));

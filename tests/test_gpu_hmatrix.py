@@ -231,3 +231,27 @@ def test_preconditioner_reuse_across_wavelengths(case, precision):
         cleaf=CLEAF, tol=tol, reuse_precond=True, refresh_steps=1)))
     rf.spectrum(exc, eneis)
     assert [i["precond_enei"] for i in rf.sweep_info][2] != 600.0
+
+
+def test_malformed_trees_are_rejected(case):
+    # host-side validation before any device work: a permutation with a
+    # repeated face, and blocks that do not partition the matrix
+    from mnpbem_gb300 import _lib
+    cp, ocp, oit = case
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=CLEAF)))
+    t = bem.hpart
+    perm = t._keep[3]
+    saved = perm.copy()
+    perm[1] = perm[0]
+    with pytest.raises(_lib.MnpbemError) as e:
+        bem.hmat_full(ENEI, "G1")
+    assert e.value.status == 1 and "permutation" in str(e.value)
+    perm[:] = saved
+    nlow = t.c.nlow
+    t.c.nlow = nlow - 1
+    with pytest.raises(_lib.MnpbemError) as e:
+        bem.hmat_full(ENEI, "G1")
+    assert e.value.status == 1 and "partition" in str(e.value)
+    t.c.nlow = nlow
+    F, _ = bem.hmat_full(ENEI, "G1")
+    assert np.isfinite(F).all()
