@@ -216,8 +216,9 @@ struct YPtrs {
 };
 
 // rs CTAs share the rows of a leaf (grid.x = nleaf * rs) so that small trees
-// still fill the SMs
-template <int N>
+// still fill the SMs; each warp takes R consecutive rows, which share the
+// gathered vector entries and give R independent accumulation chains
+template <int N, int R>
 __global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, YPtrs ys, int rs) {
   const int l = blockIdx.x / rs, part = blockIdx.x - l * rs, q = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -225,48 +226,68 @@ __global__ void __launch_bounds__(256) k_hmv_leaf(HmatDev h, YPtrs ys, int rs) {
   const float4* x = h.xs + (q < 2 ? 0 : (int64_t)h.n * N);
   double2* y = ys.y[q];
   const int e0 = h.lptr[l], e1 = h.lptr[l + 1];
-  for (int rr = part * 8 + warp; rr < lf.y; rr += 8 * rs) {
-    const int i = lf.x + rr;
-    DS re[N], im[N];
+  for (int rr = (part * 8 + warp) * R; rr < lf.y; rr += 8 * rs * R) {
+    int ii[R];
+    bool ok[R];
 #pragma unroll
-    for (int c = 0; c < N; ++c) re[c] = im[c] = DS{0.f, 0.f};
+    for (int r = 0; r < R; ++r) {
+      ok[r] = rr + r < lf.y;
+      ii[r] = lf.x + (ok[r] ? rr + r : rr);
+    }
+    DS re[R][N], im[R][N];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int c = 0; c < N; ++c) re[r][c] = im[r][c] = DS{0.f, 0.f};
     for (int e = e0; e < e1; ++e) {
       const int ent = h.lent[e];
       if (ent >= 0) {
         const int4 fb = h.fblk[ent];
-        const float4* V = reinterpret_cast<const float4*>(h.val[q] + h.foff[ent]) + (int64_t)(i - fb.x) * fb.w;
-#pragma unroll 2
+        const float4* V0 = reinterpret_cast<const float4*>(h.val[q] + h.foff[ent]);
+        const float4* V[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) V[r] = V0 + (int64_t)(ii[r] - fb.x) * fb.w;
         for (int j = lane; j < fb.w; j += 32) {
-          const float4 v = V[j];
+          float4 v[R];
+#pragma unroll
+          for (int r = 0; r < R; ++r) v[r] = V[r][j];
           const float4* xr = x + (int64_t)h.perm[fb.z + j] * N;
 #pragma unroll
           for (int c = 0; c < N; ++c) {
             const float4 xv = xr[c];
-            ds_cfma(re[c], im[c], f4hi(v), f4lo(v), f4hi(xv), f4lo(xv));
+#pragma unroll
+            for (int r = 0; r < R; ++r) ds_cfma(re[r][c], im[r][c], f4hi(v[r]), f4lo(v[r]), f4hi(xv), f4lo(xv));
           }
         }
       } else {
         const int b = ~ent;
         const int4 lb = h.lblk[b];
         const int rank = h.rank[q * h.nlow + b];
-        const float4* A = h.At[q] + h.aoff[b] + (int64_t)(i - lb.x) * h.kcap[b];
+        const int kc = h.kcap[b];
+        const float4* A0 = h.At[q] + h.aoff[b];
         const float4* T = h.T + (int64_t)q * h.tsz + h.toff[b];
         for (int kk = lane; kk < rank; kk += 32) {
-          const float4 a = A[kk];
+          float4 a[R];
+#pragma unroll
+          for (int r = 0; r < R; ++r) a[r] = A0[(int64_t)(ii[r] - lb.x) * kc + kk];
 #pragma unroll
           for (int c = 0; c < N; ++c) {
             const float4 tv = T[kk * N + c];
-            ds_cfma(re[c], im[c], f4hi(a), f4lo(a), f4hi(tv), f4lo(tv));
+#pragma unroll
+            for (int r = 0; r < R; ++r) ds_cfma(re[r][c], im[r][c], f4hi(a[r]), f4lo(a[r]), f4hi(tv), f4lo(tv));
           }
         }
       }
     }
-    warp_sum_ds<N>(re, im);
-    if (lane == 0) {
-      double2* yr = y + (int64_t)h.perm[i] * N;
 #pragma unroll
-      for (int c = 0; c < N; ++c)
-        yr[c] = make_double2((double)re[c].hi + (double)re[c].lo, (double)im[c].hi + (double)im[c].lo);
+    for (int r = 0; r < R; ++r) {
+      warp_sum_ds<N>(re[r], im[r]);
+      if (lane == 0 && ok[r]) {
+        double2* yr = y + (int64_t)h.perm[ii[r]] * N;
+#pragma unroll
+        for (int c = 0; c < N; ++c)
+          yr[c] = make_double2((double)re[r][c].hi + (double)re[r][c].lo, (double)im[r][c].hi + (double)im[r][c].lo);
+      }
     }
   }
 }
@@ -440,7 +461,7 @@ mnpbem_status hmat_mv(const HmatDev& h, int N, const double2* x1, const double2*
 #define HMV_CASE(NN)                                                                  \
   case NN:                                                                            \
     if (h.nlow > 0) k_hmv_t<NN><<<dim3((unsigned)h.nlow, 4), 256, 0, st>>>(h);        \
-    k_hmv_leaf<NN><<<dim3((unsigned)(h.nleaf * rs), 4), 256, 0, st>>>(h, ys, rs);    \
+    k_hmv_leaf<NN, (NN <= 8 ? 2 : 1)><<<dim3((unsigned)(h.nleaf * rs), 4), 256, 0, st>>>(h, ys, rs); \
     break;
   switch (N) {
     HMV_CASE(4) HMV_CASE(8) HMV_CASE(12) HMV_CASE(16)

@@ -255,3 +255,20 @@ def test_malformed_trees_are_rejected(case):
     t.c.nlow = nlow
     F, _ = bem.hmat_full(ENEI, "G1")
     assert np.isfinite(F).all()
+
+
+def test_iterative_solve_curved_sphere(gpu_lib):
+    # curved elements (interp 'curv'): the H-matrices use the curved
+    # centroids, normals and areas and the curved refinement; the iterative
+    # FP64 solve reaches the direct one within the ACA / GMRES tolerances
+    p = m.trisphere(400, 30.0, {"interp": "curv"})
+    cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
+    exc = m.planewave([[1, 0, 0]], [[0, 0, 1]])
+    direct = m.bemsolver(cp, m.bemoptions(precision="fp64")).mldivide(exc(cp, ENEI))
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", iter=m.bemiter_options(cleaf=CLEAF, tol=1e-8)))
+    sig = bem.mldivide(exc(cp, ENEI))
+    errs = {k: rel(getattr(sig, k), getattr(direct, k)) for k in ("sig1", "sig2", "h1", "h2", "ext", "sca")}
+    record("iter_curved", **errs, iter=bem.info["iter"], rank_max=bem.info["rank_max"])
+    assert bem.info["flag"] == 0 and bem.hpart.low.shape[0] > 0
+    for k, e in errs.items():
+        assert e < 1e-5, (k, e)
