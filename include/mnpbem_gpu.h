@@ -360,7 +360,8 @@ typedef struct mnpbem_cluster_tree {
 } mnpbem_cluster_tree;
 
 /* Options of the iterative solver (BEM/@bemiter/options.m; defaults in
- * brackets).  solver: 0 GMRES [0] (cgs / bicgstab are not built);
+ * brackets).  solver: 0 GMRES [0], 1 CGS, 2 BiCGStab (the preconditioner
+ * applied to the search directions; relres then is ||b - A x|| / ||b||);
  * precond: 0 none, 1 'full' [1] (the dense inverses of bemret in the
  * solve's precision: FP64, or complex64 on the tensor cores for MIXED);
  * restart 0 = no restarts (one cycle of up to maxit steps); at most 4096

@@ -616,8 +616,8 @@ class bemretiter(bemret):
     ``refresh_steps`` GMRES steps): a sweep then pays the dense inversion
     once instead of at every wavelength, with the same solutions to ``tol``.
 
-    Restrictions: solver 'gmres' only; the 'hmat' preconditioner (H-matrix LU
-    of hmatlu / hmatsolve) is not built.
+    Solvers 'gmres', 'cgs' and 'bicgstab' (@bemiter/solve.m); the 'hmat'
+    preconditioner (H-matrix LU of hmatlu / hmatsolve) is not built.
     """
 
     def __init__(self, p, op=None):
@@ -627,8 +627,8 @@ class bemretiter(bemret):
                   "refresh_steps"):
             if k in op:
                 it[k] = op[k]
-        if it["solver"] != "gmres":
-            raise NotImplementedError("only the GMRES iterative solver is built")
+        if it["solver"] not in ("gmres", "cgs", "bicgstab"):
+            raise ValueError("solver must be 'gmres', 'cgs' or 'bicgstab'")
         if it["precond"] not in ("full", None, ""):
             raise NotImplementedError("precond must be 'full' or None (the 'hmat' preconditioner is not built)")
         super().__init__(p, op)
@@ -642,7 +642,7 @@ class bemretiter(bemret):
         if reuse is not None:
             it["reuse_precond"] = reuse
         o = _lib.IterOptions()
-        o.solver = 0
+        o.solver = ("gmres", "cgs", "bicgstab").index(it["solver"])
         o.tol = float(it["tol"])
         o.maxit = int(it["maxit"])
         o.restart = int(it["restart"] or 0)

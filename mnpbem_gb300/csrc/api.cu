@@ -2215,6 +2215,7 @@ void face_eps(mnpbem_geom* G, Lane& L) {
 }
 
 struct IterOpts {
+  int solver = 0;   // 0 gmres, 1 cgs, 2 bicgstab
   double tol = 1e-6, htol = 1e-6;
   int maxit = 100, restart = 0, precond = 1, kmax = 100;
   int reuse = 0, refresh = 0;
@@ -2222,10 +2223,11 @@ struct IterOpts {
 
 mnpbem_status iter_opts(const mnpbem_iter_options* op, IterOpts& o) {
   if (op) {
-    if (op->solver != 0) {
-      set_error("iterative solver: only GMRES (solver 0) is built");
-      return MNPBEM_ERR_UNSUPPORTED;
+    if (op->solver < 0 || op->solver > 2) {
+      set_error("iterative solver: solver must be 0 (gmres), 1 (cgs) or 2 (bicgstab)");
+      return MNPBEM_ERR_INVALID_ARG;
     }
+    o.solver = op->solver;
     if (op->tol > 0) o.tol = op->tol;
     if (op->maxit > 0) o.maxit = op->maxit;
     if (op->restart > 0) o.restart = op->restart;
@@ -2437,6 +2439,136 @@ struct Gmres {
     relres = rn / nmb;
     return MNPBEM_OK;
   }
+
+  // ---- cgs / bicgstab (@bemiter/solve.m): preconditioner on the search
+  // directions, unpreconditioned residuals in the equation layout
+  // (phi, a, alpha, De; 8 n P values), unknowns in [x1 | x2]
+  DevBuf kw;
+  std::complex<double> dot(const double2* u, const double2* w) {
+    kv_dots(u, 1, len, w, part.as<double2>(), L.st);
+    hpart.resize(KV_BLOCKS);
+    cudaMemcpyAsync(hpart.data(), part.ptr, sizeof(double2) * KV_BLOCKS, cudaMemcpyDeviceToHost, L.st);
+    cudaStreamSynchronize(L.st);
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = 0; b < KV_BLOCKS; ++b) s = cadd(s, hpart[b]);
+    return std::complex<double>(s.x, s.y);
+  }
+  static double2 c2(std::complex<double> z) { return make_double2(z.real(), z.imag()); }
+  void comb(double2* out, std::initializer_list<std::pair<std::complex<double>, const double2*>> terms) {
+    KvTerms t;
+    for (const auto& pr : terms) {
+      t.c[t.n] = c2(pr.first);
+      t.v[t.n] = pr.second;
+      ++t.n;
+    }
+    kv_lincomb(t, len, out, L.st);
+  }
+  // bdst = A x (equation layout)
+  mnpbem_status aop(const double2* x, double2* bdst) {
+    const double2* z = zero.as<double2>();
+    MNP_TRY(residual(x, z, z + n * P, z + 4 * n * P, z + 7 * n * P));
+    Vec64 v = vec64(G, L, P);
+    kv_scale(v.rphi, len, -1.0, bdst, L.st);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  // xdst = M b
+  mnpbem_status mop(const double2* b, double2* xdst) {
+    return precond(b, b + n * P, b + 4 * n * P, b + 7 * n * P, xdst);
+  }
+  mnpbem_status run_cgs_bicg(int& flag, int& steps, double& relres) {
+    using cd = std::complex<double>;
+    MNP_TRY(part.ensure(sizeof(double2) * KV_BLOCKS));
+    MNP_TRY(zero.ensure(sizeof(double2) * len));
+    MNP_TRY(kw.ensure(sizeof(double2) * 10 * len));
+    MNP_CUDA(cudaMemsetAsync(zero.ptr, 0, sizeof(double2) * len, L.st));
+    Vec64 v = vec64(G, L, P);
+    double2* x = v.x1;
+    double2* W = kw.as<double2>();
+    double2 *r = W, *rt = W + len, *p = W + 2 * len, *u = W + 3 * len, *q = W + 4 * len, *vv = W + 5 * len;
+    double2 *ph = W + 6 * len, *uh = W + 7 * len, *t = W + 8 * len, *tmp = W + 9 * len;
+    const double2* b = v.phi;   // phi, a, alpha, De are contiguous
+    MNP_CUDA(cudaMemsetAsync(x, 0, sizeof(double2) * len, L.st));
+    double nb = 0.0;
+    MNP_TRY(norm(b, nb));
+    flag = 1;
+    steps = 0;
+    relres = 0.0;
+    if (!(nb > 0)) {
+      if (nb != 0) { set_error("iterative solver: non-finite right-hand side"); return MNPBEM_ERR_NOT_CONVERGED; }
+      flag = 0;
+      return MNPBEM_OK;
+    }
+    const double tolb = o.tol * nb;
+    comb(r, {{1.0, b}});
+    comb(rt, {{1.0, b}});
+    cd rho = 1.0, rho1, alpha = 1.0, omega = 1.0;
+    double rn = nb;
+    for (int ii = 1; ii <= o.maxit; ++ii) {
+      rho1 = rho;
+      rho = dot(rt, r);
+      if (rho == 0.0 || !(std::abs(rho) == std::abs(rho))) break;
+      steps = ii;
+      if (o.solver == 1) {                                   // cgs
+        if (ii == 1) {
+          comb(u, {{1.0, r}});
+          comb(p, {{1.0, u}});
+        } else {
+          const cd beta = rho / rho1;
+          comb(u, {{1.0, r}, {beta, q}});
+          comb(p, {{1.0, u}, {beta, q}, {beta * beta, p}});
+        }
+        MNP_TRY(mop(p, ph));
+        MNP_TRY(aop(ph, vv));
+        const cd rtv = dot(rt, vv);
+        if (rtv == 0.0) break;
+        alpha = rho / rtv;
+        comb(q, {{1.0, u}, {-alpha, vv}});
+        comb(tmp, {{1.0, u}, {1.0, q}});
+        MNP_TRY(mop(tmp, uh));
+        comb(x, {{1.0, x}, {alpha, uh}});
+        MNP_TRY(aop(uh, t));
+        comb(r, {{1.0, r}, {-alpha, t}});
+        MNP_TRY(norm(r, rn));
+        if (rn <= tolb) { flag = 0; break; }
+      } else {                                               // bicgstab
+        if (ii == 1) {
+          comb(p, {{1.0, r}});
+        } else {
+          const cd beta = (rho / rho1) * (alpha / omega);
+          comb(p, {{1.0, r}, {beta, p}, {-beta * omega, vv}});
+        }
+        MNP_TRY(mop(p, ph));
+        MNP_TRY(aop(ph, vv));
+        const cd rtv = dot(rt, vv);
+        if (rtv == 0.0) break;
+        alpha = rho / rtv;
+        comb(q, {{1.0, r}, {-alpha, vv}});                  // s
+        double sn = 0.0;
+        MNP_TRY(norm(q, sn));
+        if (sn <= tolb) {
+          comb(x, {{1.0, x}, {alpha, ph}});
+          flag = 0;
+          break;
+        }
+        MNP_TRY(mop(q, uh));                                 // sh
+        MNP_TRY(aop(uh, t));
+        const cd tt = dot(t, t);
+        if (tt == 0.0) break;
+        omega = dot(t, q) / tt;
+        comb(x, {{1.0, x}, {alpha, ph}, {omega, uh}});
+        comb(r, {{1.0, q}, {-omega, t}});
+        MNP_TRY(norm(r, rn));
+        if (rn <= tolb) { flag = 0; break; }
+      }
+    }
+    // true residual
+    MNP_TRY(aop(x, tmp));
+    comb(tmp, {{1.0, b}, {-1.0, tmp}});
+    MNP_TRY(norm(tmp, rn));
+    relres = rn / nb;
+    return MNPBEM_OK;
+  }
 };
 
 // one wavelength on lane 0: excitation, H-matrices, optional preconditioner
@@ -2544,7 +2676,8 @@ mnpbem_status mnpbem_solve_iter(mnpbem_geom* G, const mnpbem_cluster_tree* tree,
   Gmres gm(G, L, j.c, H, o);
   int flag = 1, steps = 0;
   double relres = 0.0;
-  MNP_TRY(gm.run(flag, steps, relres));
+  if (o.solver == 0) MNP_TRY(gm.run(flag, steps, relres));
+  else MNP_TRY(gm.run_cgs_bicg(flag, steps, relres));
   L.pc_last_steps = steps;
   // true relative residual ||b - A x|| / ||b|| with the H-matrix operator
   Vec64 v = vec64(G, L, P);

@@ -407,6 +407,14 @@ __global__ void k_kv_scale(const double2* w, int64_t len, double s, double2* out
     out[e] = make_double2(s * w[e].x, s * w[e].y);
 }
 
+__global__ void k_kv_lincomb(KvTerms t, int64_t len, double2* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < len; e += (int64_t)gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int i = 0; i < t.n; ++i) cfma(s, t.c[i], t.v[i][e]);
+    out[e] = s;
+  }
+}
+
 __global__ void k_kv_pack_bx(int64_t n, int P, const double2* phi, const double2* a, const double2* alpha,
                              const double2* De, double2* x) {
   const int64_t W = 4 * P;
@@ -492,6 +500,9 @@ void kv_norm2(const double2* w, int64_t len, double* partial, cudaStream_t st) {
 }
 void kv_scale(const double2* w, int64_t len, double s, double2* out, cudaStream_t st) {
   k_kv_scale<<<KV_BLOCKS, 256, 0, st>>>(w, len, s, out);
+}
+void kv_lincomb(const KvTerms& t, int64_t len, double2* out, cudaStream_t st) {
+  k_kv_lincomb<<<KV_BLOCKS, 256, 0, st>>>(t, len, out);
 }
 void kv_pack_bx(int64_t n, int P, const double2* phi, const double2* a, const double2* alpha, const double2* De,
                 double2* x, cudaStream_t st) {

@@ -66,6 +66,13 @@ void kv_update(const double2* V, int nv, int64_t len, const double2* h, double2*
 void kv_norm2(const double2* w, int64_t len, double* partial, cudaStream_t st);
 // out = s w (s real; out may be w)
 void kv_scale(const double2* w, int64_t len, double s, double2* out, cudaStream_t st);
+// out = sum_i c[i] v[i] over up to 4 terms (out may be one of the v[i])
+struct KvTerms {
+  int n = 0;
+  double2 c[4];
+  const double2* v[4];
+};
+void kv_lincomb(const KvTerms& t, int64_t len, double2* out, cudaStream_t st);
 // b-space (phi [n][P], a [n][3][P], alpha [n][3][P], De [n][P]) -> x-space
 // ([n][4P] of (phi | a), then [n][4P] of (De | alpha)): the identification of
 // bemretiter's pack.m / unpack.m

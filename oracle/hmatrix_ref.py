@@ -20,7 +20,9 @@ preconditioned GMRES of ``bemretiter``.  Followed files:
   full blocks hold the entries of the complete Green function (refinement
   included);
 * ``BEM/@bemretiter/private/afun.m:6-35``, ``mfun.m:1-52``,
-  ``initprecond.m:1-76`` ('full'), ``@bemiter/solve.m:1-45``.
+  ``initprecond.m:1-76`` ('full'), ``@bemiter/solve.m:1-45`` (gmres, cgs,
+  bicgstab; cgs and bicgstab restated from their published algorithms with
+  the preconditioner applied to the search directions).
 
 Deviations (also made by the GPU path, so both agree): the low-rank blocks of
 G1 = g{1,1} - g{2,1} (and H1, G2, H2) are compressed as one kernel (the
@@ -355,6 +357,100 @@ def gmres(afun, b, tol=1e-6, maxit=100, restart=None, mfun=None):
     return x, 1, np.linalg.norm(r) / nmb, steps
 
 
+def cgs(afun, b, tol=1e-6, maxit=100, mfun=None):
+    """Preconditioned conjugate gradients squared (x0 = 0; the preconditioner
+    M applied to the search directions, residuals unpreconditioned; stop when
+    the recurrence residual ||r|| <= tol ||b||).  Returns x, flag, relres =
+    ||b - A x|| / ||b|| (true residual), iterations."""
+    M = (lambda v: v) if mfun is None else mfun
+    nb = np.linalg.norm(b)
+    x = M(np.zeros_like(b)) * 0
+    if nb == 0:
+        return x, 0, 0.0, 0
+    tolb = tol * nb
+    r = b.copy()
+    rt = r.copy()
+    rho = 1.0
+    u = q = p = None
+    flag, it = 1, 0
+    for ii in range(1, maxit + 1):
+        rho1, rho = rho, np.vdot(rt, r)
+        if rho == 0:
+            break
+        if ii == 1:
+            u = r.copy()
+            p = u.copy()
+        else:
+            beta = rho / rho1
+            u = r + beta * q
+            p = u + beta * (q + beta * p)
+        ph = M(p)
+        vh = afun(ph)
+        rtv = np.vdot(rt, vh)
+        if rtv == 0:
+            break
+        alpha = rho / rtv
+        q = u - alpha * vh
+        uh = M(u + q)
+        x = x + alpha * uh
+        r = r - alpha * afun(uh)
+        it = ii
+        if np.linalg.norm(r) <= tolb:
+            flag = 0
+            break
+    return x, flag, np.linalg.norm(b - afun(x)) / nb, it
+
+
+def bicgstab(afun, b, tol=1e-6, maxit=100, mfun=None):
+    """Preconditioned BiCGStab (x0 = 0; residuals unpreconditioned; stop when
+    ||s|| or ||r|| <= tol ||b||, the half step counting as its iteration).
+    Returns x, flag, relres = ||b - A x|| / ||b||, iterations."""
+    M = (lambda v: v) if mfun is None else mfun
+    nb = np.linalg.norm(b)
+    x = M(np.zeros_like(b)) * 0
+    if nb == 0:
+        return x, 0, 0.0, 0
+    tolb = tol * nb
+    r = b.copy()
+    rt = r.copy()
+    rho = alpha = omega = 1.0
+    p = v = None
+    flag, it = 1, 0
+    for ii in range(1, maxit + 1):
+        rho1, rho = rho, np.vdot(rt, r)
+        if rho == 0:
+            break
+        if ii == 1:
+            p = r.copy()
+        else:
+            beta = (rho / rho1) * (alpha / omega)
+            p = r + beta * (p - omega * v)
+        ph = M(p)
+        v = afun(ph)
+        rtv = np.vdot(rt, v)
+        if rtv == 0:
+            break
+        alpha = rho / rtv
+        s = r - alpha * v
+        it = ii
+        if np.linalg.norm(s) <= tolb:
+            x = x + alpha * ph
+            flag = 0
+            break
+        sh = M(s)
+        t = afun(sh)
+        tt = np.vdot(t, t)
+        if tt == 0:
+            break
+        omega = np.vdot(t, s) / tt
+        x = x + alpha * ph + omega * sh
+        r = s - omega * t
+        if np.linalg.norm(r) <= tolb:
+            flag = 0
+            break
+    return x, flag, np.linalg.norm(b - afun(x)) / nb, it
+
+
 # --------------------------------------------------------------------------
 # bemretiter
 # --------------------------------------------------------------------------
@@ -363,13 +459,14 @@ class BemRetIter:
     'full' (dense chain of mldivide.m) or None."""
 
     def __init__(self, cp, cleaf=200, htol=1e-6, kmax=100, tol=1e-6, maxit=100, restart=None,
-                 precond="full", eta=2.5):
+                 precond="full", eta=2.5, solver="gmres"):
         self.p = cp
         self.bem = R.BemRet(cp)
         face_part = np.repeat(np.arange(len(cp.parts)), [q.n for q in cp.parts])
         self.tree = ClusterTree(cp.pos, face_part, cleaf)
         self.htol, self.kmax, self.eta = htol, kmax, eta
         self.tol, self.maxit, self.restart, self.precond = tol, maxit, restart, precond
+        self.solver = solver
         self.enei = None
 
     def initmat(self, enei):
@@ -421,7 +518,13 @@ class BemRetIter:
         phi, a, alpha, De = self.bem.excitation(exc)
         b = self._pack(phi, a, De, alpha)
         mf = self.mfun if self.precond == "full" else None
-        x, flag, relres, it = gmres(self.afun, b, self.tol, self.maxit, self.restart, mf)
+        if self.solver == "gmres":
+            x, flag, relres, it = gmres(self.afun, b, self.tol, self.maxit, self.restart, mf)
+        else:
+            # the unpreconditioned operator maps unknowns to equations of the same
+            # layout (pack.m / unpack.m), so both solvers run on one vector space
+            fn = cgs if self.solver == "cgs" else bicgstab
+            x, flag, relres, it = fn(self.afun, b, self.tol, self.maxit, mf)
         sig1, h1, sig2, h2 = self._split(x)
         self.flag, self.relres, self.iter = flag, relres, it
         self.true_relres = np.linalg.norm(b - self.afun(x)) / np.linalg.norm(b)

@@ -6,8 +6,9 @@
 * the oracle's ACA (mex/hlib/aca.cpp) approximates the dense G1, H1, G2, H2
   to the order of htol (expanded H-matrices within 10 htol of the dense
   matrices in the Frobenius norm);
-* the oracle's GMRES reproduces numpy's solve on random systems with and
-  without restarts, and the oracle's iterative BEM solve (preconditioned and
+* the oracle's GMRES (with and without restarts), CGS and BiCGStab reproduce
+  numpy's solve on random systems and converge in one iteration with an exact
+  preconditioner, and the oracle's iterative BEM solve (preconditioned and
   plain) reaches the direct bemret solution within tol-scaled bounds.
 """
 import numpy as np
@@ -116,3 +117,19 @@ def test_oracle_iterative_solve_matches_direct():
         scale = np.max(np.abs(direct[k]))
         assert np.max(np.abs(s[k] - direct[k])) / scale < 1e-5, k
         assert np.max(np.abs(s2[k] - direct[k])) / scale < 1e-3, k
+
+
+@pytest.mark.parametrize("solver", ["cgs", "bicgstab"])
+def test_oracle_cgs_bicgstab_random_system(solver):
+    rng = np.random.default_rng(7)
+    n = 120
+    A = np.eye(n) * 4 + (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    fn = HR.cgs if solver == "cgs" else HR.bicgstab
+    x, flag, relres, it = fn(lambda v: A @ v, b, tol=1e-10, maxit=200)
+    assert flag == 0 and relres < 1e-9
+    assert np.linalg.norm(x - np.linalg.solve(A, b)) / np.linalg.norm(x) < 1e-8
+    # an exact preconditioner converges in one iteration
+    Ai = np.linalg.inv(A)
+    x1, flag1, _, it1 = fn(lambda v: A @ v, b, tol=1e-10, maxit=20, mfun=lambda v: Ai @ v)
+    assert flag1 == 0 and it1 == 1
