@@ -200,6 +200,14 @@ def lib_stream(bem, torch):
     return torch.cuda.ExternalStream(s.value)
 
 
+def tuned_lanes(n, precision):
+    """Lane count the library uses when none is given: the tuned table's entry
+    for this size, else its automatic default."""
+    from mnpbem_gb300 import autotune
+    lanes = autotune.settings_for(n, precision).get("lanes")
+    return "tuned: %d" % lanes if lanes else "auto"
+
+
 def read_profile(bem):
     from mnpbem_gb300 import _lib
     names = ["assembly", "gemm_n3", "gemm_thin", "block_inverse", "elementwise", "spectra", "geometry",
@@ -661,7 +669,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": workload_desc(a), "faces": n, "wavelengths_per_step": a.batch,
-                           "precision": a.precision, "lanes": a.lanes or "auto",
+                           "precision": a.precision, "lanes": a.lanes or tuned_lanes(n, a.precision),
                            "refine_tol": a.refine_tol if a.precision == "mixed" else None,
                            "l2": "no flush: per-wavelength working set %.2f GB > 129 MB L2" % (wset / 1e9)},
                 "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],

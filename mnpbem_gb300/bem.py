@@ -169,7 +169,7 @@ class bemret:
             from . import autotune
             for key, val in autotune.settings_for(p.n, prec).items():
                 self.set_option(key, val)
-        if "lanes" in self.op:
+        if self.op.get("lanes"):          # 0 / None: the tuned or automatic lane count
             self.set_lanes(int(self.op["lanes"]))
 
     def __del__(self):
