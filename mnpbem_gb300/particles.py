@@ -183,11 +183,32 @@ class particle:
 
     nfaces = n
 
+    def midpoints(self, key="flat"):
+        """Particle with the nodes of curved elements
+        (Particles/@particle/midpoints.m): key 'flat' puts them at the edge
+        midpoints and quadrilateral centroids, 'curv' on cubic Bezier curves
+        through the surface tangents estimated at the vertices (refine.m).
+        As in midpoints.m:14 the element interpolation becomes ``key``."""
+        if key not in ("flat", "curv"):
+            raise ValueError("midpoints key must be 'flat' or 'curv'")
+        make = shapes.midpoints_flat if key == "flat" else shapes.midpoints_curv
+        v2, f2 = make(self.verts, self.faces)
+        return particle(v2, f2, dict(self.op, interp=key))
+
     def shift(self, vec):
         d = np.asarray(vec, dtype=np.float64)[None, :]
         if self.faces2 is not None:
             return particle(self.verts2 + d, self.faces2, self.op)
         return particle(self.verts + d, self.faces, self.op)
+
+
+def curved(p, key=None):
+    """Particle with curved elements (Particles/@particle/curved.m:1-18): new
+    nodes from ``p.midpoints(key)`` when ``p`` has none or a key is given
+    (flat midpoints by default), else the nodes ``p`` carries."""
+    if p.faces2 is None or key is not None:
+        p = p.midpoints(key or "flat")
+    return particle(p.verts2, p.faces2, dict(p.op, interp="curv"))
 
 
 def trisphere(n, diameter=1.0, op=None):

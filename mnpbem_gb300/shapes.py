@@ -97,6 +97,143 @@ def midpoints_flat(verts, faces):
     return np.vstack([verts, mids, cents]), faces2
 
 
+def _split_triangles(faces):
+    """Triangles of a face list (totriangles_flat.m): every face's corners
+    1-2-3, then corners 3-4-1 of each quadrilateral; returns the triangles and
+    the quadrilateral rows."""
+    i4 = np.nonzero(faces[:, 3] >= 0)[0]
+    return np.vstack([faces[:, :3], faces[i4][:, [2, 3, 0]]]), i4
+
+
+def _neighbour_fans(tri, nv):
+    """Ordered neighbour fan of every vertex, in the order of MNPBEM's
+    vertex_neighbours.m (Particles/@particle/private/vertex_neighbours.m:1-76),
+    which decides the opposite neighbours of the edge tangents.
+
+    A face (a, b, c) gives a the pair (b, c), b the pair (c, a) and c the pair
+    (a, b); a vertex's pairs are kept in face order.  The fan opens at the
+    first pair whose first vertex closes no other pair (a boundary vertex),
+    else at the first pair, and grows by sweeps over the pairs that append
+    the second vertex of each pair continuing the fan; a sweep that appends
+    nothing appends every missing vertex of every pair instead."""
+    owner = tri.reshape(-1)
+    other = tri[:, [1, 2, 2, 0, 0, 1]].reshape(-1, 2)
+    order = np.argsort(owner, kind="stable")
+    starts = np.searchsorted(owner[order], np.arange(nv + 1))
+    fans = []
+    for v in range(nv):
+        pairs = other[order[starts[v]:starts[v + 1]]].tolist()
+        if not pairs:
+            fans.append([])
+            continue
+        seconds = {s for _, s in pairs}
+        opening = next((k for k, (f, _) in enumerate(pairs) if f not in seconds), None)
+        fan = list(pairs[opening if opening is not None else 0])
+        seen = set(fan)
+        for _ in range(len(pairs) - 1 - (opening is None)):
+            grown = False
+            for f, s in pairs:
+                if f == fan[-1] and s not in seen:
+                    fan.append(s)
+                    seen.add(s)
+                    grown = True
+            if not grown:
+                for f, s in pairs:
+                    if f not in seen:
+                        fan.append(f)
+                        seen.add(f)
+                        if s not in seen:
+                            fan.append(s)
+                            seen.add(s)
+        for f, s in pairs:
+            for x in (f, s):
+                if x not in seen:
+                    fan.append(x)
+                    seen.add(x)
+        fans.append(fan)
+    return fans
+
+
+def midpoints_curv(verts, faces):
+    """Nodes of curved elements from the approximate curvature of a flat mesh
+    (Particles/@particle/midpoints.m:47-49, key 'curv', through
+    private/refine.m, edge_tangents.m and make_halfway_vertices.m).
+
+    Every edge i-j gets the midpoint of the cubic Bezier curve whose end
+    tangents are estimated at i and j: at a vertex P, the tangent towards the
+    neighbour Pn bisects the angle of the planar triangle (P, Pn, Pnop), Pnop
+    being the fan neighbour opposite Pn (the mean of the two nearest for an
+    odd fan), and the handle length is (|P - Pn| + |Pn - Pnop| / 2) / 6.
+    Returns ``verts2`` (the corners, then one node per edge in the order of
+    the edge's first visit: lower vertex first, fan order) and ``faces2
+    [n, 9]``: triangle midpoints of edges 12, 23, 31 in columns 4-6;
+    quadrilateral midpoints of edges 12, 23, 34, 41 in 4-7 and of the
+    diagonal 3-1 as its centre node in 8 (refine.m:35-48); -1 where unused."""
+    verts = np.ascontiguousarray(verts, dtype=np.float64)
+    faces = np.asarray(faces, dtype=np.int64)
+    if faces.shape[1] == 3:
+        faces = np.hstack([faces, -np.ones((faces.shape[0], 1), np.int64)])
+    n, nv = faces.shape[0], verts.shape[0]
+    tri, i4 = _split_triangles(faces)
+    fans = _neighbour_fans(tri, nv)
+    deg = np.array([len(f) for f in fans], np.int64)
+    src = np.repeat(np.arange(nv), deg)
+    dst = np.array([x for f in fans for x in f], np.int64)
+    # position k of each directed edge in its fan, and the opposite neighbours
+    base = np.repeat(np.cumsum(deg) - deg, deg)
+    k = np.arange(src.size) - base
+    L = deg[src]
+    o1 = np.where(L % 2 == 0, (k + L // 2) % np.maximum(L, 1), (k + (L - 1) // 2) % np.maximum(L, 1))
+    o2 = np.where(L % 2 == 0, o1, (k + (L + 1) // 2) % np.maximum(L, 1))
+    P, pn = verts[src], verts[dst]
+    pnop = (verts[dst[base + o1]] + verts[dst[base + o2]]) / 2
+
+    def length(d):
+        return np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    ec = length(pn - P) + 1e-14
+    eb = length(pnop - P) + 1e-14
+    ea = length(pn - pnop) + 1e-14
+    s = (ea + eb + ec) / 2
+    # Heron's product is clamped at zero (collinear points under rounding)
+    h = (2 / ea) * np.sqrt(np.maximum(s * (s - ea) * (s - eb) * (s - ec), 0.0)) + 1e-14
+    x = (ea * ea - eb * eb + ec * ec) / (2 * ea)
+    r1 = np.sqrt(h * h + x * x) + 1e-14
+    r2 = np.sqrt(h * h + (ea - x) * (ea - x)) + 1e-14
+    t0 = x / r1 + (ea - x) / r2          # 2-D tangent (t0, t1)
+    t1 = -(-h / r1 + h / r2)
+    pm = (pn * x[:, None] + pnop * (ea - x)[:, None]) / ea[:, None]
+    tan = (pn - pnop) / ea[:, None] * t0[:, None] + (P - pm) / h[:, None] * t1[:, None]
+    tan = tan / (length(tan) + 1e-14)[:, None]
+    vel = 0.5 * (ec + 0.5 * ea)
+    # one node per undirected edge, from its lower vertex's side
+    key = src * nv + dst
+    ordk = np.argsort(key)
+    rev = ordk[np.searchsorted(key[ordk], dst * nv + src)]
+    first = np.nonzero(dst > src)[0]
+    p0, p3 = P[first], pn[first]
+    p1 = p0 + tan[first] * vel[first][:, None] / 3
+    p2 = p3 + tan[rev[first]] * vel[rev[first]][:, None] / 3
+    c = 3 * (p1 - p0)
+    b = 3 * (p2 - p1) - c
+    a = p3 - p0 - c - b
+    mids = a * 0.125 + b * 0.250 + c * 0.500 + p0
+    ekey = key[first]
+    eord = np.argsort(ekey)
+
+    def node(u, w):
+        q = np.minimum(u, w) * nv + np.maximum(u, w)
+        return nv + eord[np.searchsorted(ekey[eord], q)]
+    m = np.stack([node(tri[:, 0], tri[:, 1]), node(tri[:, 1], tri[:, 2]), node(tri[:, 2], tri[:, 0])], 1)
+    faces2 = -np.ones((n, 9), np.int64)
+    faces2[:, :4] = faces
+    i3 = np.nonzero(faces[:, 3] < 0)[0]
+    faces2[i3, 4:7] = m[i3]
+    if i4.size:
+        faces2[i4, 4:6] = m[i4, :2]
+        faces2[i4, 6:9] = m[n:]
+    return np.vstack([verts, mids]), faces2
+
+
 def trisphere_curved(n, diameter=1.0):
     """``trisphere`` with the curved-element nodes of trisphere.m:54-61: edge
     midpoints projected onto the sphere.  Returns ``verts2, faces2``."""

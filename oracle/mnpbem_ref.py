@@ -182,6 +182,171 @@ def midpoints_flat(verts, faces):
     return verts2, faces2
 
 
+def _norm3(d):
+    """sqrt(sum(d.^2)) of a 3-vector, summed in MATLAB's order."""
+    return np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+
+
+def vertex_neighbours(tri, nv):
+    """Ordered neighbour fan of every vertex
+    (Particles/@particle/private/vertex_neighbours.m:1-76), 0-based.
+
+    Each face (a, b, c) appends the pairs (b, c), (c, a), (a, b) to the lists
+    of a, b, c (:10-17).  The fan starts at the first pair whose first vertex
+    is no pair's second vertex (an open fan), else at the first pair
+    (:25-37); it is then continued by appending the second vertex of every
+    pair whose first vertex is the current last one (:42-50), with the
+    fallbacks of :51-60 and :63-69 for irregular vertices."""
+    pairs = [[] for _ in range(nv)]
+    for a, b, c in tri:
+        a, b, c = int(a), int(b), int(c)
+        pairs[a] += [b, c]
+        pairs[b] += [c, a]
+        pairs[c] += [a, b]
+    out = []
+    for i in range(nv):
+        pf = pairs[i]
+        m = len(pf)
+        if m == 0:
+            out.append([])
+            continue
+        start, found = 0, False
+        for i1 in range(0, m, 2):
+            found = False
+            for i2 in range(1, m, 2):
+                if pf[i1] == pf[i2]:
+                    found = True
+                    break
+            if not found:
+                start = i1
+                break
+        pn = [pf[start], pf[start + 1]]
+        for _ in range(2 + int(found), m // 2 + 1):
+            hit = False
+            for idx in range(0, m, 2):
+                if pf[idx] == pn[-1] and pf[idx + 1] not in pn:
+                    hit = True
+                    pn.append(pf[idx + 1])
+            if not hit:
+                for idx in range(0, m, 2):
+                    if pf[idx] not in pn:
+                        pn.append(pf[idx])
+                        if pf[idx + 1] not in pn:
+                            pn.append(pf[idx + 1])
+        if len(pn) < m:
+            for x in pf:
+                if x not in pn:
+                    pn.append(x)
+        out.append(pn)
+    return out
+
+
+def edge_tangents(verts, ne):
+    """Tangent and velocity of every directed edge i -> ne[i][k]
+    (Particles/@particle/private/edge_tangents.m:1-72): the opposite neighbour
+    is ne[i][k + L/2] (the mean of the two nearest for odd L, :14-28); the
+    tangent bisects the 2-D triangle (P, neighbour, opposite) and is mapped
+    back to 3-D (:30-65); the velocity is (|P - Pn| + |Pn - Pnop| / 2) / 2.
+
+    The Heron product s(s-a)(s-b)(s-c) is clamped at zero: MATLAB's sqrt
+    would return a complex number for a negative product (possible only for
+    collinear points whose rounding beats the 1e-14 guards added to every
+    length)."""
+    rows, tang, vel = [], [], []
+    for i in range(len(ne)):
+        nb = ne[i]
+        L = len(nb)
+        P = verts[i]
+        for k in range(L):
+            if L % 2 == 0:
+                pnop = verts[nb[(k + L // 2) % L]]
+            else:
+                o1, o2 = (k + (L - 1) // 2) % L, (k + (L + 1) // 2) % L
+                pnop = (verts[nb[o1]] + verts[nb[o2]]) / 2
+            pn = verts[nb[k]]
+            ec = _norm3(pn - P) + 1e-14
+            eb = _norm3(pnop - P) + 1e-14
+            ea = _norm3(pn - pnop) + 1e-14
+            s = (ea + eb + ec) / 2
+            h = (2 / ea) * np.sqrt(max(s * (s - ea) * (s - eb) * (s - ec), 0.0)) + 1e-14
+            x = (ea * ea - eb * eb + ec * ec) / (2 * ea)
+            npv = np.array([-h, x])
+            npv = npv / (np.sqrt(npv[0] * npv[0] + npv[1] * npv[1]) + 1e-14)
+            nsv = np.array([h, ea - x])
+            nsv = nsv / (np.sqrt(nsv[0] * nsv[0] + nsv[1] * nsv[1]) + 1e-14)
+            nbv = npv + nsv
+            tb = (nbv[1], -nbv[0])
+            pm = (pn * x + pnop * (ea - x)) / ea
+            x3 = (pn - pnop) / ea
+            y3 = (P - pm) / h
+            t3 = x3 * tb[0] + y3 * tb[1]
+            t3 = t3 / (_norm3(t3) + 1e-14)
+            rows.append((i, nb[k]))
+            tang.append(t3)
+            vel.append(0.5 * (ec + 0.5 * ea))
+    return rows, np.asarray(tang).reshape(-1, 3), np.asarray(vel)
+
+
+def make_halfway_vertices(vel, tang, rows, verts, ne):
+    """Cubic Bezier midpoint of every edge from the end tangents and
+    velocities (Particles/@particle/private/make_halfway_vertices.m:1-69):
+    P1 = P0 + T01 v01 / 3, P2 = P3 + T10 v10 / 3, point at t = 1/2.  New
+    points are numbered in the order (i ascending, fan order of i) of the
+    edge's first visit.  Returns ``verts2`` and the map {(i, j): index}."""
+    pos = {r: k for k, r in enumerate(rows)}
+    new, idx = [], {}
+    nv = verts.shape[0]
+    for i in range(len(ne)):
+        for j in ne[i]:
+            if (i, j) in idx:
+                continue
+            a = pos[(i, j)]
+            b = pos[(j, i)]
+            p0, p3 = verts[i], verts[j]
+            p1 = p0 + tang[a] * vel[a] / 3
+            p2 = p3 + tang[b] * vel[b] / 3
+            c = 3 * (p1 - p0)
+            bb = 3 * (p2 - p1) - c
+            aa = p3 - p0 - c - bb
+            new.append(aa * 0.125 + bb * 0.250 + c * 0.500 + p0)
+            idx[(i, j)] = idx[(j, i)] = nv + len(new) - 1
+    verts2 = np.vstack([verts] + ([np.asarray(new)] if new else []))
+    return verts2, idx
+
+
+def midpoints_curv(verts, faces):
+    """Curved-element nodes from the approximate curvature
+    (Particles/@particle/midpoints.m:47-49 -> private/refine.m:1-52): the
+    faces are split into triangles (totriangles_flat.m), every edge gets the
+    Bezier midpoint of make_halfway_vertices.m, and faces2 takes for a
+    triangle the midpoints of edges 12, 23, 31 (columns 4-6) and for a
+    quadrilateral those of 12, 23 (triangle 123) and 34, 41, 13 (triangle
+    341) in columns 4-8, so that the quadrilateral's centre node is the
+    midpoint of its diagonal 3-1 (refine.m:35-48).  0-based, -1 where
+    unused."""
+    verts = np.asarray(verts, float)
+    faces = np.asarray(faces, np.int64)
+    if faces.shape[1] == 3:
+        faces = np.hstack([faces, -np.ones((faces.shape[0], 1), np.int64)])
+    n = faces.shape[0]
+    i4 = np.nonzero(faces[:, 3] >= 0)[0]
+    tri = np.vstack([faces[:, :3], faces[i4][:, [2, 3, 0]]])
+    ne = vertex_neighbours(tri, verts.shape[0])
+    rows, tang, vel = edge_tangents(verts, ne)
+    verts2, idx = make_halfway_vertices(vel, tang, rows, verts, ne)
+    mids = np.array([[idx[(a, b)], idx[(b, c)], idx[(c, a)]] for a, b, c in tri.tolist()],
+                    np.int64).reshape(-1, 3)
+    faces2 = -np.ones((n, 9), np.int64)
+    faces2[:, :4] = faces
+    i3 = np.nonzero(faces[:, 3] < 0)[0]
+    faces2[i3, 4:7] = mids[i3]
+    if i4.size:
+        ib = n + np.arange(i4.size)
+        faces2[i4, 4:6] = mids[i4][:, :2]
+        faces2[i4, 6:9] = mids[ib]
+    return verts2, faces2
+
+
 class Particle:
     """Particle boundary: ``pos``, ``area``, ``tvec1``, ``tvec2``, ``nvec``.
 

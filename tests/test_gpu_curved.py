@@ -120,3 +120,29 @@ def test_gradient_rejects_curved(sphere):
     with pytest.raises(m._lib.MnpbemError) as err:
         bem.ext_gradient(m.planewave([1, 0, 0], [0, 0, 1]), 600.0)
     assert err.value.status == 7     # UNSUPPORTED
+
+
+def test_curvature_midpoints_rod(gpu_lib):
+    """Rod whose curved nodes come from midpoints(p, 'curv') (refine.m): the
+    GPU solve on the package's nodes against the oracle on the nodes of its
+    own restatement (FP64 1e-10, mixed 1e-8)."""
+    from oracle import mnpbem_ref as Ro
+    v, f = shapes.trirod(10.0, 40.0, (15, 5, 11))
+    p = m.particle(v, f).midpoints("curv")
+    cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
+    t = shapes.tables()
+    q = Ro.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    w2, g2 = Ro.midpoints_curv(v, f)
+    ocp = Ro.ComParticle([Ro.EpsConst(1.77), Ro.drude_eps()], [Ro.Particle.curved(w2, g2, q)], [[2, 1]], [True])
+    vi, fi = shapes.trisphere(256, 2.0)
+    pw = Ro.PlaneWaveRet([0, 0, 1], [1, 0, 0], Ro.Particle(vi, fi, q))
+    enei = [600.0, 700.0]
+    oext, osca, _, _ = Ro.solve_spectrum(ocp, pw, enei)
+    exc = m.planewave([0, 0, 1], [1, 0, 0])
+    r = m.bemsolver(cp, m.bemoptions(precision="fp64")).spectrum(exc, enei)
+    rm = m.bemsolver(cp, m.bemoptions(precision="mixed")).spectrum(exc, enei)
+    e = {"ext_fp64": rel(r["ext"], oext), "sca_fp64": rel(r["sca"], osca),
+         "ext_mixed": rel(rm["ext"], oext), "sca_mixed": rel(rm["sca"], osca)}
+    record("curved_curvature_midpoints_rod", **e)
+    assert e["ext_fp64"] < 1e-10 and e["sca_fp64"] < 1e-10, e
+    assert e["ext_mixed"] < 1e-8 and e["sca_mixed"] < 1e-8, e
