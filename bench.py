@@ -78,6 +78,16 @@ def step_wavelengths(step, rank, world, batch):
     return grid()[(base + np.arange(batch)) % NGRID]
 
 
+def max_over_ranks(dist, values, device, torch):
+    """Per-rank timings reduced to their maximum over ranks (the slowest rank
+    sets the whole job's time); unchanged without a process group."""
+    if dist is None:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def workload_desc(a):
     return ("sphere d=50 nm, %d flat faces, Drude eps_inf=10 wp=9.065 eV gamma=0.0708 eV in eps=1.77, "
             "x-pol along +z, %d-point wavelength grid 450-750 nm, %d wavelengths per step per GPU"
@@ -311,10 +321,7 @@ def run_ours(a, rank, world, dist, torch):
     h2d = a.batch * (8 + 16 * nmed + 32 * n) + 48 * P + 32 * exc.spec.pinfty.n + 2 * n
     d2h = a.batch * (16 * P * 8 * n + 16 * P + 16)
     # ---------------- max over ranks
-    if dist is not None:
-        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
+    ms, e2e_ms = max_over_ranks(dist, [ms, e2e_ms], "cuda", torch)
     total = a.batch * a.steps * world
     value = total / (ms / 1e3)
     e2e_value = total / (e2e_ms / 1e3)
