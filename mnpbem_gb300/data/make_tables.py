@@ -10,7 +10,11 @@ Both tables are published data that MNPBEM ships as inputs, not code:
   ``Misc/integration/@quadface/private/triangle_unit_set.m:471-505``).
 
 The script reads them out of a MNPBEM checkout (path given on the command
-line) and writes them unchanged into ``tables.npz`` beside this file.  The
+line) and writes them unchanged into ``tables.npz`` beside this file.  It also
+writes ``epstables.npz``: the tabulated optical constants that ``epstable``
+reads (``Material/@epstable/*.dat``: photon energy in eV, n, k per row; gold
+and silver of Johnson and Christy, gold, silver and copper of Palik), one
+``[m, 3]`` float64 array per file, keyed by the file name without ``.dat``.  The
 rule is read by evaluating the scalar assignments and the three vector
 assignments of the ``rule == 18`` branch; nothing else of that file is used.
 
@@ -55,6 +59,26 @@ def _read_spheres(path):
     return sets
 
 
+def read_eps_file(path):
+    """Rows of an ``ene n k`` table; ``%`` starts a comment (the 'matlab'
+    comment style of epstable.m's textread)."""
+    rows = []
+    for line in open(path):
+        line = line.split("%")[0].strip()
+        if line:
+            rows.append([float(t) for t in line.split()[:3]])
+    return np.asarray(rows, dtype=np.float64).reshape(-1, 3)
+
+
+def _write_epstables(root):
+    folder = os.path.join(root, "Material", "@epstable")
+    tabs = {f[:-4]: read_eps_file(os.path.join(folder, f))
+            for f in sorted(os.listdir(folder)) if f.endswith(".dat")}
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "epstables.npz")
+    np.savez_compressed(dst, **tabs)
+    print("wrote", dst, {k: v.shape for k, v in tabs.items()})
+
+
 def main(root):
     x, y, w = _read_rule18(os.path.join(
         root, "Misc", "integration", "@quadface", "private", "triangle_unit_set.m"))
@@ -66,6 +90,7 @@ def main(root):
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tables.npz")
     np.savez_compressed(dst, **arrays)
     print("wrote", dst, "rule weight sum", w.sum(), "sphere sets", sorted(spheres))
+    _write_epstables(root)
 
 
 if __name__ == "__main__":

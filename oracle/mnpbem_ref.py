@@ -42,6 +42,55 @@ class EpsFun:
         return eps, 2 * np.pi / enei * np.sqrt(eps)
 
 
+def spline_not_a_knot(x, y):
+    """Cubic interpolating spline with not-a-knot ends, as MATLAB's
+    ``spline(x, y)`` for four or more distinct sites (used by
+    Material/@epstable/epstable.m:38-39; evaluated like ``ppval``).
+    Restated from the textbook second-derivative form: continuity of the
+    first derivative at the interior sites, and continuity of the third
+    derivative at the second and the last-but-one site.  Returns a function
+    of the evaluation points."""
+    order = np.argsort(x)
+    x, y = np.asarray(x, float)[order], np.asarray(y, float)[order]
+    n = x.size
+    h = np.diff(x)
+    A = np.zeros((n, n))
+    r = np.zeros(n)
+    A[0, 0], A[0, 1], A[0, 2] = h[1], -(h[0] + h[1]), h[0]
+    A[n - 1, n - 3], A[n - 1, n - 2], A[n - 1, n - 1] = h[n - 2], -(h[n - 3] + h[n - 2]), h[n - 3]
+    for i in range(1, n - 1):
+        A[i, i - 1], A[i, i], A[i, i + 1] = h[i - 1], 2 * (h[i - 1] + h[i]), h[i]
+        r[i] = 6 * ((y[i + 1] - y[i]) / h[i] - (y[i] - y[i - 1]) / h[i - 1])
+    M = np.linalg.solve(A, r)
+
+    def ev(t):
+        t = np.asarray(t, float)
+        i = np.clip(np.searchsorted(x, t, side="right") - 1, 0, n - 2)
+        hi, a, b = h[i], x[i + 1] - t, t - x[i]
+        return (M[i] * a ** 3 + M[i + 1] * b ** 3) / (6 * hi) + (y[i] / hi - M[i] * hi / 6) * a \
+            + (y[i + 1] / hi - M[i + 1] * hi / 6) * b
+    return ev
+
+
+class EpsTable:
+    """``epstable(finp)`` (Material/@epstable/epstable.m:34-40, subsref.m:17-26)
+    from rows ``ene n k`` (eV): splines of n and k over ``EV2NM / ene``,
+    eps = (n + ik)^2; wavelengths outside the table are an error."""
+
+    def __init__(self, table):
+        table = np.asarray(table, float)
+        self.enei = EV2NM / table[:, 0]
+        self.n = spline_not_a_knot(self.enei, table[:, 1])
+        self.k = spline_not_a_knot(self.enei, table[:, 2])
+
+    def __call__(self, enei):
+        enei = np.asarray(enei, dtype=float)
+        if enei.min() < self.enei.min() or enei.max() > self.enei.max():
+            raise ValueError("wavelength outside the table")
+        eps = (self.n(enei) + 1j * self.k(enei)) ** 2
+        return eps, 2 * np.pi / enei * np.sqrt(eps)
+
+
 def drude_eps(eps_inf=10.0, wp=9.065, gamma=0.0708):
     """Drude metal as ``epsfun(@(w) eps_inf - wp^2./(w.*(w+1i*gamma)), 'eV')``."""
     return EpsFun(lambda w: eps_inf - wp ** 2 / (w * (w + 1j * gamma)), "eV")
