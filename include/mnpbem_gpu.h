@@ -337,6 +337,25 @@ MNPBEM_API mnpbem_status mnpbem_fields(mnpbem_geom* g, int64_t npts, const doubl
                                        int32_t nmed, int32_t npol, const double* sig1, const double* sig2,
                                        const double* h1, const double* h2, double* e, double* h);
 
+/* Fields and potentials on the particle boundary itself, at the face
+ * centroids on side inout (1 inside, 2 outside; MNPBEM's bemret default is
+ * 2): replaces Greenfun/@compgreenret/field.m:14-38 and potential.m:16-48
+ * as called by BEM/@bemret/field.m:8-11 and potential.m:14-15 ('cart'
+ * derivative).  Faces whose inside (outside) medium is the observation
+ * face's side-inout medium contribute through sig1 / h1 (sig2 / h2);
+ *   E = i k0 (G h1 + G h2) - Hp sig1 - Hp sig2,   H = Hp x h1 + Hp x h2,
+ *   phi = G sig1 + G sig2,   phip = H sig1 + H sig2,   a, ap likewise on h,
+ * with Hp = H1p (H2p) = Gp +- 2 pi nvec [d == 0] and H = nvec . Hp (eval1.m
+ * 140-149), refined pairs from the near-field Taylor coefficients.
+ *   eps_media [nmed] complex; sig1, sig2 [n][npol], h1, h2 [n][3][npol]
+ *   complex, host; npol 1..4
+ *   e, h, a, ap [n][3][npol] and phi, phip [n][npol] complex (host; any may
+ *   be NULL, not all)                                                       */
+MNPBEM_API mnpbem_status mnpbem_surface_fields(mnpbem_geom* g, double enei, const double* eps_media, int32_t nmed,
+                                               int32_t npol, int32_t inout, const double* sig1, const double* sig2,
+                                               const double* h1, const double* h2, double* e, double* h,
+                                               double* phi, double* phip, double* a, double* ap);
+
 /* Cluster tree and block partition of an H-matrix (the arguments
  * Greenfun/hmatrices/@hmatrix/treemex.m hands to the H-matrix MEX functions,
  * mex/hmatgreenret.cpp:21-61, 0-based): clusters in the order of

@@ -326,6 +326,47 @@ class bemret:
 
     solve = mldivide
 
+    def _surface(self, sig, inout, want):
+        if inout not in (1, 2):
+            raise ValueError("inout must be 1 (inside) or 2 (outside)")
+        enei = float(sig.enei)
+        em = np.ascontiguousarray(self.p.eps_media(enei)[0])
+        parts = [np.ascontiguousarray(getattr(sig, k), dtype=np.complex128) for k in ("sig1", "sig2", "h1", "h2")]
+        n, P = parts[0].shape
+        shapes = {"e": (n, 3, P), "h": (n, 3, P), "phi": (n, P), "phip": (n, P), "a": (n, 3, P), "ap": (n, 3, P)}
+        out = {k: np.zeros(shapes[k], np.complex128) for k in want}
+        for c0 in range(0, P, 4):        # mnpbem_surface_fields takes up to four columns per call
+            cols = slice(c0, min(P, c0 + 4))
+            w = cols.stop - cols.start
+            cin = [np.ascontiguousarray(a[..., cols]) for a in parts]
+            cout = {k: np.zeros(shapes[k][:-1] + (w,), np.complex128) for k in want}
+            ptr = [cout[k].ctypes.data if k in cout else None for k in ("e", "h", "phi", "phip", "a", "ap")]
+            _lib.check(self._lib.mnpbem_surface_fields(
+                self._h, enei, em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, w, inout,
+                *[a.ctypes.data for a in cin], *ptr))
+            for k in want:
+                out[k][..., cols] = cout[k]
+        return out
+
+    def field(self, sig, inout=2):
+        """Electric and magnetic fields at the face centroids on side
+        ``inout`` (1 inside, 2 outside, the default of BEM/@bemret/field.m),
+        from ``sig = bem \\ exc``: compgreenret field.m on the particle itself,
+        by ``mnpbem_surface_fields``.  Returns ``compstruct(p, enei, e=[n, 3,
+        npol], h=[n, 3, npol])``; the incoming field is not included."""
+        r = self._surface(sig, inout, ("e", "h"))
+        return compstruct(self.p, sig.enei, e=r["e"], h=r["h"])
+
+    def potential(self, sig, inout=2):
+        """Scalar and vector potentials and their surface derivatives at the
+        faces on side ``inout`` (BEM/@bemret/potential.m -> compgreenret
+        potential.m:16-48): ``compstruct`` with ``phi1, phi1p, a1, a1p``
+        (inout = 1) or ``phi2, phi2p, a2, a2p`` (inout = 2)."""
+        r = self._surface(sig, inout, ("phi", "phip", "a", "ap"))
+        s = str(inout)
+        return compstruct(self.p, sig.enei, **{"phi" + s: r["phi"], "phi" + s + "p": r["phip"],
+                                               "a" + s: r["a"], "a" + s + "p": r["ap"]})
+
     def _solve_potentials(self, exc):
         enei = float(exc.enei)
         n = self.p.n

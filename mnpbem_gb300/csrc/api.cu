@@ -1966,6 +1966,55 @@ mnpbem_status mnpbem_fields(mnpbem_geom* G, int64_t npts, const double* pts, con
   return MNPBEM_OK;
 }
 
+mnpbem_status mnpbem_surface_fields(mnpbem_geom* G, double enei, const double* eps_media, int32_t nmed,
+                                    int32_t npol, int32_t inout, const double* sig1, const double* sig2,
+                                    const double* h1, const double* h2, double* e, double* h, double* phi,
+                                    double* phip, double* a, double* ap) {
+  MNP_TRY(check_geom(G));
+  if (!(enei > 0) || !eps_media || nmed < G->max_medium || npol < 1 || (inout != 1 && inout != 2) ||
+      !sig1 || !sig2 || !h1 || !h2 || (!e && !h && !phi && !phip && !a && !ap)) {
+    set_error("mnpbem_surface_fields: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if (npol > 4) { set_error("mnpbem_surface_fields: npol must be 1..4"); return MNPBEM_ERR_UNSUPPORTED; }
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  const int64_t n = G->g.n;
+  const double k0 = 2 * M_PI / enei;
+  std::vector<double2> km(nmed);
+  for (int m = 0; m < nmed; ++m) {
+    const std::complex<double> kk = k0 * std::sqrt(std::complex<double>(eps_media[2 * m], eps_media[2 * m + 1]));
+    km[m] = make_double2(kk.real(), kk.imag());
+  }
+  // inputs: sig1, sig2 [n][npol], h1, h2 [n][3][npol]; outputs: e, h, a, ap
+  // [n][3][npol], phi, phip [n][npol]; the wavenumbers of the media last
+  DevBuf buf;
+  const int64_t np = n * npol;
+  MNP_TRY(buf.ensure(sizeof(double2) * (8 * np + 14 * np + nmed)));
+  double2* S = buf.as<double2>();
+  double2 *s1 = S, *s2 = S + np, *q1 = S + 2 * np, *q2 = S + 5 * np, *O = S + 8 * np;
+  double2 *de = O, *dh = O + 3 * np, *dphi = O + 6 * np, *dphip = O + 7 * np, *da = O + 8 * np, *dap = O + 11 * np;
+  double2* dk = O + 14 * np;
+  cudaStream_t st = G->st;
+  MNP_CUDA(cudaMemcpyAsync(s1, sig1, sizeof(double2) * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(s2, sig2, sizeof(double2) * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q1, h1, sizeof(double2) * 3 * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q2, h2, sizeof(double2) * 3 * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(dk, km.data(), sizeof(double2) * nmed, cudaMemcpyHostToDevice, st));
+  MNP_TRY(surface_fields(G->g, G->face_med.as<int>(), dk, k0, npol, inout - 1, s1, s2, q1, q2,
+                         e ? de : nullptr, h ? dh : nullptr, phi ? dphi : nullptr, phip ? dphip : nullptr,
+                         a ? da : nullptr, ap ? dap : nullptr, st));
+  if (e) MNP_CUDA(cudaMemcpyAsync(e, de, sizeof(double2) * 3 * np, cudaMemcpyDeviceToHost, st));
+  if (h) MNP_CUDA(cudaMemcpyAsync(h, dh, sizeof(double2) * 3 * np, cudaMemcpyDeviceToHost, st));
+  if (phi) MNP_CUDA(cudaMemcpyAsync(phi, dphi, sizeof(double2) * np, cudaMemcpyDeviceToHost, st));
+  if (phip) MNP_CUDA(cudaMemcpyAsync(phip, dphip, sizeof(double2) * np, cudaMemcpyDeviceToHost, st));
+  if (a) MNP_CUDA(cudaMemcpyAsync(a, da, sizeof(double2) * 3 * np, cudaMemcpyDeviceToHost, st));
+  if (ap) MNP_CUDA(cudaMemcpyAsync(ap, dap, sizeof(double2) * 3 * np, cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  G->prof.flush();
+  return MNPBEM_OK;
+}
+
 mnpbem_status mnpbem_solve_potentials(mnpbem_geom* G, const mnpbem_potentials* pot, double enei,
                                       const double* eps_media, int32_t nmed, int32_t precision,
                                       const mnpbem_refine* refine, mnpbem_solution* out) {

@@ -224,4 +224,174 @@ mnpbem_status point_fields(const GeomDev& g, const int* face_med, int64_t npts, 
   return MNPBEM_OK;
 }
 
+// ------------------------------------------------------------------------
+// Fields and potentials on the boundary itself (Greenfun/@compgreenret/
+// field.m:14-38 and potential.m:16-48 with p1 = p2 = the particle): the
+// observation point of row i is face i's centroid on side `side` (0 inside,
+// 1 outside), its medium face_med[side][i].  Per pair (i, j)
+//     Hp = Gp + s 2 pi n_i [d == 0]      (H1p, s = +1, inside; H2p, s = -1)
+//     E  = i k0 (G h1 + G h2) - Hp sig1 - Hp sig2,   H = Hp x h1 + Hp x h2
+//     phi = G sig,  phip = (n_i . Hp) sig,  a = G h,  ap = (n_i . Hp) h
+// over the faces j whose side-1 (side-2) medium is the observation medium;
+// n_i . Hp equals F +- 2 pi [d == 0], the H1 / H2 of eval1.m:140-143.  Refined
+// pairs use the face-pair Taylor coefficients of the geometry (column j's rows
+// are ascending: binary search), including the closed-surface diagonal.
+
+struct SurfArgs {
+  GeomDev g;
+  const int* face_med;   // [2][n] 0-based
+  const double2* kmed;
+  double k0;
+  int npol, side;
+  const double2 *sig1, *sig2, *h1, *h2;
+  double2 *e, *h;               // [n][3][npol]      (field pass)
+  double2 *phi, *phip, *a, *ap; // [n][npol], [n][3][npol] (potential pass)
+};
+
+__device__ __forceinline__ void surf_pair(const SurfArgs& a, int i, int j, double3 p, double3 ni, double2 k,
+                                          double2 ik, double2& G, double2* Hp) {
+  const GeomDev& g = a.g;
+  const int O = g.order;
+  const double3 v = sub3(p, ld3(g.pos, j));
+  const double dt = sqrt(dot3(v, v));
+  const double d = fmax(dt, DBL_EPS);
+  double sn, cs;
+  sincos(k.x * d, &sn, &cs);
+  const double ee = exp(-k.y * d);
+  const double2 ph = make_double2(ee * cs, ee * sn);
+  int64_t lo = g.col_off[j], hi = g.col_off[j + 1];
+  const int64_t end = hi;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (g.ref_row[mid] < i) lo = mid + 1; else hi = mid;
+  }
+  if (lo < end && g.ref_row[lo] == i) {
+    const double* cg = g.ref_g + lo * (O + 1);
+    const double* cf = g.ref_f + lo * 3 * (O + 1);
+    double2 pw = make_double2(1, 0), gs = make_double2(0, 0), fs[3] = {gs, gs, gs};
+    for (int o = 0; o <= O; ++o) {
+      gs.x += cg[o] * pw.x; gs.y += cg[o] * pw.y;
+      for (int c = 0; c < 3; ++c) { fs[c].x += cf[c * (O + 1) + o] * pw.x; fs[c].y += cf[c * (O + 1) + o] * pw.y; }
+      pw = cmul(pw, ik);
+    }
+    G = cmul(gs, ph);
+    for (int c = 0; c < 3; ++c) Hp[c] = cmul(fs[c], ph);
+  } else {
+    const double A = g.area[j], inv = 1.0 / d;
+    G = make_double2(A * inv * ph.x, A * inv * ph.y);
+    const double2 t = cmul(make_double2(-k.y - inv, k.x), ph);
+    const double s = A * inv * inv;
+    const double vc[3] = {v.x, v.y, v.z};
+    for (int c = 0; c < 3; ++c) Hp[c] = make_double2(t.x * s * vc[c], t.y * s * vc[c]);
+  }
+  if (dt <= DBL_EPS) {     // d == 0 after d = max(d, eps): the +-2 pi term
+    const double tp = a.side == 0 ? 2 * M_PI : -2 * M_PI;
+    Hp[0].x += tp * ni.x; Hp[1].x += tp * ni.y; Hp[2].x += tp * ni.z;
+  }
+}
+
+// one block (4 warps) per observation face; POT selects the potential pass
+template <bool POT>
+__global__ void __launch_bounds__(128) k_surf(SurfArgs a) {
+  constexpr int NC = POT ? 8 : 6;   // phi, phip, a(3), ap(3)  |  E(3), H(3)
+  const int i = blockIdx.x;
+  const GeomDev& g = a.g;
+  const int n = g.n, P = a.npol;
+  const int med = a.face_med[a.side * n + i];
+  const double2 k = a.kmed[med];
+  const double2 ik = make_double2(-k.y, k.x);
+  const double3 p = ld3(g.pos, i), ni = ld3(g.nvec, i);
+  double2 acc[NC][FLD_MAXPOL];
+  for (int c = 0; c < NC; ++c)
+    for (int q = 0; q < FLD_MAXPOL; ++q) acc[c][q] = make_double2(0, 0);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const bool s1 = a.face_med[j] == med, s2 = a.face_med[n + j] == med;
+    if (!s1 && !s2) continue;
+    double2 G, Hp[3];
+    surf_pair(a, i, j, p, ni, k, ik, G, Hp);
+    const double2 Hn = cadd(cadd(make_double2(ni.x * Hp[0].x, ni.x * Hp[0].y),
+                                 make_double2(ni.y * Hp[1].x, ni.y * Hp[1].y)),
+                            make_double2(ni.z * Hp[2].x, ni.z * Hp[2].y));
+    const double2 ik0G = make_double2(-a.k0 * G.y, a.k0 * G.x);
+    for (int sd = 0; sd < 2; ++sd) {
+      if (!(sd == 0 ? s1 : s2)) continue;
+      const double2* sg = sd == 0 ? a.sig1 : a.sig2;
+      const double2* hh = sd == 0 ? a.h1 : a.h2;
+#pragma unroll
+      for (int q = 0; q < FLD_MAXPOL; ++q) {
+        if (q >= P) break;
+        const double2 sv = sg[(int64_t)j * P + q];
+        double2 hv[3];
+        for (int c = 0; c < 3; ++c) hv[c] = hh[((int64_t)j * 3 + c) * P + q];
+        if (POT) {
+          acc[0][q] = cadd(acc[0][q], cmul(G, sv));
+          acc[1][q] = cadd(acc[1][q], cmul(Hn, sv));
+          for (int c = 0; c < 3; ++c) {
+            acc[2 + c][q] = cadd(acc[2 + c][q], cmul(G, hv[c]));
+            acc[5 + c][q] = cadd(acc[5 + c][q], cmul(Hn, hv[c]));
+          }
+        } else {
+          for (int c = 0; c < 3; ++c) acc[c][q] = csub(cadd(acc[c][q], cmul(ik0G, hv[c])), cmul(Hp[c], sv));
+          acc[3][q] = cadd(acc[3][q], csub(cmul(Hp[1], hv[2]), cmul(Hp[2], hv[1])));
+          acc[4][q] = cadd(acc[4][q], csub(cmul(Hp[2], hv[0]), cmul(Hp[0], hv[2])));
+          acc[5][q] = cadd(acc[5][q], csub(cmul(Hp[0], hv[1]), cmul(Hp[1], hv[0])));
+        }
+      }
+    }
+  }
+  // fixed-order block reduction: warp shuffles, then the four warps in order
+  __shared__ double2 red[4][NC * FLD_MAXPOL];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+#pragma unroll
+    for (int q = 0; q < FLD_MAXPOL; ++q) {
+      double2 v = acc[c][q];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[wid][c * FLD_MAXPOL + q] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < NC * P; t += blockDim.x) {
+    const int c = t / P, q = t % P;
+    double2 s = make_double2(0, 0);
+    for (int w = 0; w < 4; ++w) s = cadd(s, red[w][c * FLD_MAXPOL + q]);
+    double2* out;
+    int64_t at;
+    if (POT) {
+      if (c < 2) { out = c == 0 ? a.phi : a.phip; at = (int64_t)i * P + q; }
+      else { out = c < 5 ? a.a : a.ap; at = ((int64_t)i * 3 + (c - 2) % 3) * P + q; }
+    } else {
+      out = c < 3 ? a.e : a.h;
+      at = ((int64_t)i * 3 + c % 3) * P + q;
+    }
+    if (out) out[at] = s;
+  }
+}
+
+mnpbem_status surface_fields(const GeomDev& g, const int* face_med, const double2* kmed, double k0, int npol,
+                             int side, const double2* sig1, const double2* sig2, const double2* h1,
+                             const double2* h2, double2* e, double2* h, double2* phi, double2* phip,
+                             double2* av, double2* ap, cudaStream_t st) {
+  if (g.n <= 0) return MNPBEM_OK;
+  if (npol < 1 || npol > FLD_MAXPOL) { set_error("surface fields: npol must be 1..%d", FLD_MAXPOL); return MNPBEM_ERR_UNSUPPORTED; }
+  if (side != 0 && side != 1) { set_error("surface fields: inout must be 1 or 2"); return MNPBEM_ERR_INVALID_ARG; }
+  ProfScope ps(PH_SPECTRA, st, 0.0, 0.0, (e || h) && (phi || phip || av || ap) ? 2 : 1);
+  SurfArgs a;
+  a.g = g; a.face_med = face_med; a.kmed = kmed; a.k0 = k0; a.npol = npol; a.side = side;
+  a.sig1 = sig1; a.sig2 = sig2; a.h1 = h1; a.h2 = h2;
+  a.e = e; a.h = h; a.phi = phi; a.phip = phip; a.a = av; a.ap = ap;
+  if (e || h) {
+    k_surf<false><<<(unsigned)g.n, 128, 0, st>>>(a);
+    MNP_CHECK_LAUNCH();
+  }
+  if (phi || phip || av || ap) {
+    k_surf<true><<<(unsigned)g.n, 128, 0, st>>>(a);
+    MNP_CHECK_LAUNCH();
+  }
+  return MNPBEM_OK;
+}
+
 }  // namespace mnpbem

@@ -14,4 +14,13 @@ mnpbem_status point_fields(const GeomDev& g, const int* face_med, int64_t npts, 
                            const double2* sig1, const double2* sig2, const double2* h1, const double2* h2,
                            double2* e, double2* h, double rel_cut, double abs_cut, cudaStream_t st);
 
+// Fields E, H [n][3][npol] and potentials phi, phip [n][npol], a, ap
+// [n][3][npol] (device, complex128; any output may be null) at the faces on
+// side `side` (0 inside, 1 outside) from the surface charges and currents
+// (device); kmed [nmed] device wavenumbers of the media.
+mnpbem_status surface_fields(const GeomDev& g, const int* face_med, const double2* kmed, double k0, int npol,
+                             int side, const double2* sig1, const double2* sig2, const double2* h1,
+                             const double2* h2, double2* e, double2* h, double2* phi, double2* phip,
+                             double2* av, double2* ap, cudaStream_t st);
+
 }  // namespace mnpbem

@@ -838,6 +838,29 @@ class GreenRet:
         return G * ph, F * ph, d == EPS
 
 
+def _eval_gp(gr, k, rows, cols):
+    """Cartesian derivative Gp [rows, 3, cols] of greenret (eval1.m:86-102,
+    'cart'): (ik - 1/d)/d^2 * A_j * (r_i - r_j), refined entries
+    f @ (ik)^o, all times exp(ik d); and the d == 0 mask."""
+    p = gr.p
+    x = p.pos[rows, 0][:, None] - p.pos[cols, 0][None, :]
+    y = p.pos[rows, 1][:, None] - p.pos[cols, 1][None, :]
+    z = p.pos[rows, 2][:, None] - p.pos[cols, 2][None, :]
+    d = np.maximum(np.sqrt(x ** 2 + y ** 2 + z ** 2), EPS)
+    ff = (1j * k - 1.0 / d) / d ** 2 * p.area[cols][None, :]
+    Gp = np.stack([ff * x, ff * y, ff * z], 1)
+    n = p.n
+    rpos = np.full(n, -1)
+    rpos[rows] = np.arange(rows.size)
+    cpos = np.full(n, -1)
+    cpos[cols] = np.arange(cols.size)
+    sel = (rpos[gr.rows] >= 0) & (cpos[gr.cols] >= 0)
+    if np.any(sel):
+        fr = (1j * k) ** np.arange(gr.order + 1)
+        Gp[rpos[gr.rows[sel]], :, cpos[gr.cols[sel]]] = gr.f[sel] @ fr
+    return Gp * np.exp(1j * k * d)[:, None, :], d == EPS
+
+
 def initclosed(gr, cp):
     """Fuchs-Liu sum rule on the order-0 diagonal (initclosed.m:19-89)."""
     for i in range(len(cp.parts)):
@@ -885,6 +908,83 @@ class CompGreenRet:
         if not any_block or not np.any(out):
             return 0
         return out
+
+
+    # compgreenret eval of 'Gp', 'H1p', 'H2p' (eval1.m:144-149; H1p = Gp + 2 pi
+    # outer(nvec, d == 0), H2p with -2 pi); 0 where no block connects
+    def eval_p(self, a, b, key, enei):
+        cp = self.p
+        k = np.array([e(enei)[1] for e in cp.eps], dtype=complex)
+        con = self.con[a][b]
+        out = np.zeros((cp.n, 3, cp.n), dtype=complex)
+        any_block = False
+        for i1 in range(con.shape[0]):
+            for i2 in range(con.shape[1]):
+                if con[i1, i2]:
+                    any_block = True
+                    r, c = cp.index(i1), cp.index(i2)
+                    Gp, dz = _eval_gp(self.g, k[con[i1, i2] - 1], r, c)
+                    if key != "Gp":
+                        sgn = 2 * np.pi if key == "H1p" else -2 * np.pi
+                        Gp = Gp + sgn * cp.nvec[r][:, :, None] * dz[:, None, :]
+                    out[np.ix_(r, np.arange(3), c)] = Gp
+        if not any_block or not np.any(out):
+            return 0
+        return out
+
+
+def _cross_p(Gp, h):
+    """field.m:41-57: Gp x h for Gp [n, 3, n'] and h [n', 3, npol]."""
+    if np.isscalar(Gp):
+        return 0
+    return np.stack([Gp[:, 1] @ h[:, 2] - Gp[:, 2] @ h[:, 1],
+                     Gp[:, 2] @ h[:, 0] - Gp[:, 0] @ h[:, 2],
+                     Gp[:, 0] @ h[:, 1] - Gp[:, 1] @ h[:, 0]], 1)
+
+
+def _mm(a, x):
+    """matmul.m for a Green block: 0, [n, n'] @ [n', ...] or Gp [n, 3, n'] @ [n', npol]."""
+    if np.isscalar(a):
+        return 0
+    if a.ndim == 3:
+        return np.einsum("icj,jp->icp", a, x)
+    return (a @ x.reshape(x.shape[0], -1)).reshape((a.shape[0],) + x.shape[1:])
+
+
+def surface_field(g, enei, sig1, sig2, h1, h2, inout=2):
+    """E and H at the faces, on side ``inout`` (1 inside, 2 outside), from the
+    surface charges and currents (Greenfun/@compgreenret/field.m:14-38):
+    E = i k0 (G{inout,1} h1 + G{inout,2} h2) - H{inout}p{inout,1} sig1 - ...,
+    H = Hp1 x h1 + Hp2 x h2, with H1p for inout = 1 and H2p for inout = 2.
+    Returns ``e, h [n, 3, npol]``."""
+    k0 = 2 * np.pi / enei
+    a, key = inout - 1, ("H1p" if inout == 1 else "H2p")
+    G1, G2 = g.eval(a, 0, "G", enei), g.eval(a, 1, "G", enei)
+    P1, P2 = g.eval_p(a, 0, key, enei), g.eval_p(a, 1, key, enei)
+    e = 1j * k0 * (_mm(G1, h1) + _mm(G2, h2)) - _mm(P1, sig1) - _mm(P2, sig2)
+    h = _cross_p(P1, h1) + _cross_p(P2, h2)
+    n, P = sig1.shape
+    return np.broadcast_to(e, (n, 3, P)).copy(), np.broadcast_to(h, (n, 3, P)).copy()
+
+
+def surface_potential(g, enei, sig1, sig2, h1, h2, inout=2):
+    """Potentials and their surface derivatives at the faces, on side
+    ``inout`` (Greenfun/@compgreenret/potential.m:16-48): phi = G1 sig1 +
+    G2 sig2, phip = H1 sig1 + H2 sig2, a = G1 h1 + G2 h2, ap = H1 h1 + H2 h2
+    with the blocks {inout, 1}, {inout, 2} and H = 'H1' (inout = 1) or 'H2'.
+    Returns ``phi, phip [n, npol]`` and ``a, ap [n, 3, npol]``."""
+    a, key = inout - 1, ("H1" if inout == 1 else "H2")
+    G1, G2 = g.eval(a, 0, "G", enei), g.eval(a, 1, "G", enei)
+    H1, H2 = g.eval(a, 0, key, enei), g.eval(a, 1, key, enei)
+    n, P = sig1.shape
+    phi = _matmul(G1, sig1) + _matmul(G2, sig2)
+    phip = _matmul(H1, sig1) + _matmul(H2, sig2)
+    av = _matmul(G1, h1) + _matmul(G2, h2)
+    ap = _matmul(H1, h1) + _matmul(H2, h2)
+
+    def full(x, shape):
+        return np.broadcast_to(x, shape).astype(complex)
+    return (full(phi, (n, P)), full(phip, (n, P)), full(av, (n, 3, P)), full(ap, (n, 3, P)))
 
 
 # --------------------------------------------------------------------------
