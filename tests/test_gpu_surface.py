@@ -6,8 +6,9 @@ with one medium per sphere, two polarisations, inside and outside.
 Tolerance 1e-10 of the largest entry, that of the FP64 matrices: the
 singular self coefficient g0 of flat elements (a sum over the polar points
 around the centroid) differs from the oracle's by about 1e-11 of the largest
-G entry, which the G-based outputs (phi, a, E, H: measured 2e-13 - 1.5e-12)
-inherit; the H-based ones (phip, ap) agree to 1e-14.  The GPU fields must
+G entry, which the G-based outputs (phi, a, E, H: measured 1e-13 - 4.3e-12)
+inherit; the H-based ones (phip, ap) agree to 1e-14, and with curved
+elements every output agrees to 1e-14.  The GPU fields must
 also keep the normal D continuous (1e-10)."""
 import os
 
