@@ -367,6 +367,15 @@ class bemret:
         return compstruct(self.p, sig.enei, **{"phi" + s: r["phi"], "phi" + s + "p": r["phip"],
                                                "a" + s: r["a"], "a" + s + "p": r["ap"]})
 
+    def mtimes(self, sig):
+        """phi = bem * sig (BEM/@bemret/mtimes.m): the potentials of both
+        sides, ``compstruct`` with phi1, phi1p, a1, a1p, phi2, phi2p, a2, a2p."""
+        p1, p2 = self.potential(sig, 1), self.potential(sig, 2)
+        fields = {k: v for q in (p1, p2) for k, v in q.__dict__.items() if k not in ("p", "enei")}
+        return compstruct(self.p, sig.enei, **fields)
+
+    __mul__ = mtimes
+
     def _solve_potentials(self, exc):
         enei = float(exc.enei)
         n = self.p.n

@@ -79,3 +79,22 @@ def test_surface_fields_and_potentials_match_oracle(gpu_lib, name):
     dn1 = eps_in[:, None] * np.sum(nv * e1, 1)
     dn2 = 1.77 * np.sum(nv * (e2 + inc), 1)
     assert rel(dn1, dn2) < 1e-10, rel(dn1, dn2)
+
+
+def test_mtimes_inverts_mldivide(gpu_lib):
+    """bem * (bem \\ exc) gives the potentials of the charges on both sides
+    (mtimes.m), which with the external ones are continuous across the
+    boundary: phi1 = phi2, a1 = a2 + a_ext for a plane wave from outside."""
+    cp = dict(cases())["sphere"]
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64"))
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    enei = 560.0
+    sig = bem.mldivide(exc(cp, enei))
+    phi = bem * sig
+    pot2 = bem.potential(sig, 2)
+    assert np.array_equal(phi.a2, pot2.a2) and np.array_equal(phi.phi2p, pot2.phi2p)
+    k0 = 2 * np.pi / enei
+    a_ext = (np.array([1.0, 0, 0])[None, :] * np.exp(1j * k0 * np.sqrt(1.77) * cp.pos[:, 2])[:, None]
+             / (1j * k0))[:, :, None]
+    assert rel(phi.phi1, phi.phi2) < 1e-10
+    assert rel(phi.a1, phi.a2 + a_ext) < 1e-10
