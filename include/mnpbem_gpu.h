@@ -337,6 +337,19 @@ MNPBEM_API mnpbem_status mnpbem_fields(mnpbem_geom* g, int64_t npts, const doubl
                                        int32_t nmed, int32_t npol, const double* sig1, const double* sig2,
                                        const double* h1, const double* h2, double* e, double* h);
 
+/* Far fields of the surface charges and currents in the unit directions
+ * dirs [ndir][3] (replaces Simulation/retarded/@spectrumret/farfield.m:15-74):
+ * with ph_j = exp(-i k dir . r_j) A_j over the faces whose inside (outside)
+ * medium is `medium` (1-based; k its wavenumber), through sig1 / h1 (sig2 /
+ * h2):  e = i k0 sum ph h - i k dir sum ph sig,  h = i k dir x sum ph h.
+ *   eps_media [nmed] complex; sig1, sig2 [n][npol], h1, h2 [n][3][npol]
+ *   complex, host; npol 1..4
+ *   e, h [ndir][3][npol] complex (host; either may be NULL)                  */
+MNPBEM_API mnpbem_status mnpbem_farfield(mnpbem_geom* g, double enei, const double* eps_media, int32_t nmed,
+                                         int32_t medium, int64_t ndir, const double* dirs, int32_t npol,
+                                         const double* sig1, const double* sig2, const double* h1,
+                                         const double* h2, double* e, double* h);
+
 /* Fields and potentials on the particle boundary itself, at the face
  * centroids on side inout (1 inside, 2 outside; MNPBEM's bemret default is
  * 2): replaces Greenfun/@compgreenret/field.m:14-38 and potential.m:16-48

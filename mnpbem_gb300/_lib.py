@@ -109,6 +109,9 @@ SIGNATURES = {
                                      c_double_p, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 6),
     "mnpbem_surface_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 10),
+    "mnpbem_farfield": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p, ctypes.c_int32,
+                                       ctypes.c_int32, ctypes.c_int64, c_double_p, ctypes.c_int32]
+                        + [ctypes.c_void_p] * 6),
     "mnpbem_geom_size": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p]),
     "mnpbem_geom_export": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 9),
     "mnpbem_assemble": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int32, ctypes.c_int32,

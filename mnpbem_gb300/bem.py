@@ -47,6 +47,32 @@ class spectrumret:
         self.pinfty = pinfty if pinfty is not None else trisphere(256, 2)
         self.medium = medium
 
+    def farfield(self, bem, sig, dir=None):
+        """Far fields of ``sig = bem \\ exc`` in the unit directions ``dir
+        [ndir, 3]`` (default: the normals of the sphere at infinity), in this
+        spectrum's medium (@spectrumret/farfield.m:15-74), by
+        ``mnpbem_farfield``; ``bem`` is the solver that holds the particle.
+        Returns ``compstruct`` with ``e, h [ndir, 3, npol]``."""
+        dirs = np.ascontiguousarray(self.nvec if dir is None else np.atleast_2d(dir), dtype=np.float64)
+        enei = float(sig.enei)
+        em = np.ascontiguousarray(bem.p.eps_media(enei)[0])
+        parts = [np.ascontiguousarray(getattr(sig, k), dtype=np.complex128) for k in ("sig1", "sig2", "h1", "h2")]
+        P = parts[0].shape[1]
+        nd = dirs.shape[0]
+        e = np.zeros((nd, 3, P), np.complex128)
+        h = np.zeros((nd, 3, P), np.complex128)
+        for c0 in range(0, P, 4):        # up to four columns per call
+            cols = slice(c0, min(P, c0 + 4))
+            w = cols.stop - cols.start
+            cin = [np.ascontiguousarray(a[..., cols]) for a in parts]
+            ec = np.zeros((nd, 3, w), np.complex128)
+            hc = np.zeros((nd, 3, w), np.complex128)
+            _lib.check(bem._lib.mnpbem_farfield(
+                bem._h, enei, em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, self.medium, nd,
+                _lib.dptr(dirs), w, *[a.ctypes.data for a in cin], ec.ctypes.data, hc.ctypes.data))
+            e[..., cols], h[..., cols] = ec, hc
+        return compstruct(bem.p, enei, e=e, h=h)
+
     @property
     def nvec(self):
         return np.ascontiguousarray(self.pinfty.nvec, dtype=np.float64)
@@ -485,28 +511,18 @@ class dipoleret:
                     f["a" + sfx + "p"][ind, :, col] = -1j * k0 * d[None, :] * (en * F)[:, None]
         return compstruct(p, enei, **f)
 
-    def _farfields(self, p, sig):
-        """Far fields of the induced charges and of the dipoles on the unit
-        sphere at infinity."""
+    def _farfields(self, bem, sig):
+        """Far fields of the induced charges (``mnpbem_farfield``) and of the
+        dipoles themselves (farfield.m:11-55, closed form) on the unit sphere
+        at infinity."""
+        p = bem.p
         enei = float(sig.enei)
         dirs, med = self.spec.nvec, self.spec.medium
         eps = p.eps_media(enei)[0][med - 1]
         k0 = 2 * np.pi / enei
         k = k0 * np.sqrt(eps)
-        fmed = np.repeat(p.inout, [q.n for q in p.p], axis=0)
-        phase = np.exp(-1j * k * dirs @ p.pos.T) * p.area[None, :]
-        P = sig.sig1.shape[1]
-        e = np.zeros((dirs.shape[0], 3, P), np.complex128)
-        h = np.zeros_like(e)
-        for side, (ks, kh) in enumerate((("sig1", "h1"), ("sig2", "h2"))):
-            ind = np.nonzero(fmed[:, side] == med)[0]
-            if ind.size == 0:
-                continue
-            ph = phase[:, ind]
-            Ph = np.einsum("dn,nkp->dkp", ph, getattr(sig, kh)[ind])
-            Ps = ph @ getattr(sig, ks)[ind]
-            e += 1j * k0 * Ph - 1j * k * dirs[:, :, None] * Ps[:, None, :]
-            h += 1j * k * np.cross(np.broadcast_to(dirs[:, :, None], Ph.shape), Ph, axis=1)
+        ff = self.spec.farfield(bem, sig)
+        e, h = ff.e, ff.h
         npt, ndip = self.dip.shape[0], self.dip.shape[2]
         for ipt in range(npt):
             if self.medium[ipt] != med:
@@ -527,7 +543,7 @@ class dipoleret:
         k0 = 2 * np.pi / enei
         gamma = 4.0 / 3.0 * k0 ** 3
         e, _ = meshfield(bem, self.pos, medium=self.medium)(sig)              # [npt, 3, P]
-        ef, hf = self._farfields(p, sig)
+        ef, hf = self._farfields(bem, sig)
         flux = 0.5 * np.real(np.einsum("dc,dcp->dp", self.spec.nvec, np.cross(ef, np.conj(hf), axis=1)))
         sca = self.spec.area @ flux
         npt, ndip = self.dip.shape[0], self.dip.shape[2]

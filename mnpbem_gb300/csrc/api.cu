@@ -2015,6 +2015,43 @@ mnpbem_status mnpbem_surface_fields(mnpbem_geom* G, double enei, const double* e
   return MNPBEM_OK;
 }
 
+mnpbem_status mnpbem_farfield(mnpbem_geom* G, double enei, const double* eps_media, int32_t nmed, int32_t medium,
+                              int64_t ndir, const double* dirs, int32_t npol, const double* sig1,
+                              const double* sig2, const double* h1, const double* h2, double* e, double* h) {
+  MNP_TRY(check_geom(G));
+  if (!(enei > 0) || !eps_media || nmed < G->max_medium || medium < 1 || medium > nmed || ndir <= 0 ||
+      ndir > ((int64_t)1 << 30) || !dirs || npol < 1 || !sig1 || !sig2 || !h1 || !h2 || (!e && !h)) {
+    set_error("mnpbem_farfield: invalid arguments");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  if (npol > 4) { set_error("mnpbem_farfield: npol must be 1..4"); return MNPBEM_ERR_UNSUPPORTED; }
+  MNP_CUDA(cudaSetDevice(G->device));
+  ProfBind pb_(&G->prof);
+  const int64_t n = G->g.n, np = n * npol, nd = ndir * npol;
+  const double k0 = 2 * M_PI / enei;
+  const std::complex<double> kk =
+      k0 * std::sqrt(std::complex<double>(eps_media[2 * (medium - 1)], eps_media[2 * (medium - 1) + 1]));
+  // inputs sig1, sig2 [n][npol], h1, h2 [n][3][npol]; outputs e, h [ndir][3][npol]; directions last
+  DevBuf buf;
+  MNP_TRY(buf.ensure(sizeof(double2) * (8 * np + 6 * nd) + sizeof(double) * 3 * ndir));
+  double2* S = buf.as<double2>();
+  double2 *s1 = S, *s2 = S + np, *q1 = S + 2 * np, *q2 = S + 5 * np, *de = S + 8 * np, *dh = de + 3 * nd;
+  double* dd = reinterpret_cast<double*>(dh + 3 * nd);
+  cudaStream_t st = G->st;
+  MNP_CUDA(cudaMemcpyAsync(s1, sig1, sizeof(double2) * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(s2, sig2, sizeof(double2) * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q1, h1, sizeof(double2) * 3 * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(q2, h2, sizeof(double2) * 3 * np, cudaMemcpyHostToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(dd, dirs, sizeof(double) * 3 * ndir, cudaMemcpyHostToDevice, st));
+  MNP_TRY(far_fields(G->g, G->face_med.as<int>(), medium - 1, make_double2(kk.real(), kk.imag()), k0, npol,
+                     (int)ndir, dd, s1, s2, q1, q2, e ? de : nullptr, h ? dh : nullptr, st));
+  if (e) MNP_CUDA(cudaMemcpyAsync(e, de, sizeof(double2) * 3 * nd, cudaMemcpyDeviceToHost, st));
+  if (h) MNP_CUDA(cudaMemcpyAsync(h, dh, sizeof(double2) * 3 * nd, cudaMemcpyDeviceToHost, st));
+  MNP_CUDA(cudaStreamSynchronize(st));
+  G->prof.flush();
+  return MNPBEM_OK;
+}
+
 mnpbem_status mnpbem_solve_potentials(mnpbem_geom* G, const mnpbem_potentials* pot, double enei,
                                       const double* eps_media, int32_t nmed, int32_t precision,
                                       const mnpbem_refine* refine, mnpbem_solution* out) {

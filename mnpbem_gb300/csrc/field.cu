@@ -394,4 +394,103 @@ mnpbem_status surface_fields(const GeomDev& g, const int* face_med, const double
   return MNPBEM_OK;
 }
 
+// ------------------------------------------------------------------------
+// Far fields of the surface charges and currents in given directions
+// (Simulation/retarded/@spectrumret/farfield.m:15-74): with the phase
+// ph_j = exp(-i k dir . r_j) A_j over the faces whose inside (outside) medium
+// is the embedding medium, through sig1 / h1 (sig2 / h2),
+//     e = i k0 sum ph h - i k dir sum ph sig,   h = i k dir x sum ph h.
+struct FarArgs {
+  GeomDev g;
+  const int* face_med;   // [2][n] 0-based
+  int med;               // 0-based embedding medium
+  double2 k;             // its wavenumber
+  double k0;
+  int npol;
+  const double* dirs;    // [ndir][3]
+  const double2 *sig1, *sig2, *h1, *h2;
+  double2 *e, *h;        // [ndir][3][npol]
+};
+
+// one block (4 warps) per direction
+__global__ void __launch_bounds__(128) k_far_dirs(FarArgs a) {
+  const int d = blockIdx.x;
+  const GeomDev& g = a.g;
+  const int n = g.n, P = a.npol;
+  const double3 dv = ld3(a.dirs, d);
+  double2 acc[4][FLD_MAXPOL];   // sum ph sig, sum ph h (3)
+  for (int c = 0; c < 4; ++c)
+    for (int q = 0; q < FLD_MAXPOL; ++q) acc[c][q] = make_double2(0, 0);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const bool s1 = a.face_med[j] == a.med, s2 = a.face_med[n + j] == a.med;
+    if (!s1 && !s2) continue;
+    const double s = dot3(dv, ld3(g.pos, j));
+    double sn, cs;
+    sincos(a.k.x * s, &sn, &cs);
+    const double ee = exp(a.k.y * s) * g.area[j];
+    const double2 ph = make_double2(ee * cs, -ee * sn);
+    for (int sd = 0; sd < 2; ++sd) {
+      if (!(sd == 0 ? s1 : s2)) continue;
+      const double2* sg = sd == 0 ? a.sig1 : a.sig2;
+      const double2* hh = sd == 0 ? a.h1 : a.h2;
+#pragma unroll
+      for (int q = 0; q < FLD_MAXPOL; ++q) {
+        if (q >= P) break;
+        acc[0][q] = cadd(acc[0][q], cmul(ph, sg[(int64_t)j * P + q]));
+        for (int c = 0; c < 3; ++c) acc[1 + c][q] = cadd(acc[1 + c][q], cmul(ph, hh[((int64_t)j * 3 + c) * P + q]));
+      }
+    }
+  }
+  __shared__ double2 red[4][4 * FLD_MAXPOL];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int q = 0; q < FLD_MAXPOL; ++q) {
+      double2 v = acc[c][q];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[wid][c * FLD_MAXPOL + q] = v;
+    }
+  __syncthreads();
+  if (threadIdx.x < P) {
+    const int q = threadIdx.x;
+    double2 S[4];
+    for (int c = 0; c < 4; ++c) {
+      S[c] = make_double2(0, 0);
+      for (int w = 0; w < 4; ++w) S[c] = cadd(S[c], red[w][c * FLD_MAXPOL + q]);
+    }
+    const double2 ik = make_double2(-a.k.y, a.k.x), ik0 = make_double2(0, a.k0);
+    const double dd[3] = {dv.x, dv.y, dv.z};
+    if (a.e)
+      for (int c = 0; c < 3; ++c)
+        a.e[((int64_t)d * 3 + c) * P + q] = csub(cmul(ik0, S[1 + c]), cmul(ik, make_double2(dd[c] * S[0].x, dd[c] * S[0].y)));
+    if (a.h) {
+      // i k dir x Ph
+      const double2 c0 = csub(make_double2(dd[1] * S[3].x, dd[1] * S[3].y), make_double2(dd[2] * S[2].x, dd[2] * S[2].y));
+      const double2 c1 = csub(make_double2(dd[2] * S[1].x, dd[2] * S[1].y), make_double2(dd[0] * S[3].x, dd[0] * S[3].y));
+      const double2 c2 = csub(make_double2(dd[0] * S[2].x, dd[0] * S[2].y), make_double2(dd[1] * S[1].x, dd[1] * S[1].y));
+      a.h[((int64_t)d * 3 + 0) * P + q] = cmul(ik, c0);
+      a.h[((int64_t)d * 3 + 1) * P + q] = cmul(ik, c1);
+      a.h[((int64_t)d * 3 + 2) * P + q] = cmul(ik, c2);
+    }
+  }
+}
+
+mnpbem_status far_fields(const GeomDev& g, const int* face_med, int med, double2 k, double k0, int npol,
+                         int ndir, const double* dirs, const double2* sig1, const double2* sig2,
+                         const double2* h1, const double2* h2, double2* e, double2* h, cudaStream_t st) {
+  if (ndir <= 0 || g.n <= 0) return MNPBEM_OK;
+  if (npol < 1 || npol > FLD_MAXPOL) { set_error("far fields: npol must be 1..%d", FLD_MAXPOL); return MNPBEM_ERR_UNSUPPORTED; }
+  ProfScope ps(PH_SPECTRA, st, 0.0, 0.0, 1);
+  FarArgs a;
+  a.g = g; a.face_med = face_med; a.med = med; a.k = k; a.k0 = k0; a.npol = npol; a.dirs = dirs;
+  a.sig1 = sig1; a.sig2 = sig2; a.h1 = h1; a.h2 = h2; a.e = e; a.h = h;
+  k_far_dirs<<<(unsigned)ndir, 128, 0, st>>>(a);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 }  // namespace mnpbem

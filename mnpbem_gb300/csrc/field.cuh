@@ -23,4 +23,11 @@ mnpbem_status surface_fields(const GeomDev& g, const int* face_med, const double
                              const double2* h2, double2* e, double2* h, double2* phi, double2* phip,
                              double2* av, double2* ap, cudaStream_t st);
 
+// Far fields e, h [ndir][3][npol] (device, complex128; either may be null)
+// in the unit directions dirs [ndir][3] (device) of the charges and currents
+// on the faces bordering the 0-based embedding medium `med` of wavenumber k.
+mnpbem_status far_fields(const GeomDev& g, const int* face_med, int med, double2 k, double k0, int npol,
+                         int ndir, const double* dirs, const double2* sig1, const double2* sig2,
+                         const double2* h1, const double2* h2, double2* e, double2* h, cudaStream_t st);
+
 }  // namespace mnpbem
