@@ -12,8 +12,8 @@ max |ref| unless stated):
   complex64 assembly 2e-6; double-single assembly (hi + lo) against the FP64
   pass 1e-13; mixed precision (complex64 inversion + FP64 refinement) cross
   sections 1e-8.
-Measured errors are appended to ``gpurun_out/parity.jsonl`` when that folder
-exists.
+Measured errors are appended as JSON lines to the file named by the
+environment variable ``MNPBEM_PARITY_LOG`` when it is set.
 """
 import json
 import os
@@ -39,9 +39,9 @@ def rel(a, b):
 
 
 def record(name, **vals):
-    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
-    if os.path.isdir(d):
-        with open(os.path.join(d, "parity.jsonl"), "a") as f:
+    path = os.environ.get("MNPBEM_PARITY_LOG")
+    if path:
+        with open(path, "a") as f:
             f.write(json.dumps({"test": name, **vals}) + "\n")
 
 
