@@ -119,6 +119,33 @@ class planewaveret:
         pw.inf_area = _lib.dptr(self._ar)
         return pw
 
+    def field(self, p, enei, inout=1):
+        """Incoming fields at the positions of ``p`` (Simulation/retarded/
+        @planewaveret/field.m): a comparticle (its faces, medium column
+        ``inout`` of the faces' media) or a meshfield (its points and their
+        media).  Positions in the excitation medium get
+        e = pol exp(i k dir . r), h = nb dir x e; the others zero.  Returns
+        ``compstruct`` with ``e, h [m, 3, npol]`` (closed form, on the host)."""
+        enei = float(enei)
+        if isinstance(p, meshfield):
+            pos, med, eps = p.pts, p.medium, p.bem.p.eps_media(enei)[0]
+        else:
+            pos = p.pos
+            med = np.repeat(np.asarray(p.inout)[:, inout - 1], [q.n for q in p.p])
+            eps = p.eps_media(enei)[0]
+        nb = np.sqrt(eps[self.medium - 1])
+        k0 = 2 * np.pi / enei
+        k = k0 * nb
+        m, P = pos.shape[0], self.npol
+        e = np.zeros((m, 3, P), np.complex128)
+        h = np.zeros((m, 3, P), np.complex128)
+        ind = np.nonzero(med == self.medium)[0]
+        for i in range(P):
+            ph = np.exp(1j * k * pos[ind] @ self.dir[i])
+            e[ind, :, i] = ph[:, None] * self.pol[i][None, :]
+            h[:, :, i] = nb * np.cross(np.broadcast_to(self.dir[i], (m, 3)), e[:, :, i])
+        return compstruct(p, enei, e=e, h=h)
+
     def extinction(self, sig):
         return sig.ext
 
@@ -601,6 +628,10 @@ class meshfield:
                        else np.ascontiguousarray(np.broadcast_to(medium, self.pts.shape[0]), dtype=np.int32))
 
     def __call__(self, sig):
+        if hasattr(sig, "e") and not hasattr(sig, "sig1"):
+            # fields already at the points (e.g. exc.field(emesh, enei)): reshape only
+            P = sig.e.shape[-1]
+            return sig.e.reshape(self.shape + (3, P)), sig.h.reshape(self.shape + (3, P))
         b = self.bem
         enei = float(sig.enei)
         em = np.ascontiguousarray(b.p.eps_media(enei)[0])

@@ -1190,6 +1190,23 @@ class PlaneWaveRet:
             h += 1j * k * np.cross(np.broadcast_to(dirs[:, :, None], Ph.shape), Ph, axis=1)
         return e, h, k
 
+    def field(self, cp, enei, inout=1):
+        """Incoming fields at the faces (@planewaveret/field.m): faces whose
+        medium column ``inout`` is the excitation medium get
+        e = i k0 exp(i k r.dir)/(i k0) pol; h = nb dir x e everywhere."""
+        nb = np.sqrt(complex(cp.eps[self.medium - 1](enei)[0]))
+        k0 = 2 * np.pi / enei
+        k = k0 * nb
+        ind = np.nonzero(cp.face_media()[:, inout - 1] == self.medium)[0]
+        n, P = cp.n, self.pol.shape[0]
+        e = np.zeros((n, 3, P), complex)
+        h = np.zeros((n, 3, P), complex)
+        for i in range(P):
+            phase = np.exp(1j * k * cp.pos[ind] @ self.dir[i]) / (1j * k0)
+            e[ind, :, i] = 1j * k0 * phase[:, None] * self.pol[i][None, :]
+            h[:, :, i] = nb * np.cross(np.tile(self.dir[i], (n, 1)), e[:, :, i])
+        return e, h
+
     def extinction(self, cp, sig):
         e, h, k = self.farfield(cp, sig, self.dir)
         npol = self.pol.shape[0]
