@@ -118,3 +118,17 @@ def test_particle_mirror():
     assert abs(q.area.sum() - exact) < abs(p.area.sum() - exact) / 5
     with pytest.raises(ValueError):
         p.midpoints("smooth")
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_perturbed_and_open_meshes_match_oracle(seed):
+    """Seeded random vertex perturbations (irregular fans, odd valences) and
+    an open cap of a sphere (boundary vertices open their fans)."""
+    rng = np.random.default_rng(seed)
+    v, f = shapes.trisphere(144, 20.0)
+    v = v + rng.normal(scale=0.3, size=v.shape)
+    for verts, faces in ((v, f), (v, f[np.all(v[f[:, :3], 2] > -2.0, axis=1)])):
+        v2, f2 = shapes.midpoints_curv(verts, faces)
+        w2, g2 = R.midpoints_curv(verts, faces)
+        assert np.array_equal(f2, g2)
+        assert np.max(np.abs(v2 - w2)) <= 1e-13 * np.max(np.abs(w2))
