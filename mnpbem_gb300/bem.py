@@ -386,13 +386,13 @@ class bemret:
         em = np.ascontiguousarray(self.p.eps_media(enei)[0])
         parts = [np.ascontiguousarray(getattr(sig, k), dtype=np.complex128) for k in ("sig1", "sig2", "h1", "h2")]
         n, P = parts[0].shape
-        shapes = {"e": (n, 3, P), "h": (n, 3, P), "phi": (n, P), "phip": (n, P), "a": (n, 3, P), "ap": (n, 3, P)}
-        out = {k: np.zeros(shapes[k], np.complex128) for k in want}
+        dims = {"e": (n, 3, P), "h": (n, 3, P), "phi": (n, P), "phip": (n, P), "a": (n, 3, P), "ap": (n, 3, P)}
+        out = {k: np.zeros(dims[k], np.complex128) for k in want}
         for c0 in range(0, P, 4):        # mnpbem_surface_fields takes up to four columns per call
             cols = slice(c0, min(P, c0 + 4))
             w = cols.stop - cols.start
             cin = [np.ascontiguousarray(a[..., cols]) for a in parts]
-            cout = {k: np.zeros(shapes[k][:-1] + (w,), np.complex128) for k in want}
+            cout = {k: np.zeros(dims[k][:-1] + (w,), np.complex128) for k in want}
             ptr = [cout[k].ctypes.data if k in cout else None for k in ("e", "h", "phi", "phip", "a", "ap")]
             _lib.check(self._lib.mnpbem_surface_fields(
                 self._h, enei, em.view(np.float64).ctypes.data_as(_lib.c_double_p), em.size, w, inout,
