@@ -152,6 +152,21 @@ class planewaveret:
     def scattering(self, sig):
         return sig.sca
 
+    def dscattering(self, bem, sig):
+        """``sca, dsca`` as ``[sca, dsca] = scattering(exc, sig)``
+        (@planewaveret/scattering.m, Simulation/retarded/scattering.m): the
+        Poynting flux 0.5 Re(n . (e x conj h)) of the charges' far fields on
+        the sphere at infinity (``mnpbem_farfield``) per direction, divided by
+        0.5 nb of medium 1 (``dsca [ninf, npol]``), and its area-weighted sum
+        ``sca [npol]``."""
+        ff = self.spec.farfield(bem, sig)
+        nv = self.spec.nvec
+        flux = 0.5 * np.real(np.einsum("dc,dcp->dp", nv, np.cross(ff.e, np.conj(ff.h), axis=1)))
+        nb = np.sqrt(bem.p.eps_media(float(sig.enei))[0][0])
+        dsca = np.real(flux / (0.5 * nb))
+        sca = self.spec.area @ dsca
+        return sca, compstruct(self.spec.pinfty, sig.enei, dsca=dsca)
+
     ext = extinction
     sca = scattering
 
