@@ -39,6 +39,41 @@ class compstruct:
         keys = [k for k in self.__dict__ if k not in ("p", "enei")]
         return "compstruct(enei=%r, fields=%s)" % (self.enei, keys)
 
+    def _fields(self):
+        return {k: v for k, v in self.__dict__.items() if k not in ("p", "enei")}
+
+    @staticmethod
+    def _numeric(v):
+        return isinstance(v, (np.ndarray, int, float, complex, np.number))
+
+    def __add__(self, other):
+        """Field-wise sum (@compstruct/plus.m): fields of both are added,
+        fields of one are kept; non-numeric fields keep the left operand's."""
+        out = compstruct(self.p, self.enei, **self._fields())
+        for k, v in other._fields().items():
+            mine = out.__dict__.get(k)
+            if mine is None:
+                setattr(out, k, v)
+            elif self._numeric(mine) and self._numeric(v):
+                setattr(out, k, mine + v)
+        return out
+
+    def __neg__(self):
+        """@compstruct/uminus.m on the numeric fields."""
+        return compstruct(self.p, self.enei, **{k: (-v if self._numeric(v) else v)
+                                                for k, v in self._fields().items()})
+
+    def __sub__(self, other):
+        """@compstruct/minus.m: self + (-other)."""
+        return self + (-other)
+
+    def __mul__(self, val):
+        """@compstruct/mtimes.m: every numeric field times a scalar."""
+        return compstruct(self.p, self.enei, **{k: (val * v if self._numeric(v) else v)
+                                                for k, v in self._fields().items()})
+
+    __rmul__ = __mul__
+
 
 class spectrumret:
     """Unit sphere at infinity used for far fields (@spectrumret)."""
