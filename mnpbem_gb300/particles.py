@@ -195,6 +195,56 @@ class particle:
         v2, f2 = make(self.verts, self.faces)
         return particle(v2, f2, dict(self.op, interp=key))
 
+    def _remake(self, verts, faces, verts2=None, faces2=None):
+        if self.faces2 is not None:
+            return particle(verts2, faces2, self.op)
+        return particle(verts, faces, self.op)
+
+    def rot(self, angle, dir=(0.0, 0.0, 1.0)):
+        """Rotation by ``angle`` degrees about ``dir`` (Particles/@particle/
+        rot.m): vertices times expm(-angle (d1 J1 + d2 J2 + d3 J3)) as row
+        vectors, J the generators of rotations about x, y, z."""
+        from scipy.linalg import expm
+        d = np.asarray(dir, dtype=np.float64)
+        d = d / np.linalg.norm(d)
+        j1 = np.array([[0, 0, 0], [0, 0, -1], [0, 1, 0]], float)
+        j2 = np.array([[0, 0, 1], [0, 0, 0], [-1, 0, 0]], float)
+        j3 = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 0]], float)
+        r = expm(-angle / 180 * np.pi * (d[0] * j1 + d[1] * j2 + d[2] * j3))
+        return self._remake(self.verts @ r, self.faces,
+                            None if self.verts2 is None else self.verts2 @ r, self.faces2)
+
+    def scale(self, factor):
+        """Vertices times a scalar or per-axis ``factor`` (scale.m)."""
+        f = np.asarray(factor, dtype=np.float64)
+        return self._remake(self.verts * f, self.faces,
+                            None if self.verts2 is None else self.verts2 * f, self.faces2)
+
+    def flipfaces(self):
+        """Reversed face orientation (flipfaces.m): corner order reversed, the
+        edge-midpoint columns of curved elements permuted to match."""
+        faces = self.faces.copy()
+        tri = faces[:, 3] < 0
+        faces[tri, :3] = faces[tri][:, [2, 1, 0]]
+        faces[~tri, :4] = faces[~tri][:, [3, 2, 1, 0]]
+        faces2 = None
+        if self.faces2 is not None:
+            faces2 = self.faces2.copy()
+            faces2[tri, :7] = self.faces2[tri][:, [2, 1, 0, 3, 5, 4, 6]]
+            faces2[~tri, :8] = self.faces2[~tri][:, [3, 2, 1, 0, 6, 5, 4, 7]]
+        return self._remake(self.verts, faces, self.verts2, faces2)
+
+    def flip(self, dir=1):
+        """Mirror image along axis ``dir`` (1-based: 1 = x, as flip.m), with
+        the faces flipped so that the normals stay outward."""
+        v = self.verts.copy()
+        v[:, dir - 1] *= -1
+        v2 = None
+        if self.verts2 is not None:
+            v2 = self.verts2.copy()
+            v2[:, dir - 1] *= -1
+        return self._remake(v, self.faces, v2, self.faces2).flipfaces()
+
     def shift(self, vec):
         d = np.asarray(vec, dtype=np.float64)[None, :]
         if self.faces2 is not None:

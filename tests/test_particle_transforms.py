@@ -1,0 +1,50 @@
+"""Particle transforms of the mirror (Particles/@particle rot.m, scale.m,
+flip.m, flipfaces.m) on flat and curved elements: rotations move centroids
+and normals and keep areas, scaling scales areas, flipfaces reverses the
+normals, flip mirrors the particle with the normals kept outward.  For
+curved quadrilaterals the split into two 6-node triangles follows the corner
+order (norm_curv.m takes the basis from the first, quad_curv.m sums both), so
+flipfaces moves the split to the other diagonal: their flipped normals are
+antiparallel to 2e-3 and their areas agree to 1e-3, not exactly.  That is
+the reference's behaviour too."""
+import numpy as np
+import pytest
+
+import mnpbem_gb300 as m
+from mnpbem_gb300 import shapes
+
+
+def particles():
+    v, f = shapes.trirod(10.0, 40.0, (15, 5, 11))
+    p = m.particle(v, f)
+    return {"flat": p, "curved": p.midpoints("curv")}
+
+
+@pytest.mark.parametrize("kind", ["flat", "curved"])
+def test_rotation(kind):
+    p = particles()[kind]
+    q = p.rot(90, [0, 1, 0])
+    # rot.m's expm(-angle J) on row vectors: 90 degrees about y maps (x, y, z) -> (z, y, -x)
+    r = np.array([[0, 0, -1], [0, 1, 0], [1, 0, 0]], float)
+    assert np.allclose(q.pos, p.pos @ r, atol=1e-12)
+    assert np.allclose(q.nvec, p.nvec @ r, atol=1e-12)
+    assert np.allclose(q.area, p.area, rtol=1e-12)
+    assert np.allclose(p.rot(30).rot(-30).pos, p.pos, atol=1e-12)
+
+
+@pytest.mark.parametrize("kind", ["flat", "curved"])
+def test_scale_flip(kind):
+    p = particles()[kind]
+    assert np.allclose(p.scale(2.0).area, 4 * p.area, rtol=1e-12)
+    assert np.allclose(p.scale([1, 1, 2]).pos[:, 2], 2 * p.pos[:, 2], atol=1e-12)
+    ff = p.flipfaces()
+    tol, atol = (1e-12, 1e-12) if kind == "flat" else (2e-3, 1e-3)
+    assert np.min(np.sum(ff.nvec * -p.nvec, 1)) > 1 - tol
+    assert np.allclose(ff.area, p.area, rtol=atol)
+    fl = p.flip(1)
+    mirror = np.array([-1.0, 1.0, 1.0])
+    if kind == "flat":
+        assert np.allclose(fl.pos, p.pos * mirror, atol=1e-12)
+    assert np.min(np.sum(fl.nvec * (p.nvec * mirror), 1)) > 1 - tol    # still outward
+    assert np.allclose(fl.area, p.area, rtol=atol)
+    assert np.allclose(fl.flip(1).pos, p.pos, atol=1e-12)
