@@ -261,6 +261,20 @@ def curved(p, key=None):
     return particle(p.verts2, p.faces2, dict(p.op, interp="curv"))
 
 
+def trirod(diameter, height, n=(15, 20, 20), triangles=False, op=None):
+    """Particle of ``shapes.trirod`` (Particles/particleshapes/trirod.m): rod
+    along z with hemispherical caps; ``triangles`` splits the quadrilaterals."""
+    v, f = shapes.trirod(diameter, height, n, triangles)
+    return particle(v, f, op)
+
+
+def tricube(n, length=1.0, e=0.25, triangles=False, op=None):
+    """Particle of ``shapes.tricube`` (Particles/particleshapes/tricube.m):
+    cube of edge ``length`` rounded by the super-sphere exponent ``e``."""
+    v, f = shapes.tricube(n, length, e, triangles)
+    return particle(v, f, op)
+
+
 def trisphere(n, diameter=1.0, op=None):
     """Sphere triangulated from the stored point set closest to ``n`` points;
     with ``op['interp'] = 'curv'`` the curved elements of trisphere.m:54-61

@@ -48,3 +48,13 @@ def test_scale_flip(kind):
     assert np.min(np.sum(fl.nvec * (p.nvec * mirror), 1)) > 1 - tol    # still outward
     assert np.allclose(fl.area, p.area, rtol=atol)
     assert np.allclose(fl.flip(1).pos, p.pos, atol=1e-12)
+
+
+def test_shape_particles():
+    rod = m.trirod(10.0, 40.0, (15, 5, 11))
+    v, f = shapes.trirod(10.0, 40.0, (15, 5, 11))
+    assert np.array_equal(rod.faces, f) and np.allclose(rod.verts, v)
+    assert abs(rod.midpoints("curv").area.sum() - (np.pi * 10 * 30 + 4 * np.pi * 25)) < 2.0
+    cube = m.tricube(8, 40.0, 0.25, op={"interp": "flat"})
+    assert cube.n == shapes.tricube(8, 40.0, 0.25)[1].shape[0]
+    assert np.all(np.sum(cube.nvec * cube.pos, 1) > 0)          # outward normals
