@@ -11,5 +11,6 @@ from .particles import comparticle, curved, lglnodes, particle, quadface, tricub
 from .bem import (bemiter_options, bemoptions, bemret, bemretiter, bemsolver, compstruct, dipoleret,  # noqa: F401
                   meshfield, planewave, planewaveret, point_media, spectrum_batch, spectrumret)
 from .hmatrix import clustertree, hmatrix_blocks, hpartition  # noqa: F401
+from .mie import mieret, miesolver  # noqa: F401
 
 __version__ = "0.1.0"
