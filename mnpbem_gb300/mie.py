@@ -12,11 +12,11 @@ the wavelength itself (the reference evaluates a constant one at 0).
 Closed-form series on the host: nothing here is O(faces).
 """
 import numpy as np
-from scipy.special import spherical_jn, spherical_yn
 
 
 def _riccati(z, lmax):
     """j_l, h_l (spherical, first kind) and z f_{l-1} - l f_l for l = 1..lmax."""
+    from scipy.special import spherical_jn, spherical_yn
     l = np.arange(0, lmax + 1)
     j = spherical_jn(l, z)
     h = j + 1j * spherical_yn(l, z)
