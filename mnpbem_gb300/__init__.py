@@ -7,7 +7,8 @@ sm_103a, C ABI in ``include/mnpbem_gpu.h``).  This package mirrors MNPBEM's
 MATLAB calling surface on top of that library.
 """
 from .materials import EV2NM, epsconst, epsdrude, epsfun, epstable  # noqa: F401
-from .particles import comparticle, curved, lglnodes, particle, quadface, tricube, trirod, trisphere  # noqa: F401
+from .particles import (comparticle, curved, lglnodes, particle, quadface, tricube, trirod,  # noqa: F401
+                        trisphere, trispheresegment)
 from .bem import (bemiter_options, bemoptions, bemret, bemretiter, bemsolver, compstruct, dipoleret,  # noqa: F401
                   meshfield, planewave, planewaveret, point_media, spectrum_batch, spectrumret)
 from .hmatrix import clustertree, hmatrix_blocks, hpartition  # noqa: F401

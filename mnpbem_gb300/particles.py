@@ -275,6 +275,50 @@ def tricube(n, length=1.0, e=0.25, triangles=False, op=None):
     return particle(v, f, op)
 
 
+def trispheresegment(phi, theta, diameter=1.0, triangles=False, op=None):
+    """Sphere segment on the grid of azimuths ``phi`` and polar angles
+    ``theta`` (radians; Particles/particleshapes/trispheresegment.m): a
+    quadrilateral (or, with ``triangles``, triangle) grid oriented with
+    outward normals, cleaned as @particle/clean.m does (vertices rounded to 8
+    decimals and merged in sorted order, quadrilaterals with a collapsed edge
+    made triangles, faces below 1e-10 of the mean area dropped), then
+    curved-element nodes at the flat midpoints projected onto the sphere."""
+    ph, th = np.meshgrid(np.asarray(phi, float), np.asarray(theta, float))
+    r = 0.5 * diameter
+    xyz = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], -1)
+    nt, nph = ph.shape
+    verts = np.stack([xyz[..., k].ravel(order="F") for k in range(3)], 1)
+    idx = np.arange(nt * nph).reshape(nph, nt).T          # column-major grid numbering
+    a, b, c, d = idx[:-1, :-1], idx[1:, :-1], idx[1:, 1:], idx[:-1, 1:]
+    quads = np.stack([q.ravel(order="F") for q in (a, d, c, b)], 1)      # outward for increasing phi, theta
+    if triangles:
+        faces = np.vstack([np.hstack([quads[:, [0, 1, 2]], -np.ones((quads.shape[0], 1), np.int64)]),
+                           np.hstack([quads[:, [0, 2, 3]], -np.ones((quads.shape[0], 1), np.int64)])])
+    else:
+        faces = quads.astype(np.int64)
+    # clean.m: merge vertices (rounded to 8 decimals, sorted rows), collapse faces
+    uniq, inv = np.unique(np.round(verts, 8), axis=0, return_inverse=True)
+    inv = inv.ravel()
+    faces = np.where(faces >= 0, inv[np.maximum(faces, 0)], -1)
+    out = []
+    for row in faces:
+        corners = row[row >= 0]
+        _, first = np.unique(corners, return_index=True)
+        keep = corners[np.sort(first)]
+        if keep.size >= 3:
+            out.append(np.concatenate([keep, -np.ones(4 - keep.size, np.int64)]))
+    faces = np.asarray(out, np.int64)
+    area = _norm_flat(uniq, faces)[4]
+    faces = faces[area > 1e-10 * area.mean()]
+    used = np.unique(faces[faces >= 0])
+    remap = -np.ones(uniq.shape[0] + 1, np.int64)
+    remap[used] = np.arange(used.size)
+    faces = np.where(faces >= 0, remap[np.maximum(faces, 0)], -1)
+    v2, f2 = shapes.midpoints_flat(uniq[used], faces)
+    v2 = r * v2 / np.sqrt(np.sum(v2 * v2, 1))[:, None]
+    return particle(v2, f2, op)
+
+
 def trisphere(n, diameter=1.0, op=None):
     """Sphere triangulated from the stored point set closest to ``n`` points;
     with ``op['interp'] = 'curv'`` the curved elements of trisphere.m:54-61

@@ -58,3 +58,21 @@ def test_shape_particles():
     cube = m.tricube(8, 40.0, 0.25, op={"interp": "flat"})
     assert cube.n == shapes.tricube(8, 40.0, 0.25)[1].shape[0]
     assert np.all(np.sum(cube.nvec * cube.pos, 1) > 0)          # outward normals
+
+
+def test_sphere_segments():
+    """trispheresegment.m: a full sphere from the (phi, theta^2) grid of the
+    dipole demos has outward normals, merged seam and poles (30 x 30 cells,
+    the pole cells triangles) and, with curved elements, the sphere's area
+    to 1e-4; a quarter segment and the triangle variant are outward too."""
+    full = m.trispheresegment(2 * np.pi * np.linspace(0, 1, 31), np.pi * np.linspace(0, 1, 31) ** 2, 4.0)
+    assert full.n == 900 and np.sum(full.faces[:, 3] < 0) == 60
+    assert np.all(np.sum(full.nvec * full.pos, 1) > 0)
+    assert np.allclose(np.linalg.norm(full.verts2, axis=1), 2.0, atol=1e-12)
+    curved = m.trispheresegment(2 * np.pi * np.linspace(0, 1, 31), np.pi * np.linspace(0, 1, 31) ** 2, 4.0,
+                                op={"interp": "curv"})
+    assert abs(curved.area.sum() - 16 * np.pi) < 1e-4 * 16 * np.pi
+    quarter = m.trispheresegment(np.linspace(0, np.pi / 2, 10), np.pi * np.linspace(0, 1, 15) ** 2, 10.0)
+    assert np.all(np.sum(quarter.nvec * quarter.pos, 1) > 0)
+    tri = m.trispheresegment(2 * np.pi * np.linspace(0, 1, 13), np.pi * np.linspace(0, 1, 9), 4.0, triangles=True)
+    assert np.all(tri.faces[:, 3] < 0) and np.all(np.sum(tri.nvec * tri.pos, 1) > 0)
