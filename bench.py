@@ -2,20 +2,24 @@
 """Throughput of the retarded BEM path: wavelength-solves/s on GB300.
 
 One wavelength-solve = assembly of G1, H1, G2, H2 (with near-field
-refinement), the bemret inversions and products, the mldivide chain for all
-polarisations, FP64 iterative refinement (mixed precision), and the extinction
-and scattering cross sections.  The per-geometry set-up (refinement
-coefficients, closed-surface sum rule) runs once before timing, like
-``bem = bemsolver(p, op)`` in MNPBEM.
+refinement), the bemret factorisations and products, the mldivide chain for
+all polarisations, FP64-class iterative refinement (mixed precision), and the
+extinction and scattering cross sections.  The per-geometry set-up
+(refinement coefficients, closed-surface sum rule) runs once before timing,
+like ``bem = bemsolver(p, op)`` in MNPBEM.
 
-Workload (synthetic, deterministic): sphere of diameter 50 nm with 4000 flat
-faces, Drude metal eps(w) = 10 - 9.065^2 / (w (w + 0.0708 i)) (w in eV) in
-eps = 1.77, x-polarised plane wave along +z, wavelengths on the 60-point grid
-450..750 nm.  A step is one batch of ``--batch`` wavelengths per GPU; with N
-GPUs rank r takes its own wavelengths (weak scaling, no collective on the
-data path).
+Default workload (synthetic, deterministic; the configuration the metric's
+target is stated on): a dimer of two d = 50 nm spheres with a 2 nm gap,
+12 000 flat faces each, Drude metal eps(w) = 10 - 9.065^2 / (w (w + 0.0708 i))
+(w in eV) in eps = 1.77, plane wave polarised along the dimer axis (x)
+travelling along +z, wavelengths on the 32-point grid 500..900 nm.  A step is
+one batch of ``--batch`` wavelengths per GPU; with N GPUs rank r takes its own
+wavelengths (weak scaling, no collective on the data path).  The line also
+carries the plain FP64 GPU path on one wavelength of the same workload, the
+CPU oracle on the same geometry at a smaller size (extrapolated), the GPU
+results against that oracle, and a short run of the 4000-face sphere.
 
-    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload ...]
 """
 import argparse
 import ctypes
@@ -34,12 +38,23 @@ sys.path.insert(0, ROOT)
 METRIC = "wavelength-solves/s at N faces: mixed+batched vs FP64 GPU, ext err ≤1e-6"
 UNIT = "wavelength-solves/s"
 DRUDE = (10.0, 9.065, 0.0708)
-NGRID = 60
-# DRAM bytes (read + write) of one full-size rank-256 Gauss-Jordan update of the
-# 4000-face workload, from one ncu capture (profiles/tc_gemm_rank256_update_sphere4000.md)
-TC_TRAFFIC_PER_LAUNCH = 152.7e6 + 67.5e6
-TC_TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum of the full-size rank-256 update "
-                   "(4000 x 8000 x 512 real) from one ncu capture; algorithmic bytes of that launch 280 MB")
+
+# Workloads.  dimer24k is the configuration the metric's target is stated on:
+# two d = 50 nm spheres with a 2 nm gap, 12 000 flat faces each (separate
+# media, so G1 and H1 are block-diagonal), x-polarised (along the dimer axis)
+# along +z, 32 wavelengths 500-900 nm.  sphere4000: one d = 50 nm sphere with
+# 4000 faces, 60 wavelengths 450-750 nm.
+WORKLOADS = {
+    "dimer24k": {"faces": 24000, "grid": (500.0, 900.0, 32), "batch": 4, "dimer": True},
+    "sphere4000": {"faces": 4000, "grid": (450.0, 750.0, 60), "batch": 20, "dimer": False},
+}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant
+# tensor-core launch of each workload, from one ncu capture (filled per workload
+# once captured; None: not captured)
+TC_TRAFFIC = {}
+# faces of the CPU sample (the oracle) for each workload: the same geometry at
+# a size the oracle solves in seconds
+CPU_FACES = {"dimer24k": 4000, "sphere4000": 4000}
 
 
 def parse():
@@ -48,34 +63,42 @@ def parse():
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--faces", type=int, default=4000)
-    ap.add_argument("--batch", type=int, default=20, help="wavelengths per step per GPU")
+    ap.add_argument("--workload", default="dimer24k", choices=["dimer24k", "sphere4000", "batch3", "iter24k"],
+                    help="dimer24k: two 12000-face spheres, 32 wavelengths (the headline); sphere4000: one "
+                         "4000-face sphere, 60 wavelengths; batch3: three particles of uneven size, 128 "
+                         "wavelengths, two polarisations; iter24k: the dimer through the iterative H-matrix solver")
+    ap.add_argument("--faces", type=int, default=0, help="faces of the workload (0: its own)")
+    ap.add_argument("--batch", type=int, default=0, help="wavelengths per step per GPU (0: the workload's)")
     ap.add_argument("--lanes", type=int, default=0, help="wavelengths in flight at once (0: library default)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--refine-tol", type=float, default=1e-8,
                     help="mixed precision: refinement stops at ||dx|| <= tol ||x|| (the metric asks for an "
                          "extinction error <= 1e-6 against FP64; the library default is 1e-10)")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--skip-fp64", action="store_true")
-    ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (default: workload)")
-    ap.add_argument("--workload", default="sphere4000", choices=["sphere4000", "batch3", "dimer24k", "iter24k"],
-                    help="sphere4000: the headline sweep; batch3: three particles of uneven size, 128 "
-                         "wavelengths, two polarisations; dimer24k: two 12000-face spheres, 32 wavelengths; "
-                         "iter24k: the same dimer through the iterative H-matrix solver")
+    ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 GPU wavelength at full size")
+    ap.add_argument("--skip-c2", action="store_true", help="skip the 4000-face sphere side run")
+    ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (0: the workload's)")
+    ap.add_argument("--profile-steps", type=int, default=3, help="steps of the profiled repeat")
     ap.add_argument("--iter-faces", type=int, default=24000,
                     help="iter24k: total faces of the dimer (smaller sizes for profiling runs)")
-    ap.add_argument("--fp64-faces", type=int, default=12000,
-                    help="dimer24k: total faces of the FP64 timing sample (scaled by n^3 to 24000)")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.workload in WORKLOADS:
+        w = WORKLOADS[a.workload]
+        a.faces = a.faces or w["faces"]
+        a.batch = a.batch or w["batch"]
+        a.cpu_faces = a.cpu_faces or CPU_FACES[a.workload]
+    return a
 
 
-def grid():
-    return np.linspace(450.0, 750.0, NGRID)
+def grid(a):
+    lo, hi, num = WORKLOADS[a.workload]["grid"]
+    return np.linspace(lo, hi, num)
 
 
-def step_wavelengths(step, rank, world, batch):
+def step_wavelengths(a, step, rank, world, batch):
+    g = grid(a)
     base = (step * world + rank) * batch
-    return grid()[(base + np.arange(batch)) % NGRID]
+    return g[(base + np.arange(batch)) % g.size]
 
 
 def max_over_ranks(dist, values, device, torch):
@@ -88,10 +111,16 @@ def max_over_ranks(dist, values, device, torch):
     return [float(v) for v in t]
 
 
-def workload_desc(a):
-    return ("sphere d=50 nm, %d flat faces, Drude eps_inf=10 wp=9.065 eV gamma=0.0708 eV in eps=1.77, "
-            "x-pol along +z, %d-point wavelength grid 450-750 nm, %d wavelengths per step per GPU"
-            % (a.faces, NGRID, a.batch))
+def workload_desc(a, faces=None, batch=None):
+    faces = faces or a.faces
+    lo, hi, num = WORKLOADS[a.workload]["grid"]
+    tail = ", Drude eps_inf=10 wp=9.065 eV gamma=0.0708 eV in eps=1.77, x-pol along +z, %d-point wavelength " \
+           "grid %g-%g nm" % (num, lo, hi)
+    if batch:
+        tail += ", %d wavelengths per step per GPU" % batch
+    if WORKLOADS[a.workload]["dimer"]:
+        return "dimer of two d=50 nm spheres, 2 nm gap, 2 x %d flat faces (separate media)" % (faces // 2) + tail
+    return "sphere d=50 nm, %d flat faces" % faces + tail
 
 
 # --------------------------------------------------------------------- clocks
@@ -156,14 +185,33 @@ def drude():
     return m.epsfun(lambda w: e0 - wp ** 2 / (w * (w + 1j * g)), "eV")
 
 
-def make_problem(a, device, precision):
+def geometry(faces, dimer):
+    """(particles, inout, closed) of the workload's geometry at ``faces`` faces."""
     import mnpbem_gb300 as m
     from mnpbem_gb300 import shapes
-    v, f = shapes.fibsphere(a.faces, 50.0)
-    p = m.particle(v, f)
-    cp = m.comparticle([m.epsconst(1.77), drude()], [p], [[2, 1]], 1)
-    bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device, lanes=a.lanes))
-    bem.refine_tol = a.refine_tol
+    if dimer:
+        nf = faces // 2
+        v1, f1 = shapes.fibsphere(nf, 50.0, center=(-26.0, 0.0, 0.0))
+        v2, f2 = shapes.fibsphere(nf, 50.0, center=(26.0, 0.0, 0.0))
+        return [(v1, f1), (v2, f2)], [[2, 1], [3, 1]]
+    v, f = shapes.fibsphere(faces, 50.0)
+    return [(v, f)], [[2, 1]]
+
+
+def make_solver(faces, dimer, device, precision, lanes=0, refine_tol=1e-8):
+    import mnpbem_gb300 as m
+    parts, inout = geometry(faces, dimer)
+    eps = [m.epsconst(1.77)] + [drude() for _ in parts]
+    cp = m.comparticle(eps, [m.particle(v, f) for v, f in parts], inout, *range(1, len(parts) + 1))
+    bem = m.bemsolver(cp, m.bemoptions(precision=precision, device=device, lanes=lanes))
+    bem.refine_iters = 20
+    bem.refine_tol = refine_tol
+    return cp, bem
+
+
+def make_problem(a, device, precision):
+    import mnpbem_gb300 as m
+    cp, bem = make_solver(a.faces, WORKLOADS[a.workload]["dimer"], device, precision, a.lanes, a.refine_tol)
     exc = m.planewave([1, 0, 0], [0, 0, 1])
     return cp, bem, exc
 
@@ -233,12 +281,24 @@ def read_profile(bem):
 
 
 def peaks():
+    """(HBM GB/s, bf16 TFLOP/s burst, bf16 TFLOP/s sustained, source)."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         d = json.load(open(path))
-        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+        return d["hbm_gbs"], d["bf16_tflops"], d.get("bf16_tflops_sustained", d["bf16_tflops"]), "measured"
     except Exception:
-        return 6800.0, 1900.0, "fallback"
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def solve_flops(n, dimer):
+    """Real FLOP of the n^3 work of one wavelength as the library factors it:
+    block LU of G1 (per particle block), of G2 and of Sigma (8/3 n^3 each),
+    Sigma1 = H1 G1^-1 and Sigma2 = H2 G2^-1 by two triangular solves each
+    (8 n^3, per block for G1), Deltai by Gauss-Jordan inversion (8 n^3)."""
+    nb = n / 2 if dimer else n
+    nblk = 2 if dimer else 1
+    g1 = nblk * (8.0 / 3.0 + 8.0) * nb ** 3
+    return g1 + (8.0 / 3.0 + 8.0 + 8.0 + 8.0 / 3.0) * n ** 3
 
 
 def run_ours(a, rank, world, dist, torch):
@@ -248,6 +308,7 @@ def run_ours(a, rank, world, dist, torch):
     sweep = DeviceSweep(bem, exc, a.batch, torch)
     stream = lib_stream(bem, torch)
     n, P = cp.n, exc.npol
+    sw = lambda s: step_wavelengths(a, s, rank, world, a.batch)
 
     def barrier():
         if dist is not None:
@@ -255,7 +316,7 @@ def run_ours(a, rank, world, dist, torch):
 
     bem_lib = bem._lib
     for s in range(a.warmup):
-        sweep.run(step_wavelengths(s, rank, world, a.batch))
+        sweep.run(sw(s))
     # ---------------- timed region (device-resident outputs, no per-launch events)
     bem_lib.mnpbem_profile_reset(bem.handle)
     clocks = ClockSampler(device)
@@ -265,7 +326,7 @@ def run_ours(a, rank, world, dist, torch):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for s in range(a.steps):
-        sweep.run(step_wavelengths(a.warmup + s, rank, world, a.batch))
+        sweep.run(sw(a.warmup + s))
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -273,29 +334,15 @@ def run_ours(a, rank, world, dist, torch):
     ms = e0.elapsed_time(e1)
     launches_timed = read_profile(bem)
     iters = sweep.iters.copy()
-    # ---------------- the same steps at the library's default tolerance (1e-10)
-    tol_default = None
-    if a.precision == "mixed" and a.refine_tol != 1e-10:
-        from mnpbem_gb300 import _lib as L_
-        sweep_d = DeviceSweep(bem, exc, a.batch, torch)
-        sweep_d.ref = L_.Refine(bem.refine_iters, 1e-10)
-        sweep_d.run(step_wavelengths(0, rank, world, a.batch))
-        torch.cuda.synchronize()
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record(stream)
-        for s in range(a.steps):
-            sweep_d.run(step_wavelengths(a.warmup + s, rank, world, a.batch))
-        g1.record(stream)
-        torch.cuda.synchronize()
-        tol_default = {"refine_tol": 1e-10, "value": a.batch * a.steps / (g0.elapsed_time(g1) / 1e3),
-                       "refinement_iterations": sweep_d.iters.tolist()}
-    # ---------------- profiled repeat of the same steps: CUDA events on the
-    # library stream around every launch give per-kernel-class durations
+    ext_timed = sweep.ext.cpu().numpy().copy()
+    # ---------------- profiled repeat of a few of the same steps: CUDA events on
+    # the library stream around every launch give per-kernel-class durations
     bem_lib.mnpbem_profile_enable(bem.handle, 1)
-    sweep.run(step_wavelengths(a.warmup, rank, world, a.batch))      # captures graphs with event nodes
+    sweep.run(sw(a.warmup))      # captures graphs with event nodes
     bem_lib.mnpbem_profile_reset(bem.handle)
-    for s in range(a.steps):
-        sweep.run(step_wavelengths(a.warmup + s, rank, world, a.batch))
+    nprof = max(1, min(a.profile_steps, a.steps))
+    for s in range(nprof):
+        sweep.run(sw(a.warmup + s))
     torch.cuda.synchronize()
     bem_lib.mnpbem_profile_enable(bem.handle, 0)
     prof = read_profile(bem)
@@ -310,8 +357,7 @@ def run_ours(a, rank, world, dist, torch):
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for s in range(a.steps):
-        r = bem.spectrum(exc, step_wavelengths(a.warmup + a.steps + s, rank, world, a.batch),
-                         fields=True, out=host)
+        bem.spectrum(exc, sw(a.warmup + a.steps + s), fields=True, out=host)
     f1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -325,21 +371,23 @@ def run_ours(a, rank, world, dist, torch):
     total = a.batch * a.steps * world
     value = total / (ms / 1e3)
     e2e_value = total / (e2e_ms / 1e3)
-    # ---------------- roofline: the tensor-core GEMMs (the dominant kernel class
-    # in FLOPs and, with several wavelengths in flight, in device time; the
-    # pivot-block inversions run on one 8-CTA cluster each and overlap other
-    # wavelengths' GEMMs); every other kernel class is listed in phases_roofline
-    hbm, bf16, src = peaks()
-    timing = ("CUDA events on the library stream around each launch, over a profiled repeat of "
-              "the %d timed steps (one wavelength in flight)" % a.steps)
+    # ---------------- roofline: the tensor-core GEMMs (the dominant kernel class in
+    # FLOPs and device time); timed inside seconds-long steps, so the reference
+    # peak is the sustained bf16 rate
+    hbm, bf16, bf16_sus, src = peaks()
+    timing = ("CUDA events on the library stream around each launch, over a profiled repeat of %d of "
+              "the timed steps" % nprof)
     d = prof["gemm_n3"]
     achieved = d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0
+    traffic = TC_TRAFFIC.get(a.workload)
     roof = {"kernel": "k_tc_gemm (tcgen05 kind::tf32, all tensor-core GEMM launches)", "bound": "tensor",
-            "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-            "peak_source": src + " dense bf16 (TF32 runs at half the bf16 rate: frac of the TF32 rate = %.3f)"
-                           % (2 * achieved / bf16),
-            "traffic": TC_TRAFFIC_PER_LAUNCH, "traffic_note": TC_TRAFFIC_NOTE,
-            "launches": d["launches"], "ms": d["ms"], "timing": timing}
+            "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
+            "peak_source": src + " sustained dense bf16 (kernel timed inside seconds-long steps); TF32 issues "
+                                 "at half the bf16 rate: %.3f of that derived TF32 rate" % (2 * achieved / bf16_sus),
+            "traffic": traffic["bytes"] if traffic else None,
+            "traffic_note": traffic["note"] if traffic else "no ncu capture of this configuration",
+            "launches": d["launches"], "ms": d["ms"], "timing": timing,
+            "flops_per_wavelength_n3": solve_flops(n, WORKLOADS[a.workload]["dimer"])}
     phases_roof = {}
     for k, v in prof.items():
         if v["ms"] <= 0 or k == "geometry":
@@ -349,37 +397,48 @@ def run_ours(a, rank, world, dist, torch):
                           "hbm_frac": round(v["bytes"] / (v["ms"] / 1e3) / 1e9 / hbm, 4) if v["bytes"] else None,
                           "TFLOP/s": round(v["flops"] / (v["ms"] / 1e3) / 1e12, 2) if v["flops"] else None}
     asm = prof["assembly"]
-    extra = {"phases_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "phases_roofline": phases_roof,
+    nsol_prof = a.batch * nprof
+    extra = {"phases_ms_per_wavelength": {k: round(v["ms"] / nsol_prof, 3) for k, v in prof.items()},
+             "phases_roofline": phases_roof,
              "assembly_hbm_gbs": asm["bytes"] / (asm["ms"] / 1e3) / 1e9 if asm["ms"] > 0 else None,
-             "assembled_pairs_per_s": (n * n * a.batch * a.steps) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
-             "refinement_iterations": iters.tolist(), "at_default_tolerance": tol_default}
+             "assembled_pairs_per_s": (n * n * nsol_prof) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
+             "refinement_iterations": iters.tolist(),
+             "launches_per_wavelength": sum(v["launches"] for k, v in launches_timed.items() if k != "geometry")
+                                        / float(a.batch * a.steps)}
     launches = int(sum(v["launches"] for k, v in launches_timed.items() if k != "geometry"))
     out = {"value": value, "ms": ms, "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                                              "d2h_bytes_per_step": int(d2h), "ms": e2e_ms,
                                              "wall_ms": e2e_wall},
            "roofline": roof, "gpu_launches": launches, "clocks": clk, "extra": extra,
-           "bem": bem, "exc": exc, "cp": cp, "sweep": sweep}
+           "bem": bem, "exc": exc, "cp": cp, "ext_timed": ext_timed}
     return out
 
 
-def fp64_comparison(a, cp, exc, torch, mixed_bem):
-    """Plain FP64 GPU path on one wavelength + accuracy of the mixed path."""
-    import mnpbem_gb300 as m
+def fp64_full(a, torch, mixed):
+    """The plain FP64 GPU path on one wavelength of the full workload, and the
+    mixed path's error against it there.  The mixed handle is released first
+    (both do not fit in device memory at 24 000 faces)."""
+    import gc
+    lam = 700.0
+    bem, exc = mixed["bem"], mixed["exc"]
+    rmx = bem.spectrum(exc, [lam])
+    mixed["bem"] = None
+    del bem
+    gc.collect()
+    torch.cuda.synchronize()
     device = torch.cuda.current_device()
-    bem64 = m.bemsolver(cp, m.bemoptions(precision="fp64", device=device))
-    lam = [450.0, 600.0, 750.0]
-    bem64.spectrum(exc, [500.0])          # warm-up (kernel loading)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    r64 = bem64.spectrum(exc, lam)
-    torch.cuda.synchronize()
-    t64 = (time.perf_counter() - t0) / len(lam)
-    rmx = mixed_bem.spectrum(exc, lam)
-    err_ext = float(np.max(np.abs(rmx["ext"] - r64["ext"]) / np.abs(r64["ext"])))
-    err_sca = float(np.max(np.abs(rmx["sca"] - r64["sca"]) / np.abs(r64["sca"])))
-    return {"value": 1.0 / t64, "unit": UNIT, "sample": "3 wavelengths (450, 600, 750 nm), same workload",
+    cp64, b64 = make_solver(a.faces, WORKLOADS[a.workload]["dimer"], device, "fp64", 1)
+    r64, t64 = _timed(lambda: b64.spectrum(exc, [lam]), torch)
+    del b64
+    gc.collect()
+    err_ext = float(np.max(np.abs(rmx["ext"][0] - r64["ext"][0]) / np.abs(r64["ext"][0])))
+    err_sca = float(np.max(np.abs(rmx["sca"][0] - r64["sca"][0]) / np.abs(r64["sca"][0])))
+    return {"value": 1.0 / t64, "unit": UNIT, "seconds": t64,
+            "sample": "1 wavelength (%g nm) of the same %d-face workload through the FP64 path (block LU + "
+                      "triangular solves + Gauss-Jordan inverse on CUDA-core FP64 GEMMs), host wall clock "
+                      "around bemsolver.spectrum" % (lam, a.faces),
             "ext_rel_err_mixed_vs_fp64": err_ext, "sca_rel_err_mixed_vs_fp64": err_sca,
-            "mixed_refine_tol": mixed_bem.refine_tol}
+            "mixed_refine_tol": a.refine_tol}
 
 
 # ------------------------------------------------- secondary workloads
@@ -445,59 +504,8 @@ def run_batch3(a, torch):
             "refinement_final_residual_max": float(max(float(r["ir_resid"].max()) for r in res))}
 
 
-def dimer_problem(faces_total, precision, dev, lanes):
-    import mnpbem_gb300 as m
-    from mnpbem_gb300 import shapes
-    nf = faces_total // 2
-    v1, f1 = shapes.fibsphere(nf, 50.0, center=(-26.0, 0.0, 0.0))
-    v2, f2 = shapes.fibsphere(nf, 50.0, center=(26.0, 0.0, 0.0))
-    cp = m.comparticle([m.epsconst(1.77), drude(), drude()], [m.particle(v1, f1), m.particle(v2, f2)],
-                       [[2, 1], [3, 1]], 1, 2)
-    return m.bemsolver(cp, m.bemoptions(precision=precision, device=dev, lanes=lanes))
-
-
-def run_dimer(a, torch):
-    """Two spheres d = 50 nm, 2 nm gap, 12000 faces each (separate media: G1
-    block-diagonal, factored as a full matrix), x-polarised along +z, 32
-    wavelengths 500-900 nm, mixed precision; the FP64 path is timed on one
-    wavelength of a dimer with --fp64-faces faces and scaled by n^3."""
-    import mnpbem_gb300 as m
-    dev = torch.cuda.current_device()
-    exc = m.planewave([1, 0, 0], [0, 0, 1])
-    enei = np.linspace(500.0, 900.0, 32)
-    bem = dimer_problem(24000, "mixed", dev, a.lanes)
-    bem.refine_iters = 20
-    bem.refine_tol = a.refine_tol
-    bem.spectrum(exc, enei[:max(1, a.lanes or 3)])        # warm-up: sizes and captures every lane
-    res, dt = _timed(lambda: bem.spectrum(exc, enei), torch)
-    value = enei.size / dt
-    b64 = dimer_problem(a.fp64_faces, "fp64", dev, 1)
-    b64.spectrum(exc, [700.0])
-    r64, t64 = _timed(lambda: b64.spectrum(exc, [700.0]), torch)
-    bmx = dimer_problem(a.fp64_faces, "mixed", dev, 1)
-    bmx.refine_iters, bmx.refine_tol = 20, a.refine_tol
-    rmx = bmx.spectrum(exc, [700.0])
-    err = float(abs(rmx["ext"][0, 0] - r64["ext"][0, 0]) / abs(r64["ext"][0, 0]))
-    scale = (24000.0 / a.fp64_faces) ** 3
-    v64 = 1.0 / (t64 * scale)
-    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64(tf32)+f64", "data": "synthetic",
-            "config": {"workload": "dimer of two d=50 nm spheres, 2 nm gap, 2 x 12000 faces, Drude metal in "
-                                   "eps=1.77, x-pol along +z, 32 wavelengths 500-900 nm", "faces": 24000,
-                       "timing": "host wall clock around bemsolver.spectrum (public API, ext/sca to host)",
-                       "refine_tol": a.refine_tol},
-            "fp64_gpu": {"value": v64, "unit": UNIT,
-                         "sample": "1 wavelength (700 nm) of a %d-face dimer, %.3f s, scaled by (24000/%d)^3"
-                                   % (a.fp64_faces, t64, a.fp64_faces)},
-            "speedup_vs_fp64_gpu": value / v64,
-            "ext_rel_err_mixed_vs_fp64": err, "ext_err_sample": "%d-face dimer at 700 nm" % a.fp64_faces,
-            "refinement_iterations": res["ir_iters"].tolist(),
-            "refinement_final_residual_max": float(np.max(res["ir_resid"]))}
-
-
 def run_iter(a, torch):
-    """Iterative solver (bemretiter) on the dimer of run_dimer (--iter-faces,
+    """Iterative solver (bemretiter) on the 2 nm-gap dimer (--iter-faces,
     default 24000 faces): H-matrices of G1, H1, G2, H2 (leaves of at most 200
     faces, htol 1e-6, kmax 100), GMRES (tol 1e-6) preconditioned by the
     complex64 tensor-core inverses.  Timed: a sweep of 8 wavelengths 600-740 nm
@@ -565,75 +573,150 @@ def bemret_spectrum(bem, exc, eneis):
 
 
 # ---------------------------------------------------------- CPU / reference
-def cpu_problem(faces):
+def cpu_problem(faces, dimer):
+    """The workload's geometry at ``faces`` faces as an oracle problem."""
     from mnpbem_gb300 import shapes
     from oracle import mnpbem_ref as R
     t = shapes.tables()
     q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
-    v, f = shapes.fibsphere(faces, 50.0)
-    cp = R.ComParticle([R.EpsConst(1.77), R.drude_eps(*DRUDE)], [R.Particle(v, f, q)], [[2, 1]], [True])
+    parts, inout = geometry(faces, dimer)
+    eps = [R.EpsConst(1.77)] + [R.drude_eps(*DRUDE) for _ in parts]
+    cp = R.ComParticle(eps, [R.Particle(v, f, q) for v, f in parts], inout, [True] * len(parts))
     vi, fi = shapes.trisphere(256, 2.0)
     pw = R.PlaneWaveRet([1, 0, 0], [0, 0, 1], R.Particle(vi, fi, q))
     return R, cp, pw
 
 
-def cpu_solve_one(R, bem, cp, pw, enei):
+def cpu_solve_phases(bem, cp, pw, enei):
+    """One oracle wavelength-solve split into its O(n^2) and O(n^3) parts:
+    returns (ext, sca, seconds of the assembly, of the inversions and
+    products of initmat, of the excitation + mldivide + cross sections)."""
     bem.enei = None
+    t0 = time.perf_counter()
+    bem.matrices(enei)
+    t1 = time.perf_counter()
+    bem.initmat(enei)                      # assembles again, then inverts
+    t2 = time.perf_counter()
     sig = bem.solve(pw.potential(cp, enei))
-    return pw.extinction(cp, sig), pw.scattering(cp, sig)
+    ext, sca = pw.extinction(cp, sig), pw.scattering(cp, sig)
+    t3 = time.perf_counter()
+    t_asm = t1 - t0
+    return ext, sca, t_asm, max(0.0, (t2 - t1) - t_asm), t3 - t2
+
+
+def extrapolate(a, t_asm, t_n3, t_rest):
+    """Seconds per wavelength-solve at the workload's size from a sample at
+    a.cpu_faces: the inversions and products scale as n^3, the rest as n^2."""
+    r = a.faces / float(a.cpu_faces)
+    return t_n3 * r ** 3 + (t_asm + t_rest) * r ** 2
+
+
+def cpu_sample_desc(a, nsolves):
+    cores = os.cpu_count()
+    extr = "" if a.cpu_faces == a.faces else (
+        "; extrapolated to %d faces: initmat's inversions and products (measured apart) scaled by (n/%d)^3, "
+        "assembly, excitation, mldivide and cross sections by (n/%d)^2" % (a.faces, a.cpu_faces, a.cpu_faces))
+    return ("%d wavelength-solve(s) of the NumPy/SciPy FP64 oracle (restatement of the reference CPU path: "
+            "initmat with explicit inverses, mldivide, ext, sca; set-up excluded) on the same geometry at %d "
+            "faces, OpenBLAS on all %d host threads%s" % (nsolves, a.cpu_faces, cores, extr))
 
 
 def cpu_baseline(a, nsolves=1):
-    faces = a.cpu_faces or a.faces
-    R, cp, pw = cpu_problem(faces)
+    R, cp, pw = cpu_problem(a.cpu_faces, WORKLOADS[a.workload]["dimer"])
     bem = R.BemRet(cp)              # set-up (refinement, sum rule) is not timed
-    t0 = time.perf_counter()
-    for i in range(nsolves):
-        cpu_solve_one(R, bem, cp, pw, float(grid()[(7 * i + 3) % NGRID]))
-    dt = time.perf_counter() - t0
-    cores = os.cpu_count()
-    scale = (faces / a.faces) ** 3
-    return {"value": nsolves / dt * scale, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d wavelength-solve(s) of the NumPy/SciPy FP64 oracle at %d faces "
-                      "(initmat with explicit inverses + mldivide + ext + sca; set-up excluded), "
-                      "OpenBLAS on all %d host threads%s" % (
-                          nsolves, faces, cores,
-                          "" if faces == a.faces else ", scaled by (n/%d)^3" % a.faces),
-            "seconds": dt}
+    t = np.zeros(3)
+    lams = [float(grid(a)[(7 * i + 3) % grid(a).size]) for i in range(nsolves)]
+    res = []
+    for lam in lams:
+        ext, sca, *ph = cpu_solve_phases(bem, cp, pw, lam)
+        t += ph
+        res.append((lam, ext, sca))
+    t /= nsolves
+    sec = extrapolate(a, *t)
+    return {"value": 1.0 / sec, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": cpu_sample_desc(a, nsolves),
+            "seconds_per_solve_at_sample": float(t.sum()), "phases_s_at_sample": [float(x) for x in t],
+            "extrapolated": a.cpu_faces != a.faces}, res
+
+
+def parity_at_sample(a, torch, oracle_res):
+    """GPU solves (mixed and FP64) of the CPU sample's problem at the oracle's
+    wavelengths against the oracle's cross sections."""
+    import mnpbem_gb300 as m
+    dev = torch.cuda.current_device()
+    exc = m.planewave([1, 0, 0], [0, 0, 1])
+    out = {"faces": a.cpu_faces, "geometry": WORKLOADS[a.workload]["dimer"] and "dimer" or "sphere"}
+    for prec in ("mixed", "fp64"):
+        cp, bem = make_solver(a.cpu_faces, WORKLOADS[a.workload]["dimer"], dev, prec, 1, a.refine_tol)
+        lams = [r[0] for r in oracle_res]
+        r = bem.spectrum(exc, lams)
+        e_ext = max(float(np.max(np.abs(r["ext"][i] - o[1]) / np.abs(o[1]))) for i, o in enumerate(oracle_res))
+        e_sca = max(float(np.max(np.abs(r["sca"][i] - o[2]) / np.abs(o[2]))) for i, o in enumerate(oracle_res))
+        out[prec] = {"ext_rel_err_vs_oracle": e_ext, "sca_rel_err_vs_oracle": e_sca,
+                     "refine_tol": a.refine_tol if prec == "mixed" else None}
+        del bem
+    out["wavelengths"] = [r[0] for r in oracle_res]
+    return out
+
+
+def run_c2(torch, device):
+    """Short device-timed sweep of the 4000-face sphere (configuration 2)."""
+    import argparse as _ap
+    b = _ap.Namespace(workload="sphere4000", faces=4000, batch=20, lanes=0, refine_tol=1e-8)
+    cp, bem, exc = make_problem(b, device, "mixed")
+    sweep = DeviceSweep(bem, exc, b.batch, torch)
+    stream = lib_stream(bem, torch)
+    for s in range(2):
+        sweep.run(step_wavelengths(b, s, 0, 1, b.batch))
+    bem._lib.mnpbem_profile_reset(bem.handle)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    steps = 3
+    for s in range(steps):
+        sweep.run(step_wavelengths(b, 2 + s, 0, 1, b.batch))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    lt = read_profile(bem)
+    launches = sum(v["launches"] for k, v in lt.items() if k != "geometry")
+    return {"workload": workload_desc(b, batch=b.batch), "value": steps * b.batch / (ms / 1e3), "unit": UNIT,
+            "steps": steps, "ms_per_step": ms / steps, "launches_per_wavelength": launches / float(steps * b.batch),
+            "refinement_iterations": sweep.iters.tolist(), "refine_tol": b.refine_tol}
 
 
 def run_reference(a, rank, world):
     if rank != 0:
         return None
+    dimer = WORKLOADS[a.workload]["dimer"]
     # warm-up: small solves (NumPy/BLAS thread pools, page-in)
-    R, cps, pws = cpu_problem(284)
+    R, cps, pws = cpu_problem(284, False)
     bs = R.BemRet(cps)
     for s in range(a.warmup):
-        cpu_solve_one(R, bs, cps, pws, 500.0)
-    faces = a.cpu_faces or a.faces
-    R, cp, pw = cpu_problem(faces)
+        cpu_solve_phases(bs, cps, pws, 500.0)
+    R, cp, pw = cpu_problem(a.cpu_faces, dimer)
     bem = R.BemRet(cp)
-    times = []
+    ph = np.zeros(3)
+    wall = 0.0
     for s in range(a.steps):
-        lam = float(step_wavelengths(s, 0, 1, 1)[0])
+        lam = float(step_wavelengths(a, s, 0, 1, 1)[0])
         t0 = time.perf_counter()
-        cpu_solve_one(R, bem, cp, pw, lam)
-        times.append(time.perf_counter() - t0)
-    ms = 1e3 * float(np.sum(times))
-    scale = (faces / a.faces) ** 3
-    value = a.steps / (ms / 1e3) * scale
-    cores = os.cpu_count()
-    sample = ("1 wavelength-solve per step of the NumPy/SciPy FP64 oracle (restatement of the "
-              "reference CPU path) at %d faces, OpenBLAS on all %d host threads%s"
-              % (faces, cores, "" if faces == a.faces else ", scaled by (n/%d)^3" % a.faces))
+        _, _, *t = cpu_solve_phases(bem, cp, pw, lam)
+        wall += time.perf_counter() - t0
+        ph += t
+    ph /= a.steps
+    sec = extrapolate(a, *ph)
+    value = 1.0 / sec
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
-            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+            "warmup": a.warmup, "ms_per_step": 1e3 * wall / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": workload_desc(a), "faces": a.faces, "wavelengths_per_step": 1,
                        "l2": "working set of dense n x n complex128 matrices > L2"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": cpu_sample_desc(a, 1) + " per step",
+                             "phases_s_at_sample": [float(x) for x in ph],
+                             "extrapolated": a.cpu_faces != a.faces},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -643,14 +726,18 @@ def main():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if a.impl == "reference":
+        if a.workload not in WORKLOADS:
+            print(json.dumps({"impl": "reference", "unavailable": "reference arm is defined for dimer24k and "
+                                                                   "sphere4000 only"}))
+            return
         line = run_reference(a, rank, world)
         if line is not None:
             print(json.dumps(line))
         return
     import torch
-    if a.workload != "sphere4000":
+    if a.workload not in WORKLOADS:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        line = {"batch3": run_batch3, "dimer24k": run_dimer, "iter24k": run_iter}[a.workload](a, torch)
+        line = {"batch3": run_batch3, "iter24k": run_iter}[a.workload](a, torch)
         if rank == 0:
             print(json.dumps(line))
         return
@@ -660,27 +747,34 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
     r = run_ours(a, rank, world, dist, torch)
-    fp64 = None
-    if rank == 0 and not a.skip_fp64:
-        fp64 = fp64_comparison(a, r["cp"], r["exc"], torch, r["bem"])
-    cpu = None
+    device = torch.cuda.current_device()
+    fp64 = cpu = parity = c2 = None
+    if rank == 0 and not a.skip_fp64 and a.precision == "mixed":
+        fp64 = fp64_full(a, torch, r)
+    r["bem"] = None
+    import gc
+    gc.collect()
     if rank == 0 and not a.skip_cpu:
-        cpu = cpu_baseline(a)
+        cpu, ores = cpu_baseline(a)
+        parity = parity_at_sample(a, torch, ores)
+    if rank == 0 and not a.skip_c2 and a.workload != "sphere4000":
+        c2 = run_c2(torch, device)
     if dist is not None:
         dist.barrier()
     if rank == 0:
         n = r["cp"].n
-        wset = (5 * 8 + 4 * 16) * n * n
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": r["ms"] / a.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
-                "config": {"workload": workload_desc(a), "faces": n, "wavelengths_per_step": a.batch,
+                "config": {"workload": workload_desc(a, batch=a.batch), "faces": n, "wavelengths_per_step": a.batch,
                            "precision": a.precision, "lanes": a.lanes or tuned_lanes(n, a.precision),
                            "refine_tol": a.refine_tol if a.precision == "mixed" else None,
-                           "l2": "no flush: per-wavelength working set %.2f GB > 129 MB L2" % (wset / 1e9)},
+                           "l2": "no flush: the working set of one wavelength (%.1f GB of dense matrices) is "
+                                 "far larger than the 129 MB L2" % ((5 * 8 + 4 * 16) * n * n / 1e9)},
                 "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],
-                "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64}
+                "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64, "parity_vs_oracle": parity,
+                "c2_sphere4000": c2}
         if fp64:
             line["speedup_vs_fp64_gpu"] = r["value"] / fp64["value"]
         line.update(r["extra"])

@@ -259,8 +259,9 @@ MNPBEM_API mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M
  * DEVICE pointer and the scratch (far fields) is a fixed __device__ array in
  * the library, shared by all calls on a device and held until process exit.
  * No counterpart in the reference.  Limits: npol <= 4 and npol + ninf <= 2048
- * directions (larger sizes return MNPBEM_ERR_INVALID_ARG).  The first call on
- * a device looks up the scratch address: make it before any stream capture.
+ * directions (larger sizes return MNPBEM_ERR_INVALID_ARG).  Each call looks up
+ * the scratch address in the current context (valid after a device reset); the
+ * first call on a device loads the module: make it before any stream capture.
  * Calls whose kernels overlap on the GPU race on the shared scratch.
  * Asynchronous on `stream` (cudaStream_t, NULL = default stream).
  *   pos [n][3], area [n]; exc_in / exc_out [n]: 1 where the inside / outside

@@ -16,14 +16,16 @@
 // library holds until the process exits.
 //
 // Host code cannot use the array's name as a device address (in host code it
-// is only a stand-in).  The first call on a device, with that device current,
-// looks the address up with cudaGetSymbolAddress and caches it; make that
-// first call before any stream capture.  Every call shares the array and it
+// is only a stand-in).  Every call, with its device current, looks the address
+// up with cudaGetSymbolAddress (a host-side query that allocates nothing), so
+// that a context re-created after cudaDeviceReset (MATLAB's reset(gpuDevice))
+// never leaves a stale address behind.  The first call on a device also loads
+// the library's module into that context: make it before any stream capture.
+// Every call shares the array and it
 // keeps the previous call's contents: each call first writes every entry it
 // later reads, so nothing needs clearing, but calls whose kernels overlap on
 // the GPU (different streams, or threads sharing a device) race on it.
 #include <complex>
-#include <mutex>
 
 #include "bem.cuh"
 
@@ -31,12 +33,9 @@ namespace mnpbem {
 
 constexpr int NOALLOC_MAX_POL = 4;
 constexpr int NOALLOC_MAX_DIRS = 2048;   // excitation directions + sphere-at-infinity directions
-constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) double2 g_noalloc_fields[NOALLOC_MAX_DIRS * 6 * NOALLOC_MAX_POL];
 
-static double2* g_noalloc_addr[NOALLOC_MAX_DEVICES];
-static std::mutex g_noalloc_mutex;
 
 // Far fields of one direction per block, inputs in the public solution layout
 // (sig [n][P], h [n][3][P]); direction d < P is dir[d], else inf_nvec[d - P].
@@ -114,20 +113,17 @@ __global__ void __launch_bounds__(256) k_farfield_noalloc(
   }
 }
 
-// device address of the scratch array on the current device (set-up, once per device)
-static mnpbem_status noalloc_scratch(int device, double2** out) {
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[device]) {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_fields);
-    if (e != cudaSuccess || !ptr) {
-      cudaGetLastError();
-      set_error("cudaGetSymbolAddress of the cross-section scratch failed: %s", cudaGetErrorString(e));
-      return MNPBEM_ERR_CUDA;
-    }
-    g_noalloc_addr[device] = static_cast<double2*>(ptr);
+// device address of the scratch array in the current context, looked up on
+// every call: a cached address would outlive a reset of the device's context
+static mnpbem_status noalloc_scratch(double2** out) {
+  void* ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_fields);
+  if (e != cudaSuccess || !ptr) {
+    cudaGetLastError();
+    set_error("cudaGetSymbolAddress of the cross-section scratch failed: %s", cudaGetErrorString(e));
+    return MNPBEM_ERR_CUDA;
   }
-  *out = g_noalloc_addr[device];
+  *out = static_cast<double2*>(ptr);
   return MNPBEM_OK;
 }
 
@@ -157,13 +153,15 @@ extern "C" mnpbem_status mnpbem_cross_sections_noalloc(
               (long long)npol + ninf, NOALLOC_MAX_DIRS);
     return MNPBEM_ERR_INVALID_ARG;
   }
-  if (device < 0 || device >= NOALLOC_MAX_DEVICES) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess) cudaGetLastError();
+  if (device < 0 || device >= ndev) {
     set_error("mnpbem_cross_sections_noalloc: invalid device %d", (int)device);
     return MNPBEM_ERR_INVALID_ARG;
   }
   MNP_CUDA(cudaSetDevice(device));
   double2* fields = nullptr;
-  MNP_TRY(noalloc_scratch(device, &fields));
+  MNP_TRY(noalloc_scratch(&fields));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const double k0 = 2 * M_PI / enei;
   const std::complex<double> kmed = k0 * std::sqrt(std::complex<double>(eps_exc[0], eps_exc[1]));

@@ -1,7 +1,9 @@
 """Host logic of the multi-GPU bench path on two CPU ranks (gloo): every rank
 takes its own wavelengths of each step (the ranks' sets are disjoint, and the
-steps walk the 60-point grid), and the timings are reduced to their maximum
-over ranks with no other collective."""
+steps walk the workload's grid: 60 points for the 4000-face sphere, 32 for the
+24 000-face dimer), and the timings are reduced to their maximum over ranks
+with no other collective."""
+import argparse
 import os
 import socket
 
@@ -18,7 +20,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, world, port, batch, steps, out):
+def _rank(rank, world, port, workload, batch, steps, out):
     import sys
     sys.path.insert(0, ROOT)
     import torch
@@ -27,7 +29,8 @@ def _rank(rank, world, port, batch, steps, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        mine = np.concatenate([bench.step_wavelengths(s, rank, world, batch) for s in range(steps)])
+        a = argparse.Namespace(workload=workload)
+        mine = np.concatenate([bench.step_wavelengths(a, s, rank, world, batch) for s in range(steps)])
         got = [None] * world
         dist.all_gather_object(got, mine.tolist())
         ms = bench.max_over_ranks(dist, [10.0 + rank, 5.0 - rank], "cpu", torch)
@@ -36,12 +39,13 @@ def _rank(rank, world, port, batch, steps, out):
         dist.destroy_process_group()
 
 
-def test_two_ranks_share_the_grid_and_reduce_max():
-    world, batch, steps = 2, 10, 3
+@pytest.mark.parametrize("workload,batch,steps", [("sphere4000", 10, 3), ("dimer24k", 4, 4)])
+def test_two_ranks_share_the_grid_and_reduce_max(workload, batch, steps):
+    world = 2
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, world, port, batch, steps, q)) for r in range(world)]
+    procs = [ctx.Process(target=_rank, args=(r, world, port, workload, batch, steps, q)) for r in range(world)]
     for p in procs:
         p.start()
     res = [q.get(timeout=120) for _ in range(world)]
@@ -49,7 +53,7 @@ def test_two_ranks_share_the_grid_and_reduce_max():
         p.join(timeout=60)
         assert p.exitcode == 0
     import bench
-    grid = bench.grid()
+    grid = bench.grid(argparse.Namespace(workload=workload))
     for rank, got, ms in res:
         assert ms == [10.0 + world - 1, 5.0]
         a, b = np.array(got[0]), np.array(got[1])
@@ -58,7 +62,7 @@ def test_two_ranks_share_the_grid_and_reduce_max():
         for s in range(steps):
             sa, sb = a[s * batch:(s + 1) * batch], b[s * batch:(s + 1) * batch]
             assert not set(sa.tolist()) & set(sb.tolist())
-        # three steps of two ranks x 10 wavelengths cover the 60-point grid once
+        # the steps of two ranks cover the grid once
         assert np.array_equal(np.sort(np.concatenate([a, b])), np.sort(grid))
 
 

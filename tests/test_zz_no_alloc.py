@@ -59,6 +59,7 @@ def test_cross_sections_noalloc_matches_solve(gpu_lib):
         ext.fill_(float("nan"))
         sca.fill_(float("nan"))
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
         st = gpu_lib.mnpbem_cross_sections_noalloc(
             0, None, n, P, ptr(pos), ptr(area), ptr(exc_in), ptr(exc_out), ptr(fields["sig1"]),
             ptr(fields["h1"]), ptr(fields["sig2"]), ptr(fields["h2"]), ptr(pol), ptr(dirs),
@@ -66,6 +67,9 @@ def test_cross_sections_noalloc_matches_solve(gpu_lib):
             eps_1.ctypes.data, ptr(ext), ptr(sca))
         _lib.check(st)
         torch.cuda.synchronize()
+        if w > 0:
+            # after the first call (which loads the module) no device memory is taken
+            assert torch.cuda.mem_get_info(0)[0] == free0
         got_ext, got_sca = ext.cpu().numpy(), sca.cpu().numpy()
         e_ext = np.max(np.abs(got_ext - ref["ext"][w]) / np.abs(ref["ext"][w]))
         e_sca = np.max(np.abs(got_sca - ref["sca"][w]) / np.abs(ref["sca"][w]))
@@ -77,3 +81,9 @@ def test_cross_sections_noalloc_matches_solve(gpu_lib):
         ptr(pos), ptr(pol), ptr(dirs), 5000, ptr(inf_nvec), ptr(inf_area), 500.0,
         eps_exc.ctypes.data, eps_1.ctypes.data, ptr(ext), ptr(sca))
     assert big == 1 and b"exceed the maximum" in gpu_lib.mnpbem_last_error()
+    # more polarisations than the scratch holds are rejected too
+    many = gpu_lib.mnpbem_cross_sections_noalloc(
+        0, None, n, 5, ptr(pos), ptr(area), ptr(exc_in), ptr(exc_out), ptr(pos), ptr(pos), ptr(pos),
+        ptr(pos), ptr(pol), ptr(dirs), 10, ptr(inf_nvec), ptr(inf_area), 500.0,
+        eps_exc.ctypes.data, eps_1.ctypes.data, ptr(ext), ptr(sca))
+    assert many == 1 and b"exceeds the maximum" in gpu_lib.mnpbem_last_error()
