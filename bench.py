@@ -333,6 +333,7 @@ def run_ours(a, rank, world, dist, torch):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     launches_timed = read_profile(bem)
+    block_cond = bem.stat("block_cond_max")
     iters = sweep.iters.copy()
     ext_timed = sweep.ext.cpu().numpy().copy()
     # ---------------- profiled repeat of a few of the same steps: CUDA events on
@@ -403,6 +404,10 @@ def run_ours(a, rank, world, dist, torch):
              "assembly_hbm_gbs": asm["bytes"] / (asm["ms"] / 1e3) / 1e9 if asm["ms"] > 0 else None,
              "assembled_pairs_per_s": (n * n * nsol_prof) / (asm["ms"] / 1e3) if asm["ms"] > 0 else None,
              "refinement_iterations": iters.tolist(),
+             "pivot_stat": {"block_cond_max": block_cond, "g1_blocks": int(bem.stat("g1_blocks")),
+                            "note": "largest max|A_kk| * max|inv(A_kk)| over the diagonal blocks of the LDU "
+                                    "factorisations (G1, G2, Sigma) and of the Gauss-Jordan inverse of Delta, "
+                                    "warm-up and timed steps; 1e6 fails the solve in complex64"},
              "launches_per_wavelength": sum(v["launches"] for k, v in launches_timed.items() if k != "geometry")
                                         / float(a.batch * a.steps)}
     launches = int(sum(v["launches"] for k, v in launches_timed.items() if k != "geometry"))

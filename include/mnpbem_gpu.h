@@ -290,13 +290,23 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
  * the tensor-core inversions: 256 or 512), "tc_stages" (TMA pipeline depth of
  * the tensor-core GEMM: 3 or 4), "tc_ctas" (CTAs of the persistent
  * tensor-core GEMM, 0 = one per SM; fewer leave SMs to the pivot-block
- * clusters of other lanes), "tc_pair" (CTA-pair tensor-core GEMM with
- * 256 x 256 tiles for products of at least 256 rows: 0 never (default),
- * 1 always, -1 products with K >= 1024), "tf32_round" (round A operands to nearest
+ * clusters of other lanes), "tc_pair" (only 0: the CTA-pair tensor-core GEMM
+ * is not used inside sweeps; 1 / -1 return MNPBEM_ERR_UNSUPPORTED),
+ * "lu_steps" (256-row LDU steps gathered into one trailing update: 1, 2 or
+ * 4, i.e. updates of rank 256, 512 or 1024), "tf32_round" (round A operands to nearest
  * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
  * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
  * No counterpart in the reference.                                          */
 MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t value);
+
+/* Statistics of a handle: "block_cond_max" (largest condition proxy
+ * max|A_kk| * max|inv(A_kk)| over the diagonal blocks of every factorisation
+ * and inversion since the last "block_cond_reset"; a block above 1e6
+ * (complex64) or 1e13 (FP64) fails the solve with MNPBEM_ERR_SINGULAR),
+ * "block_cond_reset", "g1_blocks" (number of diagonal blocks G1 is factored
+ * in).  No counterpart in the reference (MATLAB's inv reports a near-singular
+ * matrix as a warning).                                                      */
+MNPBEM_API mnpbem_status mnpbem_geom_stat(mnpbem_geom* g, const char* key, double* value);
 
 /* The handle's CUDA stream (cudaStream_t).  mnpbem_solve runs lane 0 on it
  * and makes it wait for the other lanes before returning, so work queued on
@@ -452,6 +462,14 @@ MNPBEM_API mnpbem_status mnpbem_solve_iter(mnpbem_geom* g, const mnpbem_cluster_
 MNPBEM_API mnpbem_status mnpbem_hmat_full(mnpbem_geom* g, const mnpbem_cluster_tree* tree,
                                           const mnpbem_iter_options* op, double enei, const double* eps_media,
                                           int32_t nmed, int32_t which, double* out, int32_t* ranks);
+
+/* Self test of the bounded device-side waits that every pipelined kernel of
+ * the library uses (mbarrier waits with a wall-clock limit): one CTA waits,
+ * with a limit of limit_us microseconds (1 .. 1e6), on a barrier that nothing
+ * completes; the wait expires, the kernel records an error code and returns.
+ * Returns MNPBEM_ERR_TIMEOUT (the expected outcome), and the context stays
+ * usable.  No counterpart in the reference (its MEX code has no device waits). */
+MNPBEM_API mnpbem_status mnpbem_selftest_bounded_wait(int32_t device, int32_t limit_us);
 
 /* Message of the last failure on the calling thread ("" if none). */
 MNPBEM_API const char* mnpbem_last_error(void);

@@ -147,6 +147,8 @@ SIGNATURES = {
     "mnpbem_geom_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_geom_set_lanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "mnpbem_geom_set_option": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int32]),
+    "mnpbem_geom_stat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p]),
+    "mnpbem_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
     "mnpbem_last_error": (ctypes.c_char_p, []),
     "mnpbem_version": (ctypes.c_char_p, []),
 }

@@ -3,9 +3,11 @@
 For a problem size it times short wavelength sweeps on the GPU over the
 options of ``mnpbem_geom_set_option`` -- the tensor-core GEMM's TMA pipeline
 depth (3 or 4 stages of 128 x 256 x 32 tiles), the Gauss-Jordan step width
-of the tensor-core inversions (256 or 512: the K extent of the rank-nb
-updates and the size of the pivot blocks), the number of wavelengths in
-flight (lanes) -- and stores the fastest combination in ``data/tuned.json``
+of the tensor-core inversion of Delta (256 or 512: the K extent of its
+rank-nb updates and the size of its pivot blocks), the number of 256-row LDU
+steps gathered into one trailing update of the factorisations (1, 2, 4: rank
+256, 512, 1024), the number of wavelengths in flight (lanes) -- and stores
+the fastest combination in ``data/tuned.json``
 keyed by the face count.  ``bemsolver`` applies the entry whose face count is
 closest (within a factor of 2) when it creates a mixed-precision solver.
 
@@ -21,7 +23,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED = os.path.join(_HERE, "data", "tuned.json")
-GRID = {"tc_stages": (3, 4), "gj_block": (256, 512), "lanes": (2, 4, 6, 8)}
+GRID = {"tc_stages": (3, 4), "gj_block": (256, 512), "lu_steps": (1, 2, 4), "lanes": (2, 4, 6, 8)}
 
 
 def load():

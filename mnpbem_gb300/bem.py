@@ -292,6 +292,14 @@ class bemret:
         """Wavelengths kept in flight at once by ``spectrum`` (0 = automatic)."""
         _lib.check(self._lib.mnpbem_geom_set_lanes(self._h, int(lanes)))
 
+    def stat(self, key):
+        """Statistic of the handle (``mnpbem_geom_stat``): 'block_cond_max'
+        (largest condition proxy of the diagonal blocks factored since the
+        last 'block_cond_reset'), 'g1_blocks'."""
+        v = ctypes.c_double()
+        _lib.check(self._lib.mnpbem_geom_stat(self._h, key.encode(), ctypes.byref(v)))
+        return v.value
+
     # ----------------------------------------------------------- queries
     @property
     def handle(self):

@@ -1,13 +1,17 @@
 // C ABI of the library: handle management and the per-wavelength solve.
 //
 // The per-wavelength sequence follows BEM/@bemret/private/initmat.m:5-74 and
-// BEM/@bemret/mldivide.m:12-49:
+// BEM/@bemret/mldivide.m:12-49, with the inverses of G1, G2 and Sigma replaced
+// by block LDU factors (dense.cu) and triangular solves:
 //   assemble G1, H1, G2, H2                    (compgreenret eval, assemble.cu)
-//   G1i = inv(G1), G2i = inv(G2)               (blocked Gauss-Jordan, dense.cu)
-//   Sigma1 = H1 G1i, Sigma2 = H2 G2i           (GEMM)
-//   Deltai = inv(Sigma1 - Sigma2)
-//   Sigma = Sigma1 L1 - Sigma2 L2 + k^2 ((L Deltai) .* (n n')) L,  Sigmai = inv(Sigma)
-//   excitation, mldivide chain, spectra        (bem.cu)
+//   G1 = L D U, G2 = L D U                     (G1 per diagonal block when the
+//                                               particles' media do not couple)
+//   Sigma1 = H1 G1^-1, Sigma2 = H2 G2^-1       (right-side triangular solves)
+//   Deltai = inv(Sigma1 - Sigma2)              (blocked Gauss-Jordan: needed
+//                                               elementwise by the Sigma term)
+//   Sigma = Sigma1 L1 - Sigma2 L2 + k^2 ((L Deltai) .* (n n')) L,  Sigma = L D U
+//   excitation, mldivide chain, spectra        (bem.cu; G1i x, G2i x, Sigmai x
+//                                               as triangular solves)
 // MNPBEM_MIXED runs the inversions and products on complex64 operands and
 // recovers FP64 accuracy by iterative refinement with the FP64 operator of
 // BEM/@bemretiter/private/afun.m:6-35 (the complex64 chain is the preconditioner).
@@ -15,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <complex>
+#include <functional>
 #include <algorithm>
 #include <memory>
 #include <thread>
@@ -99,8 +104,11 @@ struct Lane {
   DevBuf vec64, vecw, facebuf, fields, norms, outbuf, bsplit, lp_dev;
   GJWork<float> gj32;    // block width set per solve (256 on the tensor-core path)
   GJWork<double> gj64;
+  LDUWork<float> lu32;   // block LDU factors of G1, G2, Sigma
+  LDUWork<double> lu64;
+  DevBuf lu_status;      // LDU status words (see dense.cuh)
   TcGemmCtx tc;
-  int* status_host = nullptr;     // pinned: pivot status words (2)
+  int* status_host = nullptr;     // pinned: Gauss-Jordan (4), LDU (2), tensor-core error word (1), spare
   double* norms_host = nullptr;   // pinned: refinement norms (4)
   cudaEvent_t ev = nullptr;       // completion of the work last queued by the scheduler
   struct Graphs {
@@ -111,6 +119,7 @@ struct Lane {
     cudaGraphExec_t exec[NSTAGES] = {};
     Profiler::GraphRec rec[NSTAGES];
   } graphs;
+  float cond_max = 0.f;       // largest block condition proxy since the counter was reset
   // scheduler state
   enum { IDLE = 0, ITER, DONE } state = IDLE;
   int w = -1, iters = 0;
@@ -150,6 +159,8 @@ struct mnpbem_geom {
   std::vector<std::unique_ptr<Lane>> lanes;
   int lanes_req = 0;        // 0: automatic
   int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
+  int lu_steps = 2;         // LDU steps of 256 per trailing update on the tensor-core path (1, 2 or 4)
+  std::vector<int64_t> g1_off, g1_n;   // diagonal blocks of G1 (one block when G1 is full)
   bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
   bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
   bool gj_fused = true;     // fused Gauss-Jordan steps on the tensor-core path
@@ -168,6 +179,7 @@ namespace {
 
 constexpr int MAX_LANES = 16;
 constexpr int DEFAULT_LANES = 4;
+constexpr int LANE_NSTATUS = 8;
 
 mnpbem_status check_geom(const mnpbem_geom* g) {
   if (!g) { set_error("null geometry handle"); return MNPBEM_ERR_INVALID_ARG; }
@@ -200,7 +212,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
     MNP_CUDA(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking));
     L->own_stream = true;
   }
-  cudaError_t e = cudaMallocHost(&L->status_host, 2 * sizeof(int));
+  cudaError_t e = cudaMallocHost(&L->status_host, LANE_NSTATUS * sizeof(int));
   if (e == cudaSuccess) e = cudaMallocHost(&L->norms_host, 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming);
   mnpbem_status s = MNPBEM_OK;
@@ -210,11 +222,12 @@ mnpbem_status add_lane(mnpbem_geom* G) {
     s = MNPBEM_ERR_CUDA;
   }
   if (s == MNPBEM_OK) s = L->lp_dev.ensure(sizeof(LamParams));
+  if (s == MNPBEM_OK) s = L->lu_status.ensure(2 * sizeof(int));
   if (s != MNPBEM_OK) {
     lane_release(*L);
     return s;
   }
-  L->status_host[0] = L->status_host[1] = 0;
+  for (int q = 0; q < LANE_NSTATUS; ++q) L->status_host[q] = 0;
   if (G->tc_stages) L->tc.stages = G->tc_stages;
   L->tc.max_ctas = G->tc_ctas;
   L->tc.pair = G->tc_pair;
@@ -234,6 +247,41 @@ void fill_media(const mnpbem_geom* G, AsmParams& p) {
       p.med[2][a][b] = (signed char)(oa == ob ? oa : 0);  // con{2,2}
       p.med[3][a][b] = (signed char)(ia == ob ? ia : 0);  // con{1,2}
     }
+}
+
+// Diagonal blocks of G1 = G11 - G21 and H1 = H11 - H21 (initmat.m:27-31):
+// block (a, b) is non-zero when con{1,1} or con{2,1} connects the particles
+// (the same inside medium, or the outside medium of a is the inside medium of
+// b; Particles/@compound/connect.m:40-57).  Particles that couple directly
+// or through others form one block; when every group is a contiguous range
+// of particles, G1 is block-diagonal over their face ranges (e.g. the two
+// spheres of a dimer with separate media), otherwise one full block.
+void set_g1_blocks(mnpbem_geom* G) {
+  const int np = G->nparts;
+  std::vector<int> root(np);
+  for (int a = 0; a < np; ++a) root[a] = a;
+  std::function<int(int)> find = [&](int a) { return root[a] == a ? a : (root[a] = find(root[a])); };
+  for (int a = 0; a < np; ++a)
+    for (int b = 0; b < np; ++b) {
+      const int ia = G->inout[2 * a], oa = G->inout[2 * a + 1], ib = G->inout[2 * b];
+      if (a != b && (ia == ib || oa == ib)) root[find(a)] = find(b);
+    }
+  G->g1_off.clear();
+  G->g1_n.clear();
+  bool contiguous = true;
+  for (int a = 0; a < np && contiguous; ++a) {
+    if (a > 0 && find(a) == find(a - 1)) continue;   // same group as the previous particle
+    for (int b = 0; b < a; ++b)
+      if (find(b) == find(a)) contiguous = false;    // the group appeared before a gap
+    G->g1_off.push_back(G->part_off[a]);
+  }
+  if (!contiguous || (int)G->g1_off.size() > CHAIN_MAXBLK) {
+    G->g1_off.assign(1, 0);
+    G->g1_n.assign(1, G->part_off[np]);
+    return;
+  }
+  for (size_t q = 0; q < G->g1_off.size(); ++q)
+    G->g1_n.push_back((q + 1 < G->g1_off.size() ? G->g1_off[q + 1] : G->part_off[np]) - G->g1_off[q]);
 }
 
 bool con12_zero(const mnpbem_geom* G) {
@@ -335,6 +383,7 @@ static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const
   G->face_part.resize(nfaces);
   for (int i = 0; i < nparts; ++i)
     for (int64_t k = G->part_off[i]; k < G->part_off[i + 1]; ++k) G->face_part[k] = i;
+  set_g1_blocks(G);
   std::vector<int> cs, ce;
   for (int i = 0; i < nparts; ++i)
     if (!closed || closed[i]) { cs.push_back((int)G->part_off[i]); ce.push_back((int)G->part_off[i + 1]); }
@@ -398,6 +447,8 @@ static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const
   if (gjfenv && gjfenv[0] == '0') G->gj_fused = false;
   const char* nbenv = getenv("MNPBEM_GJ_NB");
   if (nbenv && atoi(nbenv) == 512) G->gj_nb = 512;
+  const char* luenv = getenv("MNPBEM_LU_STEPS");
+  if (luenv && (atoi(luenv) == 1 || atoi(luenv) == 2 || atoi(luenv) == 4)) G->lu_steps = atoi(luenv);
   const char* lenv = getenv("MNPBEM_LANES");
   if (lenv && atoi(lenv) > 0) G->lanes_req = std::min(MAX_LANES, atoi(lenv));
   *out = G;
@@ -476,11 +527,19 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
     for (auto& L : g->lanes) L->tc.stages = value;
     return MNPBEM_OK;
   }
-  if (k == "tc_pair" && value >= -1 && value <= 1) {
-    g->tc_pair = value;
-    for (auto& L : g->lanes) L->tc.pair = value;
+  if (k == "tc_pair" && value == 0) {
+    g->tc_pair = 0;
+    for (auto& L : g->lanes) L->tc.pair = 0;
     return MNPBEM_OK;
   }
+  if (k == "tc_pair" && (value == 1 || value == -1)) {
+    // a four-lane sweep with the CTA-pair GEMM once ran until its time limit
+    // without a recorded cause; the sweep keeps the single-CTA kernel until the
+    // cause is known (the pair kernel stays available to mnpbem_gemm_c64)
+    set_error("tc_pair: the CTA-pair GEMM is not enabled inside sweeps");
+    return MNPBEM_ERR_UNSUPPORTED;
+  }
+  if (k == "lu_steps" && (value == 1 || value == 2 || value == 4)) { g->lu_steps = value; return MNPBEM_OK; }
   if (k == "tc_ctas" && value >= 0 && value <= 4096) {
     g->tc_ctas = value;
     for (auto& L : g->lanes) L->tc.max_ctas = value;
@@ -489,6 +548,29 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
   if (k == "tf32_round" && (value == 0 || value == 1)) { g->tf32_rna = value != 0; return MNPBEM_OK; }
   if (k == "assembly_ds" && (value == 0 || value == 1)) { g->asm_ds = value != 0; return MNPBEM_OK; }
   set_error("unknown option '%s' or value %d out of range", key, value);
+  return MNPBEM_ERR_INVALID_ARG;
+}
+
+mnpbem_status mnpbem_geom_stat(mnpbem_geom* g, const char* key, double* value) {
+  MNP_TRY(check_geom(g));
+  if (!key || !value) { set_error("mnpbem_geom_stat: invalid arguments"); return MNPBEM_ERR_INVALID_ARG; }
+  const std::string k(key);
+  if (k == "block_cond_max") {
+    float c = 0.f;
+    for (auto& L : g->lanes) c = std::max(c, L->cond_max);
+    *value = c;
+    return MNPBEM_OK;
+  }
+  if (k == "block_cond_reset") {
+    for (auto& L : g->lanes) L->cond_max = 0.f;
+    *value = 0.0;
+    return MNPBEM_OK;
+  }
+  if (k == "g1_blocks") {
+    *value = (double)g->g1_off.size();
+    return MNPBEM_OK;
+  }
+  set_error("mnpbem_geom_stat: unknown key '%s'", key);
   return MNPBEM_ERR_INVALID_ARG;
 }
 
@@ -701,7 +783,8 @@ size_t lane_bytes_estimate(const mnpbem_geom* G, int precision, int P, int ninf)
   const size_t n = G->g.n, ld = G->ld;
   const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
   size_t b = 5 * es * n * ld;
-  if (precision == MNPBEM_MIXED) b += 4 * 2 * sizeof(float2) * n * ld + 16 * n * n;  // planes + B' of the n^3 GEMMs
+  // hi / lo planes, B' of the rank-1024 products and the LDU panels
+  if (precision == MNPBEM_MIXED) b += 4 * 2 * sizeof(float2) * n * ld + 3 * 8 * 1024 * n;
   b += sizeof(double2) * n * P * 80 + sizeof(float2) * n * P * 56;
   b += 3 * es * n * 256 + sizeof(double2) * (size_t)(P + ninf) * 6 * P + 64 * n;
   return b;
@@ -748,6 +831,15 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   };
   gj(L.gj32);
   gj(L.gj64);
+  auto lu = [&](const auto& w) {
+    mixbuf(w.ccol); mixbuf(w.rrow); mixbuf(w.xblk); mixbuf(w.tmp);
+    mix(nullptr, (size_t)w.b);
+    mix(nullptr, (size_t)w.m);
+  };
+  lu(L.lu32);
+  lu(L.lu64);
+  mixbuf(L.lu_status);
+  mix(nullptr, (size_t)G->lu_steps);
   mix(L.status_host, 0);
   mix(L.norms_host, 0);
   // tuning options baked into the captured launches
@@ -811,19 +903,39 @@ mnpbem_status gemm_w<double>(int64_t M, int64_t N, int64_t K, double2 al, const 
 }
 
 template <typename R>
-ChainMats<R> chain_mats(const mnpbem_geom* G, Lane& L) {
-  using Cx = cplx<R>;
-  ChainMats<R> m;
-  m.G1i = L.mat[0].as<Cx>();
-  m.G2i = L.mat[1].as<Cx>();
-  m.Sigma1 = L.mat[4].as<Cx>();
-  m.Deltai = L.mat[3].as<Cx>();
-  m.Sigmai = L.mat[2].as<Cx>();
-  m.ld = G->ld;
-  return m;
-}
+LDUWork<R>& luw(Lane& L);
+template <> LDUWork<float>& luw<float>(Lane& L) { return L.lu32; }
+template <> LDUWork<double>& luw<double>(Lane& L) { return L.lu64; }
 
 void* tc_ctx(mnpbem_geom* G, Lane& L) { return G->tc_enabled ? (void*)&L.tc : nullptr; }
+
+// rows of the diagonal blocks of the LDU factors: 256 on the tensor-core path
+// (cluster block inverse), else 64 (single-CTA block inverse with pivoting)
+template <typename R>
+int lu_block(const mnpbem_geom* G, void* ctx) {
+  return (sizeof(R) == 4 && ctx && G->g.n >= 1024) ? 256 : 64;
+}
+
+// Lane matrices after initmat: mat[0] LDU(G1), mat[1] LDU(G2), mat[2] Sigma1,
+// mat[3] LDU(Sigma), mat[4] Deltai
+template <typename R>
+ChainMats<R> chain_mats(mnpbem_geom* G, Lane& L) {
+  using Cx = cplx<R>;
+  ChainMats<R> m;
+  m.G1 = L.mat[0].as<Cx>();
+  m.G2 = L.mat[1].as<Cx>();
+  m.Sigma1 = L.mat[2].as<Cx>();
+  m.Sigma = L.mat[3].as<Cx>();
+  m.Deltai = L.mat[4].as<Cx>();
+  m.ld = G->ld;
+  m.b = lu_block<R>(G, sizeof(R) == 4 ? tc_ctx(G, L) : nullptr);
+  m.ng1 = (int)G->g1_off.size();
+  for (int q = 0; q < m.ng1; ++q) {
+    m.g1_off[q] = G->g1_off[q];
+    m.g1_n[q] = G->g1_n[q];
+  }
+  return m;
+}
 
 // ---------------------------------------------------------------- S0
 mnpbem_status stage_assemble(mnpbem_geom* G, Lane& L, int precision) {
@@ -858,6 +970,10 @@ mnpbem_status stage_assemble(mnpbem_geom* G, Lane& L, int precision) {
 }
 
 // ---------------------------------------------------------------- S1
+// initmat.m:27-72 with block LDU factors in place of the inverses of G1, G2
+// and Sigma (real FLOP per wavelength: 8/3 n^3 per factorisation, 8 n^3 per
+// right-side solve, 8 n^3 for the Gauss-Jordan inverse of Delta; with G1
+// block-diagonal its factorisation and solve cost the sum over its blocks).
 template <typename R>
 mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   using Cx = cplx<R>;
@@ -870,27 +986,40 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   gjw<R>(L).nb = (ctx && n >= 1024) ? G->gj_nb : 64;
   gjw<R>(L).round_a = G->tf32_rna;
   gjw<R>(L).fused = G->gj_fused;
-  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
+  LDUWork<R>& lw = luw<R>(L);
+  lw.b = lu_block<R>(G, ctx);
+  lw.m = lw.b == 256 ? G->lu_steps : 1;
+  lw.round_a = G->tf32_rna;
+  int* lus = L.lu_status.as<int>();
+  MNP_CUDA(cudaMemsetAsync(lus, 0, 2 * sizeof(int), L.st));
   const FaceData fd = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();
-  // G1i, G2i
-  MNP_TRY(gj_invert<R>(M[0], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
-  MNP_TRY(gj_invert<R>(M[1], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
-  // Sigma1 = H1 G1i -> M4 ; Sigma2 = H2 G2i -> M2 (H1, H2 are read only here:
-  // round them to TF32 for the tensor cores)
-  if (sizeof(R) == 4 && ctx && gjw<R>(L).round_a) {
-    round_tf32(reinterpret_cast<float*>(M[2]), 2 * n * ld, L.st);
-    round_tf32(reinterpret_cast<float*>(M[3]), 2 * n * ld, L.st);
+  // G1 = LDU per diagonal block, Sigma1 = H1 G1^-1 (H1 shares G1's blocks:
+  // its off-diagonal blocks are zero and stay zero)
+  for (size_t q = 0; q < G->g1_off.size(); ++q) {
+    const int64_t o = G->g1_off[q], nq = G->g1_n[q];
+    MNP_TRY(ldu_factor<R>(M[0] + o * ld + o, nq, ld, lw, lus, gemm_w<R>, ctx, L.st));
+    MNP_TRY(ldu_rsolve<R>(M[2] + o * ld + o, nq, ld, M[0] + o * ld + o, ld, lw, gemm_w<R>, ctx, L.st));
   }
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[2], ld, M[0], ld, zero, M[4], ld, L.st, ctx));
-  MNP_TRY(gemm_w<R>(n, n, n, one, M[3], ld, M[1], ld, zero, M[2], ld, L.st, ctx));
-  // Delta -> M3, Sigma (partial) -> M2
-  launch_delta_sigma<R>(n, M[4], M[2], M[3], ld, fd, L.st);
+  // G2 = LDU, Sigma2 = H2 G2^-1
+  MNP_TRY(ldu_factor<R>(M[1], n, ld, lw, lus, gemm_w<R>, ctx, L.st));
+  MNP_TRY(ldu_rsolve<R>(M[3], n, ld, M[1], ld, lw, gemm_w<R>, ctx, L.st));
+  // Delta -> M4, Sigma (partial) -> M3
+  launch_delta_sigma<R>(n, M[2], M[3], M[4], ld, fd, L.st);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[3], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
-  launch_sigma_add<R>(n, M[2], M[3], ld, fd, lp, L.st);
+  MNP_TRY(gj_invert<R>(M[4], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
+  launch_sigma_add<R>(n, M[3], M[4], ld, fd, lp, L.st);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gj_invert<R>(M[2], n, ld, gjw<R>(L), gemm_w<R>, ctx, L.st, direct));
+  MNP_TRY(ldu_factor<R>(M[3], n, ld, lw, lus, gemm_w<R>, ctx, L.st));
+  if (direct) {
+    int hs[2] = {0, 0};
+    MNP_CUDA(cudaMemcpyAsync(hs, lus, sizeof(hs), cudaMemcpyDeviceToHost, L.st));
+    MNP_CUDA(cudaStreamSynchronize(L.st));
+    if (hs[0]) {
+      set_error("block LDU factorisation: zero or non-finite pivot in a diagonal block");
+      return MNPBEM_ERR_SINGULAR;
+    }
+  }
   if (direct && ctx) MNP_TRY(tc_check_error(L.tc, L.st));
   if (direct) MNP_TRY(thin_stream_check(L.st));
   return MNPBEM_OK;
@@ -1121,17 +1250,63 @@ mnpbem_status launch_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stage
   return MNPBEM_OK;
 }
 
-mnpbem_status check_pivots(const Lane& L) {
-  if (L.status_host[0] | L.status_host[1]) {
-    set_error("block Gauss-Jordan inversion: zero or non-finite pivot");
+// Status words of a lane's last initmat, copied into pinned host memory after
+// the stage is queued and read when the lane's work has completed:
+//   [0] [1]  Gauss-Jordan (Deltai): pivot flag, block condition proxy (float bits)
+//   [2] [3]  the same for its inner level (pivot blocks wider than 64)
+//   [4] [5]  block LDU factors (G1, G2, Sigma): pivot flag, condition proxy
+//   [6]      tensor-core GEMM error word (a bounded wait expired)
+// The condition proxy of a diagonal block is max|A_kk| * max|inv(A_kk)|; above
+// these limits its inverse has lost (nearly) every digit of the precision.
+constexpr float COND_LIMIT_32 = 1e6f, COND_LIMIT_64 = 1e13f;
+
+float status_cond(const Lane& L) {
+  float c = 0.f;
+  for (int q : {1, 3, 5}) {
+    float v;
+    memcpy(&v, &L.status_host[q], sizeof(float));
+    c = std::max(c, v);
+  }
+  return c;
+}
+
+mnpbem_status check_pivots(Lane& L, int precision) {
+  const int* h = L.status_host;
+  if (h[6]) {
+    set_error("tensor-core GEMM: a bounded pipeline wait expired (code %d)", h[6]);
+    L.tc.enabled = false;
+    return MNPBEM_ERR_TIMEOUT;
+  }
+  if (h[0] | h[2] | h[4]) {
+    set_error("block factorisation: zero or non-finite pivot in a diagonal block");
+    return MNPBEM_ERR_SINGULAR;
+  }
+  const float c = status_cond(L);
+  L.cond_max = std::max(L.cond_max, c);
+  if (c > (precision == MNPBEM_FP64 ? COND_LIMIT_64 : COND_LIMIT_32)) {
+    set_error("block factorisation: a diagonal block is numerically singular (condition proxy %.3g)", (double)c);
     return MNPBEM_ERR_SINGULAR;
   }
   return MNPBEM_OK;
 }
 
 mnpbem_status status_copy(Lane& L, int precision) {
-  if (precision == MNPBEM_FP64) return gj_status_copy<double>(L.gj64, L.status_host, L.st);
-  return gj_status_copy<float>(L.gj32, L.status_host, L.st);
+  int* h = L.status_host;
+  for (int q = 0; q < LANE_NSTATUS; ++q) h[q] = 0;
+  auto cp = [&](const DevBuf& b, int slot, int words) -> mnpbem_status {
+    if (b.ptr) MNP_CUDA(cudaMemcpyAsync(h + slot, b.ptr, words * sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    return MNPBEM_OK;
+  };
+  if (precision == MNPBEM_FP64) {
+    MNP_TRY(cp(L.gj64.status, 0, 2));
+    if (L.gj64.inner) MNP_TRY(cp(L.gj64.inner->status, 2, 2));
+  } else {
+    MNP_TRY(cp(L.gj32.status, 0, 2));
+    if (L.gj32.inner) MNP_TRY(cp(L.gj32.inner->status, 2, 2));
+  }
+  MNP_TRY(cp(L.lu_status, 4, 2));
+  if (L.tc.err.ptr && L.tc.err_cleared) MNP_TRY(cp(L.tc.err, 6, 1));
+  return MNPBEM_OK;
 }
 
 struct Refine {
@@ -1180,8 +1355,7 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
                         int32_t* iters, double* resid) {
   cudaStream_t st = L.st;
   for (int stage = 0; stage < 3; ++stage) MNP_TRY(launch_stage(G, L, c, stage, graphs));
-  if (graphs) MNP_TRY(status_copy(L, c.precision));
-  else L.status_host[0] = L.status_host[1] = 0;
+  MNP_TRY(status_copy(L, c.precision));
   int used = 0;
   double final_res = -1.0;
   if (c.precision == MNPBEM_MIXED) {
@@ -1193,7 +1367,7 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
       MNP_CUDA(cudaMemcpyAsync(hn, L.norms.ptr, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       MNP_CUDA(cudaStreamSynchronize(st));
       G->prof.flush();
-      MNP_TRY(check_pivots(L));
+      MNP_TRY(check_pivots(L, c.precision));
       step_done(L, kind, hn);
       used = L.iters;
       final_res = L.res;
@@ -1204,7 +1378,7 @@ mnpbem_status solve_one(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Refine
   if (c.spectra) MNP_TRY(launch_stage(G, L, c, 4, graphs));
   MNP_CUDA(cudaStreamSynchronize(st));
   G->prof.flush();
-  MNP_TRY(check_pivots(L));
+  MNP_TRY(check_pivots(L, c.precision));
   if (iters) *iters = used;
   if (resid) *resid = final_res;
   return MNPBEM_OK;
@@ -1310,7 +1484,7 @@ mnpbem_status lane_start(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep
 // the lane's queued work has completed: decide what comes next
 mnpbem_status lane_advance(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s) {
   if (G->prof.enabled) G->prof.flush();
-  MNP_TRY(check_pivots(L));
+  MNP_TRY(check_pivots(L, c.precision));
   if (L.state == Lane::ITER) {
     const double* hn = L.norms_host;
     step_done(L, L.last_kind, hn);
@@ -1580,7 +1754,7 @@ mnpbem_status job_finish(Job& j, bool failed) {
   G->prof.flush();
   for (int l = 0; l < j.nl; ++l) {
     Lane& L = *G->lanes[l];
-    MNP_TRY(check_pivots(L));
+    MNP_TRY(check_pivots(L, j.c.precision));
     if (j.c.precision == MNPBEM_MIXED && G->tc_enabled) MNP_TRY(tc_check_error(L.tc, L.st));
   }
   MNP_TRY(thin_stream_check(G->st));
@@ -1608,38 +1782,93 @@ mnpbem_status run_jobs(std::vector<Job>& jobs) {
   return MNPBEM_OK;
 }
 
-// A^{-T} applied through the transposed chain of mldivide.m (matrices M
-// already transposed in place: G1i^T, G2i^T, Sigmai^T, Deltai^T, Sigma1^T):
-// unknown-space input (gs1, gh1 may be null: zero), equation-space output
-// lam = [phi (n) | a (3n) | De (n) | alpha (3n)]; work holds 11 n values
+template <typename C>
+__global__ void k_set_identity(C* X, int64_t n, int64_t ld) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * n) return;
+  const int64_t r = i / n, c = i - r * n;
+  X[r * ld + c] = (r == c) ? from_d<C>(make_double2(1, 0)) : from_d<C>(make_double2(0, 0));
+}
+
+// inverse of the matrix whose LDU factors lane matrix q holds (0: G1 per
+// diagonal block, 1: G2, 3: Sigma), by solves with the identity on CUDA cores
+// (export for tests; not on the solve path)
 template <typename R>
-mnpbem_status chain_transpose(const AdjParams& p, cplx<R>* const* M, int64_t ld, const cplx<R>* gs1,
-                              const cplx<R>* gh1, const cplx<R>* gs2, const cplx<R>* gh2, cplx<R>* lam,
-                              cplx<R>* work, cudaStream_t st) {
+mnpbem_status ldu_inverse(mnpbem_geom* G, Lane& L, int q, cplx<R>* X, cplx<R>* tmp) {
   using Cx = cplx<R>;
-  const int64_t n = p.n;
+  const int64_t n = G->g.n, ld = G->ld;
+  k_set_identity<Cx><<<(unsigned)cdiv_up(n * n, (int64_t)256), 256, 0, L.st>>>(X, n, ld);
+  MNP_CHECK_LAUNCH();
+  const Cx* F = L.mat[q].as<Cx>();
+  const int b = lu_block<R>(G, sizeof(R) == 4 ? tc_ctx(G, L) : nullptr);
+  if (q == 0) {
+    for (size_t k = 0; k < G->g1_off.size(); ++k) {
+      const int64_t o = G->g1_off[k];
+      MNP_TRY(ldu_solve<R>(F + o * ld + o, G->g1_n[k], ld, b, X + o * ld, ld, n, tmp, gemm_w<R>, nullptr, L.st));
+    }
+    return MNPBEM_OK;
+  }
+  return ldu_solve<R>(F, n, ld, b, X, ld, n, tmp, gemm_w<R>, nullptr, L.st);
+}
+
+// y += x (count complex values)
+template <typename C>
+__global__ void k_cacc(C* __restrict__ y, const C* __restrict__ x, int64_t count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) y[i] = cadd(y[i], x[i]);
+}
+template <typename C>
+void cacc(C* y, const C* x, int64_t count, cudaStream_t st) {
+  if (count > 0) k_cacc<C><<<(unsigned)cdiv_up(count, (int64_t)256), 256, 0, st>>>(y, x, count);
+}
+
+// A^{-T} applied through the transposed chain of mldivide.m.  The chain
+// matrices m are transposed in place beforehand: the LDU factors of G1, G2
+// and Sigma then hold the factors of G1^T, G2^T and Sigma^T (their solves are
+// the same calls), Sigma1 and Deltai hold Sigma1^T and Deltai^T.
+// Unknown-space input (gs1, gh1 may be null: zero), equation-space output
+// lam = [phi (n) | a (3n) | De (n) | alpha (3n)]; work holds 11 n values.
+template <typename R>
+mnpbem_status chain_transpose(const AdjParams& p, const ChainMats<R>& m, const cplx<R>* gs1, const cplx<R>* gh1,
+                              const cplx<R>* gs2, const cplx<R>* gh2, cplx<R>* lam, cplx<R>* work,
+                              GemmFn<R> gemm, void* ctx, cudaStream_t st) {
+  using Cx = cplx<R>;
+  const int64_t n = p.n, ld = m.ld;
+  const size_t cs = sizeof(Cx);
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
   Cx *lphi = lam, *la = lam + n, *lDe = lam + 4 * n, *lal = lam + 5 * n;
   Cx *gS2 = work, *gH2p = work + n, *v3 = work + 4 * n, *tS1 = work + 7 * n, *ga0 = work + 8 * n;
-  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[1], ld, gs2, 1, zero, gS2, 1, st));        // G2i^T w_sig2
-  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[1], ld, gh2, 3, zero, gH2p, 3, st));       // G2i^T w_h2
+  auto g1solve = [&](Cx* x, int N) -> mnpbem_status {
+    for (int q = 0; q < m.ng1; ++q)
+      MNP_TRY(ldu_solve<R>(m.G1 + m.g1_off[q] * ld + m.g1_off[q], m.g1_n[q], ld, m.b, x + m.g1_off[q] * N, N, N,
+                           nullptr, gemm, ctx, st));
+    return MNPBEM_OK;
+  };
+  // G2^-T w_sig2, G2^-T w_h2
+  MNP_CUDA(cudaMemcpyAsync(gS2, gs2, cs * n, cudaMemcpyDeviceToDevice, st));
+  MNP_CUDA(cudaMemcpyAsync(gH2p, gh2, cs * 3 * n, cudaMemcpyDeviceToDevice, st));
+  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gS2, 1, 1, nullptr, gemm, ctx, st));
+  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gH2p, 3, 3, nullptr, gemm, ctx, st));
   if (gs1) {
-    MNP_TRY(gemm_simt<R>(n, 1, n, one, M[0], ld, gs1, 1, zero, lphi, 1, st));     // G1i^T w_sig1
-    MNP_TRY(gemm_simt<R>(n, 1, n, one, M[0], ld, gs1, 1, one, gS2, 1, st));
+    MNP_CUDA(cudaMemcpyAsync(lphi, gs1, cs * n, cudaMemcpyDeviceToDevice, st));
+    MNP_TRY(g1solve(lphi, 1));                                                     // G1^-T w_sig1
+    cacc(gS2, lphi, n, st);
   } else {
-    MNP_CUDA(cudaMemsetAsync(lphi, 0, sizeof(Cx) * n, st));
+    MNP_CUDA(cudaMemsetAsync(lphi, 0, cs * n, st));
   }
   if (gh1) {
-    MNP_TRY(gemm_simt<R>(n, 3, n, one, M[0], ld, gh1, 3, zero, ga0, 3, st));      // G1i^T w_h1
-    MNP_TRY(gemm_simt<R>(n, 3, n, one, M[0], ld, gh1, 3, one, gH2p, 3, st));
+    MNP_CUDA(cudaMemcpyAsync(ga0, gh1, cs * 3 * n, cudaMemcpyDeviceToDevice, st));
+    MNP_TRY(g1solve(ga0, 3));                                                      // G1^-T w_h1
+    cacc(gH2p, ga0, 3 * n, st);
   }
-  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[3], ld, gH2p, 3, zero, lal, 3, st));       // Deltai^T
+  MNP_TRY(gemm(n, 3, n, one, m.Deltai, ld, gH2p, 3, zero, lal, 3, st, ctx));        // Deltai^T
   adj_chainT<Cx>(p, 0, lal, nullptr, gS2, nullptr, nullptr, nullptr, st);
-  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[2], ld, gS2, 1, zero, lDe, 1, st));        // Sigmai^T
+  MNP_CUDA(cudaMemcpyAsync(lDe, gS2, cs * n, cudaMemcpyDeviceToDevice, st));
+  MNP_TRY(ldu_solve<R>(m.Sigma, n, ld, m.b, lDe, 1, 1, nullptr, gemm, ctx, st));     // Sigma^-T
   adj_chainT<Cx>(p, 1, lDe, nullptr, v3, nullptr, nullptr, nullptr, st);
-  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[3], ld, v3, 3, one, lal, 3, st));          // += Deltai^T v
-  MNP_TRY(gemm_simt<R>(n, 1, n, one, M[4], ld, lDe, 1, zero, tS1, 1, st));        // Sigma1^T
-  MNP_TRY(gemm_simt<R>(n, 3, n, one, M[4], ld, lal, 3, zero, la, 3, st));
+  MNP_TRY(gemm(n, 3, n, one, m.Deltai, ld, v3, 3, one, lal, 3, st, ctx));           // += Deltai^T v
+  MNP_TRY(gemm(n, 1, n, one, m.Sigma1, ld, lDe, 1, zero, tS1, 1, st, ctx));         // Sigma1^T
+  MNP_TRY(gemm(n, 3, n, one, m.Sigma1, ld, lal, 3, zero, la, 3, st, ctx));
   adj_chainT<Cx>(p, 2, tS1, lal, lphi, la, lDe, gh1 ? ga0 : nullptr, st);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
@@ -1793,23 +2022,17 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
   MNP_CHECK_LAUNCH();
   // ---- adjoint solve A^T lam = w through the transposed chain of mldivide.m
   if (precision == MNPBEM_FP64) {
-    double2* M[5];
-    for (int q = 0; q < 5; ++q) {
-      M[q] = L.mat[q].as<double2>();
-      adj_transpose(M[q], n, ld, st);   // G1i, G2i, Sigmai, Deltai, Sigma1 -> transposes
-    }
+    for (int q = 0; q < 5; ++q) adj_transpose(L.mat[q].as<double2>(), n, ld, st);   // factors and matrices -> transposes
     MNP_CHECK_LAUNCH();
-    MNP_TRY(chain_transpose<double>(p, M, ld, nullptr, nullptr, gs2, gh2, lam, work, st));
+    MNP_TRY(chain_transpose<double>(p, chain_mats<double>(G, L), nullptr, nullptr, gs2, gh2, lam, work, gemm_w<double>,
+                                    nullptr, st));
   } else {
     // complex64 transposed chain as the preconditioner of a refinement on the
     // FP64-class operator: r = w - A^T lam with A^T lam = [G1^T U_G1 + H1^T U_H1 ;
     // G2^T U_G2 + H2^T U_H2] (the weights U of lam), products of the hi / lo
     // planes in double-single arithmetic
-    float2* M[5];
-    for (int q = 0; q < 5; ++q) {
-      M[q] = L.mat[q].as<float2>();
-      adj_transpose(M[q], n, ld, st);
-    }
+    for (int q = 0; q < 5; ++q) adj_transpose(L.mat[q].as<float2>(), n, ld, st);
+    const ChainMats<float> mT = chain_mats<float>(G, L);
     const int chunks = 32;
     MNP_TRY(G->adj2.ensure(cs * (8 * (size_t)n + 8 * (size_t)n + chunks * 4 * (size_t)n) +
                            sizeof(float2) * (8 * (size_t)n + 8 * (size_t)n + 11 * (size_t)n + 8 * (size_t)n) +
@@ -1832,7 +2055,8 @@ mnpbem_status mnpbem_cross_section_gradient(mnpbem_geom* G, const mnpbem_planewa
     for (int it = 0; it < 20; ++it) {
       launch_cvt_d2f(r64, r32, 8 * n, st);
       MNP_CHECK_LAUNCH();
-      MNP_TRY(chain_transpose<float>(p, M, ld, r32, r32 + n, r32 + 4 * n, r32 + 5 * n, dl32, w32, st));
+      MNP_TRY(chain_transpose<float>(p, mT, r32, r32 + n, r32 + 4 * n, r32 + 5 * n, dl32, w32, gemm_w<float>,
+                                     tc_ctx(G, L), st));
       MNP_CUDA(cudaMemsetAsync(nrm, 0, sizeof(double) * 4, st));
       launch_axpy_norm(lam, dl32, 8 * n, nrm, st);
       MNP_CHECK_LAUNCH();
@@ -1905,14 +2129,28 @@ mnpbem_status mnpbem_bem_matrices(mnpbem_geom* G, double enei, const double* eps
   MNP_TRY(stage_assemble(G, L, precision));
   if (precision == MNPBEM_FP64) MNP_TRY(stage_initmat<double>(G, L, true));
   else MNP_TRY(stage_initmat<float>(G, L, true));
-  double* outs[5] = {G1i, G2i, Sigmai, Deltai, Sigma1};  // order of mat[0..4]
-  DevBuf conv;
+  MNP_TRY(status_copy(L, precision));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
+  MNP_TRY(check_pivots(L, precision));
+  // Sigma1 and Deltai as stored (mat[2], mat[4]); G1i, G2i and Sigmai from the
+  // LDU factors (mat[0], mat[1], mat[3]) by solves with the identity
+  double* outs[5] = {G1i, G2i, Sigma1, Sigmai, Deltai};  // order of mat[0..4]
+  DevBuf conv, inv, tmp;
   if (precision == MNPBEM_MIXED) MNP_TRY(conv.ensure(sizeof(double2) * n * ld));
+  const size_t es = precision == MNPBEM_FP64 ? sizeof(double2) : sizeof(float2);
   for (int q = 0; q < 5; ++q) {
     if (!outs[q]) continue;
-    const double2* src = L.mat[q].as<double2>();
+    const void* m = L.mat[q].ptr;
+    if (q == 0 || q == 1 || q == 3) {
+      MNP_TRY(inv.ensure(es * n * ld));
+      MNP_TRY(tmp.ensure(es * 256 * n));
+      if (precision == MNPBEM_FP64) MNP_TRY(ldu_inverse<double>(G, L, q, inv.as<double2>(), tmp.as<double2>()));
+      else MNP_TRY(ldu_inverse<float>(G, L, q, inv.as<float2>(), tmp.as<float2>()));
+      m = inv.ptr;
+    }
+    const double2* src = static_cast<const double2*>(m);
     if (precision == MNPBEM_MIXED) {
-      launch_cvt_f2d(L.mat[q].as<float2>(), conv.as<double2>(), n * ld, L.st);
+      launch_cvt_f2d(static_cast<const float2*>(m), conv.as<double2>(), n * ld, L.st);
       MNP_CHECK_LAUNCH();
       src = conv.as<double2>();
     }

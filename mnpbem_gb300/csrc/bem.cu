@@ -1,6 +1,7 @@
 // Excitation, the bemret solution chain, the FP64 residual of the full BEM
 // operator, and the far-field cross sections.
 #include "bem.cuh"
+#include "dense.cuh"
 #include "profile.cuh"
 
 namespace mnpbem {
@@ -226,8 +227,7 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, cons
   Cx* s2 = u + n * P;
   Cx* v3 = s2 + n * P;
   Cx* h2 = v3 + n * 3 * P;
-  Cx* Y4 = h2 + n * 3 * P;
-  Cx* Z4 = Y4 + n * 4 * P;   // ends at 32 n P
+  (void)s2;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0);
   unsigned nb = (unsigned)cdiv_up(n, 128);
   if (Profiler* pr = current_profiler()) pr->acc[PH_ELEMWISE].launches += 5;
@@ -239,14 +239,19 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, cons
   MNP_TRY(gemm(n, 3 * P, n, one, m.Deltai, m.ld, al, 3 * P, zero, t3, 3 * P, st, ctx));
   k_chain_u<R><<<nb, 128, 0, st>>>(f, P, lp, Dp, t3, u);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gemm(n, P, n, one, m.Sigmai, m.ld, u, P, zero, s2, P, st, ctx));
+  // sig2 = Sigma \ u (in place)
+  MNP_TRY(ldu_solve<R>(m.Sigma, n, m.ld, m.b, u, P, P, nullptr, gemm, ctx, st));
+  s2 = u;
   k_chain_v<R><<<nb, 128, 0, st>>>(f, P, lp, s2, al, v3);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, 3 * P, n, one, m.Deltai, m.ld, v3, 3 * P, zero, h2, 3 * P, st, ctx));
-  k_chain_y<R><<<nb, 128, 0, st>>>(n, P, s2, h2, phi, a, Y4, Z4);
+  // x1 = G1 \ [sig2 + phi | h2 + a], x2 = G2 \ [sig2 | h2]
+  k_chain_y<R><<<nb, 128, 0, st>>>(n, P, s2, h2, phi, a, x1, x2);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gemm(n, 4 * P, n, one, m.G1i, m.ld, Y4, 4 * P, zero, x1, 4 * P, st, ctx));
-  MNP_TRY(gemm(n, 4 * P, n, one, m.G2i, m.ld, Z4, 4 * P, zero, x2, 4 * P, st, ctx));
+  for (int q = 0; q < m.ng1; ++q)
+    MNP_TRY(ldu_solve<R>(m.G1 + m.g1_off[q] * m.ld + m.g1_off[q], m.g1_n[q], m.ld, m.b, x1 + m.g1_off[q] * 4 * P,
+                         4 * P, 4 * P, nullptr, gemm, ctx, st));
+  MNP_TRY(ldu_solve<R>(m.G2, n, m.ld, m.b, x2, 4 * P, 4 * P, nullptr, gemm, ctx, st));
   return MNPBEM_OK;
 }
 template mnpbem_status apply_mldivide<float>(const FaceData&, int, const LamParams*, const ChainMats<float>&,

@@ -44,9 +44,19 @@ void launch_face_eps(int64_t n, const int* med_in, const int* med_out, const Lam
                      const double* nvec, double2* eps1, double2* eps2, float2* eps1f, float2* eps2f,
                      float2* Lf, float* nvecf, cudaStream_t st);
 
+// The matrices of the mldivide chain as initmat leaves them: block LDU
+// factors (dense.cuh) of G1, G2 and Sigma, explicit Sigma1 and Deltai.  G1 is
+// factored per diagonal block (g1_off / g1_n: the particle groups whose
+// media do not couple, e.g. the two spheres of a dimer; one block when G1 is
+// full), its off-diagonal blocks being zero.
+constexpr int CHAIN_MAXBLK = 16;
 template <typename R> struct ChainMats {
-  const cplx<R>* G1i; const cplx<R>* G2i; const cplx<R>* Sigma1; const cplx<R>* Deltai;
-  const cplx<R>* Sigmai; int64_t ld;
+  const cplx<R>* G1; const cplx<R>* G2; const cplx<R>* Sigma1; const cplx<R>* Deltai;
+  const cplx<R>* Sigma; int64_t ld;
+  int b = 64;                      // rows of the diagonal blocks of the LDU factors
+  int ng1 = 1;
+  int64_t g1_off[CHAIN_MAXBLK] = {0};
+  int64_t g1_n[CHAIN_MAXBLK] = {0};
 };
 
 template <typename R>

@@ -714,39 +714,72 @@ template mnpbem_status gemm_simt<double>(int64_t, int64_t, int64_t, double2, con
                                          cudaStream_t);
 
 // --------------------------------------------------- block inversion
-// In-place Gauss-Jordan of one w x w block (w <= 64).  256 threads as a 16 x 16
-// grid; thread (ty, tx) keeps the 16 entries (ty + 16 i, tx + 16 j) in
-// registers.  Each pivot step publishes the pivot row and column through a
-// double-buffered shared array, so one __syncthreads per step suffices.
+// Largest per-block condition proxy max|A_kk| * max|inv(A_kk)|, kept as the
+// bits of a non-negative float in status[1] (integer order = float order).
+__device__ __forceinline__ void record_cond(int* status, double amax, double xmax) {
+  double c = amax * xmax;
+  if (!(c == c) || c > 3.0e38) c = 3.0e38;
+  atomicMax(status + 1, __float_as_int((float)c));
+}
+
+// In-place Gauss-Jordan of one w x w block (w <= 64) with partial pivoting
+// inside the block.  256 threads as a 16 x 16 grid; thread (ty, tx) keeps the
+// 16 entries (ty + 16 i, tx + 16 j) in registers.  Pivoting is implicit: step p
+// takes as pivot row r_p the row, among those not yet used, with the largest
+// |a_rp| in column p, and eliminates with (r_p, p) in place of (p, p).  The
+// matrix M this leaves satisfies inv(A)[q][r_k] = M[r_q][k], so the block is
+// written out through the permutation.  Two __syncthreads per step: after the
+// pivot column is published, and after the pivot row is.
 template <typename R>
 __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A, int64_t lda, int w,
                                                    cplx<R>* __restrict__ X, int64_t ldx, int* status) {
   using Cx = cplx<R>;
   __shared__ Cx prow[2][64], pcol[2][64];
+  __shared__ int prow_of[64], pos_of[64];
+  __shared__ unsigned char used[64];
+  __shared__ double red[8];
   const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
   Cx a[4][4];
+  double amax = 0.0;
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int r = ty + 16 * i, c = tx + 16 * j;
       a[i][j] = (r < w && c < w) ? A[r * lda + c] : mk<R>(r == c ? 1 : 0, 0);
+      if (r < w && c < w) amax = fmax(amax, sqrt(cabs2(a[i][j])));
     }
-  // publish pivot row / column 0
-  const auto publish = [&](int p, int buf) {
+  if (t < 64) used[t] = 0;
+  for (int p = 0; p < w; ++p) {
+    const int buf = p & 1;
+    // 1. publish column p
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int r = ty + 16 * i, c = tx + 16 * j;
-        if (r == p) prow[buf][c] = a[i][j];
-        if (c == p) pcol[buf][r] = a[i][j];
-      }
-  };
-  publish(0, 0);
-  __syncthreads();
-  for (int p = 0; p < w; ++p) {
-    const int buf = p & 1;
+      for (int j = 0; j < 4; ++j)
+        if (tx + 16 * j == p) pcol[buf][ty + 16 * i] = a[i][j];
+    __syncthreads();
+    // 2. pivot row: largest modulus among the unused rows (first one on ties)
+    int rp = -1;
+    R best = -1;
+    for (int r = 0; r < w; ++r) {
+      if (used[r]) continue;
+      const Cx v = pcol[buf][r];
+      const R m2 = v.x * v.x + v.y * v.y;
+      if (rp < 0 || m2 > best) { best = m2; rp = r; }
+    }
+    // 3. publish the pivot row
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ty + 16 * i == rp) prow[buf][tx + 16 * j] = a[i][j];
+    __syncthreads();
+    if (t == 0) {
+      used[rp] = 1;
+      prow_of[p] = rp;
+      pos_of[rp] = p;
+    }
     const Cx piv = prow[buf][p];
     const R n2 = piv.x * piv.x + piv.y * piv.y;
     if (t == 0 && !(n2 > (R)1e-30 && n2 < (R)1e30)) atomicOr(status, 1);
@@ -754,8 +787,8 @@ __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A
     const Cx inv = mk<R>(piv.x * rn2, -piv.y * rn2);
     // One update a - pc_r pr_c serves every entry when the pivot column of pr
     // holds 1 + 1/a_pp and the pivot row of pc holds a_pp - 1:
-    //   row p:    a_pc - (a_pp - 1) a_pc / a_pp = a_pc / a_pp
-    //   column p: a_rp - a_rp (1 + 1/a_pp)      = -a_rp / a_pp
+    //   pivot row:    a_rc - (a_pp - 1) a_rc / a_pp = a_rc / a_pp
+    //   column p:     a_ip - a_ip (1 + 1/a_pp)      = -a_ip / a_pp
     // (the pivot itself is set to 1/a_pp directly).
     Cx pr[4], pc[4];
 #pragma unroll
@@ -766,25 +799,50 @@ __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = ty + 16 * i;
-      pc[i] = (r == p) ? mk<R>(piv.x - 1, piv.y) : pcol[buf][r];
+      pc[i] = (r == rp) ? mk<R>(piv.x - 1, piv.y) : pcol[buf][r];
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const Cx v = csub(a[i][j], cmul(pc[i], pr[j]));
-        a[i][j] = (ty + 16 * i == p && tx + 16 * j == p) ? inv : v;
+        a[i][j] = (ty + 16 * i == rp && tx + 16 * j == p) ? inv : v;
       }
-    if (p + 1 < w) publish(p + 1, buf ^ 1);
-    __syncthreads();
   }
+  __syncthreads();
+  double xmax = 0.0;
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int r = ty + 16 * i, c = tx + 16 * j;
-      if (r < w && c < w) X[r * ldx + c] = a[i][j];
+      if (r < w && c < w) {
+        X[(int64_t)pos_of[r] * ldx + prow_of[c]] = a[i][j];
+        xmax = fmax(xmax, sqrt(cabs2(a[i][j])));
+      }
     }
+  // block maxima of |A| and |X| for the condition proxy
+  for (int o = 16; o; o >>= 1) {
+    amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+  }
+  if ((t & 31) == 0) red[t >> 5] = amax;
+  __syncthreads();
+  if (t == 0) {
+    double am = 0.0;
+    for (int k = 0; k < 8; ++k) am = fmax(am, red[k]);
+    red[0] = am;
+  }
+  __syncthreads();
+  amax = red[0];
+  __syncthreads();
+  if ((t & 31) == 0) red[t >> 5] = xmax;
+  __syncthreads();
+  if (t == 0) {
+    double xm = 0.0;
+    for (int k = 0; k < 8; ++k) xm = fmax(xm, red[k]);
+    record_cond(status, amax, xm);
+  }
 }
 
 // ------------------------------------- 256-wide pivot block on a CTA cluster
@@ -823,12 +881,28 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
   const int rank = (int)cluster.block_rank();
   const int t = threadIdx.x, lr = t / PB_TPR, ph = t % PB_TPR;
   const int grow = rank * PB_RPC + lr;
+  __shared__ float cond_red[PB_THREADS / 32], cond_loc[2];
   float2 a[PB_CPT];
+  float amax = 0.f;
 #pragma unroll
   for (int j = 0; j < PB_CPT; ++j) {
     const int c = ph + PB_TPR * j;
     a[j] = (grow < w && c < w) ? A[(int64_t)grow * lda + c] : make_float2(grow == c ? 1.f : 0.f, 0.f);
+    if (grow < w && c < w) amax = fmaxf(amax, sqrtf(a[j].x * a[j].x + a[j].y * a[j].y));
   }
+  // CTA maximum of a per-thread value into cond_loc[slot]
+  const auto cta_max = [&](float v, int slot) {
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((t & 31) == 0) cond_red[t >> 5] = v;
+    __syncthreads();
+    if (t == 0) {
+      float mx = 0.f;
+      for (int k = 0; k < PB_THREADS / 32; ++k) mx = fmaxf(mx, cond_red[k]);
+      cond_loc[slot] = mx;
+    }
+    __syncthreads();
+  };
+  cta_max(amax, 0);
   const int npan = (w + PB_PAN - 1) / PB_PAN;
   for (int pp = 0; pp < npan; ++pp) {
     const int p0 = pp * PB_PAN, owner = p0 / PB_RPC, lp0 = p0 % PB_RPC, buf = pp & 1;
@@ -917,8 +991,26 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
       }
     }
   }
-  // no CTA may exit while another can still write into its shared memory
+  float xmax = 0.f;
+  if (grow < w) {
+#pragma unroll
+    for (int j = 0; j < PB_CPT; ++j) {
+      const int c = ph + PB_TPR * j;
+      if (c < w) xmax = fmaxf(xmax, sqrtf(a[j].x * a[j].x + a[j].y * a[j].y));
+    }
+  }
+  cta_max(xmax, 1);
+  // no CTA may exit while another can still write into (or read) its shared memory
   cluster.sync();
+  if (rank == 0 && t == 0) {
+    float am = 0.f, xm = 0.f;
+    for (int r = 0; r < PB_CL; ++r) {
+      const float* cl = cluster.map_shared_rank(cond_loc, r);
+      am = fmaxf(am, cl[0]);
+      xm = fmaxf(xm, cl[1]);
+    }
+    record_cond(status, am, xm);
+  }
   if (grow < w) {
 #pragma unroll
     for (int j = 0; j < PB_CPT; ++j) {
@@ -926,6 +1018,7 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
       if (c < w) X[(int64_t)grow * ldx + c] = a[j];
     }
   }
+  cluster.sync();
 }
 
 static mnpbem_status launch_block_inv_cluster(const float2* A, int64_t lda, int w, float2* X, int64_t ldx,
@@ -1004,8 +1097,8 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
   MNP_TRY(w.rrow.ensure(cs * n * nb));
   MNP_TRY(w.ncol.ensure(cs * n * nb));
   MNP_TRY(w.xblk.ensure(cs * nb * nb));
-  MNP_TRY(w.status.ensure(sizeof(int)));
-  if (!w.nested) MNP_CUDA(cudaMemsetAsync(w.status.ptr, 0, sizeof(int), st));
+  MNP_TRY(w.status.ensure(2 * sizeof(int)));
+  if (!w.nested) MNP_CUDA(cudaMemsetAsync(w.status.ptr, 0, 2 * sizeof(int), st));
   if (!w.nested && nb > 64 && (sizeof(R) == 8 || nb > PB_W)) {
     // pivot blocks wider than 64 are inverted by an inner Gauss-Jordan whose
     // pivot status this (outer) level clears now and reads at the end
@@ -1014,8 +1107,8 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
     // own pivot blocks go to the cluster kernel; otherwise 64-wide steps
     w.inner->nb = (sizeof(R) == 4 && nb > PB_W) ? PB_W : 64;
     w.inner->nested = true;
-    MNP_TRY(w.inner->status.ensure(sizeof(int)));
-    MNP_CUDA(cudaMemsetAsync(w.inner->status.ptr, 0, sizeof(int), st));
+    MNP_TRY(w.inner->status.ensure(2 * sizeof(int)));
+    MNP_CUDA(cudaMemsetAsync(w.inner->status.ptr, 0, 2 * sizeof(int), st));
   }
   Cx* Ccol = w.ccol.template as<Cx>();   // [n][nb]
   Cx* Rrow = w.rrow.template as<Cx>();   // [nb][n]
@@ -1119,5 +1212,254 @@ template mnpbem_status gj_invert<float>(float2*, int64_t, int64_t, GJWork<float>
                                         void*, cudaStream_t, bool);
 template mnpbem_status gj_invert<double>(double2*, int64_t, int64_t, GJWork<double>&,
                                          GemmFn<double>, void*, cudaStream_t, bool);
+
+// ------------------------------------------------------ block LDU factors
+// dst[rows][cols] (row stride ldd) <- src[rows][cols] (row stride lds),
+// rounded to TF32 (nearest) when rna: the A operand of a tensor-core product
+template <typename R>
+__global__ void k_copy_panel(const cplx<R>* __restrict__ src, int64_t lds, int64_t rows, int cols,
+                             cplx<R>* __restrict__ dst, int64_t ldd, int rna) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= rows * cols) return;
+  const int64_t i = idx / cols;
+  const int c = (int)(idx - i * cols);
+  cplx<R> v = src[i * lds + c];
+  if constexpr (sizeof(R) == 4) {
+    if (rna) {
+      uint32_t x, y;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(x) : "f"(v.x));
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(v.y));
+      v = mk<R>(__uint_as_float(x), __uint_as_float(y));
+    }
+  }
+  dst[i * ldd + c] = v;
+}
+
+template <typename R>
+static void copy_panel(const cplx<R>* src, int64_t lds, int64_t rows, int cols, cplx<R>* dst, int64_t ldd, bool rna,
+                       cudaStream_t st) {
+  if (rows <= 0 || cols <= 0) return;
+  ProfScope ps(PH_ELEMWISE, st, 0.0, 2.0 * sizeof(cplx<R>) * rows * cols, 1);
+  const int64_t cnt = rows * cols;
+  k_copy_panel<R><<<(unsigned)cdiv_up(cnt, (int64_t)256), 256, 0, st>>>(src, lds, rows, cols, dst, ldd, rna ? 1 : 0);
+}
+
+// X_k <- inv(A_kk): 64-wide blocks with partial pivoting on one CTA, 256-wide
+// complex64 blocks on a CTA cluster
+template <typename R>
+static mnpbem_status block_inverse(const cplx<R>* Akk, int64_t lda, int bw, cplx<R>* X, int* status,
+                                   cudaStream_t st) {
+  if (bw <= 64) {
+    ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
+    k_block_inv<R><<<1, 256, 0, st>>>(Akk, lda, bw, X, bw, status);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  if (sizeof(R) == 4 && bw <= PB_W)
+    return launch_block_inv_cluster(reinterpret_cast<const float2*>(Akk), lda, bw, reinterpret_cast<float2*>(X), bw,
+                                    status, st);
+  set_error("block LDU: diagonal blocks of %d rows are not supported in this precision", bw);
+  return MNPBEM_ERR_UNSUPPORTED;
+}
+
+template <typename R>
+mnpbem_status ldu_factor(cplx<R>* A, int64_t n, int64_t lda, LDUWork<R>& w, int* status, GemmFn<R> gemm,
+                         void* ctx, cudaStream_t st) {
+  using Cx = cplx<R>;
+  const int b = w.b, B = w.b * std::max(1, w.m);
+  if (n <= 0) return MNPBEM_OK;
+  const size_t cs = sizeof(Cx);
+  MNP_TRY(w.ccol.ensure(cs * n * B));
+  MNP_TRY(w.xblk.ensure(cs * b * b));
+  const bool tc = sizeof(R) == 4 && ctx != nullptr;
+  MNP_TRY(w.rrow.ensure(cs * n * b));
+  const bool rna = tc && w.round_a;
+  Cx* Cc = w.ccol.template as<Cx>();     // [n][B]: row i holds row k0 + i of the outer step's column panel
+  Cx* X = w.xblk.template as<Cx>();
+  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
+  for (int64_t k0 = 0; k0 < n; k0 += B) {
+    const int64_t Bw = std::min<int64_t>(B, n - k0), e = k0 + Bw;
+    for (int64_t s = 0; s < Bw; s += b) {
+      const int64_t ks = k0 + s;
+      const int bs = (int)std::min<int64_t>(b, e - ks);
+      const int64_t kb = ks + bs, below = n - kb;
+      MNP_TRY(block_inverse<R>(A + ks * lda + ks, lda, bs, X, status, st));
+      if (below > 0) {
+        Cx* Cs = Cc + (kb - k0) * B + s;
+        // unscaled column panel (the A operand of every update of this step)
+        copy_panel<R>(A + kb * lda + ks, lda, below, bs, Cs, B, rna, st);
+        MNP_CHECK_LAUNCH();
+        // L panel: A[kb:, ks:kb] = C X
+        MNP_TRY(gemm(below, bs, bs, one, Cs, B, X, bs, zero, A + kb * lda + ks, lda, st, ctx));
+        // U row: A[ks:kb, kb:] = X A[ks:kb, kb:] (the tensor-core product copies its
+        // B operand before it runs, so it may write in place; the CUDA-core
+        // products may not)
+        bool inplace = false;
+        if constexpr (sizeof(R) == 4) {
+          if (tc)
+            inplace = tc_gemm_eligible(*reinterpret_cast<TcGemmCtx*>(ctx), bs, below, bs, X, bs, A + ks * lda + kb,
+                                       lda, make_float2(0.f, 0.f));
+        }
+        if (inplace) {
+          MNP_TRY(gemm(bs, below, bs, one, X, bs, A + ks * lda + kb, lda, zero, A + ks * lda + kb, lda, st, ctx));
+        } else {
+          Cx* Rr = w.rrow.template as<Cx>();
+          MNP_CUDA(cudaMemcpy2DAsync(Rr, cs * below, A + ks * lda + kb, cs * lda, cs * below, bs,
+                                     cudaMemcpyDeviceToDevice, st));
+          MNP_TRY(gemm(bs, below, bs, one, X, bs, Rr, below, zero, A + ks * lda + kb, lda, st, ctx));
+        }
+        if (kb < e) {
+          // the later column panels of this outer step (all rows below) ...
+          MNP_TRY(gemm(below, e - kb, bs, mone, Cs, B, A + ks * lda + kb, lda, one, A + kb * lda + kb, lda, st, ctx));
+          // ... and the later rows of this outer step over the trailing columns
+          if (e < n)
+            MNP_TRY(gemm(e - kb, n - e, bs, mone, Cs, B, A + ks * lda + e, lda, one, A + kb * lda + e, lda, st, ctx));
+        }
+      }
+      MNP_CUDA(cudaMemcpy2DAsync(A + ks * lda + ks, cs * lda, X, cs * bs, cs * bs, bs, cudaMemcpyDeviceToDevice, st));
+    }
+    // trailing update of rank Bw
+    if (e < n) MNP_TRY(gemm(n - e, n - e, Bw, mone, Cc + (e - k0) * B, B, A + k0 * lda + e, lda, one, A + e * lda + e,
+                            lda, st, ctx));
+  }
+  return MNPBEM_OK;
+}
+
+template <typename R>
+mnpbem_status ldu_rsolve(cplx<R>* H, int64_t n, int64_t ldh, const cplx<R>* F, int64_t ldf, LDUWork<R>& w,
+                         GemmFn<R> gemm, void* ctx, cudaStream_t st) {
+  using Cx = cplx<R>;
+  const int b = w.b, B = w.b * std::max(1, w.m);
+  if (n <= 0) return MNPBEM_OK;
+  MNP_TRY(w.ccol.ensure(sizeof(Cx) * n * B));
+  const bool rna = sizeof(R) == 4 && ctx != nullptr && w.round_a;
+  Cx* Cc = w.ccol.template as<Cx>();     // [n][B]: columns of the outer step
+  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
+  // 1. W U = H (U unit upper), columns in increasing order; then V = W D^-1
+  //    (D^-1 = the stored X_k) on each outer step's columns once they are final
+  for (int64_t k0 = 0; k0 < n; k0 += B) {
+    const int64_t Bw = std::min<int64_t>(B, n - k0), e = k0 + Bw;
+    for (int64_t s = 0; s < Bw; s += b) {
+      const int64_t ks = k0 + s;
+      const int bs = (int)std::min<int64_t>(b, e - ks);
+      copy_panel<R>(H + ks, ldh, n, bs, Cc + s, B, rna, st);
+      MNP_CHECK_LAUNCH();
+      if (ks + bs < e)
+        MNP_TRY(gemm(n, e - ks - bs, bs, mone, Cc + s, B, F + ks * ldf + ks + bs, ldf, one, H + ks + bs, ldh, st, ctx));
+    }
+    if (e < n) MNP_TRY(gemm(n, n - e, Bw, mone, Cc, B, F + k0 * ldf + e, ldf, one, H + e, ldh, st, ctx));
+    for (int64_t s = 0; s < Bw; s += b) {
+      const int64_t ks = k0 + s;
+      const int bs = (int)std::min<int64_t>(b, e - ks);
+      MNP_TRY(gemm(n, bs, bs, one, Cc + s, B, F + ks * ldf + ks, ldf, zero, H + ks, ldh, st, ctx));
+    }
+  }
+  // 2. S L = V (L unit lower), columns in decreasing order
+  const int64_t nout = cdiv_up(n, (int64_t)B);
+  for (int64_t q = nout - 1; q >= 0; --q) {
+    const int64_t k0 = q * B, Bw = std::min<int64_t>(B, n - k0), e = k0 + Bw;
+    const int64_t nin = cdiv_up(Bw, (int64_t)b);
+    for (int64_t t = nin - 1; t >= 0; --t) {
+      const int64_t ks = k0 + t * b;
+      const int bs = (int)std::min<int64_t>(b, e - ks);
+      copy_panel<R>(H + ks, ldh, n, bs, Cc + t * b, B, rna, st);
+      MNP_CHECK_LAUNCH();
+      if (ks > k0) MNP_TRY(gemm(n, ks - k0, bs, mone, Cc + t * b, B, F + ks * ldf + k0, ldf, one, H + k0, ldh, st, ctx));
+    }
+    if (k0 > 0) MNP_TRY(gemm(n, k0, Bw, mone, Cc, B, F + k0 * ldf, ldf, one, H, ldh, st, ctx));
+  }
+  return MNPBEM_OK;
+}
+
+// X[blk] <- X_k X[blk] for every diagonal block k (one CTA per block; a warp
+// per row, lanes over the block's columns, N <= 16 right-hand sides)
+template <typename R, int NB>
+__global__ void __launch_bounds__(256) k_ldu_diag(const cplx<R>* __restrict__ F, int64_t ldf, int64_t n, int b,
+                                                  cplx<R>* __restrict__ X, int64_t ldx, int N) {
+  using Cx = cplx<R>;
+  extern __shared__ unsigned char ldu_smem[];
+  Cx* xs = reinterpret_cast<Cx*>(ldu_smem);   // [b][NB], columns N .. NB - 1 zero
+  const int64_t k0 = (int64_t)blockIdx.x * b;
+  const int bs = (int)min((int64_t)b, n - k0);
+  for (int e = threadIdx.x; e < bs * NB; e += blockDim.x) {
+    const int r = e / NB, c = e % NB;
+    xs[e] = c < N ? X[(k0 + r) * ldx + c] : mk<R>(0, 0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < bs; r += 8) {
+    const Cx* frow = F + (k0 + r) * ldf + k0;
+    Cx acc[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) acc[c] = mk<R>(0, 0);
+    for (int l = lane; l < bs; l += 32) {
+      const Cx f = frow[l];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) cfma(acc[c], f, xs[l * NB + c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      Cx v = acc[c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0 && c < N) X[(k0 + r) * ldx + c] = v;
+    }
+  }
+}
+
+template <typename R>
+mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int64_t N,
+                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st) {
+  using Cx = cplx<R>;
+  if (n <= 0 || N <= 0) return MNPBEM_OK;
+  const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
+  const int64_t nblk = cdiv_up(n, (int64_t)b);
+  // forward: L unit lower
+  for (int64_t k = 0; k + 1 < nblk; ++k) {
+    const int64_t k0 = k * b, kb = k0 + b;
+    MNP_TRY(gemm(n - kb, N, b, mone, F + kb * ldf + k0, ldf, X + k0 * ldx, ldx, one, X + kb * ldx, ldx, st, ctx));
+  }
+  // block diagonal
+  if (N <= 16) {
+    const size_t smem = sizeof(Cx) * b * (N <= 4 ? 4 : N <= 8 ? 8 : 16);
+    ProfScope ps(PH_GEMM_SMALL, st, 8.0 * n * b * N, (double)sizeof(Cx) * ((double)n * b + 2.0 * n * N));
+    const int Ni = (int)N;
+    if (N <= 4) k_ldu_diag<R, 4><<<(unsigned)nblk, 256, smem, st>>>(F, ldf, n, b, X, ldx, Ni);
+    else if (N <= 8) k_ldu_diag<R, 8><<<(unsigned)nblk, 256, smem, st>>>(F, ldf, n, b, X, ldx, Ni);
+    else k_ldu_diag<R, 16><<<(unsigned)nblk, 256, smem, st>>>(F, ldf, n, b, X, ldx, Ni);
+    MNP_CHECK_LAUNCH();
+  } else {
+    if (!tmp) { set_error("ldu_solve: workspace required for more than 16 right-hand sides"); return MNPBEM_ERR_INVALID_ARG; }
+    for (int64_t k = 0; k < nblk; ++k) {
+      const int64_t k0 = k * b;
+      const int bs = (int)std::min<int64_t>(b, n - k0);
+      MNP_CUDA(cudaMemcpy2DAsync(tmp, sizeof(Cx) * N, X + k0 * ldx, sizeof(Cx) * ldx, sizeof(Cx) * N, bs,
+                                 cudaMemcpyDeviceToDevice, st));
+      MNP_TRY(gemm(bs, N, bs, one, F + k0 * ldf + k0, ldf, tmp, N, zero, X + k0 * ldx, ldx, st, ctx));
+    }
+  }
+  // backward: U unit upper
+  for (int64_t k = nblk - 1; k >= 1; --k) {
+    const int64_t k0 = k * b;
+    const int bs = (int)std::min<int64_t>(b, n - k0);
+    MNP_TRY(gemm(k0, N, bs, mone, F + k0, ldf, X + k0 * ldx, ldx, one, X, ldx, st, ctx));
+  }
+  return MNPBEM_OK;
+}
+
+template mnpbem_status ldu_factor<float>(float2*, int64_t, int64_t, LDUWork<float>&, int*, GemmFn<float>, void*,
+                                         cudaStream_t);
+template mnpbem_status ldu_factor<double>(double2*, int64_t, int64_t, LDUWork<double>&, int*, GemmFn<double>, void*,
+                                          cudaStream_t);
+template mnpbem_status ldu_rsolve<float>(float2*, int64_t, int64_t, const float2*, int64_t, LDUWork<float>&,
+                                         GemmFn<float>, void*, cudaStream_t);
+template mnpbem_status ldu_rsolve<double>(double2*, int64_t, int64_t, const double2*, int64_t, LDUWork<double>&,
+                                          GemmFn<double>, void*, cudaStream_t);
+template mnpbem_status ldu_solve<float>(const float2*, int64_t, int64_t, int, float2*, int64_t, int64_t, float2*,
+                                        GemmFn<float>, void*, cudaStream_t);
+template mnpbem_status ldu_solve<double>(const double2*, int64_t, int64_t, int, double2*, int64_t, int64_t, double2*,
+                                         GemmFn<double>, void*, cudaStream_t);
 
 }  // namespace mnpbem

@@ -55,4 +55,37 @@ mnpbem_status gj_invert(cplx<R>* A, int64_t n, int64_t lda, GJWork<R>& w, GemmFn
 template <typename R>
 mnpbem_status gj_status_copy(GJWork<R>& w, int* host2, cudaStream_t st);
 
+// ------------------------------------------------------ block LDU factors
+// A = L D U in place: L unit block-lower (stored below the diagonal blocks),
+// D block-diagonal with the inverses X_k of its blocks stored in the diagonal
+// blocks, U unit block-upper (stored above them: U_kj = X_k A_kj after the
+// updates of the steps before k).  Blocks of w.b rows; the trailing updates
+// of w.m consecutive steps are gathered into one product of rank w.b * w.m.
+// Each diagonal block is inverted with partial pivoting inside the block
+// (CUDA-core path, 64-wide blocks) or by the 256-wide cluster kernel.
+// Status words (device, cleared by ldu_status_clear): [0] != 0 when a block
+// inverse met a zero or non-finite pivot; [1] the largest per-block condition
+// proxy max|A_kk| * max|X_k| as the bits of a non-negative float.
+template <typename R>
+struct LDUWork {
+  DevBuf ccol, rrow, xblk, tmp;
+  int b = 64;
+  int m = 1;
+  bool round_a = true;   // tensor-core path: A operands rounded to nearest TF32
+};
+// status: int[2] in device memory (see above)
+template <typename R>
+mnpbem_status ldu_factor(cplx<R>* A, int64_t n, int64_t lda, LDUWork<R>& w, int* status, GemmFn<R> gemm,
+                         void* ctx, cudaStream_t st);
+// H [n x n] <- H F^-1 with F the block LDU factors of an n x n matrix (same b)
+template <typename R>
+mnpbem_status ldu_rsolve(cplx<R>* H, int64_t n, int64_t ldh, const cplx<R>* F, int64_t ldf, LDUWork<R>& w,
+                         GemmFn<R> gemm, void* ctx, cudaStream_t st);
+// X [n x N] <- F^-1 X in place (F block LDU factors with blocks of b rows).
+// The transposed solve F^-T X is the same call on the in-place transpose of F.
+// tmp: workspace of b * N values, used only for N > 16 (may be null otherwise).
+template <typename R>
+mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int64_t N,
+                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st);
+
 }  // namespace mnpbem

@@ -36,17 +36,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; false (and err |= code) when the limit expires
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+// bounded wait with a limit of limit_ns; false (and err |= code) when it expires
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t bar, uint32_t parity, int* err, int code,
+                                             unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (gtimer() - t0 > MBAR_WAIT_NS) {
+    if (gtimer() - t0 > limit_ns) {
       atomicOr(err, code);
       return false;
     }
   }
+}
+// bounded wait with the library's limit (MBAR_WAIT_NS)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  return mbar_wait_ns(bar, parity, err, code, MBAR_WAIT_NS);
 }
 
 }  // namespace mnpbem

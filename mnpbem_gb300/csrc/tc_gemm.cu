@@ -865,6 +865,23 @@ mnpbem_status tc_check_error(TcGemmCtx& c, cudaStream_t st) {
   return MNPBEM_OK;
 }
 
+// ---------------------------------------------------- bounded-wait self test
+// One CTA waits on an mbarrier that nothing arrives at, through the same
+// bounded-wait helper as the pipelines above but with a short limit: the wait
+// expires, the error word records the code and the kernel returns, leaving
+// the context usable.  Tests check that the host then sees MNPBEM_ERR_TIMEOUT.
+__global__ void k_wait_selftest(int* err, unsigned long long limit_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  const uint32_t b = smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    mbar_init(b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait_ns(b, 0, err, 32, limit_ns);   // phase 0 never completes
+  __syncthreads();
+}
+
 void tc_release(TcGemmCtx& c) {
   c.bexp.release();
   c.err.release();
@@ -872,3 +889,30 @@ void tc_release(TcGemmCtx& c) {
 }
 
 }  // namespace mnpbem
+
+extern "C" mnpbem_status mnpbem_selftest_bounded_wait(int32_t device, int32_t limit_us) {
+  using namespace mnpbem;
+  if (limit_us < 1 || limit_us > 1000000) {
+    set_error("mnpbem_selftest_bounded_wait: limit must be 1 us .. 1 s");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess) cudaGetLastError();
+  if (device < 0 || device >= ndev) {
+    set_error("mnpbem_selftest_bounded_wait: invalid device %d", (int)device);
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  MNP_CUDA(cudaSetDevice(device));
+  DevBuf err;
+  MNP_TRY(err.ensure(sizeof(int)));
+  MNP_CUDA(cudaMemset(err.ptr, 0, sizeof(int)));
+  k_wait_selftest<<<1, 32>>>(err.as<int>(), 1000ull * (unsigned long long)limit_us);
+  MNP_CHECK_LAUNCH();
+  int h = 0;
+  MNP_CUDA(cudaMemcpy(&h, err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    set_error("bounded wait self test: the wait expired after %d us (code %d)", (int)limit_us, h);
+    return MNPBEM_ERR_TIMEOUT;
+  }
+  return MNPBEM_OK;
+}

@@ -71,6 +71,9 @@ def test_invalid_arguments_rejected_before_any_device_call(lib):
     assert lib.mnpbem_ext_gradient(None, None, 0, 500.0, None, 0, 0, None, None, None) == 1
     assert lib.mnpbem_surface_fields(None, 500.0, None, 0, 1, 2, *([None] * 10)) == 1
     assert lib.mnpbem_farfield(None, 500.0, None, 0, 1, 1, None, 1, *([None] * 6)) == 1
+    assert lib.mnpbem_geom_stat(None, b"block_cond_max", None) == 1
+    assert lib.mnpbem_selftest_bounded_wait(0, 0) == 1          # limit out of range
+    assert lib.mnpbem_selftest_bounded_wait(0, 2000000) == 1
 
 
 def test_materials():

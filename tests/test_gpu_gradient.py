@@ -86,14 +86,18 @@ def test_scattering_gradient_rod_vs_finite_differences(gpu_lib):
     assert abs(float(np.sum(gv * dv)) - fd) / abs(fd) < 1e-4
 
 
-def test_autograd_gradcheck(gpu_lib):
+@pytest.mark.parametrize("which", ["extinction", "scattering"])
+def test_autograd_gradcheck(gpu_lib, which):
     torch = pytest.importorskip("torch")
-    from mnpbem_gb300.autograd import extinction
+    from mnpbem_gb300 import autograd
+    cross_section = getattr(autograd, which)
     v, f = shapes.trisphere(32, 10.0)
     verts = torch.tensor(v, dtype=torch.float64, requires_grad=True)
     eps = torch.tensor([EPS_IN.real, EPS_IN.imag], dtype=torch.float64, requires_grad=True)
-    fn = lambda vv, ee: extinction(vv, ee, f, 520.0)
-    assert torch.autograd.gradcheck(fn, (verts, eps), eps=1e-5, atol=1e-6, rtol=1e-4, nondet_tol=1e-12)
+    fn = lambda vv, ee: cross_section(vv, ee, f, 520.0)
+    # the scattering cross section is ~1e-3 of the extinction on this 10 nm sphere
+    atol = 1e-6 if which == "extinction" else 1e-9
+    assert torch.autograd.gradcheck(fn, (verts, eps), eps=1e-5, atol=atol, rtol=1e-4, nondet_tol=1e-12)
 
 
 @pytest.mark.parametrize("which", ["ext", "sca"])
