@@ -107,6 +107,7 @@ struct Lane {
   LDUWork<float> lu32;   // block LDU factors of G1, G2, Sigma
   LDUWork<double> lu64;
   DevBuf lu_status;      // LDU status words (see dense.cuh)
+  DevBuf lu_bar;         // grid-barrier words of the one-launch triangular sweeps
   TcGemmCtx tc;
   int* status_host = nullptr;     // pinned: Gauss-Jordan (4), LDU (2), tensor-core error word (1), spare
   double* norms_host = nullptr;   // pinned: refinement norms (4)
@@ -223,6 +224,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
   }
   if (s == MNPBEM_OK) s = L->lp_dev.ensure(sizeof(LamParams));
   if (s == MNPBEM_OK) s = L->lu_status.ensure(2 * sizeof(int));
+  if (s == MNPBEM_OK) s = L->lu_bar.ensure(2 * sizeof(unsigned));
   if (s != MNPBEM_OK) {
     lane_release(*L);
     return s;
@@ -839,6 +841,7 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   lu(L.lu32);
   lu(L.lu64);
   mixbuf(L.lu_status);
+  mixbuf(L.lu_bar);
   mix(nullptr, (size_t)G->lu_steps);
   mix(L.status_host, 0);
   mix(L.norms_host, 0);
@@ -929,6 +932,7 @@ ChainMats<R> chain_mats(mnpbem_geom* G, Lane& L) {
   m.Deltai = L.mat[4].as<Cx>();
   m.ld = G->ld;
   m.b = lu_block<R>(G, sizeof(R) == 4 ? tc_ctx(G, L) : nullptr);
+  m.bar = L.lu_bar.as<unsigned>();
   m.ng1 = (int)G->g1_off.size();
   for (int q = 0; q < m.ng1; ++q) {
     m.g1_off[q] = G->g1_off[q];
@@ -1093,6 +1097,21 @@ mnpbem_status stage_first(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   return MNPBEM_OK;
 }
 
+// Y = G1 x, Z = H1 x from the hi (and, with ds, lo) planes, one product per
+// diagonal block of G1 and H1 (their off-diagonal blocks are zero)
+mnpbem_status residual_g1h1(mnpbem_geom* G, const float2* const* hl, bool ds, const double2* x, double2* Y,
+                            double2* Z, int N, float2* bs, cudaStream_t st) {
+  const int64_t n = G->g.n, ld = G->ld;
+  for (size_t q = 0; q < G->g1_off.size(); ++q) {
+    const int64_t o = G->g1_off[q], nq = G->g1_n[q], off = o * ld + o;
+    MNP_TRY(gemm_thin_ds(nq, N, nq, hl[0] + off, ds ? hl[0] + n * ld + off : nullptr, ld, x + o * N, N, Y + o * N, N,
+                         bs, st));
+    MNP_TRY(gemm_thin_ds(nq, N, nq, hl[1] + off, ds ? hl[1] + n * ld + off : nullptr, ld, x + o * N, N, Z + o * N, N,
+                         bs, st));
+  }
+  return MNPBEM_OK;
+}
+
 // ---------------------------------------------------------------- S3 / S5
 // norms[0..1] = ||r||^2, ||b||^2 ; norms[2..3] = ||dx||^2, ||x||^2
 // ds: residual products in double-single arithmetic from the hi / lo planes
@@ -1107,11 +1126,10 @@ mnpbem_status stage_iter(mnpbem_geom* G, Lane& L, const SolveCtx& c, bool ds) {
   const float2* hl[4];
   for (int q = 0; q < 4; ++q) hl[q] = L.mat64[q].as<float2>();
   double* norms = L.norms.as<double>();
-  // G1 x1, H1 x1, G2 x2, H2 x2
+  // G1 x1, H1 x1 (per diagonal block of G1 and H1), G2 x2, H2 x2
   float2* bs = L.bsplit.as<float2>();
   auto lo = [&](int q) -> const float2* { return ds ? hl[q] + n * ld : nullptr; };
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], lo(0), ld, v.x1, 4 * P, v.Y1, 4 * P, bs, st));
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], lo(1), ld, v.x1, 4 * P, v.Z1, 4 * P, bs, st));
+  MNP_TRY(residual_g1h1(G, hl, ds, v.x1, v.Y1, v.Z1, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], lo(2), ld, v.x2, 4 * P, v.Y2, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], lo(3), ld, v.x2, 4 * P, v.Z2, 4 * P, bs, st));
   MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
@@ -1143,8 +1161,7 @@ mnpbem_status stage_incr(mnpbem_geom* G, Lane& L, const SolveCtx& c) {
   launch_cvt_f2d(fx_ptr(G, L, P, 1), v.d2, 4 * n * P, st);
   MNP_CHECK_LAUNCH();
   float2* bs = L.bsplit.as<float2>();
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[0], nullptr, ld, v.d1, 4 * P, v.Y1, 4 * P, bs, st));
-  MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[1], nullptr, ld, v.d1, 4 * P, v.Z1, 4 * P, bs, st));
+  MNP_TRY(residual_g1h1(G, hl, false, v.d1, v.Y1, v.Z1, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[2], nullptr, ld, v.d2, 4 * P, v.Y2, 4 * P, bs, st));
   MNP_TRY(gemm_thin_ds(n, 4 * P, n, hl[3], nullptr, ld, v.d2, 4 * P, v.Z2, 4 * P, bs, st));
   MNP_CUDA(cudaMemsetAsync(norms, 0, sizeof(double) * 4, st));
@@ -1841,14 +1858,14 @@ mnpbem_status chain_transpose(const AdjParams& p, const ChainMats<R>& m, const c
   auto g1solve = [&](Cx* x, int N) -> mnpbem_status {
     for (int q = 0; q < m.ng1; ++q)
       MNP_TRY(ldu_solve<R>(m.G1 + m.g1_off[q] * ld + m.g1_off[q], m.g1_n[q], ld, m.b, x + m.g1_off[q] * N, N, N,
-                           nullptr, gemm, ctx, st));
+                           nullptr, gemm, ctx, st, m.bar));
     return MNPBEM_OK;
   };
   // G2^-T w_sig2, G2^-T w_h2
   MNP_CUDA(cudaMemcpyAsync(gS2, gs2, cs * n, cudaMemcpyDeviceToDevice, st));
   MNP_CUDA(cudaMemcpyAsync(gH2p, gh2, cs * 3 * n, cudaMemcpyDeviceToDevice, st));
-  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gS2, 1, 1, nullptr, gemm, ctx, st));
-  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gH2p, 3, 3, nullptr, gemm, ctx, st));
+  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gS2, 1, 1, nullptr, gemm, ctx, st, m.bar));
+  MNP_TRY(ldu_solve<R>(m.G2, n, ld, m.b, gH2p, 3, 3, nullptr, gemm, ctx, st, m.bar));
   if (gs1) {
     MNP_CUDA(cudaMemcpyAsync(lphi, gs1, cs * n, cudaMemcpyDeviceToDevice, st));
     MNP_TRY(g1solve(lphi, 1));                                                     // G1^-T w_sig1
@@ -1864,7 +1881,7 @@ mnpbem_status chain_transpose(const AdjParams& p, const ChainMats<R>& m, const c
   MNP_TRY(gemm(n, 3, n, one, m.Deltai, ld, gH2p, 3, zero, lal, 3, st, ctx));        // Deltai^T
   adj_chainT<Cx>(p, 0, lal, nullptr, gS2, nullptr, nullptr, nullptr, st);
   MNP_CUDA(cudaMemcpyAsync(lDe, gS2, cs * n, cudaMemcpyDeviceToDevice, st));
-  MNP_TRY(ldu_solve<R>(m.Sigma, n, ld, m.b, lDe, 1, 1, nullptr, gemm, ctx, st));     // Sigma^-T
+  MNP_TRY(ldu_solve<R>(m.Sigma, n, ld, m.b, lDe, 1, 1, nullptr, gemm, ctx, st, m.bar));   // Sigma^-T
   adj_chainT<Cx>(p, 1, lDe, nullptr, v3, nullptr, nullptr, nullptr, st);
   MNP_TRY(gemm(n, 3, n, one, m.Deltai, ld, v3, 3, one, lal, 3, st, ctx));           // += Deltai^T v
   MNP_TRY(gemm(n, 1, n, one, m.Sigma1, ld, lDe, 1, zero, tS1, 1, st, ctx));         // Sigma1^T

@@ -233,14 +233,19 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, cons
   if (Profiler* pr = current_profiler()) pr->acc[PH_ELEMWISE].launches += 5;
   k_chain_pre<R><<<nb, 128, 0, st>>>(f, P, phi, a, X4);
   MNP_CHECK_LAUNCH();
-  MNP_TRY(gemm(n, 4 * P, n, one, m.Sigma1, m.ld, X4, 4 * P, zero, T4, 4 * P, st, ctx));
+  // Sigma1 = H1 G1^-1 shares G1's diagonal blocks
+  for (int q = 0; q < m.ng1; ++q) {
+    const int64_t o = m.g1_off[q];
+    MNP_TRY(gemm(m.g1_n[q], 4 * P, m.g1_n[q], one, m.Sigma1 + o * m.ld + o, m.ld, X4 + o * 4 * P, 4 * P, zero,
+                 T4 + o * 4 * P, 4 * P, st, ctx));
+  }
   k_chain_alpha_de<R><<<nb, 128, 0, st>>>(f, P, lp, phi, a, alpha, De, T4, al, Dp);
   MNP_CHECK_LAUNCH();
   MNP_TRY(gemm(n, 3 * P, n, one, m.Deltai, m.ld, al, 3 * P, zero, t3, 3 * P, st, ctx));
   k_chain_u<R><<<nb, 128, 0, st>>>(f, P, lp, Dp, t3, u);
   MNP_CHECK_LAUNCH();
   // sig2 = Sigma \ u (in place)
-  MNP_TRY(ldu_solve<R>(m.Sigma, n, m.ld, m.b, u, P, P, nullptr, gemm, ctx, st));
+  MNP_TRY(ldu_solve<R>(m.Sigma, n, m.ld, m.b, u, P, P, nullptr, gemm, ctx, st, m.bar));
   s2 = u;
   k_chain_v<R><<<nb, 128, 0, st>>>(f, P, lp, s2, al, v3);
   MNP_CHECK_LAUNCH();
@@ -250,8 +255,8 @@ mnpbem_status apply_mldivide(const FaceData& f, int P, const LamParams* lp, cons
   MNP_CHECK_LAUNCH();
   for (int q = 0; q < m.ng1; ++q)
     MNP_TRY(ldu_solve<R>(m.G1 + m.g1_off[q] * m.ld + m.g1_off[q], m.g1_n[q], m.ld, m.b, x1 + m.g1_off[q] * 4 * P,
-                         4 * P, 4 * P, nullptr, gemm, ctx, st));
-  MNP_TRY(ldu_solve<R>(m.G2, n, m.ld, m.b, x2, 4 * P, 4 * P, nullptr, gemm, ctx, st));
+                         4 * P, 4 * P, nullptr, gemm, ctx, st, m.bar));
+  MNP_TRY(ldu_solve<R>(m.G2, n, m.ld, m.b, x2, 4 * P, 4 * P, nullptr, gemm, ctx, st, m.bar));
   return MNPBEM_OK;
 }
 template mnpbem_status apply_mldivide<float>(const FaceData&, int, const LamParams*, const ChainMats<float>&,

@@ -54,6 +54,7 @@ template <typename R> struct ChainMats {
   const cplx<R>* G1; const cplx<R>* G2; const cplx<R>* Sigma1; const cplx<R>* Deltai;
   const cplx<R>* Sigma; int64_t ld;
   int b = 64;                      // rows of the diagonal blocks of the LDU factors
+  unsigned* bar = nullptr;         // grid-barrier words of the one-launch triangular sweeps (per stream)
   int ng1 = 1;
   int64_t g1_off[CHAIN_MAXBLK] = {0};
   int64_t g1_n[CHAIN_MAXBLK] = {0};

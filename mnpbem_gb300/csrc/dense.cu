@@ -1409,17 +1409,169 @@ __global__ void __launch_bounds__(256) k_ldu_diag(const cplx<R>* __restrict__ F,
   }
 }
 
+// ------------------------------------------- triangular sweeps, one launch
+// The forward (unit lower L) and backward (unit upper U) sweeps of the LDU
+// solve for a few right-hand sides as one cooperative launch each.  Step s
+// takes block k (k = s forward, nblk - 1 - s backward): every CTA stages x_k
+// (b x N) in shared memory and subtracts F[i, k block] x_k from its rows i of
+// the trailing (forward) or leading (backward) part; then the CTAs meet at a
+// grid barrier before the next block is read.  Rows go to the CTAs in groups
+// of TRSV_GRP by their absolute index (group g to CTA g mod G); a warp takes a
+// row at a time (lanes along the row, coalesced) and reduces with shuffles.
+// X is read with ld.global.cg (L2), since other CTAs updated it.  The grid
+// barrier is a monotonic arrival counter (zeroed before the launch) with a
+// bounded wait; on expiry the error word of the streamed thin products is
+// set, an abort flag releases the other CTAs and every CTA returns.
+constexpr int TRSV_THREADS = 256, TRSV_GRP = 8;
+
+__device__ __forceinline__ bool coop_barrier(unsigned* ctr, unsigned target, int* abortf) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    const unsigned long long t0 = gtimer();
+    while (*(volatile unsigned*)ctr < target) {
+      if (*(volatile int*)abortf) { ok = 0; break; }
+      if (gtimer() - t0 > MBAR_WAIT_NS) {
+        atomicOr(&g_thin_stream_err, 64);
+        atomicExch(abortf, 1);
+        ok = 0;
+        break;
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <typename R, int NB, bool LOWER>
+__global__ void __launch_bounds__(TRSV_THREADS) k_trsv_unit(const cplx<R>* __restrict__ F, int64_t ldf, int64_t n,
+                                                            int b, cplx<R>* X, int64_t ldx, int N, unsigned* bar) {
+  using Cx = cplx<R>;
+  extern __shared__ unsigned char trsv_smem[];
+  Cx* xs = reinterpret_cast<Cx*>(trsv_smem);   // [b][NB], columns N .. NB - 1 zero
+  const int nblk = (int)((n + b - 1) / b);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NW = TRSV_THREADS / 32;
+  const int64_t G = gridDim.x;
+  int* abortf = reinterpret_cast<int*>(bar + 1);
+  for (int s = 0; s + 1 < nblk; ++s) {
+    const int k = LOWER ? s : nblk - 1 - s;
+    const int64_t k0 = (int64_t)k * b;
+    const int bs = (int)min((int64_t)b, n - k0);
+    for (int e = threadIdx.x; e < bs * NB; e += TRSV_THREADS) {
+      const int r = e / NB, c = e % NB;
+      xs[e] = c < N ? __ldcg(X + (k0 + r) * ldx + c) : mk<R>(0, 0);
+    }
+    __syncthreads();
+    const int64_t r0 = LOWER ? k0 + bs : 0, r1 = LOWER ? n : k0;
+    // groups of rows by absolute index: the first group this CTA owns at or after r0
+    int64_t g = r0 / TRSV_GRP;
+    g += (blockIdx.x - g % G + G) % G;
+    for (; g * TRSV_GRP < r1; g += G) {
+      for (int rr = warp; rr < TRSV_GRP; rr += NW) {
+        const int64_t i = g * TRSV_GRP + rr;
+        if (i < r0 || i >= r1) continue;
+        const Cx* frow = F + i * ldf + k0;
+        Cx acc[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) acc[c] = mk<R>(0, 0);
+#pragma unroll 4
+        for (int l = lane; l < bs; l += 32) {
+          const Cx f = __ldg(frow + l);
+#pragma unroll
+          for (int c = 0; c < NB; ++c) cfma(acc[c], f, xs[l * NB + c]);
+        }
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+          Cx v = acc[c];
+          for (int o = 16; o; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+          }
+          if (lane == c && c < N) {
+            Cx* xp = X + i * ldx + c;
+            *xp = csub(__ldcg(xp), v);
+          }
+        }
+      }
+    }
+    if (!coop_barrier(bar, (unsigned)((s + 1) * G), abortf)) return;
+  }
+}
+
+static int trsv_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+      cudaGetLastError();
+      sms = 148;
+    }
+  }
+  return sms;
+}
+
+template <typename R, int NB, bool LOWER>
+static mnpbem_status launch_trsv(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int N,
+                                 unsigned* bar, cudaStream_t st) {
+  using Cx = cplx<R>;
+  const size_t smem = sizeof(Cx) * b * NB;
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_unit<R, NB, LOWER>, TRSV_THREADS,
+                                                      sizeof(Cx) * 256 * NB) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    per_sm = std::max(1, std::min(per_sm, 2));
+  }
+  const unsigned grid = (unsigned)(per_sm * trsv_sms());
+  MNP_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+  ProfScope ps(PH_GEMM_SMALL, st, 4.0 * n * n * N, (double)sizeof(Cx) * 0.5 * n * n);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(TRSV_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MNP_CUDA(cudaLaunchKernelEx(&cfg, k_trsv_unit<R, NB, LOWER>, F, ldf, n, b, X, ldx, N, bar));
+  return MNPBEM_OK;
+}
+
+template <typename R, bool LOWER>
+static mnpbem_status trsv_sweep(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int N,
+                                unsigned* bar, cudaStream_t st) {
+  if (N <= 4) return launch_trsv<R, 4, LOWER>(F, n, ldf, b, X, ldx, N, bar, st);
+  if (N <= 8) return launch_trsv<R, 8, LOWER>(F, n, ldf, b, X, ldx, N, bar, st);
+  return launch_trsv<R, 16, LOWER>(F, n, ldf, b, X, ldx, N, bar, st);
+}
+
 template <typename R>
 mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int64_t N,
-                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st) {
+                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st, unsigned* bar) {
   using Cx = cplx<R>;
   if (n <= 0 || N <= 0) return MNPBEM_OK;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
   const int64_t nblk = cdiv_up(n, (int64_t)b);
+  const bool sweep = bar && N <= 16 && b <= 256;
   // forward: L unit lower
-  for (int64_t k = 0; k + 1 < nblk; ++k) {
-    const int64_t k0 = k * b, kb = k0 + b;
-    MNP_TRY(gemm(n - kb, N, b, mone, F + kb * ldf + k0, ldf, X + k0 * ldx, ldx, one, X + kb * ldx, ldx, st, ctx));
+  if (sweep) {
+    if (nblk > 1) MNP_TRY((trsv_sweep<R, true>(F, n, ldf, b, X, ldx, (int)N, bar, st)));
+  } else {
+    for (int64_t k = 0; k + 1 < nblk; ++k) {
+      const int64_t k0 = k * b, kb = k0 + b;
+      MNP_TRY(gemm(n - kb, N, b, mone, F + kb * ldf + k0, ldf, X + k0 * ldx, ldx, one, X + kb * ldx, ldx, st, ctx));
+    }
   }
   // block diagonal
   if (N <= 16) {
@@ -1441,6 +1593,10 @@ mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>
     }
   }
   // backward: U unit upper
+  if (sweep) {
+    if (nblk > 1) MNP_TRY((trsv_sweep<R, false>(F, n, ldf, b, X, ldx, (int)N, bar, st)));
+    return MNPBEM_OK;
+  }
   for (int64_t k = nblk - 1; k >= 1; --k) {
     const int64_t k0 = k * b;
     const int bs = (int)std::min<int64_t>(b, n - k0);
@@ -1458,8 +1614,8 @@ template mnpbem_status ldu_rsolve<float>(float2*, int64_t, int64_t, const float2
 template mnpbem_status ldu_rsolve<double>(double2*, int64_t, int64_t, const double2*, int64_t, LDUWork<double>&,
                                           GemmFn<double>, void*, cudaStream_t);
 template mnpbem_status ldu_solve<float>(const float2*, int64_t, int64_t, int, float2*, int64_t, int64_t, float2*,
-                                        GemmFn<float>, void*, cudaStream_t);
+                                        GemmFn<float>, void*, cudaStream_t, unsigned*);
 template mnpbem_status ldu_solve<double>(const double2*, int64_t, int64_t, int, double2*, int64_t, int64_t, double2*,
-                                         GemmFn<double>, void*, cudaStream_t);
+                                         GemmFn<double>, void*, cudaStream_t, unsigned*);
 
 }  // namespace mnpbem

@@ -84,8 +84,10 @@ mnpbem_status ldu_rsolve(cplx<R>* H, int64_t n, int64_t ldh, const cplx<R>* F, i
 // X [n x N] <- F^-1 X in place (F block LDU factors with blocks of b rows).
 // The transposed solve F^-T X is the same call on the in-place transpose of F.
 // tmp: workspace of b * N values, used only for N > 16 (may be null otherwise).
+// bar: two device words for the grid barrier of the one-launch triangular
+// sweeps (N <= 16; one pair per stream); null: one product per block instead.
 template <typename R>
 mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>* X, int64_t ldx, int64_t N,
-                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st);
+                        cplx<R>* tmp, GemmFn<R> gemm, void* ctx, cudaStream_t st, unsigned* bar = nullptr);
 
 }  // namespace mnpbem
