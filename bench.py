@@ -45,7 +45,7 @@ DRUDE = (10.0, 9.065, 0.0708)
 # along +z, 32 wavelengths 500-900 nm.  sphere4000: one d = 50 nm sphere with
 # 4000 faces, 60 wavelengths 450-750 nm.
 WORKLOADS = {
-    "dimer24k": {"faces": 24000, "grid": (500.0, 900.0, 32), "batch": 4, "dimer": True},
+    "dimer24k": {"faces": 24000, "grid": (500.0, 900.0, 32), "batch": 3, "dimer": True},
     "sphere4000": {"faces": 4000, "grid": (450.0, 750.0, 60), "batch": 20, "dimer": False},
 }
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant

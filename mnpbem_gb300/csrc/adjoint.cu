@@ -607,8 +607,7 @@ __global__ void k_adj_norm_flat(AdjParams p) {
   for (int tr = 0; tr < ntri; ++tr) {
     int a, b, c;
     tri_ids(f, tr, a, b, c);
-    const double3 N = vcross(vsub(vld(p.verts, a), vld(p.verts, b)), vsub(vld(p.verts, c), vld(p.verts, b)));
-    ar[tr] = 0.5 * sqrt(vdot(N, N));
+    ar[tr] = tri_area_rn(vld(p.verts, a), vld(p.verts, b), vld(p.verts, c));   // the choice of k_norm_flat
   }
   const int big = (ntri == 2 && ar[1] > ar[0]) ? 1 : 0;
   for (int tr = 0; tr < ntri; ++tr) {

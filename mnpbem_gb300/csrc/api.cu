@@ -159,8 +159,8 @@ struct mnpbem_geom {
   int64_t ld = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
   int lanes_req = 0;        // 0: automatic
-  int gj_nb = 256;          // Gauss-Jordan step width on the tensor-core path (256 or 512)
-  int lu_steps = 2;         // LDU steps of 256 per trailing update on the tensor-core path (1, 2 or 4)
+  int gj_nb = 0;            // Gauss-Jordan step width on the tensor-core path (256 or 512; 0: by size)
+  int lu_steps = 0;         // LDU steps of 256 per trailing update on the tensor-core path (1, 2 or 4; 0: by size)
   std::vector<int64_t> g1_off, g1_n;   // diagonal blocks of G1 (one block when G1 is full)
   bool tf32_rna = true;     // round tensor-core A operands to nearest TF32
   bool asm_ds = true;       // mixed-precision assembly in double-single FP32 arithmetic
@@ -843,6 +843,7 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   mixbuf(L.lu_status);
   mixbuf(L.lu_bar);
   mix(nullptr, (size_t)G->lu_steps);
+  mix(nullptr, (size_t)G->gj_nb);
   mix(L.status_host, 0);
   mix(L.norms_host, 0);
   // tuning options baked into the captured launches
@@ -987,12 +988,16 @@ mnpbem_status stage_initmat(mnpbem_geom* G, Lane& L, bool direct) {
   void* ctx = sizeof(R) == 4 ? tc_ctx(G, L) : nullptr;
   // wider Gauss-Jordan steps when the rank-nb updates run on tensor cores:
   // fewer passes over the n x n matrix (each step reads and writes it once)
-  gjw<R>(L).nb = (ctx && n >= 1024) ? G->gj_nb : 64;
+  // By size (measured on GB300, 24 000-face dimer: rank-1024 LDU updates and
+  // 512-wide Gauss-Jordan steps 1.365 against 1.265 wavelength-solves/s for
+  // rank-512 / 256-wide; at 4000 faces the 256-wide steps were faster)
+  const bool large = n >= 12000;
+  gjw<R>(L).nb = (ctx && n >= 1024) ? (G->gj_nb ? G->gj_nb : (large ? 512 : 256)) : 64;
   gjw<R>(L).round_a = G->tf32_rna;
   gjw<R>(L).fused = G->gj_fused;
   LDUWork<R>& lw = luw<R>(L);
   lw.b = lu_block<R>(G, ctx);
-  lw.m = lw.b == 256 ? G->lu_steps : 1;
+  lw.m = lw.b == 256 ? (G->lu_steps ? G->lu_steps : (large ? 4 : 2)) : 1;
   lw.round_a = G->tf32_rna;
   int* lus = L.lu_status.as<int>();
   MNP_CUDA(cudaMemsetAsync(lus, 0, 2 * sizeof(int), L.st));

@@ -92,6 +92,24 @@ struct LamParams {
   int pad;
 };
 
+// Area of the triangle (v1, v2, v3) as norm_flat.m computes it: N = (v1 - v2) x
+// (v3 - v2), 0.5 sqrt(N . N), every product and sum rounded on its own in that
+// order (no fused multiply-add).  A quadrilateral takes the basis of the
+// larger of its two triangles; for symmetric warped quadrilaterals (rounded
+// cube edges) the two areas agree to the last bits, so the choice must follow
+// the same roundings as the reference's (and the oracle's) evaluation.
+#ifdef __CUDACC__
+__device__ __forceinline__ double tri_area_rn(double3 v1, double3 v2, double3 v3) {
+  const double ax = __dsub_rn(v1.x, v2.x), ay = __dsub_rn(v1.y, v2.y), az = __dsub_rn(v1.z, v2.z);
+  const double bx = __dsub_rn(v3.x, v2.x), by = __dsub_rn(v3.y, v2.y), bz = __dsub_rn(v3.z, v2.z);
+  const double nx = __dsub_rn(__dmul_rn(ay, bz), __dmul_rn(az, by));
+  const double ny = __dsub_rn(__dmul_rn(az, bx), __dmul_rn(ax, bz));
+  const double nz = __dsub_rn(__dmul_rn(ax, by), __dmul_rn(ay, bx));
+  const double nn = __dadd_rn(__dadd_rn(__dmul_rn(nx, nx), __dmul_rn(ny, ny)), __dmul_rn(nz, nz));
+  return __dmul_rn(0.5, __dsqrt_rn(nn));
+}
+#endif
+
 inline int64_t cdiv_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return cdiv_up(a, b) * b; }
 

@@ -33,7 +33,7 @@ __global__ void k_norm_flat(int n, const double* __restrict__ verts, const int* 
   // first triangle (1,2,3): vec1 = v1 - v2, vec2 = v3 - v2
   double3 a1 = sub3(v1, v2), b1 = sub3(v3, v2);
   double3 n1 = cross3(a1, b1);
-  double ar1 = 0.5 * sqrt(dot3(n1, n1));
+  double ar1 = tri_area_rn(v1, v2, v3);
   double3 t1 = a1, nn = n1;
   double ar = ar1;
   if (quad) {
@@ -41,7 +41,7 @@ __global__ void k_norm_flat(int n, const double* __restrict__ verts, const int* 
     double3 v4 = ld3(verts, f[3]);
     double3 a2 = sub3(v3, v4), b2 = sub3(v1, v4);
     double3 n2 = cross3(a2, b2);
-    double ar2 = 0.5 * sqrt(dot3(n2, n2));
+    double ar2 = tri_area_rn(v3, v4, v1);
     ar = ar1 + ar2;
     if (ar2 > ar1) { t1 = a2; nn = n2; }
   }
