@@ -242,9 +242,11 @@ MNPBEM_API mnpbem_status mnpbem_profile_read(mnpbem_geom* g, int32_t phase, doub
  * tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation), path 2 = the
  * same on CTA pairs (cta_group::2, 256 x 256 tiles; M >= 256, else path 1)
  * with a TMA store / reduce-add epilogue, path 3 = CTA pairs with vector
- * stores / reductions from the load-store path.
- * The building block of the inversions and products of initmat.m (MATLAB
- * mtimes on complex matrices); beta must be real for paths 1 and 2.          */
+ * stores / reductions from the load-store path, path 4 = single-CTA
+ * tensor-core kernel on FP16 operands (kind::f16) scaled per row of A and per
+ * column of B by powers of two, FP32 accumulation.
+ * The building block of the factorisations and products of initmat.m (MATLAB
+ * mtimes on complex matrices); beta must be real for paths 1 to 4.           */
 MNPBEM_API mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N,
                                          int64_t K, const float* alpha, const float* A,
                                          int64_t lda, const float* B, int64_t ldb,
@@ -293,7 +295,9 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
  * clusters of other lanes), "tc_pair" (only 0: the CTA-pair tensor-core GEMM
  * is not used inside sweeps; 1 / -1 return MNPBEM_ERR_UNSUPPORTED),
  * "lu_steps" (256-row LDU steps gathered into one trailing update: 1, 2 or
- * 4, i.e. updates of rank 256, 512 or 1024), "tf32_round" (round A operands to nearest
+ * 4, i.e. updates of rank 256, 512 or 1024), "tc_f16" (tensor-core products
+ * on FP16 operands scaled per row / column by powers of two, kind::f16, 1 =
+ * default, or on TF32 operands, 0), "tf32_round" (round A operands to nearest
  * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
  * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
  * No counterpart in the reference.                                          */

@@ -168,6 +168,7 @@ struct mnpbem_geom {
   int tc_stages = 0;        // pipeline depth of the tensor-core GEMM (0: its default)
   int tc_ctas = 0;          // CTAs of the persistent tensor-core GEMM (0: one per SM)
   int tc_pair = 0;          // CTA-pair tensor-core GEMM: 1 always, 0 off, -1 long-K products
+  bool tc_f16 = true;       // tensor-core products with scaled FP16 operands (kind::f16) instead of TF32
   bool tc_enabled = true;
   bool use_graphs = true;
   Profiler prof;
@@ -233,6 +234,7 @@ mnpbem_status add_lane(mnpbem_geom* G) {
   if (G->tc_stages) L->tc.stages = G->tc_stages;
   L->tc.max_ctas = G->tc_ctas;
   L->tc.pair = G->tc_pair;
+  L->tc.f16 = G->tc_f16;
   G->lanes.push_back(std::move(L));
   return MNPBEM_OK;
 }
@@ -449,6 +451,8 @@ static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const
   if (gjfenv && gjfenv[0] == '0') G->gj_fused = false;
   const char* nbenv = getenv("MNPBEM_GJ_NB");
   if (nbenv && atoi(nbenv) == 512) G->gj_nb = 512;
+  const char* f16env = getenv("MNPBEM_TC_F16");
+  if (f16env && f16env[0] == '0') G->tc_f16 = false;
   const char* luenv = getenv("MNPBEM_LU_STEPS");
   if (luenv && (atoi(luenv) == 1 || atoi(luenv) == 2 || atoi(luenv) == 4)) G->lu_steps = atoi(luenv);
   const char* lenv = getenv("MNPBEM_LANES");
@@ -542,6 +546,11 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
     return MNPBEM_ERR_UNSUPPORTED;
   }
   if (k == "lu_steps" && (value == 1 || value == 2 || value == 4)) { g->lu_steps = value; return MNPBEM_OK; }
+  if (k == "tc_f16" && (value == 0 || value == 1)) {
+    g->tc_f16 = value != 0;
+    for (auto& L : g->lanes) L->tc.f16 = g->tc_f16;
+    return MNPBEM_OK;
+  }
   if (k == "tc_ctas" && value >= 0 && value <= 4096) {
     g->tc_ctas = value;
     for (auto& L : g->lanes) L->tc.max_ctas = value;
@@ -712,7 +721,7 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
                               const float* alpha, const float* A, int64_t lda, const float* B,
                               int64_t ldb, const float* beta, float* C, int64_t ldc) {
   if (M <= 0 || N <= 0 || K <= 0 || !alpha || !beta || !A || !B || !C || lda < K || ldb < N ||
-      ldc < N || path < 0 || path > 3) {
+      ldc < N || path < 0 || path > 4) {
     set_error("mnpbem_gemm_c64: invalid arguments");
     return MNPBEM_ERR_INVALID_ARG;
   }
@@ -731,8 +740,9 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
   MNP_CUDA(cudaMemcpyAsync(dC.ptr, C, sizeof(float2) * M * ldc, cudaMemcpyHostToDevice, st));
   const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
   if (path >= 1) {
-    tc[device].pair = path >= 2 ? 1 : 0;
+    tc[device].pair = (path == 2 || path == 3) ? 1 : 0;
     tc[device].pair_epi = path == 3 ? 1 : 0;
+    tc[device].f16 = path == 4;
     if (!tc_gemm_eligible(tc[device], M, N, K, dA.ptr, lda, dC.ptr, ldc, be)) {
       set_error("tensor-core GEMM not available for this device or shape");
       return MNPBEM_ERR_UNSUPPORTED;
@@ -850,6 +860,7 @@ uint64_t lane_sig(const mnpbem_geom* G, const Lane& L) {
   mix(nullptr, (size_t)L.tc.stages);
   mix(nullptr, (size_t)L.tc.max_ctas);
   mix(nullptr, (size_t)(L.tc.pair + 1));
+  mix(nullptr, (size_t)L.tc.f16);
   mix(nullptr, (size_t)G->tf32_rna);
   mix(nullptr, (size_t)G->asm_ds);
   mix(nullptr, (size_t)G->gj_fused);

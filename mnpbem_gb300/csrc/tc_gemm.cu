@@ -19,6 +19,7 @@
 // records an error code, waits (bounded) for its own copies in flight, frees
 // its tensor memory and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include "mbarrier.cuh"
@@ -37,6 +38,9 @@ constexpr uint32_t TC_TMEM_COLS = 256;
 constexpr unsigned long long TC_WAIT_NS = MBAR_WAIT_NS;
 
 // instruction descriptor: D f32, A/B tf32, K-major A and B, N = 256, M = 128
+// kind::f16 with FP16 A and B (the same type for both), FP32 accumulator
+constexpr uint32_t TC_IDESC_F16 = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+                                  ((uint32_t)(TC_BM >> 4) << 24);
 constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
                               ((uint32_t)(TC_BM >> 4) << 24);
 
@@ -67,6 +71,13 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b,
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
       ::"r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
@@ -168,18 +179,25 @@ __device__ __forceinline__ void epi_chunk_lsu(const uint32_t (&r)[32], float* st
   __syncwarp();
 }
 
-template <int ST, int EPI>
+// F16: A and B' are FP16 (kind::f16), scaled per row of A and per complex
+// column of B' into FP16's range; the epilogue multiplies each accumulator by
+// inv_r[row] * inv_c[column / 2] before storing.  K2 counts elements of the
+// operand type (TF32 floats or halves); a K chunk is one 128-byte swizzle row
+// either way (32 floats or 64 halves).
+template <int ST, int EPI, bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
               const __grid_constant__ CUtensorMap mapC, const __grid_constant__ CUtensorMap mapP,
-              float* __restrict__ Cp, long long ldcf, int M, int N2, int K2, int accumulate, int* tile_ctr, int* err) {
+              float* __restrict__ Cp, long long ldcf, int M, int N2, int K2, int accumulate, int* tile_ctr, int* err,
+              const float* __restrict__ inv_r, const float* __restrict__ inv_c) {
+  constexpr int BK = F16 ? 64 : TC_BK;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long bars[2 * ST + 4 + 2 * TC_TQ];
   __shared__ int tq[TC_TQ];
   __shared__ uint32_t tmem_slot;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int KT = (K2 + TC_BK - 1) / TC_BK;
+  const int KT = (K2 + BK - 1) / BK;
   const int MT = (M + TC_BM - 1) / TC_BM, NT = (N2 + TC_BN - 1) / TC_BN;
   const int ntiles = MT * NT;
   const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[ST]);
@@ -241,8 +259,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           if (it >= ST && !mbar_wait(empty0 + 8 * s, ((it / ST) - 1) & 1, err, 1)) { ok = false; break; }
           const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
           mbar_expect_tx(full0 + 8 * s, TC_STAGE_BYTES);
-          tma_load_2d(sa, &mapA, full0 + 8 * s, kt * TC_BK, m0);
-          tma_load_2d(sb, &mapB, full0 + 8 * s, kt * TC_BK, n0);
+          tma_load_2d(sa, &mapA, full0 + 8 * s, kt * BK, m0);
+          tma_load_2d(sb, &mapB, full0 + 8 * s, kt * BK, n0);
           issued = it + 1;
         }
         if (!ok) {
@@ -278,9 +296,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t sa = base + s * TC_STAGE_BYTES, sb = sa + TC_A_BYTES;
           const uint64_t da = desc_sw128(sa), db = desc_sw128(sb);
 #pragma unroll
-          for (int kk = 0; kk < TC_BK / 8; ++kk) {
-            // advance 8 tf32 = 32 bytes along K inside the swizzle row
-            mma_tf32(dt, da + 2 * kk, db + 2 * kk, TC_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < 4; ++kk) {
+            // advance 8 tf32 or 16 halves = 32 bytes along K inside the swizzle row
+            if constexpr (F16)
+              mma_f16(dt, da + 2 * kk, db + 2 * kk, TC_IDESC_F16, (kt > 0 || kk > 0) ? 1u : 0u);
+            else
+              mma_tf32(dt, da + 2 * kk, db + 2 * kk, TC_IDESC, (kt > 0 || kk > 0) ? 1u : 0u);
           }
           mma_commit(empty0 + 8 * s);
         }
@@ -316,6 +337,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * TC_TMEM_COLS + c * 32), r);
         if (col0 >= N2 || row0 >= M) continue;            // warp-uniform
+        if constexpr (F16) {
+          // undo the operand scaling: row scale of this lane's row, column
+          // scale of each complex column (two floats)
+          const float rs = (row0 + lane < M) ? __ldg(inv_r + row0 + lane) : 0.f;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int cc = (col0 >> 1) + q;
+            const float sc = rs * ((2 * cc < N2) ? __ldg(inv_c + cc) : 0.f);
+            r[2 * q] = __float_as_uint(__uint_as_float(r[2 * q]) * sc);
+            r[2 * q + 1] = __float_as_uint(__uint_as_float(r[2 * q + 1]) * sc);
+          }
+        }
         if constexpr (EPI == 1) {
           epi_chunk_lsu(r, stage_gen, lane, Cp, ldcf, row0, col0, M, N2, accumulate);
           continue;
@@ -738,6 +771,84 @@ __global__ void k_expand_b(int K, int N, float2 alpha, const float2* __restrict_
   }
 }
 
+// ------------------------------------------------ FP16 operands with scaling
+// A power of two s with s * mx in [2^14, 2^15) (1 for mx = 0): FP16's largest
+// finite value is 65504, so every scaled entry is representable, and the
+// scaling is exact.
+__device__ __forceinline__ float pow2_scale(float mx) {
+  if (!(mx > 0.f) || !isfinite(mx)) return 1.f;
+  return ldexpf(1.f, 14 - ilogbf(mx));
+}
+
+// A16[i][0 .. K2p) = fp16(s_i A_r[i][k]) for k < 2K (A_r: the complex64 row read as
+// floats), zero beyond; inv_r[i] = 1 / s_i with s_i from the row's largest entry.
+// One warp per row.
+__global__ void k_a_to_f16(const float2* __restrict__ A, int64_t lda, int M, int K, __half* __restrict__ A16,
+                           int K2p, float* __restrict__ inv_r) {
+  const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= M) return;
+  const float* a = reinterpret_cast<const float*>(A + (int64_t)row * lda);
+  float mx = 0.f;
+  for (int k = lane; k < 2 * K; k += 32) mx = fmaxf(mx, fabsf(a[k]));
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const float sc = pow2_scale(mx);
+  if (lane == 0) inv_r[row] = 1.f / sc;
+  __half* dst = A16 + (int64_t)row * K2p;
+  for (int k = lane; k < K2p; k += 32) dst[k] = __float2half_rn(k < 2 * K ? a[k] * sc : 0.f);
+}
+
+// per complex column j of alpha * B (K x N, row stride ldb): the scale c_j from
+// the largest real or imaginary part; columns [bz0, bz1) are zero (scale 1)
+__global__ void k_b_colscale(const float2* __restrict__ B, int64_t ldb, int K, int N, float2 alpha, int bz0, int bz1,
+                             float* __restrict__ sc, float* __restrict__ inv_c) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  float mx = 0.f;
+  if (j < bz0 || j >= bz1) {
+    for (int l = 0; l < K; ++l) {
+      const float2 b = B[(int64_t)l * ldb + j];
+      const float vr = alpha.x * b.x - alpha.y * b.y, vi = alpha.x * b.y + alpha.y * b.x;
+      mx = fmaxf(mx, fmaxf(fabsf(vr), fabsf(vi)));
+    }
+  }
+  const float s = pow2_scale(mx);
+  sc[j] = s;
+  inv_c[j] = 1.f / s;
+}
+
+// B'[2N][K2p] in FP16 from c_j alpha B, the same real layout as k_expand_b
+__global__ void k_expand_b16(int K, int N, float2 alpha, const float2* __restrict__ B, int64_t ldb,
+                             __half* __restrict__ Bp, int K2p, int bz0, int bz1, const float* __restrict__ sc) {
+  __shared__ float2 tile[32][33];
+  const int l0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int l = l0 + r, j = j0 + tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (l < K && j < N && (j < bz0 || j >= bz1)) {
+      const float2 b = B[(int64_t)l * ldb + j];
+      const float s = sc[j];
+      v = make_float2((alpha.x * b.x - alpha.y * b.y) * s, (alpha.x * b.y + alpha.y * b.x) * s);
+    }
+    tile[r][tx] = v;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int j = j0 + r, l = l0 + tx;
+    if (j >= N || 2 * l >= K2p) continue;
+    const float2 v = tile[tx][r];
+    __half2* r0 = reinterpret_cast<__half2*>(Bp + (int64_t)(2 * j) * K2p) + l;
+    __half2* r1 = reinterpret_cast<__half2*>(Bp + (int64_t)(2 * j + 1) * K2p) + l;
+    if (l < K) {
+      *r0 = __floats2half2_rn(v.x, -v.y);
+      *r1 = __floats2half2_rn(v.y, v.x);
+    } else {
+      *r0 = __floats2half2_rn(0.f, 0.f);
+      *r1 = __floats2half2_rn(0.f, 0.f);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode(TcGemmCtx& c) {
   if (!c.encode_fn) {
@@ -755,12 +866,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode(TcGemmCtx& c) {
 
 static bool make_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, const void* ptr, uint64_t inner,
                      uint64_t rows, uint64_t row_bytes, uint32_t box_rows, bool swizzle = true,
-                     uint32_t box_inner = TC_BK) {
+                     uint32_t box_inner = TC_BK, bool f16 = false) {
   cuuint64_t dims[2] = {inner, rows};
   cuuint64_t strides[1] = {row_bytes};
   cuuint32_t box[2] = {box_inner, box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, es,
+  CUresult r = enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                   const_cast<void*>(ptr), dims, strides, box, es,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
@@ -775,10 +887,14 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     c.usable = (major == 10 && minor == 3) && get_encode(c) != nullptr &&
-               cudaFuncSetAttribute(k_tc_gemm<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
-               cudaFuncSetAttribute(k_tc_gemm<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
-               cudaFuncSetAttribute(k_tc_gemm<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
-               cudaFuncSetAttribute(k_tc_gemm<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<3, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(3)) == cudaSuccess &&
+               cudaFuncSetAttribute(k_tc_gemm<4, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_psmem(4)) == cudaSuccess &&
                cudaFuncSetAttribute(k_tc_gemm_pair<5, 4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(5, 4)) == cudaSuccess &&
                cudaFuncSetAttribute(k_tc_gemm_pair<6, 2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(6, 2)) == cudaSuccess &&
                cudaFuncSetAttribute(k_tc_gemm_pair<6, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tp_psmem(6, 2)) == cudaSuccess &&
@@ -797,6 +913,68 @@ bool tc_gemm_eligible(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, const void*
   return M >= 128 && N >= 64 && K >= 16 && M < (1 << 30) && 2 * N < (1 << 30) && 2 * K < (1 << 30);
 }
 
+// The product with FP16 operands: A converted row by row and B' column by
+// column into FP16 with power-of-two scales (k_a_to_f16, k_b_colscale,
+// k_expand_b16), kind::f16 MMAs with FP32 accumulation, the scales undone in
+// the epilogue.  FP16 keeps TF32's 10-bit significand and issues at twice the
+// TF32 rate with half the operand bytes per multiply-add.
+static mnpbem_status tc_gemm_f16(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
+                                 int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc,
+                                 cudaStream_t st, int64_t bz0, int64_t bz1) {
+  constexpr int BK = 64;
+  const int64_t K2 = 2 * K, N2 = 2 * N, K2p = round_up(K2, BK);
+  MNP_TRY(c.bexp.ensure(sizeof(__half) * N2 * K2p));
+  MNP_TRY(c.a16.ensure(sizeof(__half) * M * K2p));
+  MNP_TRY(c.scales.ensure(sizeof(float) * (M + 2 * N)));
+  MNP_TRY(c.err.ensure(sizeof(int)));
+  __half* Bp = c.bexp.as<__half>();
+  __half* A16 = c.a16.as<__half>();
+  float* inv_r = c.scales.as<float>();
+  float* sc = inv_r + M;
+  float* inv_c = sc + N;
+  {
+    ProfScope ps(PH_ELEMWISE, st, 0.0, 16.0 * K * N + 8.0 * M * K + 4.0 * M * K + 8.0 * N * K);
+    k_a_to_f16<<<(unsigned)cdiv_up(M, (int64_t)8), 256, 0, st>>>(A, lda, (int)M, (int)K, A16, (int)K2p, inv_r);
+    k_b_colscale<<<(unsigned)cdiv_up(N, (int64_t)256), 256, 0, st>>>(B, ldb, (int)K, (int)N, alpha, (int)bz0, (int)bz1,
+                                                                     sc, inv_c);
+    dim3 g((unsigned)cdiv_up(N, 32), (unsigned)cdiv_up(K2p / 2, 32));
+    k_expand_b16<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p, (int)bz0, (int)bz1, sc);
+    MNP_CHECK_LAUNCH();
+  }
+  auto enc = get_encode(c);
+  CUtensorMap ma, mb, mc, mp;
+  if (!make_map(enc, &ma, A16, (uint64_t)K2p, (uint64_t)M, (uint64_t)K2p * 2, TC_BM, true, BK, true) ||
+      !make_map(enc, &mb, Bp, (uint64_t)K2p, (uint64_t)N2, (uint64_t)K2p * 2, TC_BN, true, BK, true) ||
+      !make_map(enc, &mc, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, 32, true) ||
+      !make_map(enc, &mp, C, (uint64_t)N2, (uint64_t)M, (uint64_t)ldc * 8, TC_BM, false, TC_BN)) {
+    set_error("cuTensorMapEncodeTiled failed");
+    return MNPBEM_ERR_CUDA;
+  }
+  if (!c.err_cleared) {
+    MNP_CUDA(cudaMemsetAsync(c.err.ptr, 0, sizeof(int), st));
+    c.err_cleared = true;
+  }
+  const int64_t MT = cdiv_up(M, TC_BM), NT = cdiv_up(N2, TC_BN);
+  if (MT * NT >= (1ll << 31)) { set_error("tc_gemm_c64: too many tiles"); return MNPBEM_ERR_INVALID_ARG; }
+  MNP_TRY(c.ctr.ensure(sizeof(int)));
+  MNP_CUDA(cudaMemsetAsync(c.ctr.ptr, 0, sizeof(int), st));
+  const bool lsu = c.pair_epi == 1 || (N2 & 3) != 0;
+  float* Cf = reinterpret_cast<float*>(C);
+  const long long ldcf = 2ll * ldc;
+  const int acc = beta.x != 0.0f ? 1 : 0;
+  int ctas = c.num_sms > 0 ? c.num_sms : 148;
+  if (c.max_ctas > 0 && c.max_ctas < ctas) ctas = c.max_ctas;
+  ProfScope ps(M >= 128 && N >= 128 ? PH_GEMM_BIG : PH_GEMM_SMALL, st, 8.0 * M * N * K,
+               8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
+  const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, ctas);
+  auto kern = c.stages == 3 ? (lsu ? k_tc_gemm<3, 1, true> : k_tc_gemm<3, 0, true>)
+                            : (lsu ? k_tc_gemm<4, 1, true> : k_tc_gemm<4, 0, true>);
+  kern<<<grid, TC_THREADS, tc_psmem(c.stages == 3 ? 3 : 4), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2, (int)K2p,
+                                                                  acc, c.ctr.as<int>(), c.err.as<int>(), inv_r, inv_c);
+  MNP_CHECK_LAUNCH();
+  return MNPBEM_OK;
+}
+
 mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
                           int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc,
                           cudaStream_t st, int64_t bz0, int64_t bz1) {
@@ -805,6 +983,7 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base, beta not 0 or 1)");
     return MNPBEM_ERR_UNSUPPORTED;
   }
+  if (c.f16 && c.pair != 1) return tc_gemm_f16(c, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, bz0, bz1);
   const int64_t K2 = 2 * K, N2 = 2 * N;
   const int64_t K2p = round_up(K2, TC_BK);
   MNP_TRY(c.bexp.ensure(sizeof(float) * N2 * K2p));
@@ -864,9 +1043,11 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
       return MNPBEM_OK;
     }
     const unsigned grid = (unsigned)std::min<int64_t>(MT * NT, ctas);
-    auto kern = c.stages == 3 ? (lsu ? k_tc_gemm<3, 1> : k_tc_gemm<3, 0>) : (lsu ? k_tc_gemm<4, 1> : k_tc_gemm<4, 0>);
+    auto kern = c.stages == 3 ? (lsu ? k_tc_gemm<3, 1, false> : k_tc_gemm<3, 0, false>)
+                              : (lsu ? k_tc_gemm<4, 1, false> : k_tc_gemm<4, 0, false>);
     kern<<<grid, TC_THREADS, tc_psmem(c.stages == 3 ? 3 : 4), st>>>(ma, mb, mc, mp, Cf, ldcf, (int)M, (int)N2, (int)K2,
-                                                                    acc, c.ctr.as<int>(), c.err.as<int>());
+                                                                    acc, c.ctr.as<int>(), c.err.as<int>(), nullptr,
+                                                                    nullptr);
     MNP_CHECK_LAUNCH();
   }
   return MNPBEM_OK;
@@ -905,6 +1086,8 @@ __global__ void k_wait_selftest(int* err, unsigned long long limit_ns) {
 
 void tc_release(TcGemmCtx& c) {
   c.bexp.release();
+  c.a16.release();
+  c.scales.release();
   c.err.release();
   c.ctr.release();
 }

@@ -9,7 +9,9 @@ struct TcGemmCtx {
   bool usable = false;    // sm_103 device, driver entry point and kernel attributes available
   bool enabled = true;    // switched off after a device-side error
   bool err_cleared = false;
-  DevBuf bexp;            // expanded B operand [2N][2K] (real, K-major, tf32)
+  DevBuf bexp;            // expanded B operand [2N][2K] (real, K-major, tf32 or fp16)
+  DevBuf a16, scales;     // FP16 path: A operand [M][2K] in fp16, row / column scales
+  bool f16 = false;       // FP16 operands with power-of-two row / column scaling (kind::f16)
   DevBuf err;             // device error word of the bounded waits
   DevBuf ctr;             // tile counter of the persistent kernel (zeroed before each launch)
   int num_sms = 0;
