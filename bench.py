@@ -381,10 +381,11 @@ def run_ours(a, rank, world, dist, torch):
     d = prof["gemm_n3"]
     achieved = d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0
     traffic = TC_TRAFFIC.get(a.workload)
-    roof = {"kernel": "k_tc_gemm (tcgen05 kind::tf32, all tensor-core GEMM launches)", "bound": "tensor",
-            "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
-            "peak_source": src + " sustained dense bf16 (kernel timed inside seconds-long steps); TF32 issues "
-                                 "at half the bf16 rate: %.3f of that derived TF32 rate" % (2 * achieved / bf16_sus),
+    roof = {"kernel": "k_tc_gemm (tcgen05; kind::f16 on scaled FP16 operands for the rank-512/1024 updates, "
+                      "kind::tf32 for the 256-wide panel products; all tensor-core GEMM launches)",
+            "bound": "tensor", "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
+            "peak_source": src + " sustained dense bf16 (FP16 MMAs issue at the bf16 rate; the kernel is timed "
+                                 "inside seconds-long steps)",
             "traffic": traffic["bytes"] if traffic else None,
             "traffic_note": traffic["note"] if traffic else "no ncu capture of this configuration",
             "launches": d["launches"], "ms": d["ms"], "timing": timing,

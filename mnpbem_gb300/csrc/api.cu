@@ -743,6 +743,8 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
     tc[device].pair = (path == 2 || path == 3) ? 1 : 0;
     tc[device].pair_epi = path == 3 ? 1 : 0;
     tc[device].f16 = path == 4;
+    tc[device].f16_min_k = 1;
+    tc[device].f16_min_mn = 1;
     if (!tc_gemm_eligible(tc[device], M, N, K, dA.ptr, lda, dC.ptr, ldc, be)) {
       set_error("tensor-core GEMM not available for this device or shape");
       return MNPBEM_ERR_UNSUPPORTED;

@@ -797,37 +797,49 @@ __global__ void k_a_to_f16(const float2* __restrict__ A, int64_t lda, int M, int
   for (int k = lane; k < K2p; k += 32) dst[k] = __float2half_rn(k < 2 * K ? a[k] * sc : 0.f);
 }
 
-// per complex column j of alpha * B (K x N, row stride ldb): the scale c_j from
-// the largest real or imaginary part; columns [bz0, bz1) are zero (scale 1)
-__global__ void k_b_colscale(const float2* __restrict__ B, int64_t ldb, int K, int N, float2 alpha, int bz0, int bz1,
-                             float* __restrict__ sc, float* __restrict__ inv_c) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= N) return;
+// per complex column j of alpha * B (K x N, row stride ldb): the largest real
+// or imaginary part, as the bits of a non-negative float (colmax zeroed
+// beforehand); columns [bz0, bz1) stay zero.  CTA (32 x 8 threads) = 32
+// columns x 128 rows of B.
+__global__ void k_b_colmax(const float2* __restrict__ B, int64_t ldb, int K, int N, float2 alpha, int bz0, int bz1,
+                           unsigned* __restrict__ colmax) {
+  __shared__ float red[8][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j = blockIdx.x * 32 + tx, l0 = blockIdx.y * 128;
   float mx = 0.f;
-  if (j < bz0 || j >= bz1) {
-    for (int l = 0; l < K; ++l) {
+  if (j < N && (j < bz0 || j >= bz1)) {
+    for (int l = l0 + ty; l < min(K, l0 + 128); l += 8) {
       const float2 b = B[(int64_t)l * ldb + j];
       const float vr = alpha.x * b.x - alpha.y * b.y, vi = alpha.x * b.y + alpha.y * b.x;
       mx = fmaxf(mx, fmaxf(fabsf(vr), fabsf(vi)));
     }
   }
-  const float s = pow2_scale(mx);
-  sc[j] = s;
-  inv_c[j] = 1.f / s;
+  red[ty][tx] = mx;
+  __syncthreads();
+  if (ty == 0 && j < N) {
+    for (int r = 1; r < 8; ++r) mx = fmaxf(mx, red[r][tx]);
+    if (mx > 0.f) atomicMax(colmax + j, __float_as_uint(mx));
+  }
 }
 
-// B'[2N][K2p] in FP16 from c_j alpha B, the same real layout as k_expand_b
+// B'[2N][K2p] in FP16 from c_j alpha B (c_j from colmax), the same real layout
+// as k_expand_b; the CTAs of the first row of tiles write inv_c
 __global__ void k_expand_b16(int K, int N, float2 alpha, const float2* __restrict__ B, int64_t ldb,
-                             __half* __restrict__ Bp, int K2p, int bz0, int bz1, const float* __restrict__ sc) {
+                             __half* __restrict__ Bp, int K2p, int bz0, int bz1, const unsigned* __restrict__ colmax,
+                             float* __restrict__ inv_c) {
   __shared__ float2 tile[32][33];
   const int l0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+  {
+    const int j = j0 + tx;
+    if (blockIdx.y == 0 && ty == 0 && j < N) inv_c[j] = 1.f / pow2_scale(__uint_as_float(colmax[j]));
+  }
   for (int r = ty; r < 32; r += 8) {
     const int l = l0 + r, j = j0 + tx;
     float2 v = make_float2(0.f, 0.f);
     if (l < K && j < N && (j < bz0 || j >= bz1)) {
       const float2 b = B[(int64_t)l * ldb + j];
-      const float s = sc[j];
+      const float s = pow2_scale(__uint_as_float(colmax[j]));
       v = make_float2((alpha.x * b.x - alpha.y * b.y) * s, (alpha.x * b.y + alpha.y * b.x) * s);
     }
     tile[r][tx] = v;
@@ -930,15 +942,17 @@ static mnpbem_status tc_gemm_f16(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, 
   __half* Bp = c.bexp.as<__half>();
   __half* A16 = c.a16.as<__half>();
   float* inv_r = c.scales.as<float>();
-  float* sc = inv_r + M;
-  float* inv_c = sc + N;
+  unsigned* colmax = reinterpret_cast<unsigned*>(inv_r + M);
+  float* inv_c = inv_r + M + N;
   {
     ProfScope ps(PH_ELEMWISE, st, 0.0, 16.0 * K * N + 8.0 * M * K + 4.0 * M * K + 8.0 * N * K);
+    MNP_CUDA(cudaMemsetAsync(colmax, 0, sizeof(unsigned) * N, st));
     k_a_to_f16<<<(unsigned)cdiv_up(M, (int64_t)8), 256, 0, st>>>(A, lda, (int)M, (int)K, A16, (int)K2p, inv_r);
-    k_b_colscale<<<(unsigned)cdiv_up(N, (int64_t)256), 256, 0, st>>>(B, ldb, (int)K, (int)N, alpha, (int)bz0, (int)bz1,
-                                                                     sc, inv_c);
+    k_b_colmax<<<dim3((unsigned)cdiv_up(N, 32), (unsigned)cdiv_up(K, 128)), dim3(32, 8), 0, st>>>(
+        B, ldb, (int)K, (int)N, alpha, (int)bz0, (int)bz1, colmax);
     dim3 g((unsigned)cdiv_up(N, 32), (unsigned)cdiv_up(K2p / 2, 32));
-    k_expand_b16<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p, (int)bz0, (int)bz1, sc);
+    k_expand_b16<<<g, dim3(32, 8), 0, st>>>((int)K, (int)N, alpha, B, ldb, Bp, (int)K2p, (int)bz0, (int)bz1, colmax,
+                                            inv_c);
     MNP_CHECK_LAUNCH();
   }
   auto enc = get_encode(c);
@@ -983,7 +997,11 @@ mnpbem_status tc_gemm_c64(TcGemmCtx& c, int64_t M, int64_t N, int64_t K, float2 
     set_error("tc_gemm_c64: unsupported layout (odd leading dimension, misaligned base, beta not 0 or 1)");
     return MNPBEM_ERR_UNSUPPORTED;
   }
-  if (c.f16 && c.pair != 1) return tc_gemm_f16(c, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, bz0, bz1);
+  // FP16 for the rank-512 and wider updates, where the n^3 work is; the
+  // narrower panel products keep TF32 operands and skip the three conversion
+  // passes (their launches dominated them at 4000 faces)
+  if (c.f16 && c.pair != 1 && K >= c.f16_min_k && M >= c.f16_min_mn && N >= c.f16_min_mn)
+    return tc_gemm_f16(c, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, st, bz0, bz1);
   const int64_t K2 = 2 * K, N2 = 2 * N;
   const int64_t K2p = round_up(K2, TC_BK);
   MNP_TRY(c.bexp.ensure(sizeof(float) * N2 * K2p));

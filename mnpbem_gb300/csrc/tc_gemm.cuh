@@ -12,6 +12,8 @@ struct TcGemmCtx {
   DevBuf bexp;            // expanded B operand [2N][2K] (real, K-major, tf32 or fp16)
   DevBuf a16, scales;     // FP16 path: A operand [M][2K] in fp16, row / column scales
   bool f16 = false;       // FP16 operands with power-of-two row / column scaling (kind::f16)
+  int f16_min_k = 512;    // ... for products with K >= f16_min_k
+  int f16_min_mn = 512;   //     and M, N >= f16_min_mn
   DevBuf err;             // device error word of the bounded waits
   DevBuf ctr;             // tile counter of the persistent kernel (zeroed before each launch)
   int num_sms = 0;
