@@ -63,10 +63,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dimer24k", choices=["dimer24k", "sphere4000", "batch3", "iter24k"],
+    ap.add_argument("--workload", default="dimer24k",
+                    choices=["dimer24k", "sphere4000", "batch3", "iter24k", "gemm_rank1024"],
                     help="dimer24k: two 12000-face spheres, 32 wavelengths (the headline); sphere4000: one "
                          "4000-face sphere, 60 wavelengths; batch3: three particles of uneven size, 128 "
-                         "wavelengths, two polarisations; iter24k: the dimer through the iterative H-matrix solver")
+                         "wavelengths, two polarisations; iter24k: the dimer through the iterative H-matrix solver; "
+                         "gemm_rank1024: one rank-1024 trailing update of the factorisations (5888 x 5888 complex "
+                         "C, device-resident) on the TF32 and the scaled-FP16 tensor-core paths")
     ap.add_argument("--faces", type=int, default=0, help="faces of the workload (0: its own)")
     ap.add_argument("--batch", type=int, default=0, help="wavelengths per step per GPU (0: the workload's)")
     ap.add_argument("--lanes", type=int, default=0, help="wavelengths in flight at once (0: library default)")
@@ -323,12 +326,14 @@ def run_ours(a, rank, world, dist, torch):
     barrier()
     torch.cuda.synchronize()
     clocks.start()
+    torch.cuda.nvtx.range_push("timed")          # for launch lists of the timed steps (ncu --nvtx)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for s in range(a.steps):
         sweep.run(sw(a.warmup + s))
     e1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     barrier()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
@@ -571,6 +576,56 @@ def run_iter(a, torch):
             "hmat_build_ms": hb["ms"]}
 
 
+def run_gemm(a, torch):
+    """The building block of the factorisations on its own: C -= A B with
+    M = N = 5888 complex (C 277 MB, larger than L2) and K = 1024, the rank of
+    the 24 000-face dimer's trailing updates, through mnpbem_gemm_c64 on
+    device-resident operands: path 1 (TF32 operands) and path 4 (FP16 operands
+    scaled per row / column).  Each step is one product per path; CUDA events
+    on the default stream."""
+    from mnpbem_gb300 import _lib
+    lib = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    M = N = 5888
+    K = 1024
+    g = torch.Generator(device=dev).manual_seed(1)
+    A = torch.randn((M, K), dtype=torch.complex64, device=dev, generator=g)
+    B = torch.randn((K, N), dtype=torch.complex64, device=dev, generator=g)
+    C0 = torch.randn((M, N), dtype=torch.complex64, device=dev, generator=g)
+    al = np.array([-1.0, 0.0], dtype=np.float32)
+    be = np.array([1.0, 0.0], dtype=np.float32)
+    ref = (C0[:64].to(torch.complex128) - A[:64].to(torch.complex128) @ B.to(torch.complex128))
+    out = {}
+    flops = 8.0 * M * N * K
+    for path, name in ((1, "tf32"), (4, "fp16_scaled")):
+        C = C0.clone()
+        run = lambda: _lib.check(lib.mnpbem_gemm_c64(0, path, M, N, K, al.ctypes.data, A.data_ptr(), K,
+                                                     B.data_ptr(), N, be.ctypes.data, C.data_ptr(), N))
+        run()
+        torch.cuda.synchronize()
+        err = float((C[:64].to(torch.complex128) - ref).abs().max() / ref.abs().max())
+        for _ in range(max(0, a.warmup - 1)):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.steps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / a.steps
+        out[name] = {"ms": ms, "TFLOP/s": flops / (ms / 1e3) / 1e12, "rel_err_first_64_rows": err}
+    hbm, bf16, bf16_sus, src = peaks()
+    best = out["fp16_scaled"]["TFLOP/s"]
+    return {"metric": "TFLOP/s of one complex rank-1024 update (5888 x 5888 x 1024)", "value": best,
+            "unit": "TFLOP/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": out["fp16_scaled"]["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16 (scaled) / tf32 operands, f32 accumulation", "data": "synthetic",
+            "config": {"workload": "gemm_rank1024: C -= A B, M = N = 5888, K = 1024 complex64, device-resident",
+                       "l2": "C (277 MB) larger than the 129 MB L2"},
+            "paths": out, "frac_of_bf16_burst": best / bf16, "peak_source": src}
+
+
 def bemret_spectrum(bem, exc, eneis):
     """Direct (bemret) sweep on a bemretiter's handle (the parent class's
     spectrum runs mnpbem_solve)."""
@@ -743,7 +798,7 @@ def main():
     import torch
     if a.workload not in WORKLOADS:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        line = {"batch3": run_batch3, "iter24k": run_iter}[a.workload](a, torch)
+        line = {"batch3": run_batch3, "iter24k": run_iter, "gemm_rank1024": run_gemm}[a.workload](a, torch)
         if rank == 0:
             print(json.dumps(line))
         return

@@ -237,8 +237,11 @@ MNPBEM_API mnpbem_status mnpbem_profile_reset(mnpbem_geom* g);
 MNPBEM_API mnpbem_status mnpbem_profile_read(mnpbem_geom* g, int32_t phase, double* ms,
                                              double* flops, double* bytes, int64_t* launches);
 
-/* Complex64 GEMM C = alpha A B + beta C on host buffers (row-major, interleaved
- * complex, leading dimensions in elements): path 0 = CUDA-core kernel, path 1 =
+/* Complex64 GEMM C = alpha A B + beta C (row-major, interleaved complex,
+ * leading dimensions in elements) on host buffers, or, when A, B and C are all
+ * device pointers, on them directly and asynchronously on the default stream
+ * (the caller synchronises; an expired wait shows at the next host-buffer
+ * call): path 0 = CUDA-core kernel, path 1 =
  * tcgen05 tensor-core kernel (TF32 inputs, FP32 accumulation), path 2 = the
  * same on CTA pairs (cta_group::2, 256 x 256 tiles; M >= 256, else path 1)
  * with a TMA store / reduce-add epilogue, path 3 = CTA pairs with vector

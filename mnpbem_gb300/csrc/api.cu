@@ -728,16 +728,31 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
   MNP_CUDA(cudaSetDevice(device));
   static TcGemmCtx tc[64];
   if (device < 0 || device >= 64) { set_error("invalid device"); return MNPBEM_ERR_INVALID_ARG; }
-  cudaStream_t st;
-  MNP_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{st};
+  // A, B, C all in device memory: the product runs on them on the default
+  // stream, without copies; otherwise host arrays go through device buffers
+  auto on_device = [](const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  };
+  const bool dev = on_device(A) && on_device(B) && on_device(C);
+  cudaStream_t st = nullptr;
+  if (!dev) MNP_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  struct StreamGuard { cudaStream_t s; ~StreamGuard() { if (s) cudaStreamDestroy(s); } } sg{st};
   DevBuf dA, dB, dC;
-  MNP_TRY(dA.ensure(sizeof(float2) * M * lda));
-  MNP_TRY(dB.ensure(sizeof(float2) * K * ldb));
-  MNP_TRY(dC.ensure(sizeof(float2) * M * ldc));
-  MNP_CUDA(cudaMemcpyAsync(dA.ptr, A, sizeof(float2) * M * lda, cudaMemcpyHostToDevice, st));
-  MNP_CUDA(cudaMemcpyAsync(dB.ptr, B, sizeof(float2) * K * ldb, cudaMemcpyHostToDevice, st));
-  MNP_CUDA(cudaMemcpyAsync(dC.ptr, C, sizeof(float2) * M * ldc, cudaMemcpyHostToDevice, st));
+  const float2 *pA = reinterpret_cast<const float2*>(A), *pB = reinterpret_cast<const float2*>(B);
+  float2* pC = reinterpret_cast<float2*>(C);
+  if (!dev) {
+    MNP_TRY(dA.ensure(sizeof(float2) * M * lda));
+    MNP_TRY(dB.ensure(sizeof(float2) * K * ldb));
+    MNP_TRY(dC.ensure(sizeof(float2) * M * ldc));
+    MNP_CUDA(cudaMemcpyAsync(dA.ptr, A, sizeof(float2) * M * lda, cudaMemcpyHostToDevice, st));
+    MNP_CUDA(cudaMemcpyAsync(dB.ptr, B, sizeof(float2) * K * ldb, cudaMemcpyHostToDevice, st));
+    MNP_CUDA(cudaMemcpyAsync(dC.ptr, C, sizeof(float2) * M * ldc, cudaMemcpyHostToDevice, st));
+    pA = dA.as<float2>();
+    pB = dB.as<float2>();
+    pC = dC.as<float2>();
+  }
   const float2 al = make_float2(alpha[0], alpha[1]), be = make_float2(beta[0], beta[1]);
   if (path >= 1) {
     tc[device].pair = (path == 2 || path == 3) ? 1 : 0;
@@ -745,19 +760,19 @@ mnpbem_status mnpbem_gemm_c64(int32_t device, int32_t path, int64_t M, int64_t N
     tc[device].f16 = path == 4;
     tc[device].f16_min_k = 1;
     tc[device].f16_min_mn = 1;
-    if (!tc_gemm_eligible(tc[device], M, N, K, dA.ptr, lda, dC.ptr, ldc, be)) {
+    if (!tc_gemm_eligible(tc[device], M, N, K, pA, lda, pC, ldc, be)) {
       set_error("tensor-core GEMM not available for this device or shape");
       return MNPBEM_ERR_UNSUPPORTED;
     }
-    MNP_TRY(tc_gemm_c64(tc[device], M, N, K, al, dA.as<float2>(), lda, dB.as<float2>(), ldb, be,
-                        dC.as<float2>(), ldc, st));
-    MNP_TRY(tc_check_error(tc[device], st));
+    MNP_TRY(tc_gemm_c64(tc[device], M, N, K, al, pA, lda, pB, ldb, be, pC, ldc, st));
+    if (!dev) MNP_TRY(tc_check_error(tc[device], st));
   } else {
-    MNP_TRY(gemm_simt<float>(M, N, K, al, dA.as<float2>(), lda, dB.as<float2>(), ldb, be,
-                             dC.as<float2>(), ldc, st));
+    MNP_TRY(gemm_simt<float>(M, N, K, al, pA, lda, pB, ldb, be, pC, ldc, st));
   }
-  MNP_CUDA(cudaMemcpyAsync(C, dC.ptr, sizeof(float2) * M * ldc, cudaMemcpyDeviceToHost, st));
-  MNP_CUDA(cudaStreamSynchronize(st));
+  if (!dev) {
+    MNP_CUDA(cudaMemcpyAsync(C, dC.ptr, sizeof(float2) * M * ldc, cudaMemcpyDeviceToHost, st));
+    MNP_CUDA(cudaStreamSynchronize(st));
+  }
   return MNPBEM_OK;
 }
 

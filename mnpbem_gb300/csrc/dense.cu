@@ -869,8 +869,8 @@ static_assert(PB_PAN % PB_TPR == 0 || PB_TPR % PB_PAN == 0, "panel / thread layo
 static_assert(PB_RPC % PB_PAN == 0, "a panel lies inside one CTA");
 
 __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
-    k_block_inv_cluster(const float2* __restrict__ A, int64_t lda, int w, float2* __restrict__ X,
-                        int64_t ldx, int* status) {
+    k_block_inv_cluster(const float2* A, int64_t lda, int w, float2* X, int64_t ldx, int* status,
+                        float2* __restrict__ Xr) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ float2 pb_smem[];
@@ -1011,25 +1011,34 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
     }
     record_cond(status, am, xm);
   }
+  // X may be the input block itself: every CTA read its rows at the start
   if (grow < w) {
 #pragma unroll
     for (int j = 0; j < PB_CPT; ++j) {
       const int c = ph + PB_TPR * j;
-      if (c < w) X[(int64_t)grow * ldx + c] = a[j];
+      if (c < w) {
+        X[(int64_t)grow * ldx + c] = a[j];
+        if (Xr) {   // copy rounded to TF32 (nearest): the A operand of tensor-core products
+          uint32_t x, y;
+          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(x) : "f"(a[j].x));
+          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(a[j].y));
+          Xr[(int64_t)grow * w + c] = make_float2(__uint_as_float(x), __uint_as_float(y));
+        }
+      }
     }
   }
   cluster.sync();
 }
 
 static mnpbem_status launch_block_inv_cluster(const float2* A, int64_t lda, int w, float2* X, int64_t ldx,
-                                              int* status, cudaStream_t st) {
+                                              int* status, cudaStream_t st, float2* Xr = nullptr) {
   static bool attr_set = false;
   if (!attr_set) {
     MNP_CUDA(cudaFuncSetAttribute(k_block_inv_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, PB_SMEM));
     attr_set = true;
   }
   ProfScope ps(PH_BLOCKINV, st, 8.0 * w * w * w, 0.0);
-  k_block_inv_cluster<<<PB_CL, PB_THREADS, PB_SMEM, st>>>(A, lda, w, X, ldx, status);
+  k_block_inv_cluster<<<PB_CL, PB_THREADS, PB_SMEM, st>>>(A, lda, w, X, ldx, status, Xr);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
 }
@@ -1244,20 +1253,23 @@ static void copy_panel(const cplx<R>* src, int64_t lds, int64_t rows, int cols, 
   k_copy_panel<R><<<(unsigned)cdiv_up(cnt, (int64_t)256), 256, 0, st>>>(src, lds, rows, cols, dst, ldd, rna ? 1 : 0);
 }
 
-// X_k <- inv(A_kk): 64-wide blocks with partial pivoting on one CTA, 256-wide
-// complex64 blocks on a CTA cluster
+// A_kk <- inv(A_kk) in place, with a copy in X (ld bw): 64-wide blocks with
+// partial pivoting on one CTA, 256-wide complex64 blocks on a CTA cluster,
+// whose copy in X is rounded to TF32 (nearest) for the tensor-core products
+// (the tensor cores would otherwise truncate it)
 template <typename R>
-static mnpbem_status block_inverse(const cplx<R>* Akk, int64_t lda, int bw, cplx<R>* X, int* status,
-                                   cudaStream_t st) {
+static mnpbem_status block_inverse(cplx<R>* Akk, int64_t lda, int bw, cplx<R>* X, int* status, cudaStream_t st) {
   if (bw <= 64) {
     ProfScope ps(PH_BLOCKINV, st, 8.0 * bw * bw * bw, 0.0);
     k_block_inv<R><<<1, 256, 0, st>>>(Akk, lda, bw, X, bw, status);
     MNP_CHECK_LAUNCH();
+    MNP_CUDA(cudaMemcpy2DAsync(Akk, sizeof(cplx<R>) * lda, X, sizeof(cplx<R>) * bw, sizeof(cplx<R>) * bw, bw,
+                               cudaMemcpyDeviceToDevice, st));
     return MNPBEM_OK;
   }
   if (sizeof(R) == 4 && bw <= PB_W)
-    return launch_block_inv_cluster(reinterpret_cast<const float2*>(Akk), lda, bw, reinterpret_cast<float2*>(X), bw,
-                                    status, st);
+    return launch_block_inv_cluster(reinterpret_cast<const float2*>(Akk), lda, bw, reinterpret_cast<float2*>(Akk), lda,
+                                    status, st, reinterpret_cast<float2*>(X));
   set_error("block LDU: diagonal blocks of %d rows are not supported in this precision", bw);
   return MNPBEM_ERR_UNSUPPORTED;
 }
@@ -1316,7 +1328,6 @@ mnpbem_status ldu_factor(cplx<R>* A, int64_t n, int64_t lda, LDUWork<R>& w, int*
             MNP_TRY(gemm(e - kb, n - e, bs, mone, Cs, B, A + ks * lda + e, lda, one, A + kb * lda + e, lda, st, ctx));
         }
       }
-      MNP_CUDA(cudaMemcpy2DAsync(A + ks * lda + ks, cs * lda, X, cs * bs, cs * bs, bs, cudaMemcpyDeviceToDevice, st));
     }
     // trailing update of rank Bw
     if (e < n) MNP_TRY(gemm(n - e, n - e, Bw, mone, Cc + (e - k0) * B, B, A + k0 * lda + e, lda, one, A + e * lda + e,
@@ -1415,14 +1426,15 @@ __global__ void __launch_bounds__(256) k_ldu_diag(const cplx<R>* __restrict__ F,
 // takes block k (k = s forward, nblk - 1 - s backward): every CTA stages x_k
 // (b x N) in shared memory and subtracts F[i, k block] x_k from its rows i of
 // the trailing (forward) or leading (backward) part; then the CTAs meet at a
-// grid barrier before the next block is read.  Rows go to the CTAs in groups
-// of TRSV_GRP by their absolute index (group g to CTA g mod G); a warp takes a
-// row at a time (lanes along the row, coalesced) and reduces with shuffles.
+// grid barrier before the next block is read.  One CTA of 16 warps per SM;
+// rows go to the CTAs in groups (16 warps x 2 rows, by absolute index: group g
+// to CTA g mod G); a warp takes two rows at a time (lanes along the rows,
+// coalesced, both rows' loads in flight together) and reduces with shuffles.
 // X is read with ld.global.cg (L2), since other CTAs updated it.  The grid
 // barrier is a monotonic arrival counter (zeroed before the launch) with a
 // bounded wait; on expiry the error word of the streamed thin products is
 // set, an abort flag releases the other CTAs and every CTA returns.
-constexpr int TRSV_THREADS = 256, TRSV_GRP = 8;
+constexpr int TRSV_THREADS = 512, TRSV_WARPS = TRSV_THREADS / 32;
 
 __device__ __forceinline__ bool coop_barrier(unsigned* ctr, unsigned target, int* abortf) {
   __shared__ int ok_s;
@@ -1448,15 +1460,63 @@ __device__ __forceinline__ bool coop_barrier(unsigned* ctr, unsigned target, int
   return ok_s != 0;
 }
 
+// one warp subtracts F[i, k block] x_k from RW rows i0, i0 + 1, ... at once
+// (independent accumulators keep the RW rows' loads in flight together)
+template <typename R, int NB, int RW>
+__device__ __forceinline__ void trsv_rows(const cplx<R>* __restrict__ F, int64_t ldf, int64_t k0, int bs,
+                                          const cplx<R>* xs, cplx<R>* X, int64_t ldx, int N, int64_t i0,
+                                          int64_t r0, int64_t r1, int lane) {
+  using Cx = cplx<R>;
+  Cx acc[RW][NB];
+#pragma unroll
+  for (int q = 0; q < RW; ++q)
+#pragma unroll
+    for (int c = 0; c < NB; ++c) acc[q][c] = mk<R>(0, 0);
+  const Cx* frow[RW];
+  bool act[RW];
+#pragma unroll
+  for (int q = 0; q < RW; ++q) {
+    act[q] = i0 + q >= r0 && i0 + q < r1;
+    frow[q] = F + (act[q] ? i0 + q : r0) * ldf + k0;
+  }
+#pragma unroll 2
+  for (int l = lane; l < bs; l += 32) {
+    Cx f[RW];
+#pragma unroll
+    for (int q = 0; q < RW; ++q) f[q] = __ldg(frow[q] + l);
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      const Cx xv = xs[l * NB + c];
+#pragma unroll
+      for (int q = 0; q < RW; ++q) cfma(acc[q][c], f[q], xv);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RW; ++q)
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      Cx v = acc[q][c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (act[q] && lane == c && c < N) {
+        Cx* xp = X + (i0 + q) * ldx + c;
+        *xp = csub(__ldcg(xp), v);
+      }
+    }
+}
+
 template <typename R, int NB, bool LOWER>
 __global__ void __launch_bounds__(TRSV_THREADS) k_trsv_unit(const cplx<R>* __restrict__ F, int64_t ldf, int64_t n,
                                                             int b, cplx<R>* X, int64_t ldx, int N, unsigned* bar) {
   using Cx = cplx<R>;
+  constexpr int RW = NB <= 8 ? 2 : 1;          // rows per warp at a time
+  constexpr int GRP = TRSV_WARPS * RW;         // rows per group: one pass of the CTA's warps
   extern __shared__ unsigned char trsv_smem[];
   Cx* xs = reinterpret_cast<Cx*>(trsv_smem);   // [b][NB], columns N .. NB - 1 zero
   const int nblk = (int)((n + b - 1) / b);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int NW = TRSV_THREADS / 32;
   const int64_t G = gridDim.x;
   int* abortf = reinterpret_cast<int*>(bar + 1);
   for (int s = 0; s + 1 < nblk; ++s) {
@@ -1469,37 +1529,11 @@ __global__ void __launch_bounds__(TRSV_THREADS) k_trsv_unit(const cplx<R>* __res
     }
     __syncthreads();
     const int64_t r0 = LOWER ? k0 + bs : 0, r1 = LOWER ? n : k0;
-    // groups of rows by absolute index: the first group this CTA owns at or after r0
-    int64_t g = r0 / TRSV_GRP;
+    // groups of GRP rows by absolute index, group g to CTA g mod G
+    int64_t g = r0 / GRP;
     g += (blockIdx.x - g % G + G) % G;
-    for (; g * TRSV_GRP < r1; g += G) {
-      for (int rr = warp; rr < TRSV_GRP; rr += NW) {
-        const int64_t i = g * TRSV_GRP + rr;
-        if (i < r0 || i >= r1) continue;
-        const Cx* frow = F + i * ldf + k0;
-        Cx acc[NB];
-#pragma unroll
-        for (int c = 0; c < NB; ++c) acc[c] = mk<R>(0, 0);
-#pragma unroll 4
-        for (int l = lane; l < bs; l += 32) {
-          const Cx f = __ldg(frow + l);
-#pragma unroll
-          for (int c = 0; c < NB; ++c) cfma(acc[c], f, xs[l * NB + c]);
-        }
-#pragma unroll
-        for (int c = 0; c < NB; ++c) {
-          Cx v = acc[c];
-          for (int o = 16; o; o >>= 1) {
-            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-          }
-          if (lane == c && c < N) {
-            Cx* xp = X + i * ldx + c;
-            *xp = csub(__ldcg(xp), v);
-          }
-        }
-      }
-    }
+    for (; g * GRP < r1; g += G)
+      trsv_rows<R, NB, RW>(F, ldf, k0, bs, xs, X, ldx, N, g * GRP + warp * RW, r0, r1, lane);
     if (!coop_barrier(bar, (unsigned)((s + 1) * G), abortf)) return;
   }
 }
@@ -1529,7 +1563,7 @@ static mnpbem_status launch_trsv(const cplx<R>* F, int64_t n, int64_t ldf, int b
       cudaGetLastError();
       per_sm = 1;
     }
-    per_sm = std::max(1, std::min(per_sm, 2));
+    per_sm = std::max(1, std::min(per_sm, 1));
   }
   const unsigned grid = (unsigned)(per_sm * trsv_sms());
   MNP_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
