@@ -921,29 +921,39 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
         for (int j = 0; j < PB_CPT; ++j) P[(lr - lp0) * PB_W + ph + PB_TPR * j] = a[j];
       }
       __syncthreads();
-      // 16 x 16 Gauss-Jordan of the pivot block, one entry per thread
-      const int bi = t / PB_PAN, bj = t % PB_PAN;
-      const bool act = t < PB_PAN * PB_PAN;
-      if (act) Xs[bi * PB_PAN + bj] = P[bi * PB_W + p0 + bj];
-      __syncthreads();
-      for (int k = 0; k < PB_PAN; ++k) {
-        float2 v = make_float2(0.f, 0.f);
-        if (act) {
+      // 16 x 16 Gauss-Jordan of the pivot block by warp 0 alone (8 entries per
+      // lane, warp barriers between the pivots instead of block barriers)
+      constexpr int PE = PB_PAN * PB_PAN / 32;
+      if (t < 32) {
+#pragma unroll
+        for (int q = 0; q < PE; ++q) {
+          const int e = t + 32 * q;
+          Xs[e] = P[(e / PB_PAN) * PB_W + p0 + e % PB_PAN];
+        }
+        __syncwarp();
+        for (int k = 0; k < PB_PAN; ++k) {
           const float2 piv = Xs[k * PB_PAN + k];
           const float n2 = piv.x * piv.x + piv.y * piv.y;
           if (t == 0 && !(n2 > 1e-30f && n2 < 1e30f)) atomicOr(status, 1);
           const float rn = 1.f / n2;
           const float2 inv = make_float2(piv.x * rn, -piv.y * rn);
-          const float2 aik = Xs[bi * PB_PAN + k], akj = Xs[k * PB_PAN + bj], aij = Xs[bi * PB_PAN + bj];
-          if (bi == k && bj == k) v = inv;
-          else if (bi == k) v = cmul(akj, inv);
-          else if (bj == k) v = make_float2(-(aik.x * inv.x - aik.y * inv.y), -(aik.x * inv.y + aik.y * inv.x));
-          else v = csub(aij, cmul(aik, cmul(akj, inv)));
+          float2 v[PE];
+#pragma unroll
+          for (int q = 0; q < PE; ++q) {
+            const int e = t + 32 * q, bi = e / PB_PAN, bj = e % PB_PAN;
+            const float2 aik = Xs[bi * PB_PAN + k], akj = Xs[k * PB_PAN + bj], aij = Xs[e];
+            if (bi == k && bj == k) v[q] = inv;
+            else if (bi == k) v[q] = cmul(akj, inv);
+            else if (bj == k) v[q] = make_float2(-(aik.x * inv.x - aik.y * inv.y), -(aik.x * inv.y + aik.y * inv.x));
+            else v[q] = csub(aij, cmul(aik, cmul(akj, inv)));
+          }
+          __syncwarp();
+#pragma unroll
+          for (int q = 0; q < PE; ++q) Xs[t + 32 * q] = v[q];
+          __syncwarp();
         }
-        __syncthreads();
-        if (act) Xs[bi * PB_PAN + bj] = v;
-        __syncthreads();
       }
+      __syncthreads();
       // R = X * P with the pivot columns replaced by X
       for (int e = t; e < PB_PAN * PB_W; e += PB_THREADS) {
         const int i = e / PB_W, c = e % PB_W;
