@@ -85,7 +85,7 @@ def parse():
                          "extinction error <= 1e-6 against FP64; the library default is 1e-10)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 GPU wavelength at full size")
-    ap.add_argument("--skip-c2", action="store_true", help="skip the 4000-face sphere side run")
+    ap.add_argument("--skip-c2", action="store_true", help="skip the side runs of configurations 2, 3 and 4")
     ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (0: the workload's)")
     ap.add_argument("--profile-steps", type=int, default=3, help="steps of the profiled repeat")
     ap.add_argument("--iter-faces", type=int, default=24000,
@@ -508,7 +508,7 @@ def run_batch3(a, torch):
     v64 = 3 * lam.size / t64
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / a.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64(tf32)+f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64(fp16/tf32)+f64", "data": "synthetic",
             "config": {"workload": "batch of 3 particles (sphere d=30 nm 1000 faces, capped rod 10x40 nm 2500 "
                                    "quadrilaterals, rounded cube 40 nm / 4 nm rounding 2904 faces), Drude metal in "
                                    "eps=1.77, x and y polarisation along +z, 128 wavelengths 400-900 nm per particle",
@@ -752,6 +752,29 @@ def run_c2(torch, device):
             "refinement_iterations": sweep.iters.tolist(), "refine_tol": b.refine_tol}
 
 
+def run_c4(torch, device):
+    """Configuration 4: adjoint gradients of the extinction on the capped rod
+    (10 x 40 nm, 2016 triangles, polarisation along the axis, 650 nm) with
+    respect to every vertex coordinate and eps, FP64 and mixed precision; host
+    wall clock around each call after a warm-up call."""
+    import mnpbem_gb300 as m
+    from mnpbem_gb300 import shapes
+    v, f = shapes.trirod(10.0, 40.0, (25, 7, 32), triangles=True)
+    cp = m.comparticle([m.epsconst(1.77), drude()], [m.particle(v, f)], [[2, 1]], 1)
+    bem = m.bemsolver(cp, m.bemoptions(precision="fp64", device=device, lanes=1))
+    exc = m.planewave([[0, 0, 1.0]], [[1.0, 0, 0]])
+    out = {"faces": int(cp.n), "vertices": int(v.shape[0]), "enei": 650.0}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        bem.cross_section_gradient(exc, 650.0, 0, "ext", prec)
+        r, dt = _timed(lambda: bem.cross_section_gradient(exc, 650.0, 0, "ext", prec), torch)
+        res[prec] = r
+        out[prec] = {"seconds": dt, "ext": r[0]}
+    out["grad_rel_diff_mixed_vs_fp64"] = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1])) /
+                                               np.max(np.abs(res["fp64"][1])))
+    return out
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return None
@@ -824,8 +847,16 @@ def main():
     if rank == 0 and not a.skip_cpu:
         cpu, ores = cpu_baseline(a)
         parity = parity_at_sample(a, torch, ores)
+    c3 = c4 = None
     if rank == 0 and not a.skip_c2 and a.workload != "sphere4000":
         c2 = run_c2(torch, device)
+        import argparse as _ap
+        b3 = run_batch3(_ap.Namespace(lanes=0, refine_tol=a.refine_tol, warmup=1, steps=1), torch)
+        c3 = {k: b3[k] for k in ("value", "unit", "ms_per_step", "speedup_vs_fp64_gpu", "ext_rel_err_mixed_vs_fp64",
+                                 "refinement_iterations_max")}
+        c3["workload"] = b3["config"]["workload"]
+        c3["timing"] = b3["config"]["timing"]
+        c4 = run_c4(torch, device)
     if dist is not None:
         dist.barrier()
     if rank == 0:
@@ -833,7 +864,7 @@ def main():
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": r["ms"] / a.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "c64(tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
+                "dtype": "c64(fp16/tf32)+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": workload_desc(a, batch=a.batch), "faces": n, "wavelengths_per_step": a.batch,
                            "precision": a.precision, "lanes": a.lanes or tuned_lanes(n, a.precision),
                            "refine_tol": a.refine_tol if a.precision == "mixed" else None,
@@ -841,7 +872,7 @@ def main():
                                  "far larger than the 129 MB L2" % ((5 * 8 + 4 * 16) * n * n / 1e9)},
                 "e2e": r["e2e"], "gpu_launches": r["gpu_launches"], "roofline": r["roofline"],
                 "cpu_baseline": cpu, "clocks": r["clocks"], "fp64_gpu": fp64, "parity_vs_oracle": parity,
-                "c2_sphere4000": c2}
+                "c2_sphere4000": c2, "c3_batch3": c3, "c4_gradient": c4}
         if fp64:
             line["speedup_vs_fp64_gpu"] = r["value"] / fp64["value"]
         line.update(r["extra"])

@@ -357,6 +357,72 @@ __global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_hi(int64_t M, int64
   }
 }
 
+// the same product with 16-byte loads of A (two k per lane and load): even K
+// and lda, 16-byte aligned A; the FP32 residual products of the refinement at
+// large n, where the 8-byte loads above leave HBM half used
+template <int N>
+__global__ void __launch_bounds__(32 * DS_WARPS) k_gemm_thin_hi4(int64_t M, int64_t K, const float2* __restrict__ Ahi,
+                                                               int64_t lda, const float2* __restrict__ Bh, int64_t ldb,
+                                                               double2* __restrict__ C, int64_t ldc) {
+  __shared__ float2 red[DS_WARPS][DS_TR][N];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row0 = (int64_t)blockIdx.x * DS_TR;
+  const int64_t KP = K >> 1;
+  const int64_t kw = (KP + DS_WARPS - 1) / DS_WARPS;
+  const int64_t pbeg = warp * kw, pend = min(KP, pbeg + kw);
+  const float4* arow[DS_TR];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r) arow[r] = reinterpret_cast<const float4*>(Ahi + min(row0 + r, M - 1) * lda);
+  float2 acc[DS_TR][N];
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) acc[r][c] = make_float2(0.f, 0.f);
+#pragma unroll 2
+  for (int64_t kp = pbeg + lane; kp < pend; kp += 32) {
+    const int64_t k = 2 * kp;
+    float2 x0[N], x1[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      x0[c] = __ldg(Bh + k * ldb + c);
+      x1[c] = __ldg(Bh + (k + 1) * ldb + c);
+    }
+    float4 a[DS_TR];
+#pragma unroll
+    for (int r = 0; r < DS_TR; ++r) a[r] = __ldg(arow[r] + kp);
+#pragma unroll
+    for (int r = 0; r < DS_TR; ++r) {
+      const float2 a0 = make_float2(a[r].x, a[r].y), a1 = make_float2(a[r].z, a[r].w);
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        cfma(acc[r][c], a0, x0[c]);
+        cfma(acc[r][c], a1, x1[c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < DS_TR; ++r)
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      float2 v = acc[r][c];
+      for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) red[warp][r][c] = v;
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < DS_TR * N; t += blockDim.x) {
+    const int r = t / N, c = t % N;
+    const int64_t row = row0 + r;
+    if (row >= M) continue;
+    float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int w = 0; w < DS_WARPS; ++w) v = cadd(v, red[w][r][c]);
+    C[row * ldc + c] = make_double2(v.x, v.y);
+  }
+}
+
 // ------------------------------------------- streamed thin GEMM (bulk copies)
 // C[M x N] = A[M x K] * B[K x N], N <= 4, for a complex64 A far larger than
 // L2 (the chain products and FP32 residuals of the refinement read a whole
@@ -612,9 +678,11 @@ static mnpbem_status gemm_thin_ds_block(int64_t M, int64_t N, int64_t K, const f
     ProfScope ps(PH_GEMM_SMALL, st, 8.0 * M * N * K, 8.0 * M * K + 8.0 * K * N + 16.0 * M * N);
     if (thin_stream_ok(M, N, K, Ahi, lda))
       return launch_thin_stream<1>(M, N, K, Ahi, lda, Bh, N, make_float2(1.f, 0.f), make_float2(0.f, 0.f), C, ldc, st);
+    const bool v4 = !(K & 1) && !(lda & 1) && !(reinterpret_cast<uintptr_t>(Ahi) & 15);
 #define HI_CASE(NN)                                                                                \
   case NN:                                                                                         \
-    k_gemm_thin_hi<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, lda, Bh, N, C, ldc);            \
+    if (v4) k_gemm_thin_hi4<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, lda, Bh, N, C, ldc);    \
+    else k_gemm_thin_hi<NN><<<nblk, 32 * DS_WARPS, 0, st>>>(M, K, Ahi, lda, Bh, N, C, ldc);        \
     break;
     switch (N) {
       HI_CASE(1) HI_CASE(2) HI_CASE(3) HI_CASE(4) HI_CASE(5) HI_CASE(6) HI_CASE(7) HI_CASE(8)
@@ -864,7 +932,7 @@ __global__ void __launch_bounds__(256) k_block_inv(const cplx<R>* __restrict__ A
 // Rows and columns beyond w are identity and stay identity.
 constexpr int PB_W = 256, PB_CL = 8, PB_RPC = PB_W / PB_CL, PB_THREADS = 512;
 constexpr int PB_TPR = PB_THREADS / PB_RPC, PB_CPT = PB_W / PB_TPR, PB_PAN = 16;
-constexpr int PB_SMEM = (3 * PB_PAN * PB_W + 2 * PB_RPC * PB_PAN + PB_PAN * PB_PAN) * (int)sizeof(float2);
+constexpr int PB_SMEM = (3 * PB_PAN * PB_W + 2 * PB_RPC * PB_PAN + 2 * PB_PAN * PB_PAN) * (int)sizeof(float2);
 static_assert(PB_PAN % PB_TPR == 0 || PB_TPR % PB_PAN == 0, "panel / thread layout");
 static_assert(PB_RPC % PB_PAN == 0, "a panel lies inside one CTA");
 
@@ -877,7 +945,7 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
   float2* Rb = pb_smem;                              // [2][PAN][W]  new panel rows
   float2* P = Rb + 2 * PB_PAN * PB_W;                // [PAN][W]     owner: raw panel rows
   float2* Cb = P + PB_PAN * PB_W;                    // [2][RPC][PAN] own panel-column entries
-  float2* Xs = Cb + 2 * PB_RPC * PB_PAN;             // [PAN][PAN] pivot block (owner)
+  float2* Xs = Cb + 2 * PB_RPC * PB_PAN;             // [2][PAN][PAN] pivot block, two copies (owner)
   const int rank = (int)cluster.block_rank();
   const int t = threadIdx.x, lr = t / PB_TPR, ph = t % PB_TPR;
   const int grow = rank * PB_RPC + lr;
@@ -921,39 +989,34 @@ __global__ void __cluster_dims__(PB_CL, 1, 1) __launch_bounds__(PB_THREADS, 1)
         for (int j = 0; j < PB_CPT; ++j) P[(lr - lp0) * PB_W + ph + PB_TPR * j] = a[j];
       }
       __syncthreads();
-      // 16 x 16 Gauss-Jordan of the pivot block by warp 0 alone (8 entries per
-      // lane, warp barriers between the pivots instead of block barriers)
-      constexpr int PE = PB_PAN * PB_PAN / 32;
-      if (t < 32) {
-#pragma unroll
-        for (int q = 0; q < PE; ++q) {
-          const int e = t + 32 * q;
-          Xs[e] = P[(e / PB_PAN) * PB_W + p0 + e % PB_PAN];
-        }
-        __syncwarp();
-        for (int k = 0; k < PB_PAN; ++k) {
-          const float2 piv = Xs[k * PB_PAN + k];
+      // 16 x 16 Gauss-Jordan of the pivot block, one entry per thread; the
+      // pivot steps alternate between two copies of the block, so that one
+      // block barrier per step suffices
+      const int bi = t / PB_PAN, bj = t % PB_PAN;
+      const bool act = t < PB_PAN * PB_PAN;
+      if (act) Xs[bi * PB_PAN + bj] = P[bi * PB_W + p0 + bj];
+      __syncthreads();
+      for (int k = 0; k < PB_PAN; ++k) {
+        const float2* Xc = Xs + (k & 1) * PB_PAN * PB_PAN;
+        float2* Xn = Xs + ((k & 1) ^ 1) * PB_PAN * PB_PAN;
+        if (act) {
+          const float2 piv = Xc[k * PB_PAN + k];
           const float n2 = piv.x * piv.x + piv.y * piv.y;
           if (t == 0 && !(n2 > 1e-30f && n2 < 1e30f)) atomicOr(status, 1);
           const float rn = 1.f / n2;
           const float2 inv = make_float2(piv.x * rn, -piv.y * rn);
-          float2 v[PE];
-#pragma unroll
-          for (int q = 0; q < PE; ++q) {
-            const int e = t + 32 * q, bi = e / PB_PAN, bj = e % PB_PAN;
-            const float2 aik = Xs[bi * PB_PAN + k], akj = Xs[k * PB_PAN + bj], aij = Xs[e];
-            if (bi == k && bj == k) v[q] = inv;
-            else if (bi == k) v[q] = cmul(akj, inv);
-            else if (bj == k) v[q] = make_float2(-(aik.x * inv.x - aik.y * inv.y), -(aik.x * inv.y + aik.y * inv.x));
-            else v[q] = csub(aij, cmul(aik, cmul(akj, inv)));
-          }
-          __syncwarp();
-#pragma unroll
-          for (int q = 0; q < PE; ++q) Xs[t + 32 * q] = v[q];
-          __syncwarp();
+          const float2 aik = Xc[bi * PB_PAN + k], akj = Xc[k * PB_PAN + bj], aij = Xc[bi * PB_PAN + bj];
+          float2 v;
+          if (bi == k && bj == k) v = inv;
+          else if (bi == k) v = cmul(akj, inv);
+          else if (bj == k) v = make_float2(-(aik.x * inv.x - aik.y * inv.y), -(aik.x * inv.y + aik.y * inv.x));
+          else v = csub(aij, cmul(aik, cmul(akj, inv)));
+          Xn[bi * PB_PAN + bj] = v;
         }
+        __syncthreads();
       }
-      __syncthreads();
+      // PB_PAN is even: the result is back in the first copy
+      static_assert(PB_PAN % 2 == 0, "the pivot block's Gauss-Jordan ends in its first copy");
       // R = X * P with the pivot columns replaced by X
       for (int e = t; e < PB_PAN * PB_W; e += PB_THREADS) {
         const int i = e / PB_W, c = e % PB_W;
