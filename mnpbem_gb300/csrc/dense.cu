@@ -1508,9 +1508,6 @@ __global__ void __launch_bounds__(256) k_ldu_diag(const cplx<R>* __restrict__ F,
 // bounded wait; on expiry the error word of the streamed thin products is
 // set, an abort flag releases the other CTAs and every CTA returns.
 constexpr int TRSV_THREADS = 512, TRSV_WARPS = TRSV_THREADS / 32;
-// row entries per lane held in registers: blocks of up to 256 (complex64) or
-// 64 (complex128, the FP64 path's block) rows
-template <typename R> constexpr int TRSV_UNR = sizeof(R) == 4 ? 8 : 2;
 
 __device__ __forceinline__ bool coop_barrier(unsigned* ctr, unsigned target, int* abortf) {
   __shared__ int ok_s;
@@ -1555,25 +1552,19 @@ __device__ __forceinline__ void trsv_rows(const cplx<R>* __restrict__ F, int64_t
     act[q] = i0 + q >= r0 && i0 + q < r1;
     frow[q] = F + (act[q] ? i0 + q : r0) * ldf + k0;
   }
-  // all of a row's entries for this lane (bs <= 32 UNR) are loaded before any
-  // is used, so that UNR x RW loads per lane are in flight together
-  constexpr int UNR = TRSV_UNR<R>;
-  Cx f[UNR][RW];
+  // two of a lane's entries per row in flight at a time: the full unroll (a
+  // row's entries all loaded first) raises the register count to 96-104 and
+  // keeps these CTAs from sharing SMs with the other lanes' kernels
+#pragma unroll 2
+  for (int l = lane; l < bs; l += 32) {
+    Cx f[RW];
 #pragma unroll
-  for (int it = 0; it < UNR; ++it) {
-    const int l = lane + 32 * it;
-#pragma unroll
-    for (int q = 0; q < RW; ++q) f[it][q] = l < bs ? __ldg(frow[q] + l) : mk<R>(0, 0);
-  }
-#pragma unroll
-  for (int it = 0; it < UNR; ++it) {
-    const int l = lane + 32 * it;
-    if (l >= bs) break;
+    for (int q = 0; q < RW; ++q) f[q] = __ldg(frow[q] + l);
 #pragma unroll
     for (int c = 0; c < NB; ++c) {
       const Cx xv = xs[l * NB + c];
 #pragma unroll
-      for (int q = 0; q < RW; ++q) cfma(acc[q][c], f[it][q], xv);
+      for (int q = 0; q < RW; ++q) cfma(acc[q][c], f[q], xv);
     }
   }
 #pragma unroll
@@ -1682,7 +1673,7 @@ mnpbem_status ldu_solve(const cplx<R>* F, int64_t n, int64_t ldf, int b, cplx<R>
   if (n <= 0 || N <= 0) return MNPBEM_OK;
   const Cx one = mk<R>(1, 0), zero = mk<R>(0, 0), mone = mk<R>(-1, 0);
   const int64_t nblk = cdiv_up(n, (int64_t)b);
-  const bool sweep = bar && N <= 16 && b <= 32 * TRSV_UNR<R>;
+  const bool sweep = bar && N <= 16 && b <= 256;
   // forward: L unit lower
   if (sweep) {
     if (nblk > 1) MNP_TRY((trsv_sweep<R, true>(F, n, ldf, b, X, ldx, (int)N, bar, st)));
