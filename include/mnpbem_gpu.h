@@ -470,6 +470,56 @@ MNPBEM_API mnpbem_status mnpbem_hmat_full(mnpbem_geom* g, const mnpbem_cluster_t
                                           const mnpbem_iter_options* op, double enei, const double* eps_media,
                                           int32_t nmed, int32_t which, double* out, int32_t* ranks);
 
+/* ---------------------------------------------------------------------------
+ * H-matrix arithmetic (LU, triangular solves, inversion, addition with ACA
+ * truncation), the operations behind bemretiter's 'hmat' preconditioner
+ * (BEM/@bemretiter/private/initprecond.m).  Each call replaces one MEX
+ * function of the reference and takes the same data: a cluster tree, the full
+ * blocks and the low-rank factors (Greenfun/hmatrices/@hmatrix val / lhs /
+ * rhs), htol and kmax (hopts of mex/hlib/hoptions.h).
+ *   vals   full blocks in tree->full order, each rows x cols column-major
+ *          complex (interleaved re / im), concatenated
+ *   ranks  [nlow] ranks of the low-rank blocks (tree->low order)
+ *   lhs    low-rank blocks' left factors, rows x rank column-major, concatenated
+ *   rhs    right factors, cols x rank column-major (block = lhs rhs^T)
+ * Rows and columns are cluster positions (tree->cind).  Leaves hold at most
+ * 1024 positions.  The arithmetic runs in FP64 on the GPU, on one stream per
+ * device; results are new handles (free with mnpbem_hm_free).  A zero pivot
+ * in a leaf's LU or inverse returns MNPBEM_ERR_SINGULAR.                    */
+typedef struct mnpbem_hm_s mnpbem_hm;
+
+MNPBEM_API mnpbem_status mnpbem_hm_create(int32_t device, const mnpbem_cluster_tree* tree, double htol, int32_t kmax,
+                                          const double* vals, const int32_t* ranks, const double* lhs,
+                                          const double* rhs, mnpbem_hm** out);
+/* options of later operations on h (BEM/@bemretiter/private/compress.m)  */
+MNPBEM_API mnpbem_status mnpbem_hm_set_options(mnpbem_hm* h, double htol, int32_t kmax);
+/* L U of a (mex/hmatlu.cpp; mex/hlib/lu.h:180-198): L lower with its
+ * diagonal, U unit upper, both in the returned blocks                        */
+MNPBEM_API mnpbem_status mnpbem_hm_lu(const mnpbem_hm* a, mnpbem_hm** out);
+/* X with X (L U) = b, lu from mnpbem_hm_lu (mex/hmatrsolve.cpp): key 'N'
+ * both factors ('U' then 'L'), 'U' or 'L' one of them; options of b         */
+MNPBEM_API mnpbem_status mnpbem_hm_rsolve(const mnpbem_hm* b, const mnpbem_hm* lu, char key, mnpbem_hm** out);
+/* inverse of a (mex/hmatinv.cpp; mex/hlib/hmatrix.h inv)                    */
+MNPBEM_API mnpbem_status mnpbem_hm_inv(const mnpbem_hm* a, mnpbem_hm** out);
+/* a + sign b, sign 1 or -1 (mex/hmatadd.cpp; @hmatrix/plus.m, minus.m)     */
+MNPBEM_API mnpbem_status mnpbem_hm_add(const mnpbem_hm* a, const mnpbem_hm* b, double sign, mnpbem_hm** out);
+/* diag(d) a (side 'L') or a diag(d) (side 'R'), d [n] complex in cluster
+ * order (@hmatrix/private/mtimes1.m)                                        */
+MNPBEM_API mnpbem_status mnpbem_hm_scale(const mnpbem_hm* a, const double* d, char side, mnpbem_hm** out);
+/* (L U) x = b in place, x [N][n] complex (column-major n x N, cluster order),
+ * key 'N' (L then U), 'L' or 'U' (mex/hmatsolve.cpp)                        */
+MNPBEM_API mnpbem_status mnpbem_hm_solve(const mnpbem_hm* lu, char key, double* x, int32_t N);
+/* y = a x, x and y column-major n x N complex in cluster order (hmatmul1)   */
+MNPBEM_API mnpbem_status mnpbem_hm_mul(const mnpbem_hm* a, const double* x, double* y, int32_t N);
+/* a expanded to out, n x n column-major complex in cluster order (hmatfull) */
+MNPBEM_API mnpbem_status mnpbem_hm_full(const mnpbem_hm* a, double* out);
+/* sizes of mnpbem_hm_export's arrays in complex entries                     */
+MNPBEM_API mnpbem_status mnpbem_hm_sizes(const mnpbem_hm* a, int64_t* nvals, int64_t* nlhs, int64_t* nrhs);
+/* blocks of a in mnpbem_hm_create's layout (any pointer may be NULL)        */
+MNPBEM_API mnpbem_status mnpbem_hm_export(const mnpbem_hm* a, double* vals, int32_t* ranks, double* lhs,
+                                          double* rhs);
+MNPBEM_API void mnpbem_hm_free(mnpbem_hm* h);
+
 /* Self test of the bounded device-side waits that every pipelined kernel of
  * the library uses (mbarrier waits with a wall-clock limit): one CTA waits,
  * with a limit of limit_us microseconds (1 .. 1e6), on a barrier that nothing

@@ -149,6 +149,27 @@ SIGNATURES = {
     "mnpbem_geom_set_option": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int32]),
     "mnpbem_geom_stat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p]),
     "mnpbem_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
+    # H-matrix arithmetic (handles are void*)
+    "mnpbem_hm_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(ClusterTree), ctypes.c_double, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32]),
+    "mnpbem_hm_lu": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_rsolve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_inv": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                     ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_scale": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char, ctypes.c_void_p, ctypes.c_int32]),
+    "mnpbem_hm_mul": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "mnpbem_hm_full": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mnpbem_hm_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64)]),
+    "mnpbem_hm_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "mnpbem_hm_free": (None, [ctypes.c_void_p]),
     "mnpbem_last_error": (ctypes.c_char_p, []),
     "mnpbem_version": (ctypes.c_char_p, []),
 }

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmnpbem_gpu.so")
 SOURCES = ["geometry.cu", "assemble.cu", "dense.cu", "bem.cu", "tc_gemm.cu", "noalloc.cu", "adjoint.cu", "field.cu", "hmat.cu",
-           "api.cu"]
+           "hlu.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]

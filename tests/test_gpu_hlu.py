@@ -1,0 +1,151 @@
+"""GPU H-matrix arithmetic (LU, right solve, inverse, addition, scaling,
+vector solve) against the NumPy restatement of mex/hlib (oracle/hlu_ref.py).
+
+Both sides start from the same H-matrices: the full blocks and ACA factors of
+the oracle's G1, H1 (and G2, H2) on a cluster tree of a 796-face sphere whose
+vertices are jittered (no symmetric ties in the ACA pivot searches).  Every
+truncation is an ACA of the same products, so the factors agree to rounding;
+the bound 1e-8 (relative, Frobenius) leaves room for it.
+"""
+import numpy as np
+import pytest
+
+from oracle import hlu_ref as HL
+from oracle import hmatrix_ref as HR
+from oracle import mnpbem_ref as R
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def prob():
+    from mnpbem_gb300 import shapes
+    from mnpbem_gb300.hmatrix import treearrays
+    t = shapes.tables()
+    q = R.QuadFace((t["rule18_x"], t["rule18_y"], t["rule18_w"]))
+    v, f = shapes.trisphere(400, 20.0)
+    rng = np.random.default_rng(1)
+    v = v * (1 + 0.02 * rng.standard_normal((v.shape[0], 1)))
+    cp = R.ComParticle([R.EpsConst(1.77), R.drude_eps()], [R.Particle(v, f, q)], [[2, 1]], [True])
+    bem = R.BemRet(cp)
+    bem.initmat(600.0)
+    ct = HR.ClusterTree(cp.pos, np.zeros(cp.n, dtype=int), 32)
+    full, low = ct.admissibility()
+    son = np.where(ct.son < 0, -1, ct.son)
+    T = HL.Tree(son, ct.cind, full, low)
+    ta = treearrays(son, ct.cind, ct.perm, full, low)
+    P = ct.perm
+    mats = {}
+    for name, M in (("G1", bem.G1), ("H1", bem.H1), ("G2", bem.G2), ("H2", bem.H2)):
+        Mc = M[np.ix_(P, P)]
+        vals = [Mc[T.rng(r), T.rng(c)] for r, c in full]
+        ls, rs = [], []
+        for r, c in low:
+            L, Rr = HL.aca_full(Mc[T.rng(r), T.rng(c)], 1e-12, 100)
+            ls.append(L)
+            rs.append(Rr)
+        mats[name] = (vals, ls, rs)
+    return {"cp": cp, "bem": bem, "T": T, "ta": ta, "full": full, "low": low, "mats": mats, "perm": P}
+
+
+def gpu(prob, name, htol, kmax):
+    from mnpbem_gb300.hmatrix import hmatrix_gpu
+    vals, ls, rs = prob["mats"][name]
+    return hmatrix_gpu(prob["ta"], vals, ls, rs, htol=htol, kmax=kmax)
+
+
+def ora(prob, name):
+    vals, ls, rs = prob["mats"][name]
+    return HL.from_blocks(prob["T"], prob["full"], prob["low"], vals, ls, rs)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def assert_blocks_match(h, ref, arith):
+    """the GPU blocks against the oracle's: expanded matrices and ranks"""
+    got = h.full()
+    want = arith.full(ref)
+    assert rel(got, want) < TOL, rel(got, want)
+    _, lhs, _ = h.export()
+    t = h.tree
+    for b, (r, c) in enumerate(t.low):
+        S = ref[(int(r), int(c))]
+        assert S.flag == HL.FLAG_RK
+        assert lhs[b].shape[1] == S.lhs.shape[1], (b, lhs[b].shape, S.lhs.shape)
+
+
+@pytest.mark.parametrize("htol,kmax", [(1e-12, 100), (1e-6, 4)])
+def test_lu_matches_oracle(prob, htol, kmax):
+    a = HL.HArith(prob["T"], htol, kmax)
+    ref = a.lu(ora(prob, "G1"))
+    lu = gpu(prob, "G1", htol, kmax).lu()
+    assert_blocks_match(lu, ref, a)
+    if kmax == 100:
+        F = lu.full()
+        L, U = np.tril(F), np.triu(F, 1) + np.eye(F.shape[0])
+        G1c = a.full(ora(prob, "G1"))
+        assert rel(L @ U, G1c) < 1e-10
+
+
+@pytest.mark.parametrize("htol,kmax", [(1e-12, 100), (1e-6, 4)])
+def test_rsolve_matches_oracle(prob, htol, kmax):
+    a = HL.HArith(prob["T"], htol, kmax)
+    lu_ref = a.lu(ora(prob, "G1"))
+    ref = a.rsolve_lu(ora(prob, "H1"), lu_ref)
+    lu = gpu(prob, "G1", htol, kmax).lu()
+    X = gpu(prob, "H1", htol, kmax).rsolve(lu)
+    assert_blocks_match(X, ref, a)
+
+
+def test_inverse_matches_oracle(prob):
+    a = HL.HArith(prob["T"], 1e-6, 4)
+    ref = a.inv(ora(prob, "G2"))
+    got = gpu(prob, "G2", 1e-6, 4).inv()
+    assert_blocks_match(got, ref, a)
+
+
+def test_add_scale_mul_solve_match_oracle(prob):
+    a = HL.HArith(prob["T"], 1e-6, 4)
+    n = prob["T"].n
+    rng = np.random.default_rng(5)
+    d = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    g1, h1 = gpu(prob, "G1", 1e-6, 4), gpu(prob, "H1", 1e-6, 4)
+    G1, H1 = ora(prob, "G1"), ora(prob, "H1")
+    assert_blocks_match(g1 - h1, a.add(G1, a.uminus(H1, 0, 0)), a)
+    assert_blocks_match(g1 + h1, a.add(G1, H1), a)
+    assert_blocks_match(g1.scale(d, "L"), a.scale(G1, d, "L"), a)
+    assert_blocks_match(g1.scale(d, "R"), a.scale(G1, d, "R"), a)
+    x = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+    assert rel(g1.mul(x), a.matvec(G1, x)) < 1e-12
+    lu_ref = a.lu(G1)
+    got = g1.lu().solve(x)
+    assert rel(got, a.solve(lu_ref, x)) < TOL
+
+
+def test_preconditioner_sequence_matches_oracle(prob):
+    """initprecond.m ('hmat') through the ABI, then mfun.m's solves"""
+    bem, cp, P = prob["bem"], prob["cp"], prob["perm"]
+    e1, e2 = cp.eps_faces(600.0, 0), cp.eps_faces(600.0, 1)
+    mats = [ora(prob, q) for q in ("G1", "H1", "G2", "H2")]
+    pc = HL.HmatPrecond(prob["T"], P, *mats, bem.k, e1, e2, bem.nvec, htol=1e-6, kmax=4)
+    g = {q: gpu(prob, q, 1e-6, 4) for q in ("G1", "H1", "G2", "H2")}
+    G1i, G2i = g["G1"].lu(), g["G2"].lu()
+    S1 = g["H1"].rsolve(G1i)
+    S2 = g["H2"].rsolve(G2i)
+    Di = (S1 - S2).inv()
+    nv = bem.nvec[P]
+    F = None
+    for c in range(3):
+        t = Di.scale(nv[:, c], "L").scale(nv[:, c], "R")
+        F = t if F is None else F + t
+    deps = (e1 - e2)[P]
+    S = S1.scale(e1[P], "L") - S2.scale(e2[P], "L")
+    S = S + F.scale(bem.k ** 2 * deps, "L").scale(deps, "R")
+    Si = S.lu()
+    a = pc.h
+    for got, want in ((G1i, pc.G1i), (S1, pc.Sigma1), (Di, pc.Deltai), (Si, pc.Sigmai)):
+        assert rel(got.full(), a.full(want)) < TOL
