@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--skip-c2", action="store_true", help="skip the side runs of configurations 2, 3 and 4")
     ap.add_argument("--cpu-faces", type=int, default=0, help="faces of the CPU sample (0: the workload's)")
     ap.add_argument("--profile-steps", type=int, default=3, help="steps of the profiled repeat")
+    ap.add_argument("--iter-precond", choices=("full", "hmat"), default="full",
+                    help="preconditioner of --workload iter24k: the dense inverses ('full') or H-matrix LU ('hmat')")
     ap.add_argument("--iter-faces", type=int, default=24000,
                     help="iter24k: total faces of the dimer (smaller sizes for profiling runs)")
     a = ap.parse_args()
@@ -525,7 +527,8 @@ def run_iter(a, torch):
     """Iterative solver (bemretiter) on the 2 nm-gap dimer (--iter-faces,
     default 24000 faces): H-matrices of G1, H1, G2, H2 (leaves of at most 200
     faces, htol 1e-6, kmax 100), GMRES (tol 1e-6) preconditioned by the
-    complex64 tensor-core inverses.  Timed: a sweep of 8 wavelengths 600-740 nm
+    complex64 tensor-core inverses (--iter-precond full) or by H-matrix LU
+    factors (hmat: no dense matrix).  Timed: a sweep of 8 wavelengths 600-740 nm
     that builds the preconditioner at its first wavelength and keeps it while
     GMRES needs at most 30 steps (reuse_precond), after a warm-up sweep of two
     wavelengths; then a profiled repeat at 600 nm (preconditioner rebuilt) for
@@ -541,7 +544,8 @@ def run_iter(a, torch):
                        [[2, 1], [3, 1]], 1, 2)
     bem = m.bemsolver(cp, m.bemoptions(precision="mixed", device=dev, lanes=1,
                                        iter=m.bemiter_options(cleaf=200, htol=1e-6, kmax=[4, 100],
-                                                              reuse_precond=True, refresh_steps=30)))
+                                                              precond=a.iter_precond, reuse_precond=True,
+                                                              refresh_steps=30)))
     exc = m.planewave([1, 0, 0], [0, 0, 1])
     bem.spectrum(exc, [650.0, 660.0])
     eneis = np.linspace(600.0, 740.0, 8)
@@ -556,15 +560,18 @@ def run_iter(a, torch):
     direct = bemret_spectrum(bem, exc, [600.0, 740.0])
     err = [abs(res["ext"][0, 0] - direct["ext"][0, 0]) / abs(direct["ext"][0, 0]),
            abs(res["ext"][-1, 0] - direct["ext"][1, 0]) / abs(direct["ext"][1, 0])]
-    hbm, _, src = peaks()
+    hbm, _, _, src = peaks()
     mv, hb = prof["hmat_matvec"], prof["hmat_build"]
     gbs = mv["bytes"] / (mv["ms"] * 1e-3) / 1e9 if mv["ms"] > 0 else None
     return {"metric": METRIC, "value": eneis.size / dt, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64-class H-matrix operator (double-single) + c64(tf32) preconditioner", "data": "synthetic",
+            "dtype": "f64-class H-matrix operator (double-single) + " + (
+                "c64(tf32) dense preconditioner" if a.iter_precond == "full" else
+                "f64 H-matrix LU preconditioner (hmat, kmax 4)"), "data": "synthetic",
             "config": {"workload": "iterative solver (bemretiter, H-matrices + GMRES) on the dimer of two d=50 nm "
                                    "spheres, 2 nm gap, 2 x %d faces, x-pol along +z, 8 wavelengths 600-740 nm" % nf,
                        "faces": 2 * nf, "cleaf": 200, "htol": 1e-6, "kmax": 100, "gmres_tol": 1e-6,
+                       "precond": a.iter_precond,
                        "reuse_precond": True, "refresh_steps": 30,
                        "timing": "host wall clock around bemretiter.spectrum (public API, one mnpbem_solve_iter "
                                  "per wavelength, charges and ext/sca to host)"},

@@ -413,11 +413,15 @@ typedef struct mnpbem_cluster_tree {
  * brackets).  solver: 0 GMRES [0], 1 CGS, 2 BiCGStab (the preconditioner
  * applied to the search directions; relres then is ||b - A x|| / ||b||);
  * precond: 0 none, 1 'full' [1] (the dense inverses of bemret in the
- * solve's precision: FP64, or complex64 on the tensor cores for MIXED);
+ * solve's precision: FP64, or complex64 on the tensor cores for MIXED),
+ * 2 'hmat' (initprecond.m / mfun.m with H-matrices: LU of G1, G2 and Sigma,
+ * Sigma1 and Deltai as H-matrices, FP64, low-rank blocks truncated by ACA
+ * with htol_precond and kmax_precond, as compress.m sets them: max(op.htol),
+ * min(op.kmax); no dense n x n matrix is formed);
  * restart 0 = no restarts (one cycle of up to maxit steps); at most 4096
  * steps per cycle.
  * reuse_precond 1 (not in the reference, which rebuilds the preconditioner
- * at every wavelength): keep the 'full' preconditioner of an earlier
+ * at every wavelength): keep the preconditioner ('full' or 'hmat') of an earlier
  * iterative solve on this handle (same precision) for this wavelength; it
  * changes the number of GMRES steps, not the solution (tol).  It is rebuilt
  * when the previous solve needed more than refresh_steps steps
@@ -432,6 +436,8 @@ typedef struct mnpbem_iter_options {
   int32_t kmax;      /* [100] largest rank of a low-rank block (<= 512) */
   int32_t reuse_precond;  /* [0] */
   int32_t refresh_steps;  /* [0] */
+  int32_t kmax_precond;   /* [4] (0: default) rank cap of the 'hmat' preconditioner */
+  double htol_precond;    /* [htol] (0: htol) ACA tolerance of the 'hmat' preconditioner */
 } mnpbem_iter_options;
 
 /* Statistics of one iterative solve. */

@@ -65,7 +65,8 @@ class ClusterTree(ctypes.Structure):
 class IterOptions(ctypes.Structure):
     _fields_ = [("solver", ctypes.c_int32), ("tol", ctypes.c_double), ("maxit", ctypes.c_int32),
                 ("restart", ctypes.c_int32), ("precond", ctypes.c_int32), ("htol", ctypes.c_double),
-                ("kmax", ctypes.c_int32), ("reuse_precond", ctypes.c_int32), ("refresh_steps", ctypes.c_int32)]
+                ("kmax", ctypes.c_int32), ("reuse_precond", ctypes.c_int32), ("refresh_steps", ctypes.c_int32),
+                ("kmax_precond", ctypes.c_int32), ("htol_precond", ctypes.c_double)]
 
 
 class IterInfo(ctypes.Structure):

@@ -763,16 +763,17 @@ class bemretiter(bemret):
     compressed by adaptive cross approximation (tolerance ``htol``, rank at
     most ``max(kmax)``).  ``sig = bem.mldivide(exc(p, enei))`` runs GMRES on
     the operator of afun.m with H-matrix products, preconditioned by the dense
-    inverses of bemret (``precond='full'``, in the solver's precision) or not
-    at all (``precond=None``).  After a solve ``bem.info`` holds flag, iter,
+    inverses of bemret (``precond='full'``, in the solver's precision), by
+    H-matrix LU factors (``precond='hmat'``: initprecond.m with the H-matrix
+    arithmetic of hlib on the GPU, FP64, truncation with ``max(htol)`` and
+    ``min(kmax)``) or not at all (``precond=None``).  After a solve ``bem.info`` holds flag, iter,
     relres, true_relres, rank_max, rank_mean, compression and precond_enei.
     ``reuse_precond=True`` (not in the reference) keeps the preconditioner of
     an earlier wavelength (rebuilt when a solve needed more than
     ``refresh_steps`` GMRES steps): a sweep then pays the dense inversion
     once instead of at every wavelength, with the same solutions to ``tol``.
 
-    Solvers 'gmres', 'cgs' and 'bicgstab' (@bemiter/solve.m); the 'hmat'
-    preconditioner (H-matrix LU of hmatlu / hmatsolve) is not built.
+    Solvers 'gmres', 'cgs' and 'bicgstab' (@bemiter/solve.m).
     """
 
     def __init__(self, p, op=None):
@@ -784,8 +785,8 @@ class bemretiter(bemret):
                 it[k] = op[k]
         if it["solver"] not in ("gmres", "cgs", "bicgstab"):
             raise ValueError("solver must be 'gmres', 'cgs' or 'bicgstab'")
-        if it["precond"] not in ("full", None, ""):
-            raise NotImplementedError("precond must be 'full' or None (the 'hmat' preconditioner is not built)")
+        if it["precond"] not in ("full", "hmat", None, ""):
+            raise ValueError("precond must be 'full', 'hmat' or None")
         super().__init__(p, op)
         from .hmatrix import hpartition
         self.iter_op = it
@@ -801,9 +802,11 @@ class bemretiter(bemret):
         o.tol = float(it["tol"])
         o.maxit = int(it["maxit"])
         o.restart = int(it["restart"] or 0)
-        o.precond = 1 if it["precond"] == "full" else 0
+        o.precond = {"full": 1, "hmat": 2}.get(it["precond"], 0)
         o.htol = float(np.min(it["htol"]))
         o.kmax = int(np.max(it["kmax"]))
+        o.kmax_precond = int(np.min(it["kmax"]))
+        o.htol_precond = float(np.max(it["htol"]))
         o.reuse_precond = int(bool(it["reuse_precond"]))
         o.refresh_steps = int(it["refresh_steps"] or 0)
         return o

@@ -31,6 +31,7 @@
 #include "dense.cuh"
 #include "geometry.cuh"
 #include "field.cuh"
+#include "hlu.cuh"
 #include "hmat.cuh"
 #include "profile.cuh"
 #include "tc_gemm.cuh"
@@ -137,6 +138,10 @@ struct Lane {
   double pc_enei = 0.0;
   int pc_last_steps = 0;
   const void* pc_mat0 = nullptr;
+  // the 'hmat' preconditioner (H-matrix LU factors, FP64) and a signature of
+  // the cluster tree it was built on
+  std::shared_ptr<hl::HPrecond> hpc;
+  uint64_t hpc_sig = 0;
 };
 
 struct mnpbem_geom {
@@ -2391,6 +2396,8 @@ struct HmatHost {
   HmatDev d;
   LeafAsm la;
   std::vector<int4> lblk;   // host copy of the low-rank blocks
+  std::vector<int4> fblk;   // host copy of the full blocks
+  std::vector<int64_t> foff, aoff, boff;   // host copies of the value / factor offsets
   std::vector<int> ranks;   // [4][nlow] ACA ranks of the current wavelength
   double mv_bytes = 0.0;    // algorithmic bytes of one product of the four matrices
 };
@@ -2557,20 +2564,83 @@ mnpbem_status hmat_setup(mnpbem_geom* G, const mnpbem_cluster_tree* t, int kmax,
   H.d.usz = usz; H.d.tsz = tsz;
   H.la.nfull = nf; H.la.nleaf = nleaf; H.la.nvals = nvals;
   H.lblk = lblk;
+  H.fblk = fblk;
+  H.foff = foff;
+  H.aoff = aoff;
+  H.boff = boff;
   MNP_CUDA(cudaStreamSynchronize(st));
   return MNPBEM_OK;
 }
 
+// FP64 values and factors of the four H-matrices as H-arithmetic blocks
+// (column-major copies on the H stream, made before hmat_split overwrites the
+// right factors); ranks already on the host
+__global__ void k_rm_to_cm(const double2* src, int m, int n, double2* dst) {
+  const int64_t cnt = (int64_t)m * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % m), j = (int)(e / m);
+    dst[e] = src[(int64_t)i * n + j];
+  }
+}
+
+mnpbem_status hmat_capture(Lane& L, HmatHost& H, hl::Ctx& c, hl::HM out[4]) {
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  for (auto& e : ev) MNP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  struct EvFree {
+    cudaEvent_t* e;
+    ~EvFree() { for (int i = 0; i < 2; ++i) if (e[i]) cudaEventDestroy(e[i]); }
+  } ef{ev};
+  MNP_CUDA(cudaEventRecord(ev[0], L.st));
+  MNP_CUDA(cudaStreamWaitEvent(c.st, ev[0], 0));
+  const hl::Tree& T = *c.t;
+  for (int q = 0; q < 4; ++q) {
+    out[q].clear();
+    for (size_t b = 0; b < T.full.size(); ++b) {
+      const int4 fb = H.fblk[b];
+      hl::Sub S;
+      S.row = T.full[b].first; S.col = T.full[b].second; S.flag = hl::FLAG_FULL;
+      MNP_TRY(hl::alloc(c, fb.y, fb.w, S.mat));
+      const int64_t cnt = (int64_t)fb.y * fb.w;
+      k_rm_to_cm<<<(unsigned)std::min<int64_t>(cdiv_up(cnt, 256), 4096), 256, 0, c.st>>>(H.d.val[q] + H.foff[b], fb.y,
+                                                                                        fb.w, S.mat.ptr());
+      MNP_CHECK_LAUNCH();
+      out[q][T.full[b]] = std::move(S);
+    }
+    for (size_t b = 0; b < T.low.size(); ++b) {
+      const int4 lb = H.lblk[b];
+      const int k = H.ranks[(size_t)q * H.d.nlow + b];
+      hl::Sub S;
+      S.row = T.low[b].first; S.col = T.low[b].second; S.flag = hl::FLAG_RK;
+      MNP_TRY(hl::alloc(c, lb.y, k, S.lhs));
+      MNP_TRY(hl::alloc(c, lb.w, k, S.rhs));
+      if (k > 0) {
+        MNP_CUDA(cudaMemcpyAsync(S.lhs.ptr(), H.d.A[q] + H.aoff[b], sizeof(double2) * lb.y * k,
+                                 cudaMemcpyDeviceToDevice, c.st));
+        MNP_CUDA(cudaMemcpyAsync(S.rhs.ptr(), H.d.B[q] + H.boff[b], sizeof(double2) * lb.w * k,
+                                 cudaMemcpyDeviceToDevice, c.st));
+      }
+      out[q][T.low[b]] = std::move(S);
+    }
+  }
+  MNP_CUDA(cudaEventRecord(ev[1], c.st));
+  MNP_CUDA(cudaStreamWaitEvent(L.st, ev[1], 0));
+  return MNPBEM_OK;
+}
+
 // full blocks and ACA of one wavelength (lane parameters lp_dev); ranks to
-// the host, bytes of a product with N columns
-mnpbem_status hmat_fill(mnpbem_geom* G, Lane& L, HmatHost& H, int N) {
+// the host, bytes of a product with N columns.  cap: copies of the FP64
+// blocks for the H-matrix arithmetic (NULL: none)
+mnpbem_status hmat_fill(mnpbem_geom* G, Lane& L, HmatHost& H, int N, hl::Ctx* cap = nullptr,
+                        hl::HM* out = nullptr) {
   AsmParams p = base_params(G, L.lp_dev.as<LamParams>());
   MNP_TRY(assemble_leaves(p, H.la, L.st));
   MNP_TRY(hmat_aca(p, H.d, L.st));
-  MNP_TRY(hmat_split(H.d, L.st));
   H.ranks.assign((size_t)4 * H.d.nlow, 0);
   if (!H.ranks.empty())
     MNP_CUDA(cudaMemcpyAsync(H.ranks.data(), H.d.rank, sizeof(int) * H.ranks.size(), cudaMemcpyDeviceToHost, L.st));
+  MNP_CUDA(cudaStreamSynchronize(L.st));
+  if (cap) MNP_TRY(hmat_capture(L, H, *cap, out));
+  MNP_TRY(hmat_split(H.d, L.st));
   MNP_CUDA(cudaStreamSynchronize(L.st));
   double entries = 4.0 * (double)H.la.nvals;
   for (int q = 0; q < 4; ++q)
@@ -2592,6 +2662,8 @@ struct IterOpts {
   int solver = 0;   // 0 gmres, 1 cgs, 2 bicgstab
   double tol = 1e-6, htol = 1e-6;
   int maxit = 100, restart = 0, precond = 1, kmax = 100;
+  int kmax_pc = 4;   // rank cap of the 'hmat' preconditioner's arithmetic (compress.m: min(op.kmax))
+  double htol_pc = 1e-6;   // its ACA tolerance (compress.m: max(op.htol))
   int reuse = 0, refresh = 0;
 };
 
@@ -2605,10 +2677,12 @@ mnpbem_status iter_opts(const mnpbem_iter_options* op, IterOpts& o) {
     if (op->tol > 0) o.tol = op->tol;
     if (op->maxit > 0) o.maxit = op->maxit;
     if (op->restart > 0) o.restart = op->restart;
-    if (op->precond == 0 || op->precond == 1) o.precond = op->precond;
-    else { set_error("iterative solver: precond must be 0 or 1"); return MNPBEM_ERR_INVALID_ARG; }
+    if (op->precond >= 0 && op->precond <= 2) o.precond = op->precond;
+    else { set_error("iterative solver: precond must be 0, 1 or 2"); return MNPBEM_ERR_INVALID_ARG; }
     if (op->htol > 0) o.htol = op->htol;
     if (op->kmax > 0) o.kmax = op->kmax;
+    if (op->kmax_precond > 0) o.kmax_pc = op->kmax_precond;
+    o.htol_pc = op->htol_precond > 0 ? op->htol_precond : o.htol;
     o.reuse = op->reuse_precond != 0;
     o.refresh = std::max(0, op->refresh_steps);
   }
@@ -2654,6 +2728,20 @@ struct Gmres {
     Vec64 v = vec64(G, L, P);
     if (!o.precond) {
       kv_pack_bx(n, P, phi, a, al, De, dst, L.st);
+    } else if (o.precond == 2) {
+      // H-matrix LU preconditioner on the H stream, ordered with the lane
+      hl::HPrecond& h = *L.hpc;
+      cudaEvent_t ev[2] = {nullptr, nullptr};
+      for (auto& e : ev) MNP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      mnpbem_status s = MNPBEM_OK;
+      cudaError_t ce = cudaEventRecord(ev[0], L.st);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(h.c->st, ev[0], 0);
+      if (ce == cudaSuccess) s = hl::precond_apply(h, P, phi, a, al, De, dst);
+      if (ce == cudaSuccess && s == MNPBEM_OK) ce = cudaEventRecord(ev[1], h.c->st);
+      if (ce == cudaSuccess && s == MNPBEM_OK) ce = cudaStreamWaitEvent(L.st, ev[1], 0);
+      for (auto& e : ev) cudaEventDestroy(e);
+      MNP_CUDA(ce);
+      MNP_TRY(s);
     } else if (c.precision == MNPBEM_FP64) {
       MNP_TRY(apply_mldivide<double>(fdp, P, lpp, chain_mats<double>(G, L), phi, a, al, De, dst, dst + 4 * n * P,
                                      v.work, gemm_w<double>, nullptr, L.st));
@@ -2945,6 +3033,27 @@ struct Gmres {
   }
 };
 
+// the cluster tree and options an 'hmat' preconditioner was built with
+uint64_t tree_signature(const mnpbem_cluster_tree* t, const IterOpts& o) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+  auto mix_arr = [&](const int32_t* a, int64_t cnt) {
+    for (int64_t i = 0; a && i < cnt; ++i) mix((uint32_t)a[i]);
+  };
+  if (!t) return 0;
+  mix((uint32_t)t->ncluster);
+  mix_arr(t->son, 2 * (int64_t)t->ncluster);
+  mix_arr(t->cind, 2 * (int64_t)t->ncluster);
+  mix_arr(t->full, 2 * (int64_t)t->nfull);
+  mix_arr(t->low, 2 * (int64_t)t->nlow);
+  uint64_t ht;
+  memcpy(&ht, &o.htol_pc, sizeof(ht));
+  mix(ht);
+  mix((uint32_t)o.kmax_pc);
+  mix((uint32_t)o.kmax);
+  return h;
+}
+
 // one wavelength on lane 0: excitation, H-matrices, optional preconditioner
 mnpbem_status iter_prepare(mnpbem_geom* G, Job& j, const double2* ext_pot, HmatHost& H, const IterOpts& o,
                            const mnpbem_cluster_tree* tree) {
@@ -2952,9 +3061,12 @@ mnpbem_status iter_prepare(mnpbem_geom* G, Job& j, const double2* ext_pot, HmatH
   MNP_TRY(upload_lp(G, L, j.s, 0));
   L.w = 0;
   MNP_TRY(hmat_setup(G, tree, o.kmax, o.htol, H, L.st));
-  const bool keep = o.precond && o.reuse && L.pc_valid && L.pc_precision == j.c.precision &&
-                    L.pc_mat0 == L.mat[0].ptr && !(o.refresh > 0 && L.pc_last_steps > o.refresh);
-  if (o.precond && !keep) {
+  const bool refresh_due = o.refresh > 0 && L.pc_last_steps > o.refresh;
+  const bool keep = o.precond == 1 && o.reuse && L.pc_valid && L.pc_precision == j.c.precision &&
+                    L.pc_mat0 == L.mat[0].ptr && !refresh_due;
+  const uint64_t tsig = tree_signature(tree, o);
+  const bool keep_h = o.precond == 2 && o.reuse && L.hpc && L.hpc_sig == tsig && !refresh_due;
+  if (o.precond == 1 && !keep) {
     MNP_TRY(run_stage(G, L, j.c, 0, true));   // per-face eps + dense matrices
     MNP_TRY(run_stage(G, L, j.c, 1, true));   // dense inverses of bemret (initmat.m)
     MNP_TRY(L.pc_face.ensure(L.facebuf.bytes));
@@ -2968,13 +3080,33 @@ mnpbem_status iter_prepare(mnpbem_geom* G, Job& j, const double2* ext_pot, HmatH
   } else {
     face_eps(G, L);
     MNP_CHECK_LAUNCH();
-    if (!o.precond) {   // the preconditioner's per-face data are the current ones (unused)
+    if (o.precond != 1) {   // the dense preconditioner's per-face data (unused)
       MNP_TRY(L.pc_face.ensure(L.facebuf.bytes));
       MNP_TRY(L.pc_lp.ensure(sizeof(LamParams)));
     }
   }
   const int P = j.c.P;
-  MNP_TRY(hmat_fill(G, L, H, 4 * P));
+  if (o.precond == 2 && !keep_h) {
+    // initprecond.m ('hmat'): H-matrix LU of G1, G2 and Sigma, Sigma1 and
+    // Deltai as H-matrices, truncated with htol and min(op.kmax)
+    std::shared_ptr<hl::Tree> T;
+    MNP_TRY(hl::tree_from_abi(tree, T));
+    std::shared_ptr<hl::Ctx> hc;
+    MNP_TRY(hl::ctx_make(G->device, T, o.htol_pc, o.kmax_pc, hc));
+    hl::HM m4[4];
+    L.hpc.reset();
+    MNP_TRY(hmat_fill(G, L, H, 4 * P, hc.get(), m4));
+    auto hp = std::make_shared<hl::HPrecond>();
+    const FaceData fd = face_data(G, L);
+    MNP_CUDA(cudaStreamSynchronize(L.st));   // per-face eps of this wavelength
+    MNP_TRY(hl::precond_build(hc, m4[0], m4[1], m4[2], m4[3], 2.0 * M_PI / j.s.enei[0], fd.eps1, fd.eps2,
+                              G->g.nvec, *hp));
+    L.hpc = hp;
+    L.hpc_sig = tsig;
+    L.pc_enei = j.s.enei[0];
+  } else {
+    MNP_TRY(hmat_fill(G, L, H, 4 * P));
+  }
   Vec64 v = vec64(G, L, P);
   const FaceData fd = face_data(G, L);
   const LamParams* lp = L.lp_dev.as<LamParams>();

@@ -356,15 +356,6 @@ __global__ void k_transpose(const double2* A, int lda, int m, int n, double2* B)
     if (i0 + ii < m && j0 + jj < n) B[j0 + jj + (int64_t)(i0 + ii) * n] = t[jj][ii];
   }
 }
-// row-major [m][n] -> column-major m x n
-__global__ void k_rm_to_cm(const double2* src, int m, int n, double2* dst) {
-  const int64_t cnt = (int64_t)m * n;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e % m), j = (int)(e / m);
-    dst[e] = src[(int64_t)i * n + j];
-  }
-}
-
 unsigned eblocks(int64_t cnt) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv_up(cnt, 256), 4096)); }
 
 // ------------------------------------------------------ device resources
@@ -1461,18 +1452,9 @@ mnpbem_status precond_apply(HPrecond& h, int P, const double2* phi, const double
 }  // namespace hl
 }  // namespace mnpbem
 
-// ====================================================================== C ABI
-// Opaque H-matrix of the C ABI: the blocks and the options (htol, kmax) of
-// one cluster tree, the arguments the reference's H-matrix MEX functions take
-// (mex/hmatlu.cpp, hmatrsolve.cpp, hmatinv.cpp, hmatadd.cpp, hmatsolve.cpp).
-struct mnpbem_hm_s {
-  std::shared_ptr<mnpbem::hl::Ctx> c;
-  mnpbem::hl::HM m;
-};
-
-namespace {
-using namespace mnpbem;
-using namespace mnpbem::hl;
+// ------------------------------------------------------ tree from the C ABI
+namespace mnpbem {
+namespace hl {
 
 mnpbem_status tree_from_abi(const mnpbem_cluster_tree* t, std::shared_ptr<Tree>& out) {
   auto bad = [](const char* why) {
@@ -1536,6 +1518,22 @@ mnpbem_status tree_from_abi(const mnpbem_cluster_tree* t, std::shared_ptr<Tree>&
   out = std::move(T);
   return MNPBEM_OK;
 }
+
+}  // namespace hl
+}  // namespace mnpbem
+
+// ====================================================================== C ABI
+// Opaque H-matrix of the C ABI: the blocks and the options (htol, kmax) of
+// one cluster tree, the arguments the reference's H-matrix MEX functions take
+// (mex/hmatlu.cpp, hmatrsolve.cpp, hmatinv.cpp, hmatadd.cpp, hmatsolve.cpp).
+struct mnpbem_hm_s {
+  std::shared_ptr<mnpbem::hl::Ctx> c;
+  mnpbem::hl::HM m;
+};
+
+namespace {
+using namespace mnpbem;
+using namespace mnpbem::hl;
 
 bool same_tree(const Tree& a, const Tree& b) {
   return a.son0 == b.son0 && a.son1 == b.son1 && a.lo == b.lo && a.hi == b.hi && a.ad == b.ad;

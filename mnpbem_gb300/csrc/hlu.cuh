@@ -78,6 +78,10 @@ struct Ctx {
 // error flags a kernel raises (dev[1]): a zero pivot of a leaf LU or inverse
 constexpr int HL_ERR_PIVOT = 1;
 
+// cluster tree of the C ABI, checked (leaf pairs full, blocks partition the
+// matrix and match the tree)
+mnpbem_status tree_from_abi(const mnpbem_cluster_tree* t, std::shared_ptr<Tree>& out);
+
 mnpbem_status ctx_make(int device, std::shared_ptr<const Tree> t, double tol, int kmax, std::shared_ptr<Ctx>& out);
 // the H-arithmetic stream of a device (created on first use)
 mnpbem_status hl_stream(int device, cudaStream_t& st);

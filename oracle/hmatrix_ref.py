@@ -20,7 +20,7 @@ preconditioned GMRES of ``bemretiter``.  Followed files:
   full blocks hold the entries of the complete Green function (refinement
   included);
 * ``BEM/@bemretiter/private/afun.m:6-35``, ``mfun.m:1-52``,
-  ``initprecond.m:1-76`` ('full'), ``@bemiter/solve.m:1-45`` (gmres, cgs,
+  ``initprecond.m:1-76`` ('full'; 'hmat' through oracle/hlu_ref.py), ``@bemiter/solve.m:1-45`` (gmres, cgs,
   bicgstab; cgs and bicgstab restated from their published algorithms with
   the preconditioner applied to the search directions).
 
@@ -459,7 +459,7 @@ class BemRetIter:
     'full' (dense chain of mldivide.m) or None."""
 
     def __init__(self, cp, cleaf=200, htol=1e-6, kmax=100, tol=1e-6, maxit=100, restart=None,
-                 precond="full", eta=2.5, solver="gmres"):
+                 precond="full", eta=2.5, solver="gmres", kmax_precond=4):
         self.p = cp
         self.bem = R.BemRet(cp)
         face_part = np.repeat(np.arange(len(cp.parts)), [q.n for q in cp.parts])
@@ -467,6 +467,7 @@ class BemRetIter:
         self.htol, self.kmax, self.eta = htol, kmax, eta
         self.tol, self.maxit, self.restart, self.precond = tol, maxit, restart, precond
         self.solver = solver
+        self.kmax_precond = kmax_precond
         self.enei = None
 
     def initmat(self, enei):
@@ -477,6 +478,17 @@ class BemRetIter:
         b = self.bem
         self.H = build_hmatrices(self.p, self.tree, (b.G1, b.H1, b.G2, b.H2), enei, self.htol,
                                  self.kmax, self.eta)
+        if self.precond == "hmat":
+            # initprecond.m 'hmat' on the compressed H-matrices (compress.m:
+            # htol, min(op.kmax))
+            from . import hlu_ref as HL
+            t = self.tree
+            full, low = self.H[0].full, self.H[0].low
+            T = HL.Tree(t.son, t.cind, full, low)
+            mats = [HL.from_blocks(T, full, low, H.val, H.lhs, H.rhs) for H in self.H]
+            e1 = self.p.eps_faces(enei, 0)
+            e2 = self.p.eps_faces(enei, 1)
+            self.hpc = HL.HmatPrecond(T, t.perm, *mats, b.k, e1, e2, b.nvec, self.htol, self.kmax_precond)
 
     def _split(self, x):
         n = self.p.n
@@ -510,6 +522,8 @@ class BemRetIter:
 
     def mfun(self, v):
         phi, a, De, alpha = self._split(v)
+        if self.precond == "hmat":
+            return self._pack(*self.hpc.apply(phi, a, De, alpha))
         s = self.bem.chain(phi, a, alpha, De)
         return self._pack(s["sig1"], s["h1"], s["sig2"], s["h2"])
 
@@ -517,7 +531,7 @@ class BemRetIter:
         self.initmat(exc["enei"])
         phi, a, alpha, De = self.bem.excitation(exc)
         b = self._pack(phi, a, De, alpha)
-        mf = self.mfun if self.precond == "full" else None
+        mf = self.mfun if self.precond in ("full", "hmat") else None
         if self.solver == "gmres":
             x, flag, relres, it = gmres(self.afun, b, self.tol, self.maxit, self.restart, mf)
         else:
