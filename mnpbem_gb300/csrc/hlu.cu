@@ -37,53 +37,88 @@ namespace {
 
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
 
-__global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double2 alpha, const double2* __restrict__ A,
-                                               int lda, int ta, const double2* __restrict__ B, int ldb, int tb,
-                                               double2 beta, double2* __restrict__ C, int ldc) {
-  __shared__ double2 As[16][33];   // [l][i]
-  __shared__ double2 Bs[16][33];   // [l][j]
+// C tile (TILE x TILE) of alpha op(A) op(B) (+ beta C) over K range
+// [k0, k1), 256 threads (16 x 16, each TILE / 16 x TILE / 16 outputs).  With
+// W != NULL the raw sums go to W + z M N (column-major M x N, z = blockIdx.z)
+// for the ordered reduction of k_zgemm_reduce instead of C.
+template <int TILE>
+__global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, int kc, double2 alpha,
+                                               const double2* __restrict__ A, int lda, int ta,
+                                               const double2* __restrict__ B, int ldb, int tb, double2 beta,
+                                               double2* __restrict__ C, int ldc, double2* __restrict__ W) {
+  constexpr int R = TILE / 16;
+  __shared__ double2 As[16][TILE + 1];   // [l][i]
+  __shared__ double2 Bs[16][TILE + 1];   // [l][j]
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-  double2 acc[2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
-  for (int l0 = 0; l0 < K; l0 += 16) {
-    for (int e = threadIdx.x; e < 512; e += 256) {
-      // A tile: 32 rows (i) x 16 (l); B tile: 16 (l) x 32 columns (j)
-      const int ii = ta ? e >> 4 : e & 31, ll = ta ? e & 15 : e >> 5;
+  const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE;
+  const int k0 = blockIdx.z * kc, k1 = min(K, k0 + kc);
+  double2 acc[R][R];
+#pragma unroll
+  for (int a = 0; a < R; ++a)
+#pragma unroll
+    for (int b = 0; b < R; ++b) acc[a][b] = make_double2(0.0, 0.0);
+  for (int l0 = k0; l0 < k1; l0 += 16) {
+    for (int e = threadIdx.x; e < 16 * TILE; e += 256) {
+      // A tile: TILE rows (i) x 16 (l); B tile: 16 (l) x TILE columns (j)
+      const int ii = ta ? e >> 4 : e % TILE, ll = ta ? e & 15 : e / TILE;
       const int i = i0 + ii, l = l0 + ll;
       double2 v = make_double2(0.0, 0.0);
-      if (i < M && l < K) v = ta ? A[l + (int64_t)i * lda] : A[i + (int64_t)l * lda];
+      if (i < M && l < k1) v = ta ? A[l + (int64_t)i * lda] : A[i + (int64_t)l * lda];
       As[ll][ii] = v;
-      const int jj = tb ? e & 31 : e >> 4, lb = tb ? e >> 5 : e & 15;
+      const int jj = tb ? e % TILE : e >> 4, lb = tb ? e / TILE : e & 15;
       const int j = j0 + jj, l2 = l0 + lb;
       double2 w = make_double2(0.0, 0.0);
-      if (j < N && l2 < K) w = tb ? B[j + (int64_t)l2 * ldb] : B[l2 + (int64_t)j * ldb];
+      if (j < N && l2 < k1) w = tb ? B[j + (int64_t)l2 * ldb] : B[l2 + (int64_t)j * ldb];
       Bs[lb][jj] = w;
     }
     __syncthreads();
 #pragma unroll 4
     for (int l = 0; l < 16; ++l) {
-      const double2 a0 = As[l][tx], a1 = As[l][tx + 16];
-      const double2 b0 = Bs[l][ty], b1 = Bs[l][ty + 16];
-      cfma(acc[0][0], a0, b0);
-      cfma(acc[0][1], a0, b1);
-      cfma(acc[1][0], a1, b0);
-      cfma(acc[1][1], a1, b1);
+      double2 av[R], bv[R];
+#pragma unroll
+      for (int a = 0; a < R; ++a) av[a] = As[l][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < R; ++b) bv[b] = Bs[l][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < R; ++a)
+#pragma unroll
+        for (int b = 0; b < R; ++b) cfma(acc[a][b], av[a], bv[b]);
     }
     __syncthreads();
   }
   const bool b0 = beta.x == 0.0 && beta.y == 0.0;
 #pragma unroll
-  for (int a = 0; a < 2; ++a)
+  for (int a = 0; a < R; ++a)
 #pragma unroll
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < R; ++b) {
       const int i = i0 + tx + 16 * a, j = j0 + ty + 16 * b;
       if (i < M && j < N) {
-        double2* cp = C + i + (int64_t)j * ldc;
-        double2 v = cmul(alpha, acc[a][b]);
-        if (!b0) v = cadd(v, cmul(beta, *cp));
-        *cp = v;
+        if (W) {
+          W[(int64_t)blockIdx.z * M * N + i + (int64_t)j * M] = acc[a][b];
+        } else {
+          double2* cp = C + i + (int64_t)j * ldc;
+          double2 v = cmul(alpha, acc[a][b]);
+          if (!b0) v = cadd(v, cmul(beta, *cp));
+          *cp = v;
+        }
       }
     }
+}
+
+// C = alpha sum_z W[z] + beta C, the parts summed in order z = 0, 1, ...
+__global__ void k_zgemm_reduce(int M, int N, int nz, const double2* __restrict__ W, double2 alpha, double2 beta,
+                               double2* __restrict__ C, int ldc) {
+  const int64_t cnt = (int64_t)M * N;
+  const bool b0 = beta.x == 0.0 && beta.y == 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+    double2 s = W[e];
+    for (int z = 1; z < nz; ++z) s = cadd(s, W[(int64_t)z * cnt + e]);
+    const int i = (int)(e % M), j = (int)(e / M);
+    double2* cp = C + i + (int64_t)j * ldc;
+    double2 v = cmul(alpha, s);
+    if (!b0) v = cadd(v, cmul(beta, *cp));
+    *cp = v;
+  }
 }
 
 // A = L U in place (n x n, ld lda): column j of L, then row j of U divided by
@@ -330,6 +365,11 @@ __global__ void k_add2(const double2* a, const double2* b, double2* out, int64_t
     out[e] = make_double2(a[e].x + sb * y.x, a[e].y + sb * y.y);
   }
 }
+__global__ void k_eye(double2* out, int n) {
+  const int64_t cnt = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = make_double2(e % n == e / n ? 1.0 : 0.0, 0.0);
+}
 __global__ void k_negate(const double2* a, double2* out, int64_t cnt) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = make_double2(-a[e].x, -a[e].y);
@@ -495,11 +535,39 @@ View block_of(const DMat& a, int r0, int nr, int c0, int nc) {
   return View{a.ptr() + r0 + (int64_t)c0 * std::max(1, a.m), std::max(1, a.m), nr, nc};
 }
 
+// FP64 runs at a small fraction of the FP32 rate on this GPU, so every product
+// is spread over the SMs: 32 x 32 tiles when they alone give a full wave, else
+// 16 x 16 tiles, and when those are still too few the K range is split
+// across CTAs whose partial sums are added in a fixed order (deterministic).
+constexpr int HL_WAVE = 148;
 mnpbem_status gemm(Ctx& c, int M, int N, int K, double2 alpha, View A, int ta, View B, int tb, double2 beta,
                    double2* C, int ldc) {
   if (M <= 0 || N <= 0) return MNPBEM_OK;
-  dim3 grid((unsigned)cdiv_up(M, 32), (unsigned)cdiv_up(N, 32));
-  k_zgemm<<<grid, 256, 0, c.st>>>(M, N, K, alpha, A.p, A.ld, ta, B.p, B.ld, tb, beta, C, ldc);
+  const int64_t t32 = cdiv_up(M, 32) * cdiv_up(N, 32);
+  if (t32 >= HL_WAVE) {
+    dim3 grid((unsigned)cdiv_up(M, 32), (unsigned)cdiv_up(N, 32), 1);
+    k_zgemm<32><<<grid, 256, 0, c.st>>>(M, N, K, std::max(K, 1), alpha, A.p, A.ld, ta, B.p, B.ld, tb, beta, C, ldc,
+                                        nullptr);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  const int64_t t16 = cdiv_up(M, 16) * cdiv_up(N, 16);
+  int nz = 1;
+  if (t16 < HL_WAVE && K > 64) nz = (int)std::min<int64_t>(cdiv_up(HL_WAVE, t16), cdiv_up(K, 64));
+  const int kc = (int)round_up(cdiv_up(std::max(K, 1), nz), 16);
+  nz = (int)cdiv_up(std::max(K, 1), kc);
+  dim3 grid((unsigned)cdiv_up(M, 16), (unsigned)cdiv_up(N, 16), (unsigned)nz);
+  if (nz == 1) {
+    k_zgemm<16><<<grid, 256, 0, c.st>>>(M, N, K, kc, alpha, A.p, A.ld, ta, B.p, B.ld, tb, beta, C, ldc, nullptr);
+    MNP_CHECK_LAUNCH();
+    return MNPBEM_OK;
+  }
+  std::shared_ptr<void> W;
+  MNP_TRY(alloc_raw(c, sizeof(double2) * (size_t)nz * M * N, W));
+  double2* w = static_cast<double2*>(W.get());
+  k_zgemm<16><<<grid, 256, 0, c.st>>>(M, N, K, kc, alpha, A.p, A.ld, ta, B.p, B.ld, tb, beta, C, ldc, w);
+  MNP_CHECK_LAUNCH();
+  k_zgemm_reduce<<<eblocks((int64_t)M * N), 256, 0, c.st>>>(M, N, nz, w, alpha, beta, C, ldc);
   MNP_CHECK_LAUNCH();
   return MNPBEM_OK;
 }
@@ -587,28 +655,47 @@ mnpbem_status trsm_left(Ctx& c, const DMat& A, char uplo, char trans, double2* X
   return MNPBEM_OK;
 }
 
-// lu.cpp:110-124 solve(side, B, transB, A, uplo) as a new matrix
-mnpbem_status trsm(Ctx& c, char side, View B, char trans, const DMat& A, char uplo, DMat& out) {
+// lu.cpp:110-124 solve(side, B, transB, A, uplo) as a new matrix, A the
+// diagonal leaf of an LU: products with the inverses of its triangles (formed
+// once per leaf) when it has them, else substitution
+mnpbem_status trsm(Ctx& c, char side, View B, char trans, const Sub& A, char uplo, DMat& out) {
+  const DMat& Ti = uplo == 'L' ? A.linv : A.uinv;
+  const int tr = trans == 'T';
+  if (Ti.p) {
+    if (side == 'L') return mul(c, whole(Ti), tr, B, 0, out);
+    return mul(c, B, 0, whole(Ti), tr, out);
+  }
   if (side == 'L') {
     MNP_TRY(copy_view(c, B, out));
-    return trsm_left(c, A, uplo, trans, out.ptr(), std::max(1, out.m), out.n);
+    return trsm_left(c, A.mat, uplo, trans, out.ptr(), std::max(1, out.m), out.n);
   }
   // X op(A) = B  <=>  op(A)^T X^T = B^T
   DMat Y;
   MNP_TRY(transpose(c, B, Y));
-  MNP_TRY(trsm_left(c, A, uplo, trans == 'T' ? 'N' : 'T', Y.ptr(), std::max(1, Y.m), Y.n));
+  MNP_TRY(trsm_left(c, A.mat, uplo, tr ? 'N' : 'T', Y.ptr(), std::max(1, Y.m), Y.n));
   return transpose(c, whole(Y), out);
 }
 
-mnpbem_status lu_dense(Ctx& c, const DMat& a, DMat& out) {
+// LU of a full leaf and the inverses of its triangles
+mnpbem_status lu_dense(Ctx& c, const DMat& a, int i, Sub& out) {
   if (a.m > HL_LEAF_MAX || a.m != a.n) {
     set_error("H-matrix LU: leaf blocks of %d x %d are not supported (square, at most %d)", a.m, a.n, HL_LEAF_MAX);
     return MNPBEM_ERR_UNSUPPORTED;
   }
-  MNP_TRY(copy_view(c, whole(a), out));
-  if (a.m > 0) {
-    k_lu_leaf<<<1, 1024, 0, c.st>>>(out.ptr(), a.m, a.m, c.dev + 1);
+  const int n = a.m;
+  out = Sub();
+  out.row = out.col = i;
+  out.flag = FLAG_FULL;
+  MNP_TRY(copy_view(c, whole(a), out.mat));
+  if (n == 0) return MNPBEM_OK;
+  k_lu_leaf<<<1, 1024, 0, c.st>>>(out.mat.ptr(), n, n, c.dev + 1);
+  MNP_CHECK_LAUNCH();
+  for (int q = 0; q < 2; ++q) {
+    DMat& X = q == 0 ? out.linv : out.uinv;
+    MNP_TRY(alloc(c, n, n, X));
+    k_eye<<<eblocks((int64_t)n * n), 256, 0, c.st>>>(X.ptr(), n);
     MNP_CHECK_LAUNCH();
+    MNP_TRY(trsm_left(c, out.mat, q == 0 ? 'L' : 'U', 'N', X.ptr(), n, n));
   }
   return MNPBEM_OK;
 }
@@ -985,12 +1072,12 @@ mnpbem_status inv_rec(Ctx& c, const HM& A, int i, HM& C) {
 mnpbem_status rsolve_ss(Ctx& c, const Sub& B, const Sub& A, int i, int j, char uplo, Sub& out) {
   if (B.flag == FLAG_FULL) {
     DMat m;
-    MNP_TRY(trsm(c, 'R', mat_view(c, B, i, j), 'N', A.mat, uplo, m));
+    MNP_TRY(trsm(c, 'R', mat_view(c, B, i, j), 'N', A, uplo, m));
     out = make_full(i, j, std::move(m));
   } else {
     DMat l, r;
     MNP_TRY(copy_view(c, lhs_view(c, B, i), l));
-    MNP_TRY(trsm(c, 'L', rhs_view(c, B, j), 'T', A.mat, uplo, r));
+    MNP_TRY(trsm(c, 'L', rhs_view(c, B, j), 'T', A, uplo, r));
     out = make_rk(i, j, std::move(l), std::move(r));
   }
   return MNPBEM_OK;
@@ -998,11 +1085,11 @@ mnpbem_status rsolve_ss(Ctx& c, const Sub& B, const Sub& A, int i, int j, char u
 mnpbem_status lsolve_ss(Ctx& c, const Sub& B, const Sub& A, int i, int j, char uplo, Sub& out) {
   if (B.flag == FLAG_FULL) {
     DMat m;
-    MNP_TRY(trsm(c, 'L', mat_view(c, B, i, j), 'N', A.mat, uplo, m));
+    MNP_TRY(trsm(c, 'L', mat_view(c, B, i, j), 'N', A, uplo, m));
     out = make_full(i, j, std::move(m));
   } else {
     DMat l, r;
-    MNP_TRY(trsm(c, 'L', lhs_view(c, B, i), 'N', A.mat, uplo, l));
+    MNP_TRY(trsm(c, 'L', lhs_view(c, B, i), 'N', A, uplo, l));
     MNP_TRY(copy_view(c, rhs_view(c, B, j), r));
     out = make_rk(i, j, std::move(l), std::move(r));
   }
@@ -1116,12 +1203,7 @@ mnpbem_status lsolve_h(Ctx& c, const HM& B, const HM& A, HM& X, int i, int j, ch
 }
 
 mnpbem_status lu_rec(Ctx& c, const HM& B, HM& A, int i) {
-  if (T(c).leaf(i)) {
-    DMat m;
-    MNP_TRY(lu_dense(c, at(B, Key(i, i)).mat, m));
-    A[Key(i, i)] = make_full(i, i, std::move(m));
-    return MNPBEM_OK;
-  }
+  if (T(c).leaf(i)) return lu_dense(c, at(B, Key(i, i)).mat, i, A[Key(i, i)]);
   const int i0 = T(c).sons(i, 0), i1 = T(c).sons(i, 1);
   MNP_TRY(lu_rec(c, B, A, i0));
   MNP_TRY(lsolve_h(c, B, A, A, i0, i1, 'L'));
@@ -1145,7 +1227,18 @@ mnpbem_status sub_apply(Ctx& c, const Sub& S, double2 alpha, const double2* x, d
 }
 
 mnpbem_status solve_vec(Ctx& c, const HM& A, double2* x, int N, int i, char uplo) {
-  if (T(c).admiss(i, i)) return trsm_left(c, at(A, Key(i, i)).mat, uplo, 'N', x + T(c).lo[i], T(c).n, N);
+  if (T(c).admiss(i, i)) {
+    const Sub& D = at(A, Key(i, i));
+    const DMat& Ti = uplo == 'L' ? D.linv : D.uinv;
+    double2* xp = x + T(c).lo[i];
+    const int n = T(c).n, m = T(c).size(i);
+    if (!Ti.p) return trsm_left(c, D.mat, uplo, 'N', xp, n, N);
+    DMat t;
+    MNP_TRY(mul(c, whole(Ti), 0, View{xp, n, m, N}, 0, t));
+    MNP_CUDA(cudaMemcpy2DAsync(xp, sizeof(double2) * n, t.ptr(), sizeof(double2) * m, sizeof(double2) * m, N,
+                               cudaMemcpyDeviceToDevice, c.st));
+    return MNPBEM_OK;
+  }
   const int i0 = uplo == 'L' ? T(c).sons(i, 0) : T(c).sons(i, 1);
   const int i1 = uplo == 'L' ? T(c).sons(i, 1) : T(c).sons(i, 0);
   MNP_TRY(solve_vec(c, A, x, N, i0, uplo));

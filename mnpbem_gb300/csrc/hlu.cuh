@@ -32,6 +32,7 @@ struct DMat {
 struct Sub {
   int row = -1, col = -1, flag = 0;
   DMat mat, lhs, rhs;
+  DMat linv, uinv;   // diagonal leaf of an LU: inverses of its L and U factors
   int rank() const { return lhs.n; }
 };
 using Key = std::pair<int, int>;
