@@ -8,7 +8,9 @@ at most ``cleaf`` faces.  ``hmatrix_blocks(tree, eta)`` follows
 clusters inside one particle each with ``eta min(rad1, rad2) < dist`` a
 low-rank block; other pairs recurse into their sons.  ``hpartition(p).c``
 hands both to the library (``mnpbem_cluster_tree``), as treemex.m hands them
-to the H-matrix MEX functions.
+to the H-matrix MEX functions.  ``hmatrix_gpu`` is an H-matrix on such a tree
+with the arithmetic of those MEX functions (LU, right solve, inverse, sum,
+diagonal scaling, solve, product) run by the library.
 """
 import ctypes
 
