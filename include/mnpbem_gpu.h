@@ -302,7 +302,11 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_lanes(mnpbem_geom* g, int32_t lanes);
  * on FP16 operands scaled per row / column by powers of two, kind::f16, 1 =
  * default, or on TF32 operands, 0), "tf32_round" (round A operands to nearest
  * TF32: 0/1), "assembly_ds" (mixed-precision assembly in double-single FP32
- * arithmetic: 0/1).  Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
+ * arithmetic: 0/1), "sweep_graph" (1 = default: the wavelengths of a sweep
+ * after each lane's first run as one CUDA graph with a device-side
+ * wavelength queue and device-side refinement decisions; 0: the host
+ * scheduler polls the lanes and queues every stage; results are identical).
+ * Unknown keys or values return MNPBEM_ERR_INVALID_ARG.
  * No counterpart in the reference.                                          */
 MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t value);
 
@@ -311,7 +315,10 @@ MNPBEM_API mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key,
  * and inversion since the last "block_cond_reset"; a block above 1e6
  * (complex64) or 1e13 (FP64) fails the solve with MNPBEM_ERR_SINGULAR),
  * "block_cond_reset", "g1_blocks" (number of diagonal blocks G1 is factored
- * in).  No counterpart in the reference (MATLAB's inv reports a near-singular
+ * in), "sweep_graph_runs" (sweeps, or batch members, run as one graph),
+ * "sweep_graph_error" (the CUDA error that turned one-graph sweeps off for
+ * the handle, 0: none), "stage_graphs" (1: stages replay captured graphs, 0:
+ * they run directly).  No counterpart in the reference (MATLAB's inv reports a near-singular
  * matrix as a warning).                                                      */
 MNPBEM_API mnpbem_status mnpbem_geom_stat(mnpbem_geom* g, const char* key, double* value);
 

@@ -119,8 +119,10 @@ struct Lane {
     bool prof = false;
     uint64_t sig = 0;             // addresses of every buffer the graphs captured
     cudaGraphExec_t exec[NSTAGES] = {};
+    cudaGraph_t graph[NSTAGES] = {};   // the captured stages (child graphs of a sweep graph)
     Profiler::GraphRec rec[NSTAGES];
   } graphs;
+  DevBuf swctl;                   // device state of the lane in a sweep graph (SweepCtl)
   float cond_max = 0.f;       // largest block condition proxy since the counter was reset
   // scheduler state
   enum { IDLE = 0, ITER, DONE } state = IDLE;
@@ -180,6 +182,13 @@ struct mnpbem_geom {
   // per-wavelength parameters: pinned host ring (one slot per wavelength)
   LamParams* lp_ring = nullptr;
   int lp_cap = 0;
+  // one-graph sweeps (device-side wavelength queue and refinement decisions)
+  bool sweep_graph = true;
+  int64_t sweep_runs = 0;   // sweeps (or batch members) run as one graph
+  int sweep_err = 0;        // CUDA error that turned them off
+  cudaGraphExec_t sweep_exec = nullptr;
+  uint64_t sweep_key = 0;
+  DevBuf sweep_lp, sweep_ctl, sweep_res;   // parameters [nenei], job control, per-wavelength results
 };
 
 namespace {
@@ -199,6 +208,8 @@ void lane_release(Lane& L) {
   for (int q = 0; q < NSTAGES; ++q) {
     if (L.graphs.exec[q]) cudaGraphExecDestroy(L.graphs.exec[q]);
     L.graphs.exec[q] = nullptr;
+    if (L.graphs.graph[q]) cudaGraphDestroy(L.graphs.graph[q]);
+    L.graphs.graph[q] = nullptr;
     Profiler::release(L.graphs.rec[q]);
   }
   if (L.status_host) cudaFreeHost(L.status_host);
@@ -462,6 +473,8 @@ static mnpbem_status geom_create_impl(const double* verts, int64_t nverts, const
   if (luenv && (atoi(luenv) == 1 || atoi(luenv) == 2 || atoi(luenv) == 4)) G->lu_steps = atoi(luenv);
   const char* lenv = getenv("MNPBEM_LANES");
   if (lenv && atoi(lenv) > 0) G->lanes_req = std::min(MAX_LANES, atoi(lenv));
+  const char* swenv = getenv("MNPBEM_SWEEP_GRAPH");
+  if (swenv && swenv[0] == '0') G->sweep_graph = false;
   *out = G;
   return MNPBEM_OK;
 }
@@ -509,6 +522,8 @@ mnpbem_status mnpbem_geom_destroy(mnpbem_geom* g) {
   cudaSetDevice(g->device);
   if (g->st) cudaStreamSynchronize(g->st);
   g->prof.flush();
+  if (g->sweep_exec) cudaGraphExecDestroy(g->sweep_exec);
+  g->sweep_exec = nullptr;
   for (auto& L : g->lanes) lane_release(*L);
   g->lanes.clear();
   if (g->lp_ring) cudaFreeHost(g->lp_ring);
@@ -561,6 +576,7 @@ mnpbem_status mnpbem_geom_set_option(mnpbem_geom* g, const char* key, int32_t va
     for (auto& L : g->lanes) L->tc.max_ctas = value;
     return MNPBEM_OK;
   }
+  if (k == "sweep_graph" && (value == 0 || value == 1)) { g->sweep_graph = value != 0; return MNPBEM_OK; }
   if (k == "tf32_round" && (value == 0 || value == 1)) { g->tf32_rna = value != 0; return MNPBEM_OK; }
   if (k == "assembly_ds" && (value == 0 || value == 1)) { g->asm_ds = value != 0; return MNPBEM_OK; }
   set_error("unknown option '%s' or value %d out of range", key, value);
@@ -584,6 +600,18 @@ mnpbem_status mnpbem_geom_stat(mnpbem_geom* g, const char* key, double* value) {
   }
   if (k == "g1_blocks") {
     *value = (double)g->g1_off.size();
+    return MNPBEM_OK;
+  }
+  if (k == "sweep_graph_runs") {
+    *value = (double)g->sweep_runs;
+    return MNPBEM_OK;
+  }
+  if (k == "sweep_graph_error") {   // CUDA error that turned the one-graph sweep off (0: none)
+    *value = (double)g->sweep_err;
+    return MNPBEM_OK;
+  }
+  if (k == "stage_graphs") {        // stages replayed from captured graphs (0: run directly)
+    *value = g->use_graphs ? 1.0 : 0.0;
     return MNPBEM_OK;
   }
   set_error("mnpbem_geom_stat: unknown key '%s'", key);
@@ -1270,11 +1298,13 @@ mnpbem_status capture_stage(mnpbem_geom* G, Lane& L, const SolveCtx& c, int stag
   MNP_CUDA(e);
   cudaGraphExec_t exec = nullptr;
   e = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) cudaGraphDestroy(graph);
   MNP_CUDA(e);
   if (gr.exec[stage]) cudaGraphExecDestroy(gr.exec[stage]);
+  if (gr.graph[stage]) cudaGraphDestroy(gr.graph[stage]);
   Profiler::release(gr.rec[stage]);
   gr.exec[stage] = exec;
+  gr.graph[stage] = graph;
   cap.move_to(gr.rec[stage]);
   return MNPBEM_OK;
 }
@@ -1286,6 +1316,8 @@ void drop_graphs(mnpbem_geom* G, Lane& L) {
   for (int q = 0; q < NSTAGES; ++q) {
     if (gr.exec[q]) cudaGraphExecDestroy(gr.exec[q]);
     gr.exec[q] = nullptr;
+    if (gr.graph[q]) cudaGraphDestroy(gr.graph[q]);
+    gr.graph[q] = nullptr;
     Profiler::release(gr.rec[q]);
   }
   gr.valid = false;
@@ -1788,6 +1820,473 @@ mnpbem_status jobs_poll(std::vector<Job*>& jobs) {
   return MNPBEM_OK;
 }
 
+// ------------------------------------------------------------ sweep graphs
+// The remaining wavelengths of a sweep as one CUDA graph: per lane a WHILE
+// node whose body takes the next wavelength from a device counter shared by
+// the job's lanes (a work queue), runs the captured stages (child graphs),
+// refines in a nested WHILE node whose body picks the step kind on the device
+// (a SWITCH over the FP32, double-single and incremental steps) and decides
+// on the norms the step left (the host scheduler's rules, restated), and
+// writes the wavelength's results into per-wavelength slots.  Every loop is
+// bounded: the queue ends at nenei, the refinement at maxit (<= 1000).  The
+// host reads the slots once the graph has completed.  Several jobs (the
+// particles of a batch) are parallel branches of one graph.
+struct SweepCtl {
+  int w, iters, ds_done, kind;
+  double res, bnorm2;
+};
+struct JobCtl {
+  int next, nenei;
+};
+// per-wavelength result slots of one job (device)
+struct SweepDst {
+  double2 *sig1, *h1, *sig2, *h2;   // [w][n][P], [w][n][3P] (NULL: not requested)
+  double *ext, *sca;                // [w][P]
+  int* iters;                       // [w]
+  double* res;                      // [w]
+  int* status;                      // [w][LANE_NSTATUS]
+  int* nan;                         // set when a refinement step produced NaN
+  int64_t n;
+  int P;
+};
+
+__global__ void k_sw_next(JobCtl* jc, SweepCtl* sc, const LamParams* lps, LamParams* lp,
+                          cudaGraphConditionalHandle h) {
+  if (threadIdx.x) return;
+  const int w = atomicAdd(&jc->next, 1);
+  const bool go = w < jc->nenei;
+  if (go) {
+    sc->w = w;
+    *lp = lps[w];
+  }
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// status words of the wavelength's initmat (the layout of Lane::status_host)
+__global__ void k_sw_status(const SweepCtl* sc, const int* gj, const int* gji, const int* lu, const int* tce,
+                            const SweepDst* dp) {
+  if (threadIdx.x) return;
+  int* o = dp->status + (int64_t)sc->w * LANE_NSTATUS;
+  for (int q = 0; q < LANE_NSTATUS; ++q) o[q] = 0;
+  if (gj) { o[0] = gj[0]; o[1] = gj[1]; }
+  if (gji) { o[2] = gji[0]; o[3] = gji[1]; }
+  if (lu) { o[4] = lu[0]; o[5] = lu[1]; }
+  if (tce) o[6] = tce[0];
+}
+
+__global__ void k_ref_init(SweepCtl* sc, cudaGraphConditionalHandle h, int run, const SweepDst* dp) {
+  if (threadIdx.x) return;
+  const SweepDst& d = *dp;
+  sc->iters = 0;
+  sc->ds_done = 0;
+  sc->res = -1.0;
+  sc->bnorm2 = 0.0;
+  d.iters[sc->w] = 0;
+  d.res[sc->w] = -1.0;
+  if (run) cudaGraphSetConditional(h, 1u);
+}
+
+// next_step(): FP32 first, the double-single step once the FP32 residual is
+// small (or after three steps), then incremental steps; body index 0 / 1 / 2
+__global__ void k_ref_pick(SweepCtl* sc, cudaGraphConditionalHandle h, double ds_switch) {
+  if (threadIdx.x) return;
+  int idx = 2;
+  if (sc->iters == 0) idx = 0;
+  else if (!sc->ds_done && (sc->res <= ds_switch || sc->iters >= 3)) idx = 1;
+  sc->kind = idx;
+  cudaGraphSetConditional(h, (unsigned)idx);
+}
+
+// step_done() and step_converged() on the norms the step left
+__global__ void k_ref_decide(SweepCtl* sc, const double* hn, double tol, int maxit, cudaGraphConditionalHandle h,
+                             const SweepDst* dp) {
+  if (threadIdx.x) return;
+  const SweepDst& d = *dp;
+  if (sc->kind != 2) sc->bnorm2 = hn[1];
+  if (sc->kind == 1) sc->ds_done = 1;
+  sc->res = sc->bnorm2 > 0 ? sqrt(hn[0] / sc->bnorm2) : 0.0;
+  sc->iters += 1;
+  const bool nan = !(hn[2] == hn[2]);
+  if (nan) atomicOr(d.nan, 1);
+  const bool conv = sc->ds_done && sqrt(hn[2]) <= tol * sqrt(hn[3]);
+  d.iters[sc->w] = sc->iters;
+  d.res[sc->w] = sc->res;
+  cudaGraphSetConditional(h, (nan || conv || sc->iters >= maxit) ? 0u : 1u);
+}
+
+// the lane's solution and cross sections into the wavelength's slots
+__global__ void k_sw_out(const SweepCtl* sc, const double2* x1, const double2* x2, const double* ob,
+                         const SweepDst* dp) {
+  const SweepDst d = *dp;
+  const int w = sc->w, P = d.P;
+  const int64_t n = d.n, W = 4 * P;
+  const int64_t cnt = n * W;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / W;
+    const int c = (int)(e - i * W);
+    if (c < P) {
+      if (d.sig1) d.sig1[(w * n + i) * P + c] = x1[e];
+      if (d.sig2) d.sig2[(w * n + i) * P + c] = x2[e];
+    } else {
+      if (d.h1) d.h1[(w * n + i) * 3 * P + (c - P)] = x1[e];
+      if (d.h2) d.h2[(w * n + i) * 3 * P + (c - P)] = x2[e];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < P) {
+    if (d.ext) d.ext[(int64_t)w * P + threadIdx.x] = ob[threadIdx.x];
+    if (d.sca) d.sca[(int64_t)w * P + threadIdx.x] = ob[P + threadIdx.x];
+  }
+}
+
+struct GraphBuild {
+  cudaGraph_t top = nullptr;
+  ~GraphBuild() {
+    if (top) cudaGraphDestroy(top);
+  }
+};
+
+template <typename... A>
+cudaError_t add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, int ndep, void (*fn)(A...),
+                       dim3 grid, dim3 block, void** args) {
+  cudaKernelNodeParams kp = {};
+  kp.func = reinterpret_cast<void*>(fn);
+  kp.gridDim = grid;
+  kp.blockDim = block;
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  return cudaGraphAddKernelNode(node, g, dep, ndep, &kp);
+}
+
+cudaError_t add_cond(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, int ndep,
+                     cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned size,
+                     cudaGraph_t* bodies) {
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = size;
+  cudaError_t e = cudaGraphAddNode(node, g, dep, nullptr, ndep, &p);
+  if (e == cudaSuccess)
+    for (unsigned q = 0; q < size; ++q) bodies[q] = p.conditional.phGraph_out[q];
+  return e;
+}
+
+// the branch of one lane: the queue loop around one wavelength's stages
+cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const Sweep& s, cudaGraph_t top,
+                              JobCtl* jc, const LamParams* lps, const SweepDst* d) {
+  auto& gr = L.graphs;
+  SweepCtl* sc = L.swctl.as<SweepCtl>();
+  LamParams* lpd = L.lp_dev.as<LamParams>();
+  cudaGraphConditionalHandle hq;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&hq, top, 0, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphNode_t first, loop;
+  void* a_next[] = {&jc, &sc, &lps, &lpd, &hq};
+  if ((e = add_kernel(&first, top, nullptr, 0, k_sw_next, 1, 32, a_next)) != cudaSuccess) return e;
+  cudaGraph_t body;
+  if ((e = add_cond(&loop, top, &first, 1, hq, cudaGraphCondTypeWhile, 1, &body)) != cudaSuccess) return e;
+  cudaGraphNode_t n0, n1, n2, nst, last;
+  if ((e = cudaGraphAddChildGraphNode(&n0, body, nullptr, 0, gr.graph[0])) != cudaSuccess) return e;
+  if ((e = cudaGraphAddChildGraphNode(&n1, body, &n0, 1, gr.graph[1])) != cudaSuccess) return e;
+  const bool f64 = c.precision == MNPBEM_FP64;
+  const GJWork<float>& g32 = L.gj32;
+  const GJWork<double>& g64 = L.gj64;
+  const int* sgj = f64 ? g64.status.as<int>() : g32.status.as<int>();
+  const int* sgji = f64 ? (g64.inner ? g64.inner->status.as<int>() : nullptr)
+                        : (g32.inner ? g32.inner->status.as<int>() : nullptr);
+  const int* slu = L.lu_status.as<int>();
+  const int* stc = (L.tc.err.ptr && L.tc.err_cleared) ? L.tc.err.as<int>() : nullptr;
+  void* a_st[] = {&sc, &sgj, &sgji, &slu, &stc, &d};
+  if ((e = add_kernel(&nst, body, &n1, 1, k_sw_status, 1, 32, a_st)) != cudaSuccess) return e;
+  if ((e = cudaGraphAddChildGraphNode(&n2, body, &nst, 1, gr.graph[2])) != cudaSuccess) return e;
+  const bool refine = c.precision == MNPBEM_MIXED && s.ref.maxit > 0;
+  cudaGraphConditionalHandle hr;
+  if ((e = cudaGraphConditionalHandleCreate(&hr, body, 0, 0)) != cudaSuccess) return e;
+  int run = refine ? 1 : 0;
+  cudaGraphNode_t ni;
+  void* a_init[] = {&sc, &hr, &run, &d};
+  if ((e = add_kernel(&ni, body, &n2, 1, k_ref_init, 1, 32, a_init)) != cudaSuccess) return e;
+  last = ni;
+  if (refine) {
+    cudaGraphNode_t rl;
+    cudaGraph_t rbody;
+    if ((e = add_cond(&rl, body, &ni, 1, hr, cudaGraphCondTypeWhile, 1, &rbody)) != cudaSuccess) return e;
+    cudaGraphConditionalHandle hs;
+    if ((e = cudaGraphConditionalHandleCreate(&hs, rbody, 0, 0)) != cudaSuccess) return e;
+    double dsw = DS_SWITCH;
+    cudaGraphNode_t pk, sw, dc;
+    void* a_pick[] = {&sc, &hs, &dsw};
+    if ((e = add_kernel(&pk, rbody, nullptr, 0, k_ref_pick, 1, 32, a_pick)) != cudaSuccess) return e;
+    cudaGraph_t sb[3];
+    if ((e = add_cond(&sw, rbody, &pk, 1, hs, cudaGraphCondTypeSwitch, 3, sb)) != cudaSuccess) return e;
+    const int stage_of[3] = {STEP_FP32, STEP_DS, STEP_INCR};
+    for (int q = 0; q < 3; ++q) {
+      cudaGraphNode_t cn;
+      if ((e = cudaGraphAddChildGraphNode(&cn, sb[q], nullptr, 0, gr.graph[stage_of[q]])) != cudaSuccess) return e;
+    }
+    const double* hn = L.norms.as<double>();
+    double tol = s.ref.tol;
+    int maxit = s.ref.maxit;
+    void* a_dec[] = {&sc, &hn, &tol, &maxit, &hr, &d};
+    if ((e = add_kernel(&dc, rbody, &sw, 1, k_ref_decide, 1, 32, a_dec)) != cudaSuccess) return e;
+    last = rl;
+  }
+  cudaGraphNode_t n4, no, nn;
+  if ((e = cudaGraphAddChildGraphNode(&n4, body, &last, 1, gr.graph[4])) != cudaSuccess) return e;
+  Vec64 v = vec64(G, L, c.P);
+  const double2* x1 = v.x1;
+  const double2* x2 = v.x2;
+  const double* ob = L.outbuf.as<double>();
+  void* a_out[] = {&sc, &x1, &x2, &ob, &d};
+  const unsigned ob_blocks = (unsigned)std::min<int64_t>(cdiv_up(G->g.n * 4 * c.P, (int64_t)256), 2048);
+  if ((e = add_kernel(&no, body, &n4, 1, k_sw_out, ob_blocks, 256, a_out)) != cudaSuccess) return e;
+  void* a_nx[] = {&jc, &sc, &lps, &lpd, &hq};
+  return add_kernel(&nn, body, &no, 1, k_sw_next, 1, 32, a_nx);
+}
+
+// is a one-graph sweep usable for these jobs (captured stages, no profiling,
+// plane-wave excitation)?
+bool sweep_graph_ok(const std::vector<Job*>& jobs) {
+  for (const Job* j : jobs) {
+    const mnpbem_geom* G = j->G;
+    if (!G->sweep_graph || !G->use_graphs || G->prof.enabled || j->c.ext_pot || j->run.empty()) return false;
+    if (j->s.ref.maxit > 1000) return false;
+    for (const Lane* L : j->run)
+      for (int q = 0; q < NSTAGES; ++q) {
+        if ((q == 3 || q == 5 || q == 6) && j->c.precision != MNPBEM_MIXED) continue;
+        if (!L->graphs.graph[q]) return false;
+      }
+  }
+  return true;
+}
+
+// per-job device buffers: wavelength parameters, control word, result slots
+struct SweepJobBufs {
+  SweepDst d = {};
+  SweepDst* dd = nullptr;       // device copy of d (the kernels' view; refreshed before every launch)
+  JobCtl* jc = nullptr;
+  LamParams* lps = nullptr;
+  double2* stage_x = nullptr;   // staging of host-side solution outputs
+  double* stage_r = nullptr;    // ext, sca, res
+  int* stage_i = nullptr;       // iters, status, nan
+  bool staged[6] = {};          // sig1, h1, sig2, h2, ext, sca copied back by the host
+};
+
+// the device address of a caller's buffer the graph's kernels may write:
+// device or managed memory, or page-locked host memory (mapped); NULL for
+// pageable host memory (then the results go through device staging)
+void* device_address(void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
+mnpbem_status sweep_bufs(Job& j, SweepJobBufs& b) {
+  mnpbem_geom* G = j.G;
+  const int nenei = j.s.nenei, P = j.c.P;
+  const int64_t n = G->g.n;
+  const mnpbem_solution* out = j.s.out;
+  const bool dev = out->outputs_on_device != 0;
+  const int64_t nx = (int64_t)nenei * n * P;
+  // host outputs go through device staging
+  const int64_t xcount = dev ? 0 : (out->sig1 ? nx : 0) + (out->h1 ? 3 * nx : 0) + (out->sig2 ? nx : 0) +
+                                    (out->h2 ? 3 * nx : 0);
+  const size_t bytes_lp = ((sizeof(LamParams) * nenei + 255) / 256) * 256;
+  MNP_TRY(G->sweep_lp.ensure(bytes_lp + 256 + sizeof(double2) * std::max<int64_t>(1, xcount)));
+  MNP_TRY(G->sweep_res.ensure(sizeof(double) * (size_t)nenei * (2 * P + 1) +
+                              sizeof(int) * ((size_t)nenei * (1 + LANE_NSTATUS) + 1) + 256));
+  char* base = G->sweep_lp.as<char>();
+  b.lps = reinterpret_cast<LamParams*>(base);
+  b.jc = reinterpret_cast<JobCtl*>(base + bytes_lp);
+  b.dd = reinterpret_cast<SweepDst*>(base + bytes_lp + 64);
+  b.stage_x = reinterpret_cast<double2*>(base + bytes_lp + 256);
+  b.stage_r = G->sweep_res.as<double>();
+  b.stage_i = reinterpret_cast<int*>(b.stage_r + (size_t)nenei * (2 * P + 1));
+  SweepDst& d = b.d;
+  d.n = n;
+  d.P = P;
+  double2* xs = b.stage_x;
+  auto place = [&](double* user, int64_t cnt, int slot) -> double2* {
+    if (!user) return nullptr;
+    if (dev) return reinterpret_cast<double2*>(user);
+    if (void* da = device_address(user)) return reinterpret_cast<double2*>(da);
+    b.staged[slot] = true;
+    double2* r = xs;
+    xs += cnt;
+    return r;
+  };
+  d.sig1 = place(out->sig1, nx, 0);
+  d.h1 = place(out->h1, 3 * nx, 1);
+  d.sig2 = place(out->sig2, nx, 2);
+  d.h2 = place(out->h2, 3 * nx, 3);
+  auto place_r = [&](double* user, double* stage, int slot) -> double* {
+    if (!user) return nullptr;
+    if (dev) return user;
+    if (void* da = device_address(user)) return static_cast<double*>(da);
+    b.staged[slot] = true;
+    return stage;
+  };
+  d.ext = place_r(out->ext, b.stage_r, 4);
+  d.sca = place_r(out->sca, b.stage_r + (size_t)nenei * P, 5);
+  d.res = b.stage_r + (size_t)nenei * 2 * P;
+  d.iters = b.stage_i;
+  d.status = b.stage_i + nenei;
+  d.nan = b.stage_i + (size_t)nenei * (1 + LANE_NSTATUS);
+  return MNPBEM_OK;
+}
+
+// the host's part after the graph: outputs to host buffers, refinement
+// counts, status checks (the checks of check_pivots per wavelength)
+mnpbem_status sweep_finish(Job& j, SweepJobBufs& b, int w0) {
+  mnpbem_geom* G = j.G;
+  const int nenei = j.s.nenei, P = j.c.P;
+  const int64_t n = G->g.n;
+  mnpbem_solution* out = j.s.out;
+  std::vector<int> iv((size_t)nenei * (1 + LANE_NSTATUS) + 1);
+  std::vector<double> rv((size_t)nenei * (2 * P + 1));
+  MNP_CUDA(cudaMemcpy(iv.data(), b.stage_i, sizeof(int) * iv.size(), cudaMemcpyDeviceToHost));
+  MNP_CUDA(cudaMemcpy(rv.data(), b.stage_r, sizeof(double) * rv.size(), cudaMemcpyDeviceToHost));
+  if (iv.back()) {
+    set_error("refinement produced NaN");
+    return MNPBEM_ERR_NOT_CONVERGED;
+  }
+  Lane& L0 = *j.run[0];
+  for (int w = w0; w < nenei; ++w) {
+    memcpy(L0.status_host, &iv[(size_t)nenei + (size_t)w * LANE_NSTATUS], sizeof(int) * LANE_NSTATUS);
+    MNP_TRY(check_pivots(L0, j.c.precision));
+  }
+  const int64_t nx = (int64_t)nenei * n * P;
+  const size_t skip = (size_t)w0 * n * P;   // wavelengths solved before the graph are already written
+  auto back = [&](double* user, const double2* stage, int width, int slot) -> mnpbem_status {
+    if (!user || !b.staged[slot] || !stage) return MNPBEM_OK;
+    const size_t off = skip * width;
+    MNP_CUDA(cudaMemcpy(reinterpret_cast<double2*>(user) + off, stage + off,
+                        sizeof(double2) * ((size_t)nx * width - off), cudaMemcpyDeviceToHost));
+    return MNPBEM_OK;
+  };
+  MNP_TRY(back(out->sig1, b.d.sig1, 1, 0));
+  MNP_TRY(back(out->h1, b.d.h1, 3, 1));
+  MNP_TRY(back(out->sig2, b.d.sig2, 1, 2));
+  MNP_TRY(back(out->h2, b.d.h2, 3, 3));
+  for (int w = w0; w < nenei; ++w) {
+    if (out->ext && b.staged[4]) memcpy(out->ext + (size_t)w * P, &rv[(size_t)w * P], sizeof(double) * P);
+    if (out->sca && b.staged[5]) memcpy(out->sca + (size_t)w * P, &rv[(size_t)(nenei + w) * P], sizeof(double) * P);
+    if (out->ir_iters) out->ir_iters[w] = iv[w];
+    if (out->ir_resid) out->ir_resid[w] = rv[(size_t)nenei * 2 * P + w];
+  }
+  return MNPBEM_OK;
+}
+
+// the remaining wavelengths of every job as one graph launch; returns
+// MNPBEM_ERR_UNSUPPORTED (nothing launched) when the graph cannot be built
+mnpbem_status jobs_graph(std::vector<Job*>& jobs) {
+  if (!sweep_graph_ok(jobs)) return MNPBEM_ERR_UNSUPPORTED;
+  bool work = false;
+  for (const Job* j : jobs) work = work || j->next < j->s.nenei;
+  if (!work) return MNPBEM_OK;
+  // job buffers: one set per handle, so one job per handle
+  for (size_t a = 0; a < jobs.size(); ++a)
+    for (size_t b2 = a + 1; b2 < jobs.size(); ++b2)
+      if (jobs[a]->G == jobs[b2]->G) return MNPBEM_ERR_UNSUPPORTED;
+  std::vector<SweepJobBufs> bufs(jobs.size());
+  std::vector<int> w0(jobs.size());
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    Job& j = *jobs[q];
+    mnpbem_geom* G = j.G;
+    ProfBind pb_(&G->prof);
+    w0[q] = j.next;
+    MNP_TRY(sweep_bufs(j, bufs[q]));
+    for (Lane* L : j.run) MNP_TRY(L->swctl.ensure(sizeof(SweepCtl)));
+    // parameters of every wavelength, the queue start, zeroed slots
+    for (int w = 0; w < j.s.nenei; ++w)
+      fill_lp(G->lp_ring[w], j.s.enei[w], j.s.eps + 2 * (size_t)j.s.nmed * w, j.s.nmed, j.s.medium, 0);
+    MNP_CUDA(cudaMemcpyAsync(bufs[q].lps, G->lp_ring, sizeof(LamParams) * j.s.nenei, cudaMemcpyHostToDevice,
+                             G->st));
+    JobCtl jc{j.next, j.s.nenei};
+    MNP_CUDA(cudaMemcpyAsync(bufs[q].jc, &jc, sizeof(JobCtl), cudaMemcpyHostToDevice, G->st));
+    MNP_CUDA(cudaMemcpyAsync(bufs[q].dd, &bufs[q].d, sizeof(SweepDst), cudaMemcpyHostToDevice, G->st));
+    MNP_CUDA(cudaMemsetAsync(G->sweep_res.ptr, 0, G->sweep_res.bytes, G->st));
+    MNP_CUDA(cudaStreamSynchronize(G->st));   // jc lives on this stack frame
+  }
+  // build (or reuse, for a single job on an unchanged handle) the graph
+  Job& j0 = *jobs[0];
+  mnpbem_geom* G0 = j0.G;
+  uint64_t key = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) { key = (key ^ v) * 1099511628211ull; };
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    const Job& j = *jobs[q];
+    mix((uint64_t)(uintptr_t)j.G);
+    mix((uint64_t)j.c.precision);
+    mix((uint64_t)j.c.P);
+    mix((uint64_t)j.s.ref.maxit);
+    uint64_t tb;
+    memcpy(&tb, &j.s.ref.tol, sizeof(tb));
+    mix(tb);
+    for (const void* ptr : {(const void*)bufs[q].dd, (const void*)bufs[q].lps, (const void*)bufs[q].jc})
+      mix((uint64_t)(uintptr_t)ptr);
+    for (const Lane* L : j.run) {
+      mix((uint64_t)(uintptr_t)L);
+      mix(L->graphs.sig);
+      for (int s = 0; s < NSTAGES; ++s) mix((uint64_t)(uintptr_t)L->graphs.graph[s]);
+    }
+  }
+  cudaGraphExec_t exec = nullptr;
+  const bool cache = jobs.size() == 1;
+  if (cache && G0->sweep_exec && G0->sweep_key == key) {
+    exec = G0->sweep_exec;
+  } else {
+    GraphBuild gb;
+    cudaError_t e = cudaGraphCreate(&gb.top, 0);
+    for (size_t q = 0; q < jobs.size() && e == cudaSuccess; ++q)
+      for (Lane* L : jobs[q]->run) {
+        e = build_lane_branch(jobs[q]->G, *L, jobs[q]->c, jobs[q]->s, gb.top, bufs[q].jc, bufs[q].lps, bufs[q].dd);
+        if (e != cudaSuccess) break;
+      }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, gb.top, 0);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      for (Job* j : jobs) {   // the host scheduler from now on
+        j->G->sweep_graph = false;
+        j->G->sweep_err = (int)e;
+      }
+      return MNPBEM_ERR_UNSUPPORTED;
+    }
+    if (cache) {
+      if (G0->sweep_exec) cudaGraphExecDestroy(G0->sweep_exec);
+      G0->sweep_exec = exec;
+      G0->sweep_key = key;
+    }
+  }
+  // every lane's stream has finished its earlier work; the graph runs on the
+  // first handle's stream after all of them
+  cudaEvent_t ev;
+  MNP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } eg{ev};
+  for (Job* j : jobs)
+    for (Lane* L : j->run) {
+      MNP_CUDA(cudaEventRecord(ev, L->st));
+      MNP_CUDA(cudaStreamWaitEvent(G0->st, ev, 0));
+    }
+  const cudaError_t le = cudaGraphLaunch(exec, G0->st);
+  const cudaError_t se = le == cudaSuccess ? cudaStreamSynchronize(G0->st) : le;
+  if (!cache) cudaGraphExecDestroy(exec);
+  MNP_CUDA(se);
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    jobs[q]->next = jobs[q]->s.nenei;
+    ++jobs[q]->G->sweep_runs;
+    ProfBind pb_(&jobs[q]->G->prof);
+    MNP_TRY(sweep_finish(*jobs[q], bufs[q], w0[q]));
+  }
+  return MNPBEM_OK;
+}
+
 // join (the handle's stream waits for every lane), synchronise, read the
 // pivot and tensor-core status words
 mnpbem_status job_finish(Job& j, bool failed) {
@@ -1825,7 +2324,8 @@ mnpbem_status run_jobs(std::vector<Job>& jobs) {
   if (st == MNPBEM_OK) {
     std::vector<Job*> js;
     for (Job& j : jobs) js.push_back(&j);
-    st = jobs_poll(js);
+    st = jobs_graph(js);
+    if (st == MNPBEM_ERR_UNSUPPORTED) st = jobs_poll(js);
   }
   if (st != MNPBEM_OK) {
     const std::string keep = get_error();
