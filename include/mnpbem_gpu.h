@@ -180,8 +180,10 @@ typedef struct mnpbem_job {
 } mnpbem_job;
 
 /* Several independent sweeps (e.g. particles of uneven size, each its own
- * handle) solved together: every handle's lanes are fed by one scheduler, so
- * the small particles' wavelengths fill the GPU while the large ones run.
+ * handle) solved together: every handle's lanes are branches of one CUDA
+ * graph whose device-side queues hand out each handle's wavelengths and whose
+ * refinement decisions are taken on the device ("sweep_graph" option), so the
+ * small particles' wavelengths fill the GPU while the large ones run.
  * Same results as one mnpbem_solve per job.  The handles must be distinct and
  * on one device.  The reference has no batch call: its user code loops over
  * particles and wavelengths (Demo/planewave/ret/demospecret*.m).             */
