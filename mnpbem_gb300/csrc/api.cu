@@ -1846,6 +1846,7 @@ struct SweepDst {
   double* res;                      // [w]
   int* status;                      // [w][LANE_NSTATUS]
   int* nan;                         // set when a refinement step produced NaN
+  unsigned long long* stages;       // [NSTAGES] stage runs (the launch accounting of the replays)
   int64_t n;
   int P;
 };
@@ -1866,6 +1867,10 @@ __global__ void k_sw_next(JobCtl* jc, SweepCtl* sc, const LamParams* lps, LamPar
 __global__ void k_sw_status(const SweepCtl* sc, const int* gj, const int* gji, const int* lu, const int* tce,
                             const SweepDst* dp) {
   if (threadIdx.x) return;
+  atomicAdd(dp->stages + 0, 1ull);
+  atomicAdd(dp->stages + 1, 1ull);
+  atomicAdd(dp->stages + 2, 1ull);
+  atomicAdd(dp->stages + 4, 1ull);
   int* o = dp->status + (int64_t)sc->w * LANE_NSTATUS;
   for (int q = 0; q < LANE_NSTATUS; ++q) o[q] = 0;
   if (gj) { o[0] = gj[0]; o[1] = gj[1]; }
@@ -1888,12 +1893,13 @@ __global__ void k_ref_init(SweepCtl* sc, cudaGraphConditionalHandle h, int run, 
 
 // next_step(): FP32 first, the double-single step once the FP32 residual is
 // small (or after three steps), then incremental steps; body index 0 / 1 / 2
-__global__ void k_ref_pick(SweepCtl* sc, cudaGraphConditionalHandle h, double ds_switch) {
+__global__ void k_ref_pick(SweepCtl* sc, cudaGraphConditionalHandle h, double ds_switch, const SweepDst* dp) {
   if (threadIdx.x) return;
   int idx = 2;
   if (sc->iters == 0) idx = 0;
   else if (!sc->ds_done && (sc->res <= ds_switch || sc->iters >= 3)) idx = 1;
   sc->kind = idx;
+  atomicAdd(dp->stages + (idx == 0 ? STEP_FP32 : idx == 1 ? STEP_DS : STEP_INCR), 1ull);
   cudaGraphSetConditional(h, (unsigned)idx);
 }
 
@@ -2001,8 +2007,9 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
   if ((e = add_kernel(&nst, body, &n1, 1, k_sw_status, 1, 32, a_st)) != cudaSuccess) return e;
   if ((e = cudaGraphAddChildGraphNode(&n2, body, &nst, 1, gr.graph[2])) != cudaSuccess) return e;
   const bool refine = c.precision == MNPBEM_MIXED && s.ref.maxit > 0;
-  cudaGraphConditionalHandle hr;
-  if ((e = cudaGraphConditionalHandleCreate(&hr, body, 0, 0)) != cudaSuccess) return e;
+  // a handle must belong to a conditional node: created only for the loop
+  cudaGraphConditionalHandle hr = 0;
+  if (refine && (e = cudaGraphConditionalHandleCreate(&hr, body, 0, 0)) != cudaSuccess) return e;
   int run = refine ? 1 : 0;
   cudaGraphNode_t ni;
   void* a_init[] = {&sc, &hr, &run, &d};
@@ -2016,7 +2023,7 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
     if ((e = cudaGraphConditionalHandleCreate(&hs, rbody, 0, 0)) != cudaSuccess) return e;
     double dsw = DS_SWITCH;
     cudaGraphNode_t pk, sw, dc;
-    void* a_pick[] = {&sc, &hs, &dsw};
+    void* a_pick[] = {&sc, &hs, &dsw, &d};
     if ((e = add_kernel(&pk, rbody, nullptr, 0, k_ref_pick, 1, 32, a_pick)) != cudaSuccess) return e;
     cudaGraph_t sb[3];
     if ((e = add_cond(&sw, rbody, &pk, 1, hs, cudaGraphCondTypeSwitch, 3, sb)) != cudaSuccess) return e;
@@ -2101,7 +2108,7 @@ mnpbem_status sweep_bufs(Job& j, SweepJobBufs& b) {
   const size_t bytes_lp = ((sizeof(LamParams) * nenei + 255) / 256) * 256;
   MNP_TRY(G->sweep_lp.ensure(bytes_lp + 256 + sizeof(double2) * std::max<int64_t>(1, xcount)));
   MNP_TRY(G->sweep_res.ensure(sizeof(double) * (size_t)nenei * (2 * P + 1) +
-                              sizeof(int) * ((size_t)nenei * (1 + LANE_NSTATUS) + 1) + 256));
+                              sizeof(int) * ((size_t)nenei * (1 + LANE_NSTATUS) + 1) + 512));
   char* base = G->sweep_lp.as<char>();
   b.lps = reinterpret_cast<LamParams*>(base);
   b.jc = reinterpret_cast<JobCtl*>(base + bytes_lp);
@@ -2139,6 +2146,8 @@ mnpbem_status sweep_bufs(Job& j, SweepJobBufs& b) {
   d.iters = b.stage_i;
   d.status = b.stage_i + nenei;
   d.nan = b.stage_i + (size_t)nenei * (1 + LANE_NSTATUS);
+  const size_t soff = (((size_t)nenei * (1 + LANE_NSTATUS) + 1) * sizeof(int) + 7) / 8 * 8;
+  d.stages = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(b.stage_i) + soff);
   return MNPBEM_OK;
 }
 
@@ -2158,6 +2167,21 @@ mnpbem_status sweep_finish(Job& j, SweepJobBufs& b, int w0) {
     return MNPBEM_ERR_NOT_CONVERGED;
   }
   Lane& L0 = *j.run[0];
+  // launch accounting: every stage run as a replay of lane 0's record, plus
+  // the graph's control kernels (4 per wavelength, 2 per refinement step)
+  {
+    unsigned long long cnt[NSTAGES];
+    MNP_CUDA(cudaMemcpy(cnt, b.d.stages, sizeof(cnt), cudaMemcpyDeviceToHost));
+    Profiler& pr = G->prof;
+    for (int q = 0; q < NSTAGES; ++q)
+      for (int ph = 0; ph < PH_COUNT; ++ph) {
+        const PhaseAcc& r = L0.graphs.rec[q].counts[ph];
+        pr.acc[ph].launches += (int64_t)cnt[q] * r.launches;
+        pr.acc[ph].flops += (double)cnt[q] * r.flops;
+        pr.acc[ph].bytes += (double)cnt[q] * r.bytes;
+      }
+    for (int w = w0; w < nenei; ++w) pr.acc[PH_ELEMWISE].launches += 4 + 2 * (int64_t)iv[w];
+  }
   for (int w = w0; w < nenei; ++w) {
     memcpy(L0.status_host, &iv[(size_t)nenei + (size_t)w * LANE_NSTATUS], sizeof(int) * LANE_NSTATUS);
     MNP_TRY(check_pivots(L0, j.c.precision));

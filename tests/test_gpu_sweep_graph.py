@@ -64,3 +64,40 @@ def test_batch_graph_bit_identical():
         for k in ("ext", "sca", "ir_iters"):
             assert np.array_equal(ra[k], rb[k]), k
         assert np.allclose(ra["ir_resid"], rb["ir_resid"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("iters", [0, 1, 2])
+def test_sweep_graph_refinement_limits(iters):
+    """the device-side stop rule at small refinement limits (0: no loop)"""
+    cp = sphere(256)
+    enei = np.linspace(500.0, 700.0, 7)
+    res = []
+    for graph in (True, False):
+        bem = m.bemsolver(cp, m.bemoptions(precision="mixed", lanes=2))
+        bem.set_option("sweep_graph", 1 if graph else 0)
+        bem.refine_iters = iters
+        exc = m.planewave([[1, 0, 0]], [[0, 0, 1]])
+        res.append(bem.spectrum(exc, enei, fields=True))
+    a, b = res
+    for k in ("ext", "sca", "sig2", "h2", "ir_iters"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.all(a["ir_iters"] <= max(iters, 0))
+
+
+def test_sweep_graph_page_locked_outputs():
+    """results written by the graph straight into page-locked host buffers
+    equal those staged for pageable buffers"""
+    torch = pytest.importorskip("torch")
+    cp = sphere(256)
+    enei = np.linspace(500.0, 700.0, 7)
+    exc = m.planewave([[1, 0, 0]], [[0, 0, 1]])
+    bem = m.bemsolver(cp, m.bemoptions(precision="mixed", lanes=2))
+    ref = bem.spectrum(exc, enei, fields=True)
+    n = cp.n
+    out = {k: torch.zeros(shape, dtype=dt, pin_memory=True).numpy() for k, shape, dt in (
+        ("ext", (7, 1), torch.float64), ("sca", (7, 1), torch.float64),
+        ("sig2", (7, n, 1), torch.complex128), ("h2", (7, n, 3, 1), torch.complex128))}
+    got = bem.spectrum(exc, enei, fields=True, out=out)
+    assert bem.stat("sweep_graph_runs") > 0
+    for k in ("ext", "sca", "sig2", "h2"):
+        assert np.array_equal(np.asarray(got[k]).reshape(ref[k].shape), ref[k]), k
