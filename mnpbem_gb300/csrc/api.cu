@@ -1851,10 +1851,14 @@ struct SweepDst {
   int P;
 };
 
+// the next wavelength of the job's queue for this lane; the queue stops for
+// the lane once a bounded tensor-core wait has expired or a refinement step
+// produced NaN (the host reports either after the graph)
 __global__ void k_sw_next(JobCtl* jc, SweepCtl* sc, const LamParams* lps, LamParams* lp,
-                          cudaGraphConditionalHandle h) {
+                          cudaGraphConditionalHandle h, const int* tce, const SweepDst* dp) {
   if (threadIdx.x) return;
-  const int w = atomicAdd(&jc->next, 1);
+  const bool failed = (tce && *(volatile const int*)tce) || *(volatile const int*)dp->nan;
+  const int w = failed ? jc->nenei : atomicAdd(&jc->next, 1);
   const bool go = w < jc->nenei;
   if (go) {
     sc->w = w;
@@ -1987,8 +1991,9 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
   cudaGraphConditionalHandle hq;
   cudaError_t e = cudaGraphConditionalHandleCreate(&hq, top, 0, 0);
   if (e != cudaSuccess) return e;
+  const int* stc = (L.tc.err.ptr && L.tc.err_cleared) ? L.tc.err.as<int>() : nullptr;
   cudaGraphNode_t first, loop;
-  void* a_next[] = {&jc, &sc, &lps, &lpd, &hq};
+  void* a_next[] = {&jc, &sc, &lps, &lpd, &hq, &stc, &d};
   if ((e = add_kernel(&first, top, nullptr, 0, k_sw_next, 1, 32, a_next)) != cudaSuccess) return e;
   cudaGraph_t body;
   if ((e = add_cond(&loop, top, &first, 1, hq, cudaGraphCondTypeWhile, 1, &body)) != cudaSuccess) return e;
@@ -2002,7 +2007,6 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
   const int* sgji = f64 ? (g64.inner ? g64.inner->status.as<int>() : nullptr)
                         : (g32.inner ? g32.inner->status.as<int>() : nullptr);
   const int* slu = L.lu_status.as<int>();
-  const int* stc = (L.tc.err.ptr && L.tc.err_cleared) ? L.tc.err.as<int>() : nullptr;
   void* a_st[] = {&sc, &sgj, &sgji, &slu, &stc, &d};
   if ((e = add_kernel(&nst, body, &n1, 1, k_sw_status, 1, 32, a_st)) != cudaSuccess) return e;
   if ((e = cudaGraphAddChildGraphNode(&n2, body, &nst, 1, gr.graph[2])) != cudaSuccess) return e;
@@ -2048,7 +2052,7 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
   void* a_out[] = {&sc, &x1, &x2, &ob, &d};
   const unsigned ob_blocks = (unsigned)std::min<int64_t>(cdiv_up(G->g.n * 4 * c.P, (int64_t)256), 2048);
   if ((e = add_kernel(&no, body, &n4, 1, k_sw_out, ob_blocks, 256, a_out)) != cudaSuccess) return e;
-  void* a_nx[] = {&jc, &sc, &lps, &lpd, &hq};
+  void* a_nx[] = {&jc, &sc, &lps, &lpd, &hq, &stc, &d};
   return add_kernel(&nn, body, &no, 1, k_sw_next, 1, 32, a_nx);
 }
 

@@ -1,6 +1,7 @@
 // Excitation, the bemret solution chain, the FP64 residual of the full BEM
 // operator, and the far-field cross sections.
 #include "bem.cuh"
+#include "farfield.cuh"
 #include "dense.cuh"
 #include "profile.cuh"
 
@@ -434,81 +435,20 @@ template void launch_sigma_add<double>(int64_t, double2*, const double2*, int64_
                                        const LamParams*, cudaStream_t);
 
 // ------------------------------------------------------------- far fields
+// charges and currents packed per face: [n][4P] of (sig | h) for each side
+struct PackedSrc {
+  const double2 *x1, *x2;
+  int P;
+  __device__ double2 sig(int side, int64_t j, int p) const { return (side ? x2 : x1)[j * 4 * P + p]; }
+  __device__ double2 h(int side, int64_t j, int c, int p) const { return (side ? x2 : x1)[j * 4 * P + P + c * P + p]; }
+};
+
 __global__ void __launch_bounds__(256) k_farfield(FaceData f, int P, const double2* x1,
                                                   const double2* x2, const double* dirs,
                                                   const LamParams* lp, double2* fields) {
   const int d = blockIdx.x;
-  const double2 k = lp->kexc;
-  const double k0 = lp->k0;
-  const double dx = dirs[3 * d], dy = dirs[3 * d + 1], dz = dirs[3 * d + 2];
-  double2 Ps[MAXPOL], Ph[3][MAXPOL];
-  for (int p = 0; p < MAXPOL; ++p) {
-    Ps[p] = make_double2(0, 0);
-    for (int c = 0; c < 3; ++c) Ph[c][p] = make_double2(0, 0);
-  }
-  const int W = 4 * P;
-  for (int64_t j = threadIdx.x; j < f.n; j += blockDim.x) {
-    bool in1 = f.exc_in[j] != 0, in2 = f.exc_out[j] != 0;
-    if (!in1 && !in2) continue;
-    double s = dx * f.pos[3 * j] + dy * f.pos[3 * j + 1] + dz * f.pos[3 * j + 2];
-    // exp(-i k s) * area
-    double sn, cs;
-    sincos(k.x * s, &sn, &cs);
-    double ee = exp(k.y * s) * f.area[j];
-    double2 ph = make_double2(ee * cs, -ee * sn);
-    for (int p = 0; p < P; ++p) {
-      double2 sv = make_double2(0, 0);
-      double2 hv[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-      if (in1) {
-        sv = cadd(sv, x1[j * W + p]);
-        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], x1[j * W + P + c * P + p]);
-      }
-      if (in2) {
-        sv = cadd(sv, x2[j * W + p]);
-        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], x2[j * W + P + c * P + p]);
-      }
-      cfma(Ps[p], ph, sv);
-      for (int c = 0; c < 3; ++c) cfma(Ph[c][p], ph, hv[c]);
-    }
-  }
-  // block reduction of 4P complex accumulators
-  __shared__ double2 red[8][4 * MAXPOL];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int p = 0; p < P; ++p) {
-    for (int q = 0; q < 4; ++q) {
-      double2 v = q == 0 ? Ps[p] : Ph[q - 1][p];
-      for (int o = 16; o; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-      }
-      if (lane == 0) red[wid][q * MAXPOL + p] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nw = blockDim.x / 32;
-    double2 ik = make_double2(-k.y, k.x);
-    double2 ik0 = make_double2(0, k0);
-    double dv[3] = {dx, dy, dz};
-    for (int p = 0; p < P; ++p) {
-      double2 S[4];
-      for (int q = 0; q < 4; ++q) {
-        S[q] = make_double2(0, 0);
-        for (int w = 0; w < nw; ++w) S[q] = cadd(S[q], red[w][q * MAXPOL + p]);
-      }
-      double2 ph3[3] = {S[1], S[2], S[3]};
-      for (int c = 0; c < 3; ++c) {
-        double2 e = csub(cmul(ik0, ph3[c]), cmul(ik, cscale(S[0], dv[c])));
-        fields[((int64_t)d * 6 + c) * P + p] = e;
-      }
-      // h = ik dir x Ph
-      double2 cr[3];
-      cr[0] = csub(cscale(ph3[2], dv[1]), cscale(ph3[1], dv[2]));
-      cr[1] = csub(cscale(ph3[0], dv[2]), cscale(ph3[2], dv[0]));
-      cr[2] = csub(cscale(ph3[1], dv[0]), cscale(ph3[0], dv[1]));
-      for (int c = 0; c < 3; ++c) fields[((int64_t)d * 6 + 3 + c) * P + p] = cmul(ik, cr[c]);
-    }
-  }
+  farfield_dir<MAXPOL>(f.n, P, f.pos, f.area, f.exc_in, f.exc_out, PackedSrc{x1, x2, P}, dirs[3 * d],
+                       dirs[3 * d + 1], dirs[3 * d + 2], lp->kexc, lp->k0, d, fields);
 }
 
 void launch_farfield(const FaceData& f, int P, const double2* x1, const double2* x2,

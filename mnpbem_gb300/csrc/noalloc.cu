@@ -28,6 +28,7 @@
 #include <complex>
 
 #include "bem.cuh"
+#include "farfield.cuh"
 
 namespace mnpbem {
 
@@ -38,8 +39,16 @@ static __device__ __align__(256) double2 g_noalloc_fields[NOALLOC_MAX_DIRS * 6 *
 
 
 // Far fields of one direction per block, inputs in the public solution layout
-// (sig [n][P], h [n][3][P]); direction d < P is dir[d], else inf_nvec[d - P].
-// Same arithmetic as the far-field kernel of the solve.
+// (sig [n][P], h [n][3][P] per side); direction d < P is dir[d], else
+// inf_nvec[d - P].  The far-field routine of the solve (farfield.cuh) with
+// this layout.
+struct SplitSrc {
+  const double2 *s1, *h1, *s2, *h2;
+  int P;
+  __device__ double2 sig(int side, int64_t j, int p) const { return (side ? s2 : s1)[j * P + p]; }
+  __device__ double2 h(int side, int64_t j, int c, int p) const { return (side ? h2 : h1)[(j * 3 + c) * P + p]; }
+};
+
 __global__ void __launch_bounds__(256) k_farfield_noalloc(
     int64_t n, int P, const double* __restrict__ pos, const double* __restrict__ area,
     const unsigned char* __restrict__ exc_in, const unsigned char* __restrict__ exc_out,
@@ -47,70 +56,9 @@ __global__ void __launch_bounds__(256) k_farfield_noalloc(
     const double2* __restrict__ h2, const double* __restrict__ dir, const double* __restrict__ inf_nvec,
     double2 k, double k0, double2* fields) {
   const int d = blockIdx.x;
-  const double* dv_ = d < P ? dir + 3 * d : inf_nvec + 3 * (d - P);
-  const double dx = dv_[0], dy = dv_[1], dz = dv_[2];
-  double2 Ps[NOALLOC_MAX_POL], Ph[3][NOALLOC_MAX_POL];
-  for (int p = 0; p < NOALLOC_MAX_POL; ++p) {
-    Ps[p] = make_double2(0, 0);
-    for (int c = 0; c < 3; ++c) Ph[c][p] = make_double2(0, 0);
-  }
-  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-    const bool in1 = exc_in[j] != 0, in2 = exc_out[j] != 0;
-    if (!in1 && !in2) continue;
-    const double s = dx * pos[3 * j] + dy * pos[3 * j + 1] + dz * pos[3 * j + 2];
-    double sn, cs;
-    sincos(k.x * s, &sn, &cs);
-    const double ee = exp(k.y * s) * area[j];
-    const double2 ph = make_double2(ee * cs, -ee * sn);
-    for (int p = 0; p < P; ++p) {
-      double2 sv = make_double2(0, 0);
-      double2 hv[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-      if (in1) {
-        sv = cadd(sv, sig1[j * P + p]);
-        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], h1[(j * 3 + c) * P + p]);
-      }
-      if (in2) {
-        sv = cadd(sv, sig2[j * P + p]);
-        for (int c = 0; c < 3; ++c) hv[c] = cadd(hv[c], h2[(j * 3 + c) * P + p]);
-      }
-      cfma(Ps[p], ph, sv);
-      for (int c = 0; c < 3; ++c) cfma(Ph[c][p], ph, hv[c]);
-    }
-  }
-  __shared__ double2 red[8][4 * NOALLOC_MAX_POL];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int p = 0; p < P; ++p) {
-    for (int q = 0; q < 4; ++q) {
-      double2 v = q == 0 ? Ps[p] : Ph[q - 1][p];
-      for (int o = 16; o; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-      }
-      if (lane == 0) red[wid][q * NOALLOC_MAX_POL + p] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nw = blockDim.x / 32;
-    const double2 ik = make_double2(-k.y, k.x);
-    const double2 ik0 = make_double2(0, k0);
-    const double dv[3] = {dx, dy, dz};
-    for (int p = 0; p < P; ++p) {
-      double2 S[4];
-      for (int q = 0; q < 4; ++q) {
-        S[q] = make_double2(0, 0);
-        for (int w = 0; w < nw; ++w) S[q] = cadd(S[q], red[w][q * NOALLOC_MAX_POL + p]);
-      }
-      const double2 ph3[3] = {S[1], S[2], S[3]};
-      for (int c = 0; c < 3; ++c)
-        fields[((int64_t)d * 6 + c) * P + p] = csub(cmul(ik0, ph3[c]), cmul(ik, cscale(S[0], dv[c])));
-      double2 cr[3];
-      cr[0] = csub(cscale(ph3[2], dv[1]), cscale(ph3[1], dv[2]));
-      cr[1] = csub(cscale(ph3[0], dv[2]), cscale(ph3[2], dv[0]));
-      cr[2] = csub(cscale(ph3[1], dv[0]), cscale(ph3[0], dv[1]));
-      for (int c = 0; c < 3; ++c) fields[((int64_t)d * 6 + 3 + c) * P + p] = cmul(ik, cr[c]);
-    }
-  }
+  const double* dv = d < P ? dir + 3 * d : inf_nvec + 3 * (d - P);
+  farfield_dir<NOALLOC_MAX_POL>(n, P, pos, area, exc_in, exc_out, SplitSrc{sig1, h1, sig2, h2, P}, dv[0], dv[1],
+                                dv[2], k, k0, d, fields);
 }
 
 // device address of the scratch array in the current context, looked up on
