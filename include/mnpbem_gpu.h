@@ -514,6 +514,11 @@ MNPBEM_API mnpbem_status mnpbem_hm_lu(const mnpbem_hm* a, mnpbem_hm** out);
 /* X with X (L U) = b, lu from mnpbem_hm_lu (mex/hmatrsolve.cpp): key 'N'
  * both factors ('U' then 'L'), 'U' or 'L' one of them; options of b         */
 MNPBEM_API mnpbem_status mnpbem_hm_rsolve(const mnpbem_hm* b, const mnpbem_hm* lu, char key, mnpbem_hm** out);
+/* X with (L U) X = b, lu from mnpbem_hm_lu (mex/hmatlsolve.cpp): key 'N'
+ * both factors ('L' then 'U'), 'L' or 'U' one of them; options of b         */
+MNPBEM_API mnpbem_status mnpbem_hm_lsolve(const mnpbem_hm* b, const mnpbem_hm* lu, char key, mnpbem_hm** out);
+/* a b (mex/hmatmul2.cpp; mex/hlib/hmatrix.h operator*), options of a        */
+MNPBEM_API mnpbem_status mnpbem_hm_matmul(const mnpbem_hm* a, const mnpbem_hm* b, mnpbem_hm** out);
 /* inverse of a (mex/hmatinv.cpp; mex/hlib/hmatrix.h inv)                    */
 MNPBEM_API mnpbem_status mnpbem_hm_inv(const mnpbem_hm* a, mnpbem_hm** out);
 /* a + sign b, sign 1 or -1 (mex/hmatadd.cpp; @hmatrix/plus.m, minus.m)     */

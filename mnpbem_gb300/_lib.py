@@ -159,6 +159,9 @@ SIGNATURES = {
     "mnpbem_hm_rsolve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_hm_inv": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_lsolve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "mnpbem_hm_matmul": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_hm_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                      ctypes.POINTER(ctypes.c_void_p)]),
     "mnpbem_hm_scale": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char,

@@ -1268,6 +1268,22 @@ mnpbem_status h_rsolve_lu(Ctx& c, const HM& B, const HM& A, char key, HM& X) {
   return check_flags(c);
 }
 
+mnpbem_status h_lsolve_lu(Ctx& c, const HM& B, const HM& A, char key, HM& X) {
+  X.clear();
+  if (key == 'L' || key == 'N') MNP_TRY(lsolve_h(c, B, A, X, 0, 0, 'L'));
+  if (key == 'U' || key == 'N') {
+    const HM Bx = key == 'N' ? X : B;
+    if (key == 'U') X.clear();
+    MNP_TRY(lsolve_h(c, Bx, A, X, 0, 0, 'U'));
+  }
+  return check_flags(c);
+}
+
+mnpbem_status h_mul(Ctx& c, const HM& A, const HM& B, HM& C) {
+  MNP_TRY(hmul(c, opH(A), opH(B), 0, 0, 0, C));
+  return check_flags(c);
+}
+
 mnpbem_status h_inv(Ctx& c, const HM& A, HM& C) {
   MNP_TRY(inv_rec(c, A, 0, C));
   return check_flags(c);
@@ -1770,6 +1786,26 @@ MNPBEM_API mnpbem_status mnpbem_hm_rsolve(const mnpbem_hm* b, const mnpbem_hm* l
     return MNPBEM_ERR_INVALID_ARG;
   }
   return hm_result(b, out, [&](Ctx& c, HM& r) { return h_rsolve_lu(c, b->m, lu->m, key, r); });
+}
+
+MNPBEM_API mnpbem_status mnpbem_hm_lsolve(const mnpbem_hm* b, const mnpbem_hm* lu, char key, mnpbem_hm** out) {
+  MNP_TRY(hm_check(b, "mnpbem_hm_lsolve"));
+  MNP_TRY(hm_check(lu, "mnpbem_hm_lsolve"));
+  if ((key != 'N' && key != 'L' && key != 'U') || !same_tree(*b->c->t, *lu->c->t) || b->c->device != lu->c->device) {
+    set_error("mnpbem_hm_lsolve: key must be 'N', 'L' or 'U' and both H-matrices on one tree and device");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  return hm_result(b, out, [&](Ctx& c, HM& r) { return h_lsolve_lu(c, b->m, lu->m, key, r); });
+}
+
+MNPBEM_API mnpbem_status mnpbem_hm_matmul(const mnpbem_hm* a, const mnpbem_hm* b, mnpbem_hm** out) {
+  MNP_TRY(hm_check(a, "mnpbem_hm_matmul"));
+  MNP_TRY(hm_check(b, "mnpbem_hm_matmul"));
+  if (!same_tree(*a->c->t, *b->c->t) || a->c->device != b->c->device) {
+    set_error("mnpbem_hm_matmul: both H-matrices must be on one tree and device");
+    return MNPBEM_ERR_INVALID_ARG;
+  }
+  return hm_result(a, out, [&](Ctx& c, HM& r) { return h_mul(c, a->m, b->m, r); });
 }
 
 MNPBEM_API mnpbem_status mnpbem_hm_inv(const mnpbem_hm* a, mnpbem_hm** out) {

@@ -94,6 +94,10 @@ mnpbem_status check_flags(Ctx& c);
 mnpbem_status h_lu(Ctx& c, const HM& B, HM& A);
 // X (L U) = B for key 'N' ('U' then 'L'), or one factor for 'U' / 'L'
 mnpbem_status h_rsolve_lu(Ctx& c, const HM& B, const HM& A, char key, HM& X);
+// X with (L U) X = B for key 'N' ('L' then 'U'), or one factor for 'L' / 'U'
+mnpbem_status h_lsolve_lu(Ctx& c, const HM& B, const HM& A, char key, HM& X);
+// C = A B (hmatrix.h operator*, truncated with the options of c)
+mnpbem_status h_mul(Ctx& c, const HM& A, const HM& B, HM& C);
 mnpbem_status h_inv(Ctx& c, const HM& A, HM& C);
 mnpbem_status h_add(Ctx& c, const HM& A, const HM& B, HM& C);
 mnpbem_status h_neg(Ctx& c, const HM& A, HM& C);

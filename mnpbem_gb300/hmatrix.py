@@ -221,6 +221,14 @@ class hmatrix_gpu:
         """@hmatrix/rsolve.m: X with X (L U) = self"""
         return self._new(lambda h, *a: self.lib.mnpbem_hm_rsolve(h, lu.h, key.encode(), *a))
 
+    def lsolve(self, lu, key="N"):
+        """@hmatrix/lsolve.m: X with (L U) X = self"""
+        return self._new(lambda h, *a: self.lib.mnpbem_hm_lsolve(h, lu.h, key.encode(), *a))
+
+    def __matmul__(self, other):
+        """self * other of two H-matrices (@hmatrix/mtimes.m, hmatmul2)"""
+        return self._new(lambda h, *a: self.lib.mnpbem_hm_matmul(h, other.h, *a))
+
     def inv(self):
         return self._new(self.lib.mnpbem_hm_inv)
 

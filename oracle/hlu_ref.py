@@ -25,8 +25,9 @@ retarded solver.  Followed files:
 * ``mex/hlib/basemat.cpp:225-240`` -- inverse of a full leaf (LAPACK
   getrf / getri, i.e. with partial pivoting);
 * ``mex/hmatlu.cpp``, ``hmatrsolve.cpp`` (X (L U) = B: the 'U' then the 'L'
-  right solve), ``hmatsolve.cpp`` (L then U), ``hmatinv.cpp``,
-  ``hmatadd.cpp``; ``Greenfun/hmatrices/@hmatrix/private/mtimes1.m``
+  right solve), ``hmatlsolve.cpp`` ((L U) X = B: 'L' then 'U'),
+  ``hmatsolve.cpp`` (L then U), ``hmatinv.cpp``, ``hmatadd.cpp``,
+  ``hmatmul2.cpp`` (A B, hmatrix.h operator*); ``Greenfun/hmatrices/@hmatrix/private/mtimes1.m``
   (diagonal times H-matrix) and ``plus2.m``;
 * ``BEM/@bemretiter/private/initprecond.m:1-76`` ('hmat'), ``compress.m``
   (the preconditioner works with htol = max(op.htol), kmax = min(op.kmax))
@@ -470,6 +471,15 @@ class HArith:
             self.rsolve(B, A, X, 0, 0, "U")
         if key in ("L", "N"):
             self.rsolve(dict(X), A, X, 0, 0, "L")
+        return X
+
+    def lsolve_lu(self, B, A, key="N"):
+        """hmatlsolve.cpp: X with (L U) X = B"""
+        X = {}
+        if key in ("L", "N"):
+            self.lsolve(B, A, X, 0, 0, "L")
+        if key in ("U", "N"):
+            self.lsolve(dict(X) if key == "N" else B, A, X, 0, 0, "U")
         return X
 
     def solve_vec(self, A, b, i=0, uplo="L"):

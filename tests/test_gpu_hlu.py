@@ -191,3 +191,13 @@ def test_iterative_solve_with_hmat_preconditioner():
     assert bem2.info["flag"] == 0 and bem2.info["precond_enei"] == 600.0
     d2 = m.bemsolver(cp, m.bemoptions(precision="fp64")).mldivide(exc(cp, 650.0))
     assert rel(s2.sig2, d2.sig2) < 5e-4
+
+
+def test_lsolve_and_product_match_oracle(prob):
+    a = HL.HArith(prob["T"], 1e-6, 4)
+    lu_ref = a.lu(ora(prob, "G1"))
+    ref = a.lsolve_lu(ora(prob, "H1"), lu_ref)
+    lu = gpu(prob, "G1", 1e-6, 4).lu()
+    assert_blocks_match(gpu(prob, "H1", 1e-6, 4).lsolve(lu), ref, a)
+    refp = a.mul(ora(prob, "G1"), ora(prob, "H1"))
+    assert_blocks_match(gpu(prob, "G1", 1e-6, 4) @ gpu(prob, "H1", 1e-6, 4), refp, a)

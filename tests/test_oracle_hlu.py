@@ -105,3 +105,12 @@ def test_reference_options_truncate(prob):
     L, U = np.tril(F), np.triu(F, 1) + np.eye(n)
     e = rel(L @ U, G1c)
     assert 1e-12 < e < 1e-1
+
+
+def test_lsolve_and_product_exact_at_tight_truncation(prob):
+    h = HL.HArith(prob["T"], 1e-12, 100)
+    G1, G1c = prob["mats"]["G1"]
+    H1, H1c = prob["mats"]["H1"]
+    X = h.lsolve_lu(H1, h.lu(G1))
+    assert rel(G1c @ h.full(X), H1c) < 1e-11
+    assert rel(h.full(h.mul(G1, H1)), G1c @ H1c) < 1e-11
