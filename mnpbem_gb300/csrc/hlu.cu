@@ -480,9 +480,18 @@ mnpbem_status ctx_make(int device, std::shared_ptr<const Tree> t, double tol, in
   return MNPBEM_OK;
 }
 
+// hand the pool's free blocks beyond a small reserve back to the device (the
+// pool keeps freed blocks for reuse inside one operation; between operations
+// they would only be missing from the solver's own allocations)
+static void pool_trim(int device) {
+  DevRes* r = nullptr;
+  if (dev_res(device, r) == MNPBEM_OK && r->pool) cudaMemPoolTrimTo(r->pool, (size_t)256 << 20);
+}
+
 mnpbem_status check_flags(Ctx& c) {
   MNP_CUDA(cudaMemcpyAsync(c.host, c.dev, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
   MNP_CUDA(cudaStreamSynchronize(c.st));
+  pool_trim(c.device);
   if (c.host[1] & HL_ERR_PIVOT) {
     MNP_CUDA(cudaMemsetAsync(c.dev + 1, 0, sizeof(int), c.st));
     set_error("H-matrix arithmetic: zero pivot in the LU or the inverse of a leaf block");
