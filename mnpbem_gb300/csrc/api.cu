@@ -1413,22 +1413,31 @@ struct Refine {
 //               is far below the 1e-10 tolerance once dx is small.
 // The stopping test (||dx|| <= tol ||x||) counts only after the double-single
 // residual.  Relative residuals are measured against ||b|| of the last full one.
+// One definition of these rules serves the host scheduler (state in the Lane)
+// and the device-side decisions of a sweep graph (state in SweepCtl): S has
+// iters, ds_done, res and bnorm2; hn are the four norms a step leaves.
 constexpr double DS_SWITCH = 1e-3;
 constexpr int STEP_DS = 3, STEP_FP32 = 5, STEP_INCR = 6;
-int next_step(const Lane& L) {
-  if (L.iters == 0) return STEP_FP32;
-  if (!L.ds_done && (L.res <= DS_SWITCH || L.iters >= 3)) return STEP_DS;
+template <typename S>
+__host__ __device__ inline int refine_next_kind(const S& s) {
+  if (s.iters == 0) return STEP_FP32;
+  if (!s.ds_done && (s.res <= DS_SWITCH || s.iters >= 3)) return STEP_DS;
   return STEP_INCR;
 }
-void step_done(Lane& L, int kind, const double* hn) {
-  if (kind != STEP_INCR) L.bnorm2 = hn[1];
-  if (kind == STEP_DS) L.ds_done = true;
-  L.res = L.bnorm2 > 0 ? sqrt(hn[0] / L.bnorm2) : 0.0;
-  ++L.iters;
+template <typename S>
+__host__ __device__ inline void refine_step_done(S& s, int kind, const double* hn) {
+  if (kind != STEP_INCR) s.bnorm2 = hn[1];
+  if (kind == STEP_DS) s.ds_done = true;
+  s.res = s.bnorm2 > 0 ? sqrt(hn[0] / s.bnorm2) : 0.0;
+  ++s.iters;
 }
-bool step_converged(const Lane& L, const double* hn, double tol) {
-  return L.ds_done && sqrt(hn[2]) <= tol * sqrt(hn[3]);
+template <typename S>
+__host__ __device__ inline bool refine_converged(const S& s, const double* hn, double tol) {
+  return s.ds_done && sqrt(hn[2]) <= tol * sqrt(hn[3]);
 }
+int next_step(const Lane& L) { return refine_next_kind(L); }
+void step_done(Lane& L, int kind, const double* hn) { refine_step_done(L, kind, hn); }
+bool step_converged(const Lane& L, const double* hn, double tol) { return refine_converged(L, hn, tol); }
 void refine_reset(Lane& L) {
   L.iters = 0;
   L.res = -1.0;
@@ -1895,30 +1904,26 @@ __global__ void k_ref_init(SweepCtl* sc, cudaGraphConditionalHandle h, int run, 
   if (run) cudaGraphSetConditional(h, 1u);
 }
 
-// next_step(): FP32 first, the double-single step once the FP32 residual is
-// small (or after three steps), then incremental steps; body index 0 / 1 / 2
-__global__ void k_ref_pick(SweepCtl* sc, cudaGraphConditionalHandle h, double ds_switch, const SweepDst* dp) {
+// refine_next_kind(): FP32 first, the double-single step once the FP32
+// residual is small (or after three steps), then incremental steps; body
+// index 0 / 1 / 2
+__global__ void k_ref_pick(SweepCtl* sc, cudaGraphConditionalHandle h, const SweepDst* dp) {
   if (threadIdx.x) return;
-  int idx = 2;
-  if (sc->iters == 0) idx = 0;
-  else if (!sc->ds_done && (sc->res <= ds_switch || sc->iters >= 3)) idx = 1;
-  sc->kind = idx;
-  atomicAdd(dp->stages + (idx == 0 ? STEP_FP32 : idx == 1 ? STEP_DS : STEP_INCR), 1ull);
-  cudaGraphSetConditional(h, (unsigned)idx);
+  const int kind = refine_next_kind(*sc);
+  sc->kind = kind;
+  atomicAdd(dp->stages + kind, 1ull);
+  cudaGraphSetConditional(h, kind == STEP_FP32 ? 0u : kind == STEP_DS ? 1u : 2u);
 }
 
-// step_done() and step_converged() on the norms the step left
+// refine_step_done() and refine_converged() on the norms the step left
 __global__ void k_ref_decide(SweepCtl* sc, const double* hn, double tol, int maxit, cudaGraphConditionalHandle h,
                              const SweepDst* dp) {
   if (threadIdx.x) return;
   const SweepDst& d = *dp;
-  if (sc->kind != 2) sc->bnorm2 = hn[1];
-  if (sc->kind == 1) sc->ds_done = 1;
-  sc->res = sc->bnorm2 > 0 ? sqrt(hn[0] / sc->bnorm2) : 0.0;
-  sc->iters += 1;
+  refine_step_done(*sc, sc->kind, hn);
   const bool nan = !(hn[2] == hn[2]);
   if (nan) atomicOr(d.nan, 1);
-  const bool conv = sc->ds_done && sqrt(hn[2]) <= tol * sqrt(hn[3]);
+  const bool conv = refine_converged(*sc, hn, tol);
   d.iters[sc->w] = sc->iters;
   d.res[sc->w] = sc->res;
   cudaGraphSetConditional(h, (nan || conv || sc->iters >= maxit) ? 0u : 1u);
@@ -2025,9 +2030,8 @@ cudaError_t build_lane_branch(mnpbem_geom* G, Lane& L, const SolveCtx& c, const 
     if ((e = add_cond(&rl, body, &ni, 1, hr, cudaGraphCondTypeWhile, 1, &rbody)) != cudaSuccess) return e;
     cudaGraphConditionalHandle hs;
     if ((e = cudaGraphConditionalHandleCreate(&hs, rbody, 0, 0)) != cudaSuccess) return e;
-    double dsw = DS_SWITCH;
     cudaGraphNode_t pk, sw, dc;
-    void* a_pick[] = {&sc, &hs, &dsw, &d};
+    void* a_pick[] = {&sc, &hs, &d};
     if ((e = add_kernel(&pk, rbody, nullptr, 0, k_ref_pick, 1, 32, a_pick)) != cudaSuccess) return e;
     cudaGraph_t sb[3];
     if ((e = add_cond(&sw, rbody, &pk, 1, hs, cudaGraphCondTypeSwitch, 3, sb)) != cudaSuccess) return e;
