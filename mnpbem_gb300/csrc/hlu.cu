@@ -768,6 +768,25 @@ View mat_view(Ctx& c, const Sub& A, int i, int j) {
 View lhs_view(Ctx& c, const Sub& A, int i) { return rows_of(A.lhs, rel(c, i, A.row), T(c).size(i)); }
 View rhs_view(Ctx& c, const Sub& A, int j) { return rows_of(A.rhs, rel(c, j, A.col), T(c).size(j)); }
 
+// a sub-block as a matrix of its own: the matrix itself (shared: blocks are
+// never modified once built) when the sub-block is all of it, else a copy
+mnpbem_status take_block(Ctx& c, const DMat& a, int r0, int nr, int c0, int nc, DMat& out) {
+  if (r0 == 0 && c0 == 0 && nr == a.m && nc == a.n) {
+    out = a;
+    return MNPBEM_OK;
+  }
+  return copy_view(c, block_of(a, r0, nr, c0, nc), out);
+}
+mnpbem_status take_rows(Ctx& c, const DMat& a, int r0, int nr, DMat& out) {
+  return take_block(c, a, r0, nr, 0, a.n, out);
+}
+mnpbem_status lhs_take(Ctx& c, const Sub& A, int i, DMat& out) {
+  return take_rows(c, A.lhs, rel(c, i, A.row), T(c).size(i), out);
+}
+mnpbem_status rhs_take(Ctx& c, const Sub& A, int j, DMat& out) {
+  return take_rows(c, A.rhs, rel(c, j, A.col), T(c).size(j), out);
+}
+
 mnpbem_status truncate(Ctx& c, Sub& A) {
   if (A.flag != FLAG_RK) return MNPBEM_OK;
   DMat L, R;
@@ -796,12 +815,12 @@ mnpbem_status convert(Ctx& c, Sub& A, int flag) {
 mnpbem_status mask(Ctx& c, const Sub& A, int r, int col, Sub& out) {
   if (A.flag == FLAG_FULL) {
     DMat m;
-    MNP_TRY(copy_view(c, mat_view(c, A, r, col), m));
+    MNP_TRY(take_block(c, A.mat, rel(c, r, A.row), T(c).size(r), rel(c, col, A.col), T(c).size(col), m));
     out = make_full(r, col, std::move(m));
   } else {
     DMat l, rr;
-    MNP_TRY(copy_view(c, lhs_view(c, A, r), l));
-    MNP_TRY(copy_view(c, rhs_view(c, A, col), rr));
+    MNP_TRY(lhs_take(c, A, r, l));
+    MNP_TRY(rhs_take(c, A, col, rr));
     out = make_rk(r, col, std::move(l), std::move(rr));
   }
   return MNPBEM_OK;
@@ -857,11 +876,11 @@ mnpbem_status mul_sub(Ctx& c, const Sub& A, const Sub& B, int i, int j, int k, S
   } else if (A.flag == FLAG_FULL) {
     DMat l, r;
     MNP_TRY(mul(c, mat_view(c, A, i, k), 0, lhs_view(c, B, k), 0, l));
-    MNP_TRY(copy_view(c, rhs_view(c, B, j), r));
+    MNP_TRY(rhs_take(c, B, j, r));
     out = make_rk(i, j, std::move(l), std::move(r));
   } else if (B.flag == FLAG_FULL) {
     DMat l, r;
-    MNP_TRY(copy_view(c, lhs_view(c, A, i), l));
+    MNP_TRY(lhs_take(c, A, i, l));
     MNP_TRY(mul(c, mat_view(c, B, k, j), 1, rhs_view(c, A, k), 0, r));
     out = make_rk(i, j, std::move(l), std::move(r));
   } else {
@@ -870,9 +889,9 @@ mnpbem_status mul_sub(Ctx& c, const Sub& A, const Sub& B, int i, int j, int k, S
     DMat l, r;
     if (S.m > S.n) {
       MNP_TRY(mul(c, lhs_view(c, A, i), 0, whole(S), 0, l));
-      MNP_TRY(copy_view(c, rhs_view(c, B, j), r));
+      MNP_TRY(rhs_take(c, B, j, r));
     } else {
-      MNP_TRY(copy_view(c, lhs_view(c, A, i), l));
+      MNP_TRY(lhs_take(c, A, i, l));
       MNP_TRY(mul(c, rhs_view(c, B, j), 0, whole(S), 1, r));
     }
     out = make_rk(i, j, std::move(l), std::move(r));
@@ -1085,7 +1104,7 @@ mnpbem_status rsolve_ss(Ctx& c, const Sub& B, const Sub& A, int i, int j, char u
     out = make_full(i, j, std::move(m));
   } else {
     DMat l, r;
-    MNP_TRY(copy_view(c, lhs_view(c, B, i), l));
+    MNP_TRY(lhs_take(c, B, i, l));
     MNP_TRY(trsm(c, 'L', rhs_view(c, B, j), 'T', A, uplo, r));
     out = make_rk(i, j, std::move(l), std::move(r));
   }
@@ -1099,7 +1118,7 @@ mnpbem_status lsolve_ss(Ctx& c, const Sub& B, const Sub& A, int i, int j, char u
   } else {
     DMat l, r;
     MNP_TRY(trsm(c, 'L', lhs_view(c, B, i), 'N', A, uplo, l));
-    MNP_TRY(copy_view(c, rhs_view(c, B, j), r));
+    MNP_TRY(rhs_take(c, B, j, r));
     out = make_rk(i, j, std::move(l), std::move(r));
   }
   return MNPBEM_OK;
