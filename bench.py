@@ -13,7 +13,10 @@ target is stated on): a dimer of two d = 50 nm spheres with a 2 nm gap,
 12 000 flat faces each, Drude metal eps(w) = 10 - 9.065^2 / (w (w + 0.0708 i))
 (w in eV) in eps = 1.77, plane wave polarised along the dimer axis (x)
 travelling along +z, wavelengths on the 32-point grid 500..900 nm.  A step is
-one batch of ``--batch`` wavelengths per GPU; with N GPUs rank r takes its own
+one batch of ``--batch`` wavelengths per GPU, which the library runs as one
+CUDA graph (its lanes take the wavelengths from a device-side queue and decide
+the refinement steps on the device; ``MNPBEM_SWEEP_GRAPH=0`` selects the
+host-polled scheduler, same results); with N GPUs rank r takes its own
 wavelengths (weak scaling, no collective on the data path).  The line also
 carries the plain FP64 GPU path on one wavelength of the same workload, the
 CPU oracle on the same geometry at a smaller size (extrapolated), the GPU
