@@ -114,3 +114,21 @@ def test_lsolve_and_product_exact_at_tight_truncation(prob):
     X = h.lsolve_lu(H1, h.lu(G1))
     assert rel(G1c @ h.full(X), H1c) < 1e-11
     assert rel(h.full(h.mul(G1, H1)), G1c @ H1c) < 1e-11
+
+
+def test_oracle_iterative_solver_with_hmat_preconditioner(prob):
+    """bemretiter with precond='hmat' in the oracle: GMRES converges in a few
+    steps (the preconditioner approximates the inverse to ~1e-3) and the
+    charges approach the direct solve to the tolerances' order"""
+    cp = prob["cp"]
+    pw = R.PlaneWaveRet([[1, 0, 0]], [[0, 0, 1]], None)
+    exc = pw.potential(cp, 600.0)
+    it = HR.BemRetIter(cp, cleaf=16, precond="hmat", maxit=100)
+    sig = it.solve(exc)
+    assert it.flag == 0 and it.iter <= 10
+    direct = R.BemRet(cp).solve(exc)
+    for k in ("sig1", "sig2"):
+        assert rel(sig[k], direct[k]) < 1e-3, k
+    plain = HR.BemRetIter(cp, cleaf=16, precond=None, maxit=300)
+    plain.solve(exc)
+    assert plain.iter > it.iter
