@@ -132,3 +132,23 @@ def test_oracle_iterative_solver_with_hmat_preconditioner(prob):
     plain = HR.BemRetIter(cp, cleaf=16, precond=None, maxit=300)
     plain.solve(exc)
     assert plain.iter > it.iter
+
+
+@pytest.mark.parametrize("cleaf", [16, 32])
+def test_tree_views_agree(cleaf):
+    """the library's tree arrays (treearrays, handed to mnpbem_hm_create) and
+    the H-arithmetic oracle's Tree describe the same partition: the pair
+    iterator below the root visits every leaf block once"""
+    import mnpbem_gb300 as m
+    from mnpbem_gb300.hmatrix import treearrays
+    cp = m.comparticle([m.epsconst(1.77), m.epsconst(-8 + 1j)], [m.trisphere(256, 20.0)], [[2, 1]], 1)
+    hp = m.hpartition(cp, cleaf)
+    ta = treearrays.of(hp)
+    assert ta.n == cp.n and ta.c.nfull == hp.full.shape[0] and ta.c.nlow == hp.low.shape[0]
+    T = HL.Tree(ta.son, ta.cind, ta.full, ta.low)
+    pairs = T.pairs(0, 0)
+    blocks = {tuple(map(int, b)) for b in np.vstack([ta.full, ta.low])}
+    assert len(pairs) == len(blocks) and set(pairs) == blocks
+    assert sum(ta.rows(r) * ta.rows(c) for r, c in pairs) == cp.n ** 2
+    for r, c in ta.full:
+        assert T.leaf(int(r)) and T.leaf(int(c))
